@@ -1,0 +1,1237 @@
+// C ABI of libedgpu.so (declared in include/edgpu.h): handle management, argument validation with
+// the reference's error classes, precision staging, the product launcher, the batched launcher and the
+// Lanczos driver.  All arithmetic on vectors runs in the CUDA kernels of enumerate.cu, hx*.cu and
+// linalg.cu; there is no CPU fallback.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "edgpu_internal.h"
+
+using namespace edgpu;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define API_BEGIN try {
+#define API_END                                                        \
+    }                                                                  \
+    catch (const Error& e) { return fail(e.code, e.what()); }          \
+    catch (const std::bad_alloc&) { return fail(EDGPU_ERR_OOM, "host allocation failed"); } \
+    catch (const std::exception& e) { return fail(EDGPU_ERR_STATE, e.what()); }            \
+    return EDGPU_OK;
+
+void require(bool cond, int code, const std::string& msg) {
+    if (!cond) throw Error(code, msg);
+}
+
+std::mutex g_init_mu;
+cudaStream_t g_stream = nullptr;
+int g_sm_count = 0;
+
+void init_device() {
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    if (g_stream) return;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+        throw Error(EDGPU_ERR_CUDA, std::string("no CUDA device available: ") + cudaGetErrorString(e));
+    int dev = 0;
+    EDGPU_CUDA(cudaGetDevice(&dev));
+    EDGPU_CUDA(cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev));
+    EDGPU_CUDA(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+}
+
+cudaStream_t pick_stream(void* s) { return s ? (cudaStream_t)s : g_stream; }
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    void ensure(size_t count) {
+        if (count <= n && p) return;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        EDGPU_CUDA(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)));
+        n = count;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    ~DevBuf() { release(); }
+};
+
+int bitwidth_of(int dim) {
+    int w = 0;
+    while ((1LL << w) < dim) ++w;
+    return w;
+}
+
+unsigned long long binom_u64(int n, int k) {
+    if (k < 0 || k > n) return 0;
+    unsigned long long r = 1;
+    for (int i = 1; i <= k; ++i) r = r * (unsigned long long)(n - k + i) / (unsigned long long)i;
+    return r;
+}
+
+// ---- operator representation ------------------------------------------------------------------
+
+struct Blob {
+    bool ready = false;
+    void* d = nullptr;
+    HxParams tmpl{};
+    size_t smem = 0;
+    int max_blocks = 0;      // resident blocks for the whole GPU
+    int rows_per_tile = 32;
+    ~Blob() {
+        if (d) cudaFree(d);
+    }
+};
+
+}  // namespace
+
+struct edgpu_space_s : public Space {};
+
+struct edgpu_op_s {
+    edgpu_space_s* space = nullptr;
+    int T = 0;
+    std::vector<uint64_t> masks, rows, cols;
+    std::vector<double> unit;         // 2T: per-unit-coupling amplitudes (the amplitudes when uncoupled)
+    std::vector<int32_t> cid;         // T
+    int n_coupl = 1;
+    std::vector<double> coupl{1.0};
+    Blob blob[2][2][2];               // [precision][direction 0 = H, 1 = H^dagger][mode 0 = product, 1 = gradient]
+    int tuned_rows[2] = {0, 0};
+    DevBuf<double> x64, y64, z64;
+    DevBuf<float> x32, y32;
+    DevBuf<double> grad_partial, grad_dev;
+};
+
+struct edgpu_batch_s {
+    std::vector<edgpu_op_s*> ops;
+    std::map<std::vector<const void*>, cudaGraphExec_t> graphs[2];
+    ~edgpu_batch_s() {
+        for (auto& m : graphs)
+            for (auto& kv : m) cudaGraphExecDestroy(kv.second);
+    }
+};
+
+namespace edgpu {
+cudaStream_t lib_stream() { return g_stream; }
+int sm_count() { return g_sm_count; }
+int hx_max_blocks_per_sm(bool w32, int gk, int prec, int mode, size_t smem);
+}  // namespace edgpu
+
+namespace {
+
+size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+
+// Build the shared-memory image of the term, phase and group tables for one (precision, direction,
+// mode) and the kernel parameter template.
+void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
+    Blob& B = op->blob[prec][dir][mode];
+    if (B.ready) return;
+    const Space& s = *op->space;
+    const bool w32 = s.w32;
+    const size_t wsz = w32 ? 4 : 8;
+    const size_t vsz = prec == EDGPU_FP64 ? 16 : 8;
+    const size_t rsz = prec == EDGPU_FP64 ? 8 : 4;
+    const Group& g = s.group;
+
+    // term split (keeps the reference's term order inside each class)
+    std::vector<int> diag, offd;
+    for (int t = 0; t < op->T; ++t) {
+        const uint64_t r = dir ? op->cols[t] : op->rows[t];
+        const uint64_t c = dir ? op->rows[t] : op->cols[t];
+        (r == c ? diag : offd).push_back(t);
+    }
+    const int T_o = (int)offd.size(), T_d = (int)diag.size();
+    require(T_o < 65536, EDGPU_ERR_ARG, "too many off-diagonal terms (max 65535)");
+
+    // divisors of G for the orbit-normalisation table
+    std::vector<int> divs;
+    for (int d = 1; d <= g.G; ++d)
+        if (g.G % d == 0) divs.push_back(d);
+    const int nd = (int)divs.size();
+    std::vector<int32_t> divi(g.G + 1, 0);
+    for (int i = 0; i < nd; ++i) divi[divs[i]] = i;
+
+    int nchunks = 0;
+    std::vector<unsigned long long> keep, lut;
+    if (g.kind == GK_TORUS) keep = torus_keep_masks(g, s.lay.nbits);
+    if (g.kind == GK_GENERIC) lut = generic_luts(g, s.lay, &nchunks);
+
+    size_t off = 0;
+    auto alloc = [&](size_t bytes) {
+        const size_t o = off;
+        off = align16(off + bytes);
+        return (int)o;
+    };
+    HxParams p{};
+    p.o_om = alloc(T_o * wsz);
+    p.o_or = alloc(T_o * wsz);
+    p.o_of = alloc(T_o * wsz);
+    p.o_oa = alloc(T_o * vsz);
+    p.o_ou = alloc(T_o * vsz);
+    p.o_oc = alloc(T_o * 4);
+    p.o_dm = alloc(T_d * wsz);
+    p.o_dr = alloc(T_d * wsz);
+    p.o_da = alloc(T_d * 16);
+    p.o_du = alloc(T_d * 16);
+    p.o_dc = alloc(T_d * 4);
+    p.o_ph = alloc(g.den * vsz);
+    p.o_num = alloc(g.G * 4);
+    p.o_divi = alloc((g.G + 1) * 4);
+    p.o_ratio = alloc(nd * nd * rsz);
+    p.o_keep = alloc(keep.size() * wsz);
+    p.o_lut = alloc(lut.size() * wsz);
+    p.o_flip = alloc((g.kind == GK_GENERIC ? g.G : 0) * wsz);
+    const size_t blob_bytes = align16(off);
+    std::vector<unsigned char> h(blob_bytes, 0);
+    auto putw = [&](int o, size_t i, uint64_t v) {
+        if (w32) { uint32_t u = (uint32_t)v; memcpy(&h[o + i * 4], &u, 4); }
+        else memcpy(&h[o + i * 8], &v, 8);
+    };
+    auto putv = [&](int o, size_t i, double re, double im) {
+        if (prec == EDGPU_FP64) { double v[2] = {re, im}; memcpy(&h[o + i * 16], v, 16); }
+        else { float v[2] = {(float)re, (float)im}; memcpy(&h[o + i * 8], v, 8); }
+    };
+    auto amp_of = [&](int t, bool unit_only, double& re, double& im) {
+        double a = op->unit[2 * t], b = op->unit[2 * t + 1];
+        if (!unit_only) {
+            const double c = op->coupl[op->cid[t]];
+            a *= c;
+            b *= c;
+        }
+        re = a;
+        im = dir ? -b : b;   // adjoint: conj(amplitude) (pure_operator.jl adjoint)
+    };
+    for (int k = 0; k < T_o; ++k) {
+        const int t = offd[k];
+        const uint64_t r = dir ? op->cols[t] : op->rows[t];
+        const uint64_t c = dir ? op->rows[t] : op->cols[t];
+        putw(p.o_om, k, op->masks[t]);
+        putw(p.o_or, k, r);
+        putw(p.o_of, k, r ^ c);
+        double re, im;
+        amp_of(t, false, re, im);
+        putv(p.o_oa, k, re, im);
+        amp_of(t, true, re, im);
+        putv(p.o_ou, k, re, im);
+        memcpy(&h[p.o_oc + k * 4], &op->cid[t], 4);
+    }
+    for (int k = 0; k < T_d; ++k) {
+        const int t = diag[k];
+        const uint64_t r = dir ? op->cols[t] : op->rows[t];
+        putw(p.o_dm, k, op->masks[t]);
+        putw(p.o_dr, k, r);
+        double v[2];
+        amp_of(t, false, v[0], v[1]);
+        memcpy(&h[p.o_da + k * 16], v, 16);
+        amp_of(t, true, v[0], v[1]);
+        memcpy(&h[p.o_du + k * 16], v, 16);
+        memcpy(&h[p.o_dc + k * 4], &op->cid[t], 4);
+    }
+    for (int j = 0; j < g.den; ++j) {
+        const double ang = 2.0 * M_PI * (double)j / (double)g.den;
+        putv(p.o_ph, j, std::cos(ang), std::sin(ang));
+    }
+    memcpy(&h[p.o_num], g.num.data(), g.G * 4);
+    memcpy(&h[p.o_divi], divi.data(), (g.G + 1) * 4);
+    for (int i = 0; i < nd; ++i)
+        for (int j = 0; j < nd; ++j) {
+            const double f = std::sqrt((double)divs[j] / (double)divs[i]);   // sqrt(|O_r| / |O_c|)
+            if (prec == EDGPU_FP64) memcpy(&h[p.o_ratio + (i * nd + j) * 8], &f, 8);
+            else { float ff = (float)f; memcpy(&h[p.o_ratio + (i * nd + j) * 4], &ff, 4); }
+        }
+    for (size_t i = 0; i < keep.size(); ++i) putw(p.o_keep, i, keep[i]);
+    for (size_t i = 0; i < lut.size(); ++i) putw(p.o_lut, i, lut[i]);
+    if (g.kind == GK_GENERIC)
+        for (int e = 0; e < g.G; ++e) putw(p.o_flip, e, e < (int)g.flips.size() ? g.flips[e] : 0ull);
+
+    size_t tot = blob_bytes;
+    p.o_grad = (int)tot;
+    tot = align16(tot + (mode ? op->n_coupl * 8 : 0));
+    p.warp_base = (int)tot;
+    tot += (size_t)(HX_THREADS / 32) * hx_warp_bytes(w32);
+    require(tot <= 227 * 1024, EDGPU_ERR_ARG,
+            "operator tables do not fit in shared memory (" + std::to_string(tot) + " bytes)");
+
+    if (B.d) cudaFree(B.d);
+    B.d = nullptr;
+    EDGPU_CUDA(cudaMalloc(&B.d, std::max<size_t>(blob_bytes, 16)));
+    EDGPU_CUDA(cudaMemcpy(B.d, h.data(), blob_bytes, cudaMemcpyHostToDevice));
+    p.blob = B.d;
+    p.blob_words16 = (int)(blob_bytes / 16);
+    p.T_o = T_o;
+    p.T_d = T_d;
+    p.G = g.G;
+    p.den = g.den;
+    p.nd = nd;
+    p.L1 = g.L1;
+    p.L2 = g.L2;
+    p.w = g.w;
+    p.rowbits = g.L1 * g.w;
+    p.nbits = s.lay.nbits;
+    p.nchunks = nchunks;
+    p.full = (s.lay.nbits >= 64) ? ~0ull : ((1ull << s.lay.nbits) - 1ull);
+    p.keys = s.d_keys;
+    p.n_rows = s.dim;
+    p.n_coupl = op->n_coupl;
+    B.tmpl = p;
+    B.smem = tot;
+    const int per_sm = std::max(1, hx_max_blocks_per_sm(w32, g.kind, prec, mode, tot));
+    B.max_blocks = per_sm * std::max(1, g_sm_count);
+    B.ready = true;
+}
+
+void invalidate_blobs(edgpu_op_s* op) {
+    for (auto& a : op->blob)
+        for (auto& b : a)
+            for (auto& c : b) {
+                if (c.d) cudaFree(c.d);
+                c.d = nullptr;
+                c.ready = false;
+            }
+}
+
+int blocks_for(const Blob& B, long long n_rows, int rows_per_tile) {
+    const long long tiles = (n_rows + rows_per_tile - 1) / rows_per_tile;
+    const long long need = (tiles + HX_THREADS / 32 - 1) / (HX_THREADS / 32);
+    return (int)std::max<long long>(1, std::min<long long>(need, B.max_blocks));
+}
+
+void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, void* y, int accumulate,
+                    const void* gy, double* grad_partial, cudaStream_t st, int* blocks_used = nullptr,
+                    int rows_override = 0) {
+    build_blob(op, prec, dir, mode);
+    Blob& B = op->blob[prec][dir][mode];
+    HxParams p = B.tmpl;
+    if (p.n_rows == 0) {
+        if (blocks_used) *blocks_used = 0;
+        return;
+    }
+    int rows = rows_override ? rows_override : (op->tuned_rows[prec] ? op->tuned_rows[prec] : B.rows_per_tile);
+    p.rows_per_tile = rows;
+    p.x = x;
+    p.y = y;
+    p.gy = gy;
+    p.grad_partial = grad_partial;
+    p.accumulate = accumulate;
+    const int blocks = blocks_for(B, p.n_rows, rows);
+    if (blocks_used) *blocks_used = blocks;
+    if (op->space->w32) hx_launch_w32(op->space->group.kind, prec, mode, p, blocks, B.smem, st);
+    else hx_launch_w64(op->space->group.kind, prec, mode, p, blocks, B.smem, st);
+}
+
+edgpu_space_s* as_space(edgpu_space s) {
+    require(s != nullptr, EDGPU_ERR_ARG, "null space handle");
+    return static_cast<edgpu_space_s*>(s);
+}
+
+edgpu_op_s* as_op(edgpu_op o) {
+    require(o != nullptr, EDGPU_ERR_ARG, "null operator handle");
+    return static_cast<edgpu_op_s*>(o);
+}
+
+void check_prec(int prec) { require(prec == EDGPU_FP64 || prec == EDGPU_MIXED, EDGPU_ERR_ARG, "bad precision"); }
+
+void check_dim(const edgpu_op_s* op, int64_t n, const char* what) {
+    if (n != op->space->dim)
+        throw Error(EDGPU_ERR_DIM, std::string(what) + " has length " + std::to_string(n) + " != dimension " +
+                                       std::to_string(op->space->dim));
+}
+
+// ---- symmetric tridiagonal helpers (Lanczos) ----------------------------------------------------
+
+// Number of eigenvalues of tridiag(a, b) below x (Sturm sequence / LDL^T pivot signs).
+int sturm_count(const std::vector<double>& a, const std::vector<double>& b, double x) {
+    int cnt = 0;
+    double d = 1.0;
+    for (size_t i = 0; i < a.size(); ++i) {
+        const double bb = i ? b[i - 1] * b[i - 1] : 0.0;
+        d = (a[i] - x) - (i ? bb / d : 0.0);
+        if (d == 0.0) d = -1e-300;
+        if (d < 0) ++cnt;
+    }
+    return cnt;
+}
+
+double lowest_eigenvalue(const std::vector<double>& a, const std::vector<double>& b) {
+    double lo = a[0], hi = a[0];
+    for (size_t i = 0; i < a.size(); ++i) {
+        const double r = (i ? std::fabs(b[i - 1]) : 0.0) + (i + 1 < a.size() ? std::fabs(b[i]) : 0.0);
+        lo = std::min(lo, a[i] - r);
+        hi = std::max(hi, a[i] + r);
+    }
+    for (int it = 0; it < 200; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
+        if (sturm_count(a, b, mid) >= 1) hi = mid;
+        else lo = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+
+// Eigenvector of tridiag(a, b) for eigenvalue lam by inverse iteration (LU with partial pivoting).
+std::vector<double> tridiag_eigvec(const std::vector<double>& a, const std::vector<double>& b, double lam) {
+    const int n = (int)a.size();
+    std::vector<double> z(n, 1.0 / std::sqrt((double)n));
+    if (n == 1) return {1.0};
+    double scale = 0.0;
+    for (int i = 0; i < n; ++i) scale = std::max(scale, std::fabs(a[i]) + (i < n - 1 ? std::fabs(b[i]) : 0.0));
+    const double shift = lam - 1e-13 * std::max(1.0, scale);
+    for (int iter = 0; iter < 4; ++iter) {
+        // factor T - shift I = L U with row interchanges (U has 3 diagonals)
+        std::vector<double> d(n), du(n, 0.0), du2(n, 0.0), dl(n, 0.0), rhs = z;
+        std::vector<int> piv(n, 0);
+        for (int i = 0; i < n; ++i) d[i] = a[i] - shift;
+        std::vector<double> sub(n, 0.0), sup(n, 0.0);
+        for (int i = 0; i < n - 1; ++i) { sub[i] = b[i]; sup[i] = b[i]; }
+        for (int i = 0; i < n; ++i) du[i] = sup[i];
+        for (int i = 0; i < n - 1; ++i) {
+            if (std::fabs(d[i]) >= std::fabs(sub[i])) {
+                const double f = (d[i] != 0.0) ? sub[i] / d[i] : 0.0;
+                dl[i] = f;
+                d[i + 1] -= f * du[i];
+                piv[i] = 0;
+            } else {
+                const double f = d[i] / sub[i];
+                d[i] = sub[i];
+                dl[i] = f;
+                const double tmp = du[i];
+                du[i] = d[i + 1];
+                d[i + 1] = tmp - f * d[i + 1];
+                if (i < n - 2) {
+                    du2[i] = du[i + 1];
+                    du[i + 1] = -f * du[i + 1];
+                }
+                piv[i] = 1;
+            }
+        }
+        for (int i = 0; i < n; ++i)
+            if (d[i] == 0.0) d[i] = 1e-300;
+        for (int i = 0; i < n - 1; ++i) {   // forward: apply L^-1 with interchanges
+            if (piv[i]) std::swap(rhs[i], rhs[i + 1]);
+            rhs[i + 1] -= dl[i] * rhs[i];
+        }
+        for (int i = n - 1; i >= 0; --i) {   // back substitution with U
+            double v = rhs[i];
+            if (i + 1 < n) v -= du[i] * rhs[i + 1];
+            if (i + 2 < n) v -= du2[i] * rhs[i + 2];
+            rhs[i] = v / d[i];
+        }
+        double nrm = 0.0;
+        for (double v : rhs) nrm += v * v;
+        nrm = std::sqrt(nrm);
+        for (int i = 0; i < n; ++i) z[i] = rhs[i] / nrm;
+    }
+    return z;
+}
+
+}  // namespace
+
+// =================================================================================================
+extern "C" {
+
+const char* edgpu_last_error(void) { return g_last_error.c_str(); }
+
+const char* edgpu_version(void) { return "edgpu 0.1.0 (sm_103a)"; }
+
+int edgpu_device_count(int32_t* out) {
+    API_BEGIN
+    require(out, EDGPU_ERR_ARG, "null output");
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) n = 0;
+    cudaGetLastError();
+    *out = n;
+    API_END
+}
+
+int edgpu_space_create(int32_t n_sites, const int32_t* site_dims, int32_t qn_len, const int64_t* state_qn,
+                       int32_t n_allowed, const int64_t* allowed_qn, int32_t flags, edgpu_space* out) {
+    API_BEGIN
+    require(out != nullptr, EDGPU_ERR_ARG, "null output handle");
+    *out = nullptr;
+    require(n_sites >= 1 && n_sites <= 64, EDGPU_ERR_ARG, "n_sites must be in [1, 64]");
+    require(site_dims != nullptr, EDGPU_ERR_ARG, "null site_dims");
+    require(qn_len >= 0 && qn_len <= 4, EDGPU_ERR_ARG, "quantum-number tuples of length 0..4 are supported");
+    std::unique_ptr<edgpu_space_s> s(new edgpu_space_s());
+    Layout& L = s->lay;
+    L.n_sites = n_sites;
+    L.qlen = qn_len;
+    L.off.push_back(0);
+    int total_states = 0;
+    for (int i = 0; i < n_sites; ++i) {
+        require(site_dims[i] >= 1 && site_dims[i] <= 65536, EDGPU_ERR_ARG, "site dimension out of range");
+        L.dims.push_back(site_dims[i]);
+        L.bw.push_back(bitwidth_of(site_dims[i]));
+        L.off.push_back(L.off.back() + L.bw.back());
+        total_states += site_dims[i];
+    }
+    L.nbits = L.off.back();
+    if (L.nbits >= 64)
+        throw Error(EDGPU_ERR_ARG, "type UInt64 not enough to represent the hilbert space (need " +
+                                       std::to_string(L.nbits) + " bits)");
+    if (qn_len > 0) {
+        require(state_qn != nullptr, EDGPU_ERR_ARG, "null state_qn");
+        L.state_qn.assign(state_qn, state_qn + (size_t)total_states * qn_len);
+    }
+    if (n_allowed < 0) {
+        L.all_sectors = true;
+    } else if (n_allowed > 0) {
+        require(qn_len > 0, EDGPU_ERR_ARG, "allowed quantum numbers given for a space without quantum numbers");
+        require(allowed_qn != nullptr, EDGPU_ERR_ARG, "null allowed_qn");
+        L.allowed.assign(allowed_qn, allowed_qn + (size_t)n_allowed * qn_len);
+    }
+    if (qn_len == 0) L.all_sectors = true;
+    // spin-1/2-like single sector: every word of nbits with a fixed popcount
+    if (!L.all_sectors && n_allowed == 1 && qn_len == 1) {
+        bool ok = true;
+        for (int i = 0; i < n_sites && ok; ++i) ok = (L.dims[i] == 2);
+        if (ok) {
+            const int64_t q0 = L.state_qn[0], q1 = L.state_qn[1];
+            for (int i = 0; i < n_sites && ok; ++i) ok = (L.state_qn[2 * i] == q0 && L.state_qn[2 * i + 1] == q1);
+            ok = ok && (q0 != q1);
+            if (ok) {
+                const int64_t v = L.allowed[0] - (int64_t)n_sites * q0, d = q1 - q0;
+                if (v % d == 0 && v / d >= 0 && v / d <= n_sites) L.popcount = (int)(v / d);
+                else L.popcount = -2;   // unreachable sector: empty basis
+            }
+        }
+    }
+    s->lazy = (flags & EDGPU_SPACE_LAZY) != 0;
+    s->w32 = L.nbits <= 31;
+    if (L.popcount == -2 || (!L.all_sectors && n_allowed == 0)) {
+        s->dim = 0;
+        L.popcount = -1;
+        if (!s->lazy) EDGPU_CUDA(cudaMalloc(&s->d_keys, 16));
+        *out = s.release();
+        return EDGPU_OK;
+    }
+    init_device();
+    enumerate_parent(*s, g_stream);
+    *out = s.release();
+    API_END
+}
+
+int edgpu_space_from_basis(int32_t n_sites, const int32_t* site_dims, const uint64_t* basis, int64_t n,
+                           edgpu_space* out) {
+    API_BEGIN
+    require(out != nullptr, EDGPU_ERR_ARG, "null output handle");
+    *out = nullptr;
+    require(n_sites >= 1 && n_sites <= 64 && site_dims, EDGPU_ERR_ARG, "bad site layout");
+    require(n >= 0 && (n == 0 || basis), EDGPU_ERR_ARG, "bad basis");
+    std::unique_ptr<edgpu_space_s> s(new edgpu_space_s());
+    Layout& L = s->lay;
+    L.n_sites = n_sites;
+    L.off.push_back(0);
+    for (int i = 0; i < n_sites; ++i) {
+        require(site_dims[i] >= 1, EDGPU_ERR_ARG, "site dimension out of range");
+        L.dims.push_back(site_dims[i]);
+        L.bw.push_back(bitwidth_of(site_dims[i]));
+        L.off.push_back(L.off.back() + L.bw.back());
+    }
+    L.nbits = L.off.back();
+    if (L.nbits >= 64)
+        throw Error(EDGPU_ERR_ARG, "type UInt64 not enough to represent the hilbert space (need " +
+                                       std::to_string(L.nbits) + " bits)");
+    L.all_sectors = true;
+    std::vector<uint64_t> b(basis, basis + n);
+    if (!std::is_sorted(b.begin(), b.end())) std::sort(b.begin(), b.end());
+    for (int64_t i = 1; i < n; ++i)
+        if (b[i] == b[i - 1]) throw Error(EDGPU_ERR_ARG, "vals contains duplicates " + std::to_string(b[i]));
+    const uint64_t full = (1ull << L.nbits) - 1ull;
+    for (int64_t i = 0; i < n; ++i)
+        require((b[i] & ~full) == 0, EDGPU_ERR_ARG, "basis state has bits beyond the site layout");
+    s->w32 = L.nbits <= 31;
+    s->dim = n;
+    init_device();
+    if (s->w32) {
+        std::vector<uint32_t> b32(b.begin(), b.end());
+        EDGPU_CUDA(cudaMalloc(&s->d_keys, std::max<int64_t>(n, 1) * 4));
+        EDGPU_CUDA(cudaMemcpy(s->d_keys, b32.data(), n * 4, cudaMemcpyHostToDevice));
+    } else {
+        EDGPU_CUDA(cudaMalloc(&s->d_keys, std::max<int64_t>(n, 1) * 8));
+        EDGPU_CUDA(cudaMemcpy(s->d_keys, b.data(), n * 8, cudaMemcpyHostToDevice));
+    }
+    *out = s.release();
+    API_END
+}
+
+int edgpu_space_dim(edgpu_space s, int64_t* out) {
+    API_BEGIN
+    require(out, EDGPU_ERR_ARG, "null output");
+    *out = as_space(s)->dim;
+    API_END
+}
+
+int edgpu_space_nbits(edgpu_space s, int32_t* out) {
+    API_BEGIN
+    require(out, EDGPU_ERR_ARG, "null output");
+    *out = as_space(s)->lay.nbits;
+    API_END
+}
+
+int edgpu_space_get_basis(edgpu_space sh, uint64_t* out, int64_t n) {
+    API_BEGIN
+    edgpu_space_s* s = as_space(sh);
+    require(s->d_keys != nullptr || s->dim == 0, EDGPU_ERR_STATE, "basis of a lazy space is not materialised");
+    if (n != s->dim) throw Error(EDGPU_ERR_DIM, "output has length " + std::to_string(n) + " != dimension " +
+                                                     std::to_string(s->dim));
+    if (n == 0) return EDGPU_OK;
+    require(out, EDGPU_ERR_ARG, "null output");
+    if (s->w32) {
+        std::vector<uint32_t> tmp(n);
+        EDGPU_CUDA(cudaMemcpy(tmp.data(), s->d_keys, n * 4, cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < n; ++i) out[i] = tmp[i];
+    } else {
+        EDGPU_CUDA(cudaMemcpy(out, s->d_keys, n * 8, cudaMemcpyDeviceToHost));
+    }
+    API_END
+}
+
+int edgpu_space_lookup(edgpu_space sh, const uint64_t* keys, int64_t n, int64_t* idx_out) {
+    API_BEGIN
+    edgpu_space_s* s = as_space(sh);
+    require(s->d_keys != nullptr, EDGPU_ERR_STATE, "basis of a lazy space is not materialised");
+    require(n >= 0 && (n == 0 || (keys && idx_out)), EDGPU_ERR_ARG, "bad arguments");
+    if (s->dim == 0) {
+        for (int64_t i = 0; i < n; ++i) idx_out[i] = -1;
+        return EDGPU_OK;
+    }
+    lookup_keys(*s, keys, n, idx_out, g_stream);
+    API_END
+}
+
+void edgpu_space_destroy(edgpu_space s) { delete static_cast<edgpu_space_s*>(s); }
+
+int edgpu_reduce(edgpu_space parent_h, int32_t n_elems, const int32_t* site_maps, const uint64_t* flip_masks,
+                 const int32_t* char_num, int32_t char_den, edgpu_space* out) {
+    API_BEGIN
+    require(out != nullptr, EDGPU_ERR_ARG, "null output handle");
+    *out = nullptr;
+    edgpu_space_s* parent = as_space(parent_h);
+    require(!parent->reduced, EDGPU_ERR_ARG, "the parent must be an unreduced representation");
+    const Layout& L = parent->lay;
+    const int n = L.n_sites;
+    require(n_elems >= 1 && n_elems <= 4096, EDGPU_ERR_ARG, "group order must be in [1, 4096]");
+    require(site_maps && char_num, EDGPU_ERR_ARG, "null group data");
+    require(char_den >= 1 && char_den <= 4096, EDGPU_ERR_ARG, "character denominator must be in [1, 4096]");
+    const uint64_t full = (1ull << L.nbits) - 1ull;
+    Group g;
+    g.G = n_elems;
+    g.den = char_den;
+    g.maps.assign(site_maps, site_maps + (size_t)n_elems * n);
+    g.flips.assign(n_elems, 0ull);
+    if (flip_masks) g.flips.assign(flip_masks, flip_masks + n_elems);
+    g.num.resize(n_elems);
+    for (int e = 0; e < n_elems; ++e) g.num[e] = ((char_num[e] % char_den) + char_den) % char_den;
+    // each element: a site permutation between sites of equal bit width; flips inside the word
+    for (int e = 0; e < n_elems; ++e) {
+        std::vector<char> seen(n, 0);
+        for (int i = 0; i < n; ++i) {
+            const int j = g.maps[(size_t)e * n + i];
+            require(j >= 0 && j < n && !seen[j], EDGPU_ERR_ARG, "site map of element " + std::to_string(e) +
+                                                                   " is not a permutation");
+            seen[j] = 1;
+            require(L.bw[i] == L.bw[j], EDGPU_ERR_ARG, "a permutation maps sites of different bit widths");
+        }
+        require((g.flips[e] & ~full) == 0, EDGPU_ERR_ARG, "flip mask has bits beyond the site layout");
+    }
+    for (int i = 0; i < n; ++i)
+        require(g.maps[i] == i, EDGPU_ERR_ARG, "element 0 must be the identity");
+    require(g.flips[0] == 0 && g.num[0] == 0, EDGPU_ERR_ARG, "element 0 must be the identity with amplitude 1");
+    // closure and the 1-D representation property: chi(g h) = chi(g) chi(h)
+    {
+        std::map<std::pair<std::vector<int32_t>, uint64_t>, int> index;
+        for (int e = 0; e < n_elems; ++e) {
+            std::vector<int32_t> m(g.maps.begin() + (size_t)e * n, g.maps.begin() + (size_t)(e + 1) * n);
+            auto key = std::make_pair(m, g.flips[e]);
+            require(index.find(key) == index.end(), EDGPU_ERR_ARG, "repeated group element");
+            index[key] = e;
+        }
+        auto apply_bits = [&](int e, uint64_t b) {
+            uint64_t o = 0;
+            for (int i = 0; i < n; ++i) {
+                const uint64_t m = (1ull << L.bw[i]) - 1ull;
+                o |= ((b >> L.off[i]) & m) << L.off[g.maps[(size_t)e * n + i]];
+            }
+            return o;
+        };
+        for (int a = 0; a < n_elems; ++a)
+            for (int b = 0; b < n_elems; ++b) {
+                std::vector<int32_t> m(n);
+                for (int i = 0; i < n; ++i) m[i] = g.maps[(size_t)a * n + g.maps[(size_t)b * n + i]];
+                const uint64_t f = apply_bits(a, g.flips[b]) ^ g.flips[a];
+                auto it = index.find(std::make_pair(m, f));
+                require(it != index.end(), EDGPU_ERR_ARG, "the symmetry operations do not form a group");
+                require((g.num[a] + g.num[b]) % char_den == g.num[it->second], EDGPU_ERR_ARG,
+                        "the amplitudes are not a one-dimensional representation of the group");
+            }
+    }
+    // torus translation structure (fast path): uniform bit width, no flips, G == n_sites
+    bool uniform = true;
+    for (int i = 0; i < n; ++i) uniform = uniform && (L.bw[i] == L.bw[0]);
+    bool noflip = true;
+    for (int e = 0; e < n_elems; ++e) noflip = noflip && g.flips[e] == 0;
+    g.kind = GK_GENERIC;
+    if (n_elems == 1) {
+        g.kind = GK_TRIVIAL;
+        g.num = {0};
+        g.den = 1;
+    } else if (uniform && noflip && n_elems == n && L.bw[0] >= 1) {
+        for (int L1 = n; L1 >= 1 && g.kind == GK_GENERIC; --L1) {
+            if (n % L1 != 0 || L1 > 64) continue;
+            const int L2 = n / L1;
+            std::vector<int> slot(n_elems, -1);
+            bool ok = true;
+            for (int e = 0; e < n_elems && ok; ++e) {
+                const int32_t* m = &g.maps[(size_t)e * n];
+                const int a = m[0] % L1, b = m[0] / L1;
+                for (int y = 0; y < L2 && ok; ++y)
+                    for (int x = 0; x < L1 && ok; ++x)
+                        ok = (m[x + L1 * y] == (x + a) % L1 + L1 * ((y + b) % L2));
+                if (ok) {
+                    const int t = a + L1 * b;
+                    ok = slot[t] < 0;
+                    slot[t] = e;
+                }
+            }
+            if (ok) {
+                std::vector<int32_t> num(n_elems);
+                for (int t = 0; t < n_elems; ++t) num[t] = g.num[slot[t]];
+                g.kind = GK_TORUS;
+                g.L1 = L1;
+                g.L2 = L2;
+                g.w = L.bw[0];
+                g.num = num;
+            }
+        }
+    }
+    std::unique_ptr<edgpu_space_s> s(new edgpu_space_s());
+    s->lay = L;
+    s->reduced = true;
+    s->parent = parent;
+    s->group = g;
+    s->w32 = parent->w32;
+    init_device();
+    if (parent->dim == 0) {
+        s->dim = 0;
+        EDGPU_CUDA(cudaMalloc(&s->d_keys, 16));
+    } else {
+        enumerate_reps(*s, *parent, g_stream);
+    }
+    *out = s.release();
+    API_END
+}
+
+int edgpu_reduce_mapping(edgpu_space reduced, int64_t* index_out, double* ampl_out, int64_t n_parent) {
+    API_BEGIN
+    edgpu_space_s* s = as_space(reduced);
+    require(s->reduced && s->parent, EDGPU_ERR_ARG, "not a reduced representation");
+    require(s->parent->d_keys != nullptr || s->parent->dim == 0, EDGPU_ERR_STATE, "the parent basis is not materialised");
+    if (n_parent != s->parent->dim) throw Error(EDGPU_ERR_DIM, "output length != parent dimension");
+    if (n_parent == 0) return EDGPU_OK;
+    require(index_out && ampl_out, EDGPU_ERR_ARG, "null output");
+    build_mapping(*s, *s->parent, index_out, ampl_out, g_stream);
+    API_END
+}
+
+int edgpu_space_orbit_sizes(edgpu_space reduced, int32_t* out, int64_t n) {
+    API_BEGIN
+    edgpu_space_s* s = as_space(reduced);
+    if (n != s->dim) throw Error(EDGPU_ERR_DIM, "output length != dimension");
+    if (n == 0) return EDGPU_OK;
+    require(out, EDGPU_ERR_ARG, "null output");
+    orbit_sizes(*s, out, g_stream);
+    API_END
+}
+
+int edgpu_op_create(edgpu_space sh, int32_t n_terms, const uint64_t* masks, const uint64_t* rows, const uint64_t* cols,
+                    const double* amps, const int32_t* coupling_ids, int32_t n_couplings, const double* couplings,
+                    edgpu_op* out) {
+    API_BEGIN
+    require(out != nullptr, EDGPU_ERR_ARG, "null output handle");
+    *out = nullptr;
+    edgpu_space_s* s = as_space(sh);
+    require(s->d_keys != nullptr, EDGPU_ERR_STATE, "the representation's basis is not materialised");
+    require(n_terms >= 0, EDGPU_ERR_ARG, "negative term count");
+    require(n_terms == 0 || (masks && rows && cols && amps), EDGPU_ERR_ARG, "null term arrays");
+    const uint64_t full = (s->lay.nbits >= 64) ? ~0ull : ((1ull << s->lay.nbits) - 1ull);
+    std::unique_ptr<edgpu_op_s> op(new edgpu_op_s());
+    op->space = s;
+    op->T = n_terms;
+    for (int t = 0; t < n_terms; ++t) {
+        if ((~masks[t]) & rows[t]) throw Error(EDGPU_ERR_ARG, "every bit of bitrow not in bitmask should be set to zero");
+        if ((~masks[t]) & cols[t]) throw Error(EDGPU_ERR_ARG, "every bit of bitcol not in bitmask should be set to zero");
+        require((masks[t] & ~full) == 0, EDGPU_ERR_ARG, "term mask has bits beyond the site layout");
+    }
+    op->masks.assign(masks, masks + n_terms);
+    op->rows.assign(rows, rows + n_terms);
+    op->cols.assign(cols, cols + n_terms);
+    op->unit.assign(amps, amps + 2 * (size_t)n_terms);
+    if (coupling_ids) {
+        require(n_couplings >= 1 && n_couplings <= 8192, EDGPU_ERR_ARG, "n_couplings must be in [1, 8192]");
+        require(couplings != nullptr, EDGPU_ERR_ARG, "null couplings");
+        op->cid.assign(coupling_ids, coupling_ids + n_terms);
+        for (int t = 0; t < n_terms; ++t)
+            require(op->cid[t] >= 0 && op->cid[t] < n_couplings, EDGPU_ERR_ARG, "coupling id out of range");
+        op->n_coupl = n_couplings;
+        op->coupl.assign(couplings, couplings + n_couplings);
+    } else {
+        op->cid.assign(n_terms, 0);
+        op->n_coupl = 1;
+        op->coupl = {1.0};
+    }
+    init_device();
+    *out = op.release();
+    API_END
+}
+
+int edgpu_op_set_couplings(edgpu_op oh, const double* couplings, int32_t n_couplings) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    require(n_couplings == op->n_coupl && couplings, EDGPU_ERR_DIM, "coupling count mismatch");
+    op->coupl.assign(couplings, couplings + n_couplings);
+    invalidate_blobs(op);
+    API_END
+}
+
+int edgpu_op_dim(edgpu_op oh, int64_t* out) {
+    API_BEGIN
+    require(out, EDGPU_ERR_ARG, "null output");
+    *out = as_op(oh)->space->dim;
+    API_END
+}
+
+void edgpu_op_destroy(edgpu_op o) {
+    edgpu_op_s* op = static_cast<edgpu_op_s*>(o);
+    if (!op) return;
+    invalidate_blobs(op);
+    delete op;
+}
+
+int edgpu_op_set_tiling(edgpu_op oh, int32_t precision, int32_t rows_per_tile) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    check_prec(precision);
+    require(rows_per_tile == 0 || (rows_per_tile >= 1 && rows_per_tile <= 32 && (32 % rows_per_tile) == 0),
+            EDGPU_ERR_ARG, "rows_per_tile must be 0 (default) or a divisor of 32");
+    op->tuned_rows[precision] = rows_per_tile;
+    API_END
+}
+
+int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out, double* best_ms_out) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    check_prec(precision);
+    const int64_t n = op->space->dim;
+    const int cands[] = {32, 16, 8};
+    int best = 32;
+    double best_ms = 1e30;
+    if (n > 0) {
+        const size_t vs = precision == EDGPU_FP64 ? 16 : 8;
+        void *x = nullptr, *y = nullptr;
+        EDGPU_CUDA(cudaMalloc(&x, n * vs));
+        EDGPU_CUDA(cudaMalloc(&y, n * vs));
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        try {
+            EDGPU_CUDA(cudaMemsetAsync(x, 0, n * vs, g_stream));
+            for (int r : cands) {
+                launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, g_stream, nullptr, r);
+                float tot = 0.f;
+                const int reps = 3;
+                for (int k = 0; k < reps; ++k) {
+                    EDGPU_CUDA(cudaEventRecord(e0, g_stream));
+                    launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, g_stream, nullptr, r);
+                    EDGPU_CUDA(cudaEventRecord(e1, g_stream));
+                    EDGPU_CUDA(cudaEventSynchronize(e1));
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    tot += ms;
+                }
+                if (tot / reps < best_ms) {
+                    best_ms = tot / reps;
+                    best = r;
+                }
+            }
+        } catch (...) {
+            cudaFree(x);
+            cudaFree(y);
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            throw;
+        }
+        cudaFree(x);
+        cudaFree(y);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    op->tuned_rows[precision] = best;
+    if (rows_per_tile_out) *rows_per_tile_out = best;
+    if (best_ms_out) *best_ms_out = best_ms;
+    API_END
+}
+
+// ---- products ----------------------------------------------------------------------------------
+
+static void host_product(edgpu_op_s* op, int prec, int dir, const double* x, double* y, int64_t n, int accumulate,
+                         bool conj_io) {
+    cudaStream_t st = g_stream;
+    op->x64.ensure(2 * n);
+    op->y64.ensure(2 * n);
+    EDGPU_CUDA(cudaMemcpyAsync(op->x64.p, x, n * 16, cudaMemcpyHostToDevice, st));
+    if (conj_io) launch_conj_c128(n, op->x64.p, st);
+    if (accumulate) {
+        EDGPU_CUDA(cudaMemcpyAsync(op->y64.p, y, n * 16, cudaMemcpyHostToDevice, st));
+        if (conj_io) launch_conj_c128(n, op->y64.p, st);
+    }
+    if (prec == EDGPU_FP64) {
+        launch_product(op, prec, dir, 0, op->x64.p, op->y64.p, accumulate, nullptr, nullptr, st);
+    } else {
+        op->x32.ensure(2 * n);
+        op->y32.ensure(2 * n);
+        launch_c128_to_c64(n, op->x64.p, op->x32.p, st);
+        launch_product(op, prec, dir, 0, op->x32.p, op->y32.p, 0, nullptr, nullptr, st);
+        launch_c64_to_c128(n, op->y32.p, op->y64.p, accumulate, st);
+    }
+    if (conj_io) launch_conj_c128(n, op->y64.p, st);
+    EDGPU_CUDA(cudaMemcpyAsync(y, op->y64.p, n * 16, cudaMemcpyDeviceToHost, st));
+    EDGPU_CUDA(cudaStreamSynchronize(st));
+}
+
+int edgpu_mul(edgpu_op oh, int32_t precision, const double* x, double* y, int64_t n, int32_t accumulate) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    check_prec(precision);
+    check_dim(op, n, "state");
+    if (n == 0) return EDGPU_OK;
+    require(x && y, EDGPU_ERR_ARG, "null vector");
+    host_product(op, precision, 0, x, y, n, accumulate ? 1 : 0, false);
+    API_END
+}
+
+int edgpu_mul_device(edgpu_op oh, int32_t precision, const void* x, void* y, int64_t n, int32_t accumulate,
+                     void* stream) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    check_prec(precision);
+    check_dim(op, n, "state");
+    if (n == 0) return EDGPU_OK;
+    require(x && y, EDGPU_ERR_ARG, "null vector");
+    require(x != y, EDGPU_ERR_ARG, "out and state must be distinct buffers");
+    launch_product(op, precision, 0, 0, x, y, accumulate ? 1 : 0, nullptr, nullptr, pick_stream(stream));
+    API_END
+}
+
+int edgpu_mul_transpose(edgpu_op oh, int32_t precision, const double* x, double* y, int64_t n, int32_t accumulate) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    check_prec(precision);
+    check_dim(op, n, "state");
+    if (n == 0) return EDGPU_OK;
+    require(x && y, EDGPU_ERR_ARG, "null vector");
+    // transpose(A) x = conj(A^dagger conj(x))
+    host_product(op, precision, 1, x, y, n, accumulate ? 1 : 0, true);
+    API_END
+}
+
+int edgpu_mul_adjoint_device(edgpu_op oh, int32_t precision, const void* x, void* y, int64_t n, int32_t accumulate,
+                             void* stream) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    check_prec(precision);
+    check_dim(op, n, "state");
+    if (n == 0) return EDGPU_OK;
+    require(x && y && x != y, EDGPU_ERR_ARG, "bad vectors");
+    launch_product(op, precision, 1, 0, x, y, accumulate ? 1 : 0, nullptr, nullptr, pick_stream(stream));
+    API_END
+}
+
+int edgpu_coupling_grad_device(edgpu_op oh, int32_t precision, const void* x, const void* gy, void* y, int64_t n,
+                               double* grad_out, void* stream) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    check_prec(precision);
+    check_dim(op, n, "state");
+    require(grad_out, EDGPU_ERR_ARG, "null gradient output");
+    if (n == 0) {
+        for (int c = 0; c < op->n_coupl; ++c) grad_out[c] = 0.0;
+        return EDGPU_OK;
+    }
+    require(x && gy, EDGPU_ERR_ARG, "null vector");
+    cudaStream_t st = pick_stream(stream);
+    void* yy = y;
+    if (!yy) {
+        if (precision == EDGPU_FP64) {
+            op->z64.ensure(2 * n);
+            yy = op->z64.p;
+        } else {
+            op->y32.ensure(2 * n);
+            yy = op->y32.p;
+        }
+    }
+    build_blob(op, precision, 0, 1);
+    const int max_blocks = op->blob[precision][0][1].max_blocks;
+    op->grad_partial.ensure((size_t)max_blocks * op->n_coupl);
+    op->grad_dev.ensure(op->n_coupl);
+    int blocks = 0;
+    launch_product(op, precision, 0, 1, x, yy, 0, gy, op->grad_partial.p, st, &blocks);
+    launch_reduce_grad(blocks, op->n_coupl, op->grad_partial.p, op->grad_dev.p, st);
+    EDGPU_CUDA(cudaMemcpyAsync(grad_out, op->grad_dev.p, op->n_coupl * sizeof(double), cudaMemcpyDeviceToHost, st));
+    EDGPU_CUDA(cudaStreamSynchronize(st));
+    API_END
+}
+
+// ---- batched sectors ---------------------------------------------------------------------------
+
+int edgpu_batch_create(int32_t n_ops, const edgpu_op* ops, edgpu_batch* out) {
+    API_BEGIN
+    require(out && n_ops >= 1 && ops, EDGPU_ERR_ARG, "bad batch arguments");
+    *out = nullptr;
+    std::unique_ptr<edgpu_batch_s> b(new edgpu_batch_s());
+    for (int i = 0; i < n_ops; ++i) b->ops.push_back(as_op(ops[i]));
+    *out = b.release();
+    API_END
+}
+
+int edgpu_batch_mul_device(edgpu_batch bh, int32_t precision, const void* const* xs, void* const* ys, int32_t use_graph,
+                           void* stream) {
+    API_BEGIN
+    require(bh && xs && ys, EDGPU_ERR_ARG, "bad batch arguments");
+    check_prec(precision);
+    edgpu_batch_s* b = bh;
+    cudaStream_t st = pick_stream(stream);
+    const int n = (int)b->ops.size();
+    for (int i = 0; i < n; ++i) build_blob(b->ops[i], precision, 0, 0);
+    auto issue = [&](cudaStream_t s) {
+        for (int i = 0; i < n; ++i)
+            launch_product(b->ops[i], precision, 0, 0, xs[i], ys[i], 0, nullptr, nullptr, s);
+    };
+    if (!use_graph) {
+        issue(st);
+        return EDGPU_OK;
+    }
+    std::vector<const void*> key;
+    for (int i = 0; i < n; ++i) {
+        key.push_back(xs[i]);
+        key.push_back(ys[i]);
+    }
+    auto& cache = b->graphs[precision];
+    auto it = cache.find(key);
+    if (it == cache.end()) {
+        cudaGraph_t graph = nullptr;
+        EDGPU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        try {
+            issue(st);
+        } catch (...) {
+            cudaStreamEndCapture(st, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            throw;
+        }
+        EDGPU_CUDA(cudaStreamEndCapture(st, &graph));
+        cudaGraphExec_t exec = nullptr;
+        cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        it = cache.emplace(key, exec).first;
+    }
+    EDGPU_CUDA(cudaGraphLaunch(it->second, st));
+    API_END
+}
+
+void edgpu_batch_destroy(edgpu_batch b) { delete b; }
+
+// ---- Lanczos -------------------------------------------------------------------------------------
+
+int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reorth, uint64_t seed, const double* v0,
+                  int32_t refine, double tol, double* e0, double* alphas, double* betas, int32_t* steps_done,
+                  double* ground_state) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    check_prec(precision);
+    require(n_steps >= 1 && e0, EDGPU_ERR_ARG, "bad Lanczos arguments");
+    const int64_t N = op->space->dim;
+    require(N >= 1, EDGPU_ERR_ARG, "empty representation");
+    cudaStream_t st = g_stream;
+    const int m = (int)std::min<int64_t>(n_steps, N);
+    const bool keep_all = reorth || ground_state || (refine && precision == EDGPU_MIXED);
+    const int nvec = keep_all ? m + 1 : 2;
+    DevBuf<double> V, w, scal, scratch, h, md, psi;
+    DevBuf<float> v32, y32;
+    V.ensure((size_t)nvec * 2 * N);
+    w.ensure(2 * N);
+    scal.ensure(8);
+    scratch.ensure(dot_scratch_doubles());
+    h.ensure(2 * (size_t)(m + 1));
+    md.ensure(2 * (size_t)(m + 1) * 64);
+    if (precision == EDGPU_MIXED) {
+        v32.ensure(2 * N);
+        y32.ensure(2 * N);
+    }
+    double* d_alpha = scal.p;      // [0]=re [1]=im of <v, w>
+    double* d_beta = scal.p + 2;   // current beta
+    double* d_bprev = scal.p + 3;  // previous beta
+    double* d_tmp = scal.p + 4;
+
+    auto vec = [&](int j) { return V.p + (size_t)(keep_all ? j : (j & 1)) * 2 * N; };
+
+    // start vector
+    if (v0) EDGPU_CUDA(cudaMemcpyAsync(vec(0), v0, N * 16, cudaMemcpyHostToDevice, st));
+    else launch_random_c128(N, seed, vec(0), st);
+    launch_norm2_c128(N, vec(0), scratch.p, d_tmp, st);
+    launch_normalize(N, vec(0), d_tmp, vec(0), precision == EDGPU_MIXED ? v32.p : nullptr, st);
+
+    auto run = [&](int prec, int steps, int start_index, std::vector<double>& A, std::vector<double>& B) {
+        // Lanczos steps j = start_index .. steps-1 over the stored/rolling basis; fills A, B
+        double bprev = 0.0;
+        for (int j = start_index; j < steps; ++j) {
+            double* vj = vec(j);
+            if (prec == EDGPU_FP64) {
+                launch_product(op, EDGPU_FP64, 0, 0, vj, w.p, 0, nullptr, nullptr, st);
+            } else {
+                launch_product(op, EDGPU_MIXED, 0, 0, v32.p, y32.p, 0, nullptr, nullptr, st);
+                launch_c64_to_c128(N, y32.p, w.p, 0, st);
+            }
+            launch_dot_c128(N, vj, w.p, scratch.p, d_alpha, st);
+            launch_lanczos_update(N, w.p, vj, j > start_index ? vec(j - 1) : nullptr, d_alpha,
+                                  j > start_index ? d_bprev : nullptr, st);
+            if (reorth) {
+                for (int pass = 0; pass < 2; ++pass) {
+                    launch_multi_dot(N, j + 1, V.p, N, w.p, md.p, h.p, st);
+                    launch_multi_axpy(N, j + 1, V.p, N, h.p, w.p, st);
+                }
+            }
+            launch_norm2_c128(N, w.p, scratch.p, d_beta, st);
+            double hb[3];
+            EDGPU_CUDA(cudaMemcpyAsync(hb, d_alpha, sizeof(double), cudaMemcpyDeviceToHost, st));
+            EDGPU_CUDA(cudaMemcpyAsync(hb + 1, d_beta, sizeof(double), cudaMemcpyDeviceToHost, st));
+            EDGPU_CUDA(cudaStreamSynchronize(st));
+            A.push_back(hb[0]);
+            const double beta = hb[1];
+            if (j == steps - 1 || beta <= 1e-12 * std::max(1.0, std::fabs(hb[0]))) break;
+            B.push_back(beta);
+            launch_normalize(N, w.p, d_beta, vec(j + 1), precision == EDGPU_MIXED ? v32.p : nullptr, st);
+            EDGPU_CUDA(cudaMemcpyAsync(d_bprev, d_beta, sizeof(double), cudaMemcpyDeviceToDevice, st));
+            bprev = beta;
+        }
+        (void)bprev;
+    };
+
+    std::vector<double> A, B;
+    run(precision, m, 0, A, B);
+    double E = lowest_eigenvalue(A, std::vector<double>(B.begin(), B.begin() + (A.size() - 1)));
+    int done = (int)A.size();
+
+    auto ritz_vector = [&](const std::vector<double>& AA, const std::vector<double>& BB, double lam) {
+        std::vector<double> s = tridiag_eigvec(AA, std::vector<double>(BB.begin(), BB.begin() + (AA.size() - 1)), lam);
+        psi.ensure(2 * N);
+        EDGPU_CUDA(cudaMemsetAsync(psi.p, 0, N * 16, st));
+        std::vector<double> coef(2 * s.size());
+        for (size_t k = 0; k < s.size(); ++k) {
+            coef[2 * k] = -s[k];
+            coef[2 * k + 1] = 0.0;
+        }
+        EDGPU_CUDA(cudaMemcpyAsync(h.p, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        launch_multi_axpy(N, (int)s.size(), V.p, N, h.p, psi.p, st);   // psi = sum_k s_k v_k
+    };
+
+    if (refine && precision == EDGPU_MIXED && keep_all) {
+        // polish: FP64 Lanczos restarted from the mixed-precision Ritz vector until |dE| < tol
+        for (int round = 0; round < 8; ++round) {
+            ritz_vector(A, B, E);
+            EDGPU_CUDA(cudaMemcpyAsync(vec(0), psi.p, N * 16, cudaMemcpyDeviceToDevice, st));
+            launch_norm2_c128(N, vec(0), scratch.p, d_tmp, st);
+            launch_normalize(N, vec(0), d_tmp, vec(0), nullptr, st);
+            std::vector<double> A2, B2;
+            const int m2 = std::min(m, 40);
+            run(EDGPU_FP64, m2, 0, A2, B2);
+            const double E2 = lowest_eigenvalue(A2, std::vector<double>(B2.begin(), B2.begin() + (A2.size() - 1)));
+            done += (int)A2.size();
+            const double dE = std::fabs(E2 - E);
+            A = A2;
+            B = B2;
+            E = E2;
+            if (dE < tol * std::max(1.0, std::fabs(E2))) break;
+        }
+    }
+    *e0 = E;
+    if (alphas)
+        for (size_t k = 0; k < (size_t)n_steps; ++k) alphas[k] = k < A.size() ? A[k] : 0.0;
+    if (betas)
+        for (size_t k = 0; k < (size_t)n_steps; ++k) betas[k] = k < B.size() ? B[k] : 0.0;
+    if (steps_done) *steps_done = done;
+    if (ground_state) {
+        ritz_vector(A, B, E);
+        launch_norm2_c128(N, psi.p, scratch.p, d_tmp, st);
+        launch_normalize(N, psi.p, d_tmp, psi.p, nullptr, st);
+        EDGPU_CUDA(cudaMemcpyAsync(ground_state, psi.p, N * 16, cudaMemcpyDeviceToHost, st));
+    }
+    EDGPU_CUDA(cudaStreamSynchronize(st));
+    API_END
+}
+
+// ---- utilities ---------------------------------------------------------------------------------
+
+int edgpu_random_vector_device(int64_t n, uint64_t seed, int32_t precision, void* dst, void* stream) {
+    API_BEGIN
+    check_prec(precision);
+    require(n >= 0 && (n == 0 || dst), EDGPU_ERR_ARG, "bad arguments");
+    if (n == 0) return EDGPU_OK;
+    init_device();
+    cudaStream_t st = pick_stream(stream);
+    DevBuf<double> tmp, scratch, nrm;
+    double* target = nullptr;
+    if (precision == EDGPU_FP64) target = (double*)dst;
+    else {
+        tmp.ensure(2 * n);
+        target = tmp.p;
+    }
+    scratch.ensure(dot_scratch_doubles());
+    nrm.ensure(1);
+    launch_random_c128(n, seed, target, st);
+    launch_norm2_c128(n, target, scratch.p, nrm.p, st);
+    launch_normalize(n, target, nrm.p, target, precision == EDGPU_MIXED ? (float*)dst : nullptr, st);
+    EDGPU_CUDA(cudaStreamSynchronize(st));
+    API_END
+}
+
+int edgpu_sync(void) {
+    API_BEGIN
+    if (g_stream) EDGPU_CUDA(cudaStreamSynchronize(g_stream));
+    API_END
+}
+
+int edgpu_host_alloc(int64_t bytes, void** out) {
+    API_BEGIN
+    require(out && bytes >= 0, EDGPU_ERR_ARG, "bad arguments");
+    init_device();
+    EDGPU_CUDA(cudaMallocHost(out, std::max<int64_t>(bytes, 1)));
+    API_END
+}
+
+void edgpu_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

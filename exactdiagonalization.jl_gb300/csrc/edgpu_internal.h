@@ -1,0 +1,168 @@
+// Internal declarations shared by the translation units of libedgpu.so.
+#pragma once
+
+#include <cstdint>
+#include <cstddef>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/edgpu.h"
+
+namespace edgpu {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define EDGPU_CUDA(call)                                                                               \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess)                                                                         \
+            throw ::edgpu::Error(e_ == cudaErrorMemoryAllocation ? EDGPU_ERR_OOM : EDGPU_ERR_CUDA,     \
+                                 std::string(#call) + ": " + cudaGetErrorString(e_));                 \
+    } while (0)
+
+enum GroupKind { GK_TRIVIAL = 0, GK_TORUS = 1, GK_GENERIC = 2 };
+
+// Symmetry group acting on basis words: element g maps word q to g.q.
+//  TRIVIAL  the identity only (unreduced representation).
+//  TORUS    translations T(a,b) of an L1 x L2 torus of w-bit sites numbered x + L1*y;
+//           g = a + L1*b; T(a,b).q rotates every row of L1*w bits left by a*w and the rows
+//           up by b rows.  num[] is in this order.
+//  GENERIC  arbitrary site permutations (+ XOR flip), applied through 4-bit chunk tables.
+struct Group {
+    int kind = GK_TRIVIAL;
+    int G = 1;
+    int den = 1;
+    std::vector<int32_t> num{0};     // character numerators: chi(g) = exp(2 pi i num[g] / den)
+    int L1 = 1, L2 = 1, w = 1;       // TORUS
+    std::vector<int32_t> maps;       // GENERIC: [G][n_sites] site maps in user order
+    std::vector<uint64_t> flips;     // GENERIC: [G]
+};
+
+struct Layout {
+    int n_sites = 0, nbits = 0, qlen = 0;
+    std::vector<int32_t> dims, bw, off;
+    std::vector<int64_t> state_qn;   // [sum(dims)][qlen], site-major
+    std::vector<int64_t> allowed;    // [n_allowed][qlen]
+    bool all_sectors = false;
+    int popcount = -1;               // >= 0: spin-1/2-like sector = all words of nbits with this popcount
+};
+
+struct Space {
+    Layout lay;
+    bool reduced = false;
+    bool lazy = false;
+    Space* parent = nullptr;         // reduced: the parent representation (not owned)
+    Group group;
+    int64_t dim = 0;
+    bool w32 = false;                // keys are uint32 (nbits <= 31) else uint64
+    void* d_keys = nullptr;          // sorted basis / representatives
+    ~Space();
+};
+
+// ---- device-side descriptors -------------------------------------------------------------------
+
+struct GroupDev {
+    int kind, G, den;
+    int L1, L2, w, rowbits, nbits, nchunks;
+    unsigned long long full;
+    const int32_t* num;              // [G]
+    const unsigned long long* keep;  // [L1] TORUS row-rotation masks (bits that do not wrap)
+    const unsigned long long* lut;   // [G][nchunks][16] GENERIC
+    const unsigned long long* flips; // [G] GENERIC
+};
+
+struct SectorDev {
+    int n_sites, qlen, n_allowed, all_sectors;
+    const int32_t* off;
+    const int32_t* bw;
+    const int32_t* dims;
+    const int32_t* qbase;            // [n_sites] first local-state row of each site in qn
+    const long long* qn;             // [sum dims][qlen]
+    const long long* allowed;        // [n_allowed][qlen]
+};
+
+// Device copy of a Group (owned).
+struct GroupBuffers {
+    GroupDev dev{};
+    int32_t* d_num = nullptr;
+    unsigned long long* d_keep = nullptr;
+    unsigned long long* d_lut = nullptr;
+    unsigned long long* d_flips = nullptr;
+    void upload(const Group& g, const Layout& lay);
+    void release();
+    ~GroupBuffers() { release(); }
+};
+
+// Host helpers used by several units.
+std::vector<unsigned long long> torus_keep_masks(const Group& g, int nbits);
+std::vector<unsigned long long> generic_luts(const Group& g, const Layout& lay, int* nchunks);
+
+// ---- enumeration (enumerate.cu) ---------------------------------------------------------------
+cudaStream_t lib_stream();
+int sm_count();
+void enumerate_parent(Space& s, cudaStream_t st);
+void enumerate_reps(Space& red, const Space& parent, cudaStream_t st);
+void build_mapping(const Space& red, const Space& parent, int64_t* index_out, double* ampl_out, cudaStream_t st);
+void orbit_sizes(const Space& red, int32_t* out_host, cudaStream_t st);
+void lookup_keys(const Space& s, const uint64_t* keys_host, int64_t n, int64_t* out_host, cudaStream_t st);
+
+// ---- matrix-free product (hx*.cu) ----------------------------------------------------------------
+struct HxParams {
+    const void* keys;
+    long long n_rows;
+    const void* x;
+    void* y;
+    const void* gy;
+    double* grad_partial;
+    int accumulate, rows_per_tile, n_coupl;
+    const void* blob;
+    int blob_words16;
+    int o_om, o_or, o_of, o_oa, o_ou, o_oc;   // off-diagonal terms: mask,row,flip,amp,unit amp,coupling id
+    int o_dm, o_dr, o_da, o_du, o_dc;         // diagonal terms
+    int o_ph, o_num, o_divi, o_ratio, o_keep, o_lut, o_flip, o_grad;
+    int T_o, T_d, G, den, nd;
+    int L1, L2, w, rowbits, nbits, nchunks;
+    unsigned long long full;
+    int warp_base;
+};
+
+constexpr int HX_QCAP = 64;          // per-warp target queue capacity (entries)
+constexpr int HX_THREADS = 256;      // threads per block of the product kernel
+int hx_warp_bytes(bool w32);
+
+// Launch the product kernel for (word width, group kind, precision, gradient mode).
+void hx_launch_w32(int gk, int prec, int mode, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
+void hx_launch_w64(int gk, int prec, int mode, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
+int hx_max_blocks_per_sm(bool w32, int gk, int prec, int mode, size_t smem);
+
+// ---- vector kernels (linalg.cu) ------------------------------------------------------------------
+void launch_random_c128(int64_t n, uint64_t seed, double* dst, cudaStream_t st);
+void launch_c128_to_c64(int64_t n, const double* src, float* dst, cudaStream_t st);
+void launch_c64_to_c128(int64_t n, const float* src, double* dst, int accumulate, cudaStream_t st);
+void launch_scale_c128(int64_t n, double s, double* v, cudaStream_t st);
+void launch_conj_c128(int64_t n, double* v, cudaStream_t st);
+// Deterministic FP64 reductions through a per-call scratch buffer of at least dot_scratch_doubles().
+size_t dot_scratch_doubles();
+void launch_dot_c128(int64_t n, const double* a, const double* b, double* scratch, double* out_dev, cudaStream_t st);
+void launch_norm2_c128(int64_t n, const double* a, double* scratch, double* out_dev, cudaStream_t st);
+void launch_reduce_grad(int nblocks, int ncoupl, const double* partial, double* out_dev, cudaStream_t st);
+// Lanczos helpers: w = w - a*v - b*u (a, b device scalars, b may be null)
+void launch_lanczos_update(int64_t n, double* w, const double* v, const double* u, const double* alpha_dev,
+                           const double* beta_dev, cudaStream_t st);
+// w = w - V h (h: k complex device values), and h = V^H w
+void launch_multi_dot(int64_t n, int k, const double* V, int64_t ldv, const double* w, double* scratch,
+                      double* h_dev, cudaStream_t st);
+void launch_multi_axpy(int64_t n, int k, const double* V, int64_t ldv, const double* h_dev, double* w,
+                       cudaStream_t st);
+// v_next = w / beta (beta device scalar); also writes a complex64 copy when v32 != null
+void launch_normalize(int64_t n, const double* w, const double* beta_dev, double* v_next, float* v32,
+                      cudaStream_t st);
+void launch_axpy_real(int64_t n, double a, const double* x, double* y, cudaStream_t st);
+
+}  // namespace edgpu

@@ -1,0 +1,637 @@
+// Sector basis and representative enumeration on the GPU.
+//
+// Replaces hs_get_basis_list(::HilbertSpaceSector) (hilbert_space_representation.jl:127-206) and the
+// representative sweep of symmetry_reduce (symmetry_reduce_generic.jl:22-106).  Candidates are
+// scanned in increasing order, 32 per thread (one bitmap word per thread, written coalesced);
+// a predicate marks the kept ones, per-block popcounts are scanned into offsets, and a second pass
+// regenerates the candidates and writes the kept ones in order: the output is sorted by
+// construction.  Candidate sources:
+//   RANGE  every word below 2^nbits (general sites: local-code validity + QN sum in the allowed set)
+//   COMBO  every nbits-bit word with k set bits, by combinatorial unranking + Gosper's next-
+//          combination step (spin-1/2 2Sz sectors; the parent basis then needs no predicate)
+//   LIST   a materialised parent basis
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+
+#include "edgpu_internal.h"
+#include "edgpu_device.cuh"
+
+namespace edgpu {
+
+namespace {
+
+constexpr int ENUM_THREADS = 256;
+
+unsigned long long* binomial_table() {
+    // C(i, j) for 0 <= i, j <= 64 (row stride 65); C(64, 32) < 2^63 so no entry overflows.
+    static unsigned long long* d_tab = nullptr;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!d_tab) {
+        std::vector<unsigned long long> h(65 * 65, 0ull);
+        for (int i = 0; i <= 64; ++i) {
+            h[i * 65] = 1;
+            for (int j = 1; j <= i; ++j) h[i * 65 + j] = h[(i - 1) * 65 + j - 1] + (j <= i - 1 ? h[(i - 1) * 65 + j] : 0ull);
+        }
+        EDGPU_CUDA(cudaMalloc(&d_tab, h.size() * sizeof(unsigned long long)));
+        EDGPU_CUDA(cudaMemcpy(d_tab, h.data(), h.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+    }
+    return d_tab;
+}
+
+unsigned long long host_binom(int n, int k) {
+    if (k < 0 || k > n) return 0;
+    unsigned long long r = 1;
+    for (int i = 1; i <= k; ++i) r = r * (unsigned long long)(n - k + i) / (unsigned long long)i;
+    return r;
+}
+
+template <typename W>
+__device__ __forceinline__ int ctz_w(W v);
+template <>
+__device__ __forceinline__ int ctz_w<uint32_t>(uint32_t v) { return __ffs((int)v) - 1; }
+template <>
+__device__ __forceinline__ int ctz_w<unsigned long long>(unsigned long long v) { return __ffsll((long long)v) - 1; }
+
+// Colex unranking: the rank-r word with k set bits among n (rank order == numeric order).
+template <typename W>
+__device__ __forceinline__ W unrank_combo(unsigned long long r, int n, int k, const unsigned long long* C) {
+    W v = 0;
+    int c = n;
+    for (int i = k; i >= 1; --i) {
+        do { --c; } while (C[c * 65 + i] > r);
+        v |= (W)1 << c;
+        r -= C[c * 65 + i];
+    }
+    return v;
+}
+
+// Next word with the same popcount (Gosper).
+template <typename W>
+__device__ __forceinline__ W gosper_next(W v) {
+    const W t = v | (v - 1);
+    return (W)((t + 1) | (((~t & (t + 1)) - 1) >> (ctz_w<W>(v) + 1)));
+}
+
+enum { SRC_RANGE = 0, SRC_COMBO = 1, SRC_LIST = 2 };
+
+struct EnumParams {
+    int src;
+    long long total;
+    int n, k;
+    const unsigned long long* C;
+    const void* list;
+    int check_sector;
+    SectorDev sec;
+    int check_rep;
+    GroupDev grp;
+    unsigned* bitmap;
+    long long* block_counts;
+    long long* block_offsets;
+    void* out;
+};
+
+template <typename W>
+__device__ __forceinline__ bool sector_ok(W s, const SectorDev& d) {
+    long long acc[4] = {0, 0, 0, 0};
+    for (int i = 0; i < d.n_sites; ++i) {
+        const int c = (int)((s >> d.off[i]) & (W)(((W)1 << d.bw[i]) - 1));
+        if (c >= d.dims[i]) return false;
+        const long long* q = d.qn + (size_t)(d.qbase[i] + c) * d.qlen;
+        for (int k = 0; k < d.qlen; ++k) acc[k] += q[k];
+    }
+    if (d.all_sectors) return true;
+    for (int a = 0; a < d.n_allowed; ++a) {
+        bool m = true;
+        for (int k = 0; k < d.qlen; ++k) m = m && (d.allowed[a * d.qlen + k] == acc[k]);
+        if (m) return true;
+    }
+    return false;
+}
+
+template <typename W>
+__device__ __forceinline__ bool rep_ok(W s, const GroupDev& g) {
+    if (g.kind == GK_TORUS) {
+        W keep[64];
+        for (int a = 0; a < g.L1; ++a) keep[a] = (W)g.keep[a];
+        return is_rep_torus<W>(s, g.L1, g.L2, g.w, g.rowbits, g.nbits, (W)g.full, keep, g.num);
+    }
+    if (g.kind == GK_GENERIC) {
+        for (int e = 1; e < g.G; ++e) {
+            W t = 0;
+            const unsigned long long* L = g.lut + (size_t)e * g.nchunks * 16;
+            for (int c = 0; c < g.nchunks; ++c) t |= (W)L[c * 16 + (int)((s >> (4 * c)) & 15u)];
+            t ^= (W)g.flips[e];
+            if (t < s) return false;
+            if (t == s && g.num[e] != 0) return false;
+        }
+        return true;
+    }
+    return true;
+}
+
+template <typename W>
+__device__ __forceinline__ W first_candidate(const EnumParams& p, long long r0) {
+    if (p.src == SRC_RANGE) return (W)r0;
+    if (p.src == SRC_COMBO) return unrank_combo<W>((unsigned long long)r0, p.n, p.k, p.C);
+    return ((const W*)p.list)[r0];
+}
+
+template <typename W>
+__device__ __forceinline__ W next_candidate(const EnumParams& p, W v, long long r) {
+    if (p.src == SRC_RANGE) return (W)(v + 1);
+    if (p.src == SRC_COMBO) return gosper_next<W>(v);
+    return ((const W*)p.list)[r];
+}
+
+template <typename W>
+__global__ void __launch_bounds__(ENUM_THREADS) k_mark(EnumParams p) {
+    __shared__ long long tmp[32];
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long r0 = t * 32;
+    unsigned word = 0;
+    if (r0 < p.total) {
+        const int cnt = (int)min(32LL, p.total - r0);
+        W v = first_candidate<W>(p, r0);
+        for (int j = 0; j < cnt; ++j) {
+            bool ok = true;
+            if (p.check_sector) ok = sector_ok<W>(v, p.sec);
+            if (ok && p.check_rep) ok = rep_ok<W>(v, p.grp);
+            if (ok) word |= 1u << j;
+            if (j + 1 < cnt) v = next_candidate<W>(p, v, r0 + j + 1);
+        }
+        p.bitmap[t] = word;
+    }
+    long long tot = 0;
+    block_exclusive_scan((long long)__popc(word), tmp, &tot);
+    if (threadIdx.x == 0) p.block_counts[blockIdx.x] = tot;
+}
+
+__global__ void k_scan_counts(const long long* counts, long long n, long long* offsets, long long* total) {
+    __shared__ long long tmp[32];
+    const long long per = (n + blockDim.x - 1) / blockDim.x;
+    const long long beg = min(n, (long long)threadIdx.x * per), end = min(n, beg + per);
+    long long s = 0;
+    for (long long i = beg; i < end; ++i) s += counts[i];
+    long long tot = 0;
+    long long ex = block_exclusive_scan(s, tmp, &tot);
+    for (long long i = beg; i < end; ++i) {
+        offsets[i] = ex;
+        ex += counts[i];
+    }
+    if (threadIdx.x == 0) *total = tot;
+}
+
+template <typename W>
+__global__ void __launch_bounds__(ENUM_THREADS) k_compact(EnumParams p) {
+    __shared__ long long tmp[32];
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long r0 = t * 32;
+    const unsigned word = (r0 < p.total) ? p.bitmap[t] : 0u;
+    long long pos = block_exclusive_scan((long long)__popc(word), tmp, nullptr) + p.block_offsets[blockIdx.x];
+    if (word) {
+        const int cnt = (int)min(32LL, p.total - r0);
+        W v = first_candidate<W>(p, r0);
+        W* out = (W*)p.out;
+        for (int j = 0; j < cnt; ++j) {
+            if ((word >> j) & 1u) out[pos++] = v;
+            if (j + 1 < cnt) v = next_candidate<W>(p, v, r0 + j + 1);
+        }
+    }
+}
+
+template <typename W>
+__global__ void k_combo_write(long long total, int n, int k, const unsigned long long* C, W* out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long r0 = t * 32;
+    if (r0 >= total) return;
+    W v = unrank_combo<W>((unsigned long long)r0, n, k, C);
+    const int cnt = (int)min(32LL, total - r0);
+    for (int j = 0; j < cnt; ++j) {
+        out[r0 + j] = v;
+        if (j + 1 < cnt) v = gosper_next<W>(v);
+    }
+}
+
+// Device copies of the sector definition for the RANGE predicate.
+struct SectorBuffers {
+    SectorDev dev{};
+    std::vector<void*> ptrs;
+    template <typename T>
+    const T* put(const std::vector<T>& v) {
+        if (v.empty()) return nullptr;
+        void* d = nullptr;
+        EDGPU_CUDA(cudaMalloc(&d, v.size() * sizeof(T)));
+        ptrs.push_back(d);
+        EDGPU_CUDA(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        return (const T*)d;
+    }
+    explicit SectorBuffers(const Layout& lay) {
+        std::vector<int32_t> qbase(lay.n_sites);
+        int acc = 0;
+        for (int i = 0; i < lay.n_sites; ++i) { qbase[i] = acc; acc += lay.dims[i]; }
+        std::vector<long long> qn(lay.state_qn.begin(), lay.state_qn.end());
+        std::vector<long long> al(lay.allowed.begin(), lay.allowed.end());
+        dev.n_sites = lay.n_sites;
+        dev.qlen = lay.qlen;
+        dev.n_allowed = lay.qlen ? (int)(lay.allowed.size() / lay.qlen) : 0;
+        dev.all_sectors = lay.all_sectors ? 1 : 0;
+        dev.off = put(lay.off);
+        dev.bw = put(lay.bw);
+        dev.dims = put(lay.dims);
+        dev.qbase = put(qbase);
+        dev.qn = put(qn);
+        dev.allowed = put(al);
+    }
+    ~SectorBuffers() {
+        for (void* p : ptrs) cudaFree(p);
+    }
+};
+
+template <typename W>
+int64_t run_filtered(EnumParams p, void** out_keys, bool write, cudaStream_t st) {
+    const long long n_words = (p.total + 31) / 32;
+    const long long n_blocks = (n_words + ENUM_THREADS - 1) / ENUM_THREADS;
+    if (n_blocks > 0x7fffffffLL) throw Error(EDGPU_ERR_ARG, "enumeration too large");
+    unsigned* d_bitmap = nullptr;
+    long long* d_counts = nullptr;
+    long long* d_offsets = nullptr;
+    long long* d_total = nullptr;
+    int64_t total = 0;
+    try {
+        EDGPU_CUDA(cudaMalloc(&d_bitmap, std::max<long long>(n_words, 1) * sizeof(unsigned)));
+        EDGPU_CUDA(cudaMalloc(&d_counts, std::max<long long>(n_blocks, 1) * sizeof(long long)));
+        EDGPU_CUDA(cudaMalloc(&d_offsets, std::max<long long>(n_blocks, 1) * sizeof(long long)));
+        EDGPU_CUDA(cudaMalloc(&d_total, sizeof(long long)));
+        p.bitmap = d_bitmap;
+        p.block_counts = d_counts;
+        p.block_offsets = d_offsets;
+        if (n_blocks > 0) {
+            k_mark<W><<<(unsigned)n_blocks, ENUM_THREADS, 0, st>>>(p);
+            EDGPU_CUDA(cudaGetLastError());
+            k_scan_counts<<<1, 1024, 0, st>>>(d_counts, n_blocks, d_offsets, d_total);
+            EDGPU_CUDA(cudaGetLastError());
+            long long h_total = 0;
+            EDGPU_CUDA(cudaMemcpyAsync(&h_total, d_total, sizeof(long long), cudaMemcpyDeviceToHost, st));
+            EDGPU_CUDA(cudaStreamSynchronize(st));
+            total = h_total;
+        }
+        if (write) {
+            void* keys = nullptr;
+            EDGPU_CUDA(cudaMalloc(&keys, std::max<int64_t>(total, 1) * sizeof(W)));
+            p.out = keys;
+            if (total > 0) {
+                k_compact<W><<<(unsigned)n_blocks, ENUM_THREADS, 0, st>>>(p);
+                cudaError_t e = cudaGetLastError();
+                if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+                if (e != cudaSuccess) {
+                    cudaFree(keys);
+                    throw Error(EDGPU_ERR_CUDA, std::string("k_compact: ") + cudaGetErrorString(e));
+                }
+            }
+            *out_keys = keys;
+        }
+    } catch (...) {
+        cudaFree(d_bitmap);
+        cudaFree(d_counts);
+        cudaFree(d_offsets);
+        cudaFree(d_total);
+        throw;
+    }
+    cudaFree(d_bitmap);
+    cudaFree(d_counts);
+    cudaFree(d_offsets);
+    cudaFree(d_total);
+    return total;
+}
+
+template <typename W>
+void enumerate_parent_t(Space& s, cudaStream_t st) {
+    const Layout& lay = s.lay;
+    if (lay.popcount >= 0) {
+        const long long total = (long long)host_binom(lay.nbits, lay.popcount);
+        s.dim = total;
+        if (s.lazy) return;
+        EDGPU_CUDA(cudaMalloc(&s.d_keys, std::max<long long>(total, 1) * sizeof(W)));
+        const long long threads = (total + 31) / 32;
+        if (threads > 0) {
+            k_combo_write<W><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(total, lay.nbits, lay.popcount,
+                                                                             binomial_table(), (W*)s.d_keys);
+            EDGPU_CUDA(cudaGetLastError());
+            EDGPU_CUDA(cudaStreamSynchronize(st));
+        }
+        return;
+    }
+    if (lay.nbits > 34)
+        throw Error(EDGPU_ERR_ARG, "sector enumeration over a generic site layout is limited to 34 bits "
+                                   "(spin-1/2 single-sector spaces have no limit)");
+    SectorBuffers sb(lay);
+    EnumParams p{};
+    p.src = SRC_RANGE;
+    p.total = 1LL << lay.nbits;
+    p.check_sector = 1;
+    p.sec = sb.dev;
+    p.check_rep = 0;
+    s.dim = run_filtered<W>(p, &s.d_keys, !s.lazy, st);
+}
+
+template <typename W>
+void enumerate_reps_t(Space& red, const Space& parent, cudaStream_t st) {
+    const Layout& lay = parent.lay;
+    GroupBuffers gb;
+    gb.upload(red.group, lay);
+    EnumParams p{};
+    p.check_rep = 1;
+    p.grp = gb.dev;
+    if (parent.d_keys) {
+        p.src = SRC_LIST;
+        p.list = parent.d_keys;
+        p.total = parent.dim;
+        red.dim = run_filtered<W>(p, &red.d_keys, true, st);
+    } else if (lay.popcount >= 0) {
+        p.src = SRC_COMBO;
+        p.total = (long long)host_binom(lay.nbits, lay.popcount);
+        p.n = lay.nbits;
+        p.k = lay.popcount;
+        p.C = binomial_table();
+        red.dim = run_filtered<W>(p, &red.d_keys, true, st);
+    } else {
+        if (lay.nbits > 34) throw Error(EDGPU_ERR_ARG, "lazy generic sector limited to 34 bits");
+        SectorBuffers sb(lay);
+        p.src = SRC_RANGE;
+        p.total = 1LL << lay.nbits;
+        p.check_sector = 1;
+        p.sec = sb.dev;
+        red.dim = run_filtered<W>(p, &red.d_keys, true, st);
+    }
+}
+
+// basis_mapping_index / basis_mapping_amplitude for every parent word: orbit minimum, its index in
+// the representative table (-1 when the orbit is incompatible), chi(h)/sqrt(|O|) with h.p = rep.
+template <typename W>
+__global__ void k_mapping(const W* parent, long long n_parent, const W* reps, long long n_reps, GroupDev g,
+                          const double2* phase, long long* index_out, double2* ampl_out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_parent) return;
+    const W q = parent[i];
+    W rep = q;
+    int gb = 0, stab = 1;
+    if (g.kind == GK_TORUS) {
+        W keep[64];
+        for (int a = 0; a < g.L1; ++a) keep[a] = (W)g.keep[a];
+        canon_torus<W>(q, g.L1, g.L2, g.w, g.rowbits, g.nbits, (W)g.full, keep, rep, gb, stab);
+    } else if (g.kind == GK_GENERIC) {
+        rep = q; gb = 0; stab = 0;
+        for (int e = 0; e < g.G; ++e) {
+            W t = 0;
+            const unsigned long long* L = g.lut + (size_t)e * g.nchunks * 16;
+            for (int c = 0; c < g.nchunks; ++c) t |= (W)L[c * 16 + (int)((q >> (4 * c)) & 15u)];
+            t ^= (W)g.flips[e];
+            if (t < rep) { rep = t; gb = e; }
+            stab += (t == q);
+        }
+    }
+    const long long c = sorted_find<W>(reps, n_reps, rep);
+    index_out[i] = c;
+    double2 a = make_double2(0.0, 0.0);
+    if (c >= 0) {
+        const double s = sqrt((double)stab / (double)g.G);
+        const double2 ph = phase[g.num[gb]];
+        a = make_double2(ph.x * s, ph.y * s);
+    }
+    ampl_out[i] = a;
+}
+
+template <typename W>
+__global__ void k_orbit_sizes(const W* reps, long long n, GroupDev g, int32_t* out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const W q = reps[i];
+    int stab = 1;
+    if (g.kind == GK_TORUS) {
+        W keep[64];
+        for (int a = 0; a < g.L1; ++a) keep[a] = (W)g.keep[a];
+        W rep;
+        int gb;
+        canon_torus<W>(q, g.L1, g.L2, g.w, g.rowbits, g.nbits, (W)g.full, keep, rep, gb, stab);
+    } else if (g.kind == GK_GENERIC) {
+        stab = 0;
+        for (int e = 0; e < g.G; ++e) {
+            W t = 0;
+            const unsigned long long* L = g.lut + (size_t)e * g.nchunks * 16;
+            for (int c = 0; c < g.nchunks; ++c) t |= (W)L[c * 16 + (int)((q >> (4 * c)) & 15u)];
+            t ^= (W)g.flips[e];
+            stab += (t == q);
+        }
+    }
+    out[i] = g.G / stab;
+}
+
+template <typename W>
+__global__ void k_lookup(const W* keys, long long n, const unsigned long long* q, long long m, long long* out,
+                         unsigned long long wmask) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const unsigned long long k = q[i];
+    out[i] = ((k & ~wmask) != 0ull) ? -1 : sorted_find<W>(keys, n, (W)k);
+}
+
+}  // namespace
+
+// ---- host side ----------------------------------------------------------------------------------
+
+std::vector<unsigned long long> torus_keep_masks(const Group& g, int nbits) {
+    const int rowbits = g.L1 * g.w;
+    std::vector<unsigned long long> keep(g.L1);
+    for (int a = 0; a < g.L1; ++a) {
+        const int s = a * g.w;
+        const unsigned long long row_keep = (rowbits - s >= 64) ? ~0ull : ((1ull << (rowbits - s)) - 1ull);
+        unsigned long long m = 0;
+        for (int r = 0; r < g.L2; ++r) m |= row_keep << (r * rowbits);
+        keep[a] = m;
+    }
+    (void)nbits;
+    return keep;
+}
+
+std::vector<unsigned long long> generic_luts(const Group& g, const Layout& lay, int* nchunks) {
+    const int nc = (lay.nbits + 3) / 4;
+    *nchunks = nc;
+    std::vector<unsigned long long> lut((size_t)g.G * nc * 16, 0ull);
+    for (int e = 0; e < g.G; ++e) {
+        const int32_t* map = g.maps.data() + (size_t)e * lay.n_sites;
+        for (int c = 0; c < nc; ++c) {
+            for (int v = 0; v < 16; ++v) {
+                const unsigned long long word = (unsigned long long)v << (4 * c);
+                unsigned long long out = 0;
+                for (int i = 0; i < lay.n_sites; ++i) {
+                    const unsigned long long m = (lay.bw[i] >= 64) ? ~0ull : ((1ull << lay.bw[i]) - 1ull);
+                    out |= ((word >> lay.off[i]) & m) << lay.off[map[i]];
+                }
+                lut[((size_t)e * nc + c) * 16 + v] = out;
+            }
+        }
+    }
+    return lut;
+}
+
+void GroupBuffers::upload(const Group& g, const Layout& lay) {
+    release();
+    dev = GroupDev{};
+    dev.kind = g.kind;
+    dev.G = g.G;
+    dev.den = g.den;
+    dev.L1 = g.L1;
+    dev.L2 = g.L2;
+    dev.w = g.w;
+    dev.rowbits = g.L1 * g.w;
+    dev.nbits = lay.nbits;
+    dev.full = (lay.nbits >= 64) ? ~0ull : ((1ull << lay.nbits) - 1ull);
+    EDGPU_CUDA(cudaMalloc(&d_num, std::max<size_t>(g.num.size(), 1) * sizeof(int32_t)));
+    EDGPU_CUDA(cudaMemcpy(d_num, g.num.data(), g.num.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    dev.num = d_num;
+    if (g.kind == GK_TORUS) {
+        auto keep = torus_keep_masks(g, lay.nbits);
+        EDGPU_CUDA(cudaMalloc(&d_keep, keep.size() * sizeof(unsigned long long)));
+        EDGPU_CUDA(cudaMemcpy(d_keep, keep.data(), keep.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+        dev.keep = d_keep;
+    } else if (g.kind == GK_GENERIC) {
+        int nc = 0;
+        auto lut = generic_luts(g, lay, &nc);
+        dev.nchunks = nc;
+        EDGPU_CUDA(cudaMalloc(&d_lut, lut.size() * sizeof(unsigned long long)));
+        EDGPU_CUDA(cudaMemcpy(d_lut, lut.data(), lut.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+        EDGPU_CUDA(cudaMalloc(&d_flips, g.G * sizeof(unsigned long long)));
+        std::vector<unsigned long long> fl(g.flips.begin(), g.flips.end());
+        fl.resize(g.G, 0ull);
+        EDGPU_CUDA(cudaMemcpy(d_flips, fl.data(), g.G * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+        dev.lut = d_lut;
+        dev.flips = d_flips;
+    }
+}
+
+void GroupBuffers::release() {
+    cudaFree(d_num);
+    cudaFree(d_keep);
+    cudaFree(d_lut);
+    cudaFree(d_flips);
+    d_num = nullptr;
+    d_keep = nullptr;
+    d_lut = nullptr;
+    d_flips = nullptr;
+}
+
+Space::~Space() {
+    if (d_keys) cudaFree(d_keys);
+}
+
+void enumerate_parent(Space& s, cudaStream_t st) {
+    if (s.w32) enumerate_parent_t<uint32_t>(s, st);
+    else enumerate_parent_t<unsigned long long>(s, st);
+}
+
+void enumerate_reps(Space& red, const Space& parent, cudaStream_t st) {
+    if (red.w32) enumerate_reps_t<uint32_t>(red, parent, st);
+    else enumerate_reps_t<unsigned long long>(red, parent, st);
+}
+
+namespace {
+template <typename W>
+void build_mapping_t(const Space& red, const Space& parent, int64_t* index_out, double* ampl_out, cudaStream_t st) {
+    GroupBuffers gb;
+    gb.upload(red.group, parent.lay);
+    std::vector<double> ph(2 * (size_t)red.group.den);
+    for (int j = 0; j < red.group.den; ++j) {
+        const double ang = 2.0 * M_PI * (double)j / (double)red.group.den;
+        ph[2 * j] = std::cos(ang);
+        ph[2 * j + 1] = std::sin(ang);
+    }
+    double2* d_ph = nullptr;
+    long long* d_idx = nullptr;
+    double2* d_amp = nullptr;
+    const long long n = parent.dim;
+    try {
+        EDGPU_CUDA(cudaMalloc(&d_ph, ph.size() * sizeof(double)));
+        EDGPU_CUDA(cudaMemcpy(d_ph, ph.data(), ph.size() * sizeof(double), cudaMemcpyHostToDevice));
+        EDGPU_CUDA(cudaMalloc(&d_idx, std::max<long long>(n, 1) * sizeof(long long)));
+        EDGPU_CUDA(cudaMalloc(&d_amp, std::max<long long>(n, 1) * sizeof(double2)));
+        if (n > 0) {
+            k_mapping<W><<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const W*)parent.d_keys, n, (const W*)red.d_keys,
+                                                                    red.dim, gb.dev, d_ph, d_idx, d_amp);
+            EDGPU_CUDA(cudaGetLastError());
+            EDGPU_CUDA(cudaMemcpyAsync(index_out, d_idx, n * sizeof(long long), cudaMemcpyDeviceToHost, st));
+            EDGPU_CUDA(cudaMemcpyAsync(ampl_out, d_amp, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+            EDGPU_CUDA(cudaStreamSynchronize(st));
+        }
+    } catch (...) {
+        cudaFree(d_ph);
+        cudaFree(d_idx);
+        cudaFree(d_amp);
+        throw;
+    }
+    cudaFree(d_ph);
+    cudaFree(d_idx);
+    cudaFree(d_amp);
+}
+
+template <typename W>
+void orbit_sizes_t(const Space& red, int32_t* out_host, cudaStream_t st) {
+    GroupBuffers gb;
+    gb.upload(red.group, red.lay);
+    int32_t* d = nullptr;
+    const long long n = red.dim;
+    EDGPU_CUDA(cudaMalloc(&d, std::max<long long>(n, 1) * sizeof(int32_t)));
+    if (n > 0) {
+        k_orbit_sizes<W><<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const W*)red.d_keys, n, gb.dev, d);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out_host, d, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            cudaFree(d);
+            throw Error(EDGPU_ERR_CUDA, std::string("orbit sizes: ") + cudaGetErrorString(e));
+        }
+    }
+    cudaFree(d);
+}
+
+template <typename W>
+void lookup_t(const Space& s, const uint64_t* keys_host, int64_t n, int64_t* out_host, cudaStream_t st) {
+    unsigned long long* dq = nullptr;
+    long long* dout = nullptr;
+    try {
+        EDGPU_CUDA(cudaMalloc(&dq, std::max<int64_t>(n, 1) * sizeof(unsigned long long)));
+        EDGPU_CUDA(cudaMalloc(&dout, std::max<int64_t>(n, 1) * sizeof(long long)));
+        EDGPU_CUDA(cudaMemcpyAsync(dq, keys_host, n * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+        const unsigned long long wmask = sizeof(W) == 4 ? 0xffffffffull : ~0ull;
+        k_lookup<W><<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const W*)s.d_keys, s.dim, dq, n, dout, wmask);
+        EDGPU_CUDA(cudaGetLastError());
+        EDGPU_CUDA(cudaMemcpyAsync(out_host, dout, n * sizeof(long long), cudaMemcpyDeviceToHost, st));
+        EDGPU_CUDA(cudaStreamSynchronize(st));
+    } catch (...) {
+        cudaFree(dq);
+        cudaFree(dout);
+        throw;
+    }
+    cudaFree(dq);
+    cudaFree(dout);
+}
+}  // namespace
+
+void build_mapping(const Space& red, const Space& parent, int64_t* index_out, double* ampl_out, cudaStream_t st) {
+    if (red.w32) build_mapping_t<uint32_t>(red, parent, index_out, ampl_out, st);
+    else build_mapping_t<unsigned long long>(red, parent, index_out, ampl_out, st);
+}
+
+void orbit_sizes(const Space& red, int32_t* out_host, cudaStream_t st) {
+    if (red.w32) orbit_sizes_t<uint32_t>(red, out_host, st);
+    else orbit_sizes_t<unsigned long long>(red, out_host, st);
+}
+
+void lookup_keys(const Space& s, const uint64_t* keys_host, int64_t n, int64_t* out_host, cudaStream_t st) {
+    if (n <= 0) return;
+    if (s.w32) lookup_t<uint32_t>(s, keys_host, n, out_host, st);
+    else lookup_t<unsigned long long>(s, keys_host, n, out_host, st);
+}
+
+}  // namespace edgpu

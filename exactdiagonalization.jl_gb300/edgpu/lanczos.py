@@ -1,0 +1,44 @@
+"""Lanczos driver for the lowest eigenvalue, on the GPU (no counterpart in the reference, which uses
+dense eigvals or an external Arpack.eigs that calls mul! repeatedly, docs/src/examples/spinhalf.md:26).
+
+FP64 throughout for the scalars, dot products, norms, reorthogonalisation and the tridiagonal
+eigensolve; `precision` selects the product (fp64, or mixed: complex64 vectors and FP32
+accumulation).  With refine=True a mixed-precision run is polished by FP64 Lanczos steps restarted
+from its Ritz vector until |dE| < tol * |E|.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from ._lib import check, lib, ptr
+from .representation import OperatorRepresentation, _prec
+
+
+@dataclass
+class LanczosResult:
+    e0: float
+    alphas: np.ndarray
+    betas: np.ndarray
+    steps: int
+    ground_state: Optional[np.ndarray] = None
+
+
+def lanczos(opr: OperatorRepresentation, n_steps: int = 200, precision="fp64", reorth: bool = True, seed: int = 1,
+            v0=None, refine: bool = False, tol: float = 1e-12, want_vector: bool = False) -> LanczosResult:
+    prec = _prec(precision)
+    e0 = ctypes.c_double()
+    al = np.zeros(n_steps, dtype=np.float64)
+    be = np.zeros(n_steps, dtype=np.float64)
+    done = ctypes.c_int32()
+    v = None if v0 is None else np.ascontiguousarray(v0, dtype=np.complex128)
+    gs = np.empty(opr.dimension, dtype=np.complex128) if want_vector else None
+    check(lib().edgpu_lanczos(opr.handle, prec, int(n_steps), int(bool(reorth)), int(seed),
+                              ptr(v.view(np.float64), ctypes.c_double) if v is not None else None,
+                              int(bool(refine)), float(tol), ctypes.byref(e0), ptr(al, ctypes.c_double),
+                              ptr(be, ctypes.c_double), ctypes.byref(done),
+                              ptr(gs.view(np.float64), ctypes.c_double) if gs is not None else None))
+    return LanczosResult(float(e0.value), al, be, int(done.value), gs)

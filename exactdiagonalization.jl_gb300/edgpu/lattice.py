@@ -1,0 +1,71 @@
+"""Lattice bond lists and spin-1/2 Hamiltonians built through the reference API
+(pauli_matrix products + simplify), as used by the benchmark configurations.
+
+Site (x, y) of an L1 x L2 torus has index x + L1*y (0-based), as in
+examples/spinhalfsquare_large.jl:35 (1 + x + L1*y, 1-based).
+"""
+from __future__ import annotations
+
+from typing import List, Sequence, Tuple
+
+import numpy as np
+
+from .operators import NullOperator, SumOperator, pauli_matrix, simplify
+
+
+def chain_bonds(L: int) -> List[Tuple[int, int]]:
+    """Nearest-neighbour bonds (i, i+1 mod L) of a periodic chain."""
+    return [(i, (i + 1) % L) for i in range(L)]
+
+
+def torus_bonds(L1: int, L2: int, vectors: Sequence[Tuple[int, int]]) -> List[Tuple[int, int]]:
+    """Bonds (x, y) -- (x + dx, y + dy) for every site and every displacement vector (periodic)."""
+    out = []
+    for dx, dy in vectors:
+        for y in range(L2):
+            for x in range(L1):
+                out.append((x + L1 * y, (x + dx) % L1 + L1 * ((y + dy) % L2)))
+    return out
+
+
+TRIANGULAR_NN = [(1, 0), (1, 1), (0, 1)]          # examples/spinhalf_triangular.jl:20
+TRIANGULAR_NNN = [(2, 1), (1, 2), (-1, 1)]        # examples/spinhalf_triangular.jl:21
+SQUARE_NN = [(1, 0), (0, 1)]
+SQUARE_NNN = [(1, 1), (1, -1)]
+
+
+def xxz_hamiltonian(hs, bonds, jxy, jz, coupling_of_bond=None):
+    """H = sum_b (Jxy_b/4 (sx sx + sy sy) + Jz_b/4 sz sz) with sigma = pauli_matrix, then simplify
+    (6 terms per bond).  jxy/jz: scalars or per-bond sequences.
+
+    With coupling_of_bond (bond -> coupling index) also returns the per-term coupling ids and the
+    per-unit amplitudes for gradients: (H, ids, unit_terms) where unit_terms is H with every bond's
+    couplings set to 1 and ids[t] the coupling of term t."""
+    nb = len(bonds)
+    jxy = np.broadcast_to(np.asarray(jxy, dtype=np.float64), (nb,))
+    jz = np.broadcast_to(np.asarray(jz, dtype=np.float64), (nb,))
+    op = NullOperator()
+    for (i, j), a, b in zip(bonds, jxy, jz):
+        bond = (a / 4.0) * (pauli_matrix(hs, i, "x") * pauli_matrix(hs, j, "x") +
+                            pauli_matrix(hs, i, "y") * pauli_matrix(hs, j, "y")) + \
+               (b / 4.0) * (pauli_matrix(hs, i, "z") * pauli_matrix(hs, j, "z"))
+        op = op + bond
+    return simplify(op)
+
+
+def heisenberg_coupled(hs, bonds):
+    """Per-bond Heisenberg terms with unit coupling: (masks, rows, cols, amps, coupling_ids) for
+    H(J) = sum_b J_b S_b.S_b' (S = sigma/2), one coupling per bond."""
+    masks, rows, cols, amps, ids = [], [], [], [], []
+    for c, (i, j) in enumerate(bonds):
+        t = simplify(0.25 * (pauli_matrix(hs, i, "x") * pauli_matrix(hs, j, "x") +
+                             pauli_matrix(hs, i, "y") * pauli_matrix(hs, j, "y") +
+                             pauli_matrix(hs, i, "z") * pauli_matrix(hs, j, "z")))
+        for p in t.terms:
+            masks.append(p.bitmask)
+            rows.append(p.bitrow)
+            cols.append(p.bitcol)
+            amps.append(p.amplitude)
+            ids.append(c)
+    return (np.array(masks, dtype=np.uint64), np.array(rows, dtype=np.uint64), np.array(cols, dtype=np.uint64),
+            np.array(amps, dtype=np.complex128), np.array(ids, dtype=np.int32))

@@ -1,0 +1,190 @@
+/*
+ * edgpu.h -- C ABI of libedgpu.so, the GB300 (sm_103a) implementation of
+ * ExactDiagonalization.jl's sector basis, translation-symmetry reduction and
+ * matrix-free (reduced) Hamiltonian application.
+ *
+ * Every entry point replaces one reference interface, cited as file:line of
+ * kyungminlee/ExactDiagonalization.jl v0.14.3.  Plain pointers and sizes only.
+ *
+ * Conventions
+ *   - Every function returns an int status (EDGPU_OK == 0).  On failure a
+ *     message is available from edgpu_last_error() (per calling thread).
+ *     The status maps to the reference's exception types:
+ *       EDGPU_ERR_ARG    ArgumentError     (bad masks, non-unit amplitudes, BR too small)
+ *       EDGPU_ERR_DIM    DimensionMismatch (vector lengths)
+ *       EDGPU_ERR_BOUNDS BoundsError       (row/column index out of range)
+ *       EDGPU_ERR_KEY    KeyError          (state not in the basis)
+ *   - Indices are 0-based; "absent" is -1 (the reference is 1-based, -1 absent).
+ *   - Basis states are uint64 words; site i occupies bits
+ *     [bitoffset(i), bitoffset(i)+bitwidth(i)) with bitwidth = ceil(log2(dim_i))
+ *     (hilbert_space.jl:25-41, site.jl:93); local state index s is stored as code s-1.
+ *   - Complex vectors are interleaved (re, im).  Host-buffer entry points take
+ *     complex128 (ComplexF64).  Device-buffer entry points take complex128 for
+ *     EDGPU_FP64 and complex64 for EDGPU_MIXED.
+ *   - Handles are not thread-safe for concurrent calls on the same handle;
+ *     distinct handles may be used from different threads.
+ */
+#ifndef EDGPU_H
+#define EDGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EDGPU_OK          0
+#define EDGPU_ERR_ARG     1
+#define EDGPU_ERR_DIM     2
+#define EDGPU_ERR_BOUNDS  3
+#define EDGPU_ERR_KEY     4
+#define EDGPU_ERR_OOM     5
+#define EDGPU_ERR_CUDA    6
+#define EDGPU_ERR_TIMEOUT 7
+#define EDGPU_ERR_STATE   8
+
+/* Arithmetic of the matrix-free product. */
+#define EDGPU_FP64   0   /* complex128 vectors, FP64 accumulation                               */
+#define EDGPU_MIXED  1   /* complex64 vectors, FP32 accumulation; phases and orbit-normalisation
+                            factors computed in FP64 and rounded once                            */
+
+/* Flags of edgpu_space_create. */
+#define EDGPU_SPACE_LAZY 1  /* do not materialise the sector basis (only its definition is kept);
+                               edgpu_reduce then enumerates representatives directly          */
+
+typedef struct edgpu_space_s* edgpu_space;  /* HilbertSpaceRepresentation or ReducedHilbertSpaceRepresentation */
+typedef struct edgpu_op_s* edgpu_op;        /* OperatorRepresentation or ReducedOperatorRepresentation         */
+typedef struct edgpu_batch_s* edgpu_batch;  /* several operator representations applied in one launch          */
+
+/* ---- library --------------------------------------------------------------------------- */
+const char* edgpu_last_error(void);
+const char* edgpu_version(void);
+/* Number of visible CUDA devices (0 when no driver or device is present). */
+int edgpu_device_count(int32_t* out);
+
+/* ---- Hilbert space sector and its basis ------------------------------------------------ */
+/* represent(HilbertSpaceSector(hs, allowed)) with the sorted basis enumerated on the GPU.
+ * Replaces hs_get_basis_list(::HilbertSpaceSector) + represent_array
+ * (hilbert_space_representation.jl:127-206, :215-230) and the sector constructor
+ * (hilbert_space_sector.jl:20-63).
+ *   site_dims[n_sites]          number of local states of each site (Site.states)
+ *   state_qn[sum(site_dims)*qn_len]  quantum-number tuple of each local state, site-major
+ *   allowed_qn[n_allowed*qn_len]     allowed total quantum numbers (n_allowed < 0: all sectors,
+ *                                    i.e. represent(hs), hilbert_space_representation.jl:109-119)
+ * EDGPU_ERR_ARG when the total bit width is >= 64 ("BR too small", :63-69). */
+int edgpu_space_create(int32_t n_sites, const int32_t* site_dims, int32_t qn_len, const int64_t* state_qn,
+                       int32_t n_allowed, const int64_t* allowed_qn, int32_t flags, edgpu_space* out);
+/* represent(hs, basis_list): basis given by the caller, sorted here if needed, duplicates rejected
+ * (hilbert_space_representation.jl:239-256, frozensortedarray.jl:14-22). */
+int edgpu_space_from_basis(int32_t n_sites, const int32_t* site_dims, const uint64_t* basis, int64_t n,
+                           edgpu_space* out);
+/* dimension(hsr) / dimension(rhsr) (hilbert_space_representation.jl:82, reduced_hilbert_space_representation.jl:38) */
+int edgpu_space_dim(edgpu_space s, int64_t* out);
+/* bitwidth(hs) (hilbert_space.jl:96) */
+int edgpu_space_nbits(edgpu_space s, int32_t* out);
+/* basis_list (sorted uint64) copied to host memory of n entries. */
+int edgpu_space_get_basis(edgpu_space s, uint64_t* out, int64_t n);
+/* get(basis_lookup, key, -1) for n keys on the device (frozensortedarray.jl:29-48). */
+int edgpu_space_lookup(edgpu_space s, const uint64_t* keys, int64_t n, int64_t* idx_out);
+void edgpu_space_destroy(edgpu_space s);
+
+/* ---- symmetry reduction ------------------------------------------------------------------ */
+/* symmetry_reduce(hsr, symops_and_amplitudes) (symmetry_reduce_generic.jl:7-106), and the
+ * IrrepComponent forms (symmetry_reduce.jl:12-20, symmetry_reduce_translation.jl) once their
+ * elements are listed.  Element g acts as: the field of site i moves to site site_maps[g*n+i]
+ * (SitePermutation, symmetry_apply.jl:82-92), then the word is XORed with flip_masks[g]
+ * (GlobalBitFlip, bitflipsymmetry.jl:23-35; NULL = no flips).  Its amplitude (the y of the
+ * reference's (op, y) pairs) is exp(2*pi*i*char_num[g]/char_den).  Element 0 must be the
+ * identity with char_num 0; the elements must form a group and the amplitudes a 1-D
+ * representation of it (EDGPU_ERR_ARG otherwise).
+ * Representatives (orbit minima whose stabiliser has character 1) are enumerated on the GPU
+ * into a sorted table; phases and orbit norms are recomputed on the fly by the product, so no
+ * parent-sized table is built. */
+int edgpu_reduce(edgpu_space parent, int32_t n_elems, const int32_t* site_maps, const uint64_t* flip_masks,
+                 const int32_t* char_num, int32_t char_den, edgpu_space* out);
+/* ReducedHilbertSpaceRepresentation.basis_mapping_index / basis_mapping_amplitude
+ * (reduced_hilbert_space_representation.jl:13-22) materialised for a parent of n_parent states:
+ * index_out[n_parent] (reduced index or -1), ampl_out[2*n_parent].  Requires a materialised parent. */
+int edgpu_reduce_mapping(edgpu_space reduced, int64_t* index_out, double* ampl_out, int64_t n_parent);
+/* Orbit size |O| of every representative (1/sqrt(|O|) is the reference's amplitude of a representative). */
+int edgpu_space_orbit_sizes(edgpu_space reduced, int32_t* out, int64_t n);
+
+/* ---- operator representation and the product ------------------------------------------- */
+/* represent(hsr, op) / represent(rhsr, op) (operator_representation.jl:34-36,
+ * reduced_operator_representation.jl:40-42) for a SumOperator given as its terms
+ * (sum_operator.jl:13-23): term t is amps[t] * prod_i (|row_i><col_i| on the bits of masks[t]).
+ * coupling_ids (nullable) tags each term with a coupling index in [0, n_couplings) for
+ * edgpu_coupling_grad; amps are then the per-unit-coupling amplitudes and the operator is
+ * sum_t couplings[coupling_ids[t]] * amps[t] * P_t.  EDGPU_ERR_ARG when (~mask) & row != 0 or
+ * (~mask) & col != 0 (pure_operator.jl:32-36). */
+int edgpu_op_create(edgpu_space s, int32_t n_terms, const uint64_t* masks, const uint64_t* rows,
+                    const uint64_t* cols, const double* amps, const int32_t* coupling_ids,
+                    int32_t n_couplings, const double* couplings, edgpu_op* out);
+/* Change the coupling values of an operator created with coupling_ids. */
+int edgpu_op_set_couplings(edgpu_op op, const double* couplings, int32_t n_couplings);
+int edgpu_op_dim(edgpu_op op, int64_t* out);
+void edgpu_op_destroy(edgpu_op op);
+/* Tile shape of the product kernel: rows per warp tile (a divisor of 32; 0 = default 32). */
+int edgpu_op_set_tiling(edgpu_op op, int32_t precision, int32_t rows_per_tile);
+/* In-library autotuner: times the product for each candidate tile shape on this operator and keeps
+ * the fastest (rows_per_tile_out, best_ms_out nullable). */
+int edgpu_op_autotune(edgpu_op op, int32_t precision, int32_t* rows_per_tile_out, double* best_ms_out);
+
+/* LinearAlgebra.mul!(out, opr, state) (accumulate = 0) and apply!(out, opr, state)
+ * (accumulate = 1) on HOST complex128 vectors of length n: copies in, applies, copies out.
+ * abstract_operator_representation.jl:110-118, :260-267, :296-316, :358-378.
+ * EDGPU_ERR_DIM when n != dimension. */
+int edgpu_mul(edgpu_op op, int32_t precision, const double* x, double* y, int64_t n, int32_t accumulate);
+/* The same on DEVICE vectors (complex128 for EDGPU_FP64, complex64 for EDGPU_MIXED) on a
+ * caller stream (cudaStream_t, NULL = the library stream).  Asynchronous. */
+int edgpu_mul_device(edgpu_op op, int32_t precision, const void* x, void* y, int64_t n, int32_t accumulate,
+                     void* stream);
+/* apply!(out, state, opr): out += transpose(state) * opr (transpose product,
+ * abstract_operator_representation.jl:278-285, :327-347; reduced_operator_representation.jl:88-116),
+ * host complex128 vectors. */
+int edgpu_mul_transpose(edgpu_op op, int32_t precision, const double* x, double* y, int64_t n, int32_t accumulate);
+/* y = H^dagger x on device vectors (the adjoint product dL/dx = H^dagger gy).  For a reduced
+ * representation the orbit phases are recomputed, not stored. */
+int edgpu_mul_adjoint_device(edgpu_op op, int32_t precision, const void* x, void* y, int64_t n,
+                             int32_t accumulate, void* stream);
+/* dL/dJ_c = Re <gy | H_c x> for every coupling c (H = sum_c J_c H_c), fused with y = H x
+ * (y may be NULL).  grad_out: n_couplings doubles in HOST memory.  Device vectors. */
+int edgpu_coupling_grad_device(edgpu_op op, int32_t precision, const void* x, const void* gy, void* y,
+                               int64_t n, double* grad_out, void* stream);
+
+/* ---- batched sectors --------------------------------------------------------------------- */
+/* Several operator representations (e.g. every momentum sector) applied in one persistent launch.
+ * All ops must share the operator terms' shape (word width and group kind). */
+int edgpu_batch_create(int32_t n_ops, const edgpu_op* ops, edgpu_batch* out);
+/* y_k = H_k x_k for every k, device vectors (array of n_ops pointers each). If use_graph != 0 the
+ * launch is captured once into a CUDA graph (per set of pointers) and replayed. */
+int edgpu_batch_mul_device(edgpu_batch b, int32_t precision, const void* const* xs, void* const* ys,
+                           int32_t use_graph, void* stream);
+void edgpu_batch_destroy(edgpu_batch b);
+
+/* ---- Lanczos driver ---------------------------------------------------------------------- */
+/* Lowest eigenvalue by Lanczos on the device: n_steps steps from a seeded complex Gaussian start
+ * vector (or v0, host complex128 of length dim, if not NULL), full FP64 reorthogonalisation when
+ * reorth != 0.  Scalars, dots, norms and the tridiagonal eigensolve are FP64; precision selects the
+ * product.  With refine != 0 and EDGPU_MIXED, the mixed-precision Ritz vector is rebuilt and
+ * polished by FP64 Lanczos steps until |dE| < tol.  Outputs: e0, alphas/betas (n_steps each,
+ * nullable), steps_done.  ground_state (nullable, host complex128 dim): Ritz vector. */
+int edgpu_lanczos(edgpu_op op, int32_t precision, int32_t n_steps, int32_t reorth, uint64_t seed,
+                  const double* v0, int32_t refine, double tol, double* e0, double* alphas, double* betas,
+                  int32_t* steps_done, double* ground_state);
+
+/* ---- utilities --------------------------------------------------------------------------- */
+/* Seeded complex Gaussian vector (SplitMix64 + Box-Muller, (g1 + i g2)/sqrt(2), normalised in FP64)
+ * written to a DEVICE buffer as complex128 (precision EDGPU_FP64) or complex64 (EDGPU_MIXED). */
+int edgpu_random_vector_device(int64_t n, uint64_t seed, int32_t precision, void* dst, void* stream);
+/* Synchronise the library stream. */
+int edgpu_sync(void);
+/* Pinned host memory for the host-buffer entry points (cudaMallocHost / cudaFreeHost). */
+int edgpu_host_alloc(int64_t bytes, void** out);
+void edgpu_host_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EDGPU_H */
