@@ -1,0 +1,422 @@
+#!/usr/bin/env python
+"""Benchmark of the symmetry-reduced Hamiltonian application (mul! on a ReducedOperatorRepresentation).
+
+Metric: reduced H*x throughput in GB/s of the byte model below, as a fraction of the measured HBM
+peak, plus the time to E0 by Lanczos in FP64 and in mixed precision.
+
+A step is one H*x over the whole sector.  Default workload: spin-1/2 Heisenberg chain L=24, periodic,
+J=1, 2Sz=0, momentum 0 (112,720 representatives), mixed precision (complex64 vectors, FP32
+accumulation).  Inputs are seeded complex Gaussian vectors generated on the GPU; successive steps
+cycle through a pool of input/output vectors larger than twice the L2 cache, so each step reads its
+x from HBM.  The operator tables (representatives, terms) stay resident.
+
+Byte model per H*x (s_c = 8 for complex64, 16 for complex128):
+    B = N_r * (8 + 8 + 2 s_c) + NNZ_off * (s_c + 8)
+N_r rows (representative word + orbit norm + x_r + y_r) and NNZ_off off-diagonal elements whose target
+lands on a representative (x gather + one table key).  NNZ_off is counted exactly on the GPU.
+
+Arms:
+  (default)         the GPU path (libedgpu.so) -- device-resident `value`, host-buffer `e2e` through the
+                    C ABI (edgpu_mul with complex128 host vectors, copies inside the timed region).
+  --impl reference  the CPU restatement of the reference's mul! (binary search over the parent basis,
+                    parent-sized mapping tables, rows split statically over all host threads), FP64,
+                    each step a block of rows of the same workload.
+Multi-GPU (torchrun): replicas -- every rank applies the same workload on its own GPU; value sums the
+ranks' bytes over the slowest rank's time.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(ROOT, "exactdiagonalization.jl_gb300")
+for p in (PKG_DIR, ROOT):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "reduced H*x GB/s & % of HBM peak; E0 time mixed vs FP64 at |dE|<1e-9"
+L2_BYTES = 129 * 1024 * 1024
+FALLBACK_HBM_GBS = 6800.0
+
+WORKLOADS = {
+    "chain24_k0": dict(kind="chain", L=24, k=0, jxy=1.0, jz=1.0, seed=2, lanczos_steps=200, reorth=True,
+                       desc="spin-1/2 Heisenberg chain L=24 PBC J=1, 2Sz=0, momentum 0 (24-site translations)"),
+    "chain16_full": dict(kind="chain_full", L=16, jxy=1.0, jz=1.0, seed=1, lanczos_steps=100, reorth=True,
+                         desc="spin-1/2 Heisenberg chain L=16 PBC J=1, 2Sz=0, no symmetry reduction"),
+    "chain28_k0": dict(kind="chain", L=28, k=0, jxy=1.0, jz=1.0, seed=5, lanczos_steps=200, reorth=True,
+                       desc="spin-1/2 Heisenberg chain L=28 PBC, 2Sz=0, momentum 0"),
+    "square6x6_k0": dict(kind="torus", shape=(6, 6), k=(0, 0), nn=[(1, 0), (0, 1)], nnn=[(1, 1), (1, -1)],
+                         j1=1.0, j2=0.5, aniso=1.0, seed=7, lanczos_steps=300, reorth=False,
+                         desc="spin-1/2 J1-J2 Heisenberg 6x6 torus (J2/J1=0.5), 2Sz=0, momentum (0,0)"),
+}
+
+
+# ---------------------------------------------------------------------------------------------------
+def bytes_model(n_rows: int, nnz_off: int, s_c: int) -> int:
+    return n_rows * (8 + 8 + 2 * s_c) + nnz_off * (s_c + 8)
+
+
+def hamiltonian_spec(wl):
+    """(n_sites, bonds, jxy, jz, group shape, momentum) of a workload."""
+    if wl["kind"] in ("chain", "chain_full"):
+        L = wl["L"]
+        bonds = [(i, (i + 1) % L) for i in range(L)]
+        return L, bonds, [wl["jxy"]] * L, [wl["jz"]] * L, (L, 1), (wl.get("k", 0), 0)
+    L1, L2 = wl["shape"]
+    bonds, jxy, jz = [], [], []
+    for vecs, j in ((wl["nn"], wl["j1"]), (wl["nnn"], wl["j2"])):
+        for dx, dy in vecs:
+            for y in range(L2):
+                for x in range(L1):
+                    bonds.append((x + L1 * y, (x + dx) % L1 + L1 * ((y + dy) % L2)))
+                    jxy.append(j)
+                    jz.append(j * wl["aniso"])
+    return L1 * L2, bonds, jxy, jz, (L1, L2), wl["k"]
+
+
+def build_gpu_operator(wl):
+    import edgpu
+    from edgpu import lattice
+    n, bonds, jxy, jz, shape, k = hamiltonian_spec(wl)
+    hs, _ = edgpu.spin_half_system(n)
+    t0 = time.perf_counter()
+    if wl["kind"] == "chain_full":
+        space = edgpu.represent(edgpu.HilbertSpaceSector(hs, 0))
+    else:
+        hsr = edgpu.represent(edgpu.HilbertSpaceSector(hs, 0), lazy=True)
+        space = edgpu.symmetry_reduce(hsr, edgpu.translation_symops(shape, k))
+    t_space = time.perf_counter() - t0
+    H = lattice.xxz_hamiltonian(hs, bonds, jxy, jz)
+    opr = edgpu.represent(space, H)
+    return space, opr, t_space
+
+
+# ---------------------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms in the background."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.samples = []
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "100", "-i", str(device_index)],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append((time.time(), [v.strip() for v in line.split(",")]))
+
+    def count_between(self, t0, t1):
+        return sum(1 for t, _ in self.samples if t0 <= t <= t1)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        if not self.proc:
+            return None
+        rows = [v for t, v in self.samples if t0 <= t <= t1] or [v for _, v in self.samples]
+        if not rows:
+            return None
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if len(r) > 2 and num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if len(r) > 2 and num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and "Active" in r[5 + i]
+                          and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback 6.8 TB/s"
+
+
+def profiled_traffic(workload):
+    """Per-launch DRAM bytes of the product kernel from the committed ncu summary, if any."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "hx_traffic.json")) as f:
+            d = json.load(f)
+        return d.get(workload)
+    except (OSError, ValueError):
+        return None
+
+
+# ---------------------------------------------------------------------------------------------------
+def dist_setup():
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return world, rank, local
+
+
+def combine_ranks(local_seconds: float, local_bytes: float):
+    """Slowest rank's time and the sum of all ranks' bytes (replicas)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return local_seconds, local_bytes
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([local_seconds], dtype=torch.float64, device=dev)
+    b = torch.tensor([local_bytes], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(b, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(b.item())
+
+
+def barrier():
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------------------------------
+def cpu_reference(wl, steps, warmup, budget_s=None, rows_per_step=None):
+    """The reference's mul! restated on the CPU (oracle, FP64, all host threads), on row blocks."""
+    import numpy as np
+    from oracle import oracle as O
+    n, bonds, jxy, jz, shape, k = hamiltonian_spec(wl)
+    sites = O.spin_half_sites(n)
+    parent = O.popcount_basis(n, n // 2)
+    terms = O.heisenberg_terms(n, bonds, jxy, jz)
+    if wl["kind"] == "chain_full":
+        space = parent
+        N = parent.size
+    else:
+        bw, off = O.bit_layout(sites)
+        maps, amps = O.translation_symops(shape, k)
+        space = O.symmetry_reduce(parent, bw, off, maps, amps)
+        N = space.dim
+    x = O.complex_gaussian(N, wl["seed"])
+    sampler = O.RowSampler(space, terms, x)
+    rows = rows_per_step or min(N, 8192)
+    blocks = [(r0, min(N, r0 + rows)) for r0 in range(0, N, rows)]
+    nnz = {}
+    pos = 0
+    for _ in range(warmup):
+        r0, r1 = blocks[pos % len(blocks)]
+        nnz[(r0, r1)] = sampler.run(r0, r1, count=True)
+        pos += 1
+    total_b, total_t, done = 0, 0.0, 0
+    while True:
+        r0, r1 = blocks[pos % len(blocks)]
+        if (r0, r1) not in nnz:
+            nnz[(r0, r1)] = sampler.run(r0, r1, count=True)
+        t0 = time.perf_counter()
+        sampler.run(r0, r1)
+        total_t += time.perf_counter() - t0
+        total_b += bytes_model(r1 - r0, nnz[(r0, r1)], 16)
+        pos += 1
+        done += 1
+        if steps is not None and done >= steps:
+            break
+        if budget_s is not None and total_t >= budget_s:
+            break
+    return {"value": total_b / total_t / 1e9, "unit": "GB/s", "cores": O.num_threads(), "kind": "port",
+            "sample": (f"{done} blocks of {rows} rows of the {N}-row H*x (FP64, oracle restatement of the reference's "
+                       f"apply_parallel!), {total_t:.2f} s of CPU time"),
+            "ms_per_step": 1e3 * total_t / done, "steps": done}
+
+
+def run_reference(args, wl):
+    world, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    if rank != 0:
+        return
+    r = cpu_reference(wl, args.steps, args.warmup)
+    line = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": "GB/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": args.workload, "description": wl["desc"], "parallelism": "host threads"},
+            "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": r["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------------------
+def run_gpu(args, wl):
+    import numpy as np
+    import torch
+    import edgpu
+
+    world, rank, local = dist_setup()
+    dev = torch.cuda.current_device()
+    space, opr, t_space = build_gpu_operator(wl)
+    N = space.dimension
+    n_targets, nnz = opr.count_nnz()
+    tune_mixed = opr.autotune("mixed")
+    tune_fp64 = opr.autotune("fp64")
+    stream = torch.cuda.current_stream()
+
+    def pool(prec):
+        s_c = 8 if prec == "mixed" else 16
+        P = max(2, min(4096, math.ceil(2 * L2_BYTES / (2 * N * s_c))))
+        xs = [edgpu.random_state(N, wl["seed"] * 1000 + i, prec) for i in range(P)]
+        ys = [torch.empty_like(xs[0]) for _ in range(P)]
+        return xs, ys, P, s_c
+
+    def timed(prec, steps, warmup):
+        xs, ys, P, s_c = pool(prec)
+        for i in range(warmup):
+            edgpu.mul_(ys[i % P], opr, xs[i % P], precision=prec)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t_wall0 = time.time()
+        e0.record(stream)
+        for i in range(steps):
+            edgpu.mul_(ys[i % P], opr, xs[i % P], precision=prec)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_wall1 = time.time()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        return ms, P, s_c, (t_wall0, t_wall1), (xs, ys)
+
+    clocks = ClockSampler(dev) if rank == 0 else None
+    ms_mixed, P_mixed, s_c, (tw0, tw1), bufs = timed("mixed", args.steps, args.warmup)
+    # keep the GPU busy until the clock sampler has seen the load (the timed region may be short)
+    if clocks and clocks.proc:
+        xs, ys = bufs
+        t_end = time.time() + 1.0
+        i = 0
+        while clocks.count_between(tw0, time.time()) < 3 and time.time() < t_end:
+            for _ in range(64):
+                edgpu.mul_(ys[i % len(xs)], opr, xs[i % len(xs)], precision="mixed")
+                i += 1
+            torch.cuda.synchronize()
+        tw1 = max(tw1, time.time())
+    del bufs
+    clk = clocks.summary(tw0 - 0.15, tw1 + 0.15) if clocks else None
+    if clocks:
+        clocks.stop()
+
+    b_mixed = bytes_model(N, nnz, 8)
+    t_max, b_all = combine_ranks(ms_mixed / 1e3, b_mixed * args.steps)
+    value = b_all / t_max / 1e9
+    per_launch_ms = ms_mixed / args.steps
+    achieved = b_mixed / (per_launch_ms / 1e3) / 1e9
+
+    fp64_steps = max(1, args.steps // 4)
+    ms64, _, _, _, bufs64 = timed("fp64", fp64_steps, max(3, args.warmup // 4))
+    del bufs64
+    b64 = bytes_model(N, nnz, 16)
+    value64 = b64 / (ms64 / fp64_steps / 1e3) / 1e9
+
+    # end to end through the C ABI with pinned host complex128 buffers (the reference's mul! interface)
+    x_h = torch.empty(N, dtype=torch.complex128, pin_memory=True)
+    y_h = torch.empty(N, dtype=torch.complex128, pin_memory=True)
+    x_h.copy_(edgpu.random_state(N, wl["seed"], "fp64").cpu())
+    xn, yn = x_h.numpy(), y_h.numpy()
+    e2e_steps = max(3, min(args.steps, 500))
+    for _ in range(3):
+        edgpu.mul_(yn, opr, xn, precision="mixed")
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        edgpu.mul_(yn, opr, xn, precision="mixed")
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    e2e = {"value": b_mixed / t_e2e / 1e9, "unit": "GB/s", "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N,
+           "ms_per_step": t_e2e * 1e3}
+
+    # time to E0 (Lanczos): FP64 product vs mixed product polished in FP64
+    e0_info = None
+    if not args.no_lanczos:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r64 = edgpu.lanczos(opr, wl["lanczos_steps"], precision="fp64", reorth=wl["reorth"], seed=wl["seed"])
+        t64 = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        rmx = edgpu.lanczos(opr, wl["lanczos_steps"], precision="mixed", reorth=wl["reorth"], seed=wl["seed"],
+                            refine=True, tol=1e-12)
+        tmx = time.perf_counter() - t0
+        e0_info = {"fp64_s": t64, "mixed_s": tmx, "e0_fp64": r64.e0, "e0_mixed": rmx.e0,
+                   "rel_diff": abs(rmx.e0 - r64.e0) / abs(r64.e0), "steps_fp64": r64.steps, "steps_mixed": rmx.steps}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        r = cpu_reference(wl, None, 2, budget_s=args.cpu_seconds)
+        cpu = {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    peak, peak_src = measured_peak()
+    traffic = profiled_traffic(args.workload)
+    line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+            "config": {"workload": args.workload, "description": wl["desc"], "N_r": N, "n_targets": n_targets,
+                       "nnz_off": nnz, "bytes_per_step": b_mixed, "l2": f"inputs cycled from a pool of {P_mixed} x/y "
+                       f"pairs ({2 * P_mixed * N * s_c / 1e6:.0f} MB > 2x L2)", "parallelism": f"replicas x{world}",
+                       "rows_per_tile": {"mixed": tune_mixed[0], "fp64": tune_fp64[0]},
+                       "setup_s": t_space},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "peak_source": peak_src},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps, "clocks": clk,
+            "fp64": {"value": value64, "unit": "GB/s", "ms_per_step": ms64 / fp64_steps, "frac": value64 / peak},
+            "e0": e0_info}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5000)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="chain24_k0")
+    ap.add_argument("--no-lanczos", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl)
+    else:
+        run_gpu(args, wl)
+
+
+if __name__ == "__main__":
+    main()

@@ -893,6 +893,21 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     API_END
 }
 
+int edgpu_op_count_nnz(edgpu_op oh, int64_t* n_targets, int64_t* nnz_off) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    require(n_targets && nnz_off, EDGPU_ERR_ARG, "null output");
+    std::vector<uint64_t> m, r, f;
+    for (int t = 0; t < op->T; ++t)
+        if (op->rows[t] != op->cols[t]) {
+            m.push_back(op->masks[t]);
+            r.push_back(op->rows[t]);
+            f.push_back(op->rows[t] ^ op->cols[t]);
+        }
+    count_nnz(*op->space, (int)m.size(), m.data(), r.data(), f.data(), n_targets, nnz_off, g_stream);
+    API_END
+}
+
 // ---- products ----------------------------------------------------------------------------------
 
 static void host_product(edgpu_op_s* op, int prec, int dir, const double* x, double* y, int64_t n, int accumulate,

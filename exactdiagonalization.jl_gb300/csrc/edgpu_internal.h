@@ -111,6 +111,9 @@ void enumerate_reps(Space& red, const Space& parent, cudaStream_t st);
 void build_mapping(const Space& red, const Space& parent, int64_t* index_out, double* ampl_out, cudaStream_t st);
 void orbit_sizes(const Space& red, int32_t* out_host, cudaStream_t st);
 void lookup_keys(const Space& s, const uint64_t* keys_host, int64_t n, int64_t* out_host, cudaStream_t st);
+// Off-diagonal targets of every row (T terms: masks/rows/flips = row ^ col) and how many land in the table.
+void count_nnz(const Space& s, int T, const uint64_t* masks, const uint64_t* rows, const uint64_t* flips,
+               int64_t* n_targets, int64_t* n_found, cudaStream_t st);
 
 // ---- matrix-free product (hx*.cu) ----------------------------------------------------------------
 struct HxParams {

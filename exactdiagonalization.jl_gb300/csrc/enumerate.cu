@@ -437,6 +437,76 @@ __global__ void k_lookup(const W* keys, long long n, const unsigned long long* q
     out[i] = ((k & ~wmask) != 0ull) ? -1 : sorted_find<W>(keys, n, (W)k);
 }
 
+template <typename W>
+__global__ void k_count_nnz(const W* keys, long long n, GroupDev g, int T, const unsigned long long* masks,
+                            const unsigned long long* rows, const unsigned long long* flips,
+                            unsigned long long* counts /* [0] targets, [1] found */) {
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long nt = 0, nf = 0;
+    if (r < n) {
+        const W b = keys[r];
+        for (int t = 0; t < T; ++t) {
+            if ((b & (W)masks[t]) != (W)rows[t]) continue;
+            const W q = b ^ (W)flips[t];
+            ++nt;
+            W rep = q;
+            int gb = 0, stab = 1;
+            if (g.kind == GK_TORUS) {
+                W keep[64];
+                for (int a = 0; a < g.L1; ++a) keep[a] = (W)g.keep[a];
+                canon_torus<W>(q, g.L1, g.L2, g.w, g.rowbits, g.nbits, (W)g.full, keep, rep, gb, stab);
+            } else if (g.kind == GK_GENERIC) {
+                for (int e = 0; e < g.G; ++e) {
+                    W tt = 0;
+                    const unsigned long long* L = g.lut + (size_t)e * g.nchunks * 16;
+                    for (int c = 0; c < g.nchunks; ++c) tt |= (W)L[c * 16 + (int)((q >> (4 * c)) & 15u)];
+                    tt ^= (W)g.flips[e];
+                    if (tt < rep) rep = tt;
+                }
+            }
+            nf += (sorted_find<W>(keys, n, rep) >= 0);
+        }
+    }
+    for (int d = 16; d > 0; d >>= 1) {
+        nt += __shfl_down_sync(0xffffffffu, nt, d);
+        nf += __shfl_down_sync(0xffffffffu, nf, d);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(counts, nt);
+        atomicAdd(counts + 1, nf);
+    }
+}
+
+template <typename W>
+void count_nnz_t(const Space& s, int T, const uint64_t* masks, const uint64_t* rows, const uint64_t* flips,
+                 int64_t* n_targets, int64_t* n_found, cudaStream_t st) {
+    GroupBuffers gb;
+    gb.upload(s.group, s.lay);
+    unsigned long long* d = nullptr;
+    const size_t tb = std::max(T, 1) * sizeof(unsigned long long);
+    EDGPU_CUDA(cudaMalloc(&d, 3 * tb + 2 * sizeof(unsigned long long)));
+    unsigned long long* dm = d;
+    unsigned long long* dr = d + std::max(T, 1);
+    unsigned long long* df = d + 2 * std::max(T, 1);
+    unsigned long long* dc = d + 3 * std::max(T, 1);
+    cudaError_t e = cudaSuccess;
+    unsigned long long h[2] = {0, 0};
+    if (T > 0) e = cudaMemcpyAsync(dm, masks, T * 8, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && T > 0) e = cudaMemcpyAsync(dr, rows, T * 8, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && T > 0) e = cudaMemcpyAsync(df, flips, T * 8, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dc, 0, 2 * sizeof(unsigned long long), st);
+    if (e == cudaSuccess && s.dim > 0) {
+        k_count_nnz<W><<<(unsigned)((s.dim + 255) / 256), 256, 0, st>>>((const W*)s.d_keys, s.dim, gb.dev, T, dm, dr, df, dc);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, dc, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d);
+    if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("count_nnz: ") + cudaGetErrorString(e));
+    *n_targets = (int64_t)h[0];
+    *n_found = (int64_t)h[1];
+}
+
 }  // namespace
 
 // ---- host side ----------------------------------------------------------------------------------
@@ -634,4 +704,12 @@ void lookup_keys(const Space& s, const uint64_t* keys_host, int64_t n, int64_t* 
     else lookup_t<unsigned long long>(s, keys_host, n, out_host, st);
 }
 
+}  // namespace edgpu
+
+namespace edgpu {
+void count_nnz(const Space& s, int T, const uint64_t* masks, const uint64_t* rows, const uint64_t* flips,
+               int64_t* n_targets, int64_t* n_found, cudaStream_t st) {
+    if (s.w32) count_nnz_t<uint32_t>(s, T, masks, rows, flips, n_targets, n_found, st);
+    else count_nnz_t<unsigned long long>(s, T, masks, rows, flips, n_targets, n_found, st);
+}
 }  // namespace edgpu

@@ -518,6 +518,12 @@ class OperatorRepresentation:
         check(lib().edgpu_op_autotune(self._h, _prec(precision), ctypes.byref(r), ctypes.byref(ms)))
         return int(r.value), float(ms.value)
 
+    def count_nnz(self):
+        """(off-diagonal targets generated, of which land on a row of the representation)."""
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        check(lib().edgpu_op_count_nnz(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return int(a.value), int(b.value)
+
     def set_tiling(self, precision, rows_per_tile):
         check(lib().edgpu_op_set_tiling(self._h, _prec(precision), int(rows_per_tile)))
 

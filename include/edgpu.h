@@ -129,6 +129,10 @@ int edgpu_op_set_tiling(edgpu_op op, int32_t precision, int32_t rows_per_tile);
 /* In-library autotuner: times the product for each candidate tile shape on this operator and keeps
  * the fastest (rows_per_tile_out, best_ms_out nullable). */
 int edgpu_op_autotune(edgpu_op op, int32_t precision, int32_t* rows_per_tile_out, double* best_ms_out);
+/* Number of off-diagonal (row, term) matches over all rows, and how many of them land on a row of
+ * the representation (the nonzero off-diagonal elements the row iterator yields with a valid column,
+ * reduced_operator_representation.jl:57-85) -- the NNZ_off of the product's byte model. */
+int edgpu_op_count_nnz(edgpu_op op, int64_t* n_targets, int64_t* nnz_off);
 
 /* LinearAlgebra.mul!(out, opr, state) (accumulate = 0) and apply!(out, opr, state)
  * (accumulate = 1) on HOST complex128 vectors of length n: copies in, applies, copies out.

@@ -173,24 +173,52 @@ static cplx row_sum(int64_t irow, const uint64_t* basis, const uint64_t* parent,
     return acc;
 }
 
-/* apply!(out, opr, state): out += opr * state (accumulate=1) or mul!: fill!(out,0) then apply!
- * (abstract_operator_representation.jl:110-118).  Rows are split statically over threads
- * like Threads.@threads in apply_parallel! (:358-378). */
-void or_apply_rows(const uint64_t* basis, int64_t nrows, const uint64_t* parent, int64_t n_parent,
-                   const int64_t* map_index, const double* map_ampl,
-                   int T, const uint64_t* masks, const uint64_t* rows, const uint64_t* cols,
-                   const double* amps, const double* state, double* out, int accumulate, int nthreads) {
+/* apply!(out, opr, state) restricted to rows [r0, r1): out += opr * state (accumulate=1) or mul!:
+ * fill!(out,0) then apply! (abstract_operator_representation.jl:110-118).  Rows are split statically
+ * over threads like Threads.@threads in apply_parallel! (:358-378).  When nnz_out is not NULL it
+ * receives the number of off-diagonal elements with a valid column in those rows. */
+void or_apply_rows_range(const uint64_t* basis, int64_t nrows, const uint64_t* parent, int64_t n_parent,
+                         const int64_t* map_index, const double* map_ampl,
+                         int T, const uint64_t* masks, const uint64_t* rows, const uint64_t* cols,
+                         const double* amps, const double* state, double* out, int accumulate, int nthreads,
+                         int64_t r0, int64_t r1, int64_t* nnz_out) {
     const cplx* a = (const cplx*)amps; const cplx* x = (const cplx*)state; cplx* y = (cplx*)out;
     const cplx* ma = (const cplx*)map_ampl;
+    if (r0 < 0) r0 = 0;
+    if (r1 > nrows) r1 = nrows;
 #ifdef _OPENMP
     if (nthreads <= 0) nthreads = omp_get_max_threads();
 #pragma omp parallel for schedule(static) num_threads(nthreads)
 #endif
-    for (int64_t r = 0; r < nrows; ++r) {
+    for (int64_t r = r0; r < r1; ++r) {
         cplx acc = accumulate ? y[r] : (cplx){0.0, 0.0};
         y[r] = row_sum(r, basis, parent, n_parent, map_index, ma, T, masks, rows, cols, a, x, nrows, acc);
     }
+    if (nnz_out) {
+        int64_t nnz = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads) reduction(+:nnz)
+#endif
+        for (int64_t r = r0; r < r1; ++r) {
+            uint64_t brow = basis[r];
+            for (int t = 0; t < T; ++t) {
+                if (rows[t] == cols[t] || (brow & masks[t]) != rows[t]) continue;
+                int64_t icol = or_lookup(parent, n_parent, (brow & ~masks[t]) | cols[t]);
+                if (icol >= 0 && map_index) icol = map_index[icol];
+                if (icol >= 0) ++nnz;
+            }
+        }
+        *nnz_out = nnz;
+    }
     (void)nthreads;
+}
+
+void or_apply_rows(const uint64_t* basis, int64_t nrows, const uint64_t* parent, int64_t n_parent,
+                   const int64_t* map_index, const double* map_ampl,
+                   int T, const uint64_t* masks, const uint64_t* rows, const uint64_t* cols,
+                   const double* amps, const double* state, double* out, int accumulate, int nthreads) {
+    or_apply_rows_range(basis, nrows, parent, n_parent, map_index, map_ampl, T, masks, rows, cols, amps, state,
+                        out, accumulate, nthreads, 0, nrows, NULL);
 }
 
 /* apply!(out, state, opr): out += transpose(state) * opr via get_column_iterator

@@ -52,6 +52,10 @@ def lib():
             f.restype = None
             f.argtypes = [u64p, ctypes.c_int64, u64p, ctypes.c_int64, i64p, dp, ctypes.c_int, u64p, u64p, u64p,
                           dp, dp, dp, ctypes.c_int, ctypes.c_int]
+        L.or_apply_rows_range.restype = None
+        L.or_apply_rows_range.argtypes = [u64p, ctypes.c_int64, u64p, ctypes.c_int64, i64p, dp, ctypes.c_int, u64p,
+                                          u64p, u64p, dp, dp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int64,
+                                          ctypes.c_int64, i64p]
         L.or_unreduce.restype = None
         L.or_unreduce.argtypes = [i64p, dp, ctypes.c_int64, dp, dp]
         L.or_reduce_vector.restype = None
@@ -373,6 +377,35 @@ def apply_rows(space, terms, x, out=None, accumulate=False, nthreads=0):
     if isinstance(space, ReducedTables):
         return _apply("or_apply_rows", space.basis_list, space.parent, space, terms, x, out, accumulate, nthreads)
     return _apply("or_apply_rows", space, space, None, terms, x, out, accumulate, nthreads)
+
+
+class RowSampler:
+    """Bounded samples of mul! for the CPU baseline: rows [r0, r1) of opr * x with all host threads.
+    The off-diagonal element count of each row block is returned for the byte model."""
+
+    def __init__(self, space, terms, x, nthreads=0):
+        if isinstance(space, ReducedTables):
+            self.basis, self.parent, self.red = space.basis_list, space.parent, space
+        else:
+            self.basis, self.parent, self.red = space, space, None
+        self.masks, self.rows, self.cols, amps = term_arrays(terms) if not isinstance(terms, tuple) else terms
+        self.amps = np.ascontiguousarray(amps, dtype=np.complex128)
+        self.x = np.ascontiguousarray(x, dtype=np.complex128)
+        self.y = np.zeros(self.basis.size, dtype=np.complex128)
+        self.nthreads = int(nthreads)
+
+    def run(self, r0, r1, count=False):
+        nnz = np.zeros(1, dtype=np.int64)
+        mi = None if self.red is None else self.red.basis_mapping_index
+        ma = None if self.red is None else self.red.basis_mapping_amplitude.view(np.float64)
+        lib().or_apply_rows_range(_p(self.basis, ctypes.c_uint64), self.basis.size, _p(self.parent, ctypes.c_uint64),
+                                  self.parent.size, _p(mi, ctypes.c_int64), _p(ma, ctypes.c_double), len(self.masks),
+                                  _p(self.masks, ctypes.c_uint64), _p(self.rows, ctypes.c_uint64),
+                                  _p(self.cols, ctypes.c_uint64), _p(self.amps.view(np.float64), ctypes.c_double),
+                                  _p(self.x.view(np.float64), ctypes.c_double),
+                                  _p(self.y.view(np.float64), ctypes.c_double), 0, self.nthreads, int(r0), int(r1),
+                                  _p(nnz, ctypes.c_int64) if count else None)
+        return int(nnz[0])
 
 
 def apply_cols(space, terms, x, out=None, accumulate=False, nthreads=0):
