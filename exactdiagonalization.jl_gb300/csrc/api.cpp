@@ -56,7 +56,8 @@ void init_device() {
     EDGPU_CUDA(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
 }
 
-cudaStream_t pick_stream(void* s) { return s ? (cudaStream_t)s : g_stream; }
+// NULL selects the CUDA default stream, like the stream argument of CUDA's own libraries.
+cudaStream_t pick_stream(void* s) { return (cudaStream_t)s; }
 
 template <typename T>
 struct DevBuf {
@@ -95,13 +96,16 @@ unsigned long long binom_u64(int n, int k) {
 
 struct Blob {
     bool ready = false;
+    int gk = 0;              // product-kernel group kind (GK_RING for 32-bit rings)
     void* d = nullptr;
     HxParams tmpl{};
     size_t smem = 0;
     int max_blocks = 0;      // resident blocks for the whole GPU
     int rows_per_tile = 32;
+    void* d_diag = nullptr;  // per-row diagonal element in the blob's precision (product mode)
     ~Blob() {
         if (d) cudaFree(d);
+        if (d_diag) cudaFree(d_diag);
     }
 };
 
@@ -170,8 +174,6 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     for (int d = 1; d <= g.G; ++d)
         if (g.G % d == 0) divs.push_back(d);
     const int nd = (int)divs.size();
-    std::vector<int32_t> divi(g.G + 1, 0);
-    for (int i = 0; i < nd; ++i) divi[divs[i]] = i;
 
     int nchunks = 0;
     std::vector<unsigned long long> keep, lut;
@@ -185,20 +187,19 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
         return (int)o;
     };
     HxParams p{};
-    p.o_om = alloc(T_o * wsz);
-    p.o_or = alloc(T_o * wsz);
-    p.o_of = alloc(T_o * wsz);
+    p.o_om = alloc(T_o * 4 * wsz);   // packed records (mask, row, row ^ col, 0)
+    p.o_or = p.o_om;
+    p.o_of = p.o_om;
     p.o_oa = alloc(T_o * vsz);
-    p.o_ou = alloc(T_o * vsz);
-    p.o_oc = alloc(T_o * 4);
-    p.o_dm = alloc(T_d * wsz);
-    p.o_dr = alloc(T_d * wsz);
-    p.o_da = alloc(T_d * 16);
-    p.o_du = alloc(T_d * 16);
-    p.o_dc = alloc(T_d * 4);
+    p.o_ou = alloc(mode ? T_o * vsz : 0);
+    p.o_oc = alloc(mode ? T_o * 4 : 0);
+    p.o_dm = alloc(mode ? T_d * wsz : 0);
+    p.o_dr = alloc(mode ? T_d * wsz : 0);
+    p.o_da = alloc(mode ? T_d * 16 : 0);
+    p.o_du = alloc(mode ? T_d * 16 : 0);
+    p.o_dc = alloc(mode ? T_d * 4 : 0);
     p.o_ph = alloc(g.den * vsz);
     p.o_num = alloc(g.G * 4);
-    p.o_divi = alloc((g.G + 1) * 4);
     p.o_ratio = alloc(nd * nd * rsz);
     p.o_keep = alloc(keep.size() * wsz);
     p.o_lut = alloc(lut.size() * wsz);
@@ -227,34 +228,43 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
         const int t = offd[k];
         const uint64_t r = dir ? op->cols[t] : op->rows[t];
         const uint64_t c = dir ? op->rows[t] : op->cols[t];
-        putw(p.o_om, k, op->masks[t]);
-        putw(p.o_or, k, r);
-        putw(p.o_of, k, r ^ c);
+        putw(p.o_om, 4 * k, op->masks[t]);
+        putw(p.o_om, 4 * k + 1, r);
+        putw(p.o_om, 4 * k + 2, r ^ c);
         double re, im;
         amp_of(t, false, re, im);
         putv(p.o_oa, k, re, im);
-        amp_of(t, true, re, im);
-        putv(p.o_ou, k, re, im);
-        memcpy(&h[p.o_oc + k * 4], &op->cid[t], 4);
+        if (mode) {
+            amp_of(t, true, re, im);
+            putv(p.o_ou, k, re, im);
+            memcpy(&h[p.o_oc + k * 4], &op->cid[t], 4);
+        }
     }
+    std::vector<uint64_t> dg_mask(T_d), dg_row(T_d);
+    std::vector<double> dg_amp(2 * (size_t)T_d);
     for (int k = 0; k < T_d; ++k) {
         const int t = diag[k];
         const uint64_t r = dir ? op->cols[t] : op->rows[t];
-        putw(p.o_dm, k, op->masks[t]);
-        putw(p.o_dr, k, r);
         double v[2];
         amp_of(t, false, v[0], v[1]);
-        memcpy(&h[p.o_da + k * 16], v, 16);
-        amp_of(t, true, v[0], v[1]);
-        memcpy(&h[p.o_du + k * 16], v, 16);
-        memcpy(&h[p.o_dc + k * 4], &op->cid[t], 4);
+        dg_mask[k] = op->masks[t];
+        dg_row[k] = r;
+        dg_amp[2 * k] = v[0];
+        dg_amp[2 * k + 1] = v[1];
+        if (mode) {
+            putw(p.o_dm, k, op->masks[t]);
+            putw(p.o_dr, k, r);
+            memcpy(&h[p.o_da + k * 16], v, 16);
+            amp_of(t, true, v[0], v[1]);
+            memcpy(&h[p.o_du + k * 16], v, 16);
+            memcpy(&h[p.o_dc + k * 4], &op->cid[t], 4);
+        }
     }
     for (int j = 0; j < g.den; ++j) {
         const double ang = 2.0 * M_PI * (double)j / (double)g.den;
         putv(p.o_ph, j, std::cos(ang), std::sin(ang));
     }
     memcpy(&h[p.o_num], g.num.data(), g.G * 4);
-    memcpy(&h[p.o_divi], divi.data(), (g.G + 1) * 4);
     for (int i = 0; i < nd; ++i)
         for (int j = 0; j < nd; ++j) {
             const double f = std::sqrt((double)divs[j] / (double)divs[i]);   // sqrt(|O_r| / |O_c|)
@@ -276,6 +286,14 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
 
     if (B.d) cudaFree(B.d);
     B.d = nullptr;
+    if (B.d_diag) cudaFree(B.d_diag);
+    B.d_diag = nullptr;
+    if (!mode) {
+        EDGPU_CUDA(cudaMalloc(&B.d_diag, std::max<int64_t>(s.dim, 1) * vsz));
+        compute_diagonal(s, T_d, dg_mask.data(), dg_row.data(), dg_amp.data(),
+                         prec == EDGPU_FP64 ? (double*)B.d_diag : nullptr,
+                         prec == EDGPU_FP64 ? nullptr : (float*)B.d_diag, g_stream);
+    }
     EDGPU_CUDA(cudaMalloc(&B.d, std::max<size_t>(blob_bytes, 16)));
     EDGPU_CUDA(cudaMemcpy(B.d, h.data(), blob_bytes, cudaMemcpyHostToDevice));
     p.blob = B.d;
@@ -295,9 +313,25 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     p.keys = s.d_keys;
     p.n_rows = s.dim;
     p.n_coupl = op->n_coupl;
+    p.sb = s.sb;
+    p.want_arg = g.den > 1 ? 1 : 0;
+    p.dir = s.d_dir;
+    p.diag = B.d_diag;
+    p.dir_shift = s.dir_shift;
+    p.dir_nb = s.dir_nb;
+    p.dir_steps = s.dir_steps;
+    int gk = g.kind;
+    p.pb = 0;
+    if (gk == GK_TORUS && g.L2 == 1 && w32 && s.lay.nbits <= 31) {
+        gk = GK_RING;
+        int pb = 0;
+        while ((1 << pb) < g.L1) ++pb;
+        p.pb = (s.lay.nbits + pb <= 32) ? pb : 0;
+    }
+    B.gk = gk;
     B.tmpl = p;
     B.smem = tot;
-    const int per_sm = std::max(1, hx_max_blocks_per_sm(w32, g.kind, prec, mode, tot));
+    const int per_sm = std::max(1, hx_max_blocks_per_sm(w32, gk, prec, mode, tot));
     B.max_blocks = per_sm * std::max(1, g_sm_count);
     B.ready = true;
 }
@@ -307,7 +341,9 @@ void invalidate_blobs(edgpu_op_s* op) {
         for (auto& b : a)
             for (auto& c : b) {
                 if (c.d) cudaFree(c.d);
+                if (c.d_diag) cudaFree(c.d_diag);
                 c.d = nullptr;
+                c.d_diag = nullptr;
                 c.ready = false;
             }
 }
@@ -337,8 +373,8 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
     p.accumulate = accumulate;
     const int blocks = blocks_for(B, p.n_rows, rows);
     if (blocks_used) *blocks_used = blocks;
-    if (op->space->w32) hx_launch_w32(op->space->group.kind, prec, mode, p, blocks, B.smem, st);
-    else hx_launch_w64(op->space->group.kind, prec, mode, p, blocks, B.smem, st);
+    if (op->space->w32) hx_launch_w32(B.gk, prec, mode, p, blocks, B.smem, st);
+    else hx_launch_w64(B.gk, prec, mode, p, blocks, B.smem, st);
 }
 
 edgpu_space_s* as_space(edgpu_space s) {
@@ -528,6 +564,7 @@ int edgpu_space_create(int32_t n_sites, const int32_t* site_dims, int32_t qn_len
     }
     init_device();
     enumerate_parent(*s, g_stream);
+    if (!s->lazy) build_search_directory(*s, g_stream);
     *out = s.release();
     API_END
 }
@@ -572,6 +609,7 @@ int edgpu_space_from_basis(int32_t n_sites, const int32_t* site_dims, const uint
         EDGPU_CUDA(cudaMalloc(&s->d_keys, std::max<int64_t>(n, 1) * 8));
         EDGPU_CUDA(cudaMemcpy(s->d_keys, b.data(), n * 8, cudaMemcpyHostToDevice));
     }
+    build_search_directory(*s, g_stream);
     *out = s.release();
     API_END
 }
@@ -598,13 +636,7 @@ int edgpu_space_get_basis(edgpu_space sh, uint64_t* out, int64_t n) {
                                                      std::to_string(s->dim));
     if (n == 0) return EDGPU_OK;
     require(out, EDGPU_ERR_ARG, "null output");
-    if (s->w32) {
-        std::vector<uint32_t> tmp(n);
-        EDGPU_CUDA(cudaMemcpy(tmp.data(), s->d_keys, n * 4, cudaMemcpyDeviceToHost));
-        for (int64_t i = 0; i < n; ++i) out[i] = tmp[i];
-    } else {
-        EDGPU_CUDA(cudaMemcpy(out, s->d_keys, n * 8, cudaMemcpyDeviceToHost));
-    }
+    get_states(*s, out, g_stream);
     API_END
 }
 
@@ -731,14 +763,18 @@ int edgpu_reduce(edgpu_space parent_h, int32_t n_elems, const int32_t* site_maps
     s->reduced = true;
     s->parent = parent;
     s->group = g;
-    s->w32 = parent->w32;
+    s->sb = g.kind == GK_TRIVIAL ? 0 : orbit_index_bits(g.G);
+    require(L.nbits + s->sb <= 64, EDGPU_ERR_ARG, "state plus orbit index does not fit a 64-bit key");
+    s->w32 = L.nbits + s->sb <= 32;
     init_device();
     if (parent->dim == 0) {
         s->dim = 0;
         EDGPU_CUDA(cudaMalloc(&s->d_keys, 16));
     } else {
         enumerate_reps(*s, *parent, g_stream);
+        embed_orbit_index(*s, g_stream);
     }
+    build_search_directory(*s, g_stream);
     *out = s.release();
     API_END
 }
@@ -1055,18 +1091,29 @@ int edgpu_batch_mul_device(edgpu_batch bh, int32_t precision, const void* const*
     auto& cache = b->graphs[precision];
     auto it = cache.find(key);
     if (it == cache.end()) {
+        // Capture on a private stream (the caller's stream may be the legacy default stream, which
+        // cannot be captured); the graph is then launched on the caller's stream.
+        cudaStream_t cap = nullptr;
+        EDGPU_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
         cudaGraph_t graph = nullptr;
-        EDGPU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            cudaStreamDestroy(cap);
+            throw Error(EDGPU_ERR_CUDA, std::string("begin capture: ") + cudaGetErrorString(e));
+        }
         try {
-            issue(st);
+            issue(cap);
         } catch (...) {
-            cudaStreamEndCapture(st, &graph);
+            cudaStreamEndCapture(cap, &graph);
             if (graph) cudaGraphDestroy(graph);
+            cudaStreamDestroy(cap);
             throw;
         }
-        EDGPU_CUDA(cudaStreamEndCapture(st, &graph));
+        e = cudaStreamEndCapture(cap, &graph);
+        cudaStreamDestroy(cap);
+        if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e));
         cudaGraphExec_t exec = nullptr;
-        cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        e = cudaGraphInstantiate(&exec, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
         it = cache.emplace(key, exec).first;

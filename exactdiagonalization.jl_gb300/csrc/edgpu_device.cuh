@@ -1,5 +1,11 @@
 // Device helpers shared by the enumeration and product kernels: group action on basis words
-// (orbit minimum, stabiliser size, representative test) and the branch-free sorted-table search.
+// (orbit minimum and the element that reaches it, stabiliser size, representative test), the key
+// encoding of representative tables and the branch-free sorted-table search.
+//
+// Key encoding.  A table of representatives stores key = (state << sb) | sidx, where sidx (sb bits)
+// is the index of the representative's stabiliser size among the divisors of the group order, so the
+// orbit norm of any row or found column comes with the key.  Unreduced tables have sb = 0 (key =
+// state).  Keys sort like states, so the search compares against (rep << sb) | (2^sb - 1).
 #pragma once
 
 #include <cstdint>
@@ -9,7 +15,6 @@
 
 namespace edgpu {
 
-// Word type of the basis table: uint32 when the state has <= 31 bits, else uint64.
 template <typename W>
 __device__ __forceinline__ W ldg_w(const W* p) { return __ldg(p); }
 
@@ -20,12 +25,12 @@ __device__ __forceinline__ W torus_row_rotate(W r, int s, W keep, W full, int ro
     return (W)(((r & keep) << s) | ((r & (full ^ keep)) >> (rowbits - s)));
 }
 
-// Minimum of the orbit of q (the representative), the element g with g.q == rep that is found
-// first, and the stabiliser size |{g : g.q == q}|.
-// TORUS: loop over row shifts b (rotate the word by rowbits) and in-row shifts a.
+// Orbit minimum of q under the torus translations, the first element g (= a + L1*b) reaching it
+// (only when want_arg), and the stabiliser size |{g : g.q == q}| (only when want_stab).
 template <typename W>
 __device__ __forceinline__ void canon_torus(W q, int L1, int L2, int w, int rowbits, int nbits, W full,
-                                            const W* keep, W& rep, int& gbest, int& stab) {
+                                            const W* keep, bool want_arg, bool want_stab, W& rep, int& gbest,
+                                            int& stab) {
     rep = q;
     gbest = 0;
     stab = 0;
@@ -33,11 +38,102 @@ __device__ __forceinline__ void canon_torus(W q, int L1, int L2, int w, int rowb
     for (int b = 0; b < L2; ++b) {
         for (int a = 0; a < L1; ++a) {
             const W t = torus_row_rotate<W>(r, a * w, keep[a], full, rowbits);
-            if (t < rep) { rep = t; gbest = a + L1 * b; }
-            stab += (t == q);
+            if (want_arg) {
+                if (t < rep) { rep = t; gbest = a + L1 * b; }
+            } else {
+                rep = t < rep ? t : rep;
+            }
+            if (want_stab) stab += (t == q);
         }
         r = (W)(((r << rowbits) | (r >> (nbits - rowbits))) & full);
     }
+}
+
+// Ring (L2 == 1) of n <= 31 bits in 32-bit words: rotations by funnel shifts of the doubled word
+// d = q | q << n, since bits [n - s, 2n - s) of d are q rotated left by s.  With pb index bits
+// (n + pb <= 32) the element index rides in the low bits of each candidate, so a single unsigned
+// min yields both the representative and the element reaching it: 3 instructions per element.
+__device__ __forceinline__ void canon_ring32(unsigned q, int n, int L1, int w, int pb, bool want_arg,
+                                             unsigned& rep, int& gbest) {
+    const unsigned mask = (n >= 32) ? 0xffffffffu : ((1u << n) - 1u);
+    if (pb > 0) {
+        const unsigned long long d = ((unsigned long long)q | ((unsigned long long)q << n)) << pb;
+        const unsigned lo = (unsigned)d, hi = (unsigned)(d >> 32);
+        const unsigned kmask = mask << pb;
+        unsigned best = 0xffffffffu;
+#pragma unroll 4
+        for (int a = 0; a < L1; ++a) {
+            const unsigned t = (__funnelshift_r(lo, hi, n - a * w) & kmask) | (unsigned)a;
+            best = min(best, t);
+        }
+        rep = best >> pb;
+        gbest = (int)(best & ((1u << pb) - 1u));
+        return;
+    }
+    const unsigned long long d = (unsigned long long)q | ((unsigned long long)q << n);
+    const unsigned lo = (unsigned)d, hi = (unsigned)(d >> 32);
+    unsigned best = 0xffffffffu;
+#pragma unroll 4
+    for (int a = 0; a < L1; ++a) best = min(best, __funnelshift_r(lo, hi, n - a * w) & mask);
+    rep = best;
+    gbest = 0;
+    if (want_arg) {
+#pragma unroll 4
+        for (int a = L1 - 1; a >= 0; --a)
+            if ((__funnelshift_r(lo, hi, n - a * w) & mask) == best) gbest = a;
+    }
+}
+
+// The same for 1-bit sites and a compile-time ring length N: fully unrolled with constant shifts.
+template <int N>
+__device__ __forceinline__ void canon_ring_n(unsigned q, int pb, bool want_arg, unsigned& rep, int& gbest) {
+    const unsigned mask = (N >= 32) ? 0xffffffffu : ((1u << N) - 1u);
+    if (pb > 0) {
+        const unsigned long long d = ((unsigned long long)q | ((unsigned long long)q << N)) << pb;
+        const unsigned lo = (unsigned)d, hi = (unsigned)(d >> 32);
+        const unsigned kmask = mask << pb;
+        unsigned best = 0xffffffffu;
+#pragma unroll
+        for (int a = 0; a < N; ++a) best = min(best, (__funnelshift_r(lo, hi, N - a) & kmask) | (unsigned)a);
+        rep = best >> pb;
+        gbest = (int)(best & ((1u << pb) - 1u));
+        return;
+    }
+    const unsigned long long d = (unsigned long long)q | ((unsigned long long)q << N);
+    const unsigned lo = (unsigned)d, hi = (unsigned)(d >> 32);
+    unsigned best = 0xffffffffu;
+#pragma unroll
+    for (int a = 0; a < N; ++a) best = min(best, __funnelshift_r(lo, hi, N - a) & mask);
+    rep = best;
+    gbest = 0;
+    if (want_arg) {
+#pragma unroll
+        for (int a = N - 1; a >= 0; --a)
+            if ((__funnelshift_r(lo, hi, N - a) & mask) == best) gbest = a;
+    }
+}
+
+// Ring canonicalisation dispatched on the (warp-uniform) ring length for 1-bit sites.
+__device__ __forceinline__ void canon_ring(unsigned q, int n, int L1, int w, int pb, bool want_arg, unsigned& rep,
+                                           int& gbest) {
+    if (w == 1) {
+        switch (n) {
+            case 8: canon_ring_n<8>(q, pb, want_arg, rep, gbest); return;
+            case 10: canon_ring_n<10>(q, pb, want_arg, rep, gbest); return;
+            case 12: canon_ring_n<12>(q, pb, want_arg, rep, gbest); return;
+            case 14: canon_ring_n<14>(q, pb, want_arg, rep, gbest); return;
+            case 16: canon_ring_n<16>(q, pb, want_arg, rep, gbest); return;
+            case 18: canon_ring_n<18>(q, pb, want_arg, rep, gbest); return;
+            case 20: canon_ring_n<20>(q, pb, want_arg, rep, gbest); return;
+            case 22: canon_ring_n<22>(q, pb, want_arg, rep, gbest); return;
+            case 24: canon_ring_n<24>(q, pb, want_arg, rep, gbest); return;
+            case 26: canon_ring_n<26>(q, pb, want_arg, rep, gbest); return;
+            case 28: canon_ring_n<28>(q, pb, want_arg, rep, gbest); return;
+            case 30: canon_ring_n<30>(q, pb, want_arg, rep, gbest); return;
+            default: break;
+        }
+    }
+    canon_ring32(q, n, L1, w, pb, want_arg, rep, gbest);
 }
 
 // GENERIC: g.q = OR_c lut[g][c][nibble_c(q)] XOR flips[g].
@@ -51,15 +147,15 @@ __device__ __forceinline__ W generic_apply(W q, int g, int nchunks, const W* lut
 }
 
 template <typename W>
-__device__ __forceinline__ void canon_generic(W q, int G, int nchunks, const W* lut, const W* flips, W& rep,
-                                              int& gbest, int& stab) {
+__device__ __forceinline__ void canon_generic(W q, int G, int nchunks, const W* lut, const W* flips,
+                                              bool want_stab, W& rep, int& gbest, int& stab) {
     rep = q;
     gbest = 0;
     stab = 0;
     for (int g = 0; g < G; ++g) {
         const W t = generic_apply<W>(q, g, nchunks, lut, flips);
         if (t < rep) { rep = t; gbest = g; }
-        stab += (t == q);
+        if (want_stab) stab += (t == q);
     }
 }
 
@@ -92,17 +188,82 @@ __device__ __forceinline__ bool is_rep_generic(W q, int G, int nchunks, const W*
     return true;
 }
 
-// Branch-free search of a sorted table: the iteration count depends on n only, so the lanes of a
-// warp stay converged.  Returns the index of key or -1 (get(FrozenSortedArrayIndex, key, -1)).
+// Branch-free search of a sorted key table for the state `rep` (keys carry sb low index bits).
+// The iteration count depends on n only, so the lanes of a warp stay converged.  Returns the index
+// or -1 (get(FrozenSortedArrayIndex, key, -1)); *key_out receives the key found.
 template <typename W>
-__device__ __forceinline__ long long sorted_find(const W* __restrict__ keys, long long n, W key) {
+__device__ __forceinline__ long long key_find(const W* __restrict__ keys, long long n, W rep, int sb, W* key_out) {
+    const W target = (W)((rep << sb) | (W)((((W)1) << sb) - 1));
     long long lo = 0, len = n;
     while (len > 1) {
         const long long half = len >> 1;
-        lo = (ldg_w(keys + lo + half) <= key) ? lo + half : lo;
+        lo = (ldg_w(keys + lo + half) <= target) ? lo + half : lo;
         len -= half;
     }
-    return (n > 0 && ldg_w(keys + lo) == key) ? lo : -1;
+    const W k = (n > 0) ? ldg_w(keys + lo) : (W)0;
+    if (key_out) *key_out = k;
+    return (n > 0 && (k >> sb) == rep) ? lo : -1;
+}
+
+// Bucketed branch-free search.  dir[b] = start | (count << 40) of the keys whose state lies in
+// [b << shift, (b + 1) << shift); b is clamped to nb (an empty sentinel bucket).  The window search
+// runs `steps` = ceil(log2(max bucket)) halvings, so one directory load and a few probes inside one
+// or two cache sectors replace the ~log2(n) dependent probes of a plain binary search.
+template <typename W>
+__device__ __forceinline__ long long key_find_dir(const W* __restrict__ keys, const unsigned long long* __restrict__ dir,
+                                                  int shift, long long nb, int steps, W rep, int sb, W* key_out) {
+    const long long b = min((long long)(rep >> shift), nb);
+    const unsigned long long e = __ldg(dir + b);
+    long long lo = (long long)(e & 0xffffffffffull);
+    int len = (int)(e >> 40);
+    *key_out = (W)0;
+    if (len == 0) return -1;
+    const W target = (W)((rep << sb) | (W)((((W)1) << sb) - 1));
+    for (int k = 0; k < steps; ++k) {
+        const int half = len >> 1;
+        if (half > 0) {
+            lo = (ldg_w(keys + lo + half) <= target) ? lo + half : lo;
+            len -= half;
+        }
+    }
+    const W kk = ldg_w(keys + lo);
+    *key_out = kk;
+    return ((kk >> sb) == rep) ? lo : -1;
+}
+
+// Two independent bucketed searches run in lockstep, so their loads overlap (memory-level
+// parallelism of 2 per lane).  act[h] == false skips target h; c[h] = index or -1.
+template <typename W>
+__device__ __forceinline__ void key_find_dir2(const W* __restrict__ keys, const unsigned long long* __restrict__ dir,
+                                              int shift, long long nb, int steps, const W* rep, const bool* act, int sb,
+                                              long long* c, W* key_out) {
+    long long lo[2];
+    int len[2];
+    W target[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const unsigned long long e = act[h] ? __ldg(dir + min((long long)(rep[h] >> shift), nb)) : 0ull;
+        lo[h] = (long long)(e & 0xffffffffffull);
+        len[h] = (int)(e >> 40);
+        target[h] = (W)((rep[h] << sb) | (W)((((W)1) << sb) - 1));
+    }
+    const bool valid0 = len[0] > 0, valid1 = len[1] > 0;
+    for (int k = 0; k < steps; ++k) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int half = len[h] >> 1;
+            if (half > 0) {
+                lo[h] = (ldg_w(keys + lo[h] + half) <= target[h]) ? lo[h] + half : lo[h];
+                len[h] -= half;
+            }
+        }
+    }
+    const W k0 = valid0 ? ldg_w(keys + lo[0]) : (W)0;
+    const W k1 = valid1 ? ldg_w(keys + lo[1]) : (W)0;
+    key_out[0] = k0;
+    key_out[1] = k1;
+    c[0] = (valid0 && (k0 >> sb) == rep[0]) ? lo[0] : -1;
+    c[1] = (valid1 && (k1 >> sb) == rep[1]) ? lo[1] : -1;
 }
 
 __device__ __forceinline__ unsigned lanemask_lt() {

@@ -26,7 +26,7 @@ struct Error : std::runtime_error {
                                  std::string(#call) + ": " + cudaGetErrorString(e_));                 \
     } while (0)
 
-enum GroupKind { GK_TRIVIAL = 0, GK_TORUS = 1, GK_GENERIC = 2 };
+enum GroupKind { GK_TRIVIAL = 0, GK_TORUS = 1, GK_GENERIC = 2, GK_RING = 3 };
 
 // Symmetry group acting on basis words: element g maps word q to g.q.
 //  TRIVIAL  the identity only (unreduced representation).
@@ -34,6 +34,7 @@ enum GroupKind { GK_TRIVIAL = 0, GK_TORUS = 1, GK_GENERIC = 2 };
 //           g = a + L1*b; T(a,b).q rotates every row of L1*w bits left by a*w and the rows
 //           up by b rows.  num[] is in this order.
 //  GENERIC  arbitrary site permutations (+ XOR flip), applied through 4-bit chunk tables.
+//  RING     (product kernel only) a TORUS with L2 == 1 in 32-bit words: funnel-shift rotations.
 struct Group {
     int kind = GK_TRIVIAL;
     int G = 1;
@@ -60,8 +61,13 @@ struct Space {
     Space* parent = nullptr;         // reduced: the parent representation (not owned)
     Group group;
     int64_t dim = 0;
-    bool w32 = false;                // keys are uint32 (nbits <= 31) else uint64
-    void* d_keys = nullptr;          // sorted basis / representatives
+    bool w32 = false;                // keys are uint32 (nbits + sb <= 32) else uint64
+    int sb = 0;                      // low key bits holding the orbit-size index (0: unreduced)
+    void* d_keys = nullptr;          // sorted keys: (state << sb) | orbit-size index
+    unsigned long long* d_dir = nullptr;   // search directory: start | count << 40 per bucket of states
+    int dir_shift = 0;               // bucket of a state = state >> dir_shift
+    long long dir_nb = 0;            // number of buckets (entry dir_nb is an empty sentinel)
+    int dir_steps = 0;               // ceil(log2(largest bucket))
     ~Space();
 };
 
@@ -111,6 +117,17 @@ void enumerate_reps(Space& red, const Space& parent, cudaStream_t st);
 void build_mapping(const Space& red, const Space& parent, int64_t* index_out, double* ampl_out, cudaStream_t st);
 void orbit_sizes(const Space& red, int32_t* out_host, cudaStream_t st);
 void lookup_keys(const Space& s, const uint64_t* keys_host, int64_t n, int64_t* out_host, cudaStream_t st);
+// Number of index bits for the divisors of G, and the divisor index of every stabiliser size.
+int orbit_index_bits(int G);
+// Rewrite a freshly enumerated representative table as keys (state << sb) | orbit-size index, and
+// build the shared-memory search tree of any table.
+void embed_orbit_index(Space& red, cudaStream_t st);
+void build_search_directory(Space& s, cudaStream_t st);
+void get_states(const Space& s, uint64_t* out_host, cudaStream_t st);
+// Diagonal element of every row: sum of the amplitudes of the row == col terms matching the row's state
+// (FP64), written as complex128 (out64) and/or complex64 (out32).
+void compute_diagonal(const Space& s, int T, const uint64_t* masks, const uint64_t* rows, const double* amps,
+                      double* out64, float* out32, cudaStream_t st);
 // Off-diagonal targets of every row (T terms: masks/rows/flips = row ^ col) and how many land in the table.
 void count_nnz(const Space& s, int T, const uint64_t* masks, const uint64_t* rows, const uint64_t* flips,
                int64_t* n_targets, int64_t* n_found, cudaStream_t st);
@@ -128,14 +145,19 @@ struct HxParams {
     int blob_words16;
     int o_om, o_or, o_of, o_oa, o_ou, o_oc;   // off-diagonal terms: mask,row,flip,amp,unit amp,coupling id
     int o_dm, o_dr, o_da, o_du, o_dc;         // diagonal terms
-    int o_ph, o_num, o_divi, o_ratio, o_keep, o_lut, o_flip, o_grad;
+    const unsigned long long* dir;
+    const void* diag;                         // per-row diagonal element (V), product mode
+    long long dir_nb;
+    int dir_shift, dir_steps;
+    int o_ph, o_num, o_ratio, o_keep, o_lut, o_flip, o_grad;
     int T_o, T_d, G, den, nd;
     int L1, L2, w, rowbits, nbits, nchunks;
+    int sb, pb, want_arg;
     unsigned long long full;
     int warp_base;
 };
 
-constexpr int HX_QCAP = 64;          // per-warp target queue capacity (entries)
+constexpr int HX_QCAP = 128;         // per-warp target queue capacity (entries; 2 batches of 32 + 31)
 constexpr int HX_THREADS = 256;      // threads per block of the product kernel
 int hx_warp_bytes(bool w32);
 

@@ -82,6 +82,7 @@ struct EnumParams {
     int n, k;
     const unsigned long long* C;
     const void* list;
+    int list_w32;
     int check_sector;
     SectorDev sec;
     int check_rep;
@@ -135,14 +136,14 @@ template <typename W>
 __device__ __forceinline__ W first_candidate(const EnumParams& p, long long r0) {
     if (p.src == SRC_RANGE) return (W)r0;
     if (p.src == SRC_COMBO) return unrank_combo<W>((unsigned long long)r0, p.n, p.k, p.C);
-    return ((const W*)p.list)[r0];
+    return p.list_w32 ? (W)((const unsigned*)p.list)[r0] : (W)((const unsigned long long*)p.list)[r0];
 }
 
 template <typename W>
 __device__ __forceinline__ W next_candidate(const EnumParams& p, W v, long long r) {
     if (p.src == SRC_RANGE) return (W)(v + 1);
     if (p.src == SRC_COMBO) return gosper_next<W>(v);
-    return ((const W*)p.list)[r];
+    return p.list_w32 ? (W)((const unsigned*)p.list)[r] : (W)((const unsigned long long*)p.list)[r];
 }
 
 template <typename W>
@@ -347,6 +348,7 @@ void enumerate_reps_t(Space& red, const Space& parent, cudaStream_t st) {
     if (parent.d_keys) {
         p.src = SRC_LIST;
         p.list = parent.d_keys;
+        p.list_w32 = parent.w32 ? 1 : 0;
         p.total = parent.dim;
         red.dim = run_filtered<W>(p, &red.d_keys, true, st);
     } else if (lay.popcount >= 0) {
@@ -369,18 +371,18 @@ void enumerate_reps_t(Space& red, const Space& parent, cudaStream_t st) {
 
 // basis_mapping_index / basis_mapping_amplitude for every parent word: orbit minimum, its index in
 // the representative table (-1 when the orbit is incompatible), chi(h)/sqrt(|O|) with h.p = rep.
-template <typename W>
-__global__ void k_mapping(const W* parent, long long n_parent, const W* reps, long long n_reps, GroupDev g,
+template <typename W, typename PW>
+__global__ void k_mapping(const PW* parent, long long n_parent, const W* reps, long long n_reps, int sb, GroupDev g,
                           const double2* phase, long long* index_out, double2* ampl_out) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_parent) return;
-    const W q = parent[i];
+    const W q = (W)parent[i];
     W rep = q;
     int gb = 0, stab = 1;
     if (g.kind == GK_TORUS) {
         W keep[64];
         for (int a = 0; a < g.L1; ++a) keep[a] = (W)g.keep[a];
-        canon_torus<W>(q, g.L1, g.L2, g.w, g.rowbits, g.nbits, (W)g.full, keep, rep, gb, stab);
+        canon_torus<W>(q, g.L1, g.L2, g.w, g.rowbits, g.nbits, (W)g.full, keep, true, true, rep, gb, stab);
     } else if (g.kind == GK_GENERIC) {
         rep = q; gb = 0; stab = 0;
         for (int e = 0; e < g.G; ++e) {
@@ -392,7 +394,7 @@ __global__ void k_mapping(const W* parent, long long n_parent, const W* reps, lo
             stab += (t == q);
         }
     }
-    const long long c = sorted_find<W>(reps, n_reps, rep);
+    const long long c = key_find<W>(reps, n_reps, rep, sb, nullptr);
     index_out[i] = c;
     double2 a = make_double2(0.0, 0.0);
     if (c >= 0) {
@@ -404,17 +406,17 @@ __global__ void k_mapping(const W* parent, long long n_parent, const W* reps, lo
 }
 
 template <typename W>
-__global__ void k_orbit_sizes(const W* reps, long long n, GroupDev g, int32_t* out) {
+__global__ void k_orbit_sizes(const W* reps, long long n, int sb, GroupDev g, int32_t* out) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const W q = reps[i];
+    const W q = reps[i] >> sb;
     int stab = 1;
     if (g.kind == GK_TORUS) {
         W keep[64];
         for (int a = 0; a < g.L1; ++a) keep[a] = (W)g.keep[a];
         W rep;
         int gb;
-        canon_torus<W>(q, g.L1, g.L2, g.w, g.rowbits, g.nbits, (W)g.full, keep, rep, gb, stab);
+        canon_torus<W>(q, g.L1, g.L2, g.w, g.rowbits, g.nbits, (W)g.full, keep, false, true, rep, gb, stab);
     } else if (g.kind == GK_GENERIC) {
         stab = 0;
         for (int e = 0; e < g.G; ++e) {
@@ -429,22 +431,79 @@ __global__ void k_orbit_sizes(const W* reps, long long n, GroupDev g, int32_t* o
 }
 
 template <typename W>
-__global__ void k_lookup(const W* keys, long long n, const unsigned long long* q, long long m, long long* out,
-                         unsigned long long wmask) {
+__global__ void k_lookup(const W* keys, long long n, int sb, const unsigned long long* q, long long m, long long* out,
+                         unsigned long long smax) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     const unsigned long long k = q[i];
-    out[i] = ((k & ~wmask) != 0ull) ? -1 : sorted_find<W>(keys, n, (W)k);
+    out[i] = (k > smax) ? -1 : key_find<W>(keys, n, (W)k, sb, nullptr);
 }
 
 template <typename W>
-__global__ void k_count_nnz(const W* keys, long long n, GroupDev g, int T, const unsigned long long* masks,
+__global__ void k_get_states(const W* keys, long long n, int sb, unsigned long long* out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (unsigned long long)(keys[i] >> sb);
+}
+
+// key = (state << sb) | index of the stabiliser size among the divisors of G
+template <typename W>
+__global__ void k_embed(W* keys, long long n, int sb, GroupDev g, const int32_t* divi) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const W q = keys[i];
+    int stab = 1;
+    if (g.kind == GK_TORUS) {
+        W keep[64];
+        for (int a = 0; a < g.L1; ++a) keep[a] = (W)g.keep[a];
+        W rep;
+        int gb;
+        canon_torus<W>(q, g.L1, g.L2, g.w, g.rowbits, g.nbits, (W)g.full, keep, false, true, rep, gb, stab);
+    } else if (g.kind == GK_GENERIC) {
+        stab = 0;
+        for (int e = 0; e < g.G; ++e) {
+            W t = 0;
+            const unsigned long long* L = g.lut + (size_t)e * g.nchunks * 16;
+            for (int c = 0; c < g.nchunks; ++c) t |= (W)L[c * 16 + (int)((q >> (4 * c)) & 15u)];
+            t ^= (W)g.flips[e];
+            stab += (t == q);
+        }
+    }
+    keys[i] = (W)((q << sb) | (W)divi[stab]);
+}
+
+// Search directory: start[b] = first index whose state lies in bucket >= b (bucket = state >> shift),
+// for b in [0, nb]; thread i fills the buckets between its predecessor's bucket and its own.
+template <typename W>
+__global__ void k_dir_fill(const W* keys, long long n, int sb, int shift, long long nb, unsigned long long* start) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n) return;
+    const long long bcur = (i < n) ? min((long long)((keys[i] >> sb) >> shift), nb) : nb;
+    const long long bprev = (i > 0) ? min((long long)((keys[i - 1] >> sb) >> shift), nb) : -1;
+    for (long long b = bprev + 1; b <= bcur; ++b) start[b] = (unsigned long long)i;
+}
+
+// dir[b] = start | count << 40; dir[nb] is the empty sentinel.  *maxcount receives the largest bucket.
+__global__ void k_dir_pack(const unsigned long long* start, long long nb, unsigned long long* dir,
+                           unsigned long long* maxcount) {
+    const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b > nb) return;
+    if (b == nb) {
+        dir[b] = 0ull;
+        return;
+    }
+    const unsigned long long cnt = start[b + 1] - start[b];
+    dir[b] = start[b] | (cnt << 40);
+    if (cnt > 1) atomicMax(maxcount, cnt);
+}
+
+template <typename W>
+__global__ void k_count_nnz(const W* keys, long long n, int sb, GroupDev g, int T, const unsigned long long* masks,
                             const unsigned long long* rows, const unsigned long long* flips,
                             unsigned long long* counts /* [0] targets, [1] found */) {
     const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long nt = 0, nf = 0;
     if (r < n) {
-        const W b = keys[r];
+        const W b = keys[r] >> sb;
         for (int t = 0; t < T; ++t) {
             if ((b & (W)masks[t]) != (W)rows[t]) continue;
             const W q = b ^ (W)flips[t];
@@ -454,7 +513,7 @@ __global__ void k_count_nnz(const W* keys, long long n, GroupDev g, int T, const
             if (g.kind == GK_TORUS) {
                 W keep[64];
                 for (int a = 0; a < g.L1; ++a) keep[a] = (W)g.keep[a];
-                canon_torus<W>(q, g.L1, g.L2, g.w, g.rowbits, g.nbits, (W)g.full, keep, rep, gb, stab);
+                canon_torus<W>(q, g.L1, g.L2, g.w, g.rowbits, g.nbits, (W)g.full, keep, false, false, rep, gb, stab);
             } else if (g.kind == GK_GENERIC) {
                 for (int e = 0; e < g.G; ++e) {
                     W tt = 0;
@@ -464,7 +523,7 @@ __global__ void k_count_nnz(const W* keys, long long n, GroupDev g, int T, const
                     if (tt < rep) rep = tt;
                 }
             }
-            nf += (sorted_find<W>(keys, n, rep) >= 0);
+            nf += (key_find<W>(keys, n, rep, sb, nullptr) >= 0);
         }
     }
     for (int d = 16; d > 0; d >>= 1) {
@@ -496,7 +555,7 @@ void count_nnz_t(const Space& s, int T, const uint64_t* masks, const uint64_t* r
     if (e == cudaSuccess && T > 0) e = cudaMemcpyAsync(df, flips, T * 8, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(dc, 0, 2 * sizeof(unsigned long long), st);
     if (e == cudaSuccess && s.dim > 0) {
-        k_count_nnz<W><<<(unsigned)((s.dim + 255) / 256), 256, 0, st>>>((const W*)s.d_keys, s.dim, gb.dev, T, dm, dr, df, dc);
+        k_count_nnz<W><<<(unsigned)((s.dim + 255) / 256), 256, 0, st>>>((const W*)s.d_keys, s.dim, s.sb, gb.dev, T, dm, dr, df, dc);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(h, dc, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
@@ -594,6 +653,7 @@ void GroupBuffers::release() {
 
 Space::~Space() {
     if (d_keys) cudaFree(d_keys);
+    if (d_dir) cudaFree(d_dir);
 }
 
 void enumerate_parent(Space& s, cudaStream_t st) {
@@ -627,8 +687,13 @@ void build_mapping_t(const Space& red, const Space& parent, int64_t* index_out, 
         EDGPU_CUDA(cudaMalloc(&d_idx, std::max<long long>(n, 1) * sizeof(long long)));
         EDGPU_CUDA(cudaMalloc(&d_amp, std::max<long long>(n, 1) * sizeof(double2)));
         if (n > 0) {
-            k_mapping<W><<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const W*)parent.d_keys, n, (const W*)red.d_keys,
-                                                                    red.dim, gb.dev, d_ph, d_idx, d_amp);
+            if (parent.w32)
+                k_mapping<W, unsigned><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+                    (const unsigned*)parent.d_keys, n, (const W*)red.d_keys, red.dim, red.sb, gb.dev, d_ph, d_idx, d_amp);
+            else
+                k_mapping<W, unsigned long long><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+                    (const unsigned long long*)parent.d_keys, n, (const W*)red.d_keys, red.dim, red.sb, gb.dev, d_ph,
+                    d_idx, d_amp);
             EDGPU_CUDA(cudaGetLastError());
             EDGPU_CUDA(cudaMemcpyAsync(index_out, d_idx, n * sizeof(long long), cudaMemcpyDeviceToHost, st));
             EDGPU_CUDA(cudaMemcpyAsync(ampl_out, d_amp, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
@@ -653,7 +718,7 @@ void orbit_sizes_t(const Space& red, int32_t* out_host, cudaStream_t st) {
     const long long n = red.dim;
     EDGPU_CUDA(cudaMalloc(&d, std::max<long long>(n, 1) * sizeof(int32_t)));
     if (n > 0) {
-        k_orbit_sizes<W><<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const W*)red.d_keys, n, gb.dev, d);
+        k_orbit_sizes<W><<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const W*)red.d_keys, n, red.sb, gb.dev, d);
         cudaError_t e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemcpyAsync(out_host, d, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -673,8 +738,8 @@ void lookup_t(const Space& s, const uint64_t* keys_host, int64_t n, int64_t* out
         EDGPU_CUDA(cudaMalloc(&dq, std::max<int64_t>(n, 1) * sizeof(unsigned long long)));
         EDGPU_CUDA(cudaMalloc(&dout, std::max<int64_t>(n, 1) * sizeof(long long)));
         EDGPU_CUDA(cudaMemcpyAsync(dq, keys_host, n * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
-        const unsigned long long wmask = sizeof(W) == 4 ? 0xffffffffull : ~0ull;
-        k_lookup<W><<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const W*)s.d_keys, s.dim, dq, n, dout, wmask);
+        const unsigned long long smax = (s.lay.nbits >= 64) ? ~0ull : ((1ull << s.lay.nbits) - 1ull);
+        k_lookup<W><<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const W*)s.d_keys, s.dim, s.sb, dq, n, dout, smax);
         EDGPU_CUDA(cudaGetLastError());
         EDGPU_CUDA(cudaMemcpyAsync(out_host, dout, n * sizeof(long long), cudaMemcpyDeviceToHost, st));
         EDGPU_CUDA(cudaStreamSynchronize(st));
@@ -711,5 +776,175 @@ void count_nnz(const Space& s, int T, const uint64_t* masks, const uint64_t* row
                int64_t* n_targets, int64_t* n_found, cudaStream_t st) {
     if (s.w32) count_nnz_t<uint32_t>(s, T, masks, rows, flips, n_targets, n_found, st);
     else count_nnz_t<unsigned long long>(s, T, masks, rows, flips, n_targets, n_found, st);
+}
+}  // namespace edgpu
+
+namespace edgpu {
+
+int orbit_index_bits(int G) {
+    int nd = 0;
+    for (int d = 1; d <= G; ++d) nd += (G % d == 0);
+    int b = 0;
+    while ((1 << b) < nd) ++b;
+    return b;
+}
+
+namespace {
+template <typename W>
+void embed_t(Space& red, cudaStream_t st) {
+    GroupBuffers gb;
+    gb.upload(red.group, red.lay);
+    std::vector<int32_t> divi(red.group.G + 1, 0);
+    int k = 0;
+    for (int d = 1; d <= red.group.G; ++d)
+        if (red.group.G % d == 0) divi[d] = k++;
+    int32_t* d_divi = nullptr;
+    EDGPU_CUDA(cudaMalloc(&d_divi, divi.size() * sizeof(int32_t)));
+    cudaError_t e = cudaMemcpy(d_divi, divi.data(), divi.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && red.dim > 0) {
+        k_embed<W><<<(unsigned)((red.dim + 255) / 256), 256, 0, st>>>((W*)red.d_keys, red.dim, red.sb, gb.dev, d_divi);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    }
+    cudaFree(d_divi);
+    if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("embed: ") + cudaGetErrorString(e));
+}
+
+template <typename W>
+void dir_t(Space& s, cudaStream_t st) {
+    const long long n = s.dim;
+    unsigned long long max_state = 0;
+    if (n > 0) {
+        W last;
+        EDGPU_CUDA(cudaMemcpy(&last, (const W*)s.d_keys + (n - 1), sizeof(W), cudaMemcpyDeviceToHost));
+        max_state = (unsigned long long)(last >> s.sb);
+    }
+    int bitlen = 0;
+    while (bitlen < 64 && (max_state >> bitlen) != 0ull) ++bitlen;
+    int nbits_n = 0;
+    while ((1ll << nbits_n) < std::max<long long>(n, 1)) ++nbits_n;
+    const size_t cap_bytes = std::max<size_t>((size_t)64 << 20, 2 * (size_t)n * sizeof(W));
+    int d = std::max(1, std::min(nbits_n, bitlen));
+    unsigned long long* start = nullptr;
+    unsigned long long* d_max = nullptr;
+    EDGPU_CUDA(cudaMalloc(&d_max, sizeof(unsigned long long)));
+    for (;;) {
+        const int shift = std::max(0, bitlen - d);
+        const long long nb = (bitlen == 0) ? 1 : ((long long)(max_state >> shift) + 1);
+        cudaFree(start);
+        start = nullptr;
+        if (s.d_dir) cudaFree(s.d_dir);
+        s.d_dir = nullptr;
+        cudaError_t e = cudaMalloc(&start, (nb + 1) * sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMalloc(&s.d_dir, (nb + 1) * sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMemsetAsync(d_max, 0, sizeof(unsigned long long), st);
+        if (e == cudaSuccess) {
+            k_dir_fill<W><<<(unsigned)((n + 1 + 255) / 256), 256, 0, st>>>((const W*)s.d_keys, n, s.sb, shift, nb, start);
+            k_dir_pack<<<(unsigned)((nb + 1 + 255) / 256), 256, 0, st>>>(start, nb, s.d_dir, d_max);
+            e = cudaGetLastError();
+        }
+        unsigned long long mx = 0;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&mx, d_max, sizeof(mx), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            cudaFree(start);
+            cudaFree(d_max);
+            throw Error(EDGPU_ERR_CUDA, std::string("search directory: ") + cudaGetErrorString(e));
+        }
+        const bool grow = mx > 8 && shift > 0 && (size_t)(2 * nb + 2) * sizeof(unsigned long long) <= cap_bytes;
+        if (!grow) {
+            s.dir_shift = shift;
+            s.dir_nb = nb;
+            int steps = 0;
+            while ((1ull << steps) < std::max<unsigned long long>(mx, 1ull)) ++steps;
+            s.dir_steps = steps;
+            break;
+        }
+        ++d;
+    }
+    cudaFree(start);
+    cudaFree(d_max);
+}
+
+template <typename W>
+void states_t(const Space& s, uint64_t* out_host, cudaStream_t st) {
+    unsigned long long* d = nullptr;
+    EDGPU_CUDA(cudaMalloc(&d, std::max<int64_t>(s.dim, 1) * 8));
+    k_get_states<W><<<(unsigned)((s.dim + 255) / 256), 256, 0, st>>>((const W*)s.d_keys, s.dim, s.sb, d);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out_host, d, s.dim * 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d);
+    if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("get_states: ") + cudaGetErrorString(e));
+}
+}  // namespace
+
+void embed_orbit_index(Space& red, cudaStream_t st) {
+    if (red.sb == 0 || red.dim == 0) return;
+    if (red.w32) embed_t<uint32_t>(red, st);
+    else embed_t<unsigned long long>(red, st);
+}
+
+void build_search_directory(Space& s, cudaStream_t st) {
+    if (s.w32) dir_t<uint32_t>(s, st);
+    else dir_t<unsigned long long>(s, st);
+}
+
+void get_states(const Space& s, uint64_t* out_host, cudaStream_t st) {
+    if (s.dim == 0) return;
+    if (s.w32) states_t<uint32_t>(s, out_host, st);
+    else states_t<unsigned long long>(s, out_host, st);
+}
+
+}  // namespace edgpu
+
+namespace edgpu {
+namespace {
+template <typename W>
+__global__ void k_diag(const W* keys, long long n, int sb, int T, const unsigned long long* masks,
+                       const unsigned long long* rows, const double2* amps, double2* out64, float2* out32) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const W b = keys[i] >> sb;
+    double2 e = make_double2(0.0, 0.0);
+    for (int t = 0; t < T; ++t)
+        if ((b & (W)masks[t]) == (W)rows[t]) {
+            e.x += amps[t].x;
+            e.y += amps[t].y;
+        }
+    if (out64) out64[i] = e;
+    if (out32) out32[i] = make_float2((float)e.x, (float)e.y);
+}
+
+template <typename W>
+void diag_t(const Space& s, int T, const uint64_t* masks, const uint64_t* rows, const double* amps, double* out64,
+            float* out32, cudaStream_t st) {
+    unsigned long long* d = nullptr;
+    const size_t Tm = std::max(T, 1);
+    EDGPU_CUDA(cudaMalloc(&d, Tm * (8 + 8 + 16)));
+    unsigned long long* dm = d;
+    unsigned long long* dr = d + Tm;
+    double2* da = (double2*)(d + 2 * Tm);
+    cudaError_t e = cudaSuccess;
+    if (T > 0) {
+        e = cudaMemcpyAsync(dm, masks, T * 8, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dr, rows, T * 8, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(da, amps, T * 16, cudaMemcpyHostToDevice, st);
+    }
+    if (e == cudaSuccess && s.dim > 0) {
+        k_diag<W><<<(unsigned)((s.dim + 255) / 256), 256, 0, st>>>((const W*)s.d_keys, s.dim, s.sb, T, dm, dr, da,
+                                                                  (double2*)out64, (float2*)out32);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d);
+    if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("diagonal: ") + cudaGetErrorString(e));
+}
+}  // namespace
+
+void compute_diagonal(const Space& s, int T, const uint64_t* masks, const uint64_t* rows, const double* amps,
+                      double* out64, float* out32, cudaStream_t st) {
+    if (s.w32) diag_t<uint32_t>(s, T, masks, rows, amps, out64, out32, st);
+    else diag_t<unsigned long long>(s, T, masks, rows, amps, out64, out32, st);
 }
 }  // namespace edgpu

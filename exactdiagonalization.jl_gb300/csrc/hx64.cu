@@ -4,11 +4,21 @@
 namespace edgpu {
 
 void hx_launch_w64(int gk, int prec, int mode, const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
-    EDGPU_HX_DISPATCH(unsigned long long, hx_launch_one, p, blocks, smem, st)
+    switch (gk * 4 + prec * 2 + mode) {
+        EDGPU_HX_CASES(unsigned long long, 0, hx_launch_one, p, blocks, smem, st)
+        EDGPU_HX_CASES(unsigned long long, 1, hx_launch_one, p, blocks, smem, st)
+        EDGPU_HX_CASES(unsigned long long, 2, hx_launch_one, p, blocks, smem, st)
+        default: throw Error(EDGPU_ERR_ARG, "bad product kernel selector");
+    }
 }
 
 int hx_occupancy_w64(int gk, int prec, int mode, size_t smem) {
-    EDGPU_HX_DISPATCH(unsigned long long, hx_occupancy_one, smem)
+    switch (gk * 4 + prec * 2 + mode) {
+        EDGPU_HX_CASES(unsigned long long, 0, hx_occupancy_one, smem)
+        EDGPU_HX_CASES(unsigned long long, 1, hx_occupancy_one, smem)
+        EDGPU_HX_CASES(unsigned long long, 2, hx_occupancy_one, smem)
+        default: throw Error(EDGPU_ERR_ARG, "bad product kernel selector");
+    }
 }
 
 int hx_warp_bytes(bool w32) {

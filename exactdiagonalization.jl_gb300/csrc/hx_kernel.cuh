@@ -4,16 +4,17 @@
 // :358-378) over get_row_iterator(::ReducedOperatorRepresentation) (reduced_operator_representation.jl:
 // 57-85) and get_row_iterator(::OperatorRepresentation) (operator_representation.jl:66-79).
 //
-// Work decomposition.  A warp owns a tile of up to 32 consecutive rows (basis words b_r).
-//  1. Each lane loads one row word, counts its stabiliser (orbit norm) and sums the diagonal terms
-//     (row == col projectors) into acc[r] = E(b_r) x[r].
+// Work decomposition.  A warp owns a tile of up to 32 consecutive rows (keys of representatives).
+//  1. Each lane loads one row key (state + orbit-size index) and the row's diagonal element E(b_r)
+//     (sum of the row == col projector terms, precomputed once per operator) into acc[r] = E x[r].
 //  2. The (row, off-diagonal term) pairs of the tile are scanned in row-major order, 32 per step; a
 //     match (b & mask == row) is compacted by warp ballot into a per-warp queue of targets
 //     q = b ^ (row ^ col), so the queue stays ordered by row.
-//  3. Whenever 32 targets are queued, every lane takes one: orbit minimum of q and the element h with
-//     h.q = rep (recomputed, never stored), branch-free search of rep in the sorted table, gather of
-//     x[c], element amp * chi(h) * sqrt(|O_r| / |O_c|), and a segmented warp scan by row that adds
-//     each row's partial sum into acc[r].  The summation order is fixed: results are deterministic.
+//  3. Whenever 64 targets are queued, every lane takes two: orbit minimum of q and the element h with
+//     h.q = rep (recomputed, never stored), bucketed branch-free search of rep (one directory load,
+//     then a few probes inside the bucket), gather of x[c], element amp * chi(h) * sqrt(|O_r| / |O_c|), and a segmented warp scan by
+//     row that adds each row's partial sum into acc[r].  The summation order is fixed: results are
+//     deterministic run to run.
 //  4. acc is written to y (coalesced); apply! semantics add the old y.
 // MODE 1 also accumulates dL/dJ_c = Re <gy | H_c x> per coupling c into per-block partial sums.
 #pragma once
@@ -65,9 +66,49 @@ __device__ __forceinline__ float2 shfl_up_v(float2 v, int d) {
     return make_float2(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d));
 }
 
+// One off-diagonal term record (mask, row, row^col) from shared memory in a single vector load.
+template <typename W>
+__device__ __forceinline__ void load_rec3(const W* r, W& m, W& row, W& f);
+template <>
+__device__ __forceinline__ void load_rec3<unsigned int>(const unsigned int* r, unsigned int& m, unsigned int& row,
+                                                        unsigned int& f) {
+    const uint4 v = *(const uint4*)r;
+    m = v.x;
+    row = v.y;
+    f = v.z;
+}
+template <>
+__device__ __forceinline__ void load_rec3<unsigned long long>(const unsigned long long* r, unsigned long long& m,
+                                                              unsigned long long& row, unsigned long long& f) {
+    const ulonglong2 a = *(const ulonglong2*)r;
+    m = a.x;
+    row = a.y;
+    f = r[2];
+}
+
 template <typename W>
 __host__ __device__ constexpr int hx_warp_bytes_t() {
     return HX_QCAP * (int)sizeof(W) + HX_QCAP * 4 + 32 * 16 + 32 * 4 + 32 * 16;
+}
+
+// Orbit minimum of q and the element reaching it, for each group kind.
+template <typename W, int GK>
+__device__ __forceinline__ void canon_rep(W q, const HxParams& p, const W* keep, const W* lut, const W* flips, W& rep,
+                                          int& g) {
+    if (GK == GK_TRIVIAL) {
+        rep = q;
+        g = 0;
+    } else if (GK == GK_RING) {
+        unsigned r;
+        canon_ring((unsigned)q, p.nbits, p.L1, p.w, p.pb, p.want_arg != 0, r, g);
+        rep = (W)r;
+    } else if (GK == GK_TORUS) {
+        int s;
+        canon_torus<W>(q, p.L1, p.L2, p.w, p.rowbits, p.nbits, (W)p.full, keep, p.want_arg != 0, false, rep, g, s);
+    } else {
+        int s;
+        canon_generic<W>(q, p.G, p.nchunks, lut, flips, false, rep, g, s);
+    }
 }
 
 template <typename W, int GK, int PREC, int MODE>
@@ -85,9 +126,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_kernel(const HxParams p) {
         for (int i = threadIdx.x; i < p.n_coupl; i += blockDim.x) sgrad[i] = 0.0;
     __syncthreads();
 
-    const W* om = (const W*)(sm + p.o_om);
-    const W* orw = (const W*)(sm + p.o_or);
-    const W* ofl = (const W*)(sm + p.o_of);
+    const W* orec = (const W*)(sm + p.o_om);   // off-diagonal term t: orec[4t] mask, [4t+1] row, [4t+2] row^col
     const V* oa = (const V*)(sm + p.o_oa);
     const V* ou = (const V*)(sm + p.o_ou);
     const int* oc = (const int*)(sm + p.o_oc);
@@ -98,7 +137,6 @@ __global__ void __launch_bounds__(HX_THREADS) hx_kernel(const HxParams p) {
     const int* dc = (const int*)(sm + p.o_dc);
     const V* ph = (const V*)(sm + p.o_ph);
     const int* num = (const int*)(sm + p.o_num);
-    const int* divi = (const int*)(sm + p.o_divi);
     const R* ratio = (const R*)(sm + p.o_ratio);
     const W* keep = (const W*)(sm + p.o_keep);
     const W* lut = (const W*)(sm + p.o_lut);
@@ -118,83 +156,110 @@ __global__ void __launch_bounds__(HX_THREADS) hx_kernel(const HxParams p) {
     const V* gy = (const V*)p.gy;
     const int RT = p.rows_per_tile;
     const long long n_tiles = (p.n_rows + RT - 1) / RT;
-    const W full = (W)p.full;
+    const int sb = p.sb;
+    const W smask = (W)((((W)1) << sb) - 1);
     const int T_o = p.T_o;
     const int inc_i = T_o ? 32 / T_o : 0, inc_j = T_o ? 32 % T_o : 0;
+    const bool want_arg = p.want_arg != 0;
 
     int head = 0;
-    // Process cnt queued targets, one per lane (see step 3 above).
+    // Process cnt (<= 64) queued targets (step 3 above): lane handles entries lane and lane + 32, whose
+    // searches and gathers overlap.  Each half of the batch is a row-ordered run of the queue.
     auto process = [&](int cnt) {
-        V contrib = czero<V>();
-        int myi = -1;
-        if (lane < cnt) {
-            const int pos = (head + lane) & (HX_QCAP - 1);
-            const W q = qs[pos];
-            const int info = qi[pos];
-            myi = info >> 16;
-            const int j = info & 0xffff;
-            W rep = q;
-            int g = 0, stab = 1;
-            if (GK == GK_TORUS) canon_torus<W>(q, p.L1, p.L2, p.w, p.rowbits, p.nbits, full, keep, rep, g, stab);
-            else if (GK == GK_GENERIC) canon_generic<W>(q, p.G, p.nchunks, lut, flips, rep, g, stab);
-            const long long c = sorted_find<W>(keys, p.n_rows, rep);
-            if (c >= 0) {
-                V coef = oa[j];
+        V contrib[2];
+        int myi[2], jj[2], g[2];
+        W q[2], rep[2], kc[2];
+        bool act[2];
+        long long c[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int e = lane + 32 * h;
+            contrib[h] = czero<V>();
+            act[h] = e < cnt;
+            myi[h] = -1;
+            jj[h] = 0;
+            q[h] = 0;
+            g[h] = 0;
+            if (act[h]) {
+                const int pos = (head + e) & (HX_QCAP - 1);
+                q[h] = qs[pos];
+                const int info = qi[pos];
+                myi[h] = info >> 16;
+                jj[h] = info & 0xffff;
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            rep[h] = q[h];
+            if (act[h]) canon_rep<W, GK>(q[h], p, keep, lut, flips, rep[h], g[h]);
+        }
+        key_find_dir2<W>(keys, p.dir, p.dir_shift, p.dir_nb, p.dir_steps, rep, act, sb, c, kc);
+        V xv[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) xv[h] = (c[h] >= 0) ? x[c[h]] : czero<V>();
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (c[h] >= 0) {
+                V coef = oa[jj[h]];
                 V phv = czero<V>();
                 R f = (R)1;
                 if (GK != GK_TRIVIAL) {
-                    phv = ph[num[g]];
-                    f = ratio[rdi[myi] * p.nd + divi[stab]];
-                    coef = cscale(cmul(coef, phv), f);
+                    f = ratio[rdi[myi[h]] * p.nd + (int)(kc[h] & smask)];
+                    if (want_arg) {
+                        phv = ph[num[g[h]]];
+                        coef = cmul(coef, phv);
+                    }
+                    coef = cscale(coef, f);
                 }
-                const V xv = x[c];
-                contrib = cmul(coef, xv);
+                contrib[h] = cmul(coef, xv[h]);
                 if (MODE) {
-                    V cu = ou[j];
-                    if (GK != GK_TRIVIAL) cu = cscale(cmul(cu, phv), f);
-                    const V t = cmul(cu, xv);
-                    const V gg = gyr[myi];
-                    atomicAdd(&sgrad[oc[j]], (double)gg.x * (double)t.x + (double)gg.y * (double)t.y);
+                    V cu = ou[jj[h]];
+                    if (GK != GK_TRIVIAL) {
+                        if (want_arg) cu = cmul(cu, phv);
+                        cu = cscale(cu, f);
+                    }
+                    const V t = cmul(cu, xv[h]);
+                    const V gg = gyr[myi[h]];
+                    atomicAdd(&sgrad[oc[jj[h]]], (double)gg.x * (double)t.x + (double)gg.y * (double)t.y);
                 }
             }
         }
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const V up = shfl_up_v(contrib, d);
-            const int iu = __shfl_up_sync(0xffffffffu, myi, d);
-            if (lane >= d && iu == myi) contrib = cadd(contrib, up);
+        for (int h = 0; h < 2; ++h) {
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const V up = shfl_up_v(contrib[h], d);
+                const int iu = __shfl_up_sync(0xffffffffu, myi[h], d);
+                if (lane >= d && iu == myi[h]) contrib[h] = cadd(contrib[h], up);
+            }
+            const int inext = __shfl_down_sync(0xffffffffu, myi[h], 1);
+            const int e = lane + 32 * h;
+            if (act[h] && (lane == 31 || e == cnt - 1 || inext != myi[h])) acc[myi[h]] = cadd(acc[myi[h]], contrib[h]);
+            __syncwarp();
         }
-        const int inext = __shfl_down_sync(0xffffffffu, myi, 1);
-        if (lane < cnt && (lane == cnt - 1 || inext != myi)) acc[myi] = cadd(acc[myi], contrib);
-        __syncwarp();
     };
 
     for (long long tile = (long long)blockIdx.x * wpb + warp; tile < n_tiles; tile += (long long)gridDim.x * wpb) {
         const long long row0 = tile * RT;
         const int nrows = (int)min((long long)RT, p.n_rows - row0);
         const bool rowact = lane < nrows;
-        const W b = rowact ? keys[row0 + lane] : (W)0;
+        const W kr = rowact ? keys[row0 + lane] : (W)0;
+        const W b = kr >> sb;
 
-        int stab_r = 1;
-        if (GK == GK_TORUS) {
-            W rp;
-            int gg;
-            canon_torus<W>(b, p.L1, p.L2, p.w, p.rowbits, p.nbits, full, keep, rp, gg, stab_r);
-        } else if (GK == GK_GENERIC) {
-            W rp;
-            int gg;
-            canon_generic<W>(b, p.G, p.nchunks, lut, flips, rp, gg, stab_r);
-        }
-
-        double2 e = make_double2(0.0, 0.0);
-        for (int t = 0; t < p.T_d; ++t)
-            if ((b & dm[t]) == dr[t]) {
-                e.x += da[t].x;
-                e.y += da[t].y;
-            }
         const V xr = rowact ? x[row0 + lane] : czero<V>();
-        acc[lane] = cmul(from_d2<V>(e), xr);
-        rdi[lane] = divi[stab_r];
+        if (MODE == 0) {
+            const V* dtab = (const V*)p.diag;
+            acc[lane] = rowact ? cmul(dtab[row0 + lane], xr) : czero<V>();
+        } else {
+            double2 e = make_double2(0.0, 0.0);
+            for (int t = 0; t < p.T_d; ++t)
+                if ((b & dm[t]) == dr[t]) {
+                    e.x += da[t].x;
+                    e.y += da[t].y;
+                }
+            acc[lane] = cmul(from_d2<V>(e), xr);
+        }
+        rdi[lane] = (int)(kr & smask);
         if (MODE) {
             const V gv = rowact ? gy[row0 + lane] : czero<V>();
             gyr[lane] = gv;
@@ -215,11 +280,13 @@ __global__ void __launch_bounds__(HX_THREADS) hx_kernel(const HxParams p) {
             for (int p0 = 0; p0 < total; p0 += 32) {
                 const bool act = (p0 + lane) < total;
                 const W bi = __shfl_sync(0xffffffffu, b, i & 31);
-                const bool m = act && ((bi & om[j]) == orw[j]);
+                W tm, tr, tf;
+                load_rec3<W>(orec + 4 * j, tm, tr, tf);
+                const bool m = act && ((bi & tm) == tr);
                 const unsigned bal = __ballot_sync(0xffffffffu, m);
                 if (m) {
                     const int pos = (tail + __popc(bal & lanemask_lt())) & (HX_QCAP - 1);
-                    qs[pos] = bi ^ ofl[j];
+                    qs[pos] = bi ^ tf;
                     qi[pos] = (i << 16) | j;
                 }
                 tail += __popc(bal);
@@ -229,15 +296,15 @@ __global__ void __launch_bounds__(HX_THREADS) hx_kernel(const HxParams p) {
                     j -= T_o;
                     ++i;
                 }
-                if (tail - head >= 32) {
+                if (tail - head >= 64) {
                     __syncwarp();
-                    process(32);
-                    head += 32;
+                    process(64);
+                    head += 64;
                 }
             }
             __syncwarp();
             while (tail > head) {
-                const int cnt = min(32, tail - head);
+                const int cnt = min(64, tail - head);
                 process(cnt);
                 head += cnt;
             }
@@ -260,7 +327,11 @@ __global__ void __launch_bounds__(HX_THREADS) hx_kernel(const HxParams p) {
 template <typename W, int GK, int PREC, int MODE>
 void hx_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
     auto kern = hx_kernel<W, GK, PREC, MODE>;
-    EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    static size_t smem_set = 0;   // the attribute is raised once per kernel, never inside a graph capture
+    if (smem > smem_set) {
+        EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        smem_set = smem;
+    }
     kern<<<blocks, HX_THREADS, smem, st>>>(p);
     EDGPU_CUDA(cudaGetLastError());
 }
@@ -274,21 +345,10 @@ int hx_occupancy_one(size_t smem) {
     return n;
 }
 
-#define EDGPU_HX_DISPATCH(W, FN, ...)                                                        \
-    switch (gk * 4 + prec * 2 + mode) {                                                      \
-        case 0: return FN<W, GK_TRIVIAL, 0, 0>(__VA_ARGS__);                                 \
-        case 1: return FN<W, GK_TRIVIAL, 0, 1>(__VA_ARGS__);                                 \
-        case 2: return FN<W, GK_TRIVIAL, 1, 0>(__VA_ARGS__);                                 \
-        case 3: return FN<W, GK_TRIVIAL, 1, 1>(__VA_ARGS__);                                 \
-        case 4: return FN<W, GK_TORUS, 0, 0>(__VA_ARGS__);                                   \
-        case 5: return FN<W, GK_TORUS, 0, 1>(__VA_ARGS__);                                   \
-        case 6: return FN<W, GK_TORUS, 1, 0>(__VA_ARGS__);                                   \
-        case 7: return FN<W, GK_TORUS, 1, 1>(__VA_ARGS__);                                   \
-        case 8: return FN<W, GK_GENERIC, 0, 0>(__VA_ARGS__);                                 \
-        case 9: return FN<W, GK_GENERIC, 0, 1>(__VA_ARGS__);                                 \
-        case 10: return FN<W, GK_GENERIC, 1, 0>(__VA_ARGS__);                                \
-        case 11: return FN<W, GK_GENERIC, 1, 1>(__VA_ARGS__);                                \
-        default: throw Error(EDGPU_ERR_ARG, "bad product kernel selector");                  \
-    }
+#define EDGPU_HX_CASES(W, GKV, FN, ...)                                                      \
+    case GKV * 4 + 0: return FN<W, GKV, 0, 0>(__VA_ARGS__);                                  \
+    case GKV * 4 + 1: return FN<W, GKV, 0, 1>(__VA_ARGS__);                                  \
+    case GKV * 4 + 2: return FN<W, GKV, 1, 0>(__VA_ARGS__);                                  \
+    case GKV * 4 + 3: return FN<W, GKV, 1, 1>(__VA_ARGS__);
 
 }  // namespace edgpu

@@ -8,7 +8,8 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libedgpu.so")
+# EDGPU_LIBRARY selects another build of the library (e.g. one with different tile constants).
+LIB_PATH = os.environ.get("EDGPU_LIBRARY") or os.path.join(HERE, "libedgpu.so")
 
 OK, ERR_ARG, ERR_DIM, ERR_BOUNDS, ERR_KEY, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_STATE = range(9)
 FP64, MIXED = 0, 1

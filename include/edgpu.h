@@ -21,6 +21,8 @@
  *   - Complex vectors are interleaved (re, im).  Host-buffer entry points take
  *     complex128 (ComplexF64).  Device-buffer entry points take complex128 for
  *     EDGPU_FP64 and complex64 for EDGPU_MIXED.
+ *   - Device-buffer entry points take a cudaStream_t as void* (NULL = the CUDA default stream) and
+ *     are asynchronous on it; host-buffer entry points return after the result is in host memory.
  *   - Handles are not thread-safe for concurrent calls on the same handle;
  *     distinct handles may be used from different threads.
  */
@@ -140,7 +142,7 @@ int edgpu_op_count_nnz(edgpu_op op, int64_t* n_targets, int64_t* nnz_off);
  * EDGPU_ERR_DIM when n != dimension. */
 int edgpu_mul(edgpu_op op, int32_t precision, const double* x, double* y, int64_t n, int32_t accumulate);
 /* The same on DEVICE vectors (complex128 for EDGPU_FP64, complex64 for EDGPU_MIXED) on a
- * caller stream (cudaStream_t, NULL = the library stream).  Asynchronous. */
+ * caller stream (cudaStream_t; NULL = the CUDA default stream).  Asynchronous. */
 int edgpu_mul_device(edgpu_op op, int32_t precision, const void* x, void* y, int64_t n, int32_t accumulate,
                      void* stream);
 /* apply!(out, state, opr): out += transpose(state) * opr (transpose product,
