@@ -484,6 +484,26 @@ std::vector<double> tridiag_eigvec(const std::vector<double>& a, const std::vect
 
 }  // namespace
 
+// Support for the entry point in noalloc.cu: expose already-built gradient tables and the error slot.
+namespace edgpu {
+bool coupling_grad_tables(edgpu_op oh, int prec, GradTables* out) {
+    edgpu_op_s* op = as_op(oh);
+    const Blob& B = op->blob[prec][0][1];
+    if (!B.ready) return false;
+    out->tmpl = B.tmpl;
+    out->smem = B.smem;
+    out->max_blocks = B.max_blocks;
+    out->gk = B.gk;
+    out->rows_per_tile = op->tuned_rows[prec] ? op->tuned_rows[prec] : B.rows_per_tile;
+    out->n_coupl = op->n_coupl;
+    out->w32 = op->space->w32;
+    out->dim = op->space->dim;
+    return true;
+}
+
+int record_api_error(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace edgpu
+
 // =================================================================================================
 extern "C" {
 

@@ -166,6 +166,20 @@ void hx_launch_w32(int gk, int prec, int mode, const HxParams& p, int blocks, si
 void hx_launch_w64(int gk, int prec, int mode, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
 int hx_max_blocks_per_sm(bool w32, int gk, int prec, int mode, size_t smem);
 
+// ---- the coupling-gradient launch for callers that cannot allocate (noalloc.cu) -----------------
+// Launch state of an operator's gradient-mode tables, read without building anything.
+struct GradTables {
+    HxParams tmpl;
+    size_t smem;
+    int max_blocks, gk, rows_per_tile, n_coupl;
+    bool w32;
+    long long dim;
+};
+// False when the tables for this precision have not been built yet (nothing is allocated here).
+bool coupling_grad_tables(edgpu_op op, int prec, GradTables* out);
+// Record an error message for edgpu_last_error() and return code.
+int record_api_error(int code, const std::string& msg);
+
 // ---- vector kernels (linalg.cu) ------------------------------------------------------------------
 void launch_random_c128(int64_t n, uint64_t seed, double* dst, cudaStream_t st);
 void launch_c128_to_c64(int64_t n, const double* src, float* dst, cudaStream_t st);

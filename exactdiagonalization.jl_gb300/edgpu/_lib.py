@@ -71,6 +71,7 @@ SIGNATURES = {
     "edgpu_mul_transpose": (ctypes.c_int, [vp, i32, P(dbl), P(dbl), i64, i32]),
     "edgpu_mul_adjoint_device": (ctypes.c_int, [vp, i32, vp, vp, i64, i32, vp]),
     "edgpu_coupling_grad_device": (ctypes.c_int, [vp, i32, vp, vp, vp, i64, P(dbl), vp]),
+    "edgpu_coupling_grad_device_noalloc": (ctypes.c_int, [vp, i32, vp, vp, vp, i64, P(dbl), vp]),
     "edgpu_batch_create": (ctypes.c_int, [i32, P(vp), P(vp)]),
     "edgpu_batch_mul_device": (ctypes.c_int, [vp, i32, P(vp), P(vp), i32, vp]),
     "edgpu_batch_destroy": (None, [vp]),

@@ -158,6 +158,19 @@ int edgpu_mul_adjoint_device(edgpu_op op, int32_t precision, const void* x, void
 int edgpu_coupling_grad_device(edgpu_op op, int32_t precision, const void* x, const void* gy, void* y,
                                int64_t n, double* grad_out, void* stream);
 
+/* The same fused product and coupling gradient for callers that cannot allocate device memory (their
+ * device memory is owned by another allocator, e.g. a Julia or PyTorch memory pool, or they keep
+ * allocation out of a time-step loop).  This entry point has no counterpart in the reference.  It
+ * allocates nothing: its scratch is a 2 MiB array inside the library (held on every GPU that loads
+ * the library), shared by all calls, so calls that overlap on the GPU race and must be serialised by
+ * the caller.  y is required.  Limit: n_couplings <= 131072 (2 doubles each in the scratch).  The operator's gradient tables must have
+ * been built by one earlier edgpu_coupling_grad_device call with the same precision (EDGPU_ERR_STATE
+ * otherwise).  The first call on a device looks up the scratch address (cudaGetSymbolAddress); make
+ * that first call before any stream capture.  grad_out: host memory; the call returns after it is
+ * written. */
+int edgpu_coupling_grad_device_noalloc(edgpu_op op, int32_t precision, const void* x, const void* gy, void* y,
+                                       int64_t n, double* grad_out, void* stream);
+
 /* ---- batched sectors --------------------------------------------------------------------- */
 /* Several operator representations (e.g. every momentum sector) applied in one persistent launch.
  * All ops must share the operator terms' shape (word width and group kind). */
