@@ -103,6 +103,8 @@ struct Blob {
     int max_blocks = 0;      // resident blocks for the whole GPU
     int rows_per_tile = 32;
     void* d_diag = nullptr;  // per-row diagonal element in the blob's precision (product mode)
+    size_t smem_rows = 0;    // shared memory of the row-per-lane kernel (no per-warp queues)
+    int max_blocks_rows = 0;
     ~Blob() {
         if (d) cudaFree(d);
         if (d_diag) cudaFree(d_diag);
@@ -204,6 +206,10 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     p.o_keep = alloc(keep.size() * wsz);
     p.o_lut = alloc(lut.size() * wsz);
     p.o_flip = alloc((g.kind == GK_GENERIC ? g.G : 0) * wsz);
+    // torus row table: smallest rotation of every row value and the rotation steps reaching it
+    const int rowbits = g.L1 * g.w;
+    const bool use_rlut = g.kind == GK_TORUS && g.L2 >= 2 && rowbits <= 10 && g.L1 <= 16;
+    p.o_rlut = use_rlut ? alloc(((size_t)1 << rowbits) * 4) : -1;
     const size_t blob_bytes = align16(off);
     std::vector<unsigned char> h(blob_bytes, 0);
     auto putw = [&](int o, size_t i, uint64_t v) {
@@ -272,6 +278,23 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
             else { float ff = (float)f; memcpy(&h[p.o_ratio + (i * nd + j) * 4], &ff, 4); }
         }
     for (size_t i = 0; i < keep.size(); ++i) putw(p.o_keep, i, keep[i]);
+    if (use_rlut) {
+        const uint32_t rmask = (1u << rowbits) - 1u;
+        for (uint32_t v = 0; v <= rmask; ++v) {
+            uint32_t best = 0xffffffffu, steps = 0;
+            for (int a = 0; a < g.L1; ++a) {
+                const int sh = a * g.w;
+                const uint32_t r = sh ? (((v << sh) | (v >> (rowbits - sh))) & rmask) : v;
+                if (r < best) {
+                    best = r;
+                    steps = 0;
+                }
+                if (r == best) steps |= 1u << a;
+            }
+            const uint32_t e = best | (steps << 16);
+            memcpy(&h[p.o_rlut + v * 4], &e, 4);
+        }
+    }
     for (size_t i = 0; i < lut.size(); ++i) putw(p.o_lut, i, lut[i]);
     if (g.kind == GK_GENERIC)
         for (int e = 0; e < g.G; ++e) putw(p.o_flip, e, e < (int)g.flips.size() ? g.flips[e] : 0ull);
@@ -333,6 +356,12 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     B.smem = tot;
     const int per_sm = std::max(1, hx_max_blocks_per_sm(w32, gk, prec, mode, tot));
     B.max_blocks = per_sm * std::max(1, g_sm_count);
+    if (!mode) {
+        B.smem_rows = std::max<size_t>(p.warp_base, 16);
+        const int per_sm_rows = std::max(1, w32 ? hx_rows_occupancy_w32(gk, prec, B.smem_rows)
+                                                : hx_rows_occupancy_w64(gk, prec, B.smem_rows));
+        B.max_blocks_rows = per_sm_rows * std::max(1, g_sm_count);
+    }
     B.ready = true;
 }
 
@@ -364,7 +393,25 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
         if (blocks_used) *blocks_used = 0;
         return;
     }
-    int rows = rows_override ? rows_override : (op->tuned_rows[prec] ? op->tuned_rows[prec] : B.rows_per_tile);
+    int rows = rows_override ? rows_override : (op->tuned_rows[prec] ? op->tuned_rows[prec] : (mode ? B.rows_per_tile : -1));
+    if (rows < 0 && mode == 0) {
+        // row-per-lane strategy: -lpr lanes per row, one warp per 32/lpr consecutive rows
+        p.lpr = -rows;
+        p.rows_per_tile = 32 / p.lpr;
+        p.x = x;
+        p.y = y;
+        p.gy = gy;
+        p.grad_partial = grad_partial;
+        p.accumulate = accumulate;
+        const long long warps = (p.n_rows + p.rows_per_tile - 1) / p.rows_per_tile;
+        const int blocks = (int)std::max<long long>(1, std::min<long long>((warps + HX_THREADS / 32 - 1) / (HX_THREADS / 32),
+                                                                          B.max_blocks_rows));
+        if (blocks_used) *blocks_used = blocks;
+        if (op->space->w32) hx_rows_launch_w32(B.gk, prec, p, blocks, B.smem_rows, st);
+        else hx_rows_launch_w64(B.gk, prec, p, blocks, B.smem_rows, st);
+        return;
+    }
+    if (rows < 0) rows = 32;
     p.rows_per_tile = rows;
     p.x = x;
     p.y = y;
@@ -494,7 +541,7 @@ bool coupling_grad_tables(edgpu_op oh, int prec, GradTables* out) {
     out->smem = B.smem;
     out->max_blocks = B.max_blocks;
     out->gk = B.gk;
-    out->rows_per_tile = op->tuned_rows[prec] ? op->tuned_rows[prec] : B.rows_per_tile;
+    out->rows_per_tile = op->tuned_rows[prec] > 0 ? op->tuned_rows[prec] : B.rows_per_tile;
     out->n_coupl = op->n_coupl;
     out->w32 = op->space->w32;
     out->dim = op->space->dim;
@@ -889,8 +936,9 @@ int edgpu_op_set_tiling(edgpu_op oh, int32_t precision, int32_t rows_per_tile) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
     check_prec(precision);
-    require(rows_per_tile == 0 || (rows_per_tile >= 1 && rows_per_tile <= 32 && (32 % rows_per_tile) == 0),
-            EDGPU_ERR_ARG, "rows_per_tile must be 0 (default) or a divisor of 32");
+    require(rows_per_tile == 0 || rows_per_tile == -1 || rows_per_tile == -2 || rows_per_tile == -4 ||
+                (rows_per_tile >= 1 && rows_per_tile <= 32 && (32 % rows_per_tile) == 0),
+            EDGPU_ERR_ARG, "rows_per_tile must be 0 (default), -1/-2/-4 (1, 2 or 4 lanes per row) or a divisor of 32");
     op->tuned_rows[precision] = rows_per_tile;
     API_END
 }
@@ -900,7 +948,7 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     edgpu_op_s* op = as_op(oh);
     check_prec(precision);
     const int64_t n = op->space->dim;
-    const int cands[] = {32, 16, 8};
+    const int cands[] = {-1, -2, -4, 32, 16};   // -k: k lanes per row; else rows per warp tile of the queued schedule
     int best = 32;
     double best_ms = 1e30;
     if (n > 0) {

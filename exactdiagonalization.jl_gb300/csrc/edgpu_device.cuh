@@ -49,6 +49,40 @@ __device__ __forceinline__ void canon_torus(W q, int L1, int L2, int w, int rowb
     }
 }
 
+// Torus canonicalisation with top-row pruning (rows of rowbits <= 10 bits).  The numerically smallest
+// translate has the smallest possible top row, M = min over rows j of the smallest rotation of row j,
+// so only translates T(a,b) whose top row (row j = L2-1-b rotated by a) equals M can be the
+// representative.  rlut[v] = smallest rotation of the row value v (low 16 bits) | the set of rotation
+// steps a reaching it (high 16 bits).  Exact: ties are broken by comparing the whole words.
+template <typename W>
+__device__ __forceinline__ void canon_torus_pruned(W q, int L1, int L2, int w, int rowbits, int nbits, W full,
+                                                   const W* keep, const unsigned* rlut, W& rep, int& gbest) {
+    const unsigned rmask = (1u << rowbits) - 1u;
+    unsigned M = 0xffffffffu;
+    for (int j = 0; j < L2; ++j) M = min(M, rlut[(unsigned)(q >> (j * rowbits)) & rmask] & 0xffffu);
+    rep = full;
+    gbest = 0;
+    bool first = true;
+    for (int j = 0; j < L2; ++j) {
+        const unsigned e = rlut[(unsigned)(q >> (j * rowbits)) & rmask];
+        if ((e & 0xffffu) != M) continue;
+        const int b = (L2 - 1 - j) % L2;
+        const int sh = b * rowbits;
+        const W rb = sh ? (W)(((q << sh) | (q >> (nbits - sh))) & full) : q;
+        unsigned am = e >> 16;
+        while (am) {
+            const int a = __ffs((int)am) - 1;
+            am &= am - 1u;
+            const W t = torus_row_rotate<W>(rb, a * w, keep[a], full, rowbits);
+            if (first || t < rep) {
+                rep = t;
+                gbest = a + L1 * b;
+                first = false;
+            }
+        }
+    }
+}
+
 // Ring (L2 == 1) of n <= 31 bits in 32-bit words: rotations by funnel shifts of the doubled word
 // d = q | q << n, since bits [n - s, 2n - s) of d are q rotated left by s.  With pb index bits
 // (n + pb <= 32) the element index rides in the low bits of each candidate, so a single unsigned

@@ -150,9 +150,10 @@ struct HxParams {
     long long dir_nb;
     int dir_shift, dir_steps;
     int o_ph, o_num, o_ratio, o_keep, o_lut, o_flip, o_grad;
+    int o_rlut;                               // torus row table for top-row pruning, -1 when absent
     int T_o, T_d, G, den, nd;
     int L1, L2, w, rowbits, nbits, nchunks;
-    int sb, pb, want_arg;
+    int sb, pb, want_arg, lpr;
     unsigned long long full;
     int warp_base;
 };
@@ -165,6 +166,11 @@ int hx_warp_bytes(bool w32);
 void hx_launch_w32(int gk, int prec, int mode, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
 void hx_launch_w64(int gk, int prec, int mode, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
 int hx_max_blocks_per_sm(bool w32, int gk, int prec, int mode, size_t smem);
+// Row-per-lane strategy (hx_rows.cuh), product mode only.
+void hx_rows_launch_w32(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
+void hx_rows_launch_w64(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
+int hx_rows_occupancy_w32(int gk, int prec, size_t smem);
+int hx_rows_occupancy_w64(int gk, int prec, size_t smem);
 
 // ---- the coupling-gradient launch for callers that cannot allocate (noalloc.cu) -----------------
 // Launch state of an operator's gradient-mode tables, read without building anything.

@@ -1,5 +1,6 @@
 // Product kernels for basis words of at most 31 bits (uint32 tables).
 #include "hx_kernel.cuh"
+#include "hx_rows.cuh"
 
 namespace edgpu {
 
@@ -19,6 +20,35 @@ int hx_occupancy_w32(int gk, int prec, int mode, size_t smem) {
         EDGPU_HX_CASES(unsigned int, 1, hx_occupancy_one, smem)
         EDGPU_HX_CASES(unsigned int, 2, hx_occupancy_one, smem)
         EDGPU_HX_CASES(unsigned int, 3, hx_occupancy_one, smem)
+        default: throw Error(EDGPU_ERR_ARG, "bad product kernel selector");
+    }
+}
+
+// Row-per-lane strategy (product mode only).
+void hx_rows_launch_w32(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
+    switch (gk * 2 + prec) {
+        case 0 * 2 + 0: return hx_rows_launch_one<unsigned int, 0, 0, 0>(p, blocks, smem, st);
+        case 0 * 2 + 1: return hx_rows_launch_one<unsigned int, 0, 1, 0>(p, blocks, smem, st);
+        case 1 * 2 + 0: return hx_rows_launch_one<unsigned int, 1, 0, 0>(p, blocks, smem, st);
+        case 1 * 2 + 1: return hx_rows_launch_one<unsigned int, 1, 1, 0>(p, blocks, smem, st);
+        case 2 * 2 + 0: return hx_rows_launch_one<unsigned int, 2, 0, 0>(p, blocks, smem, st);
+        case 2 * 2 + 1: return hx_rows_launch_one<unsigned int, 2, 1, 0>(p, blocks, smem, st);
+        case 3 * 2 + 0: return hx_rows_launch_one<unsigned int, 3, 0, 0>(p, blocks, smem, st);
+        case 3 * 2 + 1: return hx_rows_launch_one<unsigned int, 3, 1, 0>(p, blocks, smem, st);
+        default: throw Error(EDGPU_ERR_ARG, "bad product kernel selector");
+    }
+}
+
+int hx_rows_occupancy_w32(int gk, int prec, size_t smem) {
+    switch (gk * 2 + prec) {
+        case 0 * 2 + 0: return hx_rows_occupancy_one<unsigned int, 0, 0, 0>(smem);
+        case 0 * 2 + 1: return hx_rows_occupancy_one<unsigned int, 0, 1, 0>(smem);
+        case 1 * 2 + 0: return hx_rows_occupancy_one<unsigned int, 1, 0, 0>(smem);
+        case 1 * 2 + 1: return hx_rows_occupancy_one<unsigned int, 1, 1, 0>(smem);
+        case 2 * 2 + 0: return hx_rows_occupancy_one<unsigned int, 2, 0, 0>(smem);
+        case 2 * 2 + 1: return hx_rows_occupancy_one<unsigned int, 2, 1, 0>(smem);
+        case 3 * 2 + 0: return hx_rows_occupancy_one<unsigned int, 3, 0, 0>(smem);
+        case 3 * 2 + 1: return hx_rows_occupancy_one<unsigned int, 3, 1, 0>(smem);
         default: throw Error(EDGPU_ERR_ARG, "bad product kernel selector");
     }
 }

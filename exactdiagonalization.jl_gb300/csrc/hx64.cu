@@ -1,5 +1,6 @@
 // Product kernels for basis words of 32 to 63 bits (uint64 tables).
 #include "hx_kernel.cuh"
+#include "hx_rows.cuh"
 
 namespace edgpu {
 
@@ -28,6 +29,31 @@ int hx_warp_bytes(bool w32) {
 int hx_max_blocks_per_sm(bool w32, int gk, int prec, int mode, size_t smem) {
     int hx_occupancy_w32(int, int, int, size_t);
     return w32 ? hx_occupancy_w32(gk, prec, mode, smem) : hx_occupancy_w64(gk, prec, mode, smem);
+}
+
+// Row-per-lane strategy (product mode only).
+void hx_rows_launch_w64(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
+    switch (gk * 2 + prec) {
+        case 0 * 2 + 0: return hx_rows_launch_one<unsigned long long, 0, 0, 0>(p, blocks, smem, st);
+        case 0 * 2 + 1: return hx_rows_launch_one<unsigned long long, 0, 1, 0>(p, blocks, smem, st);
+        case 1 * 2 + 0: return hx_rows_launch_one<unsigned long long, 1, 0, 0>(p, blocks, smem, st);
+        case 1 * 2 + 1: return hx_rows_launch_one<unsigned long long, 1, 1, 0>(p, blocks, smem, st);
+        case 2 * 2 + 0: return hx_rows_launch_one<unsigned long long, 2, 0, 0>(p, blocks, smem, st);
+        case 2 * 2 + 1: return hx_rows_launch_one<unsigned long long, 2, 1, 0>(p, blocks, smem, st);
+        default: throw Error(EDGPU_ERR_ARG, "bad product kernel selector");
+    }
+}
+
+int hx_rows_occupancy_w64(int gk, int prec, size_t smem) {
+    switch (gk * 2 + prec) {
+        case 0 * 2 + 0: return hx_rows_occupancy_one<unsigned long long, 0, 0, 0>(smem);
+        case 0 * 2 + 1: return hx_rows_occupancy_one<unsigned long long, 0, 1, 0>(smem);
+        case 1 * 2 + 0: return hx_rows_occupancy_one<unsigned long long, 1, 0, 0>(smem);
+        case 1 * 2 + 1: return hx_rows_occupancy_one<unsigned long long, 1, 1, 0>(smem);
+        case 2 * 2 + 0: return hx_rows_occupancy_one<unsigned long long, 2, 0, 0>(smem);
+        case 2 * 2 + 1: return hx_rows_occupancy_one<unsigned long long, 2, 1, 0>(smem);
+        default: throw Error(EDGPU_ERR_ARG, "bad product kernel selector");
+    }
 }
 
 }  // namespace edgpu

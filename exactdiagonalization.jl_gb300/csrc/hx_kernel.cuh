@@ -65,6 +65,12 @@ __device__ __forceinline__ double2 shfl_up_v(double2 v, int d) {
 __device__ __forceinline__ float2 shfl_up_v(float2 v, int d) {
     return make_float2(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d));
 }
+__device__ __forceinline__ double2 shfl_xor_v(double2 v, int d) {
+    return make_double2(__shfl_xor_sync(0xffffffffu, v.x, d), __shfl_xor_sync(0xffffffffu, v.y, d));
+}
+__device__ __forceinline__ float2 shfl_xor_v(float2 v, int d) {
+    return make_float2(__shfl_xor_sync(0xffffffffu, v.x, d), __shfl_xor_sync(0xffffffffu, v.y, d));
+}
 
 // One off-diagonal term record (mask, row, row^col) from shared memory in a single vector load.
 template <typename W>
@@ -93,8 +99,8 @@ __host__ __device__ constexpr int hx_warp_bytes_t() {
 
 // Orbit minimum of q and the element reaching it, for each group kind.
 template <typename W, int GK>
-__device__ __forceinline__ void canon_rep(W q, const HxParams& p, const W* keep, const W* lut, const W* flips, W& rep,
-                                          int& g) {
+__device__ __forceinline__ void canon_rep(W q, const HxParams& p, const W* keep, const W* lut, const W* flips,
+                                          const unsigned* rlut, W& rep, int& g) {
     if (GK == GK_TRIVIAL) {
         rep = q;
         g = 0;
@@ -103,8 +109,12 @@ __device__ __forceinline__ void canon_rep(W q, const HxParams& p, const W* keep,
         canon_ring((unsigned)q, p.nbits, p.L1, p.w, p.pb, p.want_arg != 0, r, g);
         rep = (W)r;
     } else if (GK == GK_TORUS) {
-        int s;
-        canon_torus<W>(q, p.L1, p.L2, p.w, p.rowbits, p.nbits, (W)p.full, keep, p.want_arg != 0, false, rep, g, s);
+        if (p.o_rlut >= 0) {
+            canon_torus_pruned<W>(q, p.L1, p.L2, p.w, p.rowbits, p.nbits, (W)p.full, keep, rlut, rep, g);
+        } else {
+            int s;
+            canon_torus<W>(q, p.L1, p.L2, p.w, p.rowbits, p.nbits, (W)p.full, keep, p.want_arg != 0, false, rep, g, s);
+        }
     } else {
         int s;
         canon_generic<W>(q, p.G, p.nchunks, lut, flips, false, rep, g, s);
@@ -141,6 +151,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_kernel(const HxParams p) {
     const W* keep = (const W*)(sm + p.o_keep);
     const W* lut = (const W*)(sm + p.o_lut);
     const W* flips = (const W*)(sm + p.o_flip);
+    const unsigned* rlut = (const unsigned*)(sm + (p.o_rlut >= 0 ? p.o_rlut : 0));
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
     unsigned char* ws = sm + p.warp_base + warp * hx_warp_bytes_t<W>();
@@ -191,7 +202,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_kernel(const HxParams p) {
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             rep[h] = q[h];
-            if (act[h]) canon_rep<W, GK>(q[h], p, keep, lut, flips, rep[h], g[h]);
+            if (act[h]) canon_rep<W, GK>(q[h], p, keep, lut, flips, rlut, rep[h], g[h]);
         }
         key_find_dir2<W>(keys, p.dir, p.dir_shift, p.dir_nb, p.dir_steps, rep, act, sb, c, kc);
         V xv[2];

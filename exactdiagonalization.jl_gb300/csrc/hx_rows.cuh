@@ -1,0 +1,183 @@
+// Row-per-lane strategy of the matrix-free product y = H x (same result as hx_kernel, other schedule);
+// lpr = 1, 2 or 4 lanes may share a row, each taking every lpr-th term.
+//
+// Replaces the same reference loop as hx_kernel.cuh (apply_serial!/apply_parallel! over
+// get_row_iterator, abstract_operator_representation.jl:296-316, reduced_operator_representation.jl:
+// 57-85).  Every lane owns one row: it reads the row's key and diagonal element, tests its state
+// against the off-diagonal term records (broadcast shared-memory loads) into a bitmask of matching
+// terms, then walks its matches two at a time: orbit minimum and element of each target, the two
+// bucketed searches in lockstep, gathers, and accumulation in registers in term order (the order of
+// the reference's row iterator).  No queue and no cross-lane reduction: the warp runs as long as its
+// busiest row, which costs less than the bookkeeping when rows have similar numbers of targets.
+#pragma once
+
+#include "hx_kernel.cuh"
+
+namespace edgpu {
+
+template <typename W, int GK, int PREC, int MODE>
+__global__ void __launch_bounds__(HX_THREADS) hx_rows_kernel(const HxParams p) {
+    typedef typename Cx<PREC>::V V;
+    typedef typename Cx<PREC>::R R;
+    extern __shared__ __align__(16) unsigned char sm[];
+    {
+        const int4* src = (const int4*)p.blob;
+        int4* dst = (int4*)sm;
+        for (int i = threadIdx.x; i < p.blob_words16; i += blockDim.x) dst[i] = src[i];
+    }
+    double* sgrad = (double*)(sm + p.o_grad);
+    if (MODE)
+        for (int i = threadIdx.x; i < p.n_coupl; i += blockDim.x) sgrad[i] = 0.0;
+    __syncthreads();
+
+    const W* orec = (const W*)(sm + p.o_om);
+    const V* oa = (const V*)(sm + p.o_oa);
+    const V* ou = (const V*)(sm + p.o_ou);
+    const int* oc = (const int*)(sm + p.o_oc);
+    const W* dm = (const W*)(sm + p.o_dm);
+    const W* dr = (const W*)(sm + p.o_dr);
+    const double2* da = (const double2*)(sm + p.o_da);
+    const double2* du = (const double2*)(sm + p.o_du);
+    const int* dc = (const int*)(sm + p.o_dc);
+    const V* ph = (const V*)(sm + p.o_ph);
+    const int* num = (const int*)(sm + p.o_num);
+    const R* ratio = (const R*)(sm + p.o_ratio);
+    const W* keep = (const W*)(sm + p.o_keep);
+    const W* lut = (const W*)(sm + p.o_lut);
+    const W* flips = (const W*)(sm + p.o_flip);
+    const unsigned* rlut = (const unsigned*)(sm + (p.o_rlut >= 0 ? p.o_rlut : 0));
+
+    const W* __restrict__ keys = (const W*)p.keys;
+    const V* __restrict__ x = (const V*)p.x;
+    V* y = (V*)p.y;
+    const V* gy = (const V*)p.gy;
+    const int sb = p.sb;
+    const W smask = (W)((((W)1) << sb) - 1);
+    const int T_o = p.T_o;
+    const bool want_arg = p.want_arg != 0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    // lpr lanes share a row: lane sub = lane % lpr takes the terms t with t % lpr == sub
+    const int lpr = p.lpr, sub = lane & (lpr - 1), rpw = 32 / lpr;
+    const long long n_tiles = (p.n_rows + rpw - 1) / rpw;
+
+    for (long long tile = (long long)blockIdx.x * wpb + warp; tile < n_tiles; tile += (long long)gridDim.x * wpb) {
+        const long long row = tile * rpw + lane / lpr;
+        const bool act = row < p.n_rows;
+        const W kr = act ? keys[row] : (W)0;
+        const W b = kr >> sb;
+        const int ri = (int)(kr & smask);
+        const V xr = act ? x[row] : czero<V>();
+        V acc = czero<V>();
+        V gv = czero<V>();
+        if (MODE == 0) {
+            if (act && sub == 0) acc = cmul(((const V*)p.diag)[row], xr);
+        } else {
+            gv = act ? gy[row] : czero<V>();
+            double2 e = make_double2(0.0, 0.0);
+            if (act && sub == 0)
+                for (int t = 0; t < p.T_d; ++t)
+                    if ((b & dm[t]) == dr[t]) {
+                        e.x += da[t].x;
+                        e.y += da[t].y;
+                        const V cu = cmul(from_d2<V>(du[t]), xr);
+                        atomicAdd(&sgrad[dc[t]], (double)gv.x * (double)cu.x + (double)gv.y * (double)cu.y);
+                    }
+            acc = cmul(from_d2<V>(e), xr);
+        }
+        // this lane's terms: t = sub + lpr * k, in chunks of 64
+        const int my_terms = (T_o - sub + lpr - 1) / lpr;
+        for (int k0 = 0; k0 < my_terms; k0 += 64) {
+            const int kn = min(64, my_terms - k0);
+            unsigned long long mm = 0ull;
+            for (int k = 0; k < kn; ++k) {
+                W tm, tr, tf;
+                load_rec3<W>(orec + 4 * (sub + lpr * (k0 + k)), tm, tr, tf);
+                mm |= (unsigned long long)((b & tm) == tr) << k;
+            }
+            if (!act) mm = 0ull;
+            while (__any_sync(0xffffffffu, mm != 0ull)) {
+                int tt[2];
+                bool on[2];
+                W q[2], rep[2], kc[2];
+                int g[2];
+                long long c[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    on[h] = mm != 0ull;
+                    tt[h] = on[h] ? sub + lpr * (k0 + __ffsll((long long)mm) - 1) : 0;
+                    mm &= mm - 1ull;
+                    W tm, tr, tf;
+                    load_rec3<W>(orec + 4 * tt[h], tm, tr, tf);
+                    q[h] = b ^ tf;
+                    rep[h] = q[h];
+                    g[h] = 0;
+                    if (on[h]) canon_rep<W, GK>(q[h], p, keep, lut, flips, rlut, rep[h], g[h]);
+                }
+                key_find_dir2<W>(keys, p.dir, p.dir_shift, p.dir_nb, p.dir_steps, rep, on, sb, c, kc);
+                V xv[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) xv[h] = (c[h] >= 0) ? x[c[h]] : czero<V>();
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (c[h] >= 0) {
+                        V coef = oa[tt[h]];
+                        V phv = czero<V>();
+                        R f = (R)1;
+                        if (GK != GK_TRIVIAL) {
+                            f = ratio[ri * p.nd + (int)(kc[h] & smask)];
+                            if (want_arg) {
+                                phv = ph[num[g[h]]];
+                                coef = cmul(coef, phv);
+                            }
+                            coef = cscale(coef, f);
+                        }
+                        acc = cadd(acc, cmul(coef, xv[h]));
+                        if (MODE) {
+                            V cu = ou[tt[h]];
+                            if (GK != GK_TRIVIAL) {
+                                if (want_arg) cu = cmul(cu, phv);
+                                cu = cscale(cu, f);
+                            }
+                            const V t = cmul(cu, xv[h]);
+                            atomicAdd(&sgrad[oc[tt[h]]], (double)gv.x * (double)t.x + (double)gv.y * (double)t.y);
+                        }
+                    }
+                }
+            }
+        }
+        // partial sums of the row's lanes (fixed butterfly order)
+        for (int d = 1; d < lpr; d <<= 1) acc = cadd(acc, shfl_xor_v(acc, d));
+        if (act && sub == 0) {
+            if (p.accumulate) acc = cadd(acc, y[row]);
+            y[row] = acc;
+        }
+    }
+    if (MODE) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < p.n_coupl; i += blockDim.x)
+            p.grad_partial[(size_t)blockIdx.x * p.n_coupl + i] = sgrad[i];
+    }
+}
+
+template <typename W, int GK, int PREC, int MODE>
+void hx_rows_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
+    auto kern = hx_rows_kernel<W, GK, PREC, MODE>;
+    static size_t smem_set = 0;   // raised once per kernel, never inside a graph capture
+    if (smem > smem_set) {
+        EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        smem_set = smem;
+    }
+    kern<<<blocks, HX_THREADS, smem, st>>>(p);
+    EDGPU_CUDA(cudaGetLastError());
+}
+
+template <typename W, int GK, int PREC, int MODE>
+int hx_rows_occupancy_one(size_t smem) {
+    auto kern = hx_rows_kernel<W, GK, PREC, MODE>;
+    EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int n = 0;
+    EDGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, HX_THREADS, smem));
+    return n;
+}
+
+}  // namespace edgpu

@@ -126,10 +126,12 @@ int edgpu_op_create(edgpu_space s, int32_t n_terms, const uint64_t* masks, const
 int edgpu_op_set_couplings(edgpu_op op, const double* couplings, int32_t n_couplings);
 int edgpu_op_dim(edgpu_op op, int64_t* out);
 void edgpu_op_destroy(edgpu_op op);
-/* Tile shape of the product kernel: rows per warp tile (a divisor of 32; 0 = default 32). */
+/* Schedule of the product kernel: -1, -2 or -4 for 1, 2 or 4 lanes per row (0 = default, one lane
+ * per row), or the rows per warp tile of the queued schedule (a divisor of 32). */
 int edgpu_op_set_tiling(edgpu_op op, int32_t precision, int32_t rows_per_tile);
-/* In-library autotuner: times the product for each candidate tile shape on this operator and keeps
- * the fastest (rows_per_tile_out, best_ms_out nullable). */
+/* In-library autotuner: times the product for each candidate schedule (1, 2 or 4 lanes per row;
+ * queued with 32 or 16 rows per warp tile) on this operator and keeps the fastest
+ * (rows_per_tile_out: the schedule as in edgpu_op_set_tiling; best_ms_out nullable). */
 int edgpu_op_autotune(edgpu_op op, int32_t precision, int32_t* rows_per_tile_out, double* best_ms_out);
 /* Number of off-diagonal (row, term) matches over all rows, and how many of them land on a row of
  * the representation (the nonzero off-diagonal elements the row iterator yields with a valid column,

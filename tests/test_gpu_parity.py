@@ -231,15 +231,23 @@ def xxz_terms_both(E, n, bonds, jxy, jz):
     return H, O.heisenberg_terms(n, bonds, jxy, jz)
 
 
+SCHEDULES = (-1, -2, -4, 32, 8)   # 1, 2, 4 lanes per row; queued with 32 and 8 rows per warp tile
+
+
 def check_product(E, opr, space_oracle, terms, N, seed=11):
     x = O.complex_gaussian(N, seed)
     want = O.apply_rows(space_oracle, terms, x)
-    y = np.zeros(N, dtype=np.complex128)
-    E.mul_(y, opr, x, precision="fp64")
-    assert relerr(y, want) < FP64_TOL
-    y32 = np.zeros(N, dtype=np.complex128)
-    E.mul_(y32, opr, x, precision="mixed")
-    assert relerr(y32, want) < MIXED_TOL
+    for sched in SCHEDULES:
+        opr.set_tiling("fp64", sched)
+        opr.set_tiling("mixed", sched)
+        y = np.zeros(N, dtype=np.complex128)
+        E.mul_(y, opr, x, precision="fp64")
+        assert relerr(y, want) < FP64_TOL, sched
+        y32 = np.zeros(N, dtype=np.complex128)
+        E.mul_(y32, opr, x, precision="mixed")
+        assert relerr(y32, want) < MIXED_TOL, sched
+    opr.set_tiling("fp64", 0)
+    opr.set_tiling("mixed", 0)
     # apply! adds; mul! overwrites
     y2 = y.copy()
     E.apply_(y2, opr, x)
