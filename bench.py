@@ -286,6 +286,7 @@ def run_gpu(args, wl):
     space, opr, t_space = build_gpu_operator(wl)
     N = space.dimension
     n_targets, nnz = opr.count_nnz()
+    dir_stats = edgpu.search_stats(space)
     tune_mixed = opr.autotune("mixed")
     tune_fp64 = opr.autotune("fp64")
     stream = torch.cuda.current_stream()
@@ -394,7 +395,7 @@ def run_gpu(args, wl):
                        "nnz_off": nnz, "bytes_per_step": b_mixed, "l2": f"inputs cycled from a pool of {P_mixed} x/y "
                        f"pairs ({2 * P_mixed * N * s_c / 1e6:.0f} MB > 2x L2)", "parallelism": f"replicas x{world}",
                        "rows_per_tile": {"mixed": tune_mixed[0], "fp64": tune_fp64[0]},
-                       "setup_s": t_space},
+                       "setup_s": t_space, "search_directory": dir_stats},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_src},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps, "clocks": clk,

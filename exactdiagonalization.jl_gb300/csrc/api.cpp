@@ -338,11 +338,14 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     p.n_coupl = op->n_coupl;
     p.sb = s.sb;
     p.want_arg = g.den > 1 ? 1 : 0;
-    p.dir = s.d_dir;
+    p.ds.dir = s.d_dir;
+    p.ds.nb = s.dir_nb;
+    p.ds.shift = s.dir_shift;
+    p.ds.mb = s.dir_shift + s.sb;
+    p.ds.K = s.dir_K;
+    p.ds.steps = s.dir_steps;
+    p.ds.sb = s.sb;
     p.diag = B.d_diag;
-    p.dir_shift = s.dir_shift;
-    p.dir_nb = s.dir_nb;
-    p.dir_steps = s.dir_steps;
     int gk = g.kind;
     p.pb = 0;
     if (gk == GK_TORUS && g.L2 == 1 && w32 && s.lay.nbits <= 31) {
@@ -721,6 +724,19 @@ int edgpu_space_lookup(edgpu_space sh, const uint64_t* keys, int64_t n, int64_t*
 }
 
 void edgpu_space_destroy(edgpu_space s) { delete static_cast<edgpu_space_s*>(s); }
+
+int edgpu_space_search_stats(edgpu_space sh, int64_t* buckets, int32_t* shift, int32_t* inline_keys_per_bucket,
+                             int32_t* window_steps, double* inline_fraction) {
+    API_BEGIN
+    edgpu_space_s* s = as_space(sh);
+    require(s->d_dir != nullptr || s->dim == 0, EDGPU_ERR_STATE, "no search directory (lazy or empty space)");
+    if (buckets) *buckets = s->dir_nb;
+    if (shift) *shift = s->dir_shift;
+    if (inline_keys_per_bucket) *inline_keys_per_bucket = s->dir_K;
+    if (window_steps) *window_steps = s->dir_steps;
+    if (inline_fraction) *inline_fraction = s->dir_inline;
+    API_END
+}
 
 int edgpu_reduce(edgpu_space parent_h, int32_t n_elems, const int32_t* site_maps, const uint64_t* flip_masks,
                  const int32_t* char_num, int32_t char_den, edgpu_space* out) {

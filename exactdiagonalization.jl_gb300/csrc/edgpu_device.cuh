@@ -239,65 +239,65 @@ __device__ __forceinline__ long long key_find(const W* __restrict__ keys, long l
     return (n > 0 && (k >> sb) == rep) ? lo : -1;
 }
 
-// Bucketed branch-free search.  dir[b] = start | (count << 40) of the keys whose state lies in
-// [b << shift, (b + 1) << shift); b is clamped to nb (an empty sentinel bucket).  The window search
-// runs `steps` = ceil(log2(max bucket)) halvings, so one directory load and a few probes inside one
-// or two cache sectors replace the ~log2(n) dependent probes of a plain binary search.
+// Bucketed branch-free search with bucket summaries.  The table of keys is split into buckets by
+// state >> shift; dir[b] summarises bucket b in one 64-bit word:
+//     bits  0..31  index of the bucket's first key (start)
+//     bits 32..35  number of keys in the bucket, saturated at 15
+//     bits 36..63  the low mb = shift + sb bits of each key of the bucket, K of them (K*mb <= 28)
+// A bucket with at most K keys is answered from its summary alone; a larger one by a branch-free
+// window search of `steps` halvings in the sorted keys between start and the next bucket's start.
+// dir[nb] is a sentinel (start = n, count 0); buckets past the last key clamp to it.
 template <typename W>
-__device__ __forceinline__ long long key_find_dir(const W* __restrict__ keys, const unsigned long long* __restrict__ dir,
-                                                  int shift, long long nb, int steps, W rep, int sb, W* key_out) {
-    const long long b = min((long long)(rep >> shift), nb);
-    const unsigned long long e = __ldg(dir + b);
-    long long lo = (long long)(e & 0xffffffffffull);
-    int len = (int)(e >> 40);
-    *key_out = (W)0;
-    if (len == 0) return -1;
-    const W target = (W)((rep << sb) | (W)((((W)1) << sb) - 1));
-    for (int k = 0; k < steps; ++k) {
-        const int half = len >> 1;
-        if (half > 0) {
-            lo = (ldg_w(keys + lo + half) <= target) ? lo + half : lo;
-            len -= half;
-        }
-    }
-    const W kk = ldg_w(keys + lo);
-    *key_out = kk;
-    return ((kk >> sb) == rep) ? lo : -1;
-}
-
-// Two independent bucketed searches run in lockstep, so their loads overlap (memory-level
-// parallelism of 2 per lane).  act[h] == false skips target h; c[h] = index or -1.
-template <typename W>
-__device__ __forceinline__ void key_find_dir2(const W* __restrict__ keys, const unsigned long long* __restrict__ dir,
-                                              int shift, long long nb, int steps, const W* rep, const bool* act, int sb,
-                                              long long* c, W* key_out) {
-    long long lo[2];
-    int len[2];
-    W target[2];
+__device__ __forceinline__ void key_find_sum2(const W* __restrict__ keys, const DirSearch& d, const W* rep,
+                                              const bool* act, long long* c, int* sidx) {
+    const unsigned mbmask = (d.mb >= 32) ? 0xffffffffu : ((1u << d.mb) - 1u);
+    const unsigned smask = (1u << d.sb) - 1u;
+    unsigned long long e[2];
+    unsigned bk[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-        const unsigned long long e = act[h] ? __ldg(dir + min((long long)(rep[h] >> shift), nb)) : 0ull;
-        lo[h] = (long long)(e & 0xffffffffffull);
-        len[h] = (int)(e >> 40);
-        target[h] = (W)((rep[h] << sb) | (W)((((W)1) << sb) - 1));
+        const unsigned long long b = (unsigned long long)(rep[h] >> d.shift);
+        bk[h] = (unsigned)min(b, (unsigned long long)d.nb);
+        e[h] = act[h] ? __ldg(d.dir + bk[h]) : 0ull;
     }
-    const bool valid0 = len[0] > 0, valid1 = len[1] > 0;
-    for (int k = 0; k < steps; ++k) {
+    bool slow[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const unsigned start = (unsigned)e[h];
+        const unsigned hi = (unsigned)(e[h] >> 32);
+        const int cnt = (int)(hi & 15u);
+        const unsigned field = hi >> 4;                                   // K members of mb bits
+        const unsigned want = ((unsigned)rep[h] & ((1u << d.shift) - 1u)) << d.sb;   // member bits without sidx
+        unsigned hits = 0u;
+        for (int k = 0; k < d.K; ++k) hits |= (((field >> (k * d.mb)) & mbmask & ~smask) == want ? 1u : 0u) << k;
+        hits &= (1u << cnt) - 1u;                                         // only the bucket's members
+        slow[h] = act[h] && cnt > d.K;
+        const int k0 = __ffs((int)hits) - 1;
+        const bool found = act[h] && !slow[h] && hits != 0u;
+        c[h] = found ? (long long)(start + (unsigned)k0) : -1;
+        sidx[h] = found ? (int)((field >> (k0 * d.mb)) & smask) : 0;
+    }
+    if (slow[0] || slow[1]) {   // buckets larger than K: search the keys
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-            const int half = len[h] >> 1;
-            if (half > 0) {
-                lo[h] = (ldg_w(keys + lo[h] + half) <= target[h]) ? lo[h] + half : lo[h];
-                len[h] -= half;
+            if (!slow[h]) continue;
+            unsigned lo = (unsigned)e[h];
+            int len = (int)((unsigned)__ldg(d.dir + bk[h] + 1) - lo);
+            const W target = (W)((rep[h] << d.sb) | (W)smask);
+            for (int k = 0; k < d.steps; ++k) {
+                const int half = len >> 1;
+                if (half > 0) {
+                    lo = (ldg_w(keys + lo + half) <= target) ? lo + half : lo;
+                    len -= half;
+                }
+            }
+            const W kk = ldg_w(keys + lo);
+            if ((kk >> d.sb) == rep[h]) {
+                c[h] = lo;
+                sidx[h] = (int)(kk & (W)smask);
             }
         }
     }
-    const W k0 = valid0 ? ldg_w(keys + lo[0]) : (W)0;
-    const W k1 = valid1 ? ldg_w(keys + lo[1]) : (W)0;
-    key_out[0] = k0;
-    key_out[1] = k1;
-    c[0] = (valid0 && (k0 >> sb) == rep[0]) ? lo[0] : -1;
-    c[1] = (valid1 && (k1 >> sb) == rep[1]) ? lo[1] : -1;
 }
 
 __device__ __forceinline__ unsigned lanemask_lt() {

@@ -64,10 +64,12 @@ struct Space {
     bool w32 = false;                // keys are uint32 (nbits + sb <= 32) else uint64
     int sb = 0;                      // low key bits holding the orbit-size index (0: unreduced)
     void* d_keys = nullptr;          // sorted keys: (state << sb) | orbit-size index
-    unsigned long long* d_dir = nullptr;   // search directory: start | count << 40 per bucket of states
+    unsigned long long* d_dir = nullptr;   // search directory of bucket summaries (see DirSearch)
     int dir_shift = 0;               // bucket of a state = state >> dir_shift
-    long long dir_nb = 0;            // number of buckets (entry dir_nb is an empty sentinel)
-    int dir_steps = 0;               // ceil(log2(largest bucket))
+    long long dir_nb = 0;            // number of buckets (entry dir_nb is a sentinel)
+    int dir_steps = 0;               // ceil(log2(largest bucket)) for buckets searched in the keys
+    int dir_K = 0;                   // keys summarised inline per bucket
+    double dir_inline = 0.0;         // fraction of keys in buckets answered by their summary
     ~Space();
 };
 
@@ -132,6 +134,13 @@ void compute_diagonal(const Space& s, int T, const uint64_t* masks, const uint64
 void count_nnz(const Space& s, int T, const uint64_t* masks, const uint64_t* rows, const uint64_t* flips,
                int64_t* n_targets, int64_t* n_found, cudaStream_t st);
 
+// Search directory of a key table (bucket summaries; see key_find_sum2 in edgpu_device.cuh).
+struct DirSearch {
+    const unsigned long long* dir;
+    long long nb;
+    int shift, mb, K, steps, sb;
+};
+
 // ---- matrix-free product (hx*.cu) ----------------------------------------------------------------
 struct HxParams {
     const void* keys;
@@ -145,10 +154,8 @@ struct HxParams {
     int blob_words16;
     int o_om, o_or, o_of, o_oa, o_ou, o_oc;   // off-diagonal terms: mask,row,flip,amp,unit amp,coupling id
     int o_dm, o_dr, o_da, o_du, o_dc;         // diagonal terms
-    const unsigned long long* dir;
+    DirSearch ds;                             // the search directory of the table
     const void* diag;                         // per-row diagonal element (V), product mode
-    long long dir_nb;
-    int dir_shift, dir_steps;
     int o_ph, o_num, o_ratio, o_keep, o_lut, o_flip, o_grad;
     int o_rlut;                               // torus row table for top-row pruning, -1 when absent
     int T_o, T_d, G, den, nd;

@@ -482,17 +482,26 @@ __global__ void k_dir_fill(const W* keys, long long n, int sb, int shift, long l
     for (long long b = bprev + 1; b <= bcur; ++b) start[b] = (unsigned long long)i;
 }
 
-// dir[b] = start | count << 40; dir[nb] is the empty sentinel.  *maxcount receives the largest bucket.
-__global__ void k_dir_pack(const unsigned long long* start, long long nb, unsigned long long* dir,
-                           unsigned long long* maxcount) {
+// dir[b] = start | min(count, 15) << 32 | the low mb bits of each key << (36 + k*mb) when the bucket
+// holds at most K keys; dir[nb] is the sentinel (start = n).  *maxcount receives the largest bucket and
+// *inline_keys the number of keys in buckets answered by their summary.
+template <typename W>
+__global__ void k_dir_pack(const W* keys, const unsigned long long* start, long long nb, long long n, int mb, int K,
+                           unsigned long long* dir, unsigned long long* maxcount, unsigned long long* inline_keys) {
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b > nb) return;
     if (b == nb) {
-        dir[b] = 0ull;
+        dir[b] = (unsigned long long)n;
         return;
     }
-    const unsigned long long cnt = start[b + 1] - start[b];
-    dir[b] = start[b] | (cnt << 40);
+    const unsigned long long st = start[b], cnt = start[b + 1] - st;
+    unsigned long long e = st | (min(cnt, 15ull) << 32);
+    if ((long long)cnt <= K) {
+        const unsigned long long mbmask = (mb >= 64) ? ~0ull : ((1ull << mb) - 1ull);
+        for (int k = 0; k < (int)cnt; ++k) e |= ((unsigned long long)keys[st + k] & mbmask) << (36 + k * mb);
+        if (cnt) atomicAdd(inline_keys, cnt);
+    }
+    dir[b] = e;
     if (cnt > 1) atomicMax(maxcount, cnt);
 }
 
@@ -813,6 +822,7 @@ void embed_t(Space& red, cudaStream_t st) {
 template <typename W>
 void dir_t(Space& s, cudaStream_t st) {
     const long long n = s.dim;
+    if (n >= (1ll << 32)) throw Error(EDGPU_ERR_ARG, "tables of 2^32 or more rows are not supported");
     unsigned long long max_state = 0;
     if (n > 0) {
         W last;
@@ -823,47 +833,55 @@ void dir_t(Space& s, cudaStream_t st) {
     while (bitlen < 64 && (max_state >> bitlen) != 0ull) ++bitlen;
     int nbits_n = 0;
     while ((1ll << nbits_n) < std::max<long long>(n, 1)) ++nbits_n;
-    const size_t cap_bytes = std::max<size_t>((size_t)64 << 20, 2 * (size_t)n * sizeof(W));
+    // the directory may use up to 16x the key table (HBM is plentiful; a clustered table needs small
+    // buckets before most of them fit inline)
+    const size_t cap_bytes = std::max<size_t>((size_t)512 << 20, 16 * (size_t)n * sizeof(W));
     int d = std::max(1, std::min(nbits_n, bitlen));
     unsigned long long* start = nullptr;
-    unsigned long long* d_max = nullptr;
-    EDGPU_CUDA(cudaMalloc(&d_max, sizeof(unsigned long long)));
+    unsigned long long* d_stats = nullptr;   // [0] largest bucket, [1] keys answered inline
+    EDGPU_CUDA(cudaMalloc(&d_stats, 2 * sizeof(unsigned long long)));
     for (;;) {
         const int shift = std::max(0, bitlen - d);
         const long long nb = (bitlen == 0) ? 1 : ((long long)(max_state >> shift) + 1);
+        const int mb = shift + s.sb;
+        const int K = mb == 0 ? 4 : std::min(4, 28 / mb);
         cudaFree(start);
         start = nullptr;
         if (s.d_dir) cudaFree(s.d_dir);
         s.d_dir = nullptr;
         cudaError_t e = cudaMalloc(&start, (nb + 1) * sizeof(unsigned long long));
         if (e == cudaSuccess) e = cudaMalloc(&s.d_dir, (nb + 1) * sizeof(unsigned long long));
-        if (e == cudaSuccess) e = cudaMemsetAsync(d_max, 0, sizeof(unsigned long long), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(d_stats, 0, 2 * sizeof(unsigned long long), st);
         if (e == cudaSuccess) {
             k_dir_fill<W><<<(unsigned)((n + 1 + 255) / 256), 256, 0, st>>>((const W*)s.d_keys, n, s.sb, shift, nb, start);
-            k_dir_pack<<<(unsigned)((nb + 1 + 255) / 256), 256, 0, st>>>(start, nb, s.d_dir, d_max);
+            k_dir_pack<W><<<(unsigned)((nb + 1 + 255) / 256), 256, 0, st>>>((const W*)s.d_keys, start, nb, n, mb, K,
+                                                                           s.d_dir, d_stats, d_stats + 1);
             e = cudaGetLastError();
         }
-        unsigned long long mx = 0;
-        if (e == cudaSuccess) e = cudaMemcpyAsync(&mx, d_max, sizeof(mx), cudaMemcpyDeviceToHost, st);
+        unsigned long long hs[2] = {0, 0};
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hs, d_stats, sizeof(hs), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) {
             cudaFree(start);
-            cudaFree(d_max);
+            cudaFree(d_stats);
             throw Error(EDGPU_ERR_CUDA, std::string("search directory: ") + cudaGetErrorString(e));
         }
-        const bool grow = mx > 8 && shift > 0 && (size_t)(2 * nb + 2) * sizeof(unsigned long long) <= cap_bytes;
+        const double frac = n > 0 ? (double)hs[1] / (double)n : 1.0;
+        const bool grow = frac < 0.98 && shift > 0 && (size_t)(2 * nb + 2) * sizeof(unsigned long long) <= cap_bytes;
         if (!grow) {
             s.dir_shift = shift;
             s.dir_nb = nb;
+            s.dir_K = K;
+            s.dir_inline = frac;
             int steps = 0;
-            while ((1ull << steps) < std::max<unsigned long long>(mx, 1ull)) ++steps;
+            while ((1ull << steps) < std::max<unsigned long long>(hs[0], 1ull)) ++steps;
             s.dir_steps = steps;
             break;
         }
         ++d;
     }
     cudaFree(start);
-    cudaFree(d_max);
+    cudaFree(d_stats);
 }
 
 template <typename W>

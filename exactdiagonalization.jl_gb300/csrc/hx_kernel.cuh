@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_kernel(const HxParams p) {
     auto process = [&](int cnt) {
         V contrib[2];
         int myi[2], jj[2], g[2];
-        W q[2], rep[2], kc[2];
+        W q[2], rep[2];
         bool act[2];
         long long c[2];
 #pragma unroll
@@ -204,7 +204,8 @@ __global__ void __launch_bounds__(HX_THREADS) hx_kernel(const HxParams p) {
             rep[h] = q[h];
             if (act[h]) canon_rep<W, GK>(q[h], p, keep, lut, flips, rlut, rep[h], g[h]);
         }
-        key_find_dir2<W>(keys, p.dir, p.dir_shift, p.dir_nb, p.dir_steps, rep, act, sb, c, kc);
+        int sx[2];
+        key_find_sum2<W>(keys, p.ds, rep, act, c, sx);
         V xv[2];
 #pragma unroll
         for (int h = 0; h < 2; ++h) xv[h] = (c[h] >= 0) ? x[c[h]] : czero<V>();
@@ -215,7 +216,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_kernel(const HxParams p) {
                 V phv = czero<V>();
                 R f = (R)1;
                 if (GK != GK_TRIVIAL) {
-                    f = ratio[rdi[myi[h]] * p.nd + (int)(kc[h] & smask)];
+                    f = ratio[rdi[myi[h]] * p.nd + sx[h]];
                     if (want_arg) {
                         phv = ph[num[g[h]]];
                         coef = cmul(coef, phv);

@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_rows_kernel(const HxParams p) {
             while (__any_sync(0xffffffffu, mm != 0ull)) {
                 int tt[2];
                 bool on[2];
-                W q[2], rep[2], kc[2];
+                W q[2], rep[2];
                 int g[2];
                 long long c[2];
 #pragma unroll
@@ -113,7 +113,8 @@ __global__ void __launch_bounds__(HX_THREADS) hx_rows_kernel(const HxParams p) {
                     g[h] = 0;
                     if (on[h]) canon_rep<W, GK>(q[h], p, keep, lut, flips, rlut, rep[h], g[h]);
                 }
-                key_find_dir2<W>(keys, p.dir, p.dir_shift, p.dir_nb, p.dir_steps, rep, on, sb, c, kc);
+                int sx[2];
+                key_find_sum2<W>(keys, p.ds, rep, on, c, sx);
                 V xv[2];
 #pragma unroll
                 for (int h = 0; h < 2; ++h) xv[h] = (c[h] >= 0) ? x[c[h]] : czero<V>();
@@ -124,7 +125,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_rows_kernel(const HxParams p) {
                         V phv = czero<V>();
                         R f = (R)1;
                         if (GK != GK_TRIVIAL) {
-                            f = ratio[ri * p.nd + (int)(kc[h] & smask)];
+                            f = ratio[ri * p.nd + sx[h]];
                             if (want_arg) {
                                 phv = ph[num[g[h]]];
                                 coef = cmul(coef, phv);

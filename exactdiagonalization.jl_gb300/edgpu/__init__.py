@@ -11,7 +11,7 @@ from .operators import (NullOperator, PureOperator, SumOperator, pauli_matrix, p
                         spin_half_system, term_arrays)
 from .representation import (Batch, DirectProductOperation, GlobalBitFlip, HilbertSpaceRepresentation,
                              OperatorRepresentation, ReducedHilbertSpaceRepresentation, SitePermutation,
-                             apply_, coupling_grad, dimension, mul_, mul_adjoint_, random_state, represent,
+                             apply_, coupling_grad, dimension, mul_, mul_adjoint_, random_state, represent, search_stats,
                              symmetry_apply, symmetry_reduce, symmetry_unreduce, translation_symops)
 from .lanczos import LanczosResult, lanczos
 

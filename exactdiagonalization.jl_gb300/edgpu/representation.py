@@ -391,6 +391,16 @@ def _reduce_vector(rhsr: ReducedHilbertSpaceRepresentation, large):
     return small
 
 
+def search_stats(space) -> dict:
+    """Shape of a representation's search directory (buckets, shift, keys inline per bucket, window
+    halvings, fraction of rows answered by a bucket summary)."""
+    nb, sh, k, st, fr = ctypes.c_int64(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_double()
+    check(lib().edgpu_space_search_stats(space.handle, ctypes.byref(nb), ctypes.byref(sh), ctypes.byref(k),
+                                         ctypes.byref(st), ctypes.byref(fr)))
+    return {"buckets": int(nb.value), "shift": int(sh.value), "inline_per_bucket": int(k.value),
+            "window_steps": int(st.value), "inline_fraction": float(fr.value)}
+
+
 def symmetry_unreduce(rhsr: ReducedHilbertSpaceRepresentation, small):
     """symmetry_unreduce(rhsr, small_vector) -- symmetry_reduce.jl:208-225."""
     small = np.asarray(small)

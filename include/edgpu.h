@@ -89,6 +89,12 @@ int edgpu_space_get_basis(edgpu_space s, uint64_t* out, int64_t n);
 /* get(basis_lookup, key, -1) for n keys on the device (frozensortedarray.jl:29-48). */
 int edgpu_space_lookup(edgpu_space s, const uint64_t* keys, int64_t n, int64_t* idx_out);
 void edgpu_space_destroy(edgpu_space s);
+/* Shape of the search directory that replaces the binary search of FrozenSortedArrayIndex
+ * (frozensortedarray.jl:29-32) in the product: number of buckets, bucket = state >> shift, keys
+ * summarised inline per bucket, halvings for larger buckets, and the fraction of rows whose bucket is
+ * answered by its summary alone (all outputs nullable). */
+int edgpu_space_search_stats(edgpu_space s, int64_t* buckets, int32_t* shift, int32_t* inline_keys_per_bucket,
+                             int32_t* window_steps, double* inline_fraction);
 
 /* ---- symmetry reduction ------------------------------------------------------------------ */
 /* symmetry_reduce(hsr, symops_and_amplitudes) (symmetry_reduce_generic.jl:7-106), and the
