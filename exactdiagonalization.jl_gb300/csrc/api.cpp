@@ -125,17 +125,41 @@ struct edgpu_op_s {
     std::vector<double> coupl{1.0};
     Blob blob[2][2][2];               // [precision][direction 0 = H, 1 = H^dagger][mode 0 = product, 1 = gradient]
     int tuned_rows[2] = {0, 0};
+    uint64_t gen = 0;                 // bumped whenever the device tables are rebuilt
     DevBuf<double> x64, y64, z64;
     DevBuf<float> x32, y32;
     DevBuf<double> grad_partial, grad_dev;
 };
 
+// Sectors applied in one persistent launch (hx_multi_kernel).  Per precision: the common shared-memory
+// image (term, group and orbit-normalisation tables of the first operator, then every sector's
+// character table), and per set of vector pointers and lanes per row a device copy of that image
+// followed by the sector descriptors, plus the CUDA graph replaying the launch.
 struct edgpu_batch_s {
     std::vector<edgpu_op_s*> ops;
+    int lpr[2] = {0, 0};                           // lanes per row (0: default 1)
+    struct Fused {
+        bool ready = false;
+        std::vector<uint64_t> gens;                // operator table generations the image was built from
+        std::vector<unsigned char> image;          // common tables + per-sector character tables
+        std::vector<int> o_ph, o_num, want_arg;
+        HxParams tmpl{};
+        int gk = 0, per_sm = 1;
+        size_t smem = 0;
+        int64_t rows = 0;
+    } fused[2];
+    std::map<std::vector<const void*>, void*> images[2];
     std::map<std::vector<const void*>, cudaGraphExec_t> graphs[2];
+    void drop(int prec) {
+        for (auto& kv : images[prec]) cudaFree(kv.second);
+        for (auto& kv : graphs[prec]) cudaGraphExecDestroy(kv.second);
+        images[prec].clear();
+        graphs[prec].clear();
+        fused[prec] = Fused();
+    }
     ~edgpu_batch_s() {
-        for (auto& m : graphs)
-            for (auto& kv : m) cudaGraphExecDestroy(kv.second);
+        drop(0);
+        drop(1);
     }
 };
 
@@ -369,6 +393,7 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
 }
 
 void invalidate_blobs(edgpu_op_s* op) {
+    ++op->gen;
     for (auto& a : op->blob)
         for (auto& b : a)
             for (auto& c : b) {
@@ -1140,6 +1165,145 @@ int edgpu_coupling_grad_device(edgpu_op oh, int32_t precision, const void* x, co
 
 // ---- batched sectors ---------------------------------------------------------------------------
 
+namespace {
+
+// Common tables of a batch, checked for sameness: one term table, basis layout and symmetry group.
+void batch_prepare(edgpu_batch_s* b, int prec) {
+    edgpu_batch_s::Fused& F = b->fused[prec];
+    const int n = (int)b->ops.size();
+    std::vector<uint64_t> gens(n);
+    for (int i = 0; i < n; ++i) build_blob(b->ops[i], prec, 0, 0);
+    for (int i = 0; i < n; ++i) gens[i] = b->ops[i]->gen;
+    if (F.ready && F.gens == gens) return;
+    b->drop(prec);
+    const edgpu_op_s* o0 = b->ops[0];
+    const Space& s0 = *o0->space;
+    for (int i = 1; i < n; ++i) {
+        const edgpu_op_s* o = b->ops[i];
+        const Space& s = *o->space;
+        const bool same = s.w32 == s0.w32 && s.sb == s0.sb && s.lay.nbits == s0.lay.nbits &&
+                          s.group.kind == s0.group.kind && s.group.G == s0.group.G && s.group.L1 == s0.group.L1 &&
+                          s.group.L2 == s0.group.L2 && s.group.w == s0.group.w && s.group.maps == s0.group.maps &&
+                          s.group.flips == s0.group.flips && o->T == o0->T && o->masks == o0->masks &&
+                          o->rows == o0->rows && o->cols == o0->cols && o->unit == o0->unit && o->cid == o0->cid &&
+                          o->coupl == o0->coupl && o->blob[prec][0][0].gk == o0->blob[prec][0][0].gk;
+        require(same, EDGPU_ERR_ARG,
+                "batched operators must share the operator terms, the basis layout and the symmetry group "
+                "(operator " + std::to_string(i) + " differs from operator 0)");
+    }
+    const Blob& B0 = o0->blob[prec][0][0];
+    const size_t vsz = prec == EDGPU_FP64 ? 16 : 8;
+    const size_t base = (size_t)B0.tmpl.blob_words16 * 16;
+    F.image.assign(base, 0);
+    if (base) EDGPU_CUDA(cudaMemcpy(F.image.data(), B0.d, base, cudaMemcpyDeviceToHost));
+    F.o_ph.assign(n, 0);
+    F.o_num.assign(n, 0);
+    F.want_arg.assign(n, 0);
+    int any_arg = 0;
+    F.rows = 0;
+    for (int i = 0; i < n; ++i) {
+        const Group& g = b->ops[i]->space->group;
+        F.o_ph[i] = (int)F.image.size();
+        F.image.resize(align16(F.image.size() + g.den * vsz), 0);
+        for (int j = 0; j < g.den; ++j) {
+            const double ang = 2.0 * M_PI * (double)j / (double)g.den;
+            if (prec == EDGPU_FP64) {
+                const double v[2] = {std::cos(ang), std::sin(ang)};
+                memcpy(&F.image[F.o_ph[i] + j * 16], v, 16);
+            } else {
+                const float v[2] = {(float)std::cos(ang), (float)std::sin(ang)};
+                memcpy(&F.image[F.o_ph[i] + j * 8], v, 8);
+            }
+        }
+        F.o_num[i] = (int)F.image.size();
+        F.image.resize(align16(F.image.size() + g.G * 4), 0);
+        memcpy(&F.image[F.o_num[i]], g.num.data(), g.G * 4);
+        F.want_arg[i] = g.den > 1 ? 1 : 0;
+        any_arg |= F.want_arg[i];
+        F.rows += b->ops[i]->space->dim;
+    }
+    F.smem = F.image.size() + (size_t)n * sizeof(SectorDesc);
+    require(F.smem <= 227 * 1024, EDGPU_ERR_ARG,
+            "batched tables do not fit in shared memory (" + std::to_string(F.smem) + " bytes)");
+    F.tmpl = B0.tmpl;
+    F.tmpl.want_arg = any_arg;
+    F.tmpl.o_sec = (int)F.image.size();
+    F.tmpl.n_sec = n;
+    F.tmpl.accumulate = 0;
+    F.gk = B0.gk;
+    F.per_sm = std::max(1, s0.w32 ? hx_multi_occupancy_w32(F.gk, prec, F.smem) : hx_multi_occupancy_w64(F.gk, prec, F.smem));
+    F.gens = gens;
+    F.ready = true;
+}
+
+// Launch parameters of one batched product for a set of vector pointers (device image built once).
+HxParams batch_params(edgpu_batch_s* b, int prec, const void* const* xs, void* const* ys, int* blocks_out) {
+    edgpu_batch_s::Fused& F = b->fused[prec];
+    const int n = (int)b->ops.size();
+    const int lpr = b->lpr[prec] ? b->lpr[prec] : 1;
+    const int rpw = 32 / lpr;
+    std::vector<const void*> key;
+    key.push_back((const void*)(intptr_t)lpr);
+    for (int i = 0; i < n; ++i) {
+        key.push_back(xs[i]);
+        key.push_back(ys[i]);
+    }
+    std::vector<SectorDesc> d(n);
+    long long tiles = 0;
+    for (int i = 0; i < n; ++i) {
+        const edgpu_op_s* o = b->ops[i];
+        const Space& s = *o->space;
+        require(s.dim == 0 || (xs[i] && ys[i]), EDGPU_ERR_ARG, "null vector in batch");
+        d[i] = SectorDesc{};
+        d[i].keys = s.d_keys;
+        d[i].x = xs[i];
+        d[i].y = ys[i];
+        d[i].diag = o->blob[prec][0][0].d_diag;
+        d[i].dir = s.d_dir;
+        d[i].n_rows = s.dim;
+        tiles += (s.dim + rpw - 1) / rpw;
+        d[i].tile_end = tiles;
+        d[i].nb = s.dir_nb;
+        d[i].shift = s.dir_shift;
+        d[i].K = s.dir_K;
+        d[i].steps = s.dir_steps;
+        d[i].o_ph = F.o_ph[i];
+        d[i].o_num = F.o_num[i];
+        d[i].want_arg = F.want_arg[i];
+    }
+    auto it = b->images[prec].find(key);
+    if (it == b->images[prec].end()) {
+        std::vector<unsigned char> img(F.image);
+        img.resize(F.smem, 0);
+        memcpy(&img[F.image.size()], d.data(), n * sizeof(SectorDesc));
+        void* dev = nullptr;
+        EDGPU_CUDA(cudaMalloc(&dev, img.size()));
+        cudaError_t e = cudaMemcpy(dev, img.data(), img.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(dev);
+            throw Error(EDGPU_ERR_CUDA, std::string("batch image: ") + cudaGetErrorString(e));
+        }
+        it = b->images[prec].emplace(key, dev).first;
+    }
+    HxParams p = F.tmpl;
+    p.blob = it->second;
+    p.blob_words16 = (int)(F.smem / 16);
+    p.lpr = lpr;
+    p.rows_per_tile = rpw;
+    p.n_tiles = tiles;
+    const long long need = (tiles + HX_THREADS / 32 - 1) / (HX_THREADS / 32);
+    *blocks_out = (int)std::max<long long>(1, std::min<long long>(need, (long long)F.per_sm * std::max(1, g_sm_count)));
+    return p;
+}
+
+void batch_launch(edgpu_batch_s* b, int prec, const HxParams& p, int blocks, cudaStream_t st) {
+    if (p.n_tiles == 0) return;
+    if (b->ops[0]->space->w32) hx_multi_launch_w32(b->fused[prec].gk, prec, p, blocks, b->fused[prec].smem, st);
+    else hx_multi_launch_w64(b->fused[prec].gk, prec, p, blocks, b->fused[prec].smem, st);
+}
+
+}  // namespace
+
 int edgpu_batch_create(int32_t n_ops, const edgpu_op* ops, edgpu_batch* out) {
     API_BEGIN
     require(out && n_ops >= 1 && ops, EDGPU_ERR_ARG, "bad batch arguments");
@@ -1147,6 +1311,97 @@ int edgpu_batch_create(int32_t n_ops, const edgpu_op* ops, edgpu_batch* out) {
     std::unique_ptr<edgpu_batch_s> b(new edgpu_batch_s());
     for (int i = 0; i < n_ops; ++i) b->ops.push_back(as_op(ops[i]));
     *out = b.release();
+    API_END
+}
+
+int edgpu_batch_set_tiling(edgpu_batch bh, int32_t precision, int32_t lanes_per_row) {
+    API_BEGIN
+    require(bh, EDGPU_ERR_ARG, "null batch");
+    check_prec(precision);
+    require(lanes_per_row == 0 || lanes_per_row == 1 || lanes_per_row == 2 || lanes_per_row == 4, EDGPU_ERR_ARG,
+            "lanes_per_row must be 0 (default), 1, 2 or 4");
+    bh->lpr[precision] = lanes_per_row;
+    API_END
+}
+
+int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_row_out, double* best_ms_out) {
+    API_BEGIN
+    require(bh, EDGPU_ERR_ARG, "null batch");
+    check_prec(precision);
+    edgpu_batch_s* b = bh;
+    batch_prepare(b, precision);
+    const int n = (int)b->ops.size();
+    const size_t vs = precision == EDGPU_FP64 ? 16 : 8;
+    int64_t tot = 0;
+    for (auto* o : b->ops) tot += o->space->dim;
+    int best = 1;
+    double best_ms = 1e30;
+    if (tot > 0) {
+        void *x = nullptr, *y = nullptr;
+        EDGPU_CUDA(cudaMalloc(&x, tot * vs));
+        cudaError_t e = cudaMalloc(&y, tot * vs);
+        if (e != cudaSuccess) {
+            cudaFree(x);
+            throw Error(EDGPU_ERR_OOM, "batch autotune: no room for scratch vectors");
+        }
+        std::vector<const void*> xs(n);
+        std::vector<void*> ys(n);
+        int64_t off = 0;
+        for (int i = 0; i < n; ++i) {
+            xs[i] = (const char*)x + off * vs;
+            ys[i] = (char*)y + off * vs;
+            off += b->ops[i]->space->dim;
+        }
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        const int keep = b->lpr[precision];
+        try {
+            EDGPU_CUDA(cudaMemsetAsync(x, 0, tot * vs, g_stream));
+            for (int l : {1, 2, 4}) {
+                b->lpr[precision] = l;
+                int blocks = 0;
+                const HxParams p = batch_params(b, precision, xs.data(), ys.data(), &blocks);
+                batch_launch(b, precision, p, blocks, g_stream);
+                float sum = 0.f;
+                const int reps = 3;
+                for (int k = 0; k < reps; ++k) {
+                    EDGPU_CUDA(cudaEventRecord(e0, g_stream));
+                    batch_launch(b, precision, p, blocks, g_stream);
+                    EDGPU_CUDA(cudaEventRecord(e1, g_stream));
+                    EDGPU_CUDA(cudaEventSynchronize(e1));
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    sum += ms;
+                }
+                if (sum / reps < best_ms) {
+                    best_ms = sum / reps;
+                    best = l;
+                }
+            }
+        } catch (...) {
+            b->lpr[precision] = keep;
+            cudaStreamSynchronize(g_stream);
+            cudaFree(x);
+            cudaFree(y);
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            throw;
+        }
+        cudaStreamSynchronize(g_stream);
+        // the scratch images refer to freed vectors: forget them
+        for (auto& kv : b->images[precision]) cudaFree(kv.second);
+        b->images[precision].clear();
+        for (auto& kv : b->graphs[precision]) cudaGraphExecDestroy(kv.second);
+        b->graphs[precision].clear();
+        cudaFree(x);
+        cudaFree(y);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    b->lpr[precision] = best;
+    if (lanes_per_row_out) *lanes_per_row_out = best;
+    if (best_ms_out) *best_ms_out = best_ms;
     API_END
 }
 
@@ -1158,16 +1413,15 @@ int edgpu_batch_mul_device(edgpu_batch bh, int32_t precision, const void* const*
     edgpu_batch_s* b = bh;
     cudaStream_t st = pick_stream(stream);
     const int n = (int)b->ops.size();
-    for (int i = 0; i < n; ++i) build_blob(b->ops[i], precision, 0, 0);
-    auto issue = [&](cudaStream_t s) {
-        for (int i = 0; i < n; ++i)
-            launch_product(b->ops[i], precision, 0, 0, xs[i], ys[i], 0, nullptr, nullptr, s);
-    };
+    batch_prepare(b, precision);
+    int blocks = 0;
+    const HxParams p = batch_params(b, precision, xs, ys, &blocks);
     if (!use_graph) {
-        issue(st);
+        batch_launch(b, precision, p, blocks, st);
         return EDGPU_OK;
     }
     std::vector<const void*> key;
+    key.push_back((const void*)(intptr_t)p.lpr);
     for (int i = 0; i < n; ++i) {
         key.push_back(xs[i]);
         key.push_back(ys[i]);
@@ -1186,7 +1440,7 @@ int edgpu_batch_mul_device(edgpu_batch bh, int32_t precision, const void* const*
             throw Error(EDGPU_ERR_CUDA, std::string("begin capture: ") + cudaGetErrorString(e));
         }
         try {
-            issue(cap);
+            batch_launch(b, precision, p, blocks, cap);
         } catch (...) {
             cudaStreamEndCapture(cap, &graph);
             if (graph) cudaGraphDestroy(graph);

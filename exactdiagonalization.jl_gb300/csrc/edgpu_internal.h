@@ -163,6 +163,23 @@ struct HxParams {
     int sb, pb, want_arg, lpr;
     unsigned long long full;
     int warp_base;
+    int o_sec, n_sec;                         // batched launch: shared-memory offset and count of SectorDesc
+    long long n_tiles;                        // batched launch: warp tiles over all sectors
+};
+
+// One sector of a batched launch (hx_multi_kernel), kept in shared memory after the common tables.
+// The term, group and orbit-normalisation tables are common to all sectors; the basis table, its
+// search directory, the diagonal, the vectors and the character table belong to the sector.
+struct __align__(16) SectorDesc {
+    const void* keys;
+    const void* x;
+    void* y;
+    const void* diag;
+    const unsigned long long* dir;
+    long long n_rows;
+    long long tile_end;                       // cumulative warp tiles through this sector
+    long long nb;                             // directory buckets
+    int shift, K, steps, o_ph, o_num, want_arg, pad0, pad1;
 };
 
 constexpr int HX_QCAP = 128;         // per-warp target queue capacity (entries; 2 batches of 32 + 31)
@@ -178,6 +195,11 @@ void hx_rows_launch_w32(int gk, int prec, const HxParams& p, int blocks, size_t 
 void hx_rows_launch_w64(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
 int hx_rows_occupancy_w32(int gk, int prec, size_t smem);
 int hx_rows_occupancy_w64(int gk, int prec, size_t smem);
+// Batched sectors in one persistent launch (hx_rows.cuh, hx_multi_kernel), product mode only.
+void hx_multi_launch_w32(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
+void hx_multi_launch_w64(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
+int hx_multi_occupancy_w32(int gk, int prec, size_t smem);
+int hx_multi_occupancy_w64(int gk, int prec, size_t smem);
 
 // ---- the coupling-gradient launch for callers that cannot allocate (noalloc.cu) -----------------
 // Launch state of an operator's gradient-mode tables, read without building anything.

@@ -471,38 +471,98 @@ __global__ void k_embed(W* keys, long long n, int sb, GroupDev g, const int32_t*
     keys[i] = (W)((q << sb) | (W)divi[stab]);
 }
 
-// Search directory: start[b] = first index whose state lies in bucket >= b (bucket = state >> shift),
-// for b in [0, nb]; thread i fills the buckets between its predecessor's bucket and its own.
+// Bucket width of a search directory: for every candidate shift s in [s_lo, s_lo + n_shift) count
+// the keys whose bucket (state >> s) holds at most K(s) keys, K(s) = min(4, 28 / (s + sb)) (the keys
+// a bucket summary can carry).  A bucket holds more than K keys exactly when some K+1 consecutive
+// keys around key i share its bucket, so each key reads its K neighbours on either side.
 template <typename W>
-__global__ void k_dir_fill(const W* keys, long long n, int sb, int shift, long long nb, unsigned long long* start) {
+__global__ void k_dir_survey(const W* keys, long long n, int sb, int s_lo, int n_shift, unsigned long long* counts) {
+    __shared__ unsigned long long part[64];
+    for (int j = threadIdx.x; j < n_shift; j += blockDim.x) part[j] = 0ull;
+    __syncthreads();
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i > n) return;
-    const long long bcur = (i < n) ? min((long long)((keys[i] >> sb) >> shift), nb) : nb;
-    const long long bprev = (i > 0) ? min((long long)((keys[i - 1] >> sb) >> shift), nb) : -1;
-    for (long long b = bprev + 1; b <= bcur; ++b) start[b] = (unsigned long long)i;
+    const bool act = i < n;
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned long long v[9];   // states of keys i-4 .. i+4 (v valid where 0 <= index < n)
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        const long long w = i - 4 + j;
+        v[j] = (act && w >= 0 && w < n) ? (unsigned long long)(keys[w] >> sb) : 0ull;
+    }
+    for (int j = 0; j < n_shift; ++j) {
+        const int sh = s_lo + j, mb = sh + sb;
+        const int K = mb == 0 ? 4 : min(4, 28 / mb);
+        bool ok = act;
+#pragma unroll
+        for (int a = 0; a <= 4; ++a) {   // the K+1 keys from w = i-4+a (windows through i: a >= 4-K)
+            const long long w = i - 4 + a;
+            if (a >= 4 - K && w >= 0 && w + K < n && (v[a] >> sh) == (v[a + K] >> sh)) ok = false;
+        }
+        ok = ok && act;
+        const unsigned cnt = __popc(__ballot_sync(0xffffffffu, ok));
+        if (lane == 0 && cnt) atomicAdd(&part[j], (unsigned long long)cnt);
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < n_shift; j += blockDim.x)
+        if (part[j]) atomicAdd(&counts[j], part[j]);
 }
 
+// Search directory, one entry per bucket b in [0, nb) plus the sentinel dir[nb] = n:
 // dir[b] = start | min(count, 15) << 32 | the low mb bits of each key << (36 + k*mb) when the bucket
-// holds at most K keys; dir[nb] is the sentinel (start = n).  *maxcount receives the largest bucket and
-// *inline_keys the number of keys in buckets answered by their summary.
+// holds at most K keys (start = index of the bucket's first key, or of the next key when empty).
+// Each thread builds DIR_CHUNK consecutive buckets: one binary search for the first key of its
+// chunk, then a walk over the chunk's keys.  stats[0] receives the largest bucket and stats[1] the
+// number of keys answered by their bucket summary.
+constexpr int DIR_CHUNK = 128;
+
 template <typename W>
-__global__ void k_dir_pack(const W* keys, const unsigned long long* start, long long nb, long long n, int mb, int K,
-                           unsigned long long* dir, unsigned long long* maxcount, unsigned long long* inline_keys) {
-    const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (b > nb) return;
-    if (b == nb) {
-        dir[b] = (unsigned long long)n;
-        return;
-    }
-    const unsigned long long st = start[b], cnt = start[b + 1] - st;
-    unsigned long long e = st | (min(cnt, 15ull) << 32);
-    if ((long long)cnt <= K) {
+__global__ void k_dir_build(const W* keys, long long n, int sb, int shift, long long nb, int mb, int K,
+                            unsigned long long* dir, unsigned long long* stats) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long b0 = t * DIR_CHUNK;
+    unsigned long long mx = 0ull, inl = 0ull;
+    if (b0 <= nb) {
+        long long lo = 0, len = n;   // first key with bucket >= b0
+        while (len > 0) {
+            const long long half = len >> 1;
+            if ((long long)((keys[lo + half] >> sb) >> shift) < b0) {
+                lo += half + 1;
+                len -= half + 1;
+            } else {
+                len = half;
+            }
+        }
+        long long i = lo;
         const unsigned long long mbmask = (mb >= 64) ? ~0ull : ((1ull << mb) - 1ull);
-        for (int k = 0; k < (int)cnt; ++k) e |= ((unsigned long long)keys[st + k] & mbmask) << (36 + k * mb);
-        if (cnt) atomicAdd(inline_keys, cnt);
+        const long long b1 = min(b0 + DIR_CHUNK, nb + 1);
+        for (long long bb = b0; bb < b1; ++bb) {
+            if (bb == nb) {
+                dir[bb] = (unsigned long long)n;
+                break;
+            }
+            const long long st = i;
+            unsigned long long mem = 0ull;
+            int k = 0;
+            while (i < n && (long long)((keys[i] >> sb) >> shift) == bb) {
+                if (k < K) mem |= ((unsigned long long)keys[i] & mbmask) << (36 + k * mb);
+                ++k;
+                ++i;
+            }
+            const unsigned long long cnt = (unsigned long long)k;
+            if ((long long)cnt <= K) inl += cnt;
+            else mem = 0ull;
+            if (cnt > mx) mx = cnt;
+            dir[bb] = (unsigned long long)st | (min(cnt, 15ull) << 32) | mem;
+        }
     }
-    dir[b] = e;
-    if (cnt > 1) atomicMax(maxcount, cnt);
+    for (int d = 16; d > 0; d >>= 1) {
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, d));
+        inl += __shfl_xor_sync(0xffffffffu, inl, d);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (mx > 1) atomicMax(stats, mx);
+        if (inl) atomicAdd(stats + 1, inl);
+    }
 }
 
 template <typename W>
@@ -834,54 +894,70 @@ void dir_t(Space& s, cudaStream_t st) {
     int nbits_n = 0;
     while ((1ll << nbits_n) < std::max<long long>(n, 1)) ++nbits_n;
     // the directory may use up to 16x the key table (HBM is plentiful; a clustered table needs small
-    // buckets before most of them fit inline)
+    // buckets before most of its keys fit in their bucket summaries)
     const size_t cap_bytes = std::max<size_t>((size_t)512 << 20, 16 * (size_t)n * sizeof(W));
-    int d = std::max(1, std::min(nbits_n, bitlen));
-    unsigned long long* start = nullptr;
-    unsigned long long* d_stats = nullptr;   // [0] largest bucket, [1] keys answered inline
-    EDGPU_CUDA(cudaMalloc(&d_stats, 2 * sizeof(unsigned long long)));
-    for (;;) {
-        const int shift = std::max(0, bitlen - d);
-        const long long nb = (bitlen == 0) ? 1 : ((long long)(max_state >> shift) + 1);
-        const int mb = shift + s.sb;
-        const int K = mb == 0 ? 4 : std::min(4, 28 / mb);
-        cudaFree(start);
-        start = nullptr;
+    // candidate shifts: from about one bucket per key (s_hi) down to the smallest the cap allows
+    const int s_hi = std::max(0, bitlen - std::max(1, std::min(nbits_n, bitlen)));
+    int s_lo = s_hi;
+    while (s_lo > 0 && s_hi - s_lo < 63 &&
+           (size_t)((max_state >> (s_lo - 1)) + 2) * sizeof(unsigned long long) <= cap_bytes)
+        --s_lo;
+    const int n_shift = s_hi - s_lo + 1;
+    unsigned long long* d_stats = nullptr;   // survey counts [n_shift], then [largest bucket, inline keys]
+    EDGPU_CUDA(cudaMalloc(&d_stats, (n_shift + 2) * sizeof(unsigned long long)));
+    std::vector<unsigned long long> cnt(n_shift + 2, 0ull);
+    cudaError_t e = cudaMemsetAsync(d_stats, 0, (n_shift + 2) * sizeof(unsigned long long), st);
+    if (e == cudaSuccess && n > 0) {
+        k_dir_survey<W><<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const W*)s.d_keys, n, s.sb, s_lo, n_shift, d_stats);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cnt.data(), d_stats, n_shift * sizeof(unsigned long long),
+                                              cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        cudaFree(d_stats);
+        throw Error(EDGPU_ERR_CUDA, std::string("search directory survey: ") + cudaGetErrorString(e));
+    }
+    // the widest buckets whose summaries answer at least 98% of the keys, else the best fraction
+    int shift = s_hi;
+    double best = -1.0;
+    for (int sh = s_hi; sh >= s_lo; --sh) {
+        const double f = n > 0 ? (double)cnt[sh - s_lo] / (double)n : 1.0;
+        if (f > best) {
+            best = f;
+            shift = sh;
+        }
+        if (f >= 0.98) break;
+    }
+    const long long nb = (bitlen == 0) ? 1 : ((long long)(max_state >> shift) + 1);
+    const int mb = shift + s.sb;
+    const int K = mb == 0 ? 4 : std::min(4, 28 / mb);
+    if (s.d_dir) cudaFree(s.d_dir);
+    s.d_dir = nullptr;
+    e = cudaMalloc(&s.d_dir, (nb + 1) * sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+        const long long threads = nb / DIR_CHUNK + 1;
+        k_dir_build<W><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>((const W*)s.d_keys, n, s.sb, shift, nb, mb, K,
+                                                                          s.d_dir, d_stats + n_shift);
+        e = cudaGetLastError();
+    }
+    unsigned long long hs[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hs, d_stats + n_shift, sizeof(hs), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_stats);
+    if (e != cudaSuccess) {
         if (s.d_dir) cudaFree(s.d_dir);
         s.d_dir = nullptr;
-        cudaError_t e = cudaMalloc(&start, (nb + 1) * sizeof(unsigned long long));
-        if (e == cudaSuccess) e = cudaMalloc(&s.d_dir, (nb + 1) * sizeof(unsigned long long));
-        if (e == cudaSuccess) e = cudaMemsetAsync(d_stats, 0, 2 * sizeof(unsigned long long), st);
-        if (e == cudaSuccess) {
-            k_dir_fill<W><<<(unsigned)((n + 1 + 255) / 256), 256, 0, st>>>((const W*)s.d_keys, n, s.sb, shift, nb, start);
-            k_dir_pack<W><<<(unsigned)((nb + 1 + 255) / 256), 256, 0, st>>>((const W*)s.d_keys, start, nb, n, mb, K,
-                                                                           s.d_dir, d_stats, d_stats + 1);
-            e = cudaGetLastError();
-        }
-        unsigned long long hs[2] = {0, 0};
-        if (e == cudaSuccess) e = cudaMemcpyAsync(hs, d_stats, sizeof(hs), cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) {
-            cudaFree(start);
-            cudaFree(d_stats);
-            throw Error(EDGPU_ERR_CUDA, std::string("search directory: ") + cudaGetErrorString(e));
-        }
-        const double frac = n > 0 ? (double)hs[1] / (double)n : 1.0;
-        const bool grow = frac < 0.98 && shift > 0 && (size_t)(2 * nb + 2) * sizeof(unsigned long long) <= cap_bytes;
-        if (!grow) {
-            s.dir_shift = shift;
-            s.dir_nb = nb;
-            s.dir_K = K;
-            s.dir_inline = frac;
-            int steps = 0;
-            while ((1ull << steps) < std::max<unsigned long long>(hs[0], 1ull)) ++steps;
-            s.dir_steps = steps;
-            break;
-        }
-        ++d;
+        throw Error(e == cudaErrorMemoryAllocation ? EDGPU_ERR_OOM : EDGPU_ERR_CUDA,
+                    std::string("search directory: ") + cudaGetErrorString(e));
     }
-    cudaFree(start);
-    cudaFree(d_stats);
+    s.dir_shift = shift;
+    s.dir_nb = nb;
+    s.dir_K = K;
+    s.dir_inline = n > 0 ? (double)hs[1] / (double)n : 1.0;
+    int steps = 0;
+    while ((1ull << steps) < std::max<unsigned long long>(hs[0], 1ull)) ++steps;
+    s.dir_steps = steps;
 }
 
 template <typename W>

@@ -15,10 +15,160 @@
 
 namespace edgpu {
 
+// Shared-memory views of the tables of one product launch (common to all sectors of a batch).
+template <typename W, int PREC>
+struct RowsTables {
+    typedef typename Cx<PREC>::V V;
+    typedef typename Cx<PREC>::R R;
+    const W *orec, *dm, *dr, *keep, *lut, *flips;
+    const V *oa, *ou;
+    const int *oc, *dc;
+    const double2 *da, *du;
+    const R* ratio;
+    const unsigned* rlut;
+    __device__ __forceinline__ RowsTables(const HxParams& p, const unsigned char* sm) {
+        orec = (const W*)(sm + p.o_om);
+        oa = (const V*)(sm + p.o_oa);
+        ou = (const V*)(sm + p.o_ou);
+        oc = (const int*)(sm + p.o_oc);
+        dm = (const W*)(sm + p.o_dm);
+        dr = (const W*)(sm + p.o_dr);
+        da = (const double2*)(sm + p.o_da);
+        du = (const double2*)(sm + p.o_du);
+        dc = (const int*)(sm + p.o_dc);
+        ratio = (const R*)(sm + p.o_ratio);
+        keep = (const W*)(sm + p.o_keep);
+        lut = (const W*)(sm + p.o_lut);
+        flips = (const W*)(sm + p.o_flip);
+        rlut = (const unsigned*)(sm + (p.o_rlut >= 0 ? p.o_rlut : 0));
+    }
+};
+
+// The sector a warp tile belongs to: its basis table, search directory, vectors, diagonal and
+// character table.
+template <int PREC>
+struct RowsSector {
+    typedef typename Cx<PREC>::V V;
+    const void* keys;
+    const V* x;
+    V* y;
+    const V* diag;
+    long long n_rows;
+    DirSearch ds;
+    const V* ph;
+    const int* num;
+    bool want_arg;
+};
+
+// One warp tile of rows (rows_per_tile = 32 / lpr consecutive rows of the sector, lpr lanes each).
+template <typename W, int GK, int PREC, int MODE>
+__device__ __forceinline__ void rows_tile(const HxParams& p, const RowsTables<W, PREC>& tb, const RowsSector<PREC>& sc,
+                                          long long tile, int lane, double* sgrad) {
+    typedef typename Cx<PREC>::V V;
+    typedef typename Cx<PREC>::R R;
+    const W* __restrict__ keys = (const W*)sc.keys;
+    const V* __restrict__ x = sc.x;
+    const int sb = p.sb;
+    const W smask = (W)((((W)1) << sb) - 1);
+    const int T_o = p.T_o;
+    // lpr lanes share a row: lane sub = lane % lpr takes the terms t with t % lpr == sub
+    const int lpr = p.lpr, sub = lane & (lpr - 1), rpw = 32 / lpr;
+    const long long row = tile * rpw + lane / lpr;
+    const bool act = row < sc.n_rows;
+    const W kr = act ? keys[row] : (W)0;
+    const W b = kr >> sb;
+    const int ri = (int)(kr & smask);
+    const V xr = act ? x[row] : czero<V>();
+    V acc = czero<V>();
+    V gv = czero<V>();
+    if (MODE == 0) {
+        if (act && sub == 0) acc = cmul(sc.diag[row], xr);
+    } else {
+        gv = act ? ((const V*)p.gy)[row] : czero<V>();
+        double2 e = make_double2(0.0, 0.0);
+        if (act && sub == 0)
+            for (int t = 0; t < p.T_d; ++t)
+                if ((b & tb.dm[t]) == tb.dr[t]) {
+                    e.x += tb.da[t].x;
+                    e.y += tb.da[t].y;
+                    const V cu = cmul(from_d2<V>(tb.du[t]), xr);
+                    atomicAdd(&sgrad[tb.dc[t]], (double)gv.x * (double)cu.x + (double)gv.y * (double)cu.y);
+                }
+        acc = cmul(from_d2<V>(e), xr);
+    }
+    // this lane's terms: t = sub + lpr * k, in chunks of 64
+    const int my_terms = (T_o - sub + lpr - 1) / lpr;
+    for (int k0 = 0; k0 < my_terms; k0 += 64) {
+        const int kn = min(64, my_terms - k0);
+        unsigned long long mm = 0ull;
+        for (int k = 0; k < kn; ++k) {
+            W tm, tr, tf;
+            load_rec3<W>(tb.orec + 4 * (sub + lpr * (k0 + k)), tm, tr, tf);
+            mm |= (unsigned long long)((b & tm) == tr) << k;
+        }
+        if (!act) mm = 0ull;
+        while (__any_sync(0xffffffffu, mm != 0ull)) {
+            int tt[2];
+            bool on[2];
+            W q[2], rep[2];
+            int g[2];
+            long long c[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                on[h] = mm != 0ull;
+                tt[h] = on[h] ? sub + lpr * (k0 + __ffsll((long long)mm) - 1) : 0;
+                mm &= mm - 1ull;
+                W tm, tr, tf;
+                load_rec3<W>(tb.orec + 4 * tt[h], tm, tr, tf);
+                q[h] = b ^ tf;
+                rep[h] = q[h];
+                g[h] = 0;
+                if (on[h]) canon_rep<W, GK>(q[h], p, tb.keep, tb.lut, tb.flips, tb.rlut, rep[h], g[h]);
+            }
+            int sx[2];
+            key_find_sum2<W>(keys, sc.ds, rep, on, c, sx);
+            V xv[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) xv[h] = (c[h] >= 0) ? x[c[h]] : czero<V>();
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (c[h] >= 0) {
+                    V coef = tb.oa[tt[h]];
+                    V phv = czero<V>();
+                    R f = (R)1;
+                    if (GK != GK_TRIVIAL) {
+                        f = tb.ratio[ri * p.nd + sx[h]];
+                        if (sc.want_arg) {
+                            phv = sc.ph[sc.num[g[h]]];
+                            coef = cmul(coef, phv);
+                        }
+                        coef = cscale(coef, f);
+                    }
+                    acc = cadd(acc, cmul(coef, xv[h]));
+                    if (MODE) {
+                        V cu = tb.ou[tt[h]];
+                        if (GK != GK_TRIVIAL) {
+                            if (sc.want_arg) cu = cmul(cu, phv);
+                            cu = cscale(cu, f);
+                        }
+                        const V t = cmul(cu, xv[h]);
+                        atomicAdd(&sgrad[tb.oc[tt[h]]], (double)gv.x * (double)t.x + (double)gv.y * (double)t.y);
+                    }
+                }
+            }
+        }
+    }
+    // partial sums of the row's lanes (fixed butterfly order)
+    for (int d = 1; d < lpr; d <<= 1) acc = cadd(acc, shfl_xor_v(acc, d));
+    if (act && sub == 0) {
+        if (p.accumulate) acc = cadd(acc, sc.y[row]);
+        sc.y[row] = acc;
+    }
+}
+
 template <typename W, int GK, int PREC, int MODE>
 __global__ void __launch_bounds__(HX_THREADS) hx_rows_kernel(const HxParams p) {
     typedef typename Cx<PREC>::V V;
-    typedef typename Cx<PREC>::R R;
     extern __shared__ __align__(16) unsigned char sm[];
     {
         const int4* src = (const int4*)p.blob;
@@ -30,134 +180,93 @@ __global__ void __launch_bounds__(HX_THREADS) hx_rows_kernel(const HxParams p) {
         for (int i = threadIdx.x; i < p.n_coupl; i += blockDim.x) sgrad[i] = 0.0;
     __syncthreads();
 
-    const W* orec = (const W*)(sm + p.o_om);
-    const V* oa = (const V*)(sm + p.o_oa);
-    const V* ou = (const V*)(sm + p.o_ou);
-    const int* oc = (const int*)(sm + p.o_oc);
-    const W* dm = (const W*)(sm + p.o_dm);
-    const W* dr = (const W*)(sm + p.o_dr);
-    const double2* da = (const double2*)(sm + p.o_da);
-    const double2* du = (const double2*)(sm + p.o_du);
-    const int* dc = (const int*)(sm + p.o_dc);
-    const V* ph = (const V*)(sm + p.o_ph);
-    const int* num = (const int*)(sm + p.o_num);
-    const R* ratio = (const R*)(sm + p.o_ratio);
-    const W* keep = (const W*)(sm + p.o_keep);
-    const W* lut = (const W*)(sm + p.o_lut);
-    const W* flips = (const W*)(sm + p.o_flip);
-    const unsigned* rlut = (const unsigned*)(sm + (p.o_rlut >= 0 ? p.o_rlut : 0));
-
-    const W* __restrict__ keys = (const W*)p.keys;
-    const V* __restrict__ x = (const V*)p.x;
-    V* y = (V*)p.y;
-    const V* gy = (const V*)p.gy;
-    const int sb = p.sb;
-    const W smask = (W)((((W)1) << sb) - 1);
-    const int T_o = p.T_o;
-    const bool want_arg = p.want_arg != 0;
+    const RowsTables<W, PREC> tb(p, sm);
+    RowsSector<PREC> sc;
+    sc.keys = p.keys;
+    sc.x = (const V*)p.x;
+    sc.y = (V*)p.y;
+    sc.diag = (const V*)p.diag;
+    sc.n_rows = p.n_rows;
+    sc.ds = p.ds;
+    sc.ph = (const V*)(sm + p.o_ph);
+    sc.num = (const int*)(sm + p.o_num);
+    sc.want_arg = p.want_arg != 0;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-    // lpr lanes share a row: lane sub = lane % lpr takes the terms t with t % lpr == sub
-    const int lpr = p.lpr, sub = lane & (lpr - 1), rpw = 32 / lpr;
+    const int rpw = 32 / p.lpr;
     const long long n_tiles = (p.n_rows + rpw - 1) / rpw;
-
-    for (long long tile = (long long)blockIdx.x * wpb + warp; tile < n_tiles; tile += (long long)gridDim.x * wpb) {
-        const long long row = tile * rpw + lane / lpr;
-        const bool act = row < p.n_rows;
-        const W kr = act ? keys[row] : (W)0;
-        const W b = kr >> sb;
-        const int ri = (int)(kr & smask);
-        const V xr = act ? x[row] : czero<V>();
-        V acc = czero<V>();
-        V gv = czero<V>();
-        if (MODE == 0) {
-            if (act && sub == 0) acc = cmul(((const V*)p.diag)[row], xr);
-        } else {
-            gv = act ? gy[row] : czero<V>();
-            double2 e = make_double2(0.0, 0.0);
-            if (act && sub == 0)
-                for (int t = 0; t < p.T_d; ++t)
-                    if ((b & dm[t]) == dr[t]) {
-                        e.x += da[t].x;
-                        e.y += da[t].y;
-                        const V cu = cmul(from_d2<V>(du[t]), xr);
-                        atomicAdd(&sgrad[dc[t]], (double)gv.x * (double)cu.x + (double)gv.y * (double)cu.y);
-                    }
-            acc = cmul(from_d2<V>(e), xr);
-        }
-        // this lane's terms: t = sub + lpr * k, in chunks of 64
-        const int my_terms = (T_o - sub + lpr - 1) / lpr;
-        for (int k0 = 0; k0 < my_terms; k0 += 64) {
-            const int kn = min(64, my_terms - k0);
-            unsigned long long mm = 0ull;
-            for (int k = 0; k < kn; ++k) {
-                W tm, tr, tf;
-                load_rec3<W>(orec + 4 * (sub + lpr * (k0 + k)), tm, tr, tf);
-                mm |= (unsigned long long)((b & tm) == tr) << k;
-            }
-            if (!act) mm = 0ull;
-            while (__any_sync(0xffffffffu, mm != 0ull)) {
-                int tt[2];
-                bool on[2];
-                W q[2], rep[2];
-                int g[2];
-                long long c[2];
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    on[h] = mm != 0ull;
-                    tt[h] = on[h] ? sub + lpr * (k0 + __ffsll((long long)mm) - 1) : 0;
-                    mm &= mm - 1ull;
-                    W tm, tr, tf;
-                    load_rec3<W>(orec + 4 * tt[h], tm, tr, tf);
-                    q[h] = b ^ tf;
-                    rep[h] = q[h];
-                    g[h] = 0;
-                    if (on[h]) canon_rep<W, GK>(q[h], p, keep, lut, flips, rlut, rep[h], g[h]);
-                }
-                int sx[2];
-                key_find_sum2<W>(keys, p.ds, rep, on, c, sx);
-                V xv[2];
-#pragma unroll
-                for (int h = 0; h < 2; ++h) xv[h] = (c[h] >= 0) ? x[c[h]] : czero<V>();
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    if (c[h] >= 0) {
-                        V coef = oa[tt[h]];
-                        V phv = czero<V>();
-                        R f = (R)1;
-                        if (GK != GK_TRIVIAL) {
-                            f = ratio[ri * p.nd + sx[h]];
-                            if (want_arg) {
-                                phv = ph[num[g[h]]];
-                                coef = cmul(coef, phv);
-                            }
-                            coef = cscale(coef, f);
-                        }
-                        acc = cadd(acc, cmul(coef, xv[h]));
-                        if (MODE) {
-                            V cu = ou[tt[h]];
-                            if (GK != GK_TRIVIAL) {
-                                if (want_arg) cu = cmul(cu, phv);
-                                cu = cscale(cu, f);
-                            }
-                            const V t = cmul(cu, xv[h]);
-                            atomicAdd(&sgrad[oc[tt[h]]], (double)gv.x * (double)t.x + (double)gv.y * (double)t.y);
-                        }
-                    }
-                }
-            }
-        }
-        // partial sums of the row's lanes (fixed butterfly order)
-        for (int d = 1; d < lpr; d <<= 1) acc = cadd(acc, shfl_xor_v(acc, d));
-        if (act && sub == 0) {
-            if (p.accumulate) acc = cadd(acc, y[row]);
-            y[row] = acc;
-        }
-    }
+    for (long long tile = (long long)blockIdx.x * wpb + warp; tile < n_tiles; tile += (long long)gridDim.x * wpb)
+        rows_tile<W, GK, PREC, MODE>(p, tb, sc, tile, lane, sgrad);
     if (MODE) {
         __syncthreads();
         for (int i = threadIdx.x; i < p.n_coupl; i += blockDim.x)
             p.grad_partial[(size_t)blockIdx.x * p.n_coupl + i] = sgrad[i];
     }
+}
+
+// Batched sectors in one persistent launch: the warp tiles of all sectors are numbered one after the
+// other (sector s owns tiles [tile_end[s-1], tile_end[s])), and the grid strides over them.  Each
+// warp's tiles increase, so its sector index only moves forward.  The common term and group tables
+// and each sector's descriptor and character table are staged in shared memory once per block.
+template <typename W, int GK, int PREC>
+__global__ void __launch_bounds__(HX_THREADS) hx_multi_kernel(const HxParams p) {
+    typedef typename Cx<PREC>::V V;
+    extern __shared__ __align__(16) unsigned char sm[];
+    {
+        const int4* src = (const int4*)p.blob;
+        int4* dst = (int4*)sm;
+        for (int i = threadIdx.x; i < p.blob_words16; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const RowsTables<W, PREC> tb(p, sm);
+    const SectorDesc* sec = (const SectorDesc*)(sm + p.o_sec);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    int s = 0;
+    long long tile0 = 0;   // first tile of sector s
+    for (long long tile = (long long)blockIdx.x * wpb + warp; tile < p.n_tiles; tile += (long long)gridDim.x * wpb) {
+        while (s + 1 < p.n_sec && tile >= sec[s].tile_end) {
+            tile0 = sec[s].tile_end;
+            ++s;
+        }
+        const SectorDesc& d = sec[s];
+        RowsSector<PREC> sc;
+        sc.keys = d.keys;
+        sc.x = (const V*)d.x;
+        sc.y = (V*)d.y;
+        sc.diag = (const V*)d.diag;
+        sc.n_rows = d.n_rows;
+        sc.ds.dir = d.dir;
+        sc.ds.nb = d.nb;
+        sc.ds.shift = d.shift;
+        sc.ds.mb = d.shift + p.sb;
+        sc.ds.K = d.K;
+        sc.ds.steps = d.steps;
+        sc.ds.sb = p.sb;
+        sc.ph = (const V*)(sm + d.o_ph);
+        sc.num = (const int*)(sm + d.o_num);
+        sc.want_arg = d.want_arg != 0;
+        rows_tile<W, GK, PREC, 0>(p, tb, sc, tile - tile0, lane, nullptr);
+    }
+}
+
+template <typename W, int GK, int PREC>
+void hx_multi_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
+    auto kern = hx_multi_kernel<W, GK, PREC>;
+    static size_t smem_set = 0;   // raised once per kernel, never inside a graph capture
+    if (smem > smem_set) {
+        EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        smem_set = smem;
+    }
+    kern<<<blocks, HX_THREADS, smem, st>>>(p);
+    EDGPU_CUDA(cudaGetLastError());
+}
+
+template <typename W, int GK, int PREC>
+int hx_multi_occupancy_one(size_t smem) {
+    auto kern = hx_multi_kernel<W, GK, PREC>;
+    EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int n = 0;
+    EDGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, HX_THREADS, smem));
+    return n;
 }
 
 template <typename W, int GK, int PREC, int MODE>

@@ -74,6 +74,8 @@ SIGNATURES = {
     "edgpu_coupling_grad_device": (ctypes.c_int, [vp, i32, vp, vp, vp, i64, P(dbl), vp]),
     "edgpu_coupling_grad_device_noalloc": (ctypes.c_int, [vp, i32, vp, vp, vp, i64, P(dbl), vp]),
     "edgpu_batch_create": (ctypes.c_int, [i32, P(vp), P(vp)]),
+    "edgpu_batch_set_tiling": (ctypes.c_int, [vp, i32, i32]),
+    "edgpu_batch_autotune": (ctypes.c_int, [vp, i32, P(i32), P(ctypes.c_double)]),
     "edgpu_batch_mul_device": (ctypes.c_int, [vp, i32, P(vp), P(vp), i32, vp]),
     "edgpu_batch_destroy": (None, [vp]),
     "edgpu_lanczos": (ctypes.c_int, [vp, i32, i32, i32, u64, P(dbl), i32, dbl, P(dbl), P(dbl), P(dbl), P(i32),

@@ -639,8 +639,10 @@ def coupling_grad(opr, x, gy, precision="fp64", y=None) -> np.ndarray:
 
 
 class Batch:
-    """Several operator representations (e.g. every momentum sector) applied together, optionally
-    replayed from a captured CUDA graph."""
+    """Several operator representations (every momentum sector of one Hamiltonian) applied in one
+    persistent launch, optionally replayed from a captured CUDA graph.  The representations must
+    share the operator terms, the basis layout and the symmetry group; each sector's result equals
+    ``mul_`` on that sector with the same lanes per row."""
 
     def __init__(self, oprs: Sequence[OperatorRepresentation]):
         self.oprs = list(oprs)
@@ -655,8 +657,24 @@ class Batch:
             _lib._lib.edgpu_batch_destroy(h)
             self._h = None
 
+    def set_tiling(self, precision, lanes_per_row: int):
+        """Lanes per row of the batched launch: 0 (default, 1), 1, 2 or 4."""
+        check(lib().edgpu_batch_set_tiling(self._h, _prec(precision), int(lanes_per_row)))
+
+    def autotune(self, precision="mixed"):
+        """Time 1, 2 and 4 lanes per row and keep the fastest; returns (lanes_per_row, ms)."""
+        l = ctypes.c_int32()
+        ms = ctypes.c_double()
+        check(lib().edgpu_batch_autotune(self._h, _prec(precision), ctypes.byref(l), ctypes.byref(ms)))
+        return l.value, ms.value
+
     def mul_(self, outs, states, precision="mixed", use_graph=True):
         prec = _prec(precision)
+        if len(outs) != len(self.oprs) or len(states) != len(self.oprs):
+            raise ArgumentError(f"expected {len(self.oprs)} vectors, got {len(states)} and {len(outs)}")
+        for o, x, y in zip(self.oprs, states, outs):
+            _check_len(x, o.dimension, "x")
+            _check_len(y, o.dimension, "y")
         xs = (ctypes.c_void_p * len(states))(*[s.data_ptr() for s in states])
         ys = (ctypes.c_void_p * len(outs))(*[o.data_ptr() for o in outs])
         check(lib().edgpu_batch_mul_device(self._h, prec, xs, ys, int(use_graph), _torch_stream()))

@@ -180,11 +180,23 @@ int edgpu_coupling_grad_device_noalloc(edgpu_op op, int32_t precision, const voi
                                        int64_t n, double* grad_out, void* stream);
 
 /* ---- batched sectors --------------------------------------------------------------------- */
-/* Several operator representations (e.g. every momentum sector) applied in one persistent launch.
- * All ops must share the operator terms' shape (word width and group kind). */
+/* Several operator representations (e.g. every momentum sector of one Hamiltonian) applied in ONE
+ * persistent launch: the warp tiles of all sectors are numbered one after the other and the grid
+ * strides over them.  No reference counterpart (the reference applies one representation per
+ * mul!, abstract_operator_representation.jl:110-118); each sector's result equals edgpu_mul_device
+ * on that sector with the same lanes per row, bit for bit.  The operators must share the operator
+ * terms, the basis layout and the symmetry group (they differ only in the sector: basis table,
+ * characters, diagonal); EDGPU_ERR_ARG otherwise, at the first product.  The operators must outlive
+ * the batch; changing an operator's couplings rebuilds the batch's tables at the next product. */
 int edgpu_batch_create(int32_t n_ops, const edgpu_op* ops, edgpu_batch* out);
-/* y_k = H_k x_k for every k, device vectors (array of n_ops pointers each). If use_graph != 0 the
- * launch is captured once into a CUDA graph (per set of pointers) and replayed. */
+/* Lanes per row of the batched launch for this precision: 0 (default: 1), 1, 2 or 4. */
+int edgpu_batch_set_tiling(edgpu_batch b, int32_t precision, int32_t lanes_per_row);
+/* In-library autotuner: times the batched launch for 1, 2 and 4 lanes per row on scratch vectors
+ * (allocated and freed here) and keeps the fastest. */
+int edgpu_batch_autotune(edgpu_batch b, int32_t precision, int32_t* lanes_per_row_out, double* best_ms_out);
+/* y_k = H_k x_k for every k, device vectors (arrays of n_ops pointers).  The first call with a set of
+ * pointers uploads the sector descriptors (synchronous); if use_graph != 0 that launch is also
+ * captured once into a CUDA graph and replayed on the later calls with the same pointers. */
 int edgpu_batch_mul_device(edgpu_batch b, int32_t precision, const void* const* xs, void* const* ys,
                            int32_t use_graph, void* stream);
 void edgpu_batch_destroy(edgpu_batch b);
