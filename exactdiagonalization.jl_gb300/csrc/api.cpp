@@ -232,8 +232,11 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     p.o_flip = alloc((g.kind == GK_GENERIC ? g.G : 0) * wsz);
     // torus row table: smallest rotation of every row value and the rotation steps reaching it
     const int rowbits = g.L1 * g.w;
-    const bool use_rlut = g.kind == GK_TORUS && g.L2 >= 2 && rowbits <= 10 && g.L1 <= 16;
-    p.o_rlut = use_rlut ? alloc(((size_t)1 << rowbits) * 4) : -1;
+    const bool use_rlut = g.kind == GK_TORUS && g.L2 >= 2 && g.L2 <= TORUS_MAXR && rowbits <= 10 && g.L1 <= 16;
+    const bool use_pair = use_rlut && rowbits <= 6;
+    const int lut_bits = use_pair ? 2 * rowbits : rowbits;
+    p.o_rlut = use_rlut ? alloc(((size_t)1 << lut_bits) * 4) : -1;
+    p.rlut_pair = use_pair ? 1 : 0;
     const size_t blob_bytes = align16(off);
     std::vector<unsigned char> h(blob_bytes, 0);
     auto putw = [&](int o, size_t i, uint64_t v) {
@@ -303,12 +306,18 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
         }
     for (size_t i = 0; i < keep.size(); ++i) putw(p.o_keep, i, keep[i]);
     if (use_rlut) {
+        // smallest rotation of a row (or of a pair of rows: top row << rowbits | the row below it,
+        // both rotated by the same a) and the rotations a reaching it
         const uint32_t rmask = (1u << rowbits) - 1u;
-        for (uint32_t v = 0; v <= rmask; ++v) {
+        auto rot = [&](uint32_t v, int a) {
+            const int sh = a * g.w;
+            return sh ? (((v << sh) | (v >> (rowbits - sh))) & rmask) : v;
+        };
+        const uint32_t n_entries = 1u << lut_bits;
+        for (uint32_t v = 0; v < n_entries; ++v) {
             uint32_t best = 0xffffffffu, steps = 0;
             for (int a = 0; a < g.L1; ++a) {
-                const int sh = a * g.w;
-                const uint32_t r = sh ? (((v << sh) | (v >> (rowbits - sh))) & rmask) : v;
+                const uint32_t r = use_pair ? ((rot(v >> rowbits, a) << rowbits) | rot(v & rmask, a)) : rot(v, a);
                 if (r < best) {
                     best = r;
                     steps = 0;
@@ -351,6 +360,7 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     p.den = g.den;
     p.nd = nd;
     p.L1 = g.L1;
+    p.l1inv = (65536u + (unsigned)g.L1 - 1u) / (unsigned)g.L1;
     p.L2 = g.L2;
     p.w = g.w;
     p.rowbits = g.L1 * g.w;
@@ -362,13 +372,7 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     p.n_coupl = op->n_coupl;
     p.sb = s.sb;
     p.want_arg = g.den > 1 ? 1 : 0;
-    p.ds.dir = s.d_dir;
-    p.ds.nb = s.dir_nb;
-    p.ds.shift = s.dir_shift;
-    p.ds.mb = s.dir_shift + s.sb;
-    p.ds.K = s.dir_K;
-    p.ds.steps = s.dir_steps;
-    p.ds.sb = s.sb;
+    p.ds = dir_search_of(s);
     p.diag = B.d_diag;
     int gk = g.kind;
     p.pb = 0;
@@ -1259,14 +1263,10 @@ HxParams batch_params(edgpu_batch_s* b, int prec, const void* const* xs, void* c
         d[i].x = xs[i];
         d[i].y = ys[i];
         d[i].diag = o->blob[prec][0][0].d_diag;
-        d[i].dir = s.d_dir;
         d[i].n_rows = s.dim;
         tiles += (s.dim + rpw - 1) / rpw;
         d[i].tile_end = tiles;
-        d[i].nb = s.dir_nb;
-        d[i].shift = s.dir_shift;
-        d[i].K = s.dir_K;
-        d[i].steps = s.dir_steps;
+        d[i].ds = dir_search_of(s);
         d[i].o_ph = F.o_ph[i];
         d[i].o_num = F.o_num[i];
         d[i].want_arg = F.want_arg[i];

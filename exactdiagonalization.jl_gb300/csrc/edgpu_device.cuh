@@ -49,36 +49,92 @@ __device__ __forceinline__ void canon_torus(W q, int L1, int L2, int w, int rowb
     }
 }
 
-// Torus canonicalisation with top-row pruning (rows of rowbits <= 10 bits).  The numerically smallest
-// translate has the smallest possible top row, M = min over rows j of the smallest rotation of row j,
-// so only translates T(a,b) whose top row (row j = L2-1-b rotated by a) equals M can be the
-// representative.  rlut[v] = smallest rotation of the row value v (low 16 bits) | the set of rotation
-// steps a reaching it (high 16 bits).  Exact: ties are broken by comparing the whole words.
+// Torus canonicalisation with top-row pruning (rows of rowbits <= 10 bits, at most TORUS_MAXR rows).
+// The numerically smallest translate has the smallest possible top row, M = min over rows j of the
+// smallest rotation of row j, so only translates T(a,b) whose top row (row j = L2-1-b rotated by a)
+// equals M can be the representative.  rlut[v] = smallest rotation of the row value v (low 16 bits) |
+// the set of rotation steps a reaching it (high 16 bits).  The candidates (j, a) are collected into
+// one bit set (bit j*L1 + a) first, so the lanes of a warp loop over their own candidates only
+// (usually one or two) instead of over the rows.  Exact: candidates are compared as whole words.
+// l1inv = ceil(2^16 / L1): j = (c * l1inv) >> 16 for the candidate bit c < 64.
+
 template <typename W>
 __device__ __forceinline__ void canon_torus_pruned(W q, int L1, int L2, int w, int rowbits, int nbits, W full,
-                                                   const W* keep, const unsigned* rlut, W& rep, int& gbest) {
+                                                   const W* keep, const unsigned* rlut, unsigned l1inv, W& rep,
+                                                   int& gbest) {
     const unsigned rmask = (1u << rowbits) - 1u;
-    unsigned M = 0xffffffffu;
-    for (int j = 0; j < L2; ++j) M = min(M, rlut[(unsigned)(q >> (j * rowbits)) & rmask] & 0xffffu);
+    unsigned e[TORUS_MAXR];
+    unsigned M = 0xffffu;
+#pragma unroll
+    for (int j = 0; j < TORUS_MAXR; ++j) {
+        e[j] = (j < L2) ? rlut[(unsigned)(q >> (j * rowbits)) & rmask] : 0xffffffffu;
+        M = min(M, e[j] & 0xffffu);
+    }
+    unsigned long long cand = 0ull;
+#pragma unroll
+    for (int j = 0; j < TORUS_MAXR; ++j)
+        if ((e[j] & 0xffffu) == M) cand |= (unsigned long long)(e[j] >> 16) << (j * L1);
     rep = full;
     gbest = 0;
     bool first = true;
-    for (int j = 0; j < L2; ++j) {
-        const unsigned e = rlut[(unsigned)(q >> (j * rowbits)) & rmask];
-        if ((e & 0xffffu) != M) continue;
-        const int b = (L2 - 1 - j) % L2;
+    while (cand) {
+        const int c = __ffsll((long long)cand) - 1;
+        cand &= cand - 1ull;
+        const int j = (int)(((unsigned)c * l1inv) >> 16);
+        const int a = c - j * L1;
+        const int b = L2 - 1 - j;
         const int sh = b * rowbits;
         const W rb = sh ? (W)(((q << sh) | (q >> (nbits - sh))) & full) : q;
-        unsigned am = e >> 16;
-        while (am) {
-            const int a = __ffs((int)am) - 1;
-            am &= am - 1u;
-            const W t = torus_row_rotate<W>(rb, a * w, keep[a], full, rowbits);
-            if (first || t < rep) {
-                rep = t;
-                gbest = a + L1 * b;
-                first = false;
-            }
+        const W t = torus_row_rotate<W>(rb, a * w, keep[a], full, rowbits);
+        if (first || t < rep) {
+            rep = t;
+            gbest = a + L1 * b;
+            first = false;
+        }
+    }
+}
+
+// The same search with the two top rows: plut[(v_hi << rowbits) | v_lo] = the smallest of
+// rot_a(v_hi) << rowbits | rot_a(v_lo) over the row rotations a (low 16 bits) | the set of a reaching it
+// (high 16 bits), for rowbits <= 6.  A candidate (j, a) must give the smallest pair of top rows
+// (row j and the row below it, j-1 mod L2, rotated by a), which leaves far fewer ties than the top
+// row alone.
+template <typename W>
+__device__ __forceinline__ void canon_torus_pair(W q, int L1, int L2, int w, int rowbits, int nbits, W full,
+                                                 const W* keep, const unsigned* plut, unsigned l1inv, W& rep,
+                                                 int& gbest) {
+    const unsigned rmask = (1u << rowbits) - 1u;
+    unsigned v[TORUS_MAXR];
+#pragma unroll
+    for (int j = 0; j < TORUS_MAXR; ++j) v[j] = (j < L2) ? ((unsigned)(q >> (j * rowbits)) & rmask) : 0u;
+    const unsigned vtop = (unsigned)(q >> ((L2 - 1) * rowbits)) & rmask;
+    unsigned e[TORUS_MAXR];
+    unsigned M = 0xffffu;
+#pragma unroll
+    for (int j = 0; j < TORUS_MAXR; ++j) {
+        e[j] = (j < L2) ? plut[(v[j] << rowbits) | (j ? v[j > 0 ? j - 1 : 0] : vtop)] : 0xffffffffu;
+        M = min(M, e[j] & 0xffffu);
+    }
+    unsigned long long cand = 0ull;
+#pragma unroll
+    for (int j = 0; j < TORUS_MAXR; ++j)
+        if ((e[j] & 0xffffu) == M) cand |= (unsigned long long)(e[j] >> 16) << (j * L1);
+    rep = full;
+    gbest = 0;
+    bool first = true;
+    while (cand) {
+        const int c = __ffsll((long long)cand) - 1;
+        cand &= cand - 1ull;
+        const int j = (int)(((unsigned)c * l1inv) >> 16);
+        const int a = c - j * L1;
+        const int b = L2 - 1 - j;
+        const int sh = b * rowbits;
+        const W rb = sh ? (W)(((q << sh) | (q >> (nbits - sh))) & full) : q;
+        const W t = torus_row_rotate<W>(rb, a * w, keep[a], full, rowbits);
+        if (first || t < rep) {
+            rep = t;
+            gbest = a + L1 * b;
+            first = false;
         }
     }
 }
@@ -90,6 +146,18 @@ __device__ __forceinline__ void canon_torus_pruned(W q, int L1, int L2, int w, i
 __device__ __forceinline__ void canon_ring32(unsigned q, int n, int L1, int w, int pb, bool want_arg,
                                              unsigned& rep, int& gbest) {
     const unsigned mask = (n >= 32) ? 0xffffffffu : ((1u << n) - 1u);
+    if (!want_arg) {
+        // top-aligned rotations: X holds q twice from its top bit down, so the top 32 bits of X << s
+        // are rot_s(q) << (32 - n) followed by bits that only break ties between equal rotations
+        const unsigned long long X = ((unsigned long long)q << (64 - n)) | ((unsigned long long)q << (64 - 2 * n));
+        const unsigned lo = (unsigned)X, hi = (unsigned)(X >> 32);
+        unsigned best = 0xffffffffu;
+#pragma unroll 4
+        for (int a = 0; a < L1; ++a) best = min(best, __funnelshift_l(lo, hi, a * w));
+        rep = best >> (32 - n);
+        gbest = 0;
+        return;
+    }
     if (pb > 0) {
         const unsigned long long d = ((unsigned long long)q | ((unsigned long long)q << n)) << pb;
         const unsigned lo = (unsigned)d, hi = (unsigned)(d >> 32);
@@ -122,6 +190,16 @@ __device__ __forceinline__ void canon_ring32(unsigned q, int n, int L1, int w, i
 template <int N>
 __device__ __forceinline__ void canon_ring_n(unsigned q, int pb, bool want_arg, unsigned& rep, int& gbest) {
     const unsigned mask = (N >= 32) ? 0xffffffffu : ((1u << N) - 1u);
+    if (!want_arg) {   // top-aligned rotations (see canon_ring32): 2 instructions per element
+        const unsigned long long X = ((unsigned long long)q << (64 - N)) | ((unsigned long long)q << (64 - 2 * N));
+        const unsigned lo = (unsigned)X, hi = (unsigned)(X >> 32);
+        unsigned best = 0xffffffffu;
+#pragma unroll
+        for (int a = 0; a < N; ++a) best = min(best, __funnelshift_l(lo, hi, a));
+        rep = best >> (32 - N);
+        gbest = 0;
+        return;
+    }
     if (pb > 0) {
         const unsigned long long d = ((unsigned long long)q | ((unsigned long long)q << N)) << pb;
         const unsigned lo = (unsigned)d, hi = (unsigned)(d >> 32);
@@ -250,7 +328,6 @@ __device__ __forceinline__ long long key_find(const W* __restrict__ keys, long l
 template <typename W>
 __device__ __forceinline__ void key_find_sum2(const W* __restrict__ keys, const DirSearch& d, const W* rep,
                                               const bool* act, long long* c, int* sidx) {
-    const unsigned mbmask = (d.mb >= 32) ? 0xffffffffu : ((1u << d.mb) - 1u);
     const unsigned smask = (1u << d.sb) - 1u;
     unsigned long long e[2];
     unsigned bk[2];
@@ -268,14 +345,16 @@ __device__ __forceinline__ void key_find_sum2(const W* __restrict__ keys, const 
         const int cnt = (int)(hi & 15u);
         const unsigned field = hi >> 4;                                   // K members of mb bits
         const unsigned want = ((unsigned)rep[h] & ((1u << d.shift) - 1u)) << d.sb;   // member bits without sidx
-        unsigned hits = 0u;
-        for (int k = 0; k < d.K; ++k) hits |= (((field >> (k * d.mb)) & mbmask & ~smask) == want ? 1u : 0u) << k;
-        hits &= (1u << cnt) - 1u;                                         // only the bucket's members
+        // fields equal to want (state bits only) have all-zero x; the top bit of t marks nonzero fields
+        const unsigned x = (field ^ (want * d.unit)) & d.keybits;
+        const unsigned t = ((x & d.low) + d.low) | x;
         slow[h] = act[h] && cnt > d.K;
-        const int k0 = __ffs((int)hits) - 1;
-        const bool found = act[h] && !slow[h] && hits != 0u;
-        c[h] = found ? (long long)(start + (unsigned)k0) : -1;
-        sidx[h] = found ? (int)((field >> (k0 * d.mb)) & smask) : 0;
+        const unsigned valid = slow[h] ? 0u : (d.top & ((1u << (cnt * d.mb)) - 1u));   // the bucket's members
+        const unsigned hits = ~t & valid;
+        const int pos = __ffs((int)hits) - 1;                             // top bit of the first match
+        const bool found = act[h] && hits != 0u;
+        c[h] = found ? (long long)(start + (unsigned)__popc(d.top & ((1u << pos) - 1u))) : -1;
+        sidx[h] = found ? (int)((field >> (pos + 1 - d.mb)) & smask) : 0;
     }
     if (slow[0] || slow[1]) {   // buckets larger than K: search the keys
 #pragma unroll

@@ -134,12 +134,19 @@ void compute_diagonal(const Space& s, int T, const uint64_t* masks, const uint64
 void count_nnz(const Space& s, int T, const uint64_t* masks, const uint64_t* rows, const uint64_t* flips,
                int64_t* n_targets, int64_t* n_found, cudaStream_t st);
 
-// Search directory of a key table (bucket summaries; see key_find_sum2 in edgpu_device.cuh).
+constexpr int TORUS_MAXR = 8;      // most rows of a torus canonicalised with top-row pruning
+
+// Search directory of a key table (bucket summaries; see key_find_sum2 in edgpu_device.cuh) with the
+// constants of the in-register compare of a bucket's K member fields (mb bits each):
+// unit = 1 in the lowest bit of every field, keybits = the state bits of every field (above the sb
+// orbit-index bits), low = all but the top bit of every field, top = the top bit of every field.
 struct DirSearch {
     const unsigned long long* dir;
     long long nb;
     int shift, mb, K, steps, sb;
+    unsigned unit, keybits, low, top;
 };
+DirSearch dir_search_of(const Space& s);
 
 // ---- matrix-free product (hx*.cu) ----------------------------------------------------------------
 struct HxParams {
@@ -158,6 +165,8 @@ struct HxParams {
     const void* diag;                         // per-row diagonal element (V), product mode
     int o_ph, o_num, o_ratio, o_keep, o_lut, o_flip, o_grad;
     int o_rlut;                               // torus row table for top-row pruning, -1 when absent
+    unsigned l1inv;                           // ceil(2^16 / L1) (candidate bit -> row of the pruned torus search)
+    int rlut_pair;                            // the row table holds pairs of rows (rowbits <= 6)
     int T_o, T_d, G, den, nd;
     int L1, L2, w, rowbits, nbits, nchunks;
     int sb, pb, want_arg, lpr;
@@ -175,11 +184,10 @@ struct __align__(16) SectorDesc {
     const void* x;
     void* y;
     const void* diag;
-    const unsigned long long* dir;
     long long n_rows;
     long long tile_end;                       // cumulative warp tiles through this sector
-    long long nb;                             // directory buckets
-    int shift, K, steps, o_ph, o_num, want_arg, pad0, pad1;
+    DirSearch ds;
+    int o_ph, o_num, want_arg, pad0;
 };
 
 constexpr int HX_QCAP = 128;         // per-warp target queue capacity (entries; 2 batches of 32 + 31)

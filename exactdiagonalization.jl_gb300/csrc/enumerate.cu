@@ -973,6 +973,27 @@ void states_t(const Space& s, uint64_t* out_host, cudaStream_t st) {
 }
 }  // namespace
 
+DirSearch dir_search_of(const Space& s) {
+    DirSearch d{};
+    d.dir = s.d_dir;
+    d.nb = s.dir_nb;
+    d.shift = s.dir_shift;
+    d.mb = s.dir_shift + s.sb;
+    d.K = s.dir_K;
+    d.steps = s.dir_steps;
+    d.sb = s.sb;
+    const unsigned mbmask = d.mb >= 32 ? 0xffffffffu : ((1u << d.mb) - 1u);
+    const unsigned smask = (1u << d.sb) - 1u;
+    for (int k = 0; k < d.K; ++k) {
+        const int o = k * d.mb;
+        d.unit |= 1u << o;
+        d.keybits |= (mbmask & ~smask) << o;
+        d.low |= (mbmask >> 1) << o;
+        d.top |= (1u << (d.mb - 1)) << o;
+    }
+    return d;
+}
+
 void embed_orbit_index(Space& red, cudaStream_t st) {
     if (red.sb == 0 || red.dim == 0) return;
     if (red.w32) embed_t<uint32_t>(red, st);

@@ -109,8 +109,10 @@ __device__ __forceinline__ void canon_rep(W q, const HxParams& p, const W* keep,
         canon_ring((unsigned)q, p.nbits, p.L1, p.w, p.pb, p.want_arg != 0, r, g);
         rep = (W)r;
     } else if (GK == GK_TORUS) {
-        if (p.o_rlut >= 0) {
-            canon_torus_pruned<W>(q, p.L1, p.L2, p.w, p.rowbits, p.nbits, (W)p.full, keep, rlut, rep, g);
+        if (p.o_rlut >= 0 && p.rlut_pair) {
+            canon_torus_pair<W>(q, p.L1, p.L2, p.w, p.rowbits, p.nbits, (W)p.full, keep, rlut, p.l1inv, rep, g);
+        } else if (p.o_rlut >= 0) {
+            canon_torus_pruned<W>(q, p.L1, p.L2, p.w, p.rowbits, p.nbits, (W)p.full, keep, rlut, p.l1inv, rep, g);
         } else {
             int s;
             canon_torus<W>(q, p.L1, p.L2, p.w, p.rowbits, p.nbits, (W)p.full, keep, p.want_arg != 0, false, rep, g, s);

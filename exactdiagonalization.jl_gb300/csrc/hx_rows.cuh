@@ -234,13 +234,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_multi_kernel(const HxParams p) 
         sc.y = (V*)d.y;
         sc.diag = (const V*)d.diag;
         sc.n_rows = d.n_rows;
-        sc.ds.dir = d.dir;
-        sc.ds.nb = d.nb;
-        sc.ds.shift = d.shift;
-        sc.ds.mb = d.shift + p.sb;
-        sc.ds.K = d.K;
-        sc.ds.steps = d.steps;
-        sc.ds.sb = p.sb;
+        sc.ds = d.ds;
         sc.ph = (const V*)(sm + d.o_ph);
         sc.num = (const int*)(sm + d.o_num);
         sc.want_arg = d.want_arg != 0;
