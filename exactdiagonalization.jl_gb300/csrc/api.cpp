@@ -115,6 +115,9 @@ struct Blob {
 
 struct edgpu_space_s : public Space {};
 
+// Largest Krylov basis (bytes) the Lanczos driver stores; 0: half of the free device memory.
+int64_t g_krylov_limit = 0;
+
 struct edgpu_op_s {
     edgpu_space_s* space = nullptr;
     int T = 0;
@@ -228,6 +231,7 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     p.o_num = alloc(g.G * 4);
     p.o_ratio = alloc(nd * nd * rsz);
     p.o_keep = alloc(keep.size() * wsz);
+    p.o_keep32 = alloc(keep.size() * 4);
     p.o_lut = alloc(lut.size() * wsz);
     p.o_flip = alloc((g.kind == GK_GENERIC ? g.G : 0) * wsz);
     // torus row table: smallest rotation of every row value and the rotation steps reaching it
@@ -305,6 +309,10 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
             else { float ff = (float)f; memcpy(&h[p.o_ratio + (i * nd + j) * 4], &ff, 4); }
         }
     for (size_t i = 0; i < keep.size(); ++i) putw(p.o_keep, i, keep[i]);
+    for (size_t i = 0; i < keep.size(); ++i) {
+        const uint32_t k32 = (uint32_t)keep[i];
+        memcpy(&h[p.o_keep32 + i * 4], &k32, 4);
+    }
     if (use_rlut) {
         // smallest rotation of a row (or of a pair of rows: top row << rowbits | the row below it,
         // both rotated by the same a) and the rotations a reaching it
@@ -324,7 +332,8 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
                 }
                 if (r == best) steps |= 1u << a;
             }
-            const uint32_t e = best | (steps << 16);
+            // pair table: value in the high half so that one min finds the smallest pair
+            const uint32_t e = use_pair ? ((best << 16) | steps) : (best | (steps << 16));
             memcpy(&h[p.o_rlut + v * 4], &e, 4);
         }
     }
@@ -1464,116 +1473,204 @@ void edgpu_batch_destroy(edgpu_batch b) { delete b; }
 
 // ---- Lanczos -------------------------------------------------------------------------------------
 
+int edgpu_set_krylov_limit(int64_t bytes) {
+    API_BEGIN
+    require(bytes >= 0, EDGPU_ERR_ARG, "negative limit");
+    g_krylov_limit = bytes;
+    API_END
+}
+
 int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reorth, uint64_t seed, const double* v0,
                   int32_t refine, double tol, double* e0, double* alphas, double* betas, int32_t* steps_done,
                   double* ground_state) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
     check_prec(precision);
-    require(n_steps >= 1 && e0, EDGPU_ERR_ARG, "bad Lanczos arguments");
+    require(n_steps >= 1 && e0 && tol >= 0.0, EDGPU_ERR_ARG, "bad Lanczos arguments");
     const int64_t N = op->space->dim;
     require(N >= 1, EDGPU_ERR_ARG, "empty representation");
     cudaStream_t st = g_stream;
     const int m = (int)std::min<int64_t>(n_steps, N);
-    const bool keep_all = reorth || ground_state || (refine && precision == EDGPU_MIXED);
-    const int nvec = keep_all ? m + 1 : 2;
-    DevBuf<double> V, w, scal, scratch, h, md, psi;
-    DevBuf<float> v32, y32;
-    V.ensure((size_t)nvec * 2 * N);
-    w.ensure(2 * N);
+    const bool two_phase = refine && precision == EDGPU_MIXED;
+    const bool want_vec = ground_state != nullptr;
+
+    // Krylov basis storage of one run: rolling (two FP64 vectors), FP64 basis, or the complex64 product
+    // inputs of a mixed-precision run.  A basis is stored only when reorthogonalisation or a Ritz vector
+    // needs it and it fits under the Krylov limit; a Ritz vector of a rolling run is rebuilt by a second
+    // pass of the recurrence from the saved start vector (every kernel on the path is deterministic,
+    // so the pass regenerates the same vectors bit for bit).
+    enum Store { ROLL = 0, F64 = 1, F32 = 2 };
+    size_t free_b = 0, total_b = 0;
+    EDGPU_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const double limit = g_krylov_limit > 0 ? (double)g_krylov_limit : 0.5 * (double)free_b;
+    auto fits64 = [&](int k) { return (double)(k + 1) * (double)N * 16.0 <= limit; };
+    auto fits32 = [&](int k) { return (double)(k + 1) * (double)N * 8.0 <= limit; };
+
+    DevBuf<double> V64, w, scal, scratch, h, md, psi, vstart;
+    DevBuf<float> V32, y32;
     scal.ensure(8);
     scratch.ensure(dot_scratch_doubles());
     h.ensure(2 * (size_t)(m + 1));
     md.ensure(2 * (size_t)(m + 1) * 64);
-    if (precision == EDGPU_MIXED) {
-        v32.ensure(2 * N);
-        y32.ensure(2 * N);
-    }
+    w.ensure(2 * N);
     double* d_alpha = scal.p;      // [0]=re [1]=im of <v, w>
     double* d_beta = scal.p + 2;   // current beta
     double* d_bprev = scal.p + 3;  // previous beta
     double* d_tmp = scal.p + 4;
 
-    auto vec = [&](int j) { return V.p + (size_t)(keep_all ? j : (j & 1)) * 2 * N; };
+    // per-run layout
+    int cur_prec = precision, cur_store = ROLL, cur_cap = m;
+    bool cur_reorth = false;
+    auto vec64 = [&](int j) { return V64.p + (size_t)(cur_store == F64 ? j : (j & 1)) * 2 * N; };
+    auto vin32 = [&](int j) { return V32.p + (size_t)(cur_store == F32 ? j : 0) * 2 * N; };
+    auto setup = [&](int prec, int store, int cap, bool reo) {
+        cur_prec = prec;
+        cur_store = store;
+        cur_cap = cap;
+        cur_reorth = reo;
+        V64.ensure((size_t)(store == F64 ? cap + 1 : 2) * 2 * N);
+        if (prec == EDGPU_MIXED) {
+            V32.ensure((size_t)(store == F32 ? cap + 1 : 1) * 2 * N);
+            y32.ensure(2 * N);
+        }
+        if (store == ROLL) vstart.ensure(2 * N);
+    };
+    // vec64(0) <- src / |src| (and its complex64 copy); saved as the start vector of a rolling run
+    auto start_from = [&](const double* src_dev, const double* src_host) {
+        if (src_host) EDGPU_CUDA(cudaMemcpyAsync(vec64(0), src_host, N * 16, cudaMemcpyHostToDevice, st));
+        else if (src_dev) EDGPU_CUDA(cudaMemcpyAsync(vec64(0), src_dev, N * 16, cudaMemcpyDeviceToDevice, st));
+        else launch_random_c128(N, seed, vec64(0), st);
+        launch_norm2_c128(N, vec64(0), scratch.p, d_tmp, st);
+        launch_normalize(N, vec64(0), d_tmp, vec64(0), cur_prec == EDGPU_MIXED ? vin32(0) : nullptr, st);
+        if (cur_store == ROLL) EDGPU_CUDA(cudaMemcpyAsync(vstart.p, vec64(0), N * 16, cudaMemcpyDeviceToDevice, st));
+    };
 
-    // start vector
-    if (v0) EDGPU_CUDA(cudaMemcpyAsync(vec(0), v0, N * 16, cudaMemcpyHostToDevice, st));
-    else launch_random_c128(N, seed, vec(0), st);
-    launch_norm2_c128(N, vec(0), scratch.p, d_tmp, st);
-    launch_normalize(N, vec(0), d_tmp, vec(0), precision == EDGPU_MIXED ? v32.p : nullptr, st);
-
-    auto run = [&](int prec, int steps, int start_index, std::vector<double>& A, std::vector<double>& B) {
-        // Lanczos steps j = start_index .. steps-1 over the stored/rolling basis; fills A, B
-        double bprev = 0.0;
-        for (int j = start_index; j < steps; ++j) {
-            double* vj = vec(j);
-            if (prec == EDGPU_FP64) {
+    // Lanczos steps j = 0 .. steps-1 from vec64(0); fills A, B.  conv_tol > 0: stop once the lowest Ritz
+    // value moved by less than conv_tol |E| over the last 5 steps.  With acc: psi += acc[j] v_j only.
+    auto run = [&](int steps, double conv_tol, std::vector<double>& A, std::vector<double>& B,
+                   const std::vector<double>* acc) {
+        double e_prev = 0.0;
+        bool have_prev = false;
+        for (int j = 0; j < steps; ++j) {
+            double* vj = vec64(j);
+            if (acc) {
+                launch_axpy_real(N, (*acc)[j], vj, psi.p, st);
+                if (j + 1 >= (int)acc->size()) break;
+            }
+            if (cur_prec == EDGPU_FP64) {
                 launch_product(op, EDGPU_FP64, 0, 0, vj, w.p, 0, nullptr, nullptr, st);
             } else {
-                launch_product(op, EDGPU_MIXED, 0, 0, v32.p, y32.p, 0, nullptr, nullptr, st);
+                launch_product(op, EDGPU_MIXED, 0, 0, vin32(j), y32.p, 0, nullptr, nullptr, st);
                 launch_c64_to_c128(N, y32.p, w.p, 0, st);
             }
             launch_dot_c128(N, vj, w.p, scratch.p, d_alpha, st);
-            launch_lanczos_update(N, w.p, vj, j > start_index ? vec(j - 1) : nullptr, d_alpha,
-                                  j > start_index ? d_bprev : nullptr, st);
-            if (reorth) {
+            launch_lanczos_update(N, w.p, vj, j > 0 ? vec64(j - 1) : nullptr, d_alpha, j > 0 ? d_bprev : nullptr, st);
+            if (cur_reorth) {
                 for (int pass = 0; pass < 2; ++pass) {
-                    launch_multi_dot(N, j + 1, V.p, N, w.p, md.p, h.p, st);
-                    launch_multi_axpy(N, j + 1, V.p, N, h.p, w.p, st);
+                    if (cur_store == F64) {
+                        launch_multi_dot(N, j + 1, V64.p, N, w.p, md.p, h.p, st);
+                        launch_multi_axpy(N, j + 1, V64.p, N, h.p, w.p, st);
+                    } else {
+                        launch_multi_dot_c64(N, j + 1, V32.p, N, w.p, md.p, h.p, st);
+                        launch_multi_axpy_c64(N, j + 1, V32.p, N, h.p, w.p, st);
+                    }
                 }
             }
             launch_norm2_c128(N, w.p, scratch.p, d_beta, st);
-            double hb[3];
+            double hb[2];
             EDGPU_CUDA(cudaMemcpyAsync(hb, d_alpha, sizeof(double), cudaMemcpyDeviceToHost, st));
             EDGPU_CUDA(cudaMemcpyAsync(hb + 1, d_beta, sizeof(double), cudaMemcpyDeviceToHost, st));
             EDGPU_CUDA(cudaStreamSynchronize(st));
             A.push_back(hb[0]);
             const double beta = hb[1];
             if (j == steps - 1 || beta <= 1e-12 * std::max(1.0, std::fabs(hb[0]))) break;
+            if (conv_tol > 0.0 && !acc && (j + 1) % 5 == 0) {
+                const double e = lowest_eigenvalue(A, B);
+                if (have_prev && std::fabs(e - e_prev) < conv_tol * std::max(1.0, std::fabs(e))) break;
+                e_prev = e;
+                have_prev = true;
+            }
             B.push_back(beta);
-            launch_normalize(N, w.p, d_beta, vec(j + 1), precision == EDGPU_MIXED ? v32.p : nullptr, st);
+            launch_normalize(N, w.p, d_beta, vec64(j + 1), cur_prec == EDGPU_MIXED ? vin32(j + 1) : nullptr, st);
             EDGPU_CUDA(cudaMemcpyAsync(d_bprev, d_beta, sizeof(double), cudaMemcpyDeviceToDevice, st));
-            bprev = beta;
         }
-        (void)bprev;
+    };
+    auto lowest = [&](const std::vector<double>& A, const std::vector<double>& B) {
+        return lowest_eigenvalue(A, std::vector<double>(B.begin(), B.begin() + (A.size() - 1)));
+    };
+    // psi = sum_k s_k v_k for the lowest eigenvector s of the current run's tridiagonal matrix
+    auto ritz_vector = [&](const std::vector<double>& A, const std::vector<double>& B, double lam) {
+        std::vector<double> s = tridiag_eigvec(A, std::vector<double>(B.begin(), B.begin() + (A.size() - 1)), lam);
+        psi.ensure(2 * N);
+        EDGPU_CUDA(cudaMemsetAsync(psi.p, 0, N * 16, st));
+        if (cur_store == ROLL) {
+            EDGPU_CUDA(cudaMemcpyAsync(vec64(0), vstart.p, N * 16, cudaMemcpyDeviceToDevice, st));
+            if (cur_prec == EDGPU_MIXED) launch_c128_to_c64(N, vec64(0), vin32(0), st);
+            std::vector<double> A2, B2;
+            run((int)s.size(), 0.0, A2, B2, &s);
+        } else {
+            std::vector<double> coef(2 * s.size());
+            for (size_t k = 0; k < s.size(); ++k) {
+                coef[2 * k] = -s[k];
+                coef[2 * k + 1] = 0.0;
+            }
+            EDGPU_CUDA(cudaMemcpyAsync(h.p, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+            if (cur_store == F64) launch_multi_axpy(N, (int)s.size(), V64.p, N, h.p, psi.p, st);
+            else launch_multi_axpy_c64(N, (int)s.size(), V32.p, N, h.p, psi.p, st);
+        }
+        EDGPU_CUDA(cudaStreamSynchronize(st));
     };
 
     std::vector<double> A, B;
-    run(precision, m, 0, A, B);
-    double E = lowest_eigenvalue(A, std::vector<double>(B.begin(), B.begin() + (A.size() - 1)));
-    int done = (int)A.size();
-
-    auto ritz_vector = [&](const std::vector<double>& AA, const std::vector<double>& BB, double lam) {
-        std::vector<double> s = tridiag_eigvec(AA, std::vector<double>(BB.begin(), BB.begin() + (AA.size() - 1)), lam);
-        psi.ensure(2 * N);
-        EDGPU_CUDA(cudaMemsetAsync(psi.p, 0, N * 16, st));
-        std::vector<double> coef(2 * s.size());
-        for (size_t k = 0; k < s.size(); ++k) {
-            coef[2 * k] = -s[k];
-            coef[2 * k + 1] = 0.0;
+    double E = 0.0;
+    int done = 0;
+    if (!two_phase) {
+        int store = ROLL;
+        if (reorth || want_vec) {
+            if (fits64(m)) store = F64;
+            else if (precision == EDGPU_MIXED && fits32(m)) store = F32;
         }
-        EDGPU_CUDA(cudaMemcpyAsync(h.p, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-        launch_multi_axpy(N, (int)s.size(), V.p, N, h.p, psi.p, st);   // psi = sum_k s_k v_k
-    };
-
-    if (refine && precision == EDGPU_MIXED && keep_all) {
-        // polish: FP64 Lanczos restarted from the mixed-precision Ritz vector until |dE| < tol
-        for (int round = 0; round < 8; ++round) {
-            ritz_vector(A, B, E);
-            EDGPU_CUDA(cudaMemcpyAsync(vec(0), psi.p, N * 16, cudaMemcpyDeviceToDevice, st));
-            launch_norm2_c128(N, vec(0), scratch.p, d_tmp, st);
-            launch_normalize(N, vec(0), d_tmp, vec(0), nullptr, st);
-            std::vector<double> A2, B2;
-            const int m2 = std::min(m, 40);
-            run(EDGPU_FP64, m2, 0, A2, B2);
-            const double E2 = lowest_eigenvalue(A2, std::vector<double>(B2.begin(), B2.begin() + (A2.size() - 1)));
-            done += (int)A2.size();
-            const double dE = std::fabs(E2 - E);
-            A = A2;
-            B = B2;
-            E = E2;
-            if (dE < tol * std::max(1.0, std::fabs(E2))) break;
+        require(!reorth || store != ROLL, EDGPU_ERR_OOM,
+                "the Krylov basis for full reorthogonalisation does not fit in device memory (" +
+                    std::to_string((long long)((m + 1) * N * (precision == EDGPU_MIXED ? 8 : 16) >> 20)) +
+                    " MiB); use reorth = 0");
+        setup(precision, store, m, reorth != 0);
+        start_from(nullptr, v0);
+        run(m, tol, A, B, nullptr);
+        E = lowest(A, B);
+        done = (int)A.size();
+    } else {
+        // 1. mixed-precision Lanczos to about 1e-7 with a stored basis (FP64, else complex64, capped by
+        //    the Krylov limit), or rolling with a second pass for the Ritz vector
+        int store = ROLL, m1 = m;
+        if (fits64(m)) store = F64;
+        else if (fits32(m)) store = F32;
+        else {
+            int cap = 0;
+            while (cap < m && fits32(cap + 1)) ++cap;
+            if (cap >= 40 && !reorth) {
+                store = F32;
+                m1 = cap;
+            }
         }
+        require(!reorth || store != ROLL, EDGPU_ERR_OOM,
+                "the Krylov basis for full reorthogonalisation does not fit in device memory; use reorth = 0");
+        setup(EDGPU_MIXED, store, m1, reorth != 0);
+        start_from(nullptr, v0);
+        run(m1, std::max(tol, 1e-7), A, B, nullptr);
+        E = lowest(A, B);
+        done = (int)A.size();
+        ritz_vector(A, B, E);
+        // 2. FP64 Lanczos from the mixed-precision Ritz vector until the eigenvalue settles to tol
+        const bool store2 = (reorth || want_vec) && fits64(m);
+        setup(EDGPU_FP64, store2 ? F64 : ROLL, m, reorth != 0 && store2);
+        start_from(psi.p, nullptr);
+        std::vector<double> A2, B2;
+        run(m, tol, A2, B2, nullptr);
+        A = A2;
+        B = B2;
+        E = lowest(A, B);
+        done += (int)A.size();
     }
     *e0 = E;
     if (alphas)

@@ -94,48 +94,82 @@ __device__ __forceinline__ void canon_torus_pruned(W q, int L1, int L2, int w, i
     }
 }
 
-// The same search with the two top rows: plut[(v_hi << rowbits) | v_lo] = the smallest of
-// rot_a(v_hi) << rowbits | rot_a(v_lo) over the row rotations a (low 16 bits) | the set of a reaching it
-// (high 16 bits), for rowbits <= 6.  A candidate (j, a) must give the smallest pair of top rows
-// (row j and the row below it, j-1 mod L2, rotated by a), which leaves far fewer ties than the top
-// row alone.
-template <typename W>
-__device__ __forceinline__ void canon_torus_pair(W q, int L1, int L2, int w, int rowbits, int nbits, W full,
-                                                 const W* keep, const unsigned* plut, unsigned l1inv, W& rep,
-                                                 int& gbest) {
+// The same search with the two top rows (rowbits <= 6, so L1 <= 6): plut[(v_hi << rowbits) | v_lo] =
+// the smallest of rot_a(v_hi) << rowbits | rot_a(v_lo) over the row rotations a (high 16 bits) | the
+// set of a reaching it (low 8 bits).  A candidate (j, a) must give the smallest pair of top rows (row
+// j and the row below it, j-1 mod L2, rotated by a), which leaves far fewer ties than the top row
+// alone.  Rows are peeled off 32-bit halves by funnel shifts, candidates sit in 8-bit slots (bit
+// 8*j + a of clo:chi), and states of at most 32 bits are translated in 32-bit arithmetic.
+template <typename S>
+__device__ __forceinline__ void torus_pair_search(S q, int L1, int L2, int w, int rowbits, int nbits, S full,
+                                                  const S* keep, const unsigned* plut, S& rep, int& gbest) {
     const unsigned rmask = (1u << rowbits) - 1u;
+    unsigned lo = (unsigned)q, hi = sizeof(S) == 8 ? (unsigned)((unsigned long long)q >> 32) : 0u;
     unsigned v[TORUS_MAXR];
 #pragma unroll
-    for (int j = 0; j < TORUS_MAXR; ++j) v[j] = (j < L2) ? ((unsigned)(q >> (j * rowbits)) & rmask) : 0u;
+    for (int j = 0; j < TORUS_MAXR; ++j) {
+        v[j] = lo & rmask;
+        lo = __funnelshift_r(lo, hi, rowbits);
+        hi >>= rowbits;
+    }
     const unsigned vtop = (unsigned)(q >> ((L2 - 1) * rowbits)) & rmask;
     unsigned e[TORUS_MAXR];
-    unsigned M = 0xffffu;
+    unsigned Mf = 0xffffffffu;
 #pragma unroll
     for (int j = 0; j < TORUS_MAXR; ++j) {
         e[j] = (j < L2) ? plut[(v[j] << rowbits) | (j ? v[j > 0 ? j - 1 : 0] : vtop)] : 0xffffffffu;
-        M = min(M, e[j] & 0xffffu);
+        Mf = min(Mf, e[j]);
     }
-    unsigned long long cand = 0ull;
+    unsigned clo = 0u, chi = 0u;
 #pragma unroll
-    for (int j = 0; j < TORUS_MAXR; ++j)
-        if ((e[j] & 0xffffu) == M) cand |= (unsigned long long)(e[j] >> 16) << (j * L1);
+    for (int j = 0; j < TORUS_MAXR; ++j) {
+        const unsigned st = ((e[j] ^ Mf) < 0x10000u) ? (e[j] & 0xffu) : 0u;
+        if (j < 4) clo |= st << (8 * j);
+        else chi |= st << (8 * (j - 4));
+    }
+    // row-cyclic rotations of a state of at most 32 bits come from one funnel shift of q | q << nbits
+    unsigned dlo = 0u, dhi = 0u;
+    if constexpr (sizeof(S) == 4) {
+        const unsigned long long d = (unsigned long long)q | ((unsigned long long)q << nbits);
+        dlo = (unsigned)d;
+        dhi = (unsigned)(d >> 32);
+    }
     rep = full;
     gbest = 0;
     bool first = true;
-    while (cand) {
-        const int c = __ffsll((long long)cand) - 1;
-        cand &= cand - 1ull;
-        const int j = (int)(((unsigned)c * l1inv) >> 16);
-        const int a = c - j * L1;
+    while ((clo | chi) != 0u) {
+        const bool use_lo = clo != 0u;
+        unsigned x = use_lo ? clo : chi;
+        const int c = __ffs((int)x) - 1 + (use_lo ? 0 : 32);
+        x &= x - 1u;
+        clo = use_lo ? x : clo;
+        chi = use_lo ? chi : x;
+        const int j = c >> 3, a = c & 7;
         const int b = L2 - 1 - j;
         const int sh = b * rowbits;
-        const W rb = sh ? (W)(((q << sh) | (q >> (nbits - sh))) & full) : q;
-        const W t = torus_row_rotate<W>(rb, a * w, keep[a], full, rowbits);
+        S rb;
+        if constexpr (sizeof(S) == 4) rb = (S)(__funnelshift_r(dlo, dhi, nbits - sh) & (unsigned)full);
+        else rb = sh ? (S)(((q << sh) | (q >> (nbits - sh))) & full) : q;
+        const S t = torus_row_rotate<S>(rb, a * w, keep[a], full, rowbits);
         if (first || t < rep) {
             rep = t;
             gbest = a + L1 * b;
             first = false;
         }
+    }
+}
+
+template <typename W>
+__device__ __forceinline__ void canon_torus_pair(W q, int L1, int L2, int w, int rowbits, int nbits, W full,
+                                                 const W* keep32, const W* keep, const unsigned* plut, W& rep,
+                                                 int& gbest) {
+    if (sizeof(W) == 8 && nbits <= 32) {   // 64-bit keys, 32-bit states: canonicalise in 32 bits
+        unsigned r;
+        torus_pair_search<unsigned>((unsigned)q, L1, L2, w, rowbits, nbits, (unsigned)full, (const unsigned*)keep32,
+                                    plut, r, gbest);
+        rep = (W)r;
+    } else {
+        torus_pair_search<W>(q, L1, L2, w, rowbits, nbits, full, keep, plut, rep, gbest);
     }
 }
 

@@ -167,6 +167,7 @@ struct HxParams {
     int o_rlut;                               // torus row table for top-row pruning, -1 when absent
     unsigned l1inv;                           // ceil(2^16 / L1) (candidate bit -> row of the pruned torus search)
     int rlut_pair;                            // the row table holds pairs of rows (rowbits <= 6)
+    int o_keep32;                             // the torus keep masks as 32-bit words (states of <= 32 bits)
     int T_o, T_d, G, den, nd;
     int L1, L2, w, rowbits, nbits, nchunks;
     int sb, pb, want_arg, lpr;
@@ -242,6 +243,11 @@ void launch_multi_dot(int64_t n, int k, const double* V, int64_t ldv, const doub
                       double* h_dev, cudaStream_t st);
 void launch_multi_axpy(int64_t n, int k, const double* V, int64_t ldv, const double* h_dev, double* w,
                        cudaStream_t st);
+// the same with a complex64 basis V (FP64 accumulation)
+void launch_multi_dot_c64(int64_t n, int k, const float* V, int64_t ldv, const double* w, double* scratch,
+                          double* h_dev, cudaStream_t st);
+void launch_multi_axpy_c64(int64_t n, int k, const float* V, int64_t ldv, const double* h_dev, double* w,
+                           cudaStream_t st);
 // v_next = w / beta (beta device scalar); also writes a complex64 copy when v32 != null
 void launch_normalize(int64_t n, const double* w, const double* beta_dev, double* v_next, float* v32,
                       cudaStream_t st);

@@ -100,7 +100,7 @@ __host__ __device__ constexpr int hx_warp_bytes_t() {
 // Orbit minimum of q and the element reaching it, for each group kind.
 template <typename W, int GK>
 __device__ __forceinline__ void canon_rep(W q, const HxParams& p, const W* keep, const W* lut, const W* flips,
-                                          const unsigned* rlut, W& rep, int& g) {
+                                          const unsigned* rlut, const unsigned* keep32, W& rep, int& g) {
     if (GK == GK_TRIVIAL) {
         rep = q;
         g = 0;
@@ -110,7 +110,7 @@ __device__ __forceinline__ void canon_rep(W q, const HxParams& p, const W* keep,
         rep = (W)r;
     } else if (GK == GK_TORUS) {
         if (p.o_rlut >= 0 && p.rlut_pair) {
-            canon_torus_pair<W>(q, p.L1, p.L2, p.w, p.rowbits, p.nbits, (W)p.full, keep, rlut, p.l1inv, rep, g);
+            canon_torus_pair<W>(q, p.L1, p.L2, p.w, p.rowbits, p.nbits, (W)p.full, (const W*)keep32, keep, rlut, rep, g);
         } else if (p.o_rlut >= 0) {
             canon_torus_pruned<W>(q, p.L1, p.L2, p.w, p.rowbits, p.nbits, (W)p.full, keep, rlut, p.l1inv, rep, g);
         } else {
@@ -154,6 +154,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_kernel(const HxParams p) {
     const W* lut = (const W*)(sm + p.o_lut);
     const W* flips = (const W*)(sm + p.o_flip);
     const unsigned* rlut = (const unsigned*)(sm + (p.o_rlut >= 0 ? p.o_rlut : 0));
+    const unsigned* keep32 = (const unsigned*)(sm + p.o_keep32);
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
     unsigned char* ws = sm + p.warp_base + warp * hx_warp_bytes_t<W>();
@@ -204,7 +205,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_kernel(const HxParams p) {
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             rep[h] = q[h];
-            if (act[h]) canon_rep<W, GK>(q[h], p, keep, lut, flips, rlut, rep[h], g[h]);
+            if (act[h]) canon_rep<W, GK>(q[h], p, keep, lut, flips, rlut, keep32, rep[h], g[h]);
         }
         int sx[2];
         key_find_sum2<W>(keys, p.ds, rep, act, c, sx);

@@ -26,6 +26,7 @@ struct RowsTables {
     const double2 *da, *du;
     const R* ratio;
     const unsigned* rlut;
+    const unsigned* keep32;
     __device__ __forceinline__ RowsTables(const HxParams& p, const unsigned char* sm) {
         orec = (const W*)(sm + p.o_om);
         oa = (const V*)(sm + p.o_oa);
@@ -41,6 +42,7 @@ struct RowsTables {
         lut = (const W*)(sm + p.o_lut);
         flips = (const W*)(sm + p.o_flip);
         rlut = (const unsigned*)(sm + (p.o_rlut >= 0 ? p.o_rlut : 0));
+        keep32 = (const unsigned*)(sm + p.o_keep32);
     }
 };
 
@@ -123,7 +125,7 @@ __device__ __forceinline__ void rows_tile(const HxParams& p, const RowsTables<W,
                 q[h] = b ^ tf;
                 rep[h] = q[h];
                 g[h] = 0;
-                if (on[h]) canon_rep<W, GK>(q[h], p, tb.keep, tb.lut, tb.flips, tb.rlut, rep[h], g[h]);
+                if (on[h]) canon_rep<W, GK>(q[h], p, tb.keep, tb.lut, tb.flips, tb.rlut, tb.keep32, rep[h], g[h]);
             }
             int sx[2];
             key_find_sum2<W>(keys, sc.ds, rep, on, c, sx);

@@ -192,6 +192,35 @@ __global__ void k_multi_axpy(long long n, int K, const double2* V, long long ldv
     }
 }
 
+// The same over a complex64 basis (the stored Krylov basis of a mixed-precision run).
+__global__ void k_multi_dot_stage1_c64(long long n, const float2* V, long long ldv, const double2* w, double2* partial) {
+    __shared__ double2 sh[32];
+    const int k = blockIdx.y;
+    const float2* vk = V + (size_t)k * ldv;
+    double2 s = make_double2(0.0, 0.0);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 u = vk[i];
+        const double2 v = w[i];
+        s.x += (double)u.x * v.x + (double)u.y * v.y;
+        s.y += (double)u.x * v.y - (double)u.y * v.x;
+    }
+    const double2 r = block_sum2(s, sh);
+    if (threadIdx.x == 0) partial[(size_t)k * gridDim.x + blockIdx.x] = r;
+}
+
+__global__ void k_multi_axpy_c64(long long n, int K, const float2* V, long long ldv, const double2* h, double2* w) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double2 x = w[i];
+        for (int k = 0; k < K; ++k) {
+            const double2 c = h[k];
+            const float2 u = V[(size_t)k * ldv + i];
+            x.x -= c.x * (double)u.x - c.y * (double)u.y;
+            x.y -= c.x * (double)u.y + c.y * (double)u.x;
+        }
+        w[i] = x;
+    }
+}
+
 __global__ void k_normalize(long long n, const double2* w, const double* beta, double2* v, float2* v32) {
     const double inv = 1.0 / beta[0];
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -284,6 +313,22 @@ void launch_multi_dot(int64_t n, int k, const double* V, int64_t ldv, const doub
 void launch_multi_axpy(int64_t n, int k, const double* V, int64_t ldv, const double* h_dev, double* w, cudaStream_t st) {
     if (k <= 0 || n <= 0) return;
     k_multi_axpy<<<grid_for(n), 256, 0, st>>>(n, k, (const double2*)V, ldv, (const double2*)h_dev, (double2*)w);
+    EDGPU_CUDA(cudaGetLastError());
+}
+
+void launch_multi_dot_c64(int64_t n, int k, const float* V, int64_t ldv, const double* w, double* scratch, double* h_dev,
+                          cudaStream_t st) {
+    if (k <= 0) return;
+    dim3 grid(MD_BLOCKS, k);
+    k_multi_dot_stage1_c64<<<grid, RED_THREADS, 0, st>>>(n, (const float2*)V, ldv, (const double2*)w, (double2*)scratch);
+    k_multi_dot_stage2<<<k, 64, 0, st>>>(MD_BLOCKS, (const double2*)scratch, (double2*)h_dev);
+    EDGPU_CUDA(cudaGetLastError());
+}
+
+void launch_multi_axpy_c64(int64_t n, int k, const float* V, int64_t ldv, const double* h_dev, double* w,
+                           cudaStream_t st) {
+    if (k <= 0 || n <= 0) return;
+    k_multi_axpy_c64<<<grid_for(n), 256, 0, st>>>(n, k, (const float2*)V, ldv, (const double2*)h_dev, (double2*)w);
     EDGPU_CUDA(cudaGetLastError());
 }
 

@@ -13,6 +13,6 @@ from .representation import (Batch, DirectProductOperation, GlobalBitFlip, Hilbe
                              OperatorRepresentation, ReducedHilbertSpaceRepresentation, SitePermutation,
                              apply_, coupling_grad, dimension, mul_, mul_adjoint_, random_state, represent, search_stats,
                              symmetry_apply, symmetry_reduce, symmetry_unreduce, translation_symops)
-from .lanczos import LanczosResult, lanczos
+from .lanczos import LanczosResult, lanczos, set_krylov_limit
 
 lib()   # fail loudly at import when libedgpu.so is missing

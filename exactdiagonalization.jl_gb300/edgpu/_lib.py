@@ -80,6 +80,7 @@ SIGNATURES = {
     "edgpu_batch_destroy": (None, [vp]),
     "edgpu_lanczos": (ctypes.c_int, [vp, i32, i32, i32, u64, P(dbl), i32, dbl, P(dbl), P(dbl), P(dbl), P(i32),
                                      P(dbl)]),
+    "edgpu_set_krylov_limit": (ctypes.c_int, [ctypes.c_int64]),
     "edgpu_random_vector_device": (ctypes.c_int, [i64, u64, i32, vp, vp]),
     "edgpu_sync": (ctypes.c_int, []),
     "edgpu_host_alloc": (ctypes.c_int, [i64, P(vp)]),

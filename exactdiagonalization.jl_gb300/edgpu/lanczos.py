@@ -3,8 +3,11 @@ dense eigvals or an external Arpack.eigs that calls mul! repeatedly, docs/src/ex
 
 FP64 throughout for the scalars, dot products, norms, reorthogonalisation and the tridiagonal
 eigensolve; `precision` selects the product (fp64, or mixed: complex64 vectors and FP32
-accumulation).  With refine=True a mixed-precision run is polished by FP64 Lanczos steps restarted
-from its Ritz vector until |dE| < tol * |E|.
+accumulation).  tol > 0 stops a run once the lowest Ritz value moved by less than tol |E| over five
+steps.  With refine=True a mixed-precision run to about 1e-7 is followed by FP64 Lanczos from its Ritz
+vector until the eigenvalue settles to tol.  The Krylov basis is kept only when reorthogonalisation
+or a Ritz vector needs it and it fits (see set_krylov_limit); otherwise a Ritz vector is rebuilt by a
+second pass of the recurrence.
 """
 from __future__ import annotations
 
@@ -42,3 +45,9 @@ def lanczos(opr: OperatorRepresentation, n_steps: int = 200, precision="fp64", r
                               ptr(be, ctypes.c_double), ctypes.byref(done),
                               ptr(gs.view(np.float64), ctypes.c_double) if gs is not None else None))
     return LanczosResult(float(e0.value), al, be, int(done.value), gs)
+
+
+def set_krylov_limit(nbytes: int) -> None:
+    """Largest Krylov basis (bytes) the Lanczos driver stores; 0 restores the default (half of the free
+    device memory).  Below it, Ritz vectors are rebuilt by a second pass of the recurrence."""
+    check(lib().edgpu_set_krylov_limit(int(nbytes)))

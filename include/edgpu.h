@@ -202,15 +202,24 @@ int edgpu_batch_mul_device(edgpu_batch b, int32_t precision, const void* const* 
 void edgpu_batch_destroy(edgpu_batch b);
 
 /* ---- Lanczos driver ---------------------------------------------------------------------- */
-/* Lowest eigenvalue by Lanczos on the device: n_steps steps from a seeded complex Gaussian start
- * vector (or v0, host complex128 of length dim, if not NULL), full FP64 reorthogonalisation when
+/* Lowest eigenvalue by Lanczos on the device: at most n_steps steps from a seeded complex Gaussian
+ * start vector (or v0, host complex128 of length dim, if not NULL), full reorthogonalisation when
  * reorth != 0.  Scalars, dots, norms and the tridiagonal eigensolve are FP64; precision selects the
- * product.  With refine != 0 and EDGPU_MIXED, the mixed-precision Ritz vector is rebuilt and
- * polished by FP64 Lanczos steps until |dE| < tol.  Outputs: e0, alphas/betas (n_steps each,
- * nullable), steps_done.  ground_state (nullable, host complex128 dim): Ritz vector. */
+ * product.  tol > 0 stops once the lowest Ritz value moved by less than tol |E| over 5 steps.  With
+ * refine != 0 and EDGPU_MIXED: a mixed-precision run to about 1e-7, then FP64 Lanczos from its Ritz
+ * vector until the eigenvalue settles to tol.  Outputs: e0, alphas/betas of the last run (n_steps
+ * each, nullable), steps_done (all runs).  ground_state (nullable, host complex128 dim): Ritz vector.
+ * The Krylov basis is stored (FP64, or the complex64 product inputs of a mixed run) only when
+ * reorthogonalisation or a Ritz vector needs it and it fits under the Krylov limit (EDGPU_ERR_OOM when
+ * reorthogonalisation cannot be stored); otherwise two vectors roll and a Ritz vector costs a second
+ * pass of the recurrence.  No reference counterpart: the reference leaves eigensolvers to dense
+ * eigvals or Arpack (docs/src/examples/spinhalf.md:26). */
 int edgpu_lanczos(edgpu_op op, int32_t precision, int32_t n_steps, int32_t reorth, uint64_t seed,
                   const double* v0, int32_t refine, double tol, double* e0, double* alphas, double* betas,
                   int32_t* steps_done, double* ground_state);
+/* Largest Krylov basis in bytes that edgpu_lanczos may store (0, the default: half of the free device
+ * memory at the call). */
+int edgpu_set_krylov_limit(int64_t bytes);
 
 /* ---- utilities --------------------------------------------------------------------------- */
 /* Seeded complex Gaussian vector (SplitMix64 + Box-Muller, (g1 + i g2)/sqrt(2), normalised in FP64)

@@ -49,6 +49,29 @@ def test_lanczos_e0_matches_dense(edgpu):
     assert np.linalg.norm(hpsi - e_dense * psi) < 1e-6
 
 
+def test_lanczos_without_stored_basis(edgpu):
+    """Ritz vectors rebuilt by a second pass of the recurrence (Krylov basis not stored) equal the
+    stored-basis ones; mixed precision polished in FP64 reaches the FP64 eigenvalue."""
+    _, rh, opr = chain_op(edgpu, 20)
+    ref = edgpu.lanczos(opr, 90, precision="fp64", reorth=False, seed=3, want_vector=True)
+    ref_mx = edgpu.lanczos(opr, 90, precision="mixed", reorth=False, seed=3, want_vector=True)
+    try:
+        edgpu.set_krylov_limit(1)          # nothing fits: rolling vectors, two-pass Ritz vectors
+        lean = edgpu.lanczos(opr, 90, precision="fp64", reorth=False, seed=3, want_vector=True)
+        lean_mx = edgpu.lanczos(opr, 90, precision="mixed", reorth=False, seed=3, want_vector=True)
+        pol = edgpu.lanczos(opr, 90, precision="mixed", reorth=False, seed=3, refine=True, tol=1e-12)
+        with pytest.raises(MemoryError):
+            edgpu.lanczos(opr, 90, precision="fp64", reorth=True, seed=3)
+    finally:
+        edgpu.set_krylov_limit(0)
+    assert lean.e0 == ref.e0 and lean.steps == ref.steps
+    assert np.array_equal(lean.alphas, ref.alphas)
+    assert np.linalg.norm(lean.ground_state - ref.ground_state) < 1e-10
+    assert lean_mx.e0 == ref_mx.e0
+    assert np.linalg.norm(lean_mx.ground_state - ref_mx.ground_state) < 1e-10
+    assert abs(pol.e0 - ref.e0) < 1e-11 * abs(ref.e0)
+
+
 def test_lanczos_chain24_k0_known_energy(edgpu):
     # E0 of the L=24 Heisenberg chain (J=1, S=1/2 spins, H = sum S.S) in the k=0 sector
     _, rh, opr = chain_op(edgpu, 24)
