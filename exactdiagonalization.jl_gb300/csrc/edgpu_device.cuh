@@ -100,29 +100,33 @@ __device__ __forceinline__ void canon_torus_pruned(W q, int L1, int L2, int w, i
 // j and the row below it, j-1 mod L2, rotated by a), which leaves far fewer ties than the top row
 // alone.  Rows are peeled off 32-bit halves by funnel shifts, candidates sit in 8-bit slots (bit
 // 8*j + a of clo:chi), and states of at most 32 bits are translated in 32-bit arithmetic.
-template <typename S>
+// R = the number of rows L2 when it is known at compile time (R == L2), else TORUS_MAXR with the rows
+// beyond L2 masked off.
+template <typename S, int R>
 __device__ __forceinline__ void torus_pair_search(S q, int L1, int L2, int w, int rowbits, int nbits, S full,
                                                   const S* keep, const unsigned* plut, S& rep, int& gbest) {
+    const bool exact = R < TORUS_MAXR;
     const unsigned rmask = (1u << rowbits) - 1u;
     unsigned lo = (unsigned)q, hi = sizeof(S) == 8 ? (unsigned)((unsigned long long)q >> 32) : 0u;
-    unsigned v[TORUS_MAXR];
+    unsigned v[R];
 #pragma unroll
-    for (int j = 0; j < TORUS_MAXR; ++j) {
+    for (int j = 0; j < R; ++j) {
         v[j] = lo & rmask;
         lo = __funnelshift_r(lo, hi, rowbits);
         hi >>= rowbits;
     }
-    const unsigned vtop = (unsigned)(q >> ((L2 - 1) * rowbits)) & rmask;
-    unsigned e[TORUS_MAXR];
+    const unsigned vtop = exact ? v[R - 1] : ((unsigned)(q >> ((L2 - 1) * rowbits)) & rmask);
+    const unsigned rmul = rmask + 1u;   // table index v_hi * 2^rowbits + v_lo as one multiply-add
+    unsigned e[R];
     unsigned Mf = 0xffffffffu;
 #pragma unroll
-    for (int j = 0; j < TORUS_MAXR; ++j) {
-        e[j] = (j < L2) ? plut[(v[j] << rowbits) | (j ? v[j > 0 ? j - 1 : 0] : vtop)] : 0xffffffffu;
+    for (int j = 0; j < R; ++j) {
+        e[j] = (exact || j < L2) ? plut[v[j] * rmul + (j ? v[j > 0 ? j - 1 : 0] : vtop)] : 0xffffffffu;
         Mf = min(Mf, e[j]);
     }
     unsigned clo = 0u, chi = 0u;
 #pragma unroll
-    for (int j = 0; j < TORUS_MAXR; ++j) {
+    for (int j = 0; j < R; ++j) {
         const unsigned st = ((e[j] ^ Mf) < 0x10000u) ? (e[j] & 0xffu) : 0u;
         if (j < 4) clo |= st << (8 * j);
         else chi |= st << (8 * (j - 4));
@@ -159,17 +163,28 @@ __device__ __forceinline__ void torus_pair_search(S q, int L1, int L2, int w, in
     }
 }
 
+template <typename S>
+__device__ __forceinline__ void torus_pair_dispatch(S q, int L1, int L2, int w, int rowbits, int nbits, S full,
+                                                    const S* keep, const unsigned* plut, S& rep, int& gbest) {
+    switch (L2) {   // uniform over the launch
+        case 4: torus_pair_search<S, 4>(q, L1, L2, w, rowbits, nbits, full, keep, plut, rep, gbest); return;
+        case 5: torus_pair_search<S, 5>(q, L1, L2, w, rowbits, nbits, full, keep, plut, rep, gbest); return;
+        case 6: torus_pair_search<S, 6>(q, L1, L2, w, rowbits, nbits, full, keep, plut, rep, gbest); return;
+        default: torus_pair_search<S, TORUS_MAXR>(q, L1, L2, w, rowbits, nbits, full, keep, plut, rep, gbest);
+    }
+}
+
 template <typename W>
 __device__ __forceinline__ void canon_torus_pair(W q, int L1, int L2, int w, int rowbits, int nbits, W full,
                                                  const W* keep32, const W* keep, const unsigned* plut, W& rep,
                                                  int& gbest) {
     if (sizeof(W) == 8 && nbits <= 32) {   // 64-bit keys, 32-bit states: canonicalise in 32 bits
         unsigned r;
-        torus_pair_search<unsigned>((unsigned)q, L1, L2, w, rowbits, nbits, (unsigned)full, (const unsigned*)keep32,
-                                    plut, r, gbest);
+        torus_pair_dispatch<unsigned>((unsigned)q, L1, L2, w, rowbits, nbits, (unsigned)full, (const unsigned*)keep32,
+                                      plut, r, gbest);
         rep = (W)r;
     } else {
-        torus_pair_search<W>(q, L1, L2, w, rowbits, nbits, full, keep, plut, rep, gbest);
+        torus_pair_dispatch<W>(q, L1, L2, w, rowbits, nbits, full, keep, plut, rep, gbest);
     }
 }
 
