@@ -424,6 +424,14 @@ int blocks_for(const Blob& B, long long n_rows, int rows_per_tile) {
     return (int)std::max<long long>(1, std::min<long long>(need, B.max_blocks));
 }
 
+// Colex rank parameters of a mapped space (the chunk table and the parent sector's popcount).
+void set_map_params(HxParams& p, const Space& sp) {
+    p.rank_tab = sp.d_rank;
+    p.rank_wide = sp.rank_wide;
+    p.rank_k = sp.lay.popcount;
+    p.rank_nc = (sp.lay.nbits + RANK_CHUNK - 1) / RANK_CHUNK;
+}
+
 void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, void* y, int accumulate,
                     const void* gy, double* grad_partial, cudaStream_t st, int* blocks_used = nullptr,
                     int rows_override = 0) {
@@ -435,6 +443,15 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
         return;
     }
     int rows = rows_override ? rows_override : (op->tuned_rows[prec] ? op->tuned_rows[prec] : (mode ? B.rows_per_tile : -1));
+    const Space& sp = *op->space;
+    if (mode == 0 && sp.d_map) {
+        // parent-state map: targets are looked up, not canonicalised (row-per-lane schedule only)
+        set_map_params(p, sp);
+        p.map = sp.d_map;
+        p.map_wide = sp.map_wide;
+        p.map_cb = sp.map_cb;
+        if (rows > 0) rows = -1;
+    }
     if (rows < 0 && mode == 0) {
         // row-per-lane strategy: -lpr lanes per row, one warp per 32/lpr consecutive rows
         p.lpr = -rows;
@@ -773,6 +790,33 @@ int edgpu_space_search_stats(edgpu_space sh, int64_t* buckets, int32_t* shift, i
     if (inline_keys_per_bucket) *inline_keys_per_bucket = s->dir_K;
     if (window_steps) *window_steps = s->dir_steps;
     if (inline_fraction) *inline_fraction = s->dir_inline;
+    API_END
+}
+
+int edgpu_space_build_map(edgpu_space sh, int64_t max_bytes, int32_t* built) {
+    API_BEGIN
+    edgpu_space_s* s = as_space(sh);
+    require(max_bytes >= 0, EDGPU_ERR_ARG, "negative byte limit");
+    require(s->reduced, EDGPU_ERR_ARG, "parent-state maps belong to reduced representations");
+    if (!s->d_dir && s->dim > 0) build_search_directory(*s, g_stream);
+    const bool ok = build_parent_map(*s, max_bytes, g_stream);
+    if (built) *built = ok ? 1 : 0;
+    API_END
+}
+
+int edgpu_space_free_map(edgpu_space sh) {
+    API_BEGIN
+    edgpu_space_s* s = as_space(sh);
+    EDGPU_CUDA(cudaDeviceSynchronize());
+    free_parent_map(*s);
+    API_END
+}
+
+int edgpu_space_map_info(edgpu_space sh, int64_t* entries, int32_t* entry_bytes) {
+    API_BEGIN
+    edgpu_space_s* s = as_space(sh);
+    if (entries) *entries = s->d_map ? s->map_n : 0;
+    if (entry_bytes) *entry_bytes = s->d_map ? (s->map_wide ? 8 : 4) : 0;
     API_END
 }
 
@@ -1255,11 +1299,15 @@ HxParams batch_params(edgpu_batch_s* b, int prec, const void* const* xs, void* c
     const int n = (int)b->ops.size();
     const int lpr = b->lpr[prec] ? b->lpr[prec] : 1;
     const int rpw = 32 / lpr;
+    // sector maps are used when every sector has one (one colex rank table for all)
+    bool mapped = true;
+    for (int i = 0; i < n; ++i) mapped = mapped && (b->ops[i]->space->d_map != nullptr || b->ops[i]->space->dim == 0);
     std::vector<const void*> key;
     key.push_back((const void*)(intptr_t)lpr);
     for (int i = 0; i < n; ++i) {
         key.push_back(xs[i]);
         key.push_back(ys[i]);
+        key.push_back(mapped ? b->ops[i]->space->d_map : nullptr);
     }
     std::vector<SectorDesc> d(n);
     long long tiles = 0;
@@ -1276,6 +1324,9 @@ HxParams batch_params(edgpu_batch_s* b, int prec, const void* const* xs, void* c
         tiles += (s.dim + rpw - 1) / rpw;
         d[i].tile_end = tiles;
         d[i].ds = dir_search_of(s);
+        d[i].map = mapped ? s.d_map : nullptr;
+        d[i].map_wide = s.map_wide;
+        d[i].map_cb = s.map_cb;
         d[i].o_ph = F.o_ph[i];
         d[i].o_num = F.o_num[i];
         d[i].want_arg = F.want_arg[i];
@@ -1295,6 +1346,13 @@ HxParams batch_params(edgpu_batch_s* b, int prec, const void* const* xs, void* c
         it = b->images[prec].emplace(key, dev).first;
     }
     HxParams p = F.tmpl;
+    if (mapped) {
+        for (int i = 0; i < n; ++i)
+            if (b->ops[i]->space->d_map) {
+                set_map_params(p, *b->ops[i]->space);
+                break;
+            }
+    }
     p.blob = it->second;
     p.blob_words16 = (int)(F.smem / 16);
     p.lpr = lpr;
@@ -1431,6 +1489,7 @@ int edgpu_batch_mul_device(edgpu_batch bh, int32_t precision, const void* const*
     }
     std::vector<const void*> key;
     key.push_back((const void*)(intptr_t)p.lpr);
+    key.push_back(p.blob);   // the image (vectors, sector maps) the launch reads
     for (int i = 0; i < n; ++i) {
         key.push_back(xs[i]);
         key.push_back(ys[i]);

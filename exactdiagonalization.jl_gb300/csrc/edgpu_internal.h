@@ -70,8 +70,24 @@ struct Space {
     int dir_steps = 0;               // ceil(log2(largest bucket)) for buckets searched in the keys
     int dir_K = 0;                   // keys summarised inline per bucket
     double dir_inline = 0.0;         // fraction of keys in buckets answered by their summary
+    // Parent-state map of a reduced table whose parent is one fixed-popcount sector (optional):
+    // entry r, for the parent state q of colex rank r (its index in the sorted parent basis), holds the
+    // index c of q's representative | orbit-size index << map_cb | group element g (g.q = rep)
+    // << (map_cb + sb), or all ones when q's orbit has no representative in the table.
+    void* d_map = nullptr;
+    int map_wide = 0;                // entries are uint64 (else uint32)
+    int map_cb = 0;                  // bits of the index field
+    int64_t map_n = 0;               // entries = C(nbits, popcount)
+    void* d_rank = nullptr;          // colex rank chunk table [chunk][ones before][64 values]
+    int rank_wide = 0;               // rank table entries are uint64 (else uint32)
+    uint64_t map_gen = 0;            // bumped whenever the map is built or freed
     ~Space();
 };
+// Build (or free) the parent-state map of a reduced space; false when it does not apply or would
+// exceed max_bytes.
+bool build_parent_map(Space& red, int64_t max_bytes, cudaStream_t st);
+void free_parent_map(Space& red);
+constexpr int RANK_CHUNK = 6;      // bits per chunk of the colex rank tables
 
 // ---- device-side descriptors -------------------------------------------------------------------
 
@@ -175,6 +191,11 @@ struct HxParams {
     int warp_base;
     int o_sec, n_sec;                         // batched launch: shared-memory offset and count of SectorDesc
     long long n_tiles;                        // batched launch: warp tiles over all sectors
+    // parent-state map (replaces canonicalisation and search when map != null)
+    const void* map;
+    int map_wide, map_cb;
+    const void* rank_tab;                     // colex rank chunk table
+    int rank_wide, rank_k, rank_nc;           // entry width, popcount of the parent sector, chunks
 };
 
 // One sector of a batched launch (hx_multi_kernel), kept in shared memory after the common tables.
@@ -188,6 +209,8 @@ struct __align__(16) SectorDesc {
     long long n_rows;
     long long tile_end;                       // cumulative warp tiles through this sector
     DirSearch ds;
+    const void* map;                          // the sector's parent-state map (or null)
+    int map_wide, map_cb;
     int o_ph, o_num, want_arg, pad0;
 };
 

@@ -723,6 +723,8 @@ void GroupBuffers::release() {
 Space::~Space() {
     if (d_keys) cudaFree(d_keys);
     if (d_dir) cudaFree(d_dir);
+    if (d_map) cudaFree(d_map);
+    if (d_rank) cudaFree(d_rank);
 }
 
 void enumerate_parent(Space& s, cudaStream_t st) {
@@ -777,6 +779,44 @@ void build_mapping_t(const Space& red, const Space& parent, int64_t* index_out, 
     cudaFree(d_ph);
     cudaFree(d_idx);
     cudaFree(d_amp);
+}
+
+// Parent-state map over the fixed-popcount parent sector (see Space::d_map): one thread per colex rank
+// r: the parent state q = unrank(r), its orbit minimum and an element reaching it, the representative's
+// index by the search directory, packed into one entry (all ones when the orbit is not in the table).
+template <typename W, typename E>
+__global__ void k_build_map(long long n_parent, int n, int k, const unsigned long long* C, const W* reps,
+                            DirSearch ds, GroupDev g, int cb, E* out) {
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n_parent;
+         r += (long long)gridDim.x * blockDim.x) {
+        const W q = unrank_combo<W>((unsigned long long)r, n, k, C);
+        W rep = q;
+        int gb = 0, stab = 1;
+        if (g.kind == GK_TORUS) {
+            W keep[64];
+            for (int a = 0; a < g.L1; ++a) keep[a] = (W)g.keep[a];
+            canon_torus<W>(q, g.L1, g.L2, g.w, g.rowbits, g.nbits, (W)g.full, keep, true, false, rep, gb, stab);
+        } else if (g.kind == GK_GENERIC) {
+            for (int e = 0; e < g.G; ++e) {
+                W t = 0;
+                const unsigned long long* L = g.lut + (size_t)e * g.nchunks * 16;
+                for (int c = 0; c < g.nchunks; ++c) t |= (W)L[c * 16 + (int)((q >> (4 * c)) & 15u)];
+                t ^= (W)g.flips[e];
+                if (t < rep) {
+                    rep = t;
+                    gb = e;
+                }
+            }
+        }
+        W reps2[2] = {rep, rep};
+        const bool act[2] = {true, false};
+        long long c[2];
+        int sx[2];
+        key_find_sum2<W>(reps, ds, reps2, act, c, sx);
+        E e = (E)~(E)0;
+        if (c[0] >= 0) e = (E)c[0] | ((E)sx[0] << cb) | (g.den > 1 ? (E)gb << (cb + ds.sb) : (E)0);
+        out[r] = e;
+    }
 }
 
 template <typename W>
@@ -1003,6 +1043,101 @@ void embed_orbit_index(Space& red, cudaStream_t st) {
 void build_search_directory(Space& s, cudaStream_t st) {
     if (s.w32) dir_t<uint32_t>(s, st);
     else dir_t<unsigned long long>(s, st);
+}
+
+namespace {
+int bitlen_u64(unsigned long long v) {
+    int b = 0;
+    while (b < 64 && (v >> b) != 0ull) ++b;
+    return b;
+}
+
+template <typename W>
+void build_map_t(Space& red, cudaStream_t st) {
+    const Layout& L = red.lay;
+    const int n = L.nbits, k = L.popcount;
+    const long long np = (long long)red.map_n;
+    GroupBuffers gb;
+    gb.upload(red.group, L);
+    const DirSearch ds = dir_search_of(red);
+    const unsigned blocks = (unsigned)std::min<long long>((np + 255) / 256, 152ll * 64);
+    if (red.map_wide)
+        k_build_map<W, unsigned long long><<<blocks, 256, 0, st>>>(np, n, k, binomial_table(), (const W*)red.d_keys, ds,
+                                                                  gb.dev, red.map_cb, (unsigned long long*)red.d_map);
+    else
+        k_build_map<W, unsigned><<<blocks, 256, 0, st>>>(np, n, k, binomial_table(), (const W*)red.d_keys, ds, gb.dev,
+                                                        red.map_cb, (unsigned*)red.d_map);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("parent map: ") + cudaGetErrorString(e));
+}
+}  // namespace
+
+void free_parent_map(Space& red) {
+    if (red.d_map) cudaFree(red.d_map);
+    if (red.d_rank) cudaFree(red.d_rank);
+    red.d_map = nullptr;
+    red.d_rank = nullptr;
+    red.map_n = 0;
+    ++red.map_gen;
+}
+
+bool build_parent_map(Space& red, int64_t max_bytes, cudaStream_t st) {
+    const Layout& L = red.lay;
+    if (!red.reduced || L.popcount < 0 || L.nbits > 64 || red.dim == 0 || !red.d_keys || !red.d_dir) return false;
+    const int n = L.nbits, k = L.popcount;
+    const unsigned long long np = host_binom(n, k);
+    const int cb = bitlen_u64((unsigned long long)red.dim);
+    // the element is needed only for characters other than 1
+    const int gbits = red.group.den > 1 ? bitlen_u64((unsigned long long)std::max(red.group.G - 1, 0)) : 0;
+    const int wide = (cb + red.sb + gbits <= 32) ? 0 : 1;
+    if (cb + red.sb + gbits > 64) return false;
+    const double bytes = (double)np * (wide ? 8.0 : 4.0);
+    if (bytes > (double)max_bytes) return false;
+    // colex rank chunk table: T[(c * (k + 1) + j) * 64 + v] = sum over the set bits b of v, in ascending
+    // order t = 0, 1, ..., of C(6c + b, j + t + 1)
+    const int nc = (n + RANK_CHUNK - 1) / RANK_CHUNK;
+    const int rank_wide = np > 0xffffffffull ? 1 : 0;
+    std::vector<unsigned long long> T((size_t)nc * (k + 1) * 64, 0ull);
+    for (int c = 0; c < nc; ++c)
+        for (int j = 0; j <= k; ++j)
+            for (int v = 0; v < 64; ++v) {
+                unsigned long long sum = 0;
+                int t = 0;
+                for (int b = 0; b < RANK_CHUNK; ++b)
+                    if ((v >> b) & 1) {
+                        sum += host_binom(RANK_CHUNK * c + b, j + t + 1);
+                        ++t;
+                    }
+                T[((size_t)c * (k + 1) + j) * 64 + v] = sum;
+            }
+    free_parent_map(red);
+    std::vector<unsigned> T32;
+    if (!rank_wide) T32.assign(T.begin(), T.end());
+    const size_t tbytes = T.size() * (rank_wide ? 8 : 4);
+    cudaError_t e = cudaMalloc(&red.d_rank, tbytes);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(red.d_rank, rank_wide ? (const void*)T.data() : (const void*)T32.data(), tbytes,
+                       cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&red.d_map, (size_t)np * (wide ? 8 : 4));
+    if (e != cudaSuccess) {
+        free_parent_map(red);
+        if (e == cudaErrorMemoryAllocation) return false;
+        throw Error(EDGPU_ERR_CUDA, std::string("parent map: ") + cudaGetErrorString(e));
+    }
+    red.map_n = (int64_t)np;
+    red.map_wide = wide;
+    red.map_cb = cb;
+    red.rank_wide = rank_wide;
+    try {
+        if (red.w32) build_map_t<uint32_t>(red, st);
+        else build_map_t<unsigned long long>(red, st);
+    } catch (...) {
+        free_parent_map(red);
+        throw;
+    }
+    ++red.map_gen;
+    return true;
 }
 
 void get_states(const Space& s, uint64_t* out_host, cudaStream_t st) {

@@ -60,7 +60,29 @@ struct RowsSector {
     const V* ph;
     const int* num;
     bool want_arg;
+    const void* map;   // parent-state map (null: canonicalise and search)
+    int map_wide, map_cb;
 };
+
+// Colex rank of a state with rank_k set bits among the parent's bits: sum over 6-bit chunks of the
+// chunk table entry for (chunk, set bits below the chunk, chunk value).  The chunk loop is unrolled
+// (constant shifts) and skips the chunks past the parent's bits; T is the table entry type (uint32 when
+// every rank fits in 32 bits).
+template <typename T, typename W>
+__device__ __forceinline__ T colex_rank_t(W q, const T* __restrict__ tab, unsigned k1x64, int nc) {
+    T r = 0;
+    unsigned base = 0u, ones64 = 0u;
+#pragma unroll
+    for (int c = 0; c < (int)(8 * sizeof(W) + RANK_CHUNK - 1) / RANK_CHUNK; ++c) {
+        if (c < nc) {
+            const unsigned v = (unsigned)(q >> (RANK_CHUNK * c)) & 63u;
+            r += __ldg(tab + (base + ones64 + v));
+            ones64 += (unsigned)__popc(v) << 6;
+            base += k1x64;
+        }
+    }
+    return r;
+}
 
 // One warp tile of rows (rows_per_tile = 32 / lpr consecutive rows of the sector, lpr lanes each).
 template <typename W, int GK, int PREC, int MODE>
@@ -115,20 +137,50 @@ __device__ __forceinline__ void rows_tile(const HxParams& p, const RowsTables<W,
             W q[2], rep[2];
             int g[2];
             long long c[2];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                on[h] = mm != 0ull;
-                tt[h] = on[h] ? sub + lpr * (k0 + __ffsll((long long)mm) - 1) : 0;
-                mm &= mm - 1ull;
-                W tm, tr, tf;
-                load_rec3<W>(tb.orec + 4 * tt[h], tm, tr, tf);
-                q[h] = b ^ tf;
-                rep[h] = q[h];
-                g[h] = 0;
-                if (on[h]) canon_rep<W, GK>(q[h], p, tb.keep, tb.lut, tb.flips, tb.rlut, tb.keep32, rep[h], g[h]);
-            }
             int sx[2];
-            key_find_sum2<W>(keys, sc.ds, rep, on, c, sx);
+            if (sc.map) {
+                // parent-state map: colex rank of the target, one load, and the packed entry holds the
+                // representative's index, its orbit-size index and the element reaching it
+                const unsigned long long cmask = (1ull << sc.map_cb) - 1ull;
+                const unsigned k1x64 = ((unsigned)p.rank_k + 1u) << 6;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    on[h] = mm != 0ull;
+                    tt[h] = on[h] ? sub + lpr * (k0 + __ffsll((long long)mm) - 1) : 0;
+                    mm &= mm - 1ull;
+                    W tm, tr, tf;
+                    load_rec3<W>(tb.orec + 4 * tt[h], tm, tr, tf);
+                    q[h] = b ^ tf;
+                    unsigned long long e = ~0ull;
+                    if (on[h] && __popcll((unsigned long long)q[h]) == p.rank_k) {
+                        const unsigned long long r =
+                            p.rank_wide ? colex_rank_t<unsigned long long, W>(q[h], (const unsigned long long*)p.rank_tab,
+                                                                              k1x64, p.rank_nc)
+                                        : (unsigned long long)colex_rank_t<unsigned, W>(q[h], (const unsigned*)p.rank_tab,
+                                                                                        k1x64, p.rank_nc);
+                        e = sc.map_wide ? __ldg((const unsigned long long*)sc.map + r)
+                                        : (unsigned long long)__ldg((const unsigned*)sc.map + r);
+                    }
+                    const unsigned long long ci = e & cmask;
+                    c[h] = (ci == cmask) ? -1 : (long long)ci;
+                    sx[h] = (int)((e >> sc.map_cb) & ((1ull << p.sb) - 1ull));
+                    g[h] = (int)(e >> (sc.map_cb + p.sb)) & 0xfff;
+                }
+            } else {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    on[h] = mm != 0ull;
+                    tt[h] = on[h] ? sub + lpr * (k0 + __ffsll((long long)mm) - 1) : 0;
+                    mm &= mm - 1ull;
+                    W tm, tr, tf;
+                    load_rec3<W>(tb.orec + 4 * tt[h], tm, tr, tf);
+                    q[h] = b ^ tf;
+                    rep[h] = q[h];
+                    g[h] = 0;
+                    if (on[h]) canon_rep<W, GK>(q[h], p, tb.keep, tb.lut, tb.flips, tb.rlut, tb.keep32, rep[h], g[h]);
+                }
+                key_find_sum2<W>(keys, sc.ds, rep, on, c, sx);
+            }
             V xv[2];
 #pragma unroll
             for (int h = 0; h < 2; ++h) xv[h] = (c[h] >= 0) ? x[c[h]] : czero<V>();
@@ -193,6 +245,9 @@ __global__ void __launch_bounds__(HX_THREADS) hx_rows_kernel(const HxParams p) {
     sc.ph = (const V*)(sm + p.o_ph);
     sc.num = (const int*)(sm + p.o_num);
     sc.want_arg = p.want_arg != 0;
+    sc.map = p.map;
+    sc.map_wide = p.map_wide;
+    sc.map_cb = p.map_cb;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
     const int rpw = 32 / p.lpr;
     const long long n_tiles = (p.n_rows + rpw - 1) / rpw;
@@ -240,6 +295,9 @@ __global__ void __launch_bounds__(HX_THREADS) hx_multi_kernel(const HxParams p) 
         sc.ph = (const V*)(sm + d.o_ph);
         sc.num = (const int*)(sm + d.o_num);
         sc.want_arg = d.want_arg != 0;
+        sc.map = d.map;
+        sc.map_wide = d.map_wide;
+        sc.map_cb = d.map_cb;
         rows_tile<W, GK, PREC, 0>(p, tb, sc, tile - tile0, lane, nullptr);
     }
 }

@@ -57,6 +57,9 @@ SIGNATURES = {
     "edgpu_space_lookup": (ctypes.c_int, [vp, P(u64), i64, P(i64)]),
     "edgpu_space_destroy": (None, [vp]),
     "edgpu_space_search_stats": (ctypes.c_int, [vp, P(i64), P(i32), P(i32), P(i32), P(dbl)]),
+    "edgpu_space_build_map": (ctypes.c_int, [vp, i64, P(i32)]),
+    "edgpu_space_free_map": (ctypes.c_int, [vp]),
+    "edgpu_space_map_info": (ctypes.c_int, [vp, P(i64), P(i32)]),
     "edgpu_reduce": (ctypes.c_int, [vp, i32, P(i32), P(u64), P(i32), i32, P(vp)]),
     "edgpu_reduce_mapping": (ctypes.c_int, [vp, P(i64), P(dbl), i64]),
     "edgpu_space_orbit_sizes": (ctypes.c_int, [vp, P(i32), i64]),

@@ -21,7 +21,7 @@ import ctypes
 import math
 from fractions import Fraction
 from functools import reduce as _reduce
-from typing import List, Sequence, Tuple
+from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -306,6 +306,31 @@ class ReducedHilbertSpaceRepresentation:
     @property
     def dimension(self) -> int:
         return self._dim
+
+    def build_map(self, max_bytes: Optional[int] = None) -> bool:
+        """Build the compact parent-state map (the counterpart of the reference's parent-sized
+        basis_mapping_index / basis_mapping_amplitude tables, 4 or 8 bytes per parent state) when the
+        parent is one fixed-popcount sector and the map needs at most max_bytes (default: a quarter of
+        the free device memory).  Products then look targets up instead of canonicalising them.
+        Returns whether the map was built."""
+        if max_bytes is None:
+            import torch
+            free, _ = torch.cuda.mem_get_info()
+            max_bytes = free // 4
+        built = ctypes.c_int32()
+        check(lib().edgpu_space_build_map(self.handle, int(max_bytes), ctypes.byref(built)))
+        return bool(built.value)
+
+    def free_map(self) -> None:
+        check(lib().edgpu_space_free_map(self.handle))
+
+    @property
+    def map_info(self) -> Tuple[int, int]:
+        """(parent states covered, bytes per entry); (0, 0) without a map."""
+        n = ctypes.c_int64()
+        b = ctypes.c_int32()
+        check(lib().edgpu_space_map_info(self.handle, ctypes.byref(n), ctypes.byref(b)))
+        return int(n.value), int(b.value)
 
     def __len__(self):
         return self._dim

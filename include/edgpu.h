@@ -96,6 +96,20 @@ void edgpu_space_destroy(edgpu_space s);
 int edgpu_space_search_stats(edgpu_space s, int64_t* buckets, int32_t* shift, int32_t* inline_keys_per_bucket,
                              int32_t* window_steps, double* inline_fraction);
 
+/* Parent-state map of a reduced representation whose parent is one fixed-popcount sector.  The
+ * reference keeps parent-sized tables basis_mapping_index / basis_mapping_amplitude (24 bytes per parent
+ * state, symmetry_reduce_translation.jl:22-24,82-87 and symmetry_reduce_generic.jl:33-35) and its row
+ * iterator reads them for every target (reduced_operator_representation.jl:57-85).  This is the compact
+ * form: 4 (or 8) bytes per parent state, indexed by the colex rank of the state, holding the
+ * representative's index, its orbit-size index and the group element reaching it; the product then
+ * replaces orbit canonicalisation and search by one rank and one load per target (results identical).
+ * Built when it applies and needs at most max_bytes (*built = 1), else *built = 0 and nothing changes.
+ * The map belongs to the space and is used by every operator on it until edgpu_space_free_map. */
+int edgpu_space_build_map(edgpu_space s, int64_t max_bytes, int32_t* built);
+int edgpu_space_free_map(edgpu_space s);
+/* entries = parent states covered (0 without a map), entry_bytes = 4 or 8. */
+int edgpu_space_map_info(edgpu_space s, int64_t* entries, int32_t* entry_bytes);
+
 /* ---- symmetry reduction ------------------------------------------------------------------ */
 /* symmetry_reduce(hsr, symops_and_amplitudes) (symmetry_reduce_generic.jl:7-106), and the
  * IrrepComponent forms (symmetry_reduce.jl:12-20, symmetry_reduce_translation.jl) once their
