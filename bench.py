@@ -13,7 +13,9 @@ x from HBM.  The operator tables (representatives, terms) stay resident.
 Byte model per H*x (s_c = 8 for complex64, 16 for complex128):
     B = N_r * (8 + 8 + 2 s_c) + NNZ_off * (s_c + 8)
 N_r rows (representative word + orbit norm + x_r + y_r) and NNZ_off off-diagonal elements whose target
-lands on a representative (x gather + one table key).  NNZ_off is counted exactly on the GPU.
+lands on a representative (x gather + one table key).  NNZ_off is counted exactly on the GPU.  With a
+parent-state map (default when it fits; --no-map to canonicalise instead) a target costs one 4- or
+8-byte map entry instead of the key read; the model is kept as the fixed measure of work.
 
 Arms:
   (default)         the GPU path (libedgpu.so) -- device-resident `value`, host-buffer `e2e` through the
@@ -56,6 +58,11 @@ WORKLOADS = {
                                cpu_feasible=False,
                                desc="spin-1/2 XXZ J1-J2 triangular 6x5 torus (Jz/Jxy=0.8, J2/J1=0.125), 2Sz=0, "
                                     "all 30 momentum sectors in one batched persistent launch"),
+    "triangular6x5_k1": dict(kind="torus", shape=(6, 5), k=(1, 0), nn=[(1, 0), (1, 1), (0, 1)],
+                             nnn=[(2, 1), (1, 2), (-1, 1)], j1=1.0, j2=0.125, aniso=0.8, seed=3, lanczos_steps=200,
+                             reorth=True, cpu_feasible=False,
+                             desc="spin-1/2 XXZ J1-J2 triangular 6x5 torus (Jz/Jxy=0.8, J2/J1=0.125), 2Sz=0, "
+                                  "momentum (1,0) (one sector of the batched workload)"),
     "square6x6_k0": dict(kind="torus", shape=(6, 6), k=(0, 0), nn=[(1, 0), (0, 1)], nnn=[(1, 1), (1, -1)],
                          j1=1.0, j2=0.5, aniso=1.0, seed=7, lanczos_steps=300, reorth=False, cpu_feasible=False,
                          desc="spin-1/2 J1-J2 Heisenberg 6x6 torus (J2/J1=0.5), 2Sz=0, momentum (0,0)"),
@@ -99,6 +106,24 @@ def build_gpu_sectors(wl):
     t_space = time.perf_counter() - t0
     oprs = [edgpu.represent(sp, H) for sp in spaces]
     return spaces, oprs, momenta, t_space
+
+
+def build_maps(spaces, args):
+    """Parent-state maps of reduced spaces (unless --no-map): {"entries", "bytes", "build_s"} or None."""
+    import torch
+    if args.no_map or not hasattr(spaces[0], "build_map"):
+        return None
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    entries = nbytes = 0
+    for sp in spaces:
+        if not sp.build_map():
+            return {"built": False}
+        n, b = sp.map_info
+        entries += n
+        nbytes += n * b
+    torch.cuda.synchronize()
+    return {"built": True, "entries": entries, "bytes": nbytes, "build_s": time.perf_counter() - t0}
 
 
 def build_gpu_operator(wl):
@@ -321,6 +346,7 @@ def run_gpu(args, wl):
     N = space.dimension
     n_targets, nnz = opr.count_nnz()
     dir_stats = edgpu.search_stats(space)
+    map_info = build_maps([space], args)
     tune_mixed = opr.autotune("mixed")
     tune_fp64 = opr.autotune("fp64")
     stream = torch.cuda.current_stream()
@@ -434,7 +460,7 @@ def run_gpu(args, wl):
                        "nnz_off": nnz, "bytes_per_step": b_mixed, "l2": f"inputs cycled from a pool of {P_mixed} x/y "
                        f"pairs ({2 * P_mixed * N * s_c / 1e6:.0f} MB > 2x L2)", "parallelism": f"replicas x{world}",
                        "rows_per_tile": {"mixed": tune_mixed[0], "fp64": tune_fp64[0]},
-                       "setup_s": t_space, "search_directory": dir_stats},
+                       "setup_s": t_space, "search_directory": dir_stats, "parent_map": map_info},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_src},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps, "clocks": clk,
@@ -458,6 +484,7 @@ def run_gpu_batch(args, wl):
     dims = [sp.dimension for sp in spaces]
     N = sum(dims)
     nnz = sum(o.count_nnz()[1] for o in oprs)
+    map_info = build_maps(spaces, args)
     batch = edgpu.Batch(oprs)
     lpr, tune_ms = batch.autotune("mixed")
     stream = torch.cuda.current_stream()
@@ -544,7 +571,7 @@ def run_gpu_batch(args, wl):
                        "N_r_min": min(dims), "N_r_max": max(dims), "nnz_off": nnz, "bytes_per_step": b_step,
                        "lanes_per_row": lpr, "l2": f"inputs cycled from {P} sets of x/y ({2 * P * N * s_c / 1e6:.0f} MB "
                        f"> 2x L2)", "parallelism": f"replicas x{world}", "setup_s": t_space,
-                       "library_graph_ms_per_step": ms_graph},
+                       "library_graph_ms_per_step": ms_graph, "parent_map": map_info},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": profiled_traffic(args.workload), "peak_source": peak_src},
             "cpu_baseline": None if args.no_cpu_baseline else
@@ -566,6 +593,7 @@ def main():
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="chain24_k0")
     ap.add_argument("--no-lanczos", action="store_true")
+    ap.add_argument("--no-map", action="store_true", help="canonicalise targets instead of using parent-state maps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()

@@ -1047,7 +1047,9 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     check_prec(precision);
     const int64_t n = op->space->dim;
     const int cands[] = {-1, -2, -4, 32, 16};   // -k: k lanes per row; else rows per warp tile of the queued schedule
-    int best = 32;
+    // with a parent-state map only the row-per-lane schedules apply
+    const int n_cands = op->space->d_map ? 3 : 5;
+    int best = op->space->d_map ? -1 : 32;
     double best_ms = 1e30;
     if (n > 0) {
         const size_t vs = precision == EDGPU_FP64 ? 16 : 8;
@@ -1059,7 +1061,8 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
         cudaEventCreate(&e1);
         try {
             EDGPU_CUDA(cudaMemsetAsync(x, 0, n * vs, g_stream));
-            for (int r : cands) {
+            for (int ci = 0; ci < n_cands; ++ci) {
+                const int r = cands[ci];
                 launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, g_stream, nullptr, r);
                 float tot = 0.f;
                 const int reps = 3;
