@@ -105,6 +105,7 @@ struct Blob {
     void* d_diag = nullptr;  // per-row diagonal element in the blob's precision (product mode)
     size_t smem_rows = 0;    // shared memory of the row-per-lane kernel (no per-warp queues)
     int max_blocks_rows = 0;
+    int max_blocks_map = 0;  // resident blocks of the parent-state-map kernel (computed on first use)
     ~Blob() {
         if (d) cudaFree(d);
         if (d_diag) cudaFree(d_diag);
@@ -147,7 +148,7 @@ struct edgpu_batch_s {
         std::vector<unsigned char> image;          // common tables + per-sector character tables
         std::vector<int> o_ph, o_num, want_arg;
         HxParams tmpl{};
-        int gk = 0, per_sm = 1;
+        int gk = 0, per_sm = 1, per_sm_map = 0;
         size_t smem = 0;
         int64_t rows = 0;
     } fused[2];
@@ -461,12 +462,19 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
         p.gy = gy;
         p.grad_partial = grad_partial;
         p.accumulate = accumulate;
+        const bool mapped = p.map != nullptr;
+        const int gk = mapped ? GK_MAP : B.gk;
+        if (mapped && B.max_blocks_map == 0) {
+            const int per_sm = std::max(1, op->space->w32 ? hx_rows_occupancy_w32(GK_MAP, prec, B.smem_rows)
+                                                           : hx_rows_occupancy_w64(GK_MAP, prec, B.smem_rows));
+            B.max_blocks_map = per_sm * std::max(1, g_sm_count);
+        }
         const long long warps = (p.n_rows + p.rows_per_tile - 1) / p.rows_per_tile;
         const int blocks = (int)std::max<long long>(1, std::min<long long>((warps + HX_THREADS / 32 - 1) / (HX_THREADS / 32),
-                                                                          B.max_blocks_rows));
+                                                                          mapped ? B.max_blocks_map : B.max_blocks_rows));
         if (blocks_used) *blocks_used = blocks;
-        if (op->space->w32) hx_rows_launch_w32(B.gk, prec, p, blocks, B.smem_rows, st);
-        else hx_rows_launch_w64(B.gk, prec, p, blocks, B.smem_rows, st);
+        if (op->space->w32) hx_rows_launch_w32(gk, prec, p, blocks, B.smem_rows, st);
+        else hx_rows_launch_w64(gk, prec, p, blocks, B.smem_rows, st);
         return;
     }
     if (rows < 0) rows = 32;
@@ -1098,6 +1106,90 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     API_END
 }
 
+// ---- sparse assembly ---------------------------------------------------------------------------
+
+namespace {
+
+// Count (row_ptr == null) or fill the CSR rows [row0, row0 + n_run) of H (transpose == 0) or of H^T
+// (transpose == 1, as the conjugated rows of H^dagger) on the device.
+void sparse_pass(edgpu_op_s* op, int transpose, double tol, long long row0, long long n_run, long long* d_counts,
+                 const long long* d_row_ptr, long long* d_cols, double2* d_vals) {
+    build_blob(op, EDGPU_FP64, transpose, 0);
+    const Blob& B = op->blob[EDGPU_FP64][transpose][0];
+    const HxParams& p = B.tmpl;
+    const size_t t1p = (size_t)((p.T_o + 2) & ~1);   // T_o + 1 rounded up to even (see hx_sparse_kernel)
+    require(p.warp_base % 16 == 0, EDGPU_ERR_ARG, "internal: unaligned sparse scratch");
+    const size_t smem = (size_t)p.warp_base + 4 * t1p * 48;
+    require(smem <= 227 * 1024, EDGPU_ERR_ARG, "too many off-diagonal terms per row for sparse assembly");
+    if (n_run <= 0) return;
+    if (op->space->w32)
+        hx_sparse_launch_w32(B.gk, p, row0, n_run, transpose, tol, d_counts, d_row_ptr, d_cols, d_vals, smem, g_stream);
+    else
+        hx_sparse_launch_w64(B.gk, p, row0, n_run, transpose, tol, d_counts, d_row_ptr, d_cols, d_vals, smem, g_stream);
+}
+
+}  // namespace
+
+int edgpu_op_sparse(edgpu_op oh, int32_t transpose, double tol, int64_t* nnz, int64_t* row_ptr, int64_t* col_idx,
+                    double* values) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    require(nnz && tol >= 0.0 && (transpose == 0 || transpose == 1), EDGPU_ERR_ARG, "bad sparse arguments");
+    require(!row_ptr || (col_idx && values), EDGPU_ERR_ARG, "row_ptr, col_idx and values go together");
+    const long long n = op->space->dim;
+    DevBuf<long long> counts, rp, cols;
+    DevBuf<double> vals;
+    counts.ensure(std::max<long long>(n, 1));
+    sparse_pass(op, transpose, tol, 0, n, counts.p, nullptr, nullptr, nullptr);
+    std::vector<long long> hc(n);
+    if (n) EDGPU_CUDA(cudaMemcpyAsync(hc.data(), counts.p, n * sizeof(long long), cudaMemcpyDeviceToHost, g_stream));
+    EDGPU_CUDA(cudaStreamSynchronize(g_stream));
+    std::vector<long long> hp(n + 1, 0);
+    for (long long i = 0; i < n; ++i) hp[i + 1] = hp[i] + hc[i];
+    *nnz = hp[n];
+    if (!row_ptr) return EDGPU_OK;
+    for (long long i = 0; i <= n; ++i) row_ptr[i] = hp[i];
+    if (hp[n] == 0) return EDGPU_OK;
+    rp.ensure(n + 1);
+    cols.ensure(hp[n]);
+    vals.ensure(2 * hp[n]);
+    EDGPU_CUDA(cudaMemcpyAsync(rp.p, hp.data(), (n + 1) * sizeof(long long), cudaMemcpyHostToDevice, g_stream));
+    sparse_pass(op, transpose, tol, 0, n, nullptr, rp.p, cols.p, (double2*)vals.p);
+    EDGPU_CUDA(cudaMemcpyAsync(col_idx, cols.p, hp[n] * sizeof(long long), cudaMemcpyDeviceToHost, g_stream));
+    EDGPU_CUDA(cudaMemcpyAsync(values, vals.p, 2 * hp[n] * sizeof(double), cudaMemcpyDeviceToHost, g_stream));
+    EDGPU_CUDA(cudaStreamSynchronize(g_stream));
+    API_END
+}
+
+int edgpu_op_get_row(edgpu_op oh, int32_t transpose, int64_t row, double tol, int64_t cap, int64_t* count,
+                     int64_t* col_idx, double* values) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    require(count && tol >= 0.0 && (transpose == 0 || transpose == 1) && cap >= 0, EDGPU_ERR_ARG,
+            "bad get_row arguments");
+    require(row >= 0 && row < op->space->dim, EDGPU_ERR_BOUNDS, "row index out of range");
+    DevBuf<long long> c, rp, cols;
+    DevBuf<double> vals;
+    c.ensure(1);
+    sparse_pass(op, transpose, tol, row, 1, c.p, nullptr, nullptr, nullptr);
+    long long k = 0;
+    EDGPU_CUDA(cudaMemcpyAsync(&k, c.p, sizeof(long long), cudaMemcpyDeviceToHost, g_stream));
+    EDGPU_CUDA(cudaStreamSynchronize(g_stream));
+    *count = k;
+    if (!col_idx || k == 0) return EDGPU_OK;
+    require(values && cap >= k, EDGPU_ERR_DIM, "output buffers hold fewer entries than the row");
+    const long long zero = 0;
+    rp.ensure(1);
+    cols.ensure(k);
+    vals.ensure(2 * k);
+    EDGPU_CUDA(cudaMemcpyAsync(rp.p, &zero, sizeof(long long), cudaMemcpyHostToDevice, g_stream));
+    sparse_pass(op, transpose, tol, row, 1, nullptr, rp.p, cols.p, (double2*)vals.p);
+    EDGPU_CUDA(cudaMemcpyAsync(col_idx, cols.p, k * sizeof(long long), cudaMemcpyDeviceToHost, g_stream));
+    EDGPU_CUDA(cudaMemcpyAsync(values, vals.p, 2 * k * sizeof(double), cudaMemcpyDeviceToHost, g_stream));
+    EDGPU_CUDA(cudaStreamSynchronize(g_stream));
+    API_END
+}
+
 int edgpu_op_count_nnz(edgpu_op oh, int64_t* n_targets, int64_t* nnz_off) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
@@ -1361,15 +1453,21 @@ HxParams batch_params(edgpu_batch_s* b, int prec, const void* const* xs, void* c
     p.lpr = lpr;
     p.rows_per_tile = rpw;
     p.n_tiles = tiles;
+    if (mapped && F.per_sm_map == 0) {
+        const bool w32 = b->ops[0]->space->w32;
+        F.per_sm_map = std::max(1, w32 ? hx_multi_occupancy_w32(GK_MAP, prec, F.smem) : hx_multi_occupancy_w64(GK_MAP, prec, F.smem));
+    }
     const long long need = (tiles + HX_THREADS / 32 - 1) / (HX_THREADS / 32);
-    *blocks_out = (int)std::max<long long>(1, std::min<long long>(need, (long long)F.per_sm * std::max(1, g_sm_count)));
+    *blocks_out = (int)std::max<long long>(
+        1, std::min<long long>(need, (long long)(mapped ? F.per_sm_map : F.per_sm) * std::max(1, g_sm_count)));
     return p;
 }
 
 void batch_launch(edgpu_batch_s* b, int prec, const HxParams& p, int blocks, cudaStream_t st) {
     if (p.n_tiles == 0) return;
-    if (b->ops[0]->space->w32) hx_multi_launch_w32(b->fused[prec].gk, prec, p, blocks, b->fused[prec].smem, st);
-    else hx_multi_launch_w64(b->fused[prec].gk, prec, p, blocks, b->fused[prec].smem, st);
+    const int gk = p.rank_tab ? GK_MAP : b->fused[prec].gk;   // sector maps present: the map flavour
+    if (b->ops[0]->space->w32) hx_multi_launch_w32(gk, prec, p, blocks, b->fused[prec].smem, st);
+    else hx_multi_launch_w64(gk, prec, p, blocks, b->fused[prec].smem, st);
 }
 
 }  // namespace

@@ -27,6 +27,8 @@ struct Error : std::runtime_error {
     } while (0)
 
 enum GroupKind { GK_TRIVIAL = 0, GK_TORUS = 1, GK_GENERIC = 2, GK_RING = 3 };
+// Product-kernel flavour for targets looked up in a parent-state map (no canonicalisation code).
+constexpr int GK_MAP = 4;
 
 // Symmetry group acting on basis words: element g maps word q to g.q.
 //  TRIVIAL  the identity only (unreduced representation).
@@ -227,6 +229,14 @@ void hx_rows_launch_w32(int gk, int prec, const HxParams& p, int blocks, size_t 
 void hx_rows_launch_w64(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
 int hx_rows_occupancy_w32(int gk, int prec, size_t smem);
 int hx_rows_occupancy_w64(int gk, int prec, size_t smem);
+// Sparse assembly of a representation in FP64 (hx_rows.cuh, hx_sparse_kernel); shared memory:
+// the blob's warp_base plus 4 warps x (T_o + 1) x 48 bytes.
+void hx_sparse_launch_w32(int gk, const HxParams& p, long long row0, long long n_run, int conj_vals, double tol,
+                          long long* counts, const long long* row_ptr, long long* cols, double2* vals, size_t smem,
+                          cudaStream_t st);
+void hx_sparse_launch_w64(int gk, const HxParams& p, long long row0, long long n_run, int conj_vals, double tol,
+                          long long* counts, const long long* row_ptr, long long* cols, double2* vals, size_t smem,
+                          cudaStream_t st);
 // Batched sectors in one persistent launch (hx_rows.cuh, hx_multi_kernel), product mode only.
 void hx_multi_launch_w32(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
 void hx_multi_launch_w64(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);

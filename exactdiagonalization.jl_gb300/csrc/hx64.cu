@@ -40,6 +40,8 @@ void hx_rows_launch_w64(int gk, int prec, const HxParams& p, int blocks, size_t 
         case 1 * 2 + 1: return hx_rows_launch_one<unsigned long long, 1, 1, 0>(p, blocks, smem, st);
         case 2 * 2 + 0: return hx_rows_launch_one<unsigned long long, 2, 0, 0>(p, blocks, smem, st);
         case 2 * 2 + 1: return hx_rows_launch_one<unsigned long long, 2, 1, 0>(p, blocks, smem, st);
+        case 4 * 2 + 0: return hx_rows_launch_one<unsigned long long, 4, 0, 0>(p, blocks, smem, st);
+        case 4 * 2 + 1: return hx_rows_launch_one<unsigned long long, 4, 1, 0>(p, blocks, smem, st);
         default: throw Error(EDGPU_ERR_ARG, "bad product kernel selector");
     }
 }
@@ -52,6 +54,8 @@ int hx_rows_occupancy_w64(int gk, int prec, size_t smem) {
         case 1 * 2 + 1: return hx_rows_occupancy_one<unsigned long long, 1, 1, 0>(smem);
         case 2 * 2 + 0: return hx_rows_occupancy_one<unsigned long long, 2, 0, 0>(smem);
         case 2 * 2 + 1: return hx_rows_occupancy_one<unsigned long long, 2, 1, 0>(smem);
+        case 4 * 2 + 0: return hx_rows_occupancy_one<unsigned long long, 4, 0, 0>(smem);
+        case 4 * 2 + 1: return hx_rows_occupancy_one<unsigned long long, 4, 1, 0>(smem);
         default: throw Error(EDGPU_ERR_ARG, "bad product kernel selector");
     }
 }
@@ -65,6 +69,8 @@ void hx_multi_launch_w64(int gk, int prec, const HxParams& p, int blocks, size_t
         case 1 * 2 + 1: return hx_multi_launch_one<unsigned long long, 1, 1>(p, blocks, smem, st);
         case 2 * 2 + 0: return hx_multi_launch_one<unsigned long long, 2, 0>(p, blocks, smem, st);
         case 2 * 2 + 1: return hx_multi_launch_one<unsigned long long, 2, 1>(p, blocks, smem, st);
+        case 4 * 2 + 0: return hx_multi_launch_one<unsigned long long, 4, 0>(p, blocks, smem, st);
+        case 4 * 2 + 1: return hx_multi_launch_one<unsigned long long, 4, 1>(p, blocks, smem, st);
         default: throw Error(EDGPU_ERR_ARG, "bad product kernel selector");
     }
 }
@@ -77,6 +83,20 @@ int hx_multi_occupancy_w64(int gk, int prec, size_t smem) {
         case 1 * 2 + 1: return hx_multi_occupancy_one<unsigned long long, 1, 1>(smem);
         case 2 * 2 + 0: return hx_multi_occupancy_one<unsigned long long, 2, 0>(smem);
         case 2 * 2 + 1: return hx_multi_occupancy_one<unsigned long long, 2, 1>(smem);
+        case 4 * 2 + 0: return hx_multi_occupancy_one<unsigned long long, 4, 0>(smem);
+        case 4 * 2 + 1: return hx_multi_occupancy_one<unsigned long long, 4, 1>(smem);
+        default: throw Error(EDGPU_ERR_ARG, "bad product kernel selector");
+    }
+}
+
+// Sparse assembly (FP64).
+void hx_sparse_launch_w64(int gk, const HxParams& p, long long row0, long long n_run, int conj_vals, double tol,
+                         long long* counts, const long long* row_ptr, long long* cols, double2* vals, size_t smem,
+                         cudaStream_t st) {
+    switch (gk) {
+        case 0: return hx_sparse_launch_one<unsigned long long, 0>(p, row0, n_run, conj_vals, tol, counts, row_ptr, cols, vals, smem, st);
+        case 1: return hx_sparse_launch_one<unsigned long long, 1>(p, row0, n_run, conj_vals, tol, counts, row_ptr, cols, vals, smem, st);
+        case 2: return hx_sparse_launch_one<unsigned long long, 2>(p, row0, n_run, conj_vals, tol, counts, row_ptr, cols, vals, smem, st);
         default: throw Error(EDGPU_ERR_ARG, "bad product kernel selector");
     }
 }

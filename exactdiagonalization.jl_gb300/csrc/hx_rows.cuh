@@ -138,7 +138,7 @@ __device__ __forceinline__ void rows_tile(const HxParams& p, const RowsTables<W,
             int g[2];
             long long c[2];
             int sx[2];
-            if (sc.map) {
+            if constexpr (GK == GK_MAP) {
                 // parent-state map: colex rank of the target, one load, and the packed entry holds the
                 // representative's index, its orbit-size index and the element reaching it
                 const unsigned long long cmask = (1ull << sc.map_cb) - 1ull;
@@ -167,6 +167,7 @@ __device__ __forceinline__ void rows_tile(const HxParams& p, const RowsTables<W,
                     g[h] = (int)(e >> (sc.map_cb + p.sb)) & 0xfff;
                 }
             } else {
+                (void)sc.map;
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     on[h] = mm != 0ull;
@@ -300,6 +301,131 @@ __global__ void __launch_bounds__(HX_THREADS) hx_multi_kernel(const HxParams p) 
         sc.map_cb = d.map_cb;
         rows_tile<W, GK, PREC, 0>(p, tb, sc, tile - tile0, lane, nullptr);
     }
+}
+
+// Sparse assembly of the representation in FP64 (sparse(opr) and get_row,
+// abstract_operator_representation.jl:135-213): one warp per row.  The lanes evaluate the row's
+// off-diagonal terms (term t in slot t, no match: column -1) and lane 0 adds the diagonal in slot
+// T_o; lane 0 then merges the slots into a list sorted by column, summing entries of equal column,
+// and drops entries with |value| < tol (choptol!, util.jl:88-94).  Count pass (row_ptr == null):
+// counts[row] = entries; fill pass: entries written at row_ptr[row], optionally conjugated.
+constexpr int SPARSE_THREADS = 128;
+
+template <typename W, int GK>
+__global__ void __launch_bounds__(SPARSE_THREADS) hx_sparse_kernel(const HxParams p, long long row0, long long n_run,
+                                                                 int conj_vals, double tol, long long* counts,
+                                                                 const long long* row_ptr, long long* cols,
+                                                                 double2* vals) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    {
+        const int4* src = (const int4*)p.blob;
+        int4* dst = (int4*)sm;
+        for (int i = threadIdx.x; i < p.blob_words16; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const RowsTables<W, 0> tb(p, sm);
+    const W* __restrict__ keys = (const W*)p.keys;
+    const double2* ph = (const double2*)(sm + p.o_ph);
+    const int* num = (const int*)(sm + p.o_num);
+    const int T1 = p.T_o + 1;
+    const int T1p = (T1 + 1) & ~1;   // even, so that every double2 array below starts on 16 bytes
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    // per-warp scratch after the tables (warp_base is 16-byte aligned): slots (column, value), then
+    // the merged list; sizes in units of T1p entries: 8 + 16 + 8 + 16 = 48 bytes
+    unsigned char* base = sm + p.warp_base + (size_t)warp * (size_t)T1p * 48;
+    long long* sc = (long long*)base;
+    double2* sv = (double2*)(base + (size_t)T1p * 8);
+    long long* lc = (long long*)(base + (size_t)T1p * 24);
+    double2* lv = (double2*)(base + (size_t)T1p * 32);
+    const int sb = p.sb;
+    const W smask = (W)((((W)1) << sb) - 1);
+    for (long long rr = (long long)blockIdx.x * wpb + warp; rr < n_run; rr += (long long)gridDim.x * wpb) {
+        const long long row = row0 + rr;
+        const W kr = keys[row];
+        const W b = kr >> sb;
+        const int ri = (int)(kr & smask);
+        for (int t = lane; t < p.T_o; t += 32) {
+            W tm, tr, tf;
+            load_rec3<W>(tb.orec + 4 * t, tm, tr, tf);
+            long long c = -1;
+            double2 v = make_double2(0.0, 0.0);
+            if ((b & tm) == tr) {
+                const W q = b ^ tf;
+                W rep[2] = {q, q};
+                int g = 0;
+                canon_rep<W, GK>(q, p, tb.keep, tb.lut, tb.flips, tb.rlut, tb.keep32, rep[0], g);
+                const bool act[2] = {true, false};
+                long long cc[2];
+                int sx[2];
+                key_find_sum2<W>(keys, p.ds, rep, act, cc, sx);
+                if (cc[0] >= 0) {
+                    c = cc[0];
+                    v = tb.oa[t];
+                    if (GK != GK_TRIVIAL) {
+                        if (p.want_arg) v = cmul(v, ph[num[g]]);
+                        v = cscale(v, tb.ratio[ri * p.nd + sx[0]]);
+                    }
+                }
+            }
+            sc[t] = c;
+            sv[t] = v;
+        }
+        if (lane == 0) {
+            sc[p.T_o] = row;
+            sv[p.T_o] = ((const double2*)p.diag)[row];
+        }
+        __syncwarp();
+        if (lane == 0) {
+            int n = 0;
+            for (int i = 0; i < T1; ++i) {
+                const long long c = sc[i];
+                if (c < 0) continue;
+                int j = n;
+                while (j > 0 && lc[j - 1] > c) --j;
+                if (j > 0 && lc[j - 1] == c) {
+                    lv[j - 1].x += sv[i].x;
+                    lv[j - 1].y += sv[i].y;
+                    continue;
+                }
+                for (int k = n; k > j; --k) {
+                    lc[k] = lc[k - 1];
+                    lv[k] = lv[k - 1];
+                }
+                lc[j] = c;
+                lv[j] = sv[i];
+                ++n;
+            }
+            int m = 0;
+            for (int k = 0; k < n; ++k)
+                if (!(sqrt(lv[k].x * lv[k].x + lv[k].y * lv[k].y) < tol)) {
+                    lc[m] = lc[k];
+                    lv[m] = lv[k];
+                    ++m;
+                }
+            if (!row_ptr) {
+                counts[rr] = m;
+            } else {
+                const long long o = row_ptr[rr];
+                for (int k = 0; k < m; ++k) {
+                    cols[o + k] = lc[k];
+                    vals[o + k] = conj_vals ? make_double2(lv[k].x, -lv[k].y) : lv[k];
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+template <typename W, int GK>
+void hx_sparse_launch_one(const HxParams& p, long long row0, long long n_run, int conj_vals, double tol,
+                          long long* counts, const long long* row_ptr, long long* cols, double2* vals, size_t smem,
+                          cudaStream_t st) {
+    auto kern = hx_sparse_kernel<W, GK>;
+    EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const long long warps = n_run;
+    const int blocks = (int)std::max<long long>(1, std::min<long long>((warps + 3) / 4, 152ll * 16));
+    kern<<<blocks, SPARSE_THREADS, smem, st>>>(p, row0, n_run, conj_vals, tol, counts, row_ptr, cols, vals);
+    EDGPU_CUDA(cudaGetLastError());
 }
 
 template <typename W, int GK, int PREC>

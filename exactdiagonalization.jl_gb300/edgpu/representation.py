@@ -30,6 +30,8 @@ from ._lib import (ArgumentError, BoundsError, DimensionMismatch, FP64, MIXED, c
 from .hilbert import HilbertSpace, HilbertSpaceSector, basespace
 from .operators import NullOperator, RTOL, simplify, term_arrays
 
+RTOL_F64 = float(np.sqrt(np.finfo(np.float64).eps))   # Base.rtoldefault(Float64)
+
 _PREC = {"fp64": FP64, "float64": FP64, "complex128": FP64, FP64: FP64,
          "mixed": MIXED, "fp32": MIXED, "complex64": MIXED, MIXED: MIXED}
 
@@ -575,6 +577,80 @@ class OperatorRepresentation:
         """state * opr: transpose product (operator_representation.jl:132-139)."""
         out = np.zeros(self.dimension, dtype=np.complex128)
         return apply_(out, state, self)
+
+    # -- sparse assembly (sparse(opr), Matrix(opr), get_row, get_column, getindex) ---------------
+    def sparse(self, tol: float = RTOL_F64):
+        """sparse(opr) (abstract_operator_representation.jl:135-198) assembled on the GPU in FP64: the
+        matrix of the column iterators (as the reference builds it, column by column), entries of
+        equal position summed, |value| < tol dropped; a scipy.sparse CSC matrix."""
+        return self._assemble(tol, True).T.tocsc()
+
+    def sparse_rows(self, tol: float = RTOL_F64):
+        """The matrix of the row iterators, the one mul! applies (CSR).  It equals sparse() for operators
+        that commute with the symmetry group."""
+        return self._assemble(tol, False)
+
+    def _assemble(self, tol: float, transpose: bool):
+        import scipy.sparse as sps
+        n = self.dimension
+        nnz = ctypes.c_int64()
+        check(lib().edgpu_op_sparse(self._h, int(transpose), float(tol), ctypes.byref(nnz), None, None, None))
+        rp = np.zeros(n + 1, dtype=np.int64)
+        ci = np.zeros(max(nnz.value, 1), dtype=np.int64)
+        va = np.zeros(max(nnz.value, 1), dtype=np.complex128)
+        check(lib().edgpu_op_sparse(self._h, int(transpose), float(tol), ctypes.byref(nnz), ptr(rp, ctypes.c_int64),
+                                    ptr(ci, ctypes.c_int64), ptr(va.view(np.float64), ctypes.c_double)))
+        return sps.csr_matrix((va[:nnz.value], ci[:nnz.value], rp), shape=(n, n))
+
+    def todense(self) -> np.ndarray:
+        """Matrix(opr) (abstract_operator_representation.jl:121-131): column iterators, nothing dropped."""
+        return self.sparse(tol=0.0).toarray()
+
+    def _line(self, i: int, transpose: bool, tol: float):
+        n = self.dimension
+        if not 0 <= i < n:
+            raise BoundsError(f"index {i} out of range for dimension {n}")
+        cnt = ctypes.c_int64()
+        check(lib().edgpu_op_get_row(self._h, int(transpose), int(i), float(tol), 0, ctypes.byref(cnt), None, None))
+        k = cnt.value
+        ci = np.zeros(max(k, 1), dtype=np.int64)
+        va = np.zeros(max(k, 1), dtype=np.complex128)
+        check(lib().edgpu_op_get_row(self._h, int(transpose), int(i), float(tol), k, ctypes.byref(cnt),
+                                     ptr(ci, ctypes.c_int64), ptr(va.view(np.float64), ctypes.c_double)))
+        return ci[:k], va[:k]
+
+    def get_row(self, i: int, tol: float = RTOL_F64):
+        """get_row(opr, irow) (abstract_operator_representation.jl:201-213): (column indices, values)."""
+        return self._line(i, False, tol)
+
+    def get_column(self, j: int, tol: float = RTOL_F64):
+        """get_column(opr, icol) (abstract_operator_representation.jl:216-228): (row indices, values)."""
+        return self._line(j, True, tol)
+
+    def get_element(self, i: int, j: int) -> complex:
+        """opr[i, j] (get_element, reduced_operator_representation.jl:119-138): the sum of column j's
+        iterator entries in row i (zero when absent)."""
+        if not 0 <= i < self.dimension:
+            raise BoundsError(f"index {i} out of range for dimension {self.dimension}")
+        rows, vals = self._line(j, True, 0.0)
+        hit = np.nonzero(rows == i)[0]
+        return complex(vals[hit[0]]) if hit.size else 0j
+
+    def __getitem__(self, key):
+        """opr[i, :], opr[:, j], opr[:, :] and opr[i, j] (abstract_operator_representation.jl:231-250)."""
+        import scipy.sparse as sps
+        i, j = key
+        full = slice(None)
+        n = self.dimension
+        if isinstance(i, slice) and i == full and isinstance(j, slice) and j == full:
+            return self.sparse()
+        if isinstance(j, slice) and j == full:
+            cols, vals = self.get_row(int(i))
+            return sps.csr_matrix((vals, cols, [0, cols.size]), shape=(1, n))
+        if isinstance(i, slice) and i == full:
+            rows, vals = self.get_column(int(j))
+            return sps.csr_matrix((vals, rows, [0, rows.size]), shape=(1, n)).T
+        return self.get_element(int(i), int(j))
 
     def lanczos(self, *args, **kwargs):
         from .lanczos import lanczos

@@ -153,6 +153,22 @@ int edgpu_op_set_tiling(edgpu_op op, int32_t precision, int32_t rows_per_tile);
  * queued with 32 or 16 rows per warp tile) on this operator and keeps the fastest
  * (rows_per_tile_out: the schedule as in edgpu_op_set_tiling; best_ms_out nullable). */
 int edgpu_op_autotune(edgpu_op op, int32_t precision, int32_t* rows_per_tile_out, double* best_ms_out);
+/* Sparse matrix of the representation, assembled on the device in FP64: rows sorted by column,
+ * entries of equal column summed, entries with |value| < tol dropped (tol: the reference's
+ * Base.rtoldefault(Float64) = sqrt(eps) gives its default).  This is sparse(opr)
+ * (abstract_operator_representation.jl:135-198, a SparseMatrixCSC built column by column) as CSR:
+ * transpose == 0 gives the rows of H, transpose == 1 the rows of H^T (= the columns of H, the
+ * reference's CSC arrays).  Call with row_ptr == NULL for *nnz only; then with host buffers
+ * row_ptr[dim + 1], col_idx[nnz] and values[2 * nnz] (interleaved complex128). */
+int edgpu_op_sparse(edgpu_op op, int32_t transpose, double tol, int64_t* nnz, int64_t* row_ptr, int64_t* col_idx,
+                    double* values);
+/* One row (transpose == 0: get_row, abstract_operator_representation.jl:201-213) or column
+ * (transpose == 1: get_column, :216-228) as sorted (index, value) entries, summed and chopped as in
+ * edgpu_op_sparse.  *count = entries; col_idx/values (capacity cap entries) may be NULL to count only.
+ * EDGPU_ERR_BOUNDS for a row outside [0, dim). */
+int edgpu_op_get_row(edgpu_op op, int32_t transpose, int64_t row, double tol, int64_t cap, int64_t* count,
+                     int64_t* col_idx, double* values);
+
 /* Number of off-diagonal (row, term) matches over all rows, and how many of them land on a row of
  * the representation (the nonzero off-diagonal elements the row iterator yields with a valid column,
  * reduced_operator_representation.jl:57-85) -- the NNZ_off of the product's byte model. */
