@@ -130,6 +130,8 @@ struct edgpu_op_s {
     Blob blob[2][2][2];               // [precision][direction 0 = H, 1 = H^dagger][mode 0 = product, 1 = gradient]
     int tuned_rows[2] = {0, 0};
     uint64_t gen = 0;                 // bumped whenever the device tables are rebuilt
+    uint64_t invariant_gen = ~0ull;   // table generation the invariance flag belongs to
+    bool invariant = true;            // the terms commute with every element of the space's group
     DevBuf<double> x64, y64, z64;
     DevBuf<float> x32, y32;
     DevBuf<double> grad_partial, grad_dev;
@@ -1268,6 +1270,97 @@ int edgpu_mul_transpose(edgpu_op oh, int32_t precision, const double* x, double*
     API_END
 }
 
+namespace {
+
+// Site maps and flip masks of every element of a space's group, on the host.
+void host_group(const Space& s, std::vector<std::vector<int>>& maps, std::vector<uint64_t>& flips) {
+    const Group& g = s.group;
+    const int n = s.lay.n_sites;
+    std::vector<int> id(n);
+    for (int i = 0; i < n; ++i) id[i] = i;
+    if (!s.reduced || g.kind == GK_TRIVIAL) {
+        maps.push_back(id);
+        flips.push_back(0);
+    } else if (g.kind == GK_TORUS) {
+        for (int b = 0; b < g.L2; ++b)
+            for (int a = 0; a < g.L1; ++a) {
+                std::vector<int> m(n);
+                for (int y = 0; y < g.L2; ++y)
+                    for (int x = 0; x < g.L1; ++x) m[x + g.L1 * y] = (x + a) % g.L1 + g.L1 * ((y + b) % g.L2);
+                maps.push_back(m);
+                flips.push_back(0);
+            }
+    } else {
+        for (int e = 0; e < g.G; ++e) {
+            maps.emplace_back(g.maps.begin() + (size_t)e * n, g.maps.begin() + (size_t)(e + 1) * n);
+            flips.push_back(e < (int)g.flips.size() ? g.flips[e] : 0ull);
+        }
+    }
+}
+
+uint64_t permute_bits(uint64_t v, const std::vector<int>& m, const Layout& lay) {
+    uint64_t r = 0;
+    for (int i = 0; i < lay.n_sites; ++i) {
+        const uint64_t w = lay.bw[i] >= 64 ? ~0ull : ((1ull << lay.bw[i]) - 1ull);
+        r |= ((v >> lay.off[i]) & w) << lay.off[m[i]];
+    }
+    return r;
+}
+
+// Whether every group element maps the operator's term table onto itself (equal summed amplitude per
+// (mask, row, col)).  Then the reduced row and column iterators give transposed matrices.
+bool op_invariant(edgpu_op_s* op) {
+    if (op->invariant_gen == op->gen) return op->invariant;
+    const Space& s = *op->space;
+    std::vector<std::vector<int>> maps;
+    std::vector<uint64_t> flips;
+    host_group(s, maps, flips);
+    struct K {
+        uint64_t m, r, c;
+        bool operator<(const K& o) const { return m != o.m ? m < o.m : (r != o.r ? r < o.r : c < o.c); }
+    };
+    std::map<K, std::pair<double, double>> base;
+    double scale = 0.0;
+    for (int t = 0; t < op->T; ++t) {
+        const double c = op->coupl[op->cid[t]];
+        auto& a = base[K{op->masks[t], op->rows[t], op->cols[t]}];
+        a.first += op->unit[2 * t] * c;
+        a.second += op->unit[2 * t + 1] * c;
+        scale = std::max(scale, std::hypot(op->unit[2 * t] * c, op->unit[2 * t + 1] * c));
+    }
+    bool inv = true;
+    for (size_t e = 0; e < maps.size() && inv; ++e) {
+        std::map<K, std::pair<double, double>> img;
+        for (const auto& kv : base) {
+            const uint64_t m = permute_bits(kv.first.m, maps[e], s.lay);
+            const uint64_t f = flips[e] & m;
+            auto& a = img[K{m, permute_bits(kv.first.r, maps[e], s.lay) ^ f, permute_bits(kv.first.c, maps[e], s.lay) ^ f}];
+            a.first += kv.second.first;
+            a.second += kv.second.second;
+        }
+        for (const auto& kv : img) {
+            auto it = base.find(kv.first);
+            const double re = it == base.end() ? 0.0 : it->second.first;
+            const double im = it == base.end() ? 0.0 : it->second.second;
+            if (std::hypot(kv.second.first - re, kv.second.second - im) > 1e-12 * std::max(scale, 1e-300)) inv = false;
+        }
+        if (img.size() != base.size()) inv = inv && false;
+    }
+    op->invariant = inv;
+    op->invariant_gen = op->gen;
+    return inv;
+}
+
+}  // namespace
+
+int edgpu_op_is_invariant(edgpu_op oh, int32_t* invariant) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    require(invariant, EDGPU_ERR_ARG, "null output");
+    *invariant = op_invariant(op) ? 1 : 0;
+    API_END
+}
+
 int edgpu_mul_adjoint_device(edgpu_op oh, int32_t precision, const void* x, void* y, int64_t n, int32_t accumulate,
                              void* stream) {
     API_BEGIN
@@ -1276,7 +1369,24 @@ int edgpu_mul_adjoint_device(edgpu_op oh, int32_t precision, const void* x, void
     check_dim(op, n, "state");
     if (n == 0) return EDGPU_OK;
     require(x && y && x != y, EDGPU_ERR_ARG, "bad vectors");
-    launch_product(op, precision, 1, 0, x, y, accumulate ? 1 : 0, nullptr, nullptr, pick_stream(stream));
+    cudaStream_t st = pick_stream(stream);
+    if (op_invariant(op)) {
+        // the adjoint term table, applied by the row formula, is the adjoint of the product's matrix
+        launch_product(op, precision, 1, 0, x, y, accumulate ? 1 : 0, nullptr, nullptr, st);
+        return EDGPU_OK;
+    }
+    // terms that do not commute with the group: the rows of the product's matrix are scattered,
+    // y[c] += conj(H[r, c]) x[r] by atomic adds (summation order not fixed)
+    const size_t vs = precision == EDGPU_FP64 ? 16 : 8;
+    if (!accumulate) EDGPU_CUDA(cudaMemsetAsync(y, 0, n * vs, st));
+    build_blob(op, precision, 0, 0);
+    const Blob& B = op->blob[precision][0][0];
+    HxParams p = B.tmpl;
+    p.gy = x;
+    p.y = y;
+    const int blocks = (int)std::max<long long>(1, std::min<long long>((n + HX_THREADS - 1) / HX_THREADS, 152ll * 32));
+    if (op->space->w32) hx_scatter_launch_w32(B.gk, precision, p, blocks, B.smem_rows, st);
+    else hx_scatter_launch_w64(B.gk, precision, p, blocks, B.smem_rows, st);
     API_END
 }
 

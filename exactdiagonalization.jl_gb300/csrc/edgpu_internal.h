@@ -237,6 +237,10 @@ void hx_sparse_launch_w32(int gk, const HxParams& p, long long row0, long long n
 void hx_sparse_launch_w64(int gk, const HxParams& p, long long row0, long long n_run, int conj_vals, double tol,
                           long long* counts, const long long* row_ptr, long long* cols, double2* vals, size_t smem,
                           cudaStream_t st);
+// Adjoint of the product's matrix by scatter (hx_rows.cuh, hx_scatter_adjoint_kernel): p.gy = input,
+// p.y = output (zeroed or accumulated by the caller); shared memory as the row-per-lane kernel.
+void hx_scatter_launch_w32(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
+void hx_scatter_launch_w64(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
 // Batched sectors in one persistent launch (hx_rows.cuh, hx_multi_kernel), product mode only.
 void hx_multi_launch_w32(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
 void hx_multi_launch_w64(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);

@@ -101,4 +101,17 @@ void hx_sparse_launch_w64(int gk, const HxParams& p, long long row0, long long n
     }
 }
 
+// Adjoint by scatter (terms that do not commute with the group).
+void hx_scatter_launch_w64(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
+    switch (gk * 2 + prec) {
+        case 0 * 2 + 0: return hx_scatter_launch_one<unsigned long long, 0, 0>(p, blocks, smem, st);
+        case 0 * 2 + 1: return hx_scatter_launch_one<unsigned long long, 0, 1>(p, blocks, smem, st);
+        case 1 * 2 + 0: return hx_scatter_launch_one<unsigned long long, 1, 0>(p, blocks, smem, st);
+        case 1 * 2 + 1: return hx_scatter_launch_one<unsigned long long, 1, 1>(p, blocks, smem, st);
+        case 2 * 2 + 0: return hx_scatter_launch_one<unsigned long long, 2, 0>(p, blocks, smem, st);
+        case 2 * 2 + 1: return hx_scatter_launch_one<unsigned long long, 2, 1>(p, blocks, smem, st);
+        default: throw Error(EDGPU_ERR_ARG, "bad product kernel selector");
+    }
+}
+
 }  // namespace edgpu

@@ -303,6 +303,74 @@ __global__ void __launch_bounds__(HX_THREADS) hx_multi_kernel(const HxParams p) 
     }
 }
 
+// Adjoint of the product's matrix by scatter, for terms that do not commute with the group (where the
+// reduced row and column iterators are not transposes of each other): one thread per row r adds
+// conj(H[r, c]) x[r] into y[c] for every target c of the row, and conj(E_r) x[r] into y[r], by atomic
+// adds.  The elements are formed exactly as in the product (rows_tile).
+template <typename W, int GK, int PREC>
+__global__ void __launch_bounds__(HX_THREADS) hx_scatter_adjoint_kernel(const HxParams p) {
+    typedef typename Cx<PREC>::V V;
+    typedef typename Cx<PREC>::R R;
+    extern __shared__ __align__(16) unsigned char sm[];
+    {
+        const int4* src = (const int4*)p.blob;
+        int4* dst = (int4*)sm;
+        for (int i = threadIdx.x; i < p.blob_words16; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const RowsTables<W, PREC> tb(p, sm);
+    const W* __restrict__ keys = (const W*)p.keys;
+    const V* ph = (const V*)(sm + p.o_ph);
+    const int* num = (const int*)(sm + p.o_num);
+    const V* xin = (const V*)p.gy;
+    R* yout = (R*)p.y;
+    const int sb = p.sb;
+    const W smask = (W)((((W)1) << sb) - 1);
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < p.n_rows;
+         r += (long long)gridDim.x * blockDim.x) {
+        const W kr = keys[r];
+        const W b = kr >> sb;
+        const int ri = (int)(kr & smask);
+        const V xr = xin[r];
+        {
+            const V d = ((const V*)p.diag)[r];
+            const V t = cmul(make_conj(d), xr);
+            atomicAdd(yout + 2 * r, t.x);
+            atomicAdd(yout + 2 * r + 1, t.y);
+        }
+        for (int k = 0; k < p.T_o; ++k) {
+            W tm, tr, tf;
+            load_rec3<W>(tb.orec + 4 * k, tm, tr, tf);
+            if ((b & tm) != tr) continue;
+            const W q = b ^ tf;
+            W rep[2] = {q, q};
+            int g = 0;
+            canon_rep<W, GK>(q, p, tb.keep, tb.lut, tb.flips, tb.rlut, tb.keep32, rep[0], g);
+            const bool act[2] = {true, false};
+            long long c[2];
+            int sx[2];
+            key_find_sum2<W>(keys, p.ds, rep, act, c, sx);
+            if (c[0] < 0) continue;
+            V coef = tb.oa[k];
+            if (GK != GK_TRIVIAL) {
+                if (p.want_arg) coef = cmul(coef, ph[num[g]]);
+                coef = cscale(coef, tb.ratio[ri * p.nd + sx[0]]);
+            }
+            const V t = cmul(make_conj(coef), xr);
+            atomicAdd(yout + 2 * c[0], t.x);
+            atomicAdd(yout + 2 * c[0] + 1, t.y);
+        }
+    }
+}
+
+template <typename W, int GK, int PREC>
+void hx_scatter_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
+    auto kern = hx_scatter_adjoint_kernel<W, GK, PREC>;
+    EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<blocks, HX_THREADS, smem, st>>>(p);
+    EDGPU_CUDA(cudaGetLastError());
+}
+
 // Sparse assembly of the representation in FP64 (sparse(opr) and get_row,
 // abstract_operator_representation.jl:135-213): one warp per row.  The lanes evaluate the row's
 // off-diagonal terms (term t in slot t, no match: column -1) and lane 0 adds the diagonal in slot

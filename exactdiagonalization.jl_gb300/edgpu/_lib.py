@@ -71,6 +71,7 @@ SIGNATURES = {
     "edgpu_op_autotune": (ctypes.c_int, [vp, i32, P(i32), P(dbl)]),
     "edgpu_op_sparse": (ctypes.c_int, [vp, i32, dbl, P(i64), P(i64), P(i64), P(dbl)]),
     "edgpu_op_get_row": (ctypes.c_int, [vp, i32, i64, dbl, i64, P(i64), P(i64), P(dbl)]),
+    "edgpu_op_is_invariant": (ctypes.c_int, [vp, P(i32)]),
     "edgpu_op_count_nnz": (ctypes.c_int, [vp, P(i64), P(i64)]),
     "edgpu_mul": (ctypes.c_int, [vp, i32, P(dbl), P(dbl), i64, i32]),
     "edgpu_mul_device": (ctypes.c_int, [vp, i32, vp, vp, i64, i32, vp]),

@@ -578,6 +578,14 @@ class OperatorRepresentation:
         out = np.zeros(self.dimension, dtype=np.complex128)
         return apply_(out, state, self)
 
+    @property
+    def is_invariant(self) -> bool:
+        """Whether the terms commute with every element of the space's symmetry group (then the
+        reference's reduced row and column iterators are transposes of each other)."""
+        v = ctypes.c_int32()
+        check(lib().edgpu_op_is_invariant(self._h, ctypes.byref(v)))
+        return bool(v.value)
+
     # -- sparse assembly (sparse(opr), Matrix(opr), get_row, get_column, getindex) ---------------
     def sparse(self, tol: float = RTOL_F64):
         """sparse(opr) (abstract_operator_representation.jl:135-198) assembled on the GPU in FP64: the

@@ -187,6 +187,12 @@ int edgpu_mul_device(edgpu_op op, int32_t precision, const void* x, void* y, int
  * abstract_operator_representation.jl:278-285, :327-347; reduced_operator_representation.jl:88-116),
  * host complex128 vectors. */
 int edgpu_mul_transpose(edgpu_op op, int32_t precision, const double* x, double* y, int64_t n, int32_t accumulate);
+/* Whether every element of the space's symmetry group maps the operator's terms onto themselves (no
+ * reference counterpart).  Only then are the reference's reduced row iterator (mul!,
+ * reduced_operator_representation.jl:57-85) and column iterator (transpose, :88-116) transposes of
+ * each other; edgpu_mul_adjoint_device is the adjoint of the mul! matrix in both cases. */
+int edgpu_op_is_invariant(edgpu_op op, int32_t* invariant);
+
 /* y = H^dagger x on device vectors (the adjoint product dL/dx = H^dagger gy).  For a reduced
  * representation the orbit phases are recomputed, not stored. */
 int edgpu_mul_adjoint_device(edgpu_op op, int32_t precision, const void* x, void* y, int64_t n,

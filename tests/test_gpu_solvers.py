@@ -210,3 +210,58 @@ def test_full_size_properties_chain24(edgpu):
     dims = [edgpu.symmetry_reduce(hsr, edgpu.translation_symops(L, m)).dimension for m in range(L)]
     assert sum(dims) == math.comb(24, 12)
     assert dims[0] == 112720
+
+
+def test_reduced_sector_random_bond_gradients(edgpu):
+    """The benchmark's gradient setting at a smaller size: chain L=12, per-bond couplings J_b drawn from a
+    seed, 2Sz=0, momentum 0.  The terms do not commute with the translations, so the adjoint goes
+    through the scatter path.  Checked: dL/dJ_b against the oracle and central differences (h=1e-6),
+    dL/dx against directional central differences."""
+    import torch
+    from edgpu import lattice
+    L = 12
+    rng = np.random.default_rng(4)
+    J = 0.5 + rng.random(L)
+    hs, _ = edgpu.spin_half_system(L)
+    hsr = edgpu.represent(edgpu.HilbertSpaceSector(hs, 0))
+    rh = edgpu.symmetry_reduce(hsr, edgpu.translation_symops(L, 0))
+    m, r, c, a, ids = lattice.heisenberg_coupled(hs, lattice.chain_bonds(L))
+    opr = edgpu.OperatorRepresentation.from_terms(rh, m, r, c, a, coupling_ids=ids, couplings=J)
+    assert not opr.is_invariant
+    N = rh.dimension
+    sites = O.spin_half_sites(L)
+    parent = O.hs_get_basis_list(sites, [(0,)])
+    bw, off = O.bit_layout(sites)
+    maps, amps = O.translation_symops((L, 1), (0, 0))
+    red = O.symmetry_reduce(parent, bw, off, maps, amps)
+    x = O.complex_gaussian(N, 5)
+    gy = O.complex_gaussian(N, 6)
+    xd, gyd = torch.from_numpy(x).cuda(), torch.from_numpy(gy).cuda()
+    g = edgpu.coupling_grad(opr, xd, gyd, precision="fp64")
+    for b in range(L):
+        tb = [(int(m[t]), int(r[t]), int(c[t]), complex(a[t])) for t in range(len(m)) if ids[t] == b]
+        want = np.vdot(gy, O.apply_rows(red, tb, x)).real
+        assert abs(g[b] - want) < 1e-12 * max(1.0, abs(want))
+    yv = torch.empty_like(xd)
+
+    def loss(Jv, xv):
+        opr.set_couplings(Jv)
+        edgpu.mul_(yv, opr, xv, precision="fp64")
+        torch.cuda.synchronize()
+        return np.vdot(gy, yv.cpu().numpy()).real
+
+    for b in (0, 7):
+        Jp, Jm = J.copy(), J.copy()
+        Jp[b] += 1e-6
+        Jm[b] -= 1e-6
+        assert abs((loss(Jp, xd) - loss(Jm, xd)) / 2e-6 - g[b]) < 1e-6
+    opr.set_couplings(J)
+    gx = torch.empty_like(xd)
+    edgpu.mul_adjoint_(gx, opr, gyd, precision="fp64")
+    torch.cuda.synchronize()
+    gxn = gx.cpu().numpy()
+    for seed in (1, 2):
+        v = O.complex_gaussian(N, 100 + seed)
+        vd = torch.from_numpy(v).cuda()
+        fd = (loss(J, xd + 1e-6 * vd) - loss(J, xd - 1e-6 * vd)) / 2e-6
+        assert abs(fd - np.vdot(gxn, v).real) < 1e-6
