@@ -51,6 +51,9 @@ WORKLOADS = {
                        desc="spin-1/2 Heisenberg chain L=24 PBC J=1, 2Sz=0, momentum 0 (24-site translations)"),
     "chain16_full": dict(kind="chain_full", L=16, jxy=1.0, jz=1.0, seed=1, lanczos_steps=100, reorth=True,
                          desc="spin-1/2 Heisenberg chain L=16 PBC J=1, 2Sz=0, no symmetry reduction"),
+    "chain28_grad": dict(kind="chain_grad", L=28, k=0, seed=4, x_seed=5, gy_seed=6, cpu_feasible=False,
+                         desc="spin-1/2 Heisenberg chain L=28 PBC, per-bond J_b = 0.5 + U[0,1) (seed 4), 2Sz=0, "
+                              "momentum 0: forward H x, coupling gradient dL/dJ_b = Re<gy|H_b x>, adjoint H^dagger gy"),
     "chain28_k0": dict(kind="chain", L=28, k=0, jxy=1.0, jz=1.0, seed=5, lanczos_steps=200, reorth=True,
                        desc="spin-1/2 Heisenberg chain L=28 PBC, 2Sz=0, momentum 0"),
     "triangular6x5_allk": dict(kind="torus_allk", shape=(6, 5), nn=[(1, 0), (1, 1), (0, 1)],
@@ -585,6 +588,74 @@ def run_gpu_batch(args, wl):
         dist.destroy_process_group()
 
 
+def run_gpu_grad(args, wl):
+    """Forward product, fused coupling gradient and adjoint product of a per-bond-coupling chain."""
+    import numpy as np
+    import torch
+    import edgpu
+    from edgpu import lattice
+
+    world, rank, local = dist_setup()
+    dev = torch.cuda.current_device()
+    L = wl["L"]
+    hs, _ = edgpu.spin_half_system(L)
+    t0 = time.perf_counter()
+    hsr = edgpu.represent(edgpu.HilbertSpaceSector(hs, 0), lazy=True)
+    space = edgpu.symmetry_reduce(hsr, edgpu.translation_symops(L, wl["k"]))
+    t_space = time.perf_counter() - t0
+    J = 0.5 + np.random.default_rng(wl["seed"]).random(L)
+    m, r, c, a, ids = lattice.heisenberg_coupled(hs, lattice.chain_bonds(L))
+    opr = edgpu.OperatorRepresentation.from_terms(space, m, r, c, a, coupling_ids=ids, couplings=J)
+    N = space.dimension
+    n_targets, nnz = opr.count_nnz()
+    map_info = build_maps([space], args)
+    opr.autotune("mixed")
+    stream = torch.cuda.current_stream()
+    res = {}
+    for prec in ("mixed", "fp64"):
+        x = edgpu.random_state(N, wl["x_seed"], prec)
+        gy = edgpu.random_state(N, wl["gy_seed"], prec)
+        y = torch.empty_like(x)
+        gx = torch.empty_like(x)
+        for _ in range(args.warmup):
+            edgpu.mul_(y, opr, x, precision=prec)
+            edgpu.coupling_grad(opr, x, gy, precision=prec, y=y)
+            edgpu.mul_adjoint_(gx, opr, gy, precision=prec)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        times = {}
+        for name, fn in (("forward", lambda: edgpu.mul_(y, opr, x, precision=prec)),
+                         ("forward_and_coupling_grad", lambda: edgpu.coupling_grad(opr, x, gy, precision=prec, y=y)),
+                         ("adjoint", lambda: edgpu.mul_adjoint_(gx, opr, gy, precision=prec))):
+            barrier()
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(args.steps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times[name] = e0.elapsed_time(e1) / args.steps
+        res[prec] = times
+    b = bytes_model(N, nnz, 8)
+    t_fwd = res["mixed"]["forward"] / 1e3
+    t_max, b_all = combine_ranks(t_fwd * args.steps, b * args.steps)
+    peak, peak_src = measured_peak()
+    line = {"metric": METRIC, "value": b_all / t_max / 1e9, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+            "config": {"workload": args.workload, "description": wl["desc"], "N_r": N, "nnz_off": nnz,
+                       "invariant_terms": opr.is_invariant, "setup_s": t_space, "parent_map": map_info,
+                       "ms": res, "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "achieved": b / t_fwd / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": b / t_fwd / 1e9 / peak, "traffic": None, "peak_source": peak_src},
+            "cpu_baseline": None, "e2e": None, "gpu_launches": args.steps, "clocks": None}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -604,6 +675,8 @@ def main():
         run_reference(args, wl)
     elif wl["kind"] == "torus_allk":
         run_gpu_batch(args, wl)
+    elif wl["kind"] == "chain_grad":
+        run_gpu_grad(args, wl)
     else:
         run_gpu(args, wl)
 

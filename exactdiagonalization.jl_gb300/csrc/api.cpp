@@ -106,6 +106,7 @@ struct Blob {
     size_t smem_rows = 0;    // shared memory of the row-per-lane kernel (no per-warp queues)
     int max_blocks_rows = 0;
     int max_blocks_map = 0;  // resident blocks of the parent-state-map kernel (computed on first use)
+    int max_blocks_grad = 0; // resident blocks of the row-per-lane gradient kernel (computed on first use)
     ~Blob() {
         if (d) cudaFree(d);
         if (d_diag) cudaFree(d_diag);
@@ -478,6 +479,35 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
         if (op->space->w32) hx_rows_launch_w32(gk, prec, p, blocks, B.smem_rows, st);
         else hx_rows_launch_w64(gk, prec, p, blocks, B.smem_rows, st);
         return;
+    }
+    if (mode == 1) {
+        // gradient: the row-per-lane kernel with per-thread coupling accumulators when they fit in
+        // shared memory (deterministic block sums, no atomics), else the queued kernel below
+        const size_t gsmem = (size_t)p.o_grad + (size_t)op->n_coupl * HX_THREADS * 8;
+        if (gsmem <= 200 * 1024) {
+            build_blob(op, prec, dir, 0);   // the forward diagonal table
+            p.diag = op->blob[prec][dir][0].d_diag;
+            const int lpr = rows < 0 ? -rows : 1;
+            p.lpr = lpr;
+            p.rows_per_tile = 32 / lpr;
+            p.x = x;
+            p.y = y;
+            p.gy = gy;
+            p.grad_partial = grad_partial;
+            p.accumulate = accumulate;
+            if (B.max_blocks_grad == 0) {
+                const int per_sm = std::max(1, op->space->w32 ? hx_rows_grad_occupancy_w32(B.gk, prec, gsmem)
+                                                               : hx_rows_grad_occupancy_w64(B.gk, prec, gsmem));
+                B.max_blocks_grad = per_sm * std::max(1, g_sm_count);
+            }
+            const long long warps = (p.n_rows + p.rows_per_tile - 1) / p.rows_per_tile;
+            const int blocks = (int)std::max<long long>(
+                1, std::min<long long>((warps + HX_THREADS / 32 - 1) / (HX_THREADS / 32), B.max_blocks_grad));
+            if (blocks_used) *blocks_used = blocks;
+            if (op->space->w32) hx_rows_grad_launch_w32(B.gk, prec, p, blocks, gsmem, st);
+            else hx_rows_grad_launch_w64(B.gk, prec, p, blocks, gsmem, st);
+            return;
+        }
     }
     if (rows < 0) rows = 32;
     p.rows_per_tile = rows;
@@ -1414,7 +1444,8 @@ int edgpu_coupling_grad_device(edgpu_op oh, int32_t precision, const void* x, co
         }
     }
     build_blob(op, precision, 0, 1);
-    const int max_blocks = op->blob[precision][0][1].max_blocks;
+    // partial sums of either gradient kernel: at most 8 resident blocks of 256 threads per SM
+    const int max_blocks = std::max(op->blob[precision][0][1].max_blocks, 8 * std::max(1, g_sm_count));
     op->grad_partial.ensure((size_t)max_blocks * op->n_coupl);
     op->grad_dev.ensure(op->n_coupl);
     int blocks = 0;

@@ -237,6 +237,11 @@ void hx_sparse_launch_w32(int gk, const HxParams& p, long long row0, long long n
 void hx_sparse_launch_w64(int gk, const HxParams& p, long long row0, long long n_run, int conj_vals, double tol,
                           long long* counts, const long long* row_ptr, long long* cols, double2* vals, size_t smem,
                           cudaStream_t st);
+// Row-per-lane gradient mode (hx_rows_kernel MODE 1): shared memory o_grad + n_coupl x HX_THREADS x 8.
+void hx_rows_grad_launch_w32(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
+void hx_rows_grad_launch_w64(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
+int hx_rows_grad_occupancy_w32(int gk, int prec, size_t smem);
+int hx_rows_grad_occupancy_w64(int gk, int prec, size_t smem);
 // Adjoint of the product's matrix by scatter (hx_rows.cuh, hx_scatter_adjoint_kernel): p.gy = input,
 // p.y = output (zeroed or accumulated by the caller); shared memory as the row-per-lane kernel.
 void hx_scatter_launch_w32(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);

@@ -118,4 +118,33 @@ void hx_scatter_launch_w32(int gk, int prec, const HxParams& p, int blocks, size
     }
 }
 
+// Row-per-lane gradient mode (per-thread coupling accumulators in shared memory).
+void hx_rows_grad_launch_w32(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
+    switch (gk * 2 + prec) {
+        case 0 * 2 + 0: return hx_rows_launch_one<unsigned int, 0, 0, 1>(p, blocks, smem, st);
+        case 0 * 2 + 1: return hx_rows_launch_one<unsigned int, 0, 1, 1>(p, blocks, smem, st);
+        case 1 * 2 + 0: return hx_rows_launch_one<unsigned int, 1, 0, 1>(p, blocks, smem, st);
+        case 1 * 2 + 1: return hx_rows_launch_one<unsigned int, 1, 1, 1>(p, blocks, smem, st);
+        case 2 * 2 + 0: return hx_rows_launch_one<unsigned int, 2, 0, 1>(p, blocks, smem, st);
+        case 2 * 2 + 1: return hx_rows_launch_one<unsigned int, 2, 1, 1>(p, blocks, smem, st);
+        case 3 * 2 + 0: return hx_rows_launch_one<unsigned int, 3, 0, 1>(p, blocks, smem, st);
+        case 3 * 2 + 1: return hx_rows_launch_one<unsigned int, 3, 1, 1>(p, blocks, smem, st);
+        default: throw Error(EDGPU_ERR_ARG, "bad product kernel selector");
+    }
+}
+
+int hx_rows_grad_occupancy_w32(int gk, int prec, size_t smem) {
+    switch (gk * 2 + prec) {
+        case 0 * 2 + 0: return hx_rows_occupancy_one<unsigned int, 0, 0, 1>(smem);
+        case 0 * 2 + 1: return hx_rows_occupancy_one<unsigned int, 0, 1, 1>(smem);
+        case 1 * 2 + 0: return hx_rows_occupancy_one<unsigned int, 1, 0, 1>(smem);
+        case 1 * 2 + 1: return hx_rows_occupancy_one<unsigned int, 1, 1, 1>(smem);
+        case 2 * 2 + 0: return hx_rows_occupancy_one<unsigned int, 2, 0, 1>(smem);
+        case 2 * 2 + 1: return hx_rows_occupancy_one<unsigned int, 2, 1, 1>(smem);
+        case 3 * 2 + 0: return hx_rows_occupancy_one<unsigned int, 3, 0, 1>(smem);
+        case 3 * 2 + 1: return hx_rows_occupancy_one<unsigned int, 3, 1, 1>(smem);
+        default: throw Error(EDGPU_ERR_ARG, "bad product kernel selector");
+    }
+}
+
 }  // namespace edgpu

@@ -108,17 +108,18 @@ __device__ __forceinline__ void rows_tile(const HxParams& p, const RowsTables<W,
     if (MODE == 0) {
         if (act && sub == 0) acc = cmul(sc.diag[row], xr);
     } else {
+        // forward diagonal from the diagonal table; the gradient's diagonal part scans the row == col
+        // terms, forms each contribution Re(conj(gy_r) u_t x_r) in the product's precision and adds it
+        // to the coupling's FP64 accumulator
         gv = act ? ((const V*)p.gy)[row] : czero<V>();
-        double2 e = make_double2(0.0, 0.0);
-        if (act && sub == 0)
+        if (act && sub == 0) {
+            acc = cmul(sc.diag[row], xr);
             for (int t = 0; t < p.T_d; ++t)
                 if ((b & tb.dm[t]) == tb.dr[t]) {
-                    e.x += tb.da[t].x;
-                    e.y += tb.da[t].y;
                     const V cu = cmul(from_d2<V>(tb.du[t]), xr);
-                    atomicAdd(&sgrad[tb.dc[t]], (double)gv.x * (double)cu.x + (double)gv.y * (double)cu.y);
+                    sgrad[tb.dc[t] * HX_THREADS + threadIdx.x] += (double)(gv.x * cu.x + gv.y * cu.y);
                 }
-        acc = cmul(from_d2<V>(e), xr);
+        }
     }
     // this lane's terms: t = sub + lpr * k, in chunks of 64
     const int my_terms = (T_o - sub + lpr - 1) / lpr;
@@ -207,7 +208,7 @@ __device__ __forceinline__ void rows_tile(const HxParams& p, const RowsTables<W,
                             cu = cscale(cu, f);
                         }
                         const V t = cmul(cu, xv[h]);
-                        atomicAdd(&sgrad[tb.oc[tt[h]]], (double)gv.x * (double)t.x + (double)gv.y * (double)t.y);
+                        sgrad[tb.oc[tt[h]] * HX_THREADS + threadIdx.x] += (double)(gv.x * t.x + gv.y * t.y);
                     }
                 }
             }
@@ -230,9 +231,11 @@ __global__ void __launch_bounds__(HX_THREADS) hx_rows_kernel(const HxParams p) {
         int4* dst = (int4*)sm;
         for (int i = threadIdx.x; i < p.blob_words16; i += blockDim.x) dst[i] = src[i];
     }
+    // gradient mode: one FP64 accumulator per coupling and thread ([coupling][thread]), reduced per
+    // block in a fixed order at the end (no atomics)
     double* sgrad = (double*)(sm + p.o_grad);
     if (MODE)
-        for (int i = threadIdx.x; i < p.n_coupl; i += blockDim.x) sgrad[i] = 0.0;
+        for (int i = threadIdx.x; i < p.n_coupl * HX_THREADS; i += blockDim.x) sgrad[i] = 0.0;
     __syncthreads();
 
     const RowsTables<W, PREC> tb(p, sm);
@@ -256,8 +259,11 @@ __global__ void __launch_bounds__(HX_THREADS) hx_rows_kernel(const HxParams p) {
         rows_tile<W, GK, PREC, MODE>(p, tb, sc, tile, lane, sgrad);
     if (MODE) {
         __syncthreads();
-        for (int i = threadIdx.x; i < p.n_coupl; i += blockDim.x)
-            p.grad_partial[(size_t)blockIdx.x * p.n_coupl + i] = sgrad[i];
+        for (int i = threadIdx.x; i < p.n_coupl; i += blockDim.x) {
+            double sum = 0.0;
+            for (int t = 0; t < HX_THREADS; ++t) sum += sgrad[i * HX_THREADS + t];
+            p.grad_partial[(size_t)blockIdx.x * p.n_coupl + i] = sum;
+        }
     }
 }
 
