@@ -578,6 +578,61 @@ class OperatorRepresentation:
         out = np.zeros(self.dimension, dtype=np.complex128)
         return apply_(out, state, self)
 
+    # -- algebra on representations (abstract_operator_representation.jl:55-107): the operators are
+    # combined and simplified on the host, then represented again on the same space ---------------
+    def _operator(self):
+        if self.operator is None:
+            raise ArgumentError("this representation was built from a raw term table; it has no operator")
+        return self.operator
+
+    def _same_space(self, other):
+        if other.space is not self.space:
+            raise ArgumentError("The two OperatorRepresentation's do not have the same HilbertSpaceRepresentation")
+
+    def __add__(self, other):
+        if not isinstance(other, OperatorRepresentation):
+            return NotImplemented
+        self._same_space(other)
+        return represent(self.space, simplify(self._operator() + other._operator()))
+
+    def __sub__(self, other):
+        if not isinstance(other, OperatorRepresentation):
+            return NotImplemented
+        self._same_space(other)
+        return represent(self.space, simplify(self._operator() - other._operator()))
+
+    def __mul__(self, other):
+        if isinstance(other, OperatorRepresentation):
+            self._same_space(other)
+            return represent(self.space, simplify(self._operator() * other._operator()))
+        if isinstance(other, (int, float, complex, np.number)):
+            return represent(self.space, simplify(self._operator() * other))
+        return NotImplemented
+
+    def __rmul__(self, other):
+        if isinstance(other, (int, float, complex, np.number)):
+            return represent(self.space, simplify(other * self._operator()))
+        return NotImplemented
+
+    def __truediv__(self, other):
+        return represent(self.space, simplify(self._operator() / other))
+
+    def __neg__(self):
+        return represent(self.space, -self._operator())
+
+    def __pos__(self):
+        return represent(self.space, self._operator())
+
+    def simplify(self):
+        return represent(self.space, simplify(self._operator()))
+
+    def ishermitian(self) -> bool:
+        """ishermitian(opr) (abstract_operator_representation.jl:105-107): of the operator."""
+        op = simplify(self._operator())
+        if isinstance(op, NullOperator):
+            return True
+        return isinstance(simplify(op - op.adjoint()), NullOperator)
+
     @property
     def is_invariant(self) -> bool:
         """Whether the terms commute with every element of the space's symmetry group (then the

@@ -187,3 +187,28 @@ def test_adjoint_is_adjoint_of_the_product_matrix(edgpu):
                 torch.cuda.synchronize()
                 got = yd.cpu().numpy().astype(np.complex128)
                 assert np.linalg.norm(got - want) < tol * np.linalg.norm(want), (prec, m)
+
+
+def test_representation_algebra(edgpu):
+    from edgpu import lattice
+    L = 8
+    hs, hsr, parent, bw, off = chain(edgpu, L)
+    rh = edgpu.symmetry_reduce(hsr, edgpu.translation_symops(L, 2))
+    A = edgpu.represent(rh, lattice.xxz_hamiltonian(hs, lattice.chain_bonds(L), 1.0, 0.5))
+    B = edgpu.represent(rh, lattice.xxz_hamiltonian(hs, [(i, (i + 2) % L) for i in range(L)], 0.3, 0.7))
+    x = O.complex_gaussian(rh.dimension, 4)
+    ax, bx = A @ x, B @ x
+    assert np.allclose((A + B) @ x, ax + bx, atol=TOL)
+    assert np.allclose((A - B) @ x, ax - bx, atol=TOL)
+    assert np.allclose((2.5 * A) @ x, 2.5 * ax, atol=TOL)
+    assert np.allclose((A * 2.5) @ x, 2.5 * ax, atol=TOL)
+    assert np.allclose((A / 4) @ x, ax / 4, atol=TOL)
+    assert np.allclose((-A) @ x, -ax, atol=TOL)
+    assert np.allclose(A.simplify() @ x, ax, atol=TOL)
+    assert A.ishermitian()
+    C = edgpu.represent(rh, edgpu.pauli_matrix(hs, 0, "+") * edgpu.pauli_matrix(hs, 1, "-"))
+    assert not C.ishermitian()
+    other = edgpu.represent(edgpu.symmetry_reduce(hsr, edgpu.translation_symops(L, 3)),
+                            lattice.xxz_hamiltonian(hs, lattice.chain_bonds(L), 1.0, 0.5))
+    with pytest.raises(edgpu.ArgumentError):
+        A + other

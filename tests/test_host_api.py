@@ -129,3 +129,20 @@ def test_direct_product_bit_action():
     p = edgpu.SitePermutation([1, 2, 3, 0])
     m, f = _as_map_flip(hs, p * edgpu.GlobalBitFlip(True))
     assert m == [1, 2, 3, 0] and f == 0b1111
+
+
+def test_representation_algebra_host_side():
+    """opr + opr, opr - opr, number * opr, opr / number, -opr and ishermitian re-represent the combined,
+    simplified operators (abstract_operator_representation.jl:55-107); checked on the host term tables
+    without touching the device."""
+    import edgpu
+    from edgpu import operators as ops
+    hs, _ = edgpu.spin_half_system(4)
+    a = edgpu.pauli_matrix(hs, 0, "x") * edgpu.pauli_matrix(hs, 1, "x")
+    b = edgpu.pauli_matrix(hs, 1, "+") * edgpu.pauli_matrix(hs, 2, "-")
+    assert isinstance(ops.simplify(a - a), ops.NullOperator)
+    s = ops.simplify(a + 2.0 * a)
+    assert all(abs(t.amplitude - 3.0 * u.amplitude) < 1e-15 for t, u in zip(s.terms, ops.simplify(a).terms))
+    h = ops.simplify(b + b.adjoint())
+    assert isinstance(ops.simplify(h - h.adjoint()), ops.NullOperator)
+    assert not isinstance(ops.simplify(b - b.adjoint()), ops.NullOperator)
