@@ -454,6 +454,7 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
         p.map = sp.d_map;
         p.map_wide = sp.map_wide;
         p.map_cb = sp.map_cb;
+        p.map_direct = sp.map_direct;
         if (rows > 0) rows = -1;
     }
     if (rows < 0 && mode == 0) {
@@ -1563,6 +1564,7 @@ HxParams batch_params(edgpu_batch_s* b, int prec, const void* const* xs, void* c
         d[i].map = mapped ? s.d_map : nullptr;
         d[i].map_wide = s.map_wide;
         d[i].map_cb = s.map_cb;
+        d[i].map_direct = s.map_direct;
         d[i].o_ph = F.o_ph[i];
         d[i].o_num = F.o_num[i];
         d[i].want_arg = F.want_arg[i];

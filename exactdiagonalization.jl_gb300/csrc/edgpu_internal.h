@@ -73,13 +73,15 @@ struct Space {
     int dir_K = 0;                   // keys summarised inline per bucket
     double dir_inline = 0.0;         // fraction of keys in buckets answered by their summary
     // Parent-state map of a reduced table whose parent is one fixed-popcount sector (optional):
-    // entry r, for the parent state q of colex rank r (its index in the sorted parent basis), holds the
+    // entry r, for the parent state q of colex rank r (its index in the sorted parent basis; or r = q
+    // itself when the map is direct), holds the
     // index c of q's representative | orbit-size index << map_cb | group element g (g.q = rep)
     // << (map_cb + sb), or all ones when q's orbit has no representative in the table.
     void* d_map = nullptr;
     int map_wide = 0;                // entries are uint64 (else uint32)
     int map_cb = 0;                  // bits of the index field
-    int64_t map_n = 0;               // entries = C(nbits, popcount)
+    int map_direct = 0;              // entries indexed by the state itself (2^nbits entries), not the rank
+    int64_t map_n = 0;               // entries: C(nbits, popcount), or 2^nbits when direct
     void* d_rank = nullptr;          // colex rank chunk table [chunk][ones before][64 values]
     int rank_wide = 0;               // rank table entries are uint64 (else uint32)
     uint64_t map_gen = 0;            // bumped whenever the map is built or freed
@@ -195,7 +197,7 @@ struct HxParams {
     long long n_tiles;                        // batched launch: warp tiles over all sectors
     // parent-state map (replaces canonicalisation and search when map != null)
     const void* map;
-    int map_wide, map_cb;
+    int map_wide, map_cb, map_direct;
     const void* rank_tab;                     // colex rank chunk table
     int rank_wide, rank_k, rank_nc;           // entry width, popcount of the parent sector, chunks
 };
@@ -212,8 +214,8 @@ struct __align__(16) SectorDesc {
     long long tile_end;                       // cumulative warp tiles through this sector
     DirSearch ds;
     const void* map;                          // the sector's parent-state map (or null)
-    int map_wide, map_cb;
-    int o_ph, o_num, want_arg, pad0;
+    int map_wide, map_cb, map_direct;
+    int o_ph, o_num, want_arg;
 };
 
 constexpr int HX_QCAP = 128;         // per-warp target queue capacity (entries; 2 batches of 32 + 31)

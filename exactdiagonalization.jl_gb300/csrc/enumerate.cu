@@ -786,7 +786,7 @@ void build_mapping_t(const Space& red, const Space& parent, int64_t* index_out, 
 // index by the search directory, packed into one entry (all ones when the orbit is not in the table).
 template <typename W, typename E>
 __global__ void k_build_map(long long n_parent, int n, int k, const unsigned long long* C, const W* reps,
-                            DirSearch ds, GroupDev g, int cb, E* out) {
+                            DirSearch ds, GroupDev g, int cb, int direct, E* out) {
     for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n_parent;
          r += (long long)gridDim.x * blockDim.x) {
         const W q = unrank_combo<W>((unsigned long long)r, n, k, C);
@@ -815,7 +815,7 @@ __global__ void k_build_map(long long n_parent, int n, int k, const unsigned lon
         key_find_sum2<W>(reps, ds, reps2, act, c, sx);
         E e = (E)~(E)0;
         if (c[0] >= 0) e = (E)c[0] | ((E)sx[0] << cb) | (g.den > 1 ? (E)gb << (cb + ds.sb) : (E)0);
-        out[r] = e;
+        out[direct ? (long long)q : r] = e;
     }
 }
 
@@ -1056,17 +1056,18 @@ template <typename W>
 void build_map_t(Space& red, cudaStream_t st) {
     const Layout& L = red.lay;
     const int n = L.nbits, k = L.popcount;
-    const long long np = (long long)red.map_n;
+    const long long np = (long long)host_binom(n, k);   // parent states (the map may be larger when direct)
     GroupBuffers gb;
     gb.upload(red.group, L);
     const DirSearch ds = dir_search_of(red);
     const unsigned blocks = (unsigned)std::min<long long>((np + 255) / 256, 152ll * 64);
     if (red.map_wide)
         k_build_map<W, unsigned long long><<<blocks, 256, 0, st>>>(np, n, k, binomial_table(), (const W*)red.d_keys, ds,
-                                                                  gb.dev, red.map_cb, (unsigned long long*)red.d_map);
+                                                                  gb.dev, red.map_cb, red.map_direct,
+                                                                  (unsigned long long*)red.d_map);
     else
         k_build_map<W, unsigned><<<blocks, 256, 0, st>>>(np, n, k, binomial_table(), (const W*)red.d_keys, ds, gb.dev,
-                                                        red.map_cb, (unsigned*)red.d_map);
+                                                        red.map_cb, red.map_direct, (unsigned*)red.d_map);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("parent map: ") + cudaGetErrorString(e));
@@ -1094,6 +1095,10 @@ bool build_parent_map(Space& red, int64_t max_bytes, cudaStream_t st) {
     if (cb + red.sb + gbits > 64) return false;
     const double bytes = (double)np * (wide ? 8.0 : 4.0);
     if (bytes > (double)max_bytes) return false;
+    // direct indexing (entry index = the state itself, no rank) when the whole state range is small:
+    // at most 2^30 entries and 4 GB, within the limit
+    const double dbytes = n <= 30 ? (double)(1ull << n) * (wide ? 8.0 : 4.0) : 1e300;
+    const bool direct = dbytes <= std::min((double)max_bytes, 4.0 * (1ull << 30));
     // colex rank chunk table: T[(c * (k + 1) + j) * 64 + v] = sum over the set bits b of v, in ascending
     // order t = 0, 1, ..., of C(6c + b, j + t + 1)
     const int nc = (n + RANK_CHUNK - 1) / RANK_CHUNK;
@@ -1119,13 +1124,16 @@ bool build_parent_map(Space& red, int64_t max_bytes, cudaStream_t st) {
     if (e == cudaSuccess)
         e = cudaMemcpy(red.d_rank, rank_wide ? (const void*)T.data() : (const void*)T32.data(), tbytes,
                        cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&red.d_map, (size_t)np * (wide ? 8 : 4));
+    const size_t entries = direct ? ((size_t)1 << n) : (size_t)np;
+    if (e == cudaSuccess) e = cudaMalloc(&red.d_map, entries * (wide ? 8 : 4));
+    if (e == cudaSuccess && direct) e = cudaMemsetAsync(red.d_map, 0xff, entries * (wide ? 8 : 4), st);   // invalid
     if (e != cudaSuccess) {
         free_parent_map(red);
         if (e == cudaErrorMemoryAllocation) return false;
         throw Error(EDGPU_ERR_CUDA, std::string("parent map: ") + cudaGetErrorString(e));
     }
-    red.map_n = (int64_t)np;
+    red.map_direct = direct ? 1 : 0;
+    red.map_n = (int64_t)entries;
     red.map_wide = wide;
     red.map_cb = cb;
     red.rank_wide = rank_wide;

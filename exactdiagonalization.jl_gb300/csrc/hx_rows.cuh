@@ -61,7 +61,7 @@ struct RowsSector {
     const int* num;
     bool want_arg;
     const void* map;   // parent-state map (null: canonicalise and search)
-    int map_wide, map_cb;
+    int map_wide, map_cb, map_direct;
 };
 
 // Colex rank of a state with rank_k set bits among the parent's bits: sum over 6-bit chunks of the
@@ -153,7 +153,12 @@ __device__ __forceinline__ void rows_tile(const HxParams& p, const RowsTables<W,
                     load_rec3<W>(tb.orec + 4 * tt[h], tm, tr, tf);
                     q[h] = b ^ tf;
                     unsigned long long e = ~0ull;
-                    if (on[h] && __popcll((unsigned long long)q[h]) == p.rank_k) {
+                    if (sc.map_direct) {
+                        // direct map: every state of the parent's bits has an entry (invalid: all ones)
+                        if (on[h])
+                            e = sc.map_wide ? __ldg((const unsigned long long*)sc.map + (unsigned long long)q[h])
+                                            : (unsigned long long)__ldg((const unsigned*)sc.map + (unsigned long long)q[h]);
+                    } else if (on[h] && __popcll((unsigned long long)q[h]) == p.rank_k) {
                         const unsigned long long r =
                             p.rank_wide ? colex_rank_t<unsigned long long, W>(q[h], (const unsigned long long*)p.rank_tab,
                                                                               k1x64, p.rank_nc)
@@ -252,6 +257,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_rows_kernel(const HxParams p) {
     sc.map = p.map;
     sc.map_wide = p.map_wide;
     sc.map_cb = p.map_cb;
+    sc.map_direct = p.map_direct;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
     const int rpw = 32 / p.lpr;
     const long long n_tiles = (p.n_rows + rpw - 1) / rpw;
@@ -305,6 +311,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_multi_kernel(const HxParams p) 
         sc.map = d.map;
         sc.map_wide = d.map_wide;
         sc.map_cb = d.map_cb;
+        sc.map_direct = d.map_direct;
         rows_tile<W, GK, PREC, 0>(p, tb, sc, tile - tile0, lane, nullptr);
     }
 }
