@@ -136,6 +136,10 @@ struct edgpu_op_s {
     DevBuf<double> x64, y64, z64;
     DevBuf<float> x32, y32;
     DevBuf<double> grad_partial, grad_dev;
+    std::map<std::vector<const void*>, cudaGraphExec_t> host_graphs;   // replayed host-buffer products
+    ~edgpu_op_s() {
+        for (auto& kv : host_graphs) cudaGraphExecDestroy(kv.second);
+    }
 };
 
 // Sectors applied in one persistent launch (hx_multi_kernel).  Per precision: the common shared-memory
@@ -1240,11 +1244,91 @@ int edgpu_op_count_nnz(edgpu_op oh, int64_t* n_targets, int64_t* nnz_off) {
 
 // ---- products ----------------------------------------------------------------------------------
 
+static bool is_pinned(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+// Wait for the library stream by polling an event (lower wake-up latency than a blocking wait for the
+// short products of the host-buffer entry points).
+static void wait_stream(cudaStream_t st) {
+    static thread_local cudaEvent_t ev = nullptr;
+    if (!ev) EDGPU_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    EDGPU_CUDA(cudaEventRecord(ev, st));
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {   // poll for up to 2 ms, then block
+        const cudaError_t e = cudaEventQuery(ev);
+        if (e == cudaSuccess) return;
+        if (e != cudaErrorNotReady) throw Error(EDGPU_ERR_CUDA, std::string("wait: ") + cudaGetErrorString(e));
+        if (std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(2)) break;
+    }
+    EDGPU_CUDA(cudaEventSynchronize(ev));
+}
+
+static void host_product_issue(edgpu_op_s* op, int prec, int dir, const double* x, double* y, int64_t n,
+                               int accumulate, bool conj_io, cudaStream_t st);
+
+// The host-buffer product: copies in, the product (with complex64 conversions in mixed precision),
+// copies out.  With pinned host buffers the sequence is captured once into a CUDA graph per set of
+// buffers and replayed; pageable buffers take the plain stream path.
 static void host_product(edgpu_op_s* op, int prec, int dir, const double* x, double* y, int64_t n, int accumulate,
                          bool conj_io) {
     cudaStream_t st = g_stream;
     op->x64.ensure(2 * n);
     op->y64.ensure(2 * n);
+    if (prec == EDGPU_MIXED) {
+        op->x32.ensure(2 * n);
+        op->y32.ensure(2 * n);
+    }
+    if (!is_pinned(x) || !is_pinned(y)) {
+        host_product_issue(op, prec, dir, x, y, n, accumulate, conj_io, st);
+        wait_stream(st);
+        return;
+    }
+    build_blob(op, prec, dir, 0);
+    const std::vector<const void*> key = {(const void*)x, (const void*)y, (const void*)(intptr_t)n,
+                                          (const void*)(intptr_t)(prec * 8 + dir * 4 + accumulate * 2 + (conj_io ? 1 : 0)),
+                                          (const void*)op->x64.p, (const void*)op->y64.p,
+                                          (const void*)op->space->d_map, (const void*)(uintptr_t)op->gen,
+                                          (const void*)(intptr_t)op->tuned_rows[prec]};
+    auto it = op->host_graphs.find(key);
+    if (it == op->host_graphs.end()) {
+        cudaStream_t cap = nullptr;
+        EDGPU_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            try {
+                host_product_issue(op, prec, dir, x, y, n, accumulate, conj_io, cap);
+            } catch (...) {
+                cudaStreamEndCapture(cap, &graph);
+                if (graph) cudaGraphDestroy(graph);
+                cudaStreamDestroy(cap);
+                throw;
+            }
+            e = cudaStreamEndCapture(cap, &graph);
+        }
+        cudaStreamDestroy(cap);
+        cudaGraphExec_t exec = nullptr;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("host product graph: ") + cudaGetErrorString(e));
+        if (op->host_graphs.size() >= 16) {   // bounded cache
+            for (auto& kv : op->host_graphs) cudaGraphExecDestroy(kv.second);
+            op->host_graphs.clear();
+        }
+        it = op->host_graphs.emplace(key, exec).first;
+    }
+    EDGPU_CUDA(cudaGraphLaunch(it->second, st));
+    wait_stream(st);
+}
+
+static void host_product_issue(edgpu_op_s* op, int prec, int dir, const double* x, double* y, int64_t n,
+                               int accumulate, bool conj_io, cudaStream_t st) {
     EDGPU_CUDA(cudaMemcpyAsync(op->x64.p, x, n * 16, cudaMemcpyHostToDevice, st));
     if (conj_io) launch_conj_c128(n, op->x64.p, st);
     if (accumulate) {
@@ -1254,15 +1338,12 @@ static void host_product(edgpu_op_s* op, int prec, int dir, const double* x, dou
     if (prec == EDGPU_FP64) {
         launch_product(op, prec, dir, 0, op->x64.p, op->y64.p, accumulate, nullptr, nullptr, st);
     } else {
-        op->x32.ensure(2 * n);
-        op->y32.ensure(2 * n);
         launch_c128_to_c64(n, op->x64.p, op->x32.p, st);
         launch_product(op, prec, dir, 0, op->x32.p, op->y32.p, 0, nullptr, nullptr, st);
         launch_c64_to_c128(n, op->y32.p, op->y64.p, accumulate, st);
     }
     if (conj_io) launch_conj_c128(n, op->y64.p, st);
     EDGPU_CUDA(cudaMemcpyAsync(y, op->y64.p, n * 16, cudaMemcpyDeviceToHost, st));
-    EDGPU_CUDA(cudaStreamSynchronize(st));
 }
 
 int edgpu_mul(edgpu_op oh, int32_t precision, const double* x, double* y, int64_t n, int32_t accumulate) {
