@@ -132,20 +132,21 @@ __device__ __forceinline__ void rows_tile(const HxParams& p, const RowsTables<W,
             mm |= (unsigned long long)((b & tm) == tr) << k;
         }
         if (!act) mm = 0ull;
+        constexpr int NT = 2;   // targets per lane and step (the search takes two in lockstep)
         while (__any_sync(0xffffffffu, mm != 0ull)) {
-            int tt[2];
-            bool on[2];
-            W q[2], rep[2];
-            int g[2];
-            long long c[2];
-            int sx[2];
+            int tt[NT];
+            bool on[NT];
+            W q[NT], rep[NT];
+            int g[NT];
+            long long c[NT];
+            int sx[NT];
             if constexpr (GK == GK_MAP) {
                 // parent-state map: colex rank of the target, one load, and the packed entry holds the
                 // representative's index, its orbit-size index and the element reaching it
                 const unsigned long long cmask = (1ull << sc.map_cb) - 1ull;
                 const unsigned k1x64 = ((unsigned)p.rank_k + 1u) << 6;
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
+                for (int h = 0; h < NT; ++h) {
                     on[h] = mm != 0ull;
                     tt[h] = on[h] ? sub + lpr * (k0 + __ffsll((long long)mm) - 1) : 0;
                     mm &= mm - 1ull;
@@ -188,11 +189,11 @@ __device__ __forceinline__ void rows_tile(const HxParams& p, const RowsTables<W,
                 }
                 key_find_sum2<W>(keys, sc.ds, rep, on, c, sx);
             }
-            V xv[2];
+            V xv[NT];
 #pragma unroll
-            for (int h = 0; h < 2; ++h) xv[h] = (c[h] >= 0) ? x[c[h]] : czero<V>();
+            for (int h = 0; h < NT; ++h) xv[h] = (c[h] >= 0) ? x[c[h]] : czero<V>();
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
+            for (int h = 0; h < NT; ++h) {
                 if (c[h] >= 0) {
                     V coef = tb.oa[tt[h]];
                     V phv = czero<V>();
