@@ -438,6 +438,7 @@ void set_map_params(HxParams& p, const Space& sp) {
     p.rank_wide = sp.rank_wide;
     p.rank_k = sp.lay.popcount;
     p.rank_nc = (sp.lay.nbits + RANK_CHUNK - 1) / RANK_CHUNK;
+    p.rank_split = sp.rank_split;
 }
 
 void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, void* y, int accumulate,

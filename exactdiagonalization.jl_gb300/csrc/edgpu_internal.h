@@ -84,6 +84,7 @@ struct Space {
     int64_t map_n = 0;               // entries: C(nbits, popcount), or 2^nbits when direct
     void* d_rank = nullptr;          // colex rank chunk table [chunk][ones before][64 values]
     int rank_wide = 0;               // rank table entries are uint64 (else uint32)
+    int rank_split = 0;              // > 0: split rank tables A (high bits) and B (rank_split low bits)
     uint64_t map_gen = 0;            // bumped whenever the map is built or freed
     ~Space();
 };
@@ -200,6 +201,7 @@ struct HxParams {
     int map_wide, map_cb, map_direct;
     const void* rank_tab;                     // colex rank chunk table
     int rank_wide, rank_k, rank_nc;           // entry width, popcount of the parent sector, chunks
+    int rank_split;                           // > 0: rank = A[q >> rank_split] + B[q & low bits]
 };
 
 // One sector of a batched launch (hx_multi_kernel), kept in shared memory after the common tables.

@@ -1099,23 +1099,41 @@ bool build_parent_map(Space& red, int64_t max_bytes, cudaStream_t st) {
     // at most 2^30 entries and 4 GB, within the limit
     const double dbytes = n <= 30 ? (double)(1ull << n) * (wide ? 8.0 : 4.0) : 1e300;
     const bool direct = dbytes <= std::min((double)max_bytes, 4.0 * (1ull << 30));
-    // colex rank chunk table: T[(c * (k + 1) + j) * 64 + v] = sum over the set bits b of v, in ascending
-    // order t = 0, 1, ..., of C(6c + b, j + t + 1)
-    const int nc = (n + RANK_CHUNK - 1) / RANK_CHUNK;
+    // Colex rank tables.  Split form (n <= 44): with lb = n / 2 low bits, the rank of q = (H << lb) | L
+    // is A[H] + B[L], where A[H] counts the sector's states whose high part is below H (sum over
+    // H' < H of C(lb, k - popc(H'))) and B[L] is the rank of L among the lb-bit words of its popcount.
+    // Chunk form (larger n): T[(c * (k + 1) + j) * 64 + v] = sum over the set bits b of v, in ascending
+    // order t = 0, 1, ..., of C(6c + b, j + t + 1).
     const int rank_wide = np > 0xffffffffull ? 1 : 0;
-    std::vector<unsigned long long> T((size_t)nc * (k + 1) * 64, 0ull);
-    for (int c = 0; c < nc; ++c)
-        for (int j = 0; j <= k; ++j)
-            for (int v = 0; v < 64; ++v) {
-                unsigned long long sum = 0;
-                int t = 0;
-                for (int b = 0; b < RANK_CHUNK; ++b)
-                    if ((v >> b) & 1) {
-                        sum += host_binom(RANK_CHUNK * c + b, j + t + 1);
-                        ++t;
-                    }
-                T[((size_t)c * (k + 1) + j) * 64 + v] = sum;
-            }
+    const int split = n <= 44 ? n / 2 : 0;
+    std::vector<unsigned long long> T;
+    if (split) {
+        const int lb = split, hb = n - split;
+        T.assign(((size_t)1 << hb) + ((size_t)1 << lb), 0ull);
+        unsigned long long acc = 0;
+        for (size_t h = 0; h < ((size_t)1 << hb); ++h) {
+            T[h] = acc;
+            const int need = k - __builtin_popcountll(h);
+            acc += (need >= 0 && need <= lb) ? host_binom(lb, need) : 0ull;
+        }
+        std::vector<unsigned long long> cnt(lb + 1, 0ull);
+        for (size_t l = 0; l < ((size_t)1 << lb); ++l) T[((size_t)1 << hb) + l] = cnt[__builtin_popcountll(l)]++;
+    } else {
+        const int nc = (n + RANK_CHUNK - 1) / RANK_CHUNK;
+        T.assign((size_t)nc * (k + 1) * 64, 0ull);
+        for (int c = 0; c < nc; ++c)
+            for (int j = 0; j <= k; ++j)
+                for (int v = 0; v < 64; ++v) {
+                    unsigned long long sum = 0;
+                    int t = 0;
+                    for (int bb = 0; bb < RANK_CHUNK; ++bb)
+                        if ((v >> bb) & 1) {
+                            sum += host_binom(RANK_CHUNK * c + bb, j + t + 1);
+                            ++t;
+                        }
+                    T[((size_t)c * (k + 1) + j) * 64 + v] = sum;
+                }
+    }
     free_parent_map(red);
     std::vector<unsigned> T32;
     if (!rank_wide) T32.assign(T.begin(), T.end());
@@ -1137,6 +1155,7 @@ bool build_parent_map(Space& red, int64_t max_bytes, cudaStream_t st) {
     red.map_wide = wide;
     red.map_cb = cb;
     red.rank_wide = rank_wide;
+    red.rank_split = split;
     try {
         if (red.w32) build_map_t<uint32_t>(red, st);
         else build_map_t<unsigned long long>(red, st);

@@ -160,11 +160,23 @@ __device__ __forceinline__ void rows_tile(const HxParams& p, const RowsTables<W,
                             e = sc.map_wide ? __ldg((const unsigned long long*)sc.map + (unsigned long long)q[h])
                                             : (unsigned long long)__ldg((const unsigned*)sc.map + (unsigned long long)q[h]);
                     } else if (on[h] && __popcll((unsigned long long)q[h]) == p.rank_k) {
-                        const unsigned long long r =
-                            p.rank_wide ? colex_rank_t<unsigned long long, W>(q[h], (const unsigned long long*)p.rank_tab,
-                                                                              k1x64, p.rank_nc)
-                                        : (unsigned long long)colex_rank_t<unsigned, W>(q[h], (const unsigned*)p.rank_tab,
-                                                                                        k1x64, p.rank_nc);
+                        unsigned long long r;
+                        if (p.rank_split) {
+                            // split tables: rank = A[high part] + B[low part] (entries of the same width)
+                            const unsigned long long qq = (unsigned long long)q[h];
+                            const unsigned long long hi = qq >> p.rank_split;
+                            const unsigned long long lo = qq & ((1ull << p.rank_split) - 1ull);
+                            const unsigned long long nb_a = 1ull << (p.nbits - p.rank_split);
+                            r = p.rank_wide ? __ldg((const unsigned long long*)p.rank_tab + hi) +
+                                                  __ldg((const unsigned long long*)p.rank_tab + nb_a + lo)
+                                            : (unsigned long long)__ldg((const unsigned*)p.rank_tab + hi) +
+                                                  (unsigned long long)__ldg((const unsigned*)p.rank_tab + nb_a + lo);
+                        } else {
+                            r = p.rank_wide ? colex_rank_t<unsigned long long, W>(q[h], (const unsigned long long*)p.rank_tab,
+                                                                                  k1x64, p.rank_nc)
+                                            : (unsigned long long)colex_rank_t<unsigned, W>(q[h], (const unsigned*)p.rank_tab,
+                                                                                            k1x64, p.rank_nc);
+                        }
                         e = sc.map_wide ? __ldg((const unsigned long long*)sc.map + r)
                                         : (unsigned long long)__ldg((const unsigned*)sc.map + r);
                     }
