@@ -1934,8 +1934,7 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
     // value moved by less than conv_tol |E| over the last 5 steps.  With acc: psi += acc[j] v_j only.
     auto run = [&](int steps, double conv_tol, std::vector<double>& A, std::vector<double>& B,
                    const std::vector<double>* acc) {
-        double e_prev = 0.0;
-        bool have_prev = false;
+        std::vector<double> hist;   // lowest Ritz value after every step (with conv_tol > 0)
         for (int j = 0; j < steps; ++j) {
             double* vj = vec64(j);
             if (acc) {
@@ -1969,11 +1968,11 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
             A.push_back(hb[0]);
             const double beta = hb[1];
             if (j == steps - 1 || beta <= 1e-12 * std::max(1.0, std::fabs(hb[0]))) break;
-            if (conv_tol > 0.0 && !acc && (j + 1) % 5 == 0) {
+            if (conv_tol > 0.0 && !acc) {
                 const double e = lowest_eigenvalue(A, B);
-                if (have_prev && std::fabs(e - e_prev) < conv_tol * std::max(1.0, std::fabs(e))) break;
-                e_prev = e;
-                have_prev = true;
+                hist.push_back(e);
+                const size_t h = hist.size();
+                if (h > 5 && std::fabs(e - hist[h - 6]) < conv_tol * std::max(1.0, std::fabs(e))) break;
             }
             B.push_back(beta);
             launch_normalize(N, w.p, d_beta, vec64(j + 1), cur_prec == EDGPU_MIXED ? vin32(j + 1) : nullptr, st);
@@ -2042,10 +2041,20 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
                 "the Krylov basis for full reorthogonalisation does not fit in device memory; use reorth = 0");
         setup(EDGPU_MIXED, store, m1, reorth != 0);
         start_from(nullptr, v0);
-        run(m1, std::max(tol, 1e-7), A, B, nullptr);
-        E = lowest(A, B);
-        done = (int)A.size();
-        ritz_vector(A, B, E);
+        // restarted from its Ritz vector while the stored basis fills up before the eigenvalue settles
+        // (at most n_steps mixed steps in all)
+        const double tol1 = std::max(tol, 1e-9);
+        for (;;) {
+            A.clear();
+            B.clear();
+            const int budget = std::min(m1, m - done);
+            run(budget, tol1, A, B, nullptr);
+            E = lowest(A, B);
+            done += (int)A.size();
+            ritz_vector(A, B, E);
+            if ((int)A.size() < budget || done >= m || store != F32 || m1 == m) break;
+            start_from(psi.p, nullptr);
+        }
         // 2. FP64 Lanczos from the mixed-precision Ritz vector until the eigenvalue settles to tol
         const bool store2 = (reorth || want_vec) && fits64(m);
         setup(EDGPU_FP64, store2 ? F64 : ROLL, m, reorth != 0 && store2);

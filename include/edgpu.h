@@ -241,7 +241,7 @@ void edgpu_batch_destroy(edgpu_batch b);
 /* Lowest eigenvalue by Lanczos on the device: at most n_steps steps from a seeded complex Gaussian
  * start vector (or v0, host complex128 of length dim, if not NULL), full reorthogonalisation when
  * reorth != 0.  Scalars, dots, norms and the tridiagonal eigensolve are FP64; precision selects the
- * product.  tol > 0 stops once the lowest Ritz value moved by less than tol |E| over 5 steps.  With
+ * product.  tol > 0 stops once the lowest Ritz value moved by less than tol |E| over the last 5 steps.  With
  * refine != 0 and EDGPU_MIXED: a mixed-precision run to about 1e-7, then FP64 Lanczos from its Ritz
  * vector until the eigenvalue settles to tol.  Outputs: e0, alphas/betas of the last run (n_steps
  * each, nullable), steps_done (all runs).  ground_state (nullable, host complex128 dim): Ritz vector.
