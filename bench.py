@@ -120,7 +120,7 @@ def build_maps(spaces, args):
     t0 = time.perf_counter()
     entries = nbytes = 0
     for sp in spaces:
-        if not sp.build_map():
+        if not (sp.build_map(args.map_bytes) if args.map_bytes else sp.build_map()):
             return {"built": False}
         n, b = sp.map_info
         entries += n
@@ -350,6 +350,8 @@ def run_gpu(args, wl):
     n_targets, nnz = opr.count_nnz()
     dir_stats = edgpu.search_stats(space)
     map_info = build_maps([space], args)
+    if args.no_pair:
+        opr.set_pair_schedule(False)
     tune_mixed = opr.autotune("mixed")
     tune_fp64 = opr.autotune("fp64")
     stream = torch.cuda.current_stream()
@@ -463,6 +465,8 @@ def run_gpu(args, wl):
                        "nnz_off": nnz, "bytes_per_step": b_mixed, "l2": f"inputs cycled from a pool of {P_mixed} x/y "
                        f"pairs ({2 * P_mixed * N * s_c / 1e6:.0f} MB > 2x L2)", "parallelism": f"replicas x{world}",
                        "rows_per_tile": {"mixed": tune_mixed[0], "fp64": tune_fp64[0]},
+                       "pair_flip_schedule": {"mixed": opr.schedule("mixed")[1], "fp64": opr.schedule("fp64")[1],
+                                              "bond_classes": opr.pair_classes()[0]},
                        "setup_s": t_space, "search_directory": dir_stats, "parent_map": map_info},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_src},
@@ -488,6 +492,9 @@ def run_gpu_batch(args, wl):
     N = sum(dims)
     nnz = sum(o.count_nnz()[1] for o in oprs)
     map_info = build_maps(spaces, args)
+    if args.no_pair:
+        for o in oprs:
+            o.set_pair_schedule(False)
     batch = edgpu.Batch(oprs)
     lpr, tune_ms = batch.autotune("mixed")
     stream = torch.cuda.current_stream()
@@ -572,7 +579,8 @@ def run_gpu_batch(args, wl):
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
             "config": {"workload": args.workload, "description": wl["desc"], "sectors": len(dims), "N_r_total": N,
                        "N_r_min": min(dims), "N_r_max": max(dims), "nnz_off": nnz, "bytes_per_step": b_step,
-                       "lanes_per_row": lpr, "l2": f"inputs cycled from {P} sets of x/y ({2 * P * N * s_c / 1e6:.0f} MB "
+                       "lanes_per_row": lpr, "pair_flip_schedule": batch.schedule("mixed")[1],
+                       "bond_classes": oprs[0].pair_classes()[0], "l2": f"inputs cycled from {P} sets of x/y ({2 * P * N * s_c / 1e6:.0f} MB "
                        f"> 2x L2)", "parallelism": f"replicas x{world}", "setup_s": t_space,
                        "library_graph_ms_per_step": ms_graph, "parent_map": map_info},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -665,6 +673,10 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="chain24_k0")
     ap.add_argument("--no-lanczos", action="store_true")
     ap.add_argument("--no-map", action="store_true", help="canonicalise targets instead of using parent-state maps")
+    ap.add_argument("--map-bytes", type=int, default=0,
+                    help="byte limit of each parent-state map (0: the library default); below the direct map's "
+                         "size the map is rank-indexed")
+    ap.add_argument("--no-pair", action="store_true", help="test every term per row instead of the pair-flip schedule")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()

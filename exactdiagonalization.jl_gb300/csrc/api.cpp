@@ -3,6 +3,7 @@
 // Lanczos driver.  All arithmetic on vectors runs in the CUDA kernels of enumerate.cu, hx*.cu and
 // linalg.cu; there is no CPU fallback.
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -107,9 +108,17 @@ struct Blob {
     int max_blocks_rows = 0;
     int max_blocks_map = 0;  // resident blocks of the parent-state-map kernel (computed on first use)
     int max_blocks_grad = 0; // resident blocks of the row-per-lane gradient kernel (computed on first use)
+    size_t smem_bond = 0;    // shared memory of the mapped pair-flip kernel (the blob's prefix up to the bond tables)
+    size_t smem_bond_canon = 0;   // of the canonicalising one (through the torus row table)
+    size_t term_start = 0;   // offset of the term records in the term image (before: group and torus tables)
+    void* d_pair = nullptr;  // the pair-flip image: group tables, bond classes, torus row table
+    std::vector<unsigned char> pair_host;   // its host copy (batched images start from it)
+    HxParams tmpl_pair{};    // launch template of the pair-flip kernel (offsets into d_pair)
+    int max_blocks_bond[2][2] = {{0, 0}, {0, 0}};   // resident blocks of the pair-flip kernel [mapped][4 targets]
     ~Blob() {
         if (d) cudaFree(d);
         if (d_diag) cudaFree(d_diag);
+        if (d_pair) cudaFree(d_pair);
     }
 };
 
@@ -130,6 +139,9 @@ struct edgpu_op_s {
     std::vector<double> coupl{1.0};
     Blob blob[2][2][2];               // [precision][direction 0 = H, 1 = H^dagger][mode 0 = product, 1 = gradient]
     int tuned_rows[2] = {0, 0};
+    int pair_allowed = 1;             // the caller allows the pair-flip schedule (edgpu_op_set_pair_schedule)
+    int pair_use[2] = {1, 1};         // [precision]: use it where the terms allow it (chosen by the autotuner)
+    int pair_nt[2] = {2, 2};          // [precision]: targets per lane and step with a parent-state map (2 or 4)
     uint64_t gen = 0;                 // bumped whenever the device tables are rebuilt
     uint64_t invariant_gen = ~0ull;   // table generation the invariance flag belongs to
     bool invariant = true;            // the terms commute with every element of the space's group
@@ -149,13 +161,18 @@ struct edgpu_op_s {
 struct edgpu_batch_s {
     std::vector<edgpu_op_s*> ops;
     int lpr[2] = {0, 0};                           // lanes per row (0: default 1)
+    int pair_use[2] = {1, 1};                      // pair-flip schedule where the terms allow it (autotuned)
+    int pair_nt[2] = {2, 2};                       // its targets per lane and step with sector maps
     struct Fused {
         bool ready = false;
         std::vector<uint64_t> gens;                // operator table generations the image was built from
-        std::vector<unsigned char> image;          // common tables + per-sector character tables
+        std::vector<unsigned char> image;          // common tables + per-sector character tables + descriptors
+                                                   // + term records
+        size_t smem_pair = 0;                      // the image's part before the term records
         std::vector<int> o_ph, o_num, want_arg;
         HxParams tmpl{};
         int gk = 0, per_sm = 1, per_sm_map = 0;
+        int per_sm_bond[2][2] = {{0, 0}, {0, 0}};   // pair-flip kernel [mapped][4 targets per step]
         size_t smem = 0;
         int64_t rows = 0;
     } fused[2];
@@ -183,6 +200,139 @@ int hx_max_blocks_per_sm(bool w32, int gk, int prec, int mode, size_t smem);
 namespace {
 
 size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+
+// Bond classes of the pair-flip schedule (hx_bond.cuh).  Applies when every off-diagonal term flips
+// two sites of one bit each (mask = two bits = row ^ col) and each pair's terms come in complete
+// antiparallel (01, 10) and/or parallel (00, 11) couples, as in every Hermitian spin-1/2 exchange.
+// Pairs are sorted by their ring distance and assigned greedily to the first class where one of
+// their two orientations (start, shift) has a free start bit, preferring a class that already has the
+// shift as a component (at most BOND_MAXC components per class).
+struct BondClasses {
+    int ncls = 0;
+    std::vector<int32_t> info;        // [ncls] components | has_parallel << 8
+    std::vector<uint64_t> comp;       // [ncls][BOND_MAXC][4]: shift, antiparallel starts, parallel starts, 0
+    std::vector<uint64_t> flip;       // [ncls][n]
+    std::vector<double> amp;          // [ncls][n][4][2]
+    bool real = true;
+};
+
+bool build_bond_classes(const Layout& lay, const std::vector<uint64_t>& masks, const std::vector<uint64_t>& rows,
+                        const std::vector<uint64_t>& flips, const std::vector<double>& amps, BondClasses& out) {
+    const int n = lay.nbits;
+    if (masks.empty() || n < 2 || n > 64) return false;
+    for (int i = 0; i < lay.n_sites; ++i)
+        if (lay.bw[i] != 1) return false;
+    struct Pair {
+        int a, b;                      // bits a < b
+        double amp[4][2];              // by (b_a, b_b) pattern: index b_a | b_b << 1
+        bool have[4];
+    };
+    std::map<std::pair<int, int>, Pair> pairs;
+    for (size_t t = 0; t < masks.size(); ++t) {
+        const uint64_t m = masks[t];
+        if (__builtin_popcountll(m) != 2 || flips[t] != m || (rows[t] & ~m) != 0) return false;
+        const int a = __builtin_ctzll(m), b = 63 - __builtin_clzll(m);
+        Pair& P = pairs[{a, b}];
+        if (P.a == P.b) {
+            P.a = a;
+            P.b = b;
+            for (int v = 0; v < 4; ++v) {
+                P.amp[v][0] = P.amp[v][1] = 0.0;
+                P.have[v] = false;
+            }
+        }
+        const int pat = (int)((rows[t] >> a) & 1u) | (int)(((rows[t] >> b) & 1u) << 1);
+        P.amp[pat][0] += amps[2 * t];
+        P.amp[pat][1] += amps[2 * t + 1];
+        P.have[pat] = true;
+    }
+    std::vector<Pair> list;
+    for (auto& kv : pairs) {
+        const Pair& P = kv.second;
+        // complete couples only: a row whose bits match one pattern of a couple must have its term
+        if (P.have[1] != P.have[2] || P.have[0] != P.have[3]) return false;
+        list.push_back(P);
+    }
+    auto dist = [n](const Pair& P) { const int d = P.b - P.a; return std::min(d, n - d); };
+    std::stable_sort(list.begin(), list.end(), [&](const Pair& x, const Pair& y) { return dist(x) < dist(y); });
+    struct Cls {
+        uint64_t used = 0;
+        std::vector<int> shifts;
+        std::vector<uint64_t> A, P;
+        std::vector<int> partner = std::vector<int>(64, -1);
+        std::vector<std::array<double, 8>> amp = std::vector<std::array<double, 8>>(64);
+        bool par = false;
+    };
+    std::vector<Cls> cls;
+    for (const Pair& P : list) {
+        const int starts[2] = {P.a, P.b};
+        const int parts[2] = {P.b, P.a};
+        int best_c = -1, best_o = -1, best_score = 3;
+        for (int c = 0; c < (int)cls.size() && best_score > 0; ++c)
+            for (int o = 0; o < 2; ++o) {
+                if ((cls[c].used >> starts[o]) & 1ull) continue;
+                const int sh = ((parts[o] - starts[o]) % n + n) % n;
+                const bool has = std::find(cls[c].shifts.begin(), cls[c].shifts.end(), sh) != cls[c].shifts.end();
+                const int score = has ? 0 : ((int)cls[c].shifts.size() < BOND_MAXC ? 1 : 3);
+                if (score < best_score) {
+                    best_score = score;
+                    best_c = c;
+                    best_o = o;
+                }
+            }
+        if (best_c < 0) {
+            if ((int)cls.size() >= BOND_MAXCLS) return false;
+            cls.emplace_back();
+            best_c = (int)cls.size() - 1;
+            best_o = 0;
+        }
+        Cls& C = cls[best_c];
+        const int st = starts[best_o], pt = parts[best_o];
+        const int sh = ((pt - st) % n + n) % n;
+        int k = (int)(std::find(C.shifts.begin(), C.shifts.end(), sh) - C.shifts.begin());
+        if (k == (int)C.shifts.size()) {
+            C.shifts.push_back(sh);
+            C.A.push_back(0);
+            C.P.push_back(0);
+        }
+        C.used |= 1ull << st;
+        C.partner[st] = pt;
+        // v = b_start | (b_start == b_partner) << 1; pattern index = b_a | b_b << 1 of the pair
+        for (int v = 0; v < 4; ++v) {
+            const int bs = v & 1;
+            const int bp = (v >> 1) ? bs : 1 - bs;
+            const int pat = (st == P.a) ? (bs | (bp << 1)) : (bp | (bs << 1));
+            C.amp[st][2 * v] = P.amp[pat][0];
+            C.amp[st][2 * v + 1] = P.amp[pat][1];
+            if (P.amp[pat][1] != 0.0) out.real = false;
+        }
+        if (P.have[1]) C.A[k] |= 1ull << st;
+        if (P.have[0]) {
+            C.P[k] |= 1ull << st;
+            C.par = true;
+        }
+    }
+    out.ncls = (int)cls.size();
+    out.info.assign(out.ncls, 0);
+    out.comp.assign((size_t)out.ncls * BOND_MAXC * 4, 0);
+    out.flip.assign((size_t)out.ncls * n, 0);
+    out.amp.assign((size_t)out.ncls * n * 8, 0.0);
+    for (int c = 0; c < out.ncls; ++c) {
+        const Cls& C = cls[c];
+        out.info[c] = (int32_t)C.shifts.size() | (C.par ? 1 << 8 : 0);
+        for (size_t k = 0; k < C.shifts.size(); ++k) {
+            out.comp[((size_t)c * BOND_MAXC + k) * 4 + 0] = (uint64_t)C.shifts[k];
+            out.comp[((size_t)c * BOND_MAXC + k) * 4 + 1] = C.A[k];
+            out.comp[((size_t)c * BOND_MAXC + k) * 4 + 2] = C.P[k];
+        }
+        for (int i = 0; i < n; ++i) {
+            if (C.partner[i] < 0) continue;
+            out.flip[(size_t)c * n + i] = (1ull << i) | (1ull << C.partner[i]);
+            for (int e = 0; e < 8; ++e) out.amp[((size_t)c * n + i) * 8 + e] = C.amp[i][e];
+        }
+    }
+    return true;
+}
 
 // Build the shared-memory image of the term, phase and group tables for one (precision, direction,
 // mode) and the kernel parameter template.
@@ -223,18 +373,20 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
         off = align16(off + bytes);
         return (int)o;
     };
+    auto amp_of = [&](int t, bool unit_only, double& re, double& im) {
+        double a = op->unit[2 * t], b = op->unit[2 * t + 1];
+        if (!unit_only) {
+            const double c = op->coupl[op->cid[t]];
+            a *= c;
+            b *= c;
+        }
+        re = a;
+        im = dir ? -b : b;   // adjoint: conj(amplitude) (pure_operator.jl adjoint)
+    };
     HxParams p{};
-    p.o_om = alloc(T_o * 4 * wsz);   // packed records (mask, row, row ^ col, 0)
-    p.o_or = p.o_om;
-    p.o_of = p.o_om;
-    p.o_oa = alloc(T_o * vsz);
-    p.o_ou = alloc(mode ? T_o * vsz : 0);
-    p.o_oc = alloc(mode ? T_o * 4 : 0);
-    p.o_dm = alloc(mode ? T_d * wsz : 0);
-    p.o_dr = alloc(mode ? T_d * wsz : 0);
-    p.o_da = alloc(mode ? T_d * 16 : 0);
-    p.o_du = alloc(mode ? T_d * 16 : 0);
-    p.o_dc = alloc(mode ? T_d * 4 : 0);
+    // One host image: group tables, the pair-flip schedule's bond classes, the torus row table, then
+    // the term records.  Two device images are cut from it: the pair-flip image (everything before the
+    // term records) and the term image (everything but the bond classes, later offsets moved down).
     p.o_ph = alloc(g.den * vsz);
     p.o_num = alloc(g.G * 4);
     p.o_ratio = alloc(nd * nd * rsz);
@@ -247,8 +399,52 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     const bool use_rlut = g.kind == GK_TORUS && g.L2 >= 2 && g.L2 <= TORUS_MAXR && rowbits <= 10 && g.L1 <= 16;
     const bool use_pair = use_rlut && rowbits <= 6;
     const int lut_bits = use_pair ? 2 * rowbits : rowbits;
-    p.o_rlut = use_rlut ? alloc(((size_t)1 << lut_bits) * 4) : -1;
     p.rlut_pair = use_pair ? 1 : 0;
+    BondClasses bc;
+    if (mode == 0) {
+        std::vector<uint64_t> bm, br, bf;
+        std::vector<double> ba;
+        for (int t : offd) {
+            const uint64_t r = dir ? op->cols[t] : op->rows[t];
+            const uint64_t c = dir ? op->rows[t] : op->cols[t];
+            bm.push_back(op->masks[t]);
+            br.push_back(r);
+            bf.push_back(r ^ c);
+            double re, im;
+            amp_of(t, false, re, im);
+            ba.push_back(re);
+            ba.push_back(im);
+        }
+        if (!build_bond_classes(s.lay, bm, br, bf, ba, bc)) bc = BondClasses();
+        // keep the pair-flip tables small enough for full occupancy
+        // keep the pair-flip kernel's shared memory within 48 KB (five or more blocks per SM)
+        const size_t bond_bytes = (size_t)bc.ncls * (BOND_MAXC * 4 * wsz + 16 + s.lay.nbits * (wsz + 4 * vsz));
+        const size_t rlut_bytes = use_rlut ? ((size_t)1 << lut_bits) * 4 : 0;
+        if (off + bond_bytes + rlut_bytes > 48 * 1024) bc = BondClasses();
+    }
+    const int n_b = s.lay.nbits;
+    p.bond_ncls = bc.ncls;
+    p.bond_real = bc.real ? 1 : 0;
+    p.o_bcomp = alloc((size_t)bc.ncls * BOND_MAXC * 4 * wsz);
+    p.o_binfo = alloc((size_t)bc.ncls * 4);
+    p.o_bflip = alloc((size_t)bc.ncls * n_b * wsz);
+    p.o_bamp = alloc((size_t)bc.ncls * n_b * 4 * vsz);
+    // the prefix a mapped pair-flip launch copies ends here; the torus row table follows (needed by
+    // canonicalisation only)
+    const size_t bond_prefix = align16(off);
+    p.o_rlut = use_rlut ? alloc(((size_t)1 << lut_bits) * 4) : -1;
+    const size_t bond_prefix_canon = align16(off);
+    p.o_om = alloc(T_o * 4 * wsz);   // packed records (mask, row, row ^ col, 0)
+    p.o_or = p.o_om;
+    p.o_of = p.o_om;
+    p.o_oa = alloc(T_o * vsz);
+    p.o_ou = alloc(mode ? T_o * vsz : 0);
+    p.o_oc = alloc(mode ? T_o * 4 : 0);
+    p.o_dm = alloc(mode ? T_d * wsz : 0);
+    p.o_dr = alloc(mode ? T_d * wsz : 0);
+    p.o_da = alloc(mode ? T_d * 16 : 0);
+    p.o_du = alloc(mode ? T_d * 16 : 0);
+    p.o_dc = alloc(mode ? T_d * 4 : 0);
     const size_t blob_bytes = align16(off);
     std::vector<unsigned char> h(blob_bytes, 0);
     auto putw = [&](int o, size_t i, uint64_t v) {
@@ -258,16 +454,6 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     auto putv = [&](int o, size_t i, double re, double im) {
         if (prec == EDGPU_FP64) { double v[2] = {re, im}; memcpy(&h[o + i * 16], v, 16); }
         else { float v[2] = {(float)re, (float)im}; memcpy(&h[o + i * 8], v, 8); }
-    };
-    auto amp_of = [&](int t, bool unit_only, double& re, double& im) {
-        double a = op->unit[2 * t], b = op->unit[2 * t + 1];
-        if (!unit_only) {
-            const double c = op->coupl[op->cid[t]];
-            a *= c;
-            b *= c;
-        }
-        re = a;
-        im = dir ? -b : b;   // adjoint: conj(amplitude) (pure_operator.jl adjoint)
     };
     for (int k = 0; k < T_o; ++k) {
         const int t = offd[k];
@@ -348,8 +534,27 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     for (size_t i = 0; i < lut.size(); ++i) putw(p.o_lut, i, lut[i]);
     if (g.kind == GK_GENERIC)
         for (int e = 0; e < g.G; ++e) putw(p.o_flip, e, e < (int)g.flips.size() ? g.flips[e] : 0ull);
+    if (bc.ncls > 0) {
+        for (size_t i = 0; i < bc.comp.size(); ++i) putw(p.o_bcomp, i, bc.comp[i]);
+        memcpy(&h[p.o_binfo], bc.info.data(), bc.info.size() * 4);
+        for (size_t i = 0; i < bc.flip.size(); ++i) putw(p.o_bflip, i, bc.flip[i]);
+        for (size_t i = 0; i < bc.flip.size() * 4; ++i) putv(p.o_bamp, i, bc.amp[2 * i], bc.amp[2 * i + 1]);
+    }
 
-    size_t tot = blob_bytes;
+    // cut the pair-flip image and the term image
+    const size_t bstart = (size_t)p.o_bcomp, bshift = bond_prefix - bstart;
+    std::vector<unsigned char> hp(h.begin(), h.begin() + bond_prefix_canon);
+    HxParams pp = p;
+    std::vector<unsigned char> ht(h.begin(), h.begin() + bstart);
+    ht.insert(ht.end(), h.begin() + bond_prefix, h.end());
+    for (int* o : {&p.o_rlut, &p.o_om, &p.o_or, &p.o_of, &p.o_oa, &p.o_ou, &p.o_oc, &p.o_dm, &p.o_dr, &p.o_da,
+                   &p.o_du, &p.o_dc})
+        if (*o >= (int)bond_prefix) *o -= (int)bshift;
+    const size_t term_start = bond_prefix_canon - bshift;   // term records in the term image
+    h.swap(ht);
+    const size_t blob_bytes_t = h.size();
+
+    size_t tot = blob_bytes_t;
     p.o_grad = (int)tot;
     tot = align16(tot + (mode ? op->n_coupl * 8 : 0));
     p.warp_base = (int)tot;
@@ -367,10 +572,17 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
                          prec == EDGPU_FP64 ? (double*)B.d_diag : nullptr,
                          prec == EDGPU_FP64 ? nullptr : (float*)B.d_diag, g_stream);
     }
-    EDGPU_CUDA(cudaMalloc(&B.d, std::max<size_t>(blob_bytes, 16)));
-    EDGPU_CUDA(cudaMemcpy(B.d, h.data(), blob_bytes, cudaMemcpyHostToDevice));
+    EDGPU_CUDA(cudaMalloc(&B.d, std::max<size_t>(blob_bytes_t, 16)));
+    EDGPU_CUDA(cudaMemcpy(B.d, h.data(), blob_bytes_t, cudaMemcpyHostToDevice));
+    if (B.d_pair) cudaFree(B.d_pair);
+    B.d_pair = nullptr;
+    if (bc.ncls > 0) {
+        EDGPU_CUDA(cudaMalloc(&B.d_pair, std::max<size_t>(hp.size(), 16)));
+        EDGPU_CUDA(cudaMemcpy(B.d_pair, hp.data(), hp.size(), cudaMemcpyHostToDevice));
+    }
+    B.pair_host = hp;
     p.blob = B.d;
-    p.blob_words16 = (int)(blob_bytes / 16);
+    p.blob_words16 = (int)(blob_bytes_t / 16);
     p.T_o = T_o;
     p.T_d = T_d;
     p.G = g.G;
@@ -401,7 +613,19 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     }
     B.gk = gk;
     B.tmpl = p;
+    // the pair-flip template: the term template with the pair image's offsets
+    B.tmpl_pair = p;
+    B.tmpl_pair.blob = B.d_pair;
+    B.tmpl_pair.o_rlut = pp.o_rlut;
+    B.tmpl_pair.o_bcomp = pp.o_bcomp;
+    B.tmpl_pair.o_binfo = pp.o_binfo;
+    B.tmpl_pair.o_bflip = pp.o_bflip;
+    B.tmpl_pair.o_bamp = pp.o_bamp;
     B.smem = tot;
+    B.smem_bond = std::max<size_t>(bond_prefix, 16);
+    B.smem_bond_canon = std::max<size_t>(bond_prefix_canon, 16);
+    B.term_start = term_start;
+    B.max_blocks_bond[0][0] = B.max_blocks_bond[0][1] = B.max_blocks_bond[1][0] = B.max_blocks_bond[1][1] = 0;
     const int per_sm = std::max(1, hx_max_blocks_per_sm(w32, gk, prec, mode, tot));
     B.max_blocks = per_sm * std::max(1, g_sm_count);
     if (!mode) {
@@ -420,8 +644,10 @@ void invalidate_blobs(edgpu_op_s* op) {
             for (auto& c : b) {
                 if (c.d) cudaFree(c.d);
                 if (c.d_diag) cudaFree(c.d_diag);
+                if (c.d_pair) cudaFree(c.d_pair);
                 c.d = nullptr;
                 c.d_diag = nullptr;
+                c.d_pair = nullptr;
                 c.ready = false;
             }
 }
@@ -473,6 +699,32 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
         p.accumulate = accumulate;
         const bool mapped = p.map != nullptr;
         const int gk = mapped ? GK_MAP : B.gk;
+        if (p.bond_ncls > 0 && op->pair_allowed && op->pair_use[prec]) {
+            // pair-flip schedule: matching pairs from bond classes (hx_bond.cuh); copies only the
+            // blob's prefix up to the bond tables
+            const size_t smem = mapped ? B.smem_bond : B.smem_bond_canon;
+            p.blob = B.d_pair;
+            p.o_rlut = B.tmpl_pair.o_rlut;
+            p.o_bcomp = B.tmpl_pair.o_bcomp;
+            p.o_binfo = B.tmpl_pair.o_binfo;
+            p.o_bflip = B.tmpl_pair.o_bflip;
+            p.o_bamp = B.tmpl_pair.o_bamp;
+            p.blob_words16 = (int)(smem / 16);
+            p.bond_nt = (mapped && op->pair_nt[prec] == 4) ? 4 : 2;
+            const bool w32 = op->space->w32;
+            int& mb = B.max_blocks_bond[mapped ? 1 : 0][p.bond_nt == 4 ? 1 : 0];
+            if (mb == 0) {
+                const int per_sm = std::max(1, w32 ? hx_bond_occupancy_w32(gk, prec, p.bond_nt, smem)
+                                                   : hx_bond_occupancy_w64(gk, prec, p.bond_nt, smem));
+                mb = per_sm * std::max(1, g_sm_count);
+            }
+            const long long warps = (p.n_rows + p.rows_per_tile - 1) / p.rows_per_tile;
+            const int blocks = (int)std::max<long long>(1, std::min<long long>((warps + HX_THREADS / 32 - 1) / (HX_THREADS / 32), mb));
+            if (blocks_used) *blocks_used = blocks;
+            if (w32) hx_bond_launch_w32(gk, prec, p, blocks, smem, st);
+            else hx_bond_launch_w64(gk, prec, p, blocks, smem, st);
+            return;
+        }
         if (mapped && B.max_blocks_map == 0) {
             const int per_sm = std::max(1, op->space->w32 ? hx_rows_occupancy_w32(GK_MAP, prec, B.smem_rows)
                                                            : hx_rows_occupancy_w64(GK_MAP, prec, B.smem_rows));
@@ -1087,6 +1339,56 @@ int edgpu_op_set_tiling(edgpu_op oh, int32_t precision, int32_t rows_per_tile) {
     API_END
 }
 
+int edgpu_op_set_pair_schedule(edgpu_op oh, int32_t enable) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    require(enable == 0 || enable == 1 || enable == 2 || enable == 4, EDGPU_ERR_ARG, "enable must be 0, 1, 2 or 4");
+    op->pair_allowed = enable ? 1 : 0;
+    op->pair_use[0] = op->pair_use[1] = enable ? 1 : 0;
+    op->pair_nt[0] = op->pair_nt[1] = enable == 4 ? 4 : 2;
+    API_END
+}
+
+int edgpu_op_get_schedule(edgpu_op oh, int32_t precision, int32_t* rows_per_tile, int32_t* pair_flips) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    check_prec(precision);
+    if (rows_per_tile) *rows_per_tile = op->tuned_rows[precision];
+    if (pair_flips) {
+        build_blob(op, precision, 0, 0);
+        const int rows = op->tuned_rows[precision];
+        const bool on = op->blob[precision][0][0].tmpl.bond_ncls > 0 && op->pair_allowed && op->pair_use[precision] &&
+                        rows <= 0;
+        *pair_flips = on ? ((op->space->d_map && op->pair_nt[precision] == 4) ? 4 : 2) : 0;
+    }
+    API_END
+}
+
+int edgpu_op_pair_classes(edgpu_op oh, int32_t* n_classes, int32_t* n_components) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    std::vector<uint64_t> bm, br, bf;
+    std::vector<double> ba;
+    for (int t = 0; t < op->T; ++t) {
+        if (op->rows[t] == op->cols[t]) continue;
+        bm.push_back(op->masks[t]);
+        br.push_back(op->rows[t]);
+        bf.push_back(op->rows[t] ^ op->cols[t]);
+        const double c = op->coupl[op->cid[t]];
+        ba.push_back(op->unit[2 * t] * c);
+        ba.push_back(op->unit[2 * t + 1] * c);
+    }
+    BondClasses bc;
+    int nc = 0, ncomp = 0;
+    if (build_bond_classes(op->space->lay, bm, br, bf, ba, bc)) {
+        nc = bc.ncls;
+        for (int c = 0; c < nc; ++c) ncomp += bc.info[c] & 0xff;
+    }
+    if (n_classes) *n_classes = nc;
+    if (n_components) *n_components = ncomp;
+    API_END
+}
+
 int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out, double* best_ms_out) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
@@ -1097,6 +1399,12 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     const int n_cands = op->space->d_map ? 3 : 5;
     int best = op->space->d_map ? -1 : 32;
     double best_ms = 1e30;
+    // the row-per-lane schedules are timed with and without the pair-flip schedule when it applies
+    // (unless the caller switched it off): random-access order differs between the two
+    build_blob(op, precision, 0, 0);
+    const bool pair_ok = op->blob[precision][0][0].tmpl.bond_ncls > 0 && op->pair_allowed;
+    int best_pair = pair_ok ? 1 : 0, best_nt = 2;
+    const bool mapped = op->space->d_map != nullptr;
     if (n > 0) {
         const size_t vs = precision == EDGPU_FP64 ? 16 : 8;
         void *x = nullptr, *y = nullptr;
@@ -1107,26 +1415,35 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
         cudaEventCreate(&e1);
         try {
             EDGPU_CUDA(cudaMemsetAsync(x, 0, n * vs, g_stream));
-            for (int ci = 0; ci < n_cands; ++ci) {
-                const int r = cands[ci];
-                launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, g_stream, nullptr, r);
-                float tot = 0.f;
-                const int reps = 3;
-                for (int k = 0; k < reps; ++k) {
-                    EDGPU_CUDA(cudaEventRecord(e0, g_stream));
+            for (int cand = pair_ok ? (mapped ? 2 : 1) : 0; cand >= 0; --cand)
+                for (int ci = 0; ci < n_cands; ++ci) {
+                    // cand 2: pair flips with 4 targets per step, 1: with 2, 0: the term scan
+                    const int pair = cand > 0 ? 1 : 0, nt = cand == 2 ? 4 : 2;
+                    const int r = cands[ci];
+                    if (pair && r > 0) continue;   // the pair-flip schedule is row-per-lane
+                    op->pair_use[precision] = pair;
+                    op->pair_nt[precision] = nt;
                     launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, g_stream, nullptr, r);
-                    EDGPU_CUDA(cudaEventRecord(e1, g_stream));
-                    EDGPU_CUDA(cudaEventSynchronize(e1));
-                    float ms = 0.f;
-                    cudaEventElapsedTime(&ms, e0, e1);
-                    tot += ms;
+                    float tot = 0.f;
+                    const int reps = 3;
+                    for (int k = 0; k < reps; ++k) {
+                        EDGPU_CUDA(cudaEventRecord(e0, g_stream));
+                        launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, g_stream, nullptr, r);
+                        EDGPU_CUDA(cudaEventRecord(e1, g_stream));
+                        EDGPU_CUDA(cudaEventSynchronize(e1));
+                        float ms = 0.f;
+                        cudaEventElapsedTime(&ms, e0, e1);
+                        tot += ms;
+                    }
+                    if (tot / reps < best_ms) {
+                        best_ms = tot / reps;
+                        best = r;
+                        best_pair = pair;
+                        best_nt = nt;
+                    }
                 }
-                if (tot / reps < best_ms) {
-                    best_ms = tot / reps;
-                    best = r;
-                }
-            }
         } catch (...) {
+            if (pair_ok) op->pair_use[precision] = 1;
             cudaFree(x);
             cudaFree(y);
             cudaEventDestroy(e0);
@@ -1137,6 +1454,10 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
         cudaFree(y);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+    }
+    if (pair_ok) {
+        op->pair_use[precision] = best_pair;
+        op->pair_nt[precision] = best_nt;
     }
     op->tuned_rows[precision] = best;
     if (rows_per_tile_out) *rows_per_tile_out = best;
@@ -1569,9 +1890,14 @@ void batch_prepare(edgpu_batch_s* b, int prec) {
     }
     const Blob& B0 = o0->blob[prec][0][0];
     const size_t vsz = prec == EDGPU_FP64 ? 16 : 8;
-    const size_t base = (size_t)B0.tmpl.blob_words16 * 16;
-    F.image.assign(base, 0);
-    if (base) EDGPU_CUDA(cudaMemcpy(F.image.data(), B0.d, base, cudaMemcpyDeviceToHost));
+    // image: the blob's group, bond-class and torus tables, every sector's character tables, room for
+    // the sector descriptors, then the blob's term records (relocated); the pair-flip kernel copies
+    // only the part before the term records
+    const size_t full = (size_t)B0.tmpl.blob_words16 * 16;
+    const size_t tstart = std::min(B0.term_start, full);
+    std::vector<unsigned char> blob_h(full, 0);
+    if (full) EDGPU_CUDA(cudaMemcpy(blob_h.data(), B0.d, full, cudaMemcpyDeviceToHost));
+    F.image = B0.pair_host;   // group tables, bond classes, torus row table
     F.o_ph.assign(n, 0);
     F.o_num.assign(n, 0);
     F.want_arg.assign(n, 0);
@@ -1598,12 +1924,21 @@ void batch_prepare(edgpu_batch_s* b, int prec) {
         any_arg |= F.want_arg[i];
         F.rows += b->ops[i]->space->dim;
     }
-    F.smem = F.image.size() + (size_t)n * sizeof(SectorDesc);
+    F.tmpl = B0.tmpl_pair;   // offsets of the pair image; the term records are relocated below
+    F.tmpl.o_sec = (int)F.image.size();
+    F.image.resize(align16(F.image.size() + (size_t)n * sizeof(SectorDesc)), 0);
+    F.smem_pair = F.image.size();
+    const int delta = (int)F.image.size() - (int)tstart;   // term records move by this many bytes
+    F.image.insert(F.image.end(), blob_h.begin() + tstart, blob_h.end());
+    for (int* o : {&F.tmpl.o_om, &F.tmpl.o_or, &F.tmpl.o_of, &F.tmpl.o_oa, &F.tmpl.o_ou, &F.tmpl.o_oc, &F.tmpl.o_dm,
+                   &F.tmpl.o_dr, &F.tmpl.o_da, &F.tmpl.o_du, &F.tmpl.o_dc})
+        *o += delta;
+    F.tmpl.o_grad += delta;
+    F.tmpl.warp_base += delta;
+    F.smem = F.image.size();
     require(F.smem <= 227 * 1024, EDGPU_ERR_ARG,
             "batched tables do not fit in shared memory (" + std::to_string(F.smem) + " bytes)");
-    F.tmpl = B0.tmpl;
     F.tmpl.want_arg = any_arg;
-    F.tmpl.o_sec = (int)F.image.size();
     F.tmpl.n_sec = n;
     F.tmpl.accumulate = 0;
     F.gk = B0.gk;
@@ -1654,8 +1989,7 @@ HxParams batch_params(edgpu_batch_s* b, int prec, const void* const* xs, void* c
     auto it = b->images[prec].find(key);
     if (it == b->images[prec].end()) {
         std::vector<unsigned char> img(F.image);
-        img.resize(F.smem, 0);
-        memcpy(&img[F.image.size()], d.data(), n * sizeof(SectorDesc));
+        memcpy(&img[F.tmpl.o_sec], d.data(), n * sizeof(SectorDesc));
         void* dev = nullptr;
         EDGPU_CUDA(cudaMalloc(&dev, img.size()));
         cudaError_t e = cudaMemcpy(dev, img.data(), img.size(), cudaMemcpyHostToDevice);
@@ -1674,24 +2008,42 @@ HxParams batch_params(edgpu_batch_s* b, int prec, const void* const* xs, void* c
             }
     }
     p.blob = it->second;
-    p.blob_words16 = (int)(F.smem / 16);
+    p.blob_words16 = (int)(F.smem / 16);   // the pair-flip launch below copies only F.smem_pair
     p.lpr = lpr;
     p.rows_per_tile = rpw;
     p.n_tiles = tiles;
-    if (mapped && F.per_sm_map == 0) {
-        const bool w32 = b->ops[0]->space->w32;
+    const bool w32 = b->ops[0]->space->w32;
+    const bool pair = p.bond_ncls > 0 && b->ops[0]->pair_allowed && b->pair_use[prec];
+    int per_sm = mapped ? F.per_sm_map : F.per_sm;
+    p.bond_nt = (mapped && b->pair_nt[prec] == 4) ? 4 : 2;
+    if (pair) {
+        p.blob_words16 = (int)(F.smem_pair / 16);
+        int& ps = F.per_sm_bond[mapped ? 1 : 0][p.bond_nt == 4 ? 1 : 0];
+        if (ps == 0) {
+            const int gk = mapped ? GK_MAP : F.gk;
+            ps = std::max(1, w32 ? hx_bond_multi_occupancy_w32(gk, prec, p.bond_nt, F.smem_pair)
+                                 : hx_bond_multi_occupancy_w64(gk, prec, p.bond_nt, F.smem_pair));
+        }
+        per_sm = ps;
+    } else if (mapped && F.per_sm_map == 0) {
         F.per_sm_map = std::max(1, w32 ? hx_multi_occupancy_w32(GK_MAP, prec, F.smem) : hx_multi_occupancy_w64(GK_MAP, prec, F.smem));
+        per_sm = F.per_sm_map;
     }
     const long long need = (tiles + HX_THREADS / 32 - 1) / (HX_THREADS / 32);
-    *blocks_out = (int)std::max<long long>(
-        1, std::min<long long>(need, (long long)(mapped ? F.per_sm_map : F.per_sm) * std::max(1, g_sm_count)));
+    *blocks_out = (int)std::max<long long>(1, std::min<long long>(need, (long long)per_sm * std::max(1, g_sm_count)));
     return p;
 }
 
 void batch_launch(edgpu_batch_s* b, int prec, const HxParams& p, int blocks, cudaStream_t st) {
     if (p.n_tiles == 0) return;
     const int gk = p.rank_tab ? GK_MAP : b->fused[prec].gk;   // sector maps present: the map flavour
-    if (b->ops[0]->space->w32) hx_multi_launch_w32(gk, prec, p, blocks, b->fused[prec].smem, st);
+    const bool w32 = b->ops[0]->space->w32;
+    if (p.bond_ncls > 0 && b->ops[0]->pair_allowed && b->pair_use[prec]) {
+        if (w32) hx_bond_multi_launch_w32(gk, prec, p, blocks, b->fused[prec].smem_pair, st);
+        else hx_bond_multi_launch_w64(gk, prec, p, blocks, b->fused[prec].smem_pair, st);
+        return;
+    }
+    if (w32) hx_multi_launch_w32(gk, prec, p, blocks, b->fused[prec].smem, st);
     else hx_multi_launch_w64(gk, prec, p, blocks, b->fused[prec].smem, st);
 }
 
@@ -1727,7 +2079,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
     const size_t vs = precision == EDGPU_FP64 ? 16 : 8;
     int64_t tot = 0;
     for (auto* o : b->ops) tot += o->space->dim;
-    int best = 1;
+    int best = 1, best_pair = 1, best_nt = 2;
     double best_ms = 1e30;
     if (tot > 0) {
         void *x = nullptr, *y = nullptr;
@@ -1751,29 +2103,40 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
         const int keep = b->lpr[precision];
         try {
             EDGPU_CUDA(cudaMemsetAsync(x, 0, tot * vs, g_stream));
-            for (int l : {1, 2, 4}) {
-                b->lpr[precision] = l;
-                int blocks = 0;
-                const HxParams p = batch_params(b, precision, xs.data(), ys.data(), &blocks);
-                batch_launch(b, precision, p, blocks, g_stream);
-                float sum = 0.f;
-                const int reps = 3;
-                for (int k = 0; k < reps; ++k) {
-                    EDGPU_CUDA(cudaEventRecord(e0, g_stream));
+            // lanes per row, with and without the pair-flip schedule where it applies
+            const bool pair_ok = b->fused[precision].tmpl.bond_ncls > 0 && b->ops[0]->pair_allowed;
+            bool mapped = true;
+            for (auto* o : b->ops) mapped = mapped && (o->space->d_map != nullptr || o->space->dim == 0);
+            for (int cand = pair_ok ? (mapped ? 2 : 1) : 0; cand >= 0; --cand)
+                for (int l : {1, 2, 4}) {
+                    b->lpr[precision] = l;
+                    b->pair_use[precision] = cand > 0 ? 1 : 0;
+                    b->pair_nt[precision] = cand == 2 ? 4 : 2;
+                    int blocks = 0;
+                    const HxParams p = batch_params(b, precision, xs.data(), ys.data(), &blocks);
                     batch_launch(b, precision, p, blocks, g_stream);
-                    EDGPU_CUDA(cudaEventRecord(e1, g_stream));
-                    EDGPU_CUDA(cudaEventSynchronize(e1));
-                    float ms = 0.f;
-                    cudaEventElapsedTime(&ms, e0, e1);
-                    sum += ms;
+                    float sum = 0.f;
+                    const int reps = 3;
+                    for (int k = 0; k < reps; ++k) {
+                        EDGPU_CUDA(cudaEventRecord(e0, g_stream));
+                        batch_launch(b, precision, p, blocks, g_stream);
+                        EDGPU_CUDA(cudaEventRecord(e1, g_stream));
+                        EDGPU_CUDA(cudaEventSynchronize(e1));
+                        float ms = 0.f;
+                        cudaEventElapsedTime(&ms, e0, e1);
+                        sum += ms;
+                    }
+                    if (sum / reps < best_ms) {
+                        best_ms = sum / reps;
+                        best = l;
+                        best_pair = cand > 0 ? 1 : 0;
+                        best_nt = cand == 2 ? 4 : 2;
+                    }
                 }
-                if (sum / reps < best_ms) {
-                    best_ms = sum / reps;
-                    best = l;
-                }
-            }
         } catch (...) {
             b->lpr[precision] = keep;
+            b->pair_use[precision] = 1;
+            b->pair_nt[precision] = 2;
             cudaStreamSynchronize(g_stream);
             cudaFree(x);
             cudaFree(y);
@@ -1793,8 +2156,25 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
         cudaEventDestroy(e1);
     }
     b->lpr[precision] = best;
+    b->pair_use[precision] = best_pair;
+    b->pair_nt[precision] = best_nt;
     if (lanes_per_row_out) *lanes_per_row_out = best;
     if (best_ms_out) *best_ms_out = best_ms;
+    API_END
+}
+
+int edgpu_batch_get_schedule(edgpu_batch bh, int32_t precision, int32_t* lanes_per_row, int32_t* pair_flips) {
+    API_BEGIN
+    require(bh, EDGPU_ERR_ARG, "null batch");
+    check_prec(precision);
+    if (lanes_per_row) *lanes_per_row = bh->lpr[precision];
+    if (pair_flips) {
+        batch_prepare(bh, precision);
+        bool mapped = true;
+        for (auto* o : bh->ops) mapped = mapped && (o->space->d_map != nullptr || o->space->dim == 0);
+        const bool on = bh->fused[precision].tmpl.bond_ncls > 0 && bh->ops[0]->pair_allowed && bh->pair_use[precision];
+        *pair_flips = on ? ((mapped && bh->pair_nt[precision] == 4) ? 4 : 2) : 0;
+    }
     API_END
 }
 
@@ -1815,6 +2195,7 @@ int edgpu_batch_mul_device(edgpu_batch bh, int32_t precision, const void* const*
     }
     std::vector<const void*> key;
     key.push_back((const void*)(intptr_t)p.lpr);
+    key.push_back((const void*)(intptr_t)(b->pair_use[precision] * 8 + b->pair_nt[precision]));   // the kernel
     key.push_back(p.blob);   // the image (vectors, sector maps) the launch reads
     for (int i = 0; i < n; ++i) {
         key.push_back(xs[i]);

@@ -202,6 +202,12 @@ struct HxParams {
     const void* rank_tab;                     // colex rank chunk table
     int rank_wide, rank_k, rank_nc;           // entry width, popcount of the parent sector, chunks
     int rank_split;                           // > 0: rank = A[q >> rank_split] + B[q & low bits]
+    // pair-flip schedule (hx_bond.cuh): bond classes of the off-diagonal terms, 0 when the terms are not
+    // all two-site flips of 1-bit sites
+    int bond_ncls;
+    int o_bcomp, o_binfo, o_bflip, o_bamp;    // shared-memory offsets of the class tables
+    int bond_real;                            // every pair amplitude is real
+    int bond_nt;                              // targets per lane and step: 2, or 4 (parent-state map only)
 };
 
 // One sector of a batched launch (hx_multi_kernel), kept in shared memory after the common tables.
@@ -219,6 +225,9 @@ struct __align__(16) SectorDesc {
     int map_wide, map_cb, map_direct;
     int o_ph, o_num, want_arg;
 };
+
+constexpr int BOND_MAXC = 4;       // rotation components per bond class of the pair-flip schedule
+constexpr int BOND_MAXCLS = 24;    // bond classes at most (more: the term-matching schedule)
 
 constexpr int HX_QCAP = 128;         // per-warp target queue capacity (entries; 2 batches of 32 + 31)
 constexpr int HX_THREADS = 256;      // threads per block of the product kernel
@@ -255,6 +264,16 @@ void hx_multi_launch_w32(int gk, int prec, const HxParams& p, int blocks, size_t
 void hx_multi_launch_w64(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
 int hx_multi_occupancy_w32(int gk, int prec, size_t smem);
 int hx_multi_occupancy_w64(int gk, int prec, size_t smem);
+
+// Pair-flip schedule (hx_bond.cuh), product mode only: one sector, and all sectors of a batch.
+void hx_bond_launch_w32(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
+void hx_bond_launch_w64(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
+int hx_bond_occupancy_w32(int gk, int prec, int nt, size_t smem);
+int hx_bond_occupancy_w64(int gk, int prec, int nt, size_t smem);
+void hx_bond_multi_launch_w32(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
+void hx_bond_multi_launch_w64(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
+int hx_bond_multi_occupancy_w32(int gk, int prec, int nt, size_t smem);
+int hx_bond_multi_occupancy_w64(int gk, int prec, int nt, size_t smem);
 
 // ---- the coupling-gradient launch for callers that cannot allocate (noalloc.cu) -----------------
 // Launch state of an operator's gradient-mode tables, read without building anything.

@@ -937,9 +937,12 @@ void dir_t(Space& s, cudaStream_t st) {
     // buckets before most of its keys fit in their bucket summaries)
     const size_t cap_bytes = std::max<size_t>((size_t)512 << 20, 16 * (size_t)n * sizeof(W));
     // candidate shifts: from about one bucket per key (s_hi) down to the smallest the cap allows
-    const int s_hi = std::max(0, bitlen - std::max(1, std::min(nbits_n, bitlen)));
+    // bucket summaries need member fields of at least one bit (shift + sb >= 1): a dense table of
+    // unreduced keys (every state present) gets buckets of two states
+    const int min_shift = s.sb == 0 ? 1 : 0;
+    const int s_hi = std::max(min_shift, bitlen - std::max(1, std::min(nbits_n, bitlen)));
     int s_lo = s_hi;
-    while (s_lo > 0 && s_hi - s_lo < 63 &&
+    while (s_lo > min_shift && s_hi - s_lo < 63 &&
            (size_t)((max_state >> (s_lo - 1)) + 2) * sizeof(unsigned long long) <= cap_bytes)
         --s_lo;
     const int n_shift = s_hi - s_lo + 1;

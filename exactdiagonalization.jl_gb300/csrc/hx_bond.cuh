@@ -1,0 +1,291 @@
+// Pair-flip schedule of the matrix-free product y = H x, for operators whose off-diagonal terms all
+// flip two sites of one bit each (spin-1/2 exchange S+S- + S-S+, and S+S+ / S-S- pair terms): every
+// XXZ, Heisenberg and J1-J2 Hamiltonian built from pauli_matrix products.
+//
+// Replaces the same reference loop as hx_rows.cuh (apply_serial!/apply_parallel! over
+// get_row_iterator, abstract_operator_representation.jl:296-316, reduced_operator_representation.jl:
+// 57-85), with the same elements; only the way a row finds its matching terms differs.  The
+// reference tests every term of the SumOperator against the row (operator_iterator.jl:48-54); for a
+// pair-flip term on sites (i, j) the match depends only on whether bits i and j are equal.
+//
+// The pairs are grouped on the host into bond classes.  Within a class every pair (i, j) is oriented
+// so that its start bits i are distinct, and the class is a union of at most BOND_MAXC rotation
+// components: pairs with j = (i + s) mod n for one shift s.  For a row state b, the bits of
+//     x_s = b ^ rotr_n(b, s)                       (bit i of x_s: b_i != b_{i+s})
+// give every pair of component s whose two bits differ, so
+//     D = OR_s (x_s & A_s) | (~x_s & P_s)
+// (A_s: starts of pairs with a term on antiparallel bits, P_s: on parallel bits) is the set of the
+// class's matching pairs, found with a handful of word operations instead of one test per term.  On
+// a translation-invariant lattice a class is one bond direction (a chain: one class of one component;
+// the 6x6 J1-J2 torus: four classes).  Each lane owns one row (or 1/lpr of its pairs, split by start
+// bit) and walks its classes' set bits, two targets per step: flip mask and amplitude from shared
+// memory (amplitude indexed by the start bit's value and parallel/antiparallel), then the parent-state
+// map or canonicalisation plus search, the gather of x, and accumulation in registers.  The summation
+// order (class, then start bit) is fixed, so results are bit-identical run to run.
+#pragma once
+
+#include "hx_rows.cuh"
+
+namespace edgpu {
+
+// Shared-memory views of the bond-class tables (offsets in HxParams):
+//   comp  [ncls][BOND_MAXC][4] words: shift s, antiparallel starts A, parallel starts P, unused
+//   ninfo [ncls] ints: components | has_parallel << 8
+//   flip  [ncls][n] words: flip mask of the pair starting at bit i (0 when there is none)
+//   amp   [ncls][n][4] amplitudes by v = b_i | (b_i == b_j) << 1
+template <typename W, int PREC>
+struct BondTables {
+    typedef typename Cx<PREC>::V V;
+    const W* comp;
+    const int* ninfo;
+    const W* flip;
+    const V* amp;
+    __device__ __forceinline__ BondTables(const HxParams& p, const unsigned char* sm) {
+        comp = (const W*)(sm + p.o_bcomp);
+        ninfo = (const int*)(sm + p.o_binfo);
+        flip = (const W*)(sm + p.o_bflip);
+        amp = (const V*)(sm + p.o_bamp);
+    }
+};
+
+// Matching pairs of class cls for the row state b (n parent bits, full = the n-bit mask).
+template <typename W, int PREC>
+__device__ __forceinline__ W bond_class_mask(W b, const BondTables<W, PREC>& bt, int cls, int n, W full) {
+    const int info = bt.ninfo[cls];
+    const int nc = info & 0xff;
+    W D = 0;
+    for (int k = 0; k < nc; ++k) {
+        const W* cp = bt.comp + 4 * (cls * BOND_MAXC + k);
+        W s_w, A, P;
+        load_rec3<W>(cp, s_w, A, P);
+        const int s = (int)s_w;
+        const W r = (W)(((b >> s) | (b << (n - s))) & full);   // bit i = b_{(i + s) mod n}
+        const W xs = b ^ r;
+        D |= (xs & A) | (~xs & P);
+    }
+    return D;
+}
+
+__device__ __forceinline__ double fma_r(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fma_r(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+template <typename W>
+__device__ __forceinline__ int lowest_bit(W m) {
+    if constexpr (sizeof(W) == 8) return __ffsll((long long)m) - 1;
+    else return __ffs((int)m) - 1;
+}
+
+// One warp tile of rows (32 / lpr consecutive rows of the sector, lpr lanes each) of the pair-flip
+// schedule; lane sub of a row takes the pairs whose start bit i has i % lpr == sub.  NT targets per
+// lane and step (2 or 4): their lookups, then their gathers, are issued together.
+template <typename W, int GK, int PREC, int NT>
+__device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W, PREC>& tb,
+                                          const BondTables<W, PREC>& bt, const RowsSector<PREC>& sc, long long tile,
+                                          int lane) {
+    typedef typename Cx<PREC>::V V;
+    typedef typename Cx<PREC>::R R;
+    const W* __restrict__ keys = (const W*)sc.keys;
+    const V* __restrict__ x = sc.x;
+    const int sb = p.sb;
+    const W smask = (W)((((W)1) << sb) - 1);
+    const int lpr = p.lpr, sub = lane & (lpr - 1), rpw = 32 / lpr;
+    const long long row = tile * rpw + lane / lpr;
+    const bool act = row < sc.n_rows;
+    const W kr = act ? keys[row] : (W)0;
+    const W b = kr >> sb;
+    const int ri = (int)(kr & smask);
+    const V xr = act ? x[row] : czero<V>();
+    V acc = czero<V>();
+    if (act && sub == 0) acc = cmul(sc.diag[row], xr);
+    const int n = p.nbits;
+    const W full = (W)p.full;
+    // start bits of this lane: i % lpr == sub
+    const W split = lpr == 1 ? (W)~(W)0
+                             : (W)((lpr == 2 ? (W)0x5555555555555555ull : (W)0x1111111111111111ull) << sub);
+    const int ncls = act ? p.bond_ncls : 0;
+    const R* __restrict__ rrow = tb.ratio + ri * p.nd;
+    const bool real_fast = p.bond_real && !sc.want_arg;
+    int cls = -1;
+    bool cpar = false;   // the current class has terms on parallel bits
+    W m = 0;
+    while (true) {
+        // lanes whose class ran out move on to their next class with matching pairs
+        while (m == 0 && cls + 1 < ncls) {
+            ++cls;
+            m = bond_class_mask<W, PREC>(b, bt, cls, n, full) & split;
+            cpar = (bt.ninfo[cls] >> 8) != 0;
+        }
+        if (!__any_sync(0xffffffffu, m != 0)) break;
+        int ti[NT];
+        bool on[NT];
+        W q[NT];
+        int g[NT], sx[NT];
+        long long c[NT];
+#pragma unroll
+        for (int h = 0; h < NT; ++h) {
+            on[h] = m != 0;
+            const int i = on[h] ? lowest_bit<W>(m) : 0;
+            m &= m - 1;
+            ti[h] = on[h] ? cls * n + i : 0;
+            const W f = bt.flip[ti[h]];
+            q[h] = b ^ f;
+            // amplitude slot: b_i, and whether the pair's bits are parallel (classes with such terms)
+            int v = (int)(b >> i) & 1;
+            if (cpar) v |= (__popcll((unsigned long long)(b & f)) != 1) << 1;
+            ti[h] = (ti[h] << 2) | v;
+        }
+#pragma unroll
+        for (int h = 0; h < NT; h += 2) resolve_targets2<W, GK, PREC>(p, tb, sc, q + h, on + h, c + h, sx + h, g + h);
+        V xv[NT];
+#pragma unroll
+        for (int h = 0; h < NT; ++h) xv[h] = (c[h] >= 0) ? x[c[h]] : czero<V>();
+#pragma unroll
+        for (int h = 0; h < NT; ++h) {
+            if (c[h] >= 0) {
+                const V a = bt.amp[ti[h]];
+                if (GK == GK_TRIVIAL) {
+                    acc = cadd(acc, cmul(a, xv[h]));
+                } else if (real_fast) {
+                    // real amplitude, trivial characters: one scale and two fused multiply-adds
+                    const R f = a.x * rrow[sx[h]];
+                    acc.x = fma_r(f, xv[h].x, acc.x);
+                    acc.y = fma_r(f, xv[h].y, acc.y);
+                } else if (p.bond_real) {
+                    // real amplitude times the character: chi(g) (a sqrt(|O_r| / |O_c|))
+                    const R f = a.x * rrow[sx[h]];
+                    const V ph = sc.ph[sc.num[g[h]]];
+                    acc = cadd(acc, cmul(cscale(ph, f), xv[h]));
+                } else {
+                    V coef = a;
+                    if (sc.want_arg) coef = cmul(coef, sc.ph[sc.num[g[h]]]);
+                    coef = cscale(coef, rrow[sx[h]]);
+                    acc = cadd(acc, cmul(coef, xv[h]));
+                }
+            }
+        }
+    }
+    // partial sums of the row's lanes (fixed butterfly order)
+    for (int d = 1; d < lpr; d <<= 1) acc = cadd(acc, shfl_xor_v(acc, d));
+    if (act && sub == 0) {
+        if (p.accumulate) acc = cadd(acc, sc.y[row]);
+        sc.y[row] = acc;
+    }
+}
+
+template <typename W, int GK, int PREC, int NT>
+__global__ void __launch_bounds__(HX_THREADS) hx_bond_kernel(const HxParams p) {
+    typedef typename Cx<PREC>::V V;
+    extern __shared__ __align__(16) unsigned char sm[];
+    {
+        const int4* src = (const int4*)p.blob;
+        int4* dst = (int4*)sm;
+        for (int i = threadIdx.x; i < p.blob_words16; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const RowsTables<W, PREC> tb(p, sm);
+    const BondTables<W, PREC> bt(p, sm);
+    RowsSector<PREC> sc;
+    sc.keys = p.keys;
+    sc.x = (const V*)p.x;
+    sc.y = (V*)p.y;
+    sc.diag = (const V*)p.diag;
+    sc.n_rows = p.n_rows;
+    sc.ds = p.ds;
+    sc.ph = (const V*)(sm + p.o_ph);
+    sc.num = (const int*)(sm + p.o_num);
+    sc.want_arg = p.want_arg != 0;
+    sc.map = p.map;
+    sc.map_wide = p.map_wide;
+    sc.map_cb = p.map_cb;
+    sc.map_direct = p.map_direct;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    const int rpw = 32 / p.lpr;
+    const long long n_tiles = (p.n_rows + rpw - 1) / rpw;
+    for (long long tile = (long long)blockIdx.x * wpb + warp; tile < n_tiles; tile += (long long)gridDim.x * wpb)
+        bond_tile<W, GK, PREC, NT>(p, tb, bt, sc, tile, lane);
+}
+
+// All sectors of a batch in one persistent launch (the tile numbering of hx_multi_kernel).
+template <typename W, int GK, int PREC, int NT>
+__global__ void __launch_bounds__(HX_THREADS) hx_bond_multi_kernel(const HxParams p) {
+    typedef typename Cx<PREC>::V V;
+    extern __shared__ __align__(16) unsigned char sm[];
+    {
+        const int4* src = (const int4*)p.blob;
+        int4* dst = (int4*)sm;
+        for (int i = threadIdx.x; i < p.blob_words16; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const RowsTables<W, PREC> tb(p, sm);
+    const BondTables<W, PREC> bt(p, sm);
+    const SectorDesc* sec = (const SectorDesc*)(sm + p.o_sec);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    int s = 0;
+    long long tile0 = 0;
+    for (long long tile = (long long)blockIdx.x * wpb + warp; tile < p.n_tiles; tile += (long long)gridDim.x * wpb) {
+        while (s + 1 < p.n_sec && tile >= sec[s].tile_end) {
+            tile0 = sec[s].tile_end;
+            ++s;
+        }
+        const SectorDesc& d = sec[s];
+        RowsSector<PREC> sc;
+        sc.keys = d.keys;
+        sc.x = (const V*)d.x;
+        sc.y = (V*)d.y;
+        sc.diag = (const V*)d.diag;
+        sc.n_rows = d.n_rows;
+        sc.ds = d.ds;
+        sc.ph = (const V*)(sm + d.o_ph);
+        sc.num = (const int*)(sm + d.o_num);
+        sc.want_arg = d.want_arg != 0;
+        sc.map = d.map;
+        sc.map_wide = d.map_wide;
+        sc.map_cb = d.map_cb;
+        sc.map_direct = d.map_direct;
+        bond_tile<W, GK, PREC, NT>(p, tb, bt, sc, tile - tile0, lane);
+    }
+}
+
+template <typename W, int GK, int PREC, int NT>
+void hx_bond_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
+    auto kern = hx_bond_kernel<W, GK, PREC, NT>;
+    static size_t smem_set = 0;   // raised once per kernel, never inside a graph capture
+    if (smem > smem_set) {
+        EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        smem_set = smem;
+    }
+    kern<<<blocks, HX_THREADS, smem, st>>>(p);
+    EDGPU_CUDA(cudaGetLastError());
+}
+
+template <typename W, int GK, int PREC, int NT>
+int hx_bond_occupancy_one(size_t smem) {
+    auto kern = hx_bond_kernel<W, GK, PREC, NT>;
+    EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int n = 0;
+    EDGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, HX_THREADS, smem));
+    return n;
+}
+
+template <typename W, int GK, int PREC, int NT>
+void hx_bond_multi_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
+    auto kern = hx_bond_multi_kernel<W, GK, PREC, NT>;
+    static size_t smem_set = 0;
+    if (smem > smem_set) {
+        EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        smem_set = smem;
+    }
+    kern<<<blocks, HX_THREADS, smem, st>>>(p);
+    EDGPU_CUDA(cudaGetLastError());
+}
+
+template <typename W, int GK, int PREC, int NT>
+int hx_bond_multi_occupancy_one(size_t smem) {
+    auto kern = hx_bond_multi_kernel<W, GK, PREC, NT>;
+    EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int n = 0;
+    EDGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, HX_THREADS, smem));
+    return n;
+}
+
+}  // namespace edgpu

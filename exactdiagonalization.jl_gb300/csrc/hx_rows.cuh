@@ -84,6 +84,69 @@ __device__ __forceinline__ T colex_rank_t(W q, const T* __restrict__ tab, unsign
     return r;
 }
 
+// Row c of the representative of a target q in the sector's table (-1: its orbit has no
+// representative there), the representative's orbit-size index sx and the group element g reaching
+// it, through the parent-state map: the entry of q (indexed by q itself for a direct map, else by its
+// colex rank among the parent's states) packs c | sx << map_cb | g << (map_cb + sb).
+template <typename W, int PREC>
+__device__ __forceinline__ void map_lookup(const HxParams& p, const RowsSector<PREC>& sc, W q, bool on, long long& c,
+                                           int& sx, int& g) {
+    const unsigned long long cmask = (1ull << sc.map_cb) - 1ull;
+    unsigned long long e = ~0ull;
+    if (sc.map_direct) {
+        // direct map: every state of the parent's bits has an entry (invalid: all ones)
+        if (on)
+            e = sc.map_wide ? __ldg((const unsigned long long*)sc.map + (unsigned long long)q)
+                            : (unsigned long long)__ldg((const unsigned*)sc.map + (unsigned long long)q);
+    } else if (on && __popcll((unsigned long long)q) == p.rank_k) {
+        unsigned long long r;
+        if (p.rank_split) {
+            // split tables: rank = A[high part] + B[low part] (entries of the same width)
+            const unsigned long long qq = (unsigned long long)q;
+            const unsigned long long hi = qq >> p.rank_split;
+            const unsigned long long lo = qq & ((1ull << p.rank_split) - 1ull);
+            const unsigned long long nb_a = 1ull << (p.nbits - p.rank_split);
+            r = p.rank_wide ? __ldg((const unsigned long long*)p.rank_tab + hi) +
+                                  __ldg((const unsigned long long*)p.rank_tab + nb_a + lo)
+                            : (unsigned long long)__ldg((const unsigned*)p.rank_tab + hi) +
+                                  (unsigned long long)__ldg((const unsigned*)p.rank_tab + nb_a + lo);
+        } else {
+            const unsigned k1x64 = ((unsigned)p.rank_k + 1u) << 6;
+            r = p.rank_wide ? colex_rank_t<unsigned long long, W>(q, (const unsigned long long*)p.rank_tab, k1x64,
+                                                                  p.rank_nc)
+                            : (unsigned long long)colex_rank_t<unsigned, W>(q, (const unsigned*)p.rank_tab, k1x64,
+                                                                            p.rank_nc);
+        }
+        e = sc.map_wide ? __ldg((const unsigned long long*)sc.map + r) : (unsigned long long)__ldg((const unsigned*)sc.map + r);
+    }
+    const unsigned long long ci = e & cmask;
+    c = (ci == cmask) ? -1 : (long long)ci;
+    sx = (int)((e >> sc.map_cb) & ((1ull << p.sb) - 1ull));
+    g = (int)(e >> (sc.map_cb + p.sb)) & 0xfff;
+}
+
+// Resolve two targets q[0..1] (on[h]: the slot holds a target): row c[h] (-1: none), orbit-size
+// index sx[h] and group element g[h], by the parent-state map (GK_MAP) or by canonicalisation to the
+// orbit minimum and the bucketed search of the sector's table (both searches in lockstep).
+template <typename W, int GK, int PREC>
+__device__ __forceinline__ void resolve_targets2(const HxParams& p, const RowsTables<W, PREC>& tb,
+                                                 const RowsSector<PREC>& sc, const W* q, const bool* on, long long* c,
+                                                 int* sx, int* g) {
+    if constexpr (GK == GK_MAP) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) map_lookup<W, PREC>(p, sc, q[h], on[h], c[h], sx[h], g[h]);
+    } else {
+        W rep[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            rep[h] = q[h];
+            g[h] = 0;
+            if (on[h]) canon_rep<W, GK>(q[h], p, tb.keep, tb.lut, tb.flips, tb.rlut, tb.keep32, rep[h], g[h]);
+        }
+        key_find_sum2<W>((const W*)sc.keys, sc.ds, rep, on, c, sx);
+    }
+}
+
 // One warp tile of rows (rows_per_tile = 32 / lpr consecutive rows of the sector, lpr lanes each).
 template <typename W, int GK, int PREC, int MODE>
 __device__ __forceinline__ void rows_tile(const HxParams& p, const RowsTables<W, PREC>& tb, const RowsSector<PREC>& sc,
@@ -136,71 +199,20 @@ __device__ __forceinline__ void rows_tile(const HxParams& p, const RowsTables<W,
         while (__any_sync(0xffffffffu, mm != 0ull)) {
             int tt[NT];
             bool on[NT];
-            W q[NT], rep[NT];
+            W q[NT];
             int g[NT];
             long long c[NT];
             int sx[NT];
-            if constexpr (GK == GK_MAP) {
-                // parent-state map: colex rank of the target, one load, and the packed entry holds the
-                // representative's index, its orbit-size index and the element reaching it
-                const unsigned long long cmask = (1ull << sc.map_cb) - 1ull;
-                const unsigned k1x64 = ((unsigned)p.rank_k + 1u) << 6;
 #pragma unroll
-                for (int h = 0; h < NT; ++h) {
-                    on[h] = mm != 0ull;
-                    tt[h] = on[h] ? sub + lpr * (k0 + __ffsll((long long)mm) - 1) : 0;
-                    mm &= mm - 1ull;
-                    W tm, tr, tf;
-                    load_rec3<W>(tb.orec + 4 * tt[h], tm, tr, tf);
-                    q[h] = b ^ tf;
-                    unsigned long long e = ~0ull;
-                    if (sc.map_direct) {
-                        // direct map: every state of the parent's bits has an entry (invalid: all ones)
-                        if (on[h])
-                            e = sc.map_wide ? __ldg((const unsigned long long*)sc.map + (unsigned long long)q[h])
-                                            : (unsigned long long)__ldg((const unsigned*)sc.map + (unsigned long long)q[h]);
-                    } else if (on[h] && __popcll((unsigned long long)q[h]) == p.rank_k) {
-                        unsigned long long r;
-                        if (p.rank_split) {
-                            // split tables: rank = A[high part] + B[low part] (entries of the same width)
-                            const unsigned long long qq = (unsigned long long)q[h];
-                            const unsigned long long hi = qq >> p.rank_split;
-                            const unsigned long long lo = qq & ((1ull << p.rank_split) - 1ull);
-                            const unsigned long long nb_a = 1ull << (p.nbits - p.rank_split);
-                            r = p.rank_wide ? __ldg((const unsigned long long*)p.rank_tab + hi) +
-                                                  __ldg((const unsigned long long*)p.rank_tab + nb_a + lo)
-                                            : (unsigned long long)__ldg((const unsigned*)p.rank_tab + hi) +
-                                                  (unsigned long long)__ldg((const unsigned*)p.rank_tab + nb_a + lo);
-                        } else {
-                            r = p.rank_wide ? colex_rank_t<unsigned long long, W>(q[h], (const unsigned long long*)p.rank_tab,
-                                                                                  k1x64, p.rank_nc)
-                                            : (unsigned long long)colex_rank_t<unsigned, W>(q[h], (const unsigned*)p.rank_tab,
-                                                                                            k1x64, p.rank_nc);
-                        }
-                        e = sc.map_wide ? __ldg((const unsigned long long*)sc.map + r)
-                                        : (unsigned long long)__ldg((const unsigned*)sc.map + r);
-                    }
-                    const unsigned long long ci = e & cmask;
-                    c[h] = (ci == cmask) ? -1 : (long long)ci;
-                    sx[h] = (int)((e >> sc.map_cb) & ((1ull << p.sb) - 1ull));
-                    g[h] = (int)(e >> (sc.map_cb + p.sb)) & 0xfff;
-                }
-            } else {
-                (void)sc.map;
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    on[h] = mm != 0ull;
-                    tt[h] = on[h] ? sub + lpr * (k0 + __ffsll((long long)mm) - 1) : 0;
-                    mm &= mm - 1ull;
-                    W tm, tr, tf;
-                    load_rec3<W>(tb.orec + 4 * tt[h], tm, tr, tf);
-                    q[h] = b ^ tf;
-                    rep[h] = q[h];
-                    g[h] = 0;
-                    if (on[h]) canon_rep<W, GK>(q[h], p, tb.keep, tb.lut, tb.flips, tb.rlut, tb.keep32, rep[h], g[h]);
-                }
-                key_find_sum2<W>(keys, sc.ds, rep, on, c, sx);
+            for (int h = 0; h < NT; ++h) {
+                on[h] = mm != 0ull;
+                tt[h] = on[h] ? sub + lpr * (k0 + __ffsll((long long)mm) - 1) : 0;
+                mm &= mm - 1ull;
+                W tm, tr, tf;
+                load_rec3<W>(tb.orec + 4 * tt[h], tm, tr, tf);
+                q[h] = b ^ tf;
             }
+            resolve_targets2<W, GK, PREC>(p, tb, sc, q, on, c, sx, g);
             V xv[NT];
 #pragma unroll
             for (int h = 0; h < NT; ++h) xv[h] = (c[h] >= 0) ? x[c[h]] : czero<V>();

@@ -564,6 +564,25 @@ class OperatorRepresentation:
     def set_tiling(self, precision, rows_per_tile):
         check(lib().edgpu_op_set_tiling(self._h, _prec(precision), int(rows_per_tile)))
 
+    def set_pair_schedule(self, enable, targets_per_step: int = 2):
+        """Use (default) or bypass the pair-flip schedule of the product for operators whose
+        off-diagonal terms all flip two spin-1/2 sites; bypassed, every row tests every term.
+        targets_per_step: 2, or 4 (with a parent-state map)."""
+        check(lib().edgpu_op_set_pair_schedule(self._h, int(targets_per_step) if enable else 0))
+
+    def schedule(self, precision="mixed"):
+        """(rows_per_tile as in set_tiling, pair flips) used by the product: pair flips = 0 when
+        every row tests every term, else the targets per lane and step of the pair-flip schedule."""
+        a, b = ctypes.c_int32(), ctypes.c_int32()
+        check(lib().edgpu_op_get_schedule(self._h, _prec(precision), ctypes.byref(a), ctypes.byref(b)))
+        return int(a.value), int(b.value)
+
+    def pair_classes(self):
+        """(bond classes, rotation components) of the pair-flip schedule; (0, 0) when it does not apply."""
+        a, b = ctypes.c_int32(), ctypes.c_int32()
+        check(lib().edgpu_op_pair_classes(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return int(a.value), int(b.value)
+
     def __matmul__(self, state):
         """opr * state: allocates out and calls apply! (operator_representation.jl:122-129)."""
         if _is_torch(state):
@@ -825,8 +844,15 @@ class Batch:
         """Lanes per row of the batched launch: 0 (default, 1), 1, 2 or 4."""
         check(lib().edgpu_batch_set_tiling(self._h, _prec(precision), int(lanes_per_row)))
 
+    def schedule(self, precision="mixed"):
+        """(lanes per row, pair flips as in OperatorRepresentation.schedule) of the batched launch."""
+        a, b = ctypes.c_int32(), ctypes.c_int32()
+        check(lib().edgpu_batch_get_schedule(self._h, _prec(precision), ctypes.byref(a), ctypes.byref(b)))
+        return int(a.value), int(b.value)
+
     def autotune(self, precision="mixed"):
-        """Time 1, 2 and 4 lanes per row and keep the fastest; returns (lanes_per_row, ms)."""
+        """Time 1, 2 and 4 lanes per row, with and without the pair-flip schedule, and keep the
+        fastest; returns (lanes_per_row, ms)."""
         l = ctypes.c_int32()
         ms = ctypes.c_double()
         check(lib().edgpu_batch_autotune(self._h, _prec(precision), ctypes.byref(l), ctypes.byref(ms)))

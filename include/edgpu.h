@@ -149,10 +149,26 @@ void edgpu_op_destroy(edgpu_op op);
 /* Schedule of the product kernel: -1, -2 or -4 for 1, 2 or 4 lanes per row (0 = default, one lane
  * per row), or the rows per warp tile of the queued schedule (a divisor of 32). */
 int edgpu_op_set_tiling(edgpu_op op, int32_t precision, int32_t rows_per_tile);
-/* In-library autotuner: times the product for each candidate schedule (1, 2 or 4 lanes per row;
- * queued with 32 or 16 rows per warp tile) on this operator and keeps the fastest
- * (rows_per_tile_out: the schedule as in edgpu_op_set_tiling; best_ms_out nullable). */
+/* In-library autotuner: times the product for each candidate schedule (1, 2 or 4 lanes per row, each
+ * with and without the pair-flip schedule where it applies; queued with 32 or 16 rows per warp tile)
+ * on this operator and keeps the fastest (rows_per_tile_out: the schedule as in edgpu_op_set_tiling;
+ * best_ms_out nullable). */
 int edgpu_op_autotune(edgpu_op op, int32_t precision, int32_t* rows_per_tile_out, double* best_ms_out);
+/* Pair-flip schedule of the row-per-lane product (enable = 1, the default): when every off-diagonal
+ * term flips two 1-bit sites (spin-1/2 exchange and pair terms), a row finds its matching terms from
+ * bond classes (a few word operations per class) instead of testing every term.  Same elements as the
+ * term scan of get_row_iterator (operator_iterator.jl:48-54, reduced_operator_representation.jl:57-85);
+ * the targets are summed by bond class, then start bit, rather than in term order.  enable = 0 keeps
+ * the term scan; 2 or 4 sets the targets each lane looks up per step (4 applies with a parent-state
+ * map; 1 = 2).  edgpu_op_autotune may change the choice. */
+int edgpu_op_set_pair_schedule(edgpu_op op, int32_t enable);
+/* Bond classes of the pair-flip schedule for this operator (0 when the terms do not allow it) and
+ * their rotation components in total. */
+int edgpu_op_pair_classes(edgpu_op op, int32_t* n_classes, int32_t* n_components);
+/* The schedule the product uses for this precision: rows_per_tile as in edgpu_op_set_tiling (0 =
+ * default) and pair_flips = 0 when every row tests every term, else the targets each lane looks up
+ * per step in the pair-flip schedule (2, or 4 with a parent-state map); either pointer nullable. */
+int edgpu_op_get_schedule(edgpu_op op, int32_t precision, int32_t* rows_per_tile, int32_t* pair_flips);
 /* Sparse matrix of the representation, assembled on the device in FP64: rows sorted by column,
  * entries of equal column summed, entries with |value| < tol dropped (tol: the reference's
  * Base.rtoldefault(Float64) = sqrt(eps) gives its default).  This is sparse(opr)
@@ -227,9 +243,12 @@ int edgpu_coupling_grad_device_noalloc(edgpu_op op, int32_t precision, const voi
 int edgpu_batch_create(int32_t n_ops, const edgpu_op* ops, edgpu_batch* out);
 /* Lanes per row of the batched launch for this precision: 0 (default: 1), 1, 2 or 4. */
 int edgpu_batch_set_tiling(edgpu_batch b, int32_t precision, int32_t lanes_per_row);
-/* In-library autotuner: times the batched launch for 1, 2 and 4 lanes per row on scratch vectors
+/* In-library autotuner: times the batched launch for 1, 2 and 4 lanes per row, with and without the
+ * pair-flip schedule where it applies (and the first operator allows it), on scratch vectors
  * (allocated and freed here) and keeps the fastest. */
 int edgpu_batch_autotune(edgpu_batch b, int32_t precision, int32_t* lanes_per_row_out, double* best_ms_out);
+/* The batched launch's lanes per row (0 = default) and pair_flips as in edgpu_op_get_schedule. */
+int edgpu_batch_get_schedule(edgpu_batch b, int32_t precision, int32_t* lanes_per_row, int32_t* pair_flips);
 /* y_k = H_k x_k for every k, device vectors (arrays of n_ops pointers).  The first call with a set of
  * pointers uploads the sector descriptors (synchronous); if use_graph != 0 that launch is also
  * captured once into a CUDA graph and replayed on the later calls with the same pointers. */
