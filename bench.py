@@ -352,8 +352,15 @@ def run_gpu(args, wl):
     map_info = build_maps([space], args)
     if args.no_pair:
         opr.set_pair_schedule(False)
-    tune_mixed = opr.autotune("mixed")
-    tune_fp64 = opr.autotune("fp64")
+    if args.tiling:
+        # a fixed schedule instead of the autotuner (reproducible profiles)
+        opr.set_pair_schedule(args.pair_targets > 0, max(args.pair_targets, 2))
+        for prec in ("mixed", "fp64"):
+            opr.set_tiling(prec, args.tiling)
+        tune_mixed = tune_fp64 = (args.tiling, None)
+    else:
+        tune_mixed = opr.autotune("mixed")
+        tune_fp64 = opr.autotune("fp64")
     stream = torch.cuda.current_stream()
 
     def pool(prec):
@@ -676,6 +683,10 @@ def main():
     ap.add_argument("--map-bytes", type=int, default=0,
                     help="byte limit of each parent-state map (0: the library default); below the direct map's "
                          "size the map is rank-indexed")
+    ap.add_argument("--tiling", type=int, default=0,
+                    help="fixed schedule instead of the autotuner: -1/-2/-4 lanes per row (single-sector workloads)")
+    ap.add_argument("--pair-targets", type=int, default=2, choices=[0, 2, 4],
+                    help="with --tiling: targets per lane and step of the pair-flip schedule (0: term scan)")
     ap.add_argument("--no-pair", action="store_true", help="test every term per row instead of the pair-flip schedule")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)

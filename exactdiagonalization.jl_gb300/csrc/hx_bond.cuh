@@ -66,6 +66,10 @@ __device__ __forceinline__ W bond_class_mask(W b, const BondTables<W, PREC>& bt,
     return D;
 }
 
+// Programmatic dependent launch (griddepcontrol): no-ops when the launch did not enable it.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ __forceinline__ double fma_r(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float fma_r(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
@@ -176,12 +180,17 @@ template <typename W, int GK, int PREC, int NT>
 __global__ void __launch_bounds__(HX_THREADS) hx_bond_kernel(const HxParams p) {
     typedef typename Cx<PREC>::V V;
     extern __shared__ __align__(16) unsigned char sm[];
+    // programmatic dependent launch: the next kernel in the stream may start its own prologue now;
+    // this kernel copies its (constant) tables, then waits for the previous kernel in the stream to
+    // complete before touching any vector or table it may have written
+    pdl_launch_dependents();
     {
         const int4* src = (const int4*)p.blob;
         int4* dst = (int4*)sm;
         for (int i = threadIdx.x; i < p.blob_words16; i += blockDim.x) dst[i] = src[i];
     }
     __syncthreads();
+    pdl_wait();
     const RowsTables<W, PREC> tb(p, sm);
     const BondTables<W, PREC> bt(p, sm);
     RowsSector<PREC> sc;
@@ -207,15 +216,20 @@ __global__ void __launch_bounds__(HX_THREADS) hx_bond_kernel(const HxParams p) {
 
 // All sectors of a batch in one persistent launch (the tile numbering of hx_multi_kernel).
 template <typename W, int GK, int PREC, int NT>
-__global__ void __launch_bounds__(HX_THREADS) hx_bond_multi_kernel(const HxParams p) {
+__global__ void __launch_bounds__(HX_THREADS, 5) hx_bond_multi_kernel(const HxParams p) {
     typedef typename Cx<PREC>::V V;
     extern __shared__ __align__(16) unsigned char sm[];
+    // programmatic dependent launch: the next kernel in the stream may start its own prologue now;
+    // this kernel copies its (constant) tables, then waits for the previous kernel in the stream to
+    // complete before touching any vector or table it may have written
+    pdl_launch_dependents();
     {
         const int4* src = (const int4*)p.blob;
         int4* dst = (int4*)sm;
         for (int i = threadIdx.x; i < p.blob_words16; i += blockDim.x) dst[i] = src[i];
     }
     __syncthreads();
+    pdl_wait();
     const RowsTables<W, PREC> tb(p, sm);
     const BondTables<W, PREC> bt(p, sm);
     const SectorDesc* sec = (const SectorDesc*)(sm + p.o_sec);
@@ -246,6 +260,23 @@ __global__ void __launch_bounds__(HX_THREADS) hx_bond_multi_kernel(const HxParam
     }
 }
 
+// Launch with programmatic stream serialisation: the kernel may begin while the previous kernel in
+// the stream finishes (it waits for it with griddepcontrol.wait before reading any vector).
+template <typename K>
+void pdl_launch(K kern, const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3(HX_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    EDGPU_CUDA(cudaLaunchKernelEx(&cfg, kern, p));
+}
+
 template <typename W, int GK, int PREC, int NT>
 void hx_bond_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
     auto kern = hx_bond_kernel<W, GK, PREC, NT>;
@@ -254,8 +285,7 @@ void hx_bond_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t
         EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         smem_set = smem;
     }
-    kern<<<blocks, HX_THREADS, smem, st>>>(p);
-    EDGPU_CUDA(cudaGetLastError());
+    pdl_launch(kern, p, blocks, smem, st);
 }
 
 template <typename W, int GK, int PREC, int NT>
@@ -275,8 +305,7 @@ void hx_bond_multi_launch_one(const HxParams& p, int blocks, size_t smem, cudaSt
         EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         smem_set = smem;
     }
-    kern<<<blocks, HX_THREADS, smem, st>>>(p);
-    EDGPU_CUDA(cudaGetLastError());
+    pdl_launch(kern, p, blocks, smem, st);
 }
 
 template <typename W, int GK, int PREC, int NT>
