@@ -115,6 +115,7 @@ struct Blob {
     std::vector<unsigned char> pair_host;   // its host copy (batched images start from it)
     HxParams tmpl_pair{};    // launch template of the pair-flip kernel (offsets into d_pair)
     int max_blocks_bond[2][2] = {{0, 0}, {0, 0}};   // resident blocks of the pair-flip kernel [mapped][4 targets]
+    int max_blocks_table[2] = {0, 0};               // of its target-table flavour [4 targets]
     ~Blob() {
         if (d) cudaFree(d);
         if (d_diag) cudaFree(d_diag);
@@ -149,8 +150,22 @@ struct edgpu_op_s {
     DevBuf<float> x32, y32;
     DevBuf<double> grad_partial, grad_dev;
     std::map<std::vector<const void*>, cudaGraphExec_t> host_graphs;   // replayed host-buffer products
+    // target table of the pair-flip schedule (optional, edgpu_op_build_targets)
+    void* d_tab = nullptr;
+    long long* d_tile_off = nullptr;
+    int tab_wide = 0, tab_cb = 0;
+    int64_t tab_n = 0;
+    int tab_use[2] = {1, 1};          // [precision]: products read the table (chosen by the autotuner)
+    void free_table() {
+        if (d_tab) cudaFree(d_tab);
+        if (d_tile_off) cudaFree(d_tile_off);
+        d_tab = nullptr;
+        d_tile_off = nullptr;
+        tab_n = 0;
+    }
     ~edgpu_op_s() {
         for (auto& kv : host_graphs) cudaGraphExecDestroy(kv.second);
+        free_table();
     }
 };
 
@@ -163,6 +178,7 @@ struct edgpu_batch_s {
     int lpr[2] = {0, 0};                           // lanes per row (0: default 1)
     int pair_use[2] = {1, 1};                      // pair-flip schedule where the terms allow it (autotuned)
     int pair_nt[2] = {2, 2};                       // its targets per lane and step with sector maps
+    int tab_use[2] = {1, 1};                       // read the sectors' target tables (autotuned)
     struct Fused {
         bool ready = false;
         std::vector<uint64_t> gens;                // operator table generations the image was built from
@@ -173,6 +189,7 @@ struct edgpu_batch_s {
         HxParams tmpl{};
         int gk = 0, per_sm = 1, per_sm_map = 0;
         int per_sm_bond[2][2] = {{0, 0}, {0, 0}};   // pair-flip kernel [mapped][4 targets per step]
+        int per_sm_table[2] = {0, 0};               // its target-table flavour [4 targets per step]
         size_t smem = 0;
         int64_t rows = 0;
     } fused[2];
@@ -626,6 +643,7 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     B.smem_bond_canon = std::max<size_t>(bond_prefix_canon, 16);
     B.term_start = term_start;
     B.max_blocks_bond[0][0] = B.max_blocks_bond[0][1] = B.max_blocks_bond[1][0] = B.max_blocks_bond[1][1] = 0;
+    B.max_blocks_table[0] = B.max_blocks_table[1] = 0;
     const int per_sm = std::max(1, hx_max_blocks_per_sm(w32, gk, prec, mode, tot));
     B.max_blocks = per_sm * std::max(1, g_sm_count);
     if (!mode) {
@@ -702,7 +720,8 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
         if (p.bond_ncls > 0 && op->pair_allowed && op->pair_use[prec]) {
             // pair-flip schedule: matching pairs from bond classes (hx_bond.cuh); copies only the
             // blob's prefix up to the bond tables
-            const size_t smem = mapped ? B.smem_bond : B.smem_bond_canon;
+            const bool table = op->d_tab && op->tab_use[prec];
+            const size_t smem = (mapped || table) ? B.smem_bond : B.smem_bond_canon;
             p.blob = B.d_pair;
             p.o_rlut = B.tmpl_pair.o_rlut;
             p.o_bcomp = B.tmpl_pair.o_bcomp;
@@ -710,8 +729,24 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
             p.o_bflip = B.tmpl_pair.o_bflip;
             p.o_bamp = B.tmpl_pair.o_bamp;
             p.blob_words16 = (int)(smem / 16);
-            p.bond_nt = (mapped && op->pair_nt[prec] == 4) ? 4 : 2;
+            p.bond_nt = ((mapped || table) && op->pair_nt[prec] == 4) ? 4 : 2;
             const bool w32 = op->space->w32;
+            if (table) {
+                // the target table: one lane per row, entries streamed in the schedule's order
+                p.lpr = 1;
+                p.rows_per_tile = 32;
+                p.tab = op->d_tab;
+                p.tile_off = op->d_tile_off;
+                p.tab_wide = op->tab_wide;
+                p.tab_cb = op->tab_cb;
+                int& mt = B.max_blocks_table[p.bond_nt == 4 ? 1 : 0];
+                if (mt == 0) mt = std::max(1, hx_table_occupancy(w32, prec, p.bond_nt, smem)) * std::max(1, g_sm_count);
+                const long long warps = (p.n_rows + 31) / 32;
+                const int blocks = (int)std::max<long long>(1, std::min<long long>((warps + HX_THREADS / 32 - 1) / (HX_THREADS / 32), mt));
+                if (blocks_used) *blocks_used = blocks;
+                hx_table_launch(w32, prec, p, blocks, smem, st);
+                return;
+            }
             int& mb = B.max_blocks_bond[mapped ? 1 : 0][p.bond_nt == 4 ? 1 : 0];
             if (mb == 0) {
                 const int per_sm = std::max(1, w32 ? hx_bond_occupancy_w32(gk, prec, p.bond_nt, smem)
@@ -1349,18 +1384,119 @@ int edgpu_op_set_pair_schedule(edgpu_op oh, int32_t enable) {
     API_END
 }
 
-int edgpu_op_get_schedule(edgpu_op oh, int32_t precision, int32_t* rows_per_tile, int32_t* pair_flips) {
+int edgpu_op_get_schedule(edgpu_op oh, int32_t precision, int32_t* rows_per_tile, int32_t* pair_flips,
+                          int32_t* target_table) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
     check_prec(precision);
     if (rows_per_tile) *rows_per_tile = op->tuned_rows[precision];
-    if (pair_flips) {
-        build_blob(op, precision, 0, 0);
-        const int rows = op->tuned_rows[precision];
-        const bool on = op->blob[precision][0][0].tmpl.bond_ncls > 0 && op->pair_allowed && op->pair_use[precision] &&
-                        rows <= 0;
-        *pair_flips = on ? ((op->space->d_map && op->pair_nt[precision] == 4) ? 4 : 2) : 0;
+    build_blob(op, precision, 0, 0);
+    const int rows = op->tuned_rows[precision];
+    const bool on = op->blob[precision][0][0].tmpl.bond_ncls > 0 && op->pair_allowed && op->pair_use[precision] &&
+                    rows <= 0;
+    const bool table = on && op->d_tab && op->tab_use[precision];
+    if (pair_flips) *pair_flips = on ? (((op->space->d_map || table) && op->pair_nt[precision] == 4) ? 4 : 2) : 0;
+    if (target_table) *target_table = table ? 1 : 0;
+    API_END
+}
+
+int edgpu_op_build_targets(edgpu_op oh, int64_t max_bytes, int32_t* built) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    require(max_bytes >= 0, EDGPU_ERR_ARG, "negative byte limit");
+    if (built) *built = 0;
+    op->free_table();
+    const Space& sp = *op->space;
+    // the pair-flip tables of either precision (the bond classes do not depend on it)
+    int prec = EDGPU_MIXED;
+    build_blob(op, prec, 0, 0);
+    if (op->blob[prec][0][0].tmpl.bond_ncls == 0) {
+        prec = EDGPU_FP64;
+        build_blob(op, prec, 0, 0);
     }
+    Blob& B = op->blob[prec][0][0];
+    if (B.tmpl.bond_ncls == 0 || sp.dim == 0) return EDGPU_OK;
+    const bool mapped = sp.d_map != nullptr;
+    HxParams p = B.tmpl;
+    if (mapped) {
+        set_map_params(p, sp);
+        p.map = sp.d_map;
+        p.map_wide = sp.map_wide;
+        p.map_cb = sp.map_cb;
+        p.map_direct = sp.map_direct;
+    }
+    const size_t smem = mapped ? B.smem_bond : B.smem_bond_canon;
+    p.blob = B.d_pair;
+    p.o_rlut = B.tmpl_pair.o_rlut;
+    p.o_bcomp = B.tmpl_pair.o_bcomp;
+    p.o_binfo = B.tmpl_pair.o_binfo;
+    p.o_bflip = B.tmpl_pair.o_bflip;
+    p.o_bamp = B.tmpl_pair.o_bamp;
+    p.blob_words16 = (int)(smem / 16);
+    p.lpr = 1;
+    p.rows_per_tile = 32;
+    // entry format of the parent-state map: c | sx << cb | g << (cb + sb), g only for characters other
+    // than 1; all ones = no representative
+    int cb = 1;
+    while (cb < 63 && ((int64_t)1 << cb) <= sp.dim) ++cb;
+    int gbits = 0;
+    if (sp.group.den > 1)
+        while (gbits < 12 && (1 << gbits) < sp.group.G) ++gbits;
+    require(cb + sp.sb + gbits <= 64, EDGPU_ERR_ARG, "target entries do not fit in 64 bits");
+    const int wide = cb + sp.sb + gbits > 32 ? 1 : 0;
+    const long long n_tiles = (sp.dim + 31) / 32;
+    DevBuf<long long> cnt;
+    cnt.ensure((size_t)n_tiles);
+    long long* d_off = nullptr;
+    EDGPU_CUDA(cudaMalloc(&d_off, (size_t)n_tiles * sizeof(long long)));
+    try {
+        hx_table_count(sp.w32, p, n_tiles, cnt.p, smem, g_stream);
+        const long long total = hx_table_scan(cnt.p, n_tiles, d_off, g_stream);
+        const double bytes = (double)total * (wide ? 8.0 : 4.0) + (double)n_tiles * 8.0;
+        if (bytes > (double)max_bytes) {
+            cudaFree(d_off);
+            return EDGPU_OK;
+        }
+        void* d_tab = nullptr;
+        EDGPU_CUDA(cudaMalloc(&d_tab, std::max<size_t>((size_t)total * (wide ? 8 : 4), 16)));
+        p.tab = d_tab;
+        p.tile_off = d_off;
+        p.tab_wide = wide;
+        p.tab_cb = cb;
+        try {
+            hx_table_fill(sp.w32, mapped ? GK_MAP : B.gk, p, n_tiles, smem, g_stream);
+            EDGPU_CUDA(cudaStreamSynchronize(g_stream));
+        } catch (...) {
+            cudaFree(d_tab);
+            throw;
+        }
+        op->d_tab = d_tab;
+        op->d_tile_off = d_off;
+        op->tab_wide = wide;
+        op->tab_cb = cb;
+        op->tab_n = total;
+        op->tab_use[0] = op->tab_use[1] = 1;
+    } catch (...) {
+        if (!op->d_tile_off) cudaFree(d_off);
+        throw;
+    }
+    if (built) *built = 1;
+    API_END
+}
+
+int edgpu_op_free_targets(edgpu_op oh) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    EDGPU_CUDA(cudaStreamSynchronize(g_stream));
+    op->free_table();
+    API_END
+}
+
+int edgpu_op_targets_info(edgpu_op oh, int64_t* entries, int32_t* entry_bytes) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    if (entries) *entries = op->d_tab ? op->tab_n : 0;
+    if (entry_bytes) *entry_bytes = op->d_tab ? (op->tab_wide ? 8 : 4) : 0;
     API_END
 }
 
@@ -1394,17 +1530,27 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     edgpu_op_s* op = as_op(oh);
     check_prec(precision);
     const int64_t n = op->space->dim;
-    const int cands[] = {-1, -2, -4, 32, 16};   // -k: k lanes per row; else rows per warp tile of the queued schedule
-    // with a parent-state map only the row-per-lane schedules apply
-    const int n_cands = op->space->d_map ? 3 : 5;
-    int best = op->space->d_map ? -1 : 32;
-    double best_ms = 1e30;
-    // the row-per-lane schedules are timed with and without the pair-flip schedule when it applies
-    // (unless the caller switched it off): random-access order differs between the two
+    // Candidates: the term scan with 1, 2 or 4 lanes per row (and the queued schedule with 32 or 16
+    // rows per warp tile when there is no parent-state map); where the pair-flip schedule applies
+    // (and the caller allows it), that schedule with 2 or 4 targets per step (4 with a map or a
+    // target table) and 1, 2 or 4 lanes per row, and its target-table flavour (one lane per row).
+    struct Cand { int pair, nt, table, rows; };
+    std::vector<Cand> cands;
     build_blob(op, precision, 0, 0);
     const bool pair_ok = op->blob[precision][0][0].tmpl.bond_ncls > 0 && op->pair_allowed;
-    int best_pair = pair_ok ? 1 : 0, best_nt = 2;
     const bool mapped = op->space->d_map != nullptr;
+    if (pair_ok) {
+        if (op->d_tab)
+            for (int nt : {4, 2}) cands.push_back({1, nt, 1, -1});
+        for (int nt : (mapped ? std::vector<int>{4, 2} : std::vector<int>{2}))
+            for (int r : {-1, -2, -4}) cands.push_back({1, nt, 0, r});
+    }
+    for (int r : {-1, -2, -4}) cands.push_back({0, 2, 0, r});
+    if (!mapped)
+        for (int r : {32, 16}) cands.push_back({0, 2, 0, r});
+    Cand best = cands.front();
+    double best_ms = 1e30;
+    const int keep_pair = op->pair_use[precision], keep_nt = op->pair_nt[precision], keep_tab = op->tab_use[precision];
     if (n > 0) {
         const size_t vs = precision == EDGPU_FP64 ? 16 : 8;
         void *x = nullptr, *y = nullptr;
@@ -1415,35 +1561,31 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
         cudaEventCreate(&e1);
         try {
             EDGPU_CUDA(cudaMemsetAsync(x, 0, n * vs, g_stream));
-            for (int cand = pair_ok ? (mapped ? 2 : 1) : 0; cand >= 0; --cand)
-                for (int ci = 0; ci < n_cands; ++ci) {
-                    // cand 2: pair flips with 4 targets per step, 1: with 2, 0: the term scan
-                    const int pair = cand > 0 ? 1 : 0, nt = cand == 2 ? 4 : 2;
-                    const int r = cands[ci];
-                    if (pair && r > 0) continue;   // the pair-flip schedule is row-per-lane
-                    op->pair_use[precision] = pair;
-                    op->pair_nt[precision] = nt;
-                    launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, g_stream, nullptr, r);
-                    float tot = 0.f;
-                    const int reps = 3;
-                    for (int k = 0; k < reps; ++k) {
-                        EDGPU_CUDA(cudaEventRecord(e0, g_stream));
-                        launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, g_stream, nullptr, r);
-                        EDGPU_CUDA(cudaEventRecord(e1, g_stream));
-                        EDGPU_CUDA(cudaEventSynchronize(e1));
-                        float ms = 0.f;
-                        cudaEventElapsedTime(&ms, e0, e1);
-                        tot += ms;
-                    }
-                    if (tot / reps < best_ms) {
-                        best_ms = tot / reps;
-                        best = r;
-                        best_pair = pair;
-                        best_nt = nt;
-                    }
+            for (const Cand& c : cands) {
+                op->pair_use[precision] = c.pair;
+                op->pair_nt[precision] = c.nt;
+                op->tab_use[precision] = c.table;
+                launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, g_stream, nullptr, c.rows);
+                float tot = 0.f;
+                const int reps = 3;
+                for (int k = 0; k < reps; ++k) {
+                    EDGPU_CUDA(cudaEventRecord(e0, g_stream));
+                    launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, g_stream, nullptr, c.rows);
+                    EDGPU_CUDA(cudaEventRecord(e1, g_stream));
+                    EDGPU_CUDA(cudaEventSynchronize(e1));
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    tot += ms;
                 }
+                if (tot / reps < best_ms) {
+                    best_ms = tot / reps;
+                    best = c;
+                }
+            }
         } catch (...) {
-            if (pair_ok) op->pair_use[precision] = 1;
+            op->pair_use[precision] = keep_pair;
+            op->pair_nt[precision] = keep_nt;
+            op->tab_use[precision] = keep_tab;
             cudaFree(x);
             cudaFree(y);
             cudaEventDestroy(e0);
@@ -1455,12 +1597,11 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
     }
-    if (pair_ok) {
-        op->pair_use[precision] = best_pair;
-        op->pair_nt[precision] = best_nt;
-    }
-    op->tuned_rows[precision] = best;
-    if (rows_per_tile_out) *rows_per_tile_out = best;
+    op->pair_use[precision] = best.pair;
+    op->pair_nt[precision] = best.nt;
+    op->tab_use[precision] = best.table ? 1 : (op->d_tab ? 0 : 1);
+    op->tuned_rows[precision] = best.rows;
+    if (rows_per_tile_out) *rows_per_tile_out = best.rows;
     if (best_ms_out) *best_ms_out = best_ms;
     API_END
 }
@@ -1951,17 +2092,24 @@ void batch_prepare(edgpu_batch_s* b, int prec) {
 HxParams batch_params(edgpu_batch_s* b, int prec, const void* const* xs, void* const* ys, int* blocks_out) {
     edgpu_batch_s::Fused& F = b->fused[prec];
     const int n = (int)b->ops.size();
-    const int lpr = b->lpr[prec] ? b->lpr[prec] : 1;
+    // sector maps are used when every sector has one (one colex rank table for all); target tables
+    // when every sector's operator has one (pair-flip schedule, one lane per row)
+    bool mapped = true, tabled = true;
+    for (int i = 0; i < n; ++i) {
+        mapped = mapped && (b->ops[i]->space->d_map != nullptr || b->ops[i]->space->dim == 0);
+        tabled = tabled && (b->ops[i]->d_tab != nullptr || b->ops[i]->space->dim == 0);
+    }
+    const bool pair = F.tmpl.bond_ncls > 0 && b->ops[0]->pair_allowed && b->pair_use[prec];
+    tabled = tabled && pair && b->tab_use[prec];
+    const int lpr = tabled ? 1 : (b->lpr[prec] ? b->lpr[prec] : 1);
     const int rpw = 32 / lpr;
-    // sector maps are used when every sector has one (one colex rank table for all)
-    bool mapped = true;
-    for (int i = 0; i < n; ++i) mapped = mapped && (b->ops[i]->space->d_map != nullptr || b->ops[i]->space->dim == 0);
     std::vector<const void*> key;
     key.push_back((const void*)(intptr_t)lpr);
     for (int i = 0; i < n; ++i) {
         key.push_back(xs[i]);
         key.push_back(ys[i]);
         key.push_back(mapped ? b->ops[i]->space->d_map : nullptr);
+        key.push_back(tabled ? b->ops[i]->d_tab : nullptr);
     }
     std::vector<SectorDesc> d(n);
     long long tiles = 0;
@@ -1985,6 +2133,12 @@ HxParams batch_params(edgpu_batch_s* b, int prec, const void* const* xs, void* c
         d[i].o_ph = F.o_ph[i];
         d[i].o_num = F.o_num[i];
         d[i].want_arg = F.want_arg[i];
+        if (tabled) {
+            d[i].tab = o->d_tab;
+            d[i].tile_off = o->d_tile_off;
+            d[i].tab_wide = o->tab_wide;
+            d[i].tab_cb = o->tab_cb;
+        }
     }
     auto it = b->images[prec].find(key);
     if (it == b->images[prec].end()) {
@@ -2013,10 +2167,20 @@ HxParams batch_params(edgpu_batch_s* b, int prec, const void* const* xs, void* c
     p.rows_per_tile = rpw;
     p.n_tiles = tiles;
     const bool w32 = b->ops[0]->space->w32;
-    const bool pair = p.bond_ncls > 0 && b->ops[0]->pair_allowed && b->pair_use[prec];
     int per_sm = mapped ? F.per_sm_map : F.per_sm;
-    p.bond_nt = (mapped && b->pair_nt[prec] == 4) ? 4 : 2;
-    if (pair) {
+    p.bond_nt = ((mapped || tabled) && b->pair_nt[prec] == 4) ? 4 : 2;
+    p.tab = nullptr;
+    if (tabled) {
+        for (int i = 0; i < n; ++i)
+            if (b->ops[i]->d_tab) {
+                p.tab = b->ops[i]->d_tab;   // marks the target-table launch; the kernel reads each sector's
+                break;
+            }
+        p.blob_words16 = (int)(F.smem_pair / 16);
+        int& ps = F.per_sm_table[p.bond_nt == 4 ? 1 : 0];
+        if (ps == 0) ps = std::max(1, hx_table_multi_occupancy(w32, prec, p.bond_nt, F.smem_pair));
+        per_sm = ps;
+    } else if (pair) {
         p.blob_words16 = (int)(F.smem_pair / 16);
         int& ps = F.per_sm_bond[mapped ? 1 : 0][p.bond_nt == 4 ? 1 : 0];
         if (ps == 0) {
@@ -2038,6 +2202,10 @@ void batch_launch(edgpu_batch_s* b, int prec, const HxParams& p, int blocks, cud
     if (p.n_tiles == 0) return;
     const int gk = p.rank_tab ? GK_MAP : b->fused[prec].gk;   // sector maps present: the map flavour
     const bool w32 = b->ops[0]->space->w32;
+    if (p.tab) {
+        hx_table_multi_launch(w32, prec, p, blocks, b->fused[prec].smem_pair, st);
+        return;
+    }
     if (p.bond_ncls > 0 && b->ops[0]->pair_allowed && b->pair_use[prec]) {
         if (w32) hx_bond_multi_launch_w32(gk, prec, p, blocks, b->fused[prec].smem_pair, st);
         else hx_bond_multi_launch_w64(gk, prec, p, blocks, b->fused[prec].smem_pair, st);
@@ -2079,7 +2247,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
     const size_t vs = precision == EDGPU_FP64 ? 16 : 8;
     int64_t tot = 0;
     for (auto* o : b->ops) tot += o->space->dim;
-    int best = 1, best_pair = 1, best_nt = 2;
+    int best = 1, best_pair = 1, best_nt = 2, best_tab = 1;
     double best_ms = 1e30;
     if (tot > 0) {
         void *x = nullptr, *y = nullptr;
@@ -2107,11 +2275,16 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
             const bool pair_ok = b->fused[precision].tmpl.bond_ncls > 0 && b->ops[0]->pair_allowed;
             bool mapped = true;
             for (auto* o : b->ops) mapped = mapped && (o->space->d_map != nullptr || o->space->dim == 0);
-            for (int cand = pair_ok ? (mapped ? 2 : 1) : 0; cand >= 0; --cand)
+            bool tabled = pair_ok;
+            for (auto* o : b->ops) tabled = tabled && (o->d_tab != nullptr || o->space->dim == 0);
+            // cand 4/3: target tables with 4/2 targets per step; 2/1: pair flips with 4/2; 0: term scan
+            for (int cand = tabled ? 4 : (pair_ok ? (mapped ? 2 : 1) : 0); cand >= 0; --cand)
                 for (int l : {1, 2, 4}) {
+                    if (cand >= 3 && l != 1) continue;   // target tables: one lane per row
                     b->lpr[precision] = l;
                     b->pair_use[precision] = cand > 0 ? 1 : 0;
-                    b->pair_nt[precision] = cand == 2 ? 4 : 2;
+                    b->pair_nt[precision] = (cand == 2 || cand == 4) ? 4 : 2;
+                    b->tab_use[precision] = cand >= 3 ? 1 : 0;
                     int blocks = 0;
                     const HxParams p = batch_params(b, precision, xs.data(), ys.data(), &blocks);
                     batch_launch(b, precision, p, blocks, g_stream);
@@ -2130,13 +2303,15 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
                         best_ms = sum / reps;
                         best = l;
                         best_pair = cand > 0 ? 1 : 0;
-                        best_nt = cand == 2 ? 4 : 2;
+                        best_nt = (cand == 2 || cand == 4) ? 4 : 2;
+                        best_tab = cand >= 3 ? 1 : 0;
                     }
                 }
         } catch (...) {
             b->lpr[precision] = keep;
             b->pair_use[precision] = 1;
             b->pair_nt[precision] = 2;
+            b->tab_use[precision] = 1;
             cudaStreamSynchronize(g_stream);
             cudaFree(x);
             cudaFree(y);
@@ -2158,12 +2333,14 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
     b->lpr[precision] = best;
     b->pair_use[precision] = best_pair;
     b->pair_nt[precision] = best_nt;
+    b->tab_use[precision] = best_tab;
     if (lanes_per_row_out) *lanes_per_row_out = best;
     if (best_ms_out) *best_ms_out = best_ms;
     API_END
 }
 
-int edgpu_batch_get_schedule(edgpu_batch bh, int32_t precision, int32_t* lanes_per_row, int32_t* pair_flips) {
+int edgpu_batch_get_schedule(edgpu_batch bh, int32_t precision, int32_t* lanes_per_row, int32_t* pair_flips,
+                             int32_t* target_table) {
     API_BEGIN
     require(bh, EDGPU_ERR_ARG, "null batch");
     check_prec(precision);
@@ -2172,8 +2349,18 @@ int edgpu_batch_get_schedule(edgpu_batch bh, int32_t precision, int32_t* lanes_p
         batch_prepare(bh, precision);
         bool mapped = true;
         for (auto* o : bh->ops) mapped = mapped && (o->space->d_map != nullptr || o->space->dim == 0);
+        bool tabled = true;
+        for (auto* o : bh->ops) tabled = tabled && (o->d_tab != nullptr || o->space->dim == 0);
         const bool on = bh->fused[precision].tmpl.bond_ncls > 0 && bh->ops[0]->pair_allowed && bh->pair_use[precision];
-        *pair_flips = on ? ((mapped && bh->pair_nt[precision] == 4) ? 4 : 2) : 0;
+        tabled = tabled && on && bh->tab_use[precision];
+        *pair_flips = on ? (((mapped || tabled) && bh->pair_nt[precision] == 4) ? 4 : 2) : 0;
+        if (target_table) *target_table = tabled ? 1 : 0;
+    } else if (target_table) {
+        bool tabled = true;
+        for (auto* o : bh->ops) tabled = tabled && (o->d_tab != nullptr || o->space->dim == 0);
+        batch_prepare(bh, precision);
+        *target_table = (tabled && bh->fused[precision].tmpl.bond_ncls > 0 && bh->ops[0]->pair_allowed &&
+                         bh->pair_use[precision] && bh->tab_use[precision]) ? 1 : 0;
     }
     API_END
 }
@@ -2195,7 +2382,8 @@ int edgpu_batch_mul_device(edgpu_batch bh, int32_t precision, const void* const*
     }
     std::vector<const void*> key;
     key.push_back((const void*)(intptr_t)p.lpr);
-    key.push_back((const void*)(intptr_t)(b->pair_use[precision] * 8 + b->pair_nt[precision]));   // the kernel
+    key.push_back((const void*)(intptr_t)(b->pair_use[precision] * 8 + b->pair_nt[precision] +
+                                          (p.tab ? 16 : 0)));   // the kernel
     key.push_back(p.blob);   // the image (vectors, sector maps) the launch reads
     for (int i = 0; i < n; ++i) {
         key.push_back(xs[i]);

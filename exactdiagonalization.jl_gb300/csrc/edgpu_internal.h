@@ -29,6 +29,9 @@ struct Error : std::runtime_error {
 enum GroupKind { GK_TRIVIAL = 0, GK_TORUS = 1, GK_GENERIC = 2, GK_RING = 3 };
 // Product-kernel flavour for targets looked up in a parent-state map (no canonicalisation code).
 constexpr int GK_MAP = 4;
+// Pair-flip product flavour that reads every target's map-format entry from the operator's target
+// table (row after row, in the schedule's order) instead of looking it up.
+constexpr int GK_TABLE = 5;
 
 // Symmetry group acting on basis words: element g maps word q to g.q.
 //  TRIVIAL  the identity only (unreduced representation).
@@ -208,6 +211,10 @@ struct HxParams {
     int o_bcomp, o_binfo, o_bflip, o_bamp;    // shared-memory offsets of the class tables
     int bond_real;                            // every pair amplitude is real
     int bond_nt;                              // targets per lane and step: 2, or 4 (parent-state map only)
+    // target table of the pair-flip schedule (GK_TABLE launches and the table's build pass)
+    const void* tab;
+    const long long* tile_off;
+    int tab_wide, tab_cb;
 };
 
 // One sector of a batched launch (hx_multi_kernel), kept in shared memory after the common tables.
@@ -224,6 +231,9 @@ struct __align__(16) SectorDesc {
     const void* map;                          // the sector's parent-state map (or null)
     int map_wide, map_cb, map_direct;
     int o_ph, o_num, want_arg;
+    const void* tab;                          // the sector's target table (pair-flip schedule, or null)
+    const long long* tile_off;
+    int tab_wide, tab_cb;
 };
 
 constexpr int BOND_MAXC = 4;       // rotation components per bond class of the pair-flip schedule
@@ -274,6 +284,19 @@ void hx_bond_multi_launch_w32(int gk, int prec, const HxParams& p, int blocks, s
 void hx_bond_multi_launch_w64(int gk, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
 int hx_bond_multi_occupancy_w32(int gk, int prec, int nt, size_t smem);
 int hx_bond_multi_occupancy_w64(int gk, int prec, int nt, size_t smem);
+
+// Target table of the pair-flip schedule (hxtable.cu): count the targets of every warp tile of 32 rows,
+// scan the counts into tile offsets (returns the total), and write every target's map-format entry,
+// looked up with flavour gk (GK_MAP or a canonicalising kind).  p: the pair-flip launch template with
+// lpr = 1; p.tab / p.tile_off / p.tab_wide / p.tab_cb set for the fill.
+void hx_table_count(bool w32, const HxParams& p, long long n_tiles, long long* tile_cnt, size_t smem, cudaStream_t st);
+long long hx_table_scan(const long long* tile_cnt, long long n_tiles, long long* tile_off, cudaStream_t st);
+void hx_table_fill(bool w32, int gk, const HxParams& p, long long n_tiles, size_t smem, cudaStream_t st);
+// The product through the table (GK_TABLE), one sector and all sectors of a batch.
+void hx_table_launch(bool w32, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
+int hx_table_occupancy(bool w32, int prec, int nt, size_t smem);
+void hx_table_multi_launch(bool w32, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
+int hx_table_multi_occupancy(bool w32, int prec, int nt, size_t smem);
 
 // ---- the coupling-gradient launch for callers that cannot allocate (noalloc.cu) -----------------
 // Launch state of an operator's gradient-mode tables, read without building anything.

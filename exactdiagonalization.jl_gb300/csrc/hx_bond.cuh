@@ -79,10 +79,43 @@ __device__ __forceinline__ int lowest_bit(W m) {
     else return __ffs((int)m) - 1;
 }
 
+// Entry of the target table at pos (map format: c | sx << cb | g << (cb + sb); all ones when the
+// target's orbit has no representative in the table).
+template <int PREC>
+__device__ __forceinline__ void table_entry(const RowsSector<PREC>& sc, long long pos, bool on, int sb, long long& c,
+                                            int& sx, int& g) {
+    if (!sc.tab_wide) {
+        const unsigned e = on ? __ldg((const unsigned*)sc.tab + pos) : 0xffffffffu;
+        const unsigned cmask = (sc.tab_cb >= 32) ? 0xffffffffu : ((1u << sc.tab_cb) - 1u);
+        const unsigned ci = e & cmask;
+        c = (ci == cmask) ? -1 : (long long)ci;
+        sx = (int)((e >> sc.tab_cb) & ((1u << sb) - 1u));
+        g = (int)((e >> (sc.tab_cb + sb)) & 0xfffu);
+    } else {
+        const unsigned long long e = on ? __ldg((const unsigned long long*)sc.tab + pos) : ~0ull;
+        const unsigned long long cmask = (1ull << sc.tab_cb) - 1ull;
+        const unsigned long long ci = e & cmask;
+        c = (ci == cmask) ? -1 : (long long)ci;
+        sx = (int)((e >> sc.tab_cb) & ((1ull << sb) - 1ull));
+        g = (int)((e >> (sc.tab_cb + sb)) & 0xfffull);
+    }
+}
+
+// Matching pairs of every class of the row state b (lpr == 1): the row's number of targets.
+template <typename W, int PREC>
+__device__ __forceinline__ int bond_row_count(W b, const BondTables<W, PREC>& bt, int ncls, int n, W full) {
+    int cnt = 0;
+    for (int c = 0; c < ncls; ++c) cnt += __popcll((unsigned long long)bond_class_mask<W, PREC>(b, bt, c, n, full));
+    return cnt;
+}
+
 // One warp tile of rows (32 / lpr consecutive rows of the sector, lpr lanes each) of the pair-flip
 // schedule; lane sub of a row takes the pairs whose start bit i has i % lpr == sub.  NT targets per
 // lane and step (2 or 4): their lookups, then their gathers, are issued together.
-template <typename W, int GK, int PREC, int NT>
+//   GK_TABLE  the targets' entries are read from the sector's target table (lpr == 1) in this order;
+//   FILL      the build pass of that table: the entries are looked up with the flavour GK and written
+//             to the table (sc.tab) instead of being gathered and accumulated.
+template <typename W, int GK, int PREC, int NT, bool FILL = false>
 __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W, PREC>& tb,
                                           const BondTables<W, PREC>& bt, const RowsSector<PREC>& sc, long long tile,
                                           int lane) {
@@ -98,9 +131,11 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
     const W kr = act ? keys[row] : (W)0;
     const W b = kr >> sb;
     const int ri = (int)(kr & smask);
-    const V xr = act ? x[row] : czero<V>();
     V acc = czero<V>();
-    if (act && sub == 0) acc = cmul(sc.diag[row], xr);
+    if (!FILL) {
+        const V xr = act ? x[row] : czero<V>();
+        if (act && sub == 0) acc = cmul(sc.diag[row], xr);
+    }
     const int n = p.nbits;
     const W full = (W)p.full;
     // start bits of this lane: i % lpr == sub
@@ -109,6 +144,19 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
     const int ncls = act ? p.bond_ncls : 0;
     const R* __restrict__ rrow = tb.ratio + ri * p.nd;
     const bool real_fast = p.bond_real && !sc.want_arg;
+    // target table position of this lane's first target: the tile's offset plus the targets of the
+    // rows before it in the tile
+    long long tpos = 0;
+    if (GK == GK_TABLE || FILL) {
+        const int cnt = bond_row_count<W, PREC>(b, bt, ncls, n, full);
+        int incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += u;
+        }
+        tpos = sc.tile_off[tile] + (incl - cnt);
+    }
     int cls = -1;
     bool cpar = false;   // the current class has terms on parallel bits
     W m = 0;
@@ -138,8 +186,33 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
             if (cpar) v |= (__popcll((unsigned long long)(b & f)) != 1) << 1;
             ti[h] = (ti[h] << 2) | v;
         }
+        if constexpr (GK == GK_TABLE) {
 #pragma unroll
-        for (int h = 0; h < NT; h += 2) resolve_targets2<W, GK, PREC>(p, tb, sc, q + h, on + h, c + h, sx + h, g + h);
+            for (int h = 0; h < NT; ++h) {
+                table_entry<PREC>(sc, tpos, on[h], sb, c[h], sx[h], g[h]);
+                tpos += on[h] ? 1 : 0;
+            }
+        } else {
+#pragma unroll
+            for (int h = 0; h < NT; h += 2)
+                resolve_targets2<W, GK, PREC>(p, tb, sc, q + h, on + h, c + h, sx + h, g + h);
+        }
+        if constexpr (FILL) {
+            const bool with_g = sc.want_arg;
+#pragma unroll
+            for (int h = 0; h < NT; ++h) {
+                if (!on[h]) continue;
+                unsigned long long e = ~0ull;
+                if (c[h] >= 0) {
+                    e = (unsigned long long)c[h] | ((unsigned long long)sx[h] << sc.tab_cb);
+                    if (with_g) e |= (unsigned long long)g[h] << (sc.tab_cb + sb);
+                }
+                if (sc.tab_wide) ((unsigned long long*)sc.tab)[tpos] = e;
+                else ((unsigned*)sc.tab)[tpos] = (unsigned)e;
+                ++tpos;
+            }
+            continue;
+        }
         V xv[NT];
 #pragma unroll
         for (int h = 0; h < NT; ++h) xv[h] = (c[h] >= 0) ? x[c[h]] : czero<V>();
@@ -168,6 +241,7 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
             }
         }
     }
+    if (FILL) return;
     // partial sums of the row's lanes (fixed butterfly order)
     for (int d = 1; d < lpr; d <<= 1) acc = cadd(acc, shfl_xor_v(acc, d));
     if (act && sub == 0) {
@@ -207,6 +281,10 @@ __global__ void __launch_bounds__(HX_THREADS) hx_bond_kernel(const HxParams p) {
     sc.map_wide = p.map_wide;
     sc.map_cb = p.map_cb;
     sc.map_direct = p.map_direct;
+    sc.tab = p.tab;
+    sc.tile_off = p.tile_off;
+    sc.tab_wide = p.tab_wide;
+    sc.tab_cb = p.tab_cb;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
     const int rpw = 32 / p.lpr;
     const long long n_tiles = (p.n_rows + rpw - 1) / rpw;
@@ -256,6 +334,10 @@ __global__ void __launch_bounds__(HX_THREADS, 5) hx_bond_multi_kernel(const HxPa
         sc.map_wide = d.map_wide;
         sc.map_cb = d.map_cb;
         sc.map_direct = d.map_direct;
+        sc.tab = d.tab;
+        sc.tile_off = d.tile_off;
+        sc.tab_wide = d.tab_wide;
+        sc.tab_cb = d.tab_cb;
         bond_tile<W, GK, PREC, NT>(p, tb, bt, sc, tile - tile0, lane);
     }
 }

@@ -62,6 +62,11 @@ struct RowsSector {
     bool want_arg;
     const void* map;   // parent-state map (null: canonicalise and search)
     int map_wide, map_cb, map_direct;
+    // target table of the pair-flip schedule (GK_TABLE): the map-format entry of every (row, target),
+    // rows in warp tiles of 32, each tile's entries from tile_off[tile], row after row
+    const void* tab;
+    const long long* tile_off;
+    int tab_wide, tab_cb;
 };
 
 // Colex rank of a state with rank_k set bits among the parent's bits: sum over 6-bit chunks of the

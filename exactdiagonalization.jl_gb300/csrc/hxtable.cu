@@ -1,0 +1,201 @@
+// Target table of the pair-flip schedule: the map-format entry of every (row, target) of the product,
+// stored once per operator in the order the product walks them (warp tiles of 32 rows, row after row,
+// each row's targets by bond class and start bit).  The product then streams the table instead of
+// looking every target up (a parent-state map read or canonicalisation plus search per target), and
+// gathers x: the entries are the same, so the results are bit-identical to the looked-up product.
+//
+// This is the compact, index-only form of the reference's precomputed parent-sized
+// basis_mapping_index (symmetry_reduce_generic.jl:33-35), taken one step further: indexed by (row,
+// target) rather than by parent state, as read by the row iterator (reduced_operator_representation.jl
+// :57-85).
+#include "hx_bond.cuh"
+
+namespace edgpu {
+
+namespace {
+
+// Targets of every warp tile of 32 rows (the pair-flip schedule with one lane per row).
+template <typename W, int PREC>
+__global__ void __launch_bounds__(HX_THREADS) hx_table_count_kernel(const HxParams p, long long n_tiles,
+                                                                  long long* tile_cnt) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    {
+        const int4* src = (const int4*)p.blob;
+        int4* dst = (int4*)sm;
+        for (int i = threadIdx.x; i < p.blob_words16; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const BondTables<W, PREC> bt(p, sm);
+    const W* __restrict__ keys = (const W*)p.keys;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    const W smask = (W)((((W)1) << p.sb) - 1);
+    for (long long tile = (long long)blockIdx.x * wpb + warp; tile < n_tiles; tile += (long long)gridDim.x * wpb) {
+        const long long row = tile * 32 + lane;
+        const bool act = row < p.n_rows;
+        const W b = act ? (W)(keys[row] >> p.sb) : (W)0;
+        (void)smask;
+        int cnt = bond_row_count<W, PREC>(b, bt, act ? p.bond_ncls : 0, p.nbits, (W)p.full);
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, d);
+        if (lane == 0) tile_cnt[tile] = cnt;
+    }
+}
+
+// Exclusive scan of n counts in one block (each thread a contiguous run); *total = their sum.
+__global__ void k_table_scan(const long long* cnt, long long n, long long* off, long long* total) {
+    __shared__ long long tmp[32];
+    const long long per = (n + blockDim.x - 1) / blockDim.x;
+    const long long beg = min(n, (long long)threadIdx.x * per), end = min(n, beg + per);
+    long long s = 0;
+    for (long long i = beg; i < end; ++i) s += cnt[i];
+    long long tot = 0;
+    long long ex = block_exclusive_scan(s, tmp, &tot);
+    for (long long i = beg; i < end; ++i) {
+        off[i] = ex;
+        ex += cnt[i];
+    }
+    if (threadIdx.x == 0) *total = tot;
+}
+
+// The build pass: every target of every row looked up with flavour GK and written to the table.
+template <typename W, int GK, int PREC>
+__global__ void __launch_bounds__(HX_THREADS) hx_table_fill_kernel(const HxParams p, long long n_tiles) {
+    typedef typename Cx<PREC>::V V;
+    extern __shared__ __align__(16) unsigned char sm[];
+    {
+        const int4* src = (const int4*)p.blob;
+        int4* dst = (int4*)sm;
+        for (int i = threadIdx.x; i < p.blob_words16; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const RowsTables<W, PREC> tb(p, sm);
+    const BondTables<W, PREC> bt(p, sm);
+    RowsSector<PREC> sc{};
+    sc.keys = p.keys;
+    sc.n_rows = p.n_rows;
+    sc.ds = p.ds;
+    sc.ph = (const V*)(sm + p.o_ph);
+    sc.num = (const int*)(sm + p.o_num);
+    sc.want_arg = p.want_arg != 0;
+    sc.map = p.map;
+    sc.map_wide = p.map_wide;
+    sc.map_cb = p.map_cb;
+    sc.map_direct = p.map_direct;
+    sc.tab = p.tab;
+    sc.tile_off = p.tile_off;
+    sc.tab_wide = p.tab_wide;
+    sc.tab_cb = p.tab_cb;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    for (long long tile = (long long)blockIdx.x * wpb + warp; tile < n_tiles; tile += (long long)gridDim.x * wpb)
+        bond_tile<W, GK, PREC, 2, true>(p, tb, bt, sc, tile, lane);
+}
+
+template <typename K>
+void set_smem(K kern, size_t smem) {
+    EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+}
+
+int grid_for(long long n_tiles) {
+    return (int)std::max<long long>(1, std::min<long long>((n_tiles + HX_THREADS / 32 - 1) / (HX_THREADS / 32),
+                                                           (long long)sm_count() * 8));
+}
+
+template <typename W>
+void fill_one(int gk, const HxParams& p, long long n_tiles, size_t smem, cudaStream_t st) {
+    const int blocks = grid_for(n_tiles);
+    switch (gk) {
+        case GK_TRIVIAL: set_smem(hx_table_fill_kernel<W, GK_TRIVIAL, 1>, smem);
+            hx_table_fill_kernel<W, GK_TRIVIAL, 1><<<blocks, HX_THREADS, smem, st>>>(p, n_tiles); break;
+        case GK_TORUS: set_smem(hx_table_fill_kernel<W, GK_TORUS, 1>, smem);
+            hx_table_fill_kernel<W, GK_TORUS, 1><<<blocks, HX_THREADS, smem, st>>>(p, n_tiles); break;
+        case GK_GENERIC: set_smem(hx_table_fill_kernel<W, GK_GENERIC, 1>, smem);
+            hx_table_fill_kernel<W, GK_GENERIC, 1><<<blocks, HX_THREADS, smem, st>>>(p, n_tiles); break;
+        case GK_RING:
+            if constexpr (sizeof(W) == 4) {
+                set_smem(hx_table_fill_kernel<W, GK_RING, 1>, smem);
+                hx_table_fill_kernel<W, GK_RING, 1><<<blocks, HX_THREADS, smem, st>>>(p, n_tiles);
+                break;
+            }
+            throw Error(EDGPU_ERR_ARG, "ring lookups need 32-bit tables");
+        case GK_MAP: set_smem(hx_table_fill_kernel<W, GK_MAP, 1>, smem);
+            hx_table_fill_kernel<W, GK_MAP, 1><<<blocks, HX_THREADS, smem, st>>>(p, n_tiles); break;
+        default: throw Error(EDGPU_ERR_ARG, "bad target-table lookup flavour");
+    }
+    EDGPU_CUDA(cudaGetLastError());
+}
+
+template <typename W>
+void launch_t(int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st, bool multi) {
+    const int nt = p.bond_nt == 4 ? 4 : 2;
+#define EDGPU_TABLE_CASE(PR, NTV)                                                                          \
+    if (prec == PR && nt == NTV) {                                                                         \
+        if (multi) return hx_bond_multi_launch_one<W, GK_TABLE, PR, NTV>(p, blocks, smem, st);             \
+        return hx_bond_launch_one<W, GK_TABLE, PR, NTV>(p, blocks, smem, st);                              \
+    }
+    EDGPU_TABLE_CASE(0, 2)
+    EDGPU_TABLE_CASE(0, 4)
+    EDGPU_TABLE_CASE(1, 2)
+    EDGPU_TABLE_CASE(1, 4)
+#undef EDGPU_TABLE_CASE
+    throw Error(EDGPU_ERR_ARG, "bad target-table kernel selector");
+}
+
+template <typename W>
+int occupancy_t(int prec, int nt, size_t smem, bool multi) {
+    if (prec == 0 && nt != 4) return multi ? hx_bond_multi_occupancy_one<W, GK_TABLE, 0, 2>(smem) : hx_bond_occupancy_one<W, GK_TABLE, 0, 2>(smem);
+    if (prec == 0) return multi ? hx_bond_multi_occupancy_one<W, GK_TABLE, 0, 4>(smem) : hx_bond_occupancy_one<W, GK_TABLE, 0, 4>(smem);
+    if (nt != 4) return multi ? hx_bond_multi_occupancy_one<W, GK_TABLE, 1, 2>(smem) : hx_bond_occupancy_one<W, GK_TABLE, 1, 2>(smem);
+    return multi ? hx_bond_multi_occupancy_one<W, GK_TABLE, 1, 4>(smem) : hx_bond_occupancy_one<W, GK_TABLE, 1, 4>(smem);
+}
+
+}  // namespace
+
+void hx_table_count(bool w32, const HxParams& p, long long n_tiles, long long* tile_cnt, size_t smem, cudaStream_t st) {
+    const int blocks = grid_for(n_tiles);
+    if (w32) {
+        set_smem(hx_table_count_kernel<unsigned, 1>, smem);
+        hx_table_count_kernel<unsigned, 1><<<blocks, HX_THREADS, smem, st>>>(p, n_tiles, tile_cnt);
+    } else {
+        set_smem(hx_table_count_kernel<unsigned long long, 1>, smem);
+        hx_table_count_kernel<unsigned long long, 1><<<blocks, HX_THREADS, smem, st>>>(p, n_tiles, tile_cnt);
+    }
+    EDGPU_CUDA(cudaGetLastError());
+}
+
+long long hx_table_scan(const long long* tile_cnt, long long n_tiles, long long* tile_off, cudaStream_t st) {
+    long long* d_total = nullptr;
+    EDGPU_CUDA(cudaMalloc(&d_total, sizeof(long long)));
+    k_table_scan<<<1, 1024, 0, st>>>(tile_cnt, n_tiles, tile_off, d_total);
+    cudaError_t e = cudaGetLastError();
+    long long total = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&total, d_total, sizeof(long long), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_total);
+    if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("target table scan: ") + cudaGetErrorString(e));
+    return total;
+}
+
+void hx_table_fill(bool w32, int gk, const HxParams& p, long long n_tiles, size_t smem, cudaStream_t st) {
+    if (w32) fill_one<unsigned>(gk, p, n_tiles, smem, st);
+    else fill_one<unsigned long long>(gk, p, n_tiles, smem, st);
+}
+
+void hx_table_launch(bool w32, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
+    if (w32) launch_t<unsigned>(prec, p, blocks, smem, st, false);
+    else launch_t<unsigned long long>(prec, p, blocks, smem, st, false);
+}
+
+int hx_table_occupancy(bool w32, int prec, int nt, size_t smem) {
+    return w32 ? occupancy_t<unsigned>(prec, nt, smem, false) : occupancy_t<unsigned long long>(prec, nt, smem, false);
+}
+
+void hx_table_multi_launch(bool w32, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
+    if (w32) launch_t<unsigned>(prec, p, blocks, smem, st, true);
+    else launch_t<unsigned long long>(prec, p, blocks, smem, st, true);
+}
+
+int hx_table_multi_occupancy(bool w32, int prec, int nt, size_t smem) {
+    return w32 ? occupancy_t<unsigned>(prec, nt, smem, true) : occupancy_t<unsigned long long>(prec, nt, smem, true);
+}
+
+}  // namespace edgpu

@@ -71,8 +71,11 @@ SIGNATURES = {
     "edgpu_op_autotune": (ctypes.c_int, [vp, i32, P(i32), P(dbl)]),
     "edgpu_op_set_pair_schedule": (ctypes.c_int, [vp, i32]),
     "edgpu_op_pair_classes": (ctypes.c_int, [vp, P(i32), P(i32)]),
-    "edgpu_op_get_schedule": (ctypes.c_int, [vp, i32, P(i32), P(i32)]),
-    "edgpu_batch_get_schedule": (ctypes.c_int, [vp, i32, P(i32), P(i32)]),
+    "edgpu_op_get_schedule": (ctypes.c_int, [vp, i32, P(i32), P(i32), P(i32)]),
+    "edgpu_op_build_targets": (ctypes.c_int, [vp, i64, P(i32)]),
+    "edgpu_op_free_targets": (ctypes.c_int, [vp]),
+    "edgpu_op_targets_info": (ctypes.c_int, [vp, P(i64), P(i32)]),
+    "edgpu_batch_get_schedule": (ctypes.c_int, [vp, i32, P(i32), P(i32), P(i32)]),
     "edgpu_op_sparse": (ctypes.c_int, [vp, i32, dbl, P(i64), P(i64), P(i64), P(dbl)]),
     "edgpu_op_get_row": (ctypes.c_int, [vp, i32, i64, dbl, i64, P(i64), P(i64), P(dbl)]),
     "edgpu_op_is_invariant": (ctypes.c_int, [vp, P(i32)]),

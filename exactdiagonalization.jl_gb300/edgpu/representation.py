@@ -574,8 +574,35 @@ class OperatorRepresentation:
         """(rows_per_tile as in set_tiling, pair flips) used by the product: pair flips = 0 when
         every row tests every term, else the targets per lane and step of the pair-flip schedule."""
         a, b = ctypes.c_int32(), ctypes.c_int32()
-        check(lib().edgpu_op_get_schedule(self._h, _prec(precision), ctypes.byref(a), ctypes.byref(b)))
+        check(lib().edgpu_op_get_schedule(self._h, _prec(precision), ctypes.byref(a), ctypes.byref(b), None))
         return int(a.value), int(b.value)
+
+    def uses_target_table(self, precision="mixed") -> bool:
+        t = ctypes.c_int32()
+        check(lib().edgpu_op_get_schedule(self._h, _prec(precision), None, None, ctypes.byref(t)))
+        return bool(t.value)
+
+    def build_targets(self, max_bytes: Optional[int] = None) -> bool:
+        """Build the target table of the pair-flip schedule (the entry of every (row, target) of the
+        product, 4 or 8 bytes each) when the terms allow the schedule and the table needs at most
+        max_bytes (default: a quarter of the free device memory).  Returns whether it was built."""
+        if max_bytes is None:
+            import torch
+            free, _ = torch.cuda.mem_get_info()
+            max_bytes = free // 4
+        built = ctypes.c_int32()
+        check(lib().edgpu_op_build_targets(self._h, int(max_bytes), ctypes.byref(built)))
+        return bool(built.value)
+
+    def free_targets(self) -> None:
+        check(lib().edgpu_op_free_targets(self._h))
+
+    @property
+    def targets_info(self) -> Tuple[int, int]:
+        """(entries, bytes per entry) of the target table; (0, 0) without one."""
+        n, b = ctypes.c_int64(), ctypes.c_int32()
+        check(lib().edgpu_op_targets_info(self._h, ctypes.byref(n), ctypes.byref(b)))
+        return int(n.value), int(b.value)
 
     def pair_classes(self):
         """(bond classes, rotation components) of the pair-flip schedule; (0, 0) when it does not apply."""
@@ -847,8 +874,13 @@ class Batch:
     def schedule(self, precision="mixed"):
         """(lanes per row, pair flips as in OperatorRepresentation.schedule) of the batched launch."""
         a, b = ctypes.c_int32(), ctypes.c_int32()
-        check(lib().edgpu_batch_get_schedule(self._h, _prec(precision), ctypes.byref(a), ctypes.byref(b)))
+        check(lib().edgpu_batch_get_schedule(self._h, _prec(precision), ctypes.byref(a), ctypes.byref(b), None))
         return int(a.value), int(b.value)
+
+    def uses_target_tables(self, precision="mixed") -> bool:
+        t = ctypes.c_int32()
+        check(lib().edgpu_batch_get_schedule(self._h, _prec(precision), None, None, ctypes.byref(t)))
+        return bool(t.value)
 
     def autotune(self, precision="mixed"):
         """Time 1, 2 and 4 lanes per row, with and without the pair-flip schedule, and keep the

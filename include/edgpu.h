@@ -166,9 +166,23 @@ int edgpu_op_set_pair_schedule(edgpu_op op, int32_t enable);
  * their rotation components in total. */
 int edgpu_op_pair_classes(edgpu_op op, int32_t* n_classes, int32_t* n_components);
 /* The schedule the product uses for this precision: rows_per_tile as in edgpu_op_set_tiling (0 =
- * default) and pair_flips = 0 when every row tests every term, else the targets each lane looks up
- * per step in the pair-flip schedule (2, or 4 with a parent-state map); either pointer nullable. */
-int edgpu_op_get_schedule(edgpu_op op, int32_t precision, int32_t* rows_per_tile, int32_t* pair_flips);
+ * default), pair_flips = 0 when every row tests every term, else the targets each lane looks up per
+ * step in the pair-flip schedule (2, or 4 with a parent-state map or a target table), and
+ * target_table = 1 when the product reads the target table; every pointer nullable. */
+int edgpu_op_get_schedule(edgpu_op op, int32_t precision, int32_t* rows_per_tile, int32_t* pair_flips,
+                          int32_t* target_table);
+/* Target table of the pair-flip schedule: the entry (representative row, orbit-size index and, for
+ * characters other than 1, group element; 4 or 8 bytes) of every (row, target) of the product, stored
+ * once in the order the product walks them.  It is the (row, target)-indexed form of the
+ * reference's parent-sized basis_mapping_index, read per target by the row iterator
+ * (reduced_operator_representation.jl:57-85; symmetry_reduce_generic.jl:33-35): products then stream
+ * it instead of looking every target up, with bit-identical results.  Built (with the space's
+ * parent-state map when it has one, else by canonicalisation and search) when the operator's terms
+ * allow the pair-flip schedule and the table needs at most max_bytes; *built = 0 otherwise. */
+int edgpu_op_build_targets(edgpu_op op, int64_t max_bytes, int32_t* built);
+int edgpu_op_free_targets(edgpu_op op);
+/* Entries of the target table and bytes per entry; 0 and 0 without a table. */
+int edgpu_op_targets_info(edgpu_op op, int64_t* entries, int32_t* entry_bytes);
 /* Sparse matrix of the representation, assembled on the device in FP64: rows sorted by column,
  * entries of equal column summed, entries with |value| < tol dropped (tol: the reference's
  * Base.rtoldefault(Float64) = sqrt(eps) gives its default).  This is sparse(opr)
@@ -247,8 +261,10 @@ int edgpu_batch_set_tiling(edgpu_batch b, int32_t precision, int32_t lanes_per_r
  * pair-flip schedule where it applies (and the first operator allows it), on scratch vectors
  * (allocated and freed here) and keeps the fastest. */
 int edgpu_batch_autotune(edgpu_batch b, int32_t precision, int32_t* lanes_per_row_out, double* best_ms_out);
-/* The batched launch's lanes per row (0 = default) and pair_flips as in edgpu_op_get_schedule. */
-int edgpu_batch_get_schedule(edgpu_batch b, int32_t precision, int32_t* lanes_per_row, int32_t* pair_flips);
+/* The batched launch's lanes per row (0 = default), and pair_flips and target_table as in
+ * edgpu_op_get_schedule (the batch reads target tables when every operator has one). */
+int edgpu_batch_get_schedule(edgpu_batch b, int32_t precision, int32_t* lanes_per_row, int32_t* pair_flips,
+                             int32_t* target_table);
 /* y_k = H_k x_k for every k, device vectors (arrays of n_ops pointers).  The first call with a set of
  * pointers uploads the sector descriptors (synchronous); if use_graph != 0 that launch is also
  * captured once into a CUDA graph and replayed on the later calls with the same pointers. */

@@ -27,13 +27,13 @@ def relerr(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
 
 
-def run(E, opr, x, prec, sched, pair):
+def run(E, opr, x, prec, sched, pair, tps=2):
     import torch
     dt = torch.complex128 if prec == "fp64" else torch.complex64
     xd = torch.from_numpy(x).to(dt).cuda()
     yd = torch.empty_like(xd)
     opr.set_tiling(prec, sched)
-    opr.set_pair_schedule(pair)
+    opr.set_pair_schedule(pair, tps)
     E.mul_(yd, opr, xd, precision=prec)
     torch.cuda.synchronize()
     opr.set_tiling(prec, 0)
@@ -297,3 +297,154 @@ def test_autotune_picks_a_schedule(edgpu):
     b = edgpu.Batch([opr])
     lpr, _ = b.autotune("mixed")
     assert lpr in (1, 2, 4) and b.schedule("mixed") == (lpr, 0)
+
+
+def products_lpr1(E, opr, x):
+    """Pair-flip products at one lane per row in both precisions (2 targets per step)."""
+    return {p: run(E, opr, x, p, -1, True) for p in ("fp64", "mixed")}
+
+
+def test_target_table_chain_all_momenta(edgpu):
+    """The target table holds the entry of every (row, target) in the product's order: the product
+    that streams it equals the looked-up product bit for bit (built with and without a parent-state
+    map, at every momentum, so with group elements in the entries) and the oracle."""
+    import torch
+    from edgpu import lattice
+    L = 14
+    hs, hsr, parent, bw, off = chain(edgpu, L)
+    bonds = lattice.chain_bonds(L) + [(i, (i + 2) % L) for i in range(L)]
+    jxy = [1.0] * L + [0.35] * L
+    jz = [0.8] * L + [0.2] * L
+    H = lattice.xxz_hamiltonian(hs, bonds, jxy, jz)
+    terms = O.heisenberg_terms(L, bonds, jxy, jz)
+    for m in range(L):
+        rh = edgpu.symmetry_reduce(hsr, edgpu.translation_symops(L, m))
+        maps, amps = O.translation_symops((L, 1), (m, 0))
+        red = O.symmetry_reduce(parent, bw, off, maps, amps)
+        opr = edgpu.represent(rh, H)
+        x = O.complex_gaussian(rh.dimension, 70 + m)
+        plain = products_lpr1(edgpu, opr, x)
+        for with_map in (False, True):
+            if with_map:
+                assert rh.build_map(1 << 28)
+            assert opr.build_targets(1 << 28)
+            n, b = opr.targets_info
+            nt, nnz = opr.count_nnz()
+            assert n == nt and b in (4, 8)
+            for prec in ("fp64", "mixed"):
+                assert opr.uses_target_table(prec)
+                for tps in (2, 4):
+                    y = run(edgpu, opr, x, prec, -1, True, tps)
+                    assert torch.equal(y, plain[prec]), (m, with_map, prec, tps)
+            y = run(edgpu, opr, x, "fp64", -1, True).cpu().numpy()
+            assert relerr(y, O.apply_rows(red, terms, x)) < FP64_TOL
+            opr.free_targets()
+            assert opr.targets_info == (0, 0)
+            rh.free_map()
+
+
+@pytest.mark.parametrize("shape,vectors", [((4, 4), "square"), ((6, 3), "triangular")])
+def test_target_table_torus(edgpu, shape, vectors):
+    import torch
+    from edgpu import lattice
+    L1, L2 = shape
+    n = L1 * L2
+    hs, _ = edgpu.spin_half_system(n)
+    hsr = edgpu.represent(edgpu.HilbertSpaceSector(hs, 0), lazy=True)
+    nn, nnn = ((lattice.SQUARE_NN, lattice.SQUARE_NNN) if vectors == "square"
+               else (lattice.TRIANGULAR_NN, lattice.TRIANGULAR_NNN))
+    bonds = lattice.torus_bonds(L1, L2, nn) + lattice.torus_bonds(L1, L2, nnn)
+    H = lattice.xxz_hamiltonian(hs, bonds, 1.0, 0.7)
+    for k in [(0, 0), (1, 1), (L1 - 1, 0)]:
+        rh = edgpu.symmetry_reduce(hsr, edgpu.translation_symops(shape, k))
+        opr = edgpu.represent(rh, H)
+        x = O.complex_gaussian(rh.dimension, 11)
+        plain = products_lpr1(edgpu, opr, x)
+        assert opr.build_targets(1 << 28)
+        for prec in ("fp64", "mixed"):
+            assert torch.equal(run(edgpu, opr, x, prec, -1, True), plain[prec]), (k, prec)
+        opr.free_targets()
+
+
+def test_target_table_pair_terms_full_space(edgpu):
+    """Entries of targets outside the table (here none are) and parallel-bit terms in the full space."""
+    import torch
+    L = 10
+    hs, _ = edgpu.spin_half_system(L)
+    full = edgpu.represent(hs)
+    _, offs = O.bit_layout(O.spin_half_sites(L))
+    op_o = []
+    for i in range(L):
+        j = (i + 1) % L
+        op_o += O.op_scale(0.6 + 0.35j, O.op_mul(O.pauli_matrix(offs, i, "+"), O.pauli_matrix(offs, j, "-")))
+        op_o += O.op_scale(0.6 - 0.35j, O.op_mul(O.pauli_matrix(offs, i, "-"), O.pauli_matrix(offs, j, "+")))
+        op_o += O.op_scale(0.25, O.op_mul(O.pauli_matrix(offs, i, "+"), O.pauli_matrix(offs, j, "+")))
+        op_o += O.op_scale(0.25, O.op_mul(O.pauli_matrix(offs, i, "-"), O.pauli_matrix(offs, j, "-")))
+    op_o = O.simplify(op_o)
+    m_, r_, c_, a_ = O.term_arrays(op_o)
+    for m in (0, 3):
+        rh = edgpu.symmetry_reduce(full, edgpu.translation_symops(L, m))
+        opr = edgpu.OperatorRepresentation.from_terms(rh, m_, r_, c_, a_)
+        x = O.complex_gaussian(rh.dimension, 5)
+        plain = products_lpr1(edgpu, opr, x)
+        assert opr.build_targets(1 << 26)
+        for prec in ("fp64", "mixed"):
+            assert torch.equal(run(edgpu, opr, x, prec, -1, True), plain[prec])
+
+
+def test_target_table_limit_and_term_scan(edgpu):
+    """No table when it would exceed the byte limit or when the terms do not allow pair flips."""
+    from edgpu import lattice
+    hs, hsr, _, _, _ = chain(edgpu, 12)
+    rh = edgpu.symmetry_reduce(hsr, edgpu.translation_symops(12, 0))
+    opr = edgpu.represent(rh, lattice.xxz_hamiltonian(hs, lattice.chain_bonds(12), 1.0, 1.0))
+    assert not opr.build_targets(16)
+    assert opr.targets_info == (0, 0)
+    Hx = lattice.xxz_hamiltonian(hs, lattice.chain_bonds(12), 1.0, 1.0) + 0.3 * edgpu.pauli_matrix(hs, 0, "x")
+    opx = edgpu.represent(edgpu.represent(hs), Hx)
+    assert not opx.build_targets(1 << 26)
+
+
+def test_target_table_batch(edgpu):
+    """All momentum sectors of a triangular 4x3 torus in one launch through their target tables equal
+    the per-sector products bit for bit."""
+    import torch
+    from edgpu import lattice
+    L1, L2 = 4, 3
+    n = L1 * L2
+    hs, _ = edgpu.spin_half_system(n)
+    hsr = edgpu.represent(edgpu.HilbertSpaceSector(hs, 0))
+    bonds = lattice.torus_bonds(L1, L2, lattice.TRIANGULAR_NN) + lattice.torus_bonds(L1, L2, lattice.TRIANGULAR_NNN)
+    H = lattice.xxz_hamiltonian(hs, bonds, 1.0, 0.8)
+    spaces = [edgpu.symmetry_reduce(hsr, edgpu.translation_symops((L1, L2), (a, b)))
+              for b in range(L2) for a in range(L1)]
+    oprs = [edgpu.represent(sp, H) for sp in spaces]
+    for prec in ("fp64", "mixed"):
+        xs = [edgpu.random_state(o.dimension, 80 + i, prec) for i, o in enumerate(oprs)]
+        ref = []
+        for o, x in zip(oprs, xs):
+            o.set_tiling(prec, -1)
+            y = torch.empty_like(x)
+            edgpu.mul_(y, o, x, precision=prec)
+            ref.append(y)
+            o.set_tiling(prec, 0)
+        for o in oprs:
+            assert o.build_targets(1 << 26)
+        b = edgpu.Batch(oprs)
+        b.set_tiling(prec, 1)
+        assert b.uses_target_tables(prec)
+        for use_graph in (False, True):
+            ys = [torch.empty_like(x) for x in xs]
+            b.mul_(ys, xs, precision=prec, use_graph=use_graph)
+            torch.cuda.synchronize()
+            for y, r in zip(ys, ref):
+                assert torch.equal(y, r), (prec, use_graph)
+        lpr, _ = b.autotune(prec)
+        ys = [torch.empty_like(x) for x in xs]
+        b.mul_(ys, xs, precision=prec, use_graph=True)
+        torch.cuda.synchronize()
+        tol = FP64_TOL if prec == "fp64" else MIXED_TOL
+        for y, r in zip(ys, ref):
+            assert (torch.linalg.vector_norm(y - r) / torch.linalg.vector_norm(r)).item() < tol
+        for o in oprs:
+            o.free_targets()
