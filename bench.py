@@ -129,6 +129,33 @@ def build_maps(spaces, args):
     return {"built": True, "entries": entries, "bytes": nbytes, "build_s": time.perf_counter() - t0}
 
 
+def build_tables(oprs, spaces, args):
+    """Target tables of the pair-flip schedule (unless --no-table): {"built", "entries", "bytes",
+    "build_s", "maps_freed"} or None.  Each table may take up to 80% of the free device memory; once
+    every operator has one, the parent-state maps (used only to build them faster) are freed."""
+    import torch
+    if args.no_table or args.no_pair or not hasattr(oprs[0], "build_targets"):
+        return None
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    entries = nbytes = 0
+    for o in oprs:
+        free, _ = torch.cuda.mem_get_info()
+        if not o.build_targets(int(0.8 * free)):
+            return {"built": False}
+        n, b = o.targets_info
+        entries += n
+        nbytes += n * b
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    freed = False
+    for sp in spaces:
+        if hasattr(sp, "free_map") and sp.map_info[0] > 0:
+            sp.free_map()
+            freed = True
+    return {"built": True, "entries": entries, "bytes": nbytes, "build_s": dt, "maps_freed": freed}
+
+
 def build_gpu_operator(wl):
     import edgpu
     from edgpu import lattice
@@ -350,6 +377,7 @@ def run_gpu(args, wl):
     n_targets, nnz = opr.count_nnz()
     dir_stats = edgpu.search_stats(space)
     map_info = build_maps([space], args)
+    table_info = build_tables([opr], [space], args)
     if args.no_pair:
         opr.set_pair_schedule(False)
     if args.tiling:
@@ -439,21 +467,36 @@ def run_gpu(args, wl):
     # time to E0 (Lanczos): FP64 product vs mixed product polished in FP64
     e0_info = None
     if not args.no_lanczos:
-        # Time to E0 with both runs stopped once the lowest Ritz value settles to 1e-12 relative over five
-        # steps: FP64 Lanczos from the seeded start vector, and mixed-precision Lanczos (complex64
-        # products) to about 1e-7 followed by FP64 Lanczos from its Ritz vector.
+        # Time to E0.  The FP64 oracle: FP64 Lanczos from the seeded start vector until the lowest Ritz
+        # value settles to 1e-12 relative over five steps.  Against the 1e-9 target both arms then run to
+        # 1e-10: FP64 Lanczos (settled to 1e-10), and mixed-precision Lanczos (complex64 products, settled
+        # to 1e-9) followed by the FP64 Rayleigh quotient of its Ritz vector, accepted when the
+        # Kato-Temple estimate of its error is below 1e-10 relative (else FP64 Lanczos from that vector).
+        # the stored Krylov basis (which gives the Ritz vector without a second pass of the recurrence)
+        # may take 80% of the device memory left after the operator's tables
         torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        free_b, _ = torch.cuda.mem_get_info()
+        krylov_limit = int(0.8 * free_b)
+        edgpu.set_krylov_limit(krylov_limit)
         t0 = time.perf_counter()
         r64 = edgpu.lanczos(opr, wl["lanczos_steps"], precision="fp64", reorth=wl["reorth"], seed=wl["seed"], tol=1e-12)
         t64 = time.perf_counter() - t0
         t0 = time.perf_counter()
+        r64b = edgpu.lanczos(opr, wl["lanczos_steps"], precision="fp64", reorth=wl["reorth"], seed=wl["seed"], tol=1e-10)
+        t64b = time.perf_counter() - t0
+        t0 = time.perf_counter()
         rmx = edgpu.lanczos(opr, wl["lanczos_steps"], precision="mixed", reorth=wl["reorth"], seed=wl["seed"],
-                            refine=True, tol=1e-12)
+                            refine=True, tol=1e-10)
         tmx = time.perf_counter() - t0
-        e0_info = {"fp64_s": t64, "mixed_s": tmx, "e0_fp64": r64.e0, "e0_mixed": rmx.e0,
-                   "rel_diff": abs(rmx.e0 - r64.e0) / abs(r64.e0), "steps_fp64": r64.steps, "steps_mixed": rmx.steps,
-                   "reorth": bool(wl["reorth"]), "max_steps": wl["lanczos_steps"],
+        e0_info = {"fp64_oracle_s": t64, "fp64_s": t64b, "mixed_s": tmx, "target_rel": 1e-9, "tol": 1e-10,
+                   "e0_fp64_oracle": r64.e0, "e0_fp64": r64b.e0, "e0_mixed": rmx.e0,
+                   "rel_diff": abs(rmx.e0 - r64.e0) / abs(r64.e0),
+                   "rel_diff_fp64": abs(r64b.e0 - r64.e0) / abs(r64.e0),
+                   "steps_fp64_oracle": r64.steps, "steps_fp64": r64b.steps, "steps_mixed": rmx.steps,
+                   "reorth": bool(wl["reorth"]), "max_steps": wl["lanczos_steps"], "krylov_limit_bytes": krylov_limit,
                    "fp64_e0_change_last_20_steps": tridiagonal_e0_change(r64, 20)}
+        edgpu.set_krylov_limit(0)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not wl.get("cpu_feasible", True):
@@ -474,6 +517,9 @@ def run_gpu(args, wl):
                        "rows_per_tile": {"mixed": tune_mixed[0], "fp64": tune_fp64[0]},
                        "pair_flip_schedule": {"mixed": opr.schedule("mixed")[1], "fp64": opr.schedule("fp64")[1],
                                               "bond_classes": opr.pair_classes()[0]},
+                       "target_table": dict(table_info or {"built": False},
+                                            used={"mixed": opr.uses_target_table("mixed"),
+                                                  "fp64": opr.uses_target_table("fp64")}),
                        "setup_s": t_space, "search_directory": dir_stats, "parent_map": map_info},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_src},
@@ -499,6 +545,7 @@ def run_gpu_batch(args, wl):
     N = sum(dims)
     nnz = sum(o.count_nnz()[1] for o in oprs)
     map_info = build_maps(spaces, args)
+    table_info = build_tables(oprs, spaces, args)
     if args.no_pair:
         for o in oprs:
             o.set_pair_schedule(False)
@@ -587,6 +634,7 @@ def run_gpu_batch(args, wl):
             "config": {"workload": args.workload, "description": wl["desc"], "sectors": len(dims), "N_r_total": N,
                        "N_r_min": min(dims), "N_r_max": max(dims), "nnz_off": nnz, "bytes_per_step": b_step,
                        "lanes_per_row": lpr, "pair_flip_schedule": batch.schedule("mixed")[1],
+                       "target_table": dict(table_info or {"built": False}, used=batch.uses_target_tables("mixed")),
                        "bond_classes": oprs[0].pair_classes()[0], "l2": f"inputs cycled from {P} sets of x/y ({2 * P * N * s_c / 1e6:.0f} MB "
                        f"> 2x L2)", "parallelism": f"replicas x{world}", "setup_s": t_space,
                        "library_graph_ms_per_step": ms_graph, "parent_map": map_info},
@@ -687,6 +735,7 @@ def main():
                     help="fixed schedule instead of the autotuner: -1/-2/-4 lanes per row (single-sector workloads)")
     ap.add_argument("--pair-targets", type=int, default=2, choices=[0, 2, 4],
                     help="with --tiling: targets per lane and step of the pair-flip schedule (0: term scan)")
+    ap.add_argument("--no-table", action="store_true", help="no target tables (look every target up per product)")
     ap.add_argument("--no-pair", action="store_true", help="test every term per row instead of the pair-flip schedule")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)

@@ -111,6 +111,7 @@ struct Blob {
     size_t smem_bond = 0;    // shared memory of the mapped pair-flip kernel (the blob's prefix up to the bond tables)
     size_t smem_bond_canon = 0;   // of the canonicalising one (through the torus row table)
     size_t term_start = 0;   // offset of the term records in the term image (before: group and torus tables)
+    size_t bond_end = 0;     // end of the bond classes in the pair-flip image (the torus row table follows)
     void* d_pair = nullptr;  // the pair-flip image: group tables, bond classes, torus row table
     std::vector<unsigned char> pair_host;   // its host copy (batched images start from it)
     HxParams tmpl_pair{};    // launch template of the pair-flip kernel (offsets into d_pair)
@@ -156,6 +157,7 @@ struct edgpu_op_s {
     int tab_wide = 0, tab_cb = 0;
     int64_t tab_n = 0;
     int tab_use[2] = {1, 1};          // [precision]: products read the table (chosen by the autotuner)
+    int tab_pf[2] = {0, 0};           // [precision]: x prefetched this many steps ahead (chosen by the autotuner)
     void free_table() {
         if (d_tab) cudaFree(d_tab);
         if (d_tile_off) cudaFree(d_tile_off);
@@ -179,12 +181,14 @@ struct edgpu_batch_s {
     int pair_use[2] = {1, 1};                      // pair-flip schedule where the terms allow it (autotuned)
     int pair_nt[2] = {2, 2};                       // its targets per lane and step with sector maps
     int tab_use[2] = {1, 1};                       // read the sectors' target tables (autotuned)
+    int tab_pf[2] = {0, 0};                        // their x prefetch distance in steps (autotuned)
     struct Fused {
         bool ready = false;
         std::vector<uint64_t> gens;                // operator table generations the image was built from
         std::vector<unsigned char> image;          // common tables + per-sector character tables + descriptors
                                                    // + term records
         size_t smem_pair = 0;                      // the image's part before the term records
+        size_t smem_lookup = 0;                    // its part before the torus row table
         std::vector<int> o_ph, o_num, want_arg;
         HxParams tmpl{};
         int gk = 0, per_sm = 1, per_sm_map = 0;
@@ -642,6 +646,7 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     B.smem_bond = std::max<size_t>(bond_prefix, 16);
     B.smem_bond_canon = std::max<size_t>(bond_prefix_canon, 16);
     B.term_start = term_start;
+    B.bond_end = bond_prefix;
     B.max_blocks_bond[0][0] = B.max_blocks_bond[0][1] = B.max_blocks_bond[1][0] = B.max_blocks_bond[1][1] = 0;
     B.max_blocks_table[0] = B.max_blocks_table[1] = 0;
     const int per_sm = std::max(1, hx_max_blocks_per_sm(w32, gk, prec, mode, tot));
@@ -739,6 +744,7 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
                 p.tile_off = op->d_tile_off;
                 p.tab_wide = op->tab_wide;
                 p.tab_cb = op->tab_cb;
+                p.bond_pf = op->tab_pf[prec];
                 int& mt = B.max_blocks_table[p.bond_nt == 4 ? 1 : 0];
                 if (mt == 0) mt = std::max(1, hx_table_occupancy(w32, prec, p.bond_nt, smem)) * std::max(1, g_sm_count);
                 const long long warps = (p.n_rows + 31) / 32;
@@ -846,6 +852,23 @@ int sturm_count(const std::vector<double>& a, const std::vector<double>& b, doub
         if (d < 0) ++cnt;
     }
     return cnt;
+}
+
+// k-th lowest eigenvalue (k = 1, 2, ...) of tridiag(a, b) by Sturm bisection.
+double kth_eigenvalue(const std::vector<double>& a, const std::vector<double>& b, int k) {
+    double lo = a[0], hi = a[0];
+    for (size_t i = 0; i < a.size(); ++i) {
+        const double r = (i ? std::fabs(b[i - 1]) : 0.0) + (i + 1 < a.size() ? std::fabs(b[i]) : 0.0);
+        lo = std::min(lo, a[i] - r);
+        hi = std::max(hi, a[i] + r);
+    }
+    for (int it = 0; it < 200; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
+        if (sturm_count(a, b, mid) >= k) hi = mid;
+        else lo = mid;
+    }
+    return 0.5 * (lo + hi);
 }
 
 double lowest_eigenvalue(const std::vector<double>& a, const std::vector<double>& b) {
@@ -1534,20 +1557,21 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     // rows per warp tile when there is no parent-state map); where the pair-flip schedule applies
     // (and the caller allows it), that schedule with 2 or 4 targets per step (4 with a map or a
     // target table) and 1, 2 or 4 lanes per row, and its target-table flavour (one lane per row).
-    struct Cand { int pair, nt, table, rows; };
+    struct Cand { int pair, nt, table, rows, pf; };
     std::vector<Cand> cands;
     build_blob(op, precision, 0, 0);
     const bool pair_ok = op->blob[precision][0][0].tmpl.bond_ncls > 0 && op->pair_allowed;
     const bool mapped = op->space->d_map != nullptr;
     if (pair_ok) {
         if (op->d_tab)
-            for (int nt : {4, 2}) cands.push_back({1, nt, 1, -1});
+            for (int nt : {4, 2})
+                for (int pf : {0, 4, 64}) cands.push_back({1, nt, 1, -1, pf});
         for (int nt : (mapped ? std::vector<int>{4, 2} : std::vector<int>{2}))
-            for (int r : {-1, -2, -4}) cands.push_back({1, nt, 0, r});
+            for (int r : {-1, -2, -4}) cands.push_back({1, nt, 0, r, 0});
     }
-    for (int r : {-1, -2, -4}) cands.push_back({0, 2, 0, r});
+    for (int r : {-1, -2, -4}) cands.push_back({0, 2, 0, r, 0});
     if (!mapped)
-        for (int r : {32, 16}) cands.push_back({0, 2, 0, r});
+        for (int r : {32, 16}) cands.push_back({0, 2, 0, r, 0});
     Cand best = cands.front();
     double best_ms = 1e30;
     const int keep_pair = op->pair_use[precision], keep_nt = op->pair_nt[precision], keep_tab = op->tab_use[precision];
@@ -1565,6 +1589,7 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
                 op->pair_use[precision] = c.pair;
                 op->pair_nt[precision] = c.nt;
                 op->tab_use[precision] = c.table;
+                op->tab_pf[precision] = c.pf;
                 launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, g_stream, nullptr, c.rows);
                 float tot = 0.f;
                 const int reps = 3;
@@ -1600,6 +1625,7 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     op->pair_use[precision] = best.pair;
     op->pair_nt[precision] = best.nt;
     op->tab_use[precision] = best.table ? 1 : (op->d_tab ? 0 : 1);
+    op->tab_pf[precision] = best.pf;
     op->tuned_rows[precision] = best.rows;
     if (rows_per_tile_out) *rows_per_tile_out = best.rows;
     if (best_ms_out) *best_ms_out = best_ms;
@@ -2031,22 +2057,32 @@ void batch_prepare(edgpu_batch_s* b, int prec) {
     }
     const Blob& B0 = o0->blob[prec][0][0];
     const size_t vsz = prec == EDGPU_FP64 ? 16 : 8;
-    // image: the blob's group, bond-class and torus tables, every sector's character tables, room for
-    // the sector descriptors, then the blob's term records (relocated); the pair-flip kernel copies
-    // only the part before the term records
+    // image: the blob's group tables and bond classes, every sector's character tables (phase tables
+    // shared between sectors of the same denominator), room for the sector descriptors, the torus row
+    // table, then the blob's term records (relocated).  The pair-flip kernel copies the part before the
+    // torus row table when it reads parent-state maps or target tables, through it when it
+    // canonicalises; the term scan copies everything.  Shared memory left to L1 keeps the lanes' table
+    // runs cached.
     const size_t full = (size_t)B0.tmpl.blob_words16 * 16;
     const size_t tstart = std::min(B0.term_start, full);
     std::vector<unsigned char> blob_h(full, 0);
     if (full) EDGPU_CUDA(cudaMemcpy(blob_h.data(), B0.d, full, cudaMemcpyDeviceToHost));
-    F.image = B0.pair_host;   // group tables, bond classes, torus row table
+    const size_t bend = std::min(B0.bond_end, B0.pair_host.size());
+    F.image.assign(B0.pair_host.begin(), B0.pair_host.begin() + bend);   // group tables, bond classes
     F.o_ph.assign(n, 0);
     F.o_num.assign(n, 0);
     F.want_arg.assign(n, 0);
     int any_arg = 0;
     F.rows = 0;
+    std::map<int, int> ph_of_den;
     for (int i = 0; i < n; ++i) {
         const Group& g = b->ops[i]->space->group;
+        auto known = ph_of_den.find(g.den);
+        if (known != ph_of_den.end()) {
+            F.o_ph[i] = known->second;
+        } else {
         F.o_ph[i] = (int)F.image.size();
+        ph_of_den[g.den] = F.o_ph[i];
         F.image.resize(align16(F.image.size() + g.den * vsz), 0);
         for (int j = 0; j < g.den; ++j) {
             const double ang = 2.0 * M_PI * (double)j / (double)g.den;
@@ -2058,6 +2094,7 @@ void batch_prepare(edgpu_batch_s* b, int prec) {
                 memcpy(&F.image[F.o_ph[i] + j * 8], v, 8);
             }
         }
+        }
         F.o_num[i] = (int)F.image.size();
         F.image.resize(align16(F.image.size() + g.G * 4), 0);
         memcpy(&F.image[F.o_num[i]], g.num.data(), g.G * 4);
@@ -2065,9 +2102,15 @@ void batch_prepare(edgpu_batch_s* b, int prec) {
         any_arg |= F.want_arg[i];
         F.rows += b->ops[i]->space->dim;
     }
-    F.tmpl = B0.tmpl_pair;   // offsets of the pair image; the term records are relocated below
+    F.tmpl = B0.tmpl_pair;   // offsets of the pair image; the torus table and term records are relocated
     F.tmpl.o_sec = (int)F.image.size();
     F.image.resize(align16(F.image.size() + (size_t)n * sizeof(SectorDesc)), 0);
+    F.smem_lookup = F.image.size();
+    if (F.tmpl.o_rlut >= 0) {
+        F.tmpl.o_rlut = (int)F.image.size();
+        F.image.insert(F.image.end(), B0.pair_host.begin() + bend, B0.pair_host.end());
+        F.image.resize(align16(F.image.size()), 0);
+    }
     F.smem_pair = F.image.size();
     const int delta = (int)F.image.size() - (int)tstart;   // term records move by this many bytes
     F.image.insert(F.image.end(), blob_h.begin() + tstart, blob_h.end());
@@ -2176,17 +2219,19 @@ HxParams batch_params(edgpu_batch_s* b, int prec, const void* const* xs, void* c
                 p.tab = b->ops[i]->d_tab;   // marks the target-table launch; the kernel reads each sector's
                 break;
             }
-        p.blob_words16 = (int)(F.smem_pair / 16);
+        p.blob_words16 = (int)(F.smem_lookup / 16);
+        p.bond_pf = b->tab_pf[prec];
         int& ps = F.per_sm_table[p.bond_nt == 4 ? 1 : 0];
-        if (ps == 0) ps = std::max(1, hx_table_multi_occupancy(w32, prec, p.bond_nt, F.smem_pair));
+        if (ps == 0) ps = std::max(1, hx_table_multi_occupancy(w32, prec, p.bond_nt, F.smem_lookup));
         per_sm = ps;
     } else if (pair) {
-        p.blob_words16 = (int)(F.smem_pair / 16);
+        const size_t sm_b = mapped ? F.smem_lookup : F.smem_pair;
+        p.blob_words16 = (int)(sm_b / 16);
         int& ps = F.per_sm_bond[mapped ? 1 : 0][p.bond_nt == 4 ? 1 : 0];
         if (ps == 0) {
             const int gk = mapped ? GK_MAP : F.gk;
-            ps = std::max(1, w32 ? hx_bond_multi_occupancy_w32(gk, prec, p.bond_nt, F.smem_pair)
-                                 : hx_bond_multi_occupancy_w64(gk, prec, p.bond_nt, F.smem_pair));
+            ps = std::max(1, w32 ? hx_bond_multi_occupancy_w32(gk, prec, p.bond_nt, sm_b)
+                                 : hx_bond_multi_occupancy_w64(gk, prec, p.bond_nt, sm_b));
         }
         per_sm = ps;
     } else if (mapped && F.per_sm_map == 0) {
@@ -2203,12 +2248,13 @@ void batch_launch(edgpu_batch_s* b, int prec, const HxParams& p, int blocks, cud
     const int gk = p.rank_tab ? GK_MAP : b->fused[prec].gk;   // sector maps present: the map flavour
     const bool w32 = b->ops[0]->space->w32;
     if (p.tab) {
-        hx_table_multi_launch(w32, prec, p, blocks, b->fused[prec].smem_pair, st);
+        hx_table_multi_launch(w32, prec, p, blocks, b->fused[prec].smem_lookup, st);
         return;
     }
     if (p.bond_ncls > 0 && b->ops[0]->pair_allowed && b->pair_use[prec]) {
-        if (w32) hx_bond_multi_launch_w32(gk, prec, p, blocks, b->fused[prec].smem_pair, st);
-        else hx_bond_multi_launch_w64(gk, prec, p, blocks, b->fused[prec].smem_pair, st);
+        const size_t sm_b = gk == GK_MAP ? b->fused[prec].smem_lookup : b->fused[prec].smem_pair;
+        if (w32) hx_bond_multi_launch_w32(gk, prec, p, blocks, sm_b, st);
+        else hx_bond_multi_launch_w64(gk, prec, p, blocks, sm_b, st);
         return;
     }
     if (w32) hx_multi_launch_w32(gk, prec, p, blocks, b->fused[prec].smem, st);
@@ -2247,7 +2293,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
     const size_t vs = precision == EDGPU_FP64 ? 16 : 8;
     int64_t tot = 0;
     for (auto* o : b->ops) tot += o->space->dim;
-    int best = 1, best_pair = 1, best_nt = 2, best_tab = 1;
+    int best = 1, best_pair = 1, best_nt = 2, best_tab = 1, best_pf = 0;
     double best_ms = 1e30;
     if (tot > 0) {
         void *x = nullptr, *y = nullptr;
@@ -2279,8 +2325,14 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
             for (auto* o : b->ops) tabled = tabled && (o->d_tab != nullptr || o->space->dim == 0);
             // cand 4/3: target tables with 4/2 targets per step; 2/1: pair flips with 4/2; 0: term scan
             for (int cand = tabled ? 4 : (pair_ok ? (mapped ? 2 : 1) : 0); cand >= 0; --cand)
-                for (int l : {1, 2, 4}) {
-                    if (cand >= 3 && l != 1) continue;   // target tables: one lane per row
+                for (int l : {1, 2, 4, 5, 6}) {
+                    // target tables: one lane per row, x prefetched 0 (l = 1), 4 (l = 5) or 64 (l = 6)
+                    // steps ahead; the other schedules: l lanes per row
+                    if (cand >= 3 && !(l == 1 || l >= 5)) continue;
+                    if (cand < 3 && l >= 5) continue;
+                    const int pf = l == 5 ? 4 : (l == 6 ? 64 : 0);
+                    b->tab_pf[precision] = pf;
+                    if (l >= 5) l = 1;
                     b->lpr[precision] = l;
                     b->pair_use[precision] = cand > 0 ? 1 : 0;
                     b->pair_nt[precision] = (cand == 2 || cand == 4) ? 4 : 2;
@@ -2302,6 +2354,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
                     if (sum / reps < best_ms) {
                         best_ms = sum / reps;
                         best = l;
+                        best_pf = pf;
                         best_pair = cand > 0 ? 1 : 0;
                         best_nt = (cand == 2 || cand == 4) ? 4 : 2;
                         best_tab = cand >= 3 ? 1 : 0;
@@ -2334,6 +2387,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
     b->pair_use[precision] = best_pair;
     b->pair_nt[precision] = best_nt;
     b->tab_use[precision] = best_tab;
+    b->tab_pf[precision] = best_pf;
     if (lanes_per_row_out) *lanes_per_row_out = best;
     if (best_ms_out) *best_ms_out = best_ms;
     API_END
@@ -2383,7 +2437,7 @@ int edgpu_batch_mul_device(edgpu_batch bh, int32_t precision, const void* const*
     std::vector<const void*> key;
     key.push_back((const void*)(intptr_t)p.lpr);
     key.push_back((const void*)(intptr_t)(b->pair_use[precision] * 8 + b->pair_nt[precision] +
-                                          (p.tab ? 16 : 0)));   // the kernel
+                                          (p.tab ? 16 : 0) + 32 * p.bond_pf));   // the kernel
     key.push_back(p.blob);   // the image (vectors, sector maps) the launch reads
     for (int i = 0; i < n; ++i) {
         key.push_back(xs[i]);
@@ -2577,6 +2631,7 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
     std::vector<double> A, B;
     double E = 0.0;
     int done = 0;
+    bool want_vec_done = false;
     if (!two_phase) {
         int store = ROLL;
         if (reorth || want_vec) {
@@ -2624,16 +2679,47 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
             if ((int)A.size() < budget || done >= m || store != F32 || m1 == m) break;
             start_from(psi.p, nullptr);
         }
-        // 2. FP64 Lanczos from the mixed-precision Ritz vector until the eigenvalue settles to tol
+        // 2. the FP64 Rayleigh quotient of the mixed-precision Ritz vector psi, one FP64 product:
+        //    E_RQ = <psi|H psi>, r = H psi - E_RQ psi.  Its error is of second order in the error of
+        //    psi and is estimated by the Kato-Temple bound |r|^2 / (theta_2 - E_RQ), theta_2 the
+        //    second-lowest Ritz value of the mixed run; accepted when that is below tol |E_RQ|.
+        bool certified = false;
+        if (A.size() >= 2) {
+            launch_norm2_c128(N, psi.p, scratch.p, d_tmp, st);
+            launch_normalize(N, psi.p, d_tmp, psi.p, nullptr, st);
+            launch_product(op, EDGPU_FP64, 0, 0, psi.p, w.p, 0, nullptr, nullptr, st);
+            launch_dot_c128(N, psi.p, w.p, scratch.p, d_alpha, st);
+            launch_lanczos_update(N, w.p, psi.p, nullptr, d_alpha, nullptr, st);
+            launch_norm2_c128(N, w.p, scratch.p, d_beta, st);
+            double hb[2];
+            EDGPU_CUDA(cudaMemcpyAsync(hb, d_alpha, sizeof(double), cudaMemcpyDeviceToHost, st));
+            EDGPU_CUDA(cudaMemcpyAsync(hb + 1, d_beta, sizeof(double), cudaMemcpyDeviceToHost, st));
+            EDGPU_CUDA(cudaStreamSynchronize(st));
+            const double e_rq = hb[0], rn = hb[1];
+            const double theta2 = kth_eigenvalue(A, std::vector<double>(B.begin(), B.begin() + (A.size() - 1)), 2);
+            ++done;
+            if (theta2 > e_rq && rn * rn / (theta2 - e_rq) <= tol * std::max(1.0, std::fabs(e_rq))) {
+                E = e_rq;
+                certified = true;
+            }
+        }
+        // 3. otherwise FP64 Lanczos from the mixed-precision Ritz vector until the eigenvalue settles to tol
         const bool store2 = (reorth || want_vec) && fits64(m);
-        setup(EDGPU_FP64, store2 ? F64 : ROLL, m, reorth != 0 && store2);
-        start_from(psi.p, nullptr);
-        std::vector<double> A2, B2;
-        run(m, tol, A2, B2, nullptr);
-        A = A2;
-        B = B2;
-        E = lowest(A, B);
-        done += (int)A.size();
+        if (!certified) {
+            setup(EDGPU_FP64, store2 ? F64 : ROLL, m, reorth != 0 && store2);
+            start_from(psi.p, nullptr);
+            std::vector<double> A2, B2;
+            run(m, tol, A2, B2, nullptr);
+            A = A2;
+            B = B2;
+            E = lowest(A, B);
+            done += (int)A.size();
+        } else if (want_vec) {
+            // psi is the certified ground state: return it as is
+            EDGPU_CUDA(cudaMemcpyAsync(ground_state, psi.p, N * 16, cudaMemcpyDeviceToHost, st));
+            EDGPU_CUDA(cudaStreamSynchronize(st));
+            want_vec_done = true;
+        }
     }
     *e0 = E;
     if (alphas)
@@ -2641,7 +2727,7 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
     if (betas)
         for (size_t k = 0; k < (size_t)n_steps; ++k) betas[k] = k < B.size() ? B[k] : 0.0;
     if (steps_done) *steps_done = done;
-    if (ground_state) {
+    if (ground_state && !want_vec_done) {
         ritz_vector(A, B, E);
         launch_norm2_c128(N, psi.p, scratch.p, d_tmp, st);
         launch_normalize(N, psi.p, d_tmp, psi.p, nullptr, st);

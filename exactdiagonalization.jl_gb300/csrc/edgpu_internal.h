@@ -211,6 +211,7 @@ struct HxParams {
     int o_bcomp, o_binfo, o_bflip, o_bamp;    // shared-memory offsets of the class tables
     int bond_real;                            // every pair amplitude is real
     int bond_nt;                              // targets per lane and step: 2, or 4 (parent-state map only)
+    int bond_pf;                              // target tables: x prefetched this many steps ahead (0: none)
     // target table of the pair-flip schedule (GK_TABLE launches and the table's build pass)
     const void* tab;
     const long long* tile_off;

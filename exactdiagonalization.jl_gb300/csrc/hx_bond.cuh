@@ -101,6 +101,16 @@ __device__ __forceinline__ void table_entry(const RowsSector<PREC>& sc, long lon
     }
 }
 
+// Prefetch into L2 the x element of the target-table entry at pos (nothing for an entry without a
+// representative), so that the product's later gather of it does not wait for DRAM.
+template <int PREC>
+__device__ __forceinline__ void table_prefetch_x(const RowsSector<PREC>& sc, long long pos, int sb) {
+    long long c;
+    int sx, g;
+    table_entry<PREC>(sc, pos, true, sb, c, sx, g);
+    if (c >= 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(sc.x + c));
+}
+
 // Matching pairs of every class of the row state b (lpr == 1): the row's number of targets.
 template <typename W, int PREC>
 __device__ __forceinline__ int bond_row_count(W b, const BondTables<W, PREC>& bt, int ncls, int n, W full) {
@@ -146,7 +156,7 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
     const bool real_fast = p.bond_real && !sc.want_arg;
     // target table position of this lane's first target: the tile's offset plus the targets of the
     // rows before it in the tile
-    long long tpos = 0;
+    long long tpos = 0, tend = 0, tpf = 0;
     if (GK == GK_TABLE || FILL) {
         const int cnt = bond_row_count<W, PREC>(b, bt, ncls, n, full);
         int incl = cnt;
@@ -156,6 +166,14 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
             if (lane >= d) incl += u;
         }
         tpos = sc.tile_off[tile] + (incl - cnt);
+        tend = tpos + cnt;
+        tpf = tpos;
+        // software prefetch of the gathers: the x elements of the first bond_pf steps' targets now,
+        // then NT more each step (bond_pf steps ahead)
+        if (GK == GK_TABLE && !FILL && p.bond_pf > 0) {
+            const long long lim = min(tend, tpos + (long long)p.bond_pf * NT);
+            for (; tpf < lim; ++tpf) table_prefetch_x<PREC>(sc, tpf, sb);
+        }
     }
     int cls = -1;
     bool cpar = false;   // the current class has terms on parallel bits
@@ -179,7 +197,8 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
             const int i = on[h] ? lowest_bit<W>(m) : 0;
             m &= m - 1;
             ti[h] = on[h] ? cls * n + i : 0;
-            const W f = bt.flip[ti[h]];
+            // (a table read needs the flip mask only for the parallel test)
+            const W f = (GK != GK_TABLE || cpar) ? bt.flip[ti[h]] : (W)0;
             q[h] = b ^ f;
             // amplitude slot: b_i, and whether the pair's bits are parallel (classes with such terms)
             int v = (int)(b >> i) & 1;
@@ -191,6 +210,10 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
             for (int h = 0; h < NT; ++h) {
                 table_entry<PREC>(sc, tpos, on[h], sb, c[h], sx[h], g[h]);
                 tpos += on[h] ? 1 : 0;
+            }
+            if (!FILL && p.bond_pf > 0) {
+                const long long lim = min(tend, tpf + NT);
+                for (; tpf < lim; ++tpf) table_prefetch_x<PREC>(sc, tpf, sb);
             }
         } else {
 #pragma unroll
@@ -294,7 +317,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_bond_kernel(const HxParams p) {
 
 // All sectors of a batch in one persistent launch (the tile numbering of hx_multi_kernel).
 template <typename W, int GK, int PREC, int NT>
-__global__ void __launch_bounds__(HX_THREADS, 5) hx_bond_multi_kernel(const HxParams p) {
+__global__ void __launch_bounds__(HX_THREADS, 4) hx_bond_multi_kernel(const HxParams p) {
     typedef typename Cx<PREC>::V V;
     extern __shared__ __align__(16) unsigned char sm[];
     // programmatic dependent launch: the next kernel in the stream may start its own prologue now;
