@@ -151,8 +151,8 @@ void edgpu_op_destroy(edgpu_op op);
 int edgpu_op_set_tiling(edgpu_op op, int32_t precision, int32_t rows_per_tile);
 /* In-library autotuner: times the product for each candidate schedule (1, 2 or 4 lanes per row, each
  * with and without the pair-flip schedule where it applies; queued with 32 or 16 rows per warp tile)
- * on this operator and keeps the fastest (rows_per_tile_out: the schedule as in edgpu_op_set_tiling;
- * best_ms_out nullable). */
+ * on this operator and keeps the fastest per launch in back-to-back bursts of launches
+ * (rows_per_tile_out: the schedule as in edgpu_op_set_tiling; best_ms_out nullable). */
 int edgpu_op_autotune(edgpu_op op, int32_t precision, int32_t* rows_per_tile_out, double* best_ms_out);
 /* Pair-flip schedule of the row-per-lane product (enable = 1, the default): when every off-diagonal
  * term flips two 1-bit sites (spin-1/2 exchange and pair terms), a row finds its matching terms from

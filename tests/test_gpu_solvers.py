@@ -42,6 +42,18 @@ def test_lanczos_e0_matches_dense(edgpu):
     assert abs(rmx.e0 - e_dense) < 1e-10 * abs(e_dense)
     rnr = edgpu.lanczos(opr, 120, precision="fp64", reorth=False, seed=1)
     assert abs(rnr.e0 - e_dense) < 1e-10 * abs(e_dense)
+    # mixed run closed by the FP64 Rayleigh quotient of its Ritz vector (accepted at 1e-10), and a
+    # tolerance no estimate can meet, which falls back to FP64 Lanczos from that vector
+    rrq = edgpu.lanczos(opr, 120, precision="mixed", reorth=False, seed=1, refine=True, tol=1e-10)
+    assert abs(rrq.e0 - e_dense) < 1e-10 * abs(e_dense)
+    rfb = edgpu.lanczos(opr, 120, precision="mixed", reorth=False, seed=1, refine=True, tol=1e-17)
+    assert abs(rfb.e0 - e_dense) < 1e-10 * abs(e_dense)
+    assert rfb.steps > rrq.steps
+    rgs = edgpu.lanczos(opr, 120, precision="mixed", reorth=False, seed=1, refine=True, tol=1e-10,
+                        want_vector=True)
+    g = rgs.ground_state
+    assert abs(np.linalg.norm(g) - 1.0) < 1e-12
+    assert abs(np.vdot(g, opr @ g).real - e_dense) < 1e-9 * abs(e_dense)
     rv = edgpu.lanczos(opr, 120, precision="fp64", reorth=True, seed=1, want_vector=True)
     psi = rv.ground_state
     hpsi = opr @ psi
