@@ -116,7 +116,7 @@ struct Blob {
     std::vector<unsigned char> pair_host;   // its host copy (batched images start from it)
     HxParams tmpl_pair{};    // launch template of the pair-flip kernel (offsets into d_pair)
     int max_blocks_bond[2][2] = {{0, 0}, {0, 0}};   // resident blocks of the pair-flip kernel [mapped][4 targets]
-    int max_blocks_table[2] = {0, 0};               // of its target-table flavour [4 targets]
+    int max_blocks_table[3] = {0, 0, 0};            // of its target-table flavour [2, 4, 8 targets]
     ~Blob() {
         if (d) cudaFree(d);
         if (d_diag) cudaFree(d_diag);
@@ -648,7 +648,7 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     B.term_start = term_start;
     B.bond_end = bond_prefix;
     B.max_blocks_bond[0][0] = B.max_blocks_bond[0][1] = B.max_blocks_bond[1][0] = B.max_blocks_bond[1][1] = 0;
-    B.max_blocks_table[0] = B.max_blocks_table[1] = 0;
+    B.max_blocks_table[0] = B.max_blocks_table[1] = B.max_blocks_table[2] = 0;
     const int per_sm = std::max(1, hx_max_blocks_per_sm(w32, gk, prec, mode, tot));
     B.max_blocks = per_sm * std::max(1, g_sm_count);
     if (!mode) {
@@ -734,7 +734,9 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
             p.o_bflip = B.tmpl_pair.o_bflip;
             p.o_bamp = B.tmpl_pair.o_bamp;
             p.blob_words16 = (int)(smem / 16);
-            p.bond_nt = ((mapped || table) && op->pair_nt[prec] == 4) ? 4 : 2;
+            // targets per lane and step: 2; 4 with a map or a table; 8 with a table (one product launch)
+            p.bond_nt = op->pair_nt[prec] == 8 ? (table ? 8 : 4) : op->pair_nt[prec] == 4 ? 4 : 2;
+            if (!(mapped || table)) p.bond_nt = 2;
             const bool w32 = op->space->w32;
             if (table) {
                 // the target table: one lane per row, entries streamed in the schedule's order
@@ -745,7 +747,7 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
                 p.tab_wide = op->tab_wide;
                 p.tab_cb = op->tab_cb;
                 p.bond_pf = op->tab_pf[prec];
-                int& mt = B.max_blocks_table[p.bond_nt == 4 ? 1 : 0];
+                int& mt = B.max_blocks_table[p.bond_nt == 8 ? 2 : p.bond_nt == 4 ? 1 : 0];
                 if (mt == 0) mt = std::max(1, hx_table_occupancy(w32, prec, p.bond_nt, smem)) * std::max(1, g_sm_count);
                 const long long warps = (p.n_rows + 31) / 32;
                 const int blocks = (int)std::max<long long>(1, std::min<long long>((warps + HX_THREADS / 32 - 1) / (HX_THREADS / 32), mt));
@@ -1400,10 +1402,11 @@ int edgpu_op_set_tiling(edgpu_op oh, int32_t precision, int32_t rows_per_tile) {
 int edgpu_op_set_pair_schedule(edgpu_op oh, int32_t enable) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
-    require(enable == 0 || enable == 1 || enable == 2 || enable == 4, EDGPU_ERR_ARG, "enable must be 0, 1, 2 or 4");
+    require(enable == 0 || enable == 1 || enable == 2 || enable == 4 || enable == 8, EDGPU_ERR_ARG,
+            "enable must be 0, 1, 2, 4 or 8");
     op->pair_allowed = enable ? 1 : 0;
     op->pair_use[0] = op->pair_use[1] = enable ? 1 : 0;
-    op->pair_nt[0] = op->pair_nt[1] = enable == 4 ? 4 : 2;
+    op->pair_nt[0] = op->pair_nt[1] = enable >= 4 ? enable : 2;
     API_END
 }
 
@@ -1418,7 +1421,9 @@ int edgpu_op_get_schedule(edgpu_op oh, int32_t precision, int32_t* rows_per_tile
     const bool on = op->blob[precision][0][0].tmpl.bond_ncls > 0 && op->pair_allowed && op->pair_use[precision] &&
                     rows <= 0;
     const bool table = on && op->d_tab && op->tab_use[precision];
-    if (pair_flips) *pair_flips = on ? (((op->space->d_map || table) && op->pair_nt[precision] == 4) ? 4 : 2) : 0;
+    int nt = 2;
+    if (on && (op->space->d_map || table) && op->pair_nt[precision] >= 4) nt = (table && op->pair_nt[precision] == 8) ? 8 : 4;
+    if (pair_flips) *pair_flips = on ? nt : 0;
     if (target_table) *target_table = table ? 1 : 0;
     API_END
 }
@@ -1564,7 +1569,7 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     const bool mapped = op->space->d_map != nullptr;
     if (pair_ok) {
         if (op->d_tab)
-            for (int nt : {4, 2})
+            for (int nt : {8, 4, 2})
                 for (int pf : {0, 4, 64}) cands.push_back({1, nt, 1, -1, pf});
         for (int nt : (mapped ? std::vector<int>{4, 2} : std::vector<int>{2}))
             for (int r : {-1, -2, -4}) cands.push_back({1, nt, 0, r, 0});

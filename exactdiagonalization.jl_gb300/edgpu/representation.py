@@ -567,7 +567,8 @@ class OperatorRepresentation:
     def set_pair_schedule(self, enable, targets_per_step: int = 2):
         """Use (default) or bypass the pair-flip schedule of the product for operators whose
         off-diagonal terms all flip two spin-1/2 sites; bypassed, every row tests every term.
-        targets_per_step: 2, or 4 (with a parent-state map)."""
+        targets_per_step: 2, 4 (with a parent-state map or a target table) or 8 (with a target
+        table)."""
         check(lib().edgpu_op_set_pair_schedule(self._h, int(targets_per_step) if enable else 0))
 
     def schedule(self, precision="mixed"):

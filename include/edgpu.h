@@ -159,15 +159,16 @@ int edgpu_op_autotune(edgpu_op op, int32_t precision, int32_t* rows_per_tile_out
  * bond classes (a few word operations per class) instead of testing every term.  Same elements as the
  * term scan of get_row_iterator (operator_iterator.jl:48-54, reduced_operator_representation.jl:57-85);
  * the targets are summed by bond class, then start bit, rather than in term order.  enable = 0 keeps
- * the term scan; 2 or 4 sets the targets each lane looks up per step (4 applies with a parent-state
- * map; 1 = 2).  edgpu_op_autotune may change the choice. */
+ * the term scan; 2, 4 or 8 sets the targets each lane looks up per step (4 applies with a
+ * parent-state map or a target table, 8 with a target table; 1 = 2).  edgpu_op_autotune may change
+ * the choice. */
 int edgpu_op_set_pair_schedule(edgpu_op op, int32_t enable);
 /* Bond classes of the pair-flip schedule for this operator (0 when the terms do not allow it) and
  * their rotation components in total. */
 int edgpu_op_pair_classes(edgpu_op op, int32_t* n_classes, int32_t* n_components);
 /* The schedule the product uses for this precision: rows_per_tile as in edgpu_op_set_tiling (0 =
  * default), pair_flips = 0 when every row tests every term, else the targets each lane looks up per
- * step in the pair-flip schedule (2, or 4 with a parent-state map or a target table), and
+ * step in the pair-flip schedule (2; 4 with a parent-state map or a target table; 8 with a table), and
  * target_table = 1 when the product reads the target table; every pointer nullable. */
 int edgpu_op_get_schedule(edgpu_op op, int32_t precision, int32_t* rows_per_tile, int32_t* pair_flips,
                           int32_t* target_table);

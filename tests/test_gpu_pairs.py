@@ -333,7 +333,7 @@ def test_target_table_chain_all_momenta(edgpu):
             assert n == nt and b in (4, 8)
             for prec in ("fp64", "mixed"):
                 assert opr.uses_target_table(prec)
-                for tps in (2, 4):
+                for tps in (2, 4, 8):
                     y = run(edgpu, opr, x, prec, -1, True, tps)
                     assert torch.equal(y, plain[prec]), (m, with_map, prec, tps)
             y = run(edgpu, opr, x, "fp64", -1, True).cpu().numpy()
