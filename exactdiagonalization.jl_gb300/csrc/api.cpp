@@ -1528,6 +1528,40 @@ int edgpu_op_targets_info(edgpu_op oh, int64_t* entries, int32_t* entry_bytes) {
     API_END
 }
 
+int edgpu_pair_classes_of_terms(int32_t n_bits, int32_t n_terms, const uint64_t* masks, const uint64_t* rows,
+                                const uint64_t* cols, const double* amps, int32_t cap_classes, int32_t* n_classes,
+                                int32_t* info, uint64_t* comps, uint64_t* flips, double* class_amps) {
+    API_BEGIN
+    require(n_bits >= 1 && n_bits <= 64 && n_terms >= 0 && n_classes, EDGPU_ERR_ARG, "bad arguments");
+    require(n_terms == 0 || (masks && rows && cols && amps), EDGPU_ERR_ARG, "null term arrays");
+    Layout lay;
+    lay.n_sites = lay.nbits = n_bits;
+    lay.bw.assign(n_bits, 1);
+    std::vector<uint64_t> bm, br, bf;
+    std::vector<double> ba;
+    for (int t = 0; t < n_terms; ++t) {
+        if (rows[t] == cols[t]) continue;
+        bm.push_back(masks[t]);
+        br.push_back(rows[t]);
+        bf.push_back(rows[t] ^ cols[t]);
+        ba.push_back(amps[2 * t]);
+        ba.push_back(amps[2 * t + 1]);
+    }
+    BondClasses bc;
+    *n_classes = build_bond_classes(lay, bm, br, bf, ba, bc) ? bc.ncls : 0;
+    if (*n_classes > 0 && cap_classes >= *n_classes) {
+        for (int c = 0; c < bc.ncls; ++c) {
+            if (info) info[c] = bc.info[c];
+            for (int k = 0; k < BOND_MAXC; ++k)
+                for (int f = 0; f < 3; ++f)
+                    if (comps) comps[((size_t)c * BOND_MAXC + k) * 3 + f] = bc.comp[((size_t)c * BOND_MAXC + k) * 4 + f];
+        }
+        if (flips) std::copy(bc.flip.begin(), bc.flip.end(), flips);
+        if (class_amps) std::copy(bc.amp.begin(), bc.amp.end(), class_amps);
+    }
+    API_END
+}
+
 int edgpu_op_pair_classes(edgpu_op oh, int32_t* n_classes, int32_t* n_components) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
@@ -1756,6 +1790,17 @@ static bool is_pinned(const void* p) {
     return a.type == cudaMemoryTypeHost;
 }
 
+// The device's address of pinned host memory (null when the device cannot address it): kernels then
+// read and write the host buffer directly over the host link, without a staging copy.
+static void* device_alias(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 // Wait for the library stream by polling an event (lower wake-up latency than a blocking wait for the
 // short products of the host-buffer entry points).
 static void wait_stream(cudaStream_t st) {
@@ -1832,6 +1877,18 @@ static void host_product(edgpu_op_s* op, int prec, int dir, const double* x, dou
 
 static void host_product_issue(edgpu_op_s* op, int prec, int dir, const double* x, double* y, int64_t n,
                                int accumulate, bool conj_io, cudaStream_t st) {
+    if (prec == EDGPU_MIXED && !conj_io) {
+        // pinned buffers the device can address: the complex64 conversion kernels read x from and
+        // write y to host memory directly (no staging copies)
+        const double* xd = (const double*)device_alias(x);
+        double* yd = (double*)device_alias(y);
+        if (xd && yd) {
+            launch_c128_to_c64(n, xd, op->x32.p, st);
+            launch_product(op, prec, dir, 0, op->x32.p, op->y32.p, 0, nullptr, nullptr, st);
+            launch_c64_to_c128(n, op->y32.p, yd, accumulate, st);
+            return;
+        }
+    }
     EDGPU_CUDA(cudaMemcpyAsync(op->x64.p, x, n * 16, cudaMemcpyHostToDevice, st));
     if (conj_io) launch_conj_c128(n, op->x64.p, st);
     if (accumulate) {

@@ -71,6 +71,8 @@ SIGNATURES = {
     "edgpu_op_autotune": (ctypes.c_int, [vp, i32, P(i32), P(dbl)]),
     "edgpu_op_set_pair_schedule": (ctypes.c_int, [vp, i32]),
     "edgpu_op_pair_classes": (ctypes.c_int, [vp, P(i32), P(i32)]),
+    "edgpu_pair_classes_of_terms": (ctypes.c_int, [i32, i32, P(u64), P(u64), P(u64), P(dbl), i32, P(i32), P(i32),
+                                                   P(u64), P(u64), P(dbl)]),
     "edgpu_op_get_schedule": (ctypes.c_int, [vp, i32, P(i32), P(i32), P(i32)]),
     "edgpu_op_build_targets": (ctypes.c_int, [vp, i64, P(i32)]),
     "edgpu_op_free_targets": (ctypes.c_int, [vp]),

@@ -166,6 +166,15 @@ int edgpu_op_set_pair_schedule(edgpu_op op, int32_t enable);
 /* Bond classes of the pair-flip schedule for this operator (0 when the terms do not allow it) and
  * their rotation components in total. */
 int edgpu_op_pair_classes(edgpu_op op, int32_t* n_classes, int32_t* n_components);
+/* Host-only inspection of the pair-flip schedule's bond classes for a term table over n_bits sites
+ * of one bit each (no device work; no reference counterpart).  *n_classes = 0 when some off-diagonal
+ * term is not a two-site flip.  When cap_classes >= *n_classes, the nullable outputs receive, per
+ * class: info (components | has_parallel << 8), comps [BOND_MAXC = 4][3] (shift s, starts of pairs
+ * with antiparallel terms, starts with parallel terms), flips [n_bits] (flip mask of the pair starting
+ * at each bit, 0 if none) and class_amps [n_bits][4][2] (amplitude by b_i | (b_i == b_j) << 1). */
+int edgpu_pair_classes_of_terms(int32_t n_bits, int32_t n_terms, const uint64_t* masks, const uint64_t* rows,
+                                const uint64_t* cols, const double* amps, int32_t cap_classes, int32_t* n_classes,
+                                int32_t* info, uint64_t* comps, uint64_t* flips, double* class_amps);
 /* The schedule the product uses for this precision: rows_per_tile as in edgpu_op_set_tiling (0 =
  * default), pair_flips = 0 when every row tests every term, else the targets each lane looks up per
  * step in the pair-flip schedule (2; 4 with a parent-state map or a target table; 8 with a table), and
