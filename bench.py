@@ -733,7 +733,7 @@ def main():
                          "size the map is rank-indexed")
     ap.add_argument("--tiling", type=int, default=0,
                     help="fixed schedule instead of the autotuner: -1/-2/-4 lanes per row (single-sector workloads)")
-    ap.add_argument("--pair-targets", type=int, default=2, choices=[0, 2, 4],
+    ap.add_argument("--pair-targets", type=int, default=2, choices=[0, 2, 4, 8],
                     help="with --tiling: targets per lane and step of the pair-flip schedule (0: term scan)")
     ap.add_argument("--no-table", action="store_true", help="no target tables (look every target up per product)")
     ap.add_argument("--no-pair", action="store_true", help="test every term per row instead of the pair-flip schedule")
