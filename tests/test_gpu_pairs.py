@@ -448,3 +448,53 @@ def test_target_table_batch(edgpu):
             assert (torch.linalg.vector_norm(y - r) / torch.linalg.vector_norm(r)).item() < tol
         for o in oprs:
             o.free_targets()
+
+
+def hermitian_checks(E, opr, N, prec_tol=1e-12):
+    """<u|H v> = conj(<v|H u>), linearity and determinism of the FP64 product on seeded vectors."""
+    import torch
+    u = E.random_state(N, 1, "fp64")
+    v = E.random_state(N, 2, "fp64")
+    Hu, Hv = torch.empty_like(u), torch.empty_like(v)
+    E.mul_(Hu, opr, u)
+    E.mul_(Hv, opr, v)
+    lhs = torch.vdot(u, Hv).item()
+    rhs = torch.vdot(v, Hu).item().conjugate()
+    assert abs(lhs - rhs) < prec_tol * max(1.0, abs(lhs))
+    w = (0.3 - 0.2j) * u + 1.7 * v
+    Hw = torch.empty_like(w)
+    E.mul_(Hw, opr, w)
+    ref = (0.3 - 0.2j) * Hu + 1.7 * Hv
+    assert (torch.linalg.vector_norm(Hw - ref) / torch.linalg.vector_norm(Hw)).item() < prec_tol
+    Hu2 = torch.empty_like(u)
+    E.mul_(Hu2, opr, u)
+    assert torch.equal(Hu, Hu2)
+    return u, Hu
+
+
+@pytest.mark.parametrize("workload", ["triangular6x5_k1", "chain28_k0"])
+def test_full_size_target_table(edgpu, workload):
+    """At the benchmark sizes (5,170,578 and 1,432,860 rows): the product through the target table is
+    Hermitian, linear and deterministic in FP64, equals the looked-up product bit for bit, and the
+    mixed product agrees with FP64 to single precision."""
+    import torch
+    import bench
+    wl = bench.WORKLOADS[workload]
+    space, opr, _ = bench.build_gpu_operator(wl)
+    assert space.build_map(8 << 30)
+    N = space.dimension
+    opr.set_tiling("fp64", -1)
+    opr.set_tiling("mixed", -1)
+    u, Hu_map = hermitian_checks(edgpu, opr, N)
+    assert opr.build_targets(8 << 30)
+    n, _ = opr.targets_info
+    assert n == opr.count_nnz()[0]
+    assert opr.uses_target_table("fp64")
+    _, Hu_tab = hermitian_checks(edgpu, opr, N)
+    assert torch.equal(Hu_tab, Hu_map)
+    u32, H32 = u.to(torch.complex64), torch.empty(N, dtype=torch.complex64, device="cuda")
+    edgpu.mul_(H32, opr, u32, precision="mixed")
+    assert (torch.linalg.vector_norm(H32.to(torch.complex128) - Hu_tab) /
+            torch.linalg.vector_norm(Hu_tab)).item() < 1e-6
+    opr.free_targets()
+    space.free_map()
