@@ -690,9 +690,13 @@ void set_map_params(HxParams& p, const Space& sp) {
     p.rank_split = sp.rank_split;
 }
 
+// y_c128 (mixed precision, product mode): when the launch goes through the pair-flip kernel, it writes
+// y as complex128 to y_c128 (adding the old value there when acc_c128) instead of complex64 to y, and
+// *wrote_c128 is set; otherwise y is written as usual.
 void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, void* y, int accumulate,
                     const void* gy, double* grad_partial, cudaStream_t st, int* blocks_used = nullptr,
-                    int rows_override = 0) {
+                    int rows_override = 0, void* y_c128 = nullptr, int acc_c128 = 0, bool* wrote_c128 = nullptr) {
+    if (wrote_c128) *wrote_c128 = false;
     build_blob(op, prec, dir, mode);
     Blob& B = op->blob[prec][dir][mode];
     HxParams p = B.tmpl;
@@ -727,6 +731,11 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
             // blob's prefix up to the bond tables
             const bool table = op->d_tab && op->tab_use[prec];
             const size_t smem = (mapped || table) ? B.smem_bond : B.smem_bond_canon;
+            if (y_c128 && prec == EDGPU_MIXED) {
+                p.y_c128 = y_c128;
+                p.accumulate = acc_c128;
+                if (wrote_c128) *wrote_c128 = true;
+            }
             p.blob = B.d_pair;
             p.o_rlut = B.tmpl_pair.o_rlut;
             p.o_bcomp = B.tmpl_pair.o_bcomp;
@@ -1884,8 +1893,11 @@ static void host_product_issue(edgpu_op_s* op, int prec, int dir, const double* 
         double* yd = (double*)device_alias(y);
         if (xd && yd) {
             launch_c128_to_c64(n, xd, op->x32.p, st);
-            launch_product(op, prec, dir, 0, op->x32.p, op->y32.p, 0, nullptr, nullptr, st);
-            launch_c64_to_c128(n, op->y32.p, yd, accumulate, st);
+            // the pair-flip kernel writes the complex128 result to the host buffer itself
+            bool fused = false;
+            launch_product(op, prec, dir, 0, op->x32.p, op->y32.p, 0, nullptr, nullptr, st, nullptr, 0, yd,
+                           accumulate, &fused);
+            if (!fused) launch_c64_to_c128(n, op->y32.p, yd, accumulate, st);
             return;
         }
     }

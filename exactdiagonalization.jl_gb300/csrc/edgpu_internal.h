@@ -216,6 +216,7 @@ struct HxParams {
     const void* tab;
     const long long* tile_off;
     int tab_wide, tab_cb;
+    void* y_c128;                             // mixed precision: write y as complex128 here instead (or null)
 };
 
 // One sector of a batched launch (hx_multi_kernel), kept in shared memory after the common tables.

@@ -268,8 +268,21 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
     // partial sums of the row's lanes (fixed butterfly order)
     for (int d = 1; d < lpr; d <<= 1) acc = cadd(acc, shfl_xor_v(acc, d));
     if (act && sub == 0) {
-        if (p.accumulate) acc = cadd(acc, sc.y[row]);
-        sc.y[row] = acc;
+        if (PREC == 1 && p.y_c128) {
+            // complex128 output (the host-buffer product, written to the caller's buffer): the
+            // complex64 result widened, plus the old value for apply!, as the separate conversion does
+            double2* y2 = (double2*)p.y_c128;
+            double2 o = make_double2((double)acc.x, (double)acc.y);
+            if (p.accumulate) {
+                const double2 a = y2[row];
+                o.x += a.x;
+                o.y += a.y;
+            }
+            y2[row] = o;
+        } else {
+            if (p.accumulate) acc = cadd(acc, sc.y[row]);
+            sc.y[row] = acc;
+        }
     }
 }
 
