@@ -148,3 +148,22 @@ def test_terms_outside_the_schedule():
     assert classes_of(n, O.heisenberg_terms(n, lattice.chain_bonds(n), [1.0] * n, [1.0] * n) + field) == []
     half = O.op_mul(O.pauli_matrix(offs, 0, "+"), O.pauli_matrix(offs, 1, "-"))   # no Hermitian partner
     assert classes_of(n, half) == []
+
+
+def test_argument_errors():
+    L = _lib.lib()
+    nc = ctypes.c_int32()
+    z = np.zeros(1, np.uint64)
+    a = np.zeros(2, np.float64)
+    for n_bits in (0, 65):
+        assert L.edgpu_pair_classes_of_terms(n_bits, 0, None, None, None, None, 0, ctypes.byref(nc),
+                                             None, None, None, None) == _lib.ERR_ARG
+    assert L.edgpu_pair_classes_of_terms(8, 1, None, None, None, None, 0, ctypes.byref(nc),
+                                         None, None, None, None) == _lib.ERR_ARG
+    assert L.edgpu_pair_classes_of_terms(8, 1, ptr(z, ctypes.c_uint64), ptr(z, ctypes.c_uint64),
+                                         ptr(z, ctypes.c_uint64), ptr(a, ctypes.c_double), 0, None,
+                                         None, None, None, None) == _lib.ERR_ARG
+    # no terms at all: no classes
+    assert L.edgpu_pair_classes_of_terms(8, 0, None, None, None, None, 0, ctypes.byref(nc),
+                                         None, None, None, None) == 0
+    assert nc.value == 0
