@@ -36,6 +36,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG_DIR = os.path.join(ROOT, "exactdiagonalization.jl_gb300")
 for p in (PKG_DIR, ROOT):
@@ -48,26 +50,31 @@ FALLBACK_HBM_GBS = 6800.0
 
 WORKLOADS = {
     "chain24_k0": dict(kind="chain", L=24, k=0, jxy=1.0, jz=1.0, seed=2, lanczos_steps=200, reorth=True,
+                       N_r=112720, nnz_off=1411488, steps=2000,
                        desc="spin-1/2 Heisenberg chain L=24 PBC J=1, 2Sz=0, momentum 0 (24-site translations)"),
     "chain16_full": dict(kind="chain_full", L=16, jxy=1.0, jz=1.0, seed=1, lanczos_steps=100, reorth=True,
+                         N_r=12870, nnz_off=109824, steps=2000,
                          desc="spin-1/2 Heisenberg chain L=16 PBC J=1, 2Sz=0, no symmetry reduction"),
-    "chain28_grad": dict(kind="chain_grad", L=28, k=0, seed=4, x_seed=5, gy_seed=6, cpu_feasible=False,
+    "chain28_grad": dict(kind="chain_grad", L=28, k=0, seed=4, x_seed=5, gy_seed=6, cpu_feasible=True,
+                         N_r=1432860, nnz_off=None, steps=200,
                          desc="spin-1/2 Heisenberg chain L=28 PBC, per-bond J_b = 0.5 + U[0,1) (seed 4), 2Sz=0, "
                               "momentum 0: forward H x, coupling gradient dL/dJ_b = Re<gy|H_b x>, adjoint H^dagger gy"),
     "chain28_k0": dict(kind="chain", L=28, k=0, jxy=1.0, jz=1.0, seed=5, lanczos_steps=200, reorth=True,
+                       N_r=1432860, nnz_off=None, steps=500,
                        desc="spin-1/2 Heisenberg chain L=28 PBC, 2Sz=0, momentum 0"),
     "triangular6x5_allk": dict(kind="torus_allk", shape=(6, 5), nn=[(1, 0), (1, 1), (0, 1)],
                                nnn=[(2, 1), (1, 2), (-1, 1)], j1=1.0, j2=0.125, aniso=0.8, seed=3,
-                               cpu_feasible=False,
+                               cpu_feasible=False, N_r=155117520, nnz_off=None, steps=20,
                                desc="spin-1/2 XXZ J1-J2 triangular 6x5 torus (Jz/Jxy=0.8, J2/J1=0.125), 2Sz=0, "
                                     "all 30 momentum sectors in one batched persistent launch"),
     "triangular6x5_k1": dict(kind="torus", shape=(6, 5), k=(1, 0), nn=[(1, 0), (1, 1), (0, 1)],
                              nnn=[(2, 1), (1, 2), (-1, 1)], j1=1.0, j2=0.125, aniso=0.8, seed=3, lanczos_steps=200,
-                             reorth=True, cpu_feasible=False,
+                             reorth=True, cpu_feasible=False, N_r=5170578, nnz_off=None, steps=200,
                              desc="spin-1/2 XXZ J1-J2 triangular 6x5 torus (Jz/Jxy=0.8, J2/J1=0.125), 2Sz=0, "
                                   "momentum (1,0) (one sector of the batched workload)"),
     "square6x6_k0": dict(kind="torus", shape=(6, 6), k=(0, 0), nn=[(1, 0), (0, 1)], nnn=[(1, 1), (1, -1)],
                          j1=1.0, j2=0.5, aniso=1.0, seed=7, lanczos_steps=300, reorth=False, cpu_feasible=False,
+                         N_r=252091362, nnz_off=18669175824, steps=20,
                          desc="spin-1/2 J1-J2 Heisenberg 6x6 torus (J2/J1=0.5), 2Sz=0, momentum (0,0)"),
 }
 
@@ -285,51 +292,109 @@ def barrier():
 
 
 # ---------------------------------------------------------------------------------------------------
-def cpu_reference(wl, steps, warmup, budget_s=None, rows_per_step=None):
-    """The reference's mul! restated on the CPU (oracle, FP64, all host threads), on row blocks."""
-    import numpy as np
+def workload_config(wl, name):
+    """The workload's constants, identical in both arms: sizes, exact off-diagonal nonzero count, the
+    byte model of one mixed-precision H*x, and how the timing keeps x out of L2."""
+    N, nnz = wl["N_r"], wl["nnz_off"]
+    x_mb = N * 8 / 1e6
+    if x_mb > 2 * L2_BYTES / 1e6:
+        l2 = f"x alone ({x_mb:.0f} MB complex64) exceeds twice the 129 MB L2"
+    else:
+        l2 = "inputs cycled from a pool of x/y vectors larger than twice the 129 MB L2"
+    return {"workload": name, "description": wl["desc"], "N_r": N, "nnz_off": nnz,
+            "bytes_per_step": bytes_model(N, nnz, 8), "bytes_model": "N_r*(8+8+2*8) + nnz_off*(8+8)",
+            "step": "one H*x over the whole sector", "l2": l2}
+
+
+def _tables_restatement(wl):
+    """The reference's own data structures on the host (parent basis, parent-sized mapping tables),
+    for the workloads where they fit: (space, terms, N)."""
     from oracle import oracle as O
     n, bonds, jxy, jz, shape, k = hamiltonian_spec(wl)
-    sites = O.spin_half_sites(n)
     parent = O.popcount_basis(n, n // 2)
     terms = O.heisenberg_terms(n, bonds, jxy, jz)
     if wl["kind"] == "chain_full":
-        space = parent
-        N = parent.size
-    else:
-        bw, off = O.bit_layout(sites)
-        maps, amps = O.translation_symops(shape, k)
-        space = O.symmetry_reduce(parent, bw, off, maps, amps)
-        N = space.dim
+        return parent, terms, parent.size
+    sites = O.spin_half_sites(n)
+    bw, off = O.bit_layout(sites)
+    maps, amps = O.translation_symops(shape, k)
+    red = O.symmetry_reduce(parent, bw, off, maps, amps)
+    return red, terms, red.dim
+
+
+def cpu_tables(wl, steps, warmup, budget_s=None):
+    """The reference's mul! restated on the host with its own data structures (binary search over the
+    parent basis, parent-sized mapping tables, rows split statically over all host threads as
+    apply_parallel! does), FP64.  A step is one whole H*x."""
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    space, terms, N = _tables_restatement(wl)
+    setup = time.perf_counter() - t0
     x = O.complex_gaussian(N, wl["seed"])
-    sampler = O.RowSampler(space, terms, x)
-    rows = rows_per_step or min(N, 8192)
-    blocks = [(r0, min(N, r0 + rows)) for r0 in range(0, N, rows)]
-    nnz = {}
-    pos = 0
+    y = np.zeros(N, dtype=np.complex128)
     for _ in range(warmup):
-        r0, r1 = blocks[pos % len(blocks)]
-        nnz[(r0, r1)] = sampler.run(r0, r1, count=True)
-        pos += 1
-    total_b, total_t, done = 0, 0.0, 0
+        O.apply_rows(space, terms, x, out=y)
+    done, tot = 0, 0.0
     while True:
-        r0, r1 = blocks[pos % len(blocks)]
-        if (r0, r1) not in nnz:
-            nnz[(r0, r1)] = sampler.run(r0, r1, count=True)
         t0 = time.perf_counter()
-        sampler.run(r0, r1)
-        total_t += time.perf_counter() - t0
-        total_b += bytes_model(r1 - r0, nnz[(r0, r1)], 16)
-        pos += 1
+        O.apply_rows(space, terms, x, out=y)
+        tot += time.perf_counter() - t0
         done += 1
         if steps is not None and done >= steps:
             break
-        if budget_s is not None and total_t >= budget_s:
+        if budget_s is not None and tot >= budget_s:
             break
-    return {"value": total_b / total_t / 1e9, "unit": "GB/s", "cores": O.num_threads(), "kind": "port",
-            "sample": (f"{done} blocks of {rows} rows of the {N}-row H*x (FP64, oracle restatement of the reference's "
-                       f"apply_parallel!), {total_t:.2f} s of CPU time"),
-            "ms_per_step": 1e3 * total_t / done, "steps": done}
+    ms = 1e3 * tot / done
+    return {"ms_per_step": ms, "steps": done, "cores": O.num_threads(), "kind": "port", "setup_s": setup,
+            "sample": f"{done} whole H*x of the {N}-row sector (FP64, the reference's parent-sized tables), "
+                      f"{tot:.2f} s of CPU time"}
+
+
+def cpu_orbit_rows(wl, steps, warmup, budget_s=None, rows_per_step=4096):
+    """The reference's row formula on the host for sectors whose parent-sized tables do not fit in host
+    memory (the 6x6 torus: ~290 GB): the representatives are enumerated on the host (orbit minima with
+    trivial stabiliser character, the set the reference's sweep keeps), and the mapping entries each
+    row needs are evaluated orbit by orbit (oracle.OrbitTables), FP64, all host threads.  A step is a
+    block of rows_per_step random rows; its time is extrapolated to one whole H*x."""
+    from oracle import oracle as O
+    n, bonds, jxy, jz, shape, k = hamiltonian_spec(wl)
+    t0 = time.perf_counter()
+    basis = O.torus_representatives(shape, n // 2, k)
+    maps, amps = O.translation_symops(shape, k)
+    ot = O.OrbitTables(n, n // 2, maps, amps, basis)
+    terms = O.heisenberg_terms(n, bonds, jxy, jz)
+    N = basis.size
+    x = O.complex_gaussian(N, wl["seed"])
+    setup = time.perf_counter() - t0
+    rng = np.random.default_rng(wl["seed"])
+    for _ in range(warmup):
+        ot.rows(terms, x, rng.integers(0, N, rows_per_step))
+    done, tot = 0, 0.0
+    while True:
+        sample = rng.integers(0, N, rows_per_step)
+        t0 = time.perf_counter()
+        ot.rows(terms, x, sample)
+        tot += time.perf_counter() - t0
+        done += 1
+        if steps is not None and done >= steps:
+            break
+        if budget_s is not None and tot >= budget_s:
+            break
+    per_row = tot / (done * rows_per_step)
+    return {"ms_per_step": 1e3 * per_row * N, "steps": done, "cores": O.num_threads(), "kind": "port",
+            "setup_s": setup, "N_r_host": int(N),
+            "sample": f"{done} blocks of {rows_per_step} random rows of the {N}-row sector (FP64; representatives "
+                      f"enumerated on the host, mapping entries evaluated orbit by orbit because the reference's "
+                      f"parent-sized tables (~{24 * math.comb(n, n // 2) / 1e9:.0f} GB) exceed host memory), "
+                      f"{tot:.2f} s of CPU time, extrapolated to one whole H*x"}
+
+
+def cpu_reference(wl, steps, warmup, budget_s=None):
+    """The CPU arm for a workload: the table-based restatement where the reference's tables fit, else
+    the orbit-by-orbit restatement of the same row formula on sampled rows."""
+    if wl.get("cpu_feasible", True):
+        return cpu_tables(wl, steps, warmup, budget_s)
+    return cpu_orbit_rows(wl, steps, warmup, budget_s)
 
 
 def tridiagonal_e0_change(r, k):
@@ -346,21 +411,38 @@ def tridiagonal_e0_change(r, k):
 
 
 def run_reference(args, wl):
-    world, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    """The reference arm: the reference's mul! restated on the host cores, on the same workload, metric
+    and config as the GPU arm.  value = the workload's bytes_per_step over the time of one whole H*x
+    (so the ratio of the two arms' values is the ratio of their H*x times)."""
+    world, rank = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    if not wl.get("cpu_feasible", True):
-        print(json.dumps({"impl": "reference", "metric": METRIC, "value": None, "unit": "GB/s",
-                          "config": {"workload": args.workload},
-                          "note": "the reference's parent-sized tables for this sector (~290 GB) exceed host memory"}))
-        return
-    r = cpu_reference(wl, args.steps, args.warmup)
-    line = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": "GB/s", "n_gpus": args.gpus,
+    cfg = workload_config(wl, args.workload)
+    if wl["kind"] == "torus_allk":
+        # the batched workload: the per-sector restatement on one momentum sector of it, scaled by the
+        # sector count (all sectors have the same size to within 29 rows)
+        one = dict(WORKLOADS["triangular6x5_k1"])
+        r = cpu_orbit_rows(one, args.steps, args.warmup)
+        r["ms_per_step"] *= 30
+        r["sample"] += "; one sector (k=(1,0)) of the 30, time multiplied by 30"
+    else:
+        r = cpu_reference(wl, args.steps, args.warmup)
+    value = cfg["bytes_per_step"] / (r["ms_per_step"] / 1e3) / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": args.workload, "description": wl["desc"], "parallelism": "host threads"},
-            "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
-            "e2e": {"value": r["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": value, "unit": "GB/s", "cores": r["cores"], "kind": r["kind"],
+                             "sample": r["sample"]},
+            "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "setup_s": r["setup_s"]}
+    if not wl.get("cpu_feasible", True) and not args.no_cpu_baseline:
+        # the reference's own data structures on the largest configuration where they fit in seconds
+        t = cpu_tables(WORKLOADS["chain24_k0"], None, 1, budget_s=args.cpu_seconds)
+        c24 = workload_config(WORKLOADS["chain24_k0"], "chain24_k0")
+        t["value"] = c24["bytes_per_step"] / (t["ms_per_step"] / 1e3) / 1e9
+        t["unit"] = "GB/s"
+        t["config"] = c24
+        line["cpu_reference_tables_chain24_k0"] = t
     print(json.dumps(line), flush=True)
 
 
@@ -375,6 +457,9 @@ def run_gpu(args, wl):
     space, opr, t_space = build_gpu_operator(wl)
     N = space.dimension
     n_targets, nnz = opr.count_nnz()
+    if N != wl["N_r"] or (wl["nnz_off"] is not None and nnz != wl["nnz_off"]):
+        raise RuntimeError(f"sector size {N} / nonzeros {nnz} differ from the workload's {wl['N_r']} / {wl['nnz_off']}")
+    cfg = workload_config(dict(wl, nnz_off=nnz), args.workload)
     dir_stats = edgpu.search_stats(space)
     map_info = build_maps([space], args)
     table_info = build_tables([opr], [space], args)
@@ -382,7 +467,7 @@ def run_gpu(args, wl):
         opr.set_pair_schedule(False)
     if args.tiling:
         # a fixed schedule instead of the autotuner (reproducible profiles)
-        opr.set_pair_schedule(args.pair_targets > 0, max(args.pair_targets, 2))
+        opr.set_pair_schedule(args.pair_targets > 0, max(args.pair_targets, 2), args.uniform)
         for prec in ("mixed", "fp64"):
             opr.set_tiling(prec, args.tiling)
         tune_mixed = tune_fp64 = (args.tiling, None)
@@ -448,21 +533,54 @@ def run_gpu(args, wl):
     b64 = bytes_model(N, nnz, 16)
     value64 = b64 / (ms64 / fp64_steps / 1e3) / 1e9
 
-    # end to end through the C ABI with pinned host complex128 buffers (the reference's mul! interface)
+    # end to end through the C ABI with host complex128 buffers (the reference's mul! interface on
+    # Vector{ComplexF64}): pinned buffers (graph-replayed, kernels address the host buffers), and the
+    # ordinary pageable buffers a Julia ccall passes (copies through the library's device buffers)
     x_h = torch.empty(N, dtype=torch.complex128, pin_memory=True)
     y_h = torch.empty(N, dtype=torch.complex128, pin_memory=True)
     x_h.copy_(edgpu.random_state(N, wl["seed"], "fp64").cpu())
     xn, yn = x_h.numpy(), y_h.numpy()
     e2e_steps = max(3, min(args.steps, 500))
-    for _ in range(3):
-        edgpu.mul_(yn, opr, xn, precision="mixed")
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        edgpu.mul_(yn, opr, xn, precision="mixed")
-    t_e2e = (time.perf_counter() - t0) / e2e_steps
+
+    def host_timed(xa, ya, prec, k):
+        for _ in range(2):
+            edgpu.mul_(ya, opr, xa, precision=prec)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            edgpu.mul_(ya, opr, xa, precision=prec)
+        return (time.perf_counter() - t0) / k
+
+    t_e2e = host_timed(xn, yn, "mixed", e2e_steps)
     e2e = {"value": b_mixed / t_e2e / 1e9, "unit": "GB/s", "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N,
-           "ms_per_step": t_e2e * 1e3}
+           "ms_per_step": t_e2e * 1e3, "buffers": "pinned complex128", "product": "mixed"}
+    t_e2e64 = host_timed(xn, yn, "fp64", max(3, e2e_steps // 4))
+    xp, yp = np.array(xn), np.empty_like(xn)          # pageable copies
+    t_pg = host_timed(xp, yp, "mixed", max(3, e2e_steps // 4))
+    del xp, yp
+    # the host link itself: plain pinned copies of the same bytes each way (cudaMemcpyAsync)
+    dbuf = torch.empty(N, dtype=torch.complex128, device="cuda")
+    for _ in range(2):
+        dbuf.copy_(x_h, non_blocking=True)
+    torch.cuda.synchronize()
+    e0_, e1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0_.record()
+    for _ in range(3):
+        dbuf.copy_(x_h, non_blocking=True)
+    e1_.record()
+    torch.cuda.synchronize()
+    h2d = 3 * 16 * N / (e0_.elapsed_time(e1_) / 1e3) / 1e9
+    e0_.record()
+    for _ in range(3):
+        y_h.copy_(dbuf, non_blocking=True)
+    e1_.record()
+    torch.cuda.synchronize()
+    d2h = 3 * 16 * N / (e0_.elapsed_time(e1_) / 1e3) / 1e9
+    del dbuf
+    host_link = {"h2d_gbs": h2d, "d2h_gbs": d2h, "bytes_each_way": 16 * N,
+                 "copy_only_ms": 16 * N / h2d / 1e6 + 16 * N / d2h / 1e6}
+    e2e_more = {"fp64_pinned": {"value": b_mixed / t_e2e64 / 1e9, "ms_per_step": t_e2e64 * 1e3},
+                "mixed_pageable": {"value": b_mixed / t_pg / 1e9, "ms_per_step": t_pg * 1e3}}
 
     # time to E0 (Lanczos): FP64 product vs mixed product polished in FP64
     e0_info = None
@@ -499,21 +617,19 @@ def run_gpu(args, wl):
         edgpu.set_krylov_limit(0)
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline and not wl.get("cpu_feasible", True):
-        cpu = {"value": None, "unit": "GB/s", "cores": None, "kind": "port",
-               "sample": "not run: the reference's parent-sized tables for this sector exceed host memory"}
-    elif rank == 0 and world == 1 and not args.no_cpu_baseline:
-        r = cpu_reference(wl, None, 2, budget_s=args.cpu_seconds)
-        cpu = {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        r = cpu_reference(wl, None, 1, budget_s=args.cpu_seconds)
+        cpu = {"value": cfg["bytes_per_step"] / (r["ms_per_step"] / 1e3) / 1e9, "unit": "GB/s", "cores": r["cores"],
+               "kind": r["kind"], "sample": r["sample"], "ms_per_step": r["ms_per_step"]}
 
     peak, peak_src = measured_peak()
     traffic = profiled_traffic(args.workload)
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-            "config": {"workload": args.workload, "description": wl["desc"], "N_r": N, "n_targets": n_targets,
-                       "nnz_off": nnz, "bytes_per_step": b_mixed, "l2": f"inputs cycled from a pool of {P_mixed} x/y "
-                       f"pairs ({2 * P_mixed * N * s_c / 1e6:.0f} MB > 2x L2)", "parallelism": f"replicas x{world}",
+            "config": cfg,
+            "gpu_setup": {"n_targets": n_targets, "pool": f"{P_mixed} x/y pairs ({2 * P_mixed * N * s_c / 1e6:.0f} MB)",
+                       "parallelism": f"replicas x{world}",
                        "rows_per_tile": {"mixed": tune_mixed[0], "fp64": tune_fp64[0]},
                        "pair_flip_schedule": {"mixed": opr.schedule("mixed")[1], "fp64": opr.schedule("fp64")[1],
                                               "bond_classes": opr.pair_classes()[0]},
@@ -523,7 +639,8 @@ def run_gpu(args, wl):
                        "setup_s": t_space, "search_directory": dir_stats, "parent_map": map_info},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_src},
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps, "clocks": clk,
+            "cpu_baseline": cpu, "e2e": e2e, "e2e_more": e2e_more, "host_link": host_link,
+            "gpu_launches": args.steps, "clocks": clk,
             "fp64": {"value": value64, "unit": "GB/s", "ms_per_step": ms64 / fp64_steps, "frac": value64 / peak},
             "e0": e0_info}
     if rank == 0:
@@ -544,6 +661,9 @@ def run_gpu_batch(args, wl):
     dims = [sp.dimension for sp in spaces]
     N = sum(dims)
     nnz = sum(o.count_nnz()[1] for o in oprs)
+    if N != wl["N_r"] or (wl["nnz_off"] is not None and nnz != wl["nnz_off"]):
+        raise RuntimeError(f"sector sizes {N} / nonzeros {nnz} differ from the workload's {wl['N_r']} / {wl['nnz_off']}")
+    cfg = workload_config(dict(wl, nnz_off=nnz), args.workload)
     map_info = build_maps(spaces, args)
     table_info = build_tables(oprs, spaces, args)
     if args.no_pair:
@@ -631,8 +751,8 @@ def run_gpu_batch(args, wl):
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-            "config": {"workload": args.workload, "description": wl["desc"], "sectors": len(dims), "N_r_total": N,
-                       "N_r_min": min(dims), "N_r_max": max(dims), "nnz_off": nnz, "bytes_per_step": b_step,
+            "config": cfg,
+            "gpu_setup": {"sectors": len(dims), "N_r_min": min(dims), "N_r_max": max(dims),
                        "lanes_per_row": lpr, "pair_flip_schedule": batch.schedule("mixed")[1],
                        "target_table": dict(table_info or {"built": False}, used=batch.uses_target_tables("mixed")),
                        "bond_classes": oprs[0].pair_classes()[0], "l2": f"inputs cycled from {P} sets of x/y ({2 * P * N * s_c / 1e6:.0f} MB "
@@ -671,6 +791,9 @@ def run_gpu_grad(args, wl):
     opr = edgpu.OperatorRepresentation.from_terms(space, m, r, c, a, coupling_ids=ids, couplings=J)
     N = space.dimension
     n_targets, nnz = opr.count_nnz()
+    if N != wl["N_r"] or (wl["nnz_off"] is not None and nnz != wl["nnz_off"]):
+        raise RuntimeError(f"sector size {N} / nonzeros {nnz} differ from the workload's {wl['N_r']} / {wl['nnz_off']}")
+    cfg = workload_config(dict(wl, nnz_off=nnz), args.workload)
     map_info = build_maps([space], args)
     opr.autotune("mixed")
     stream = torch.cuda.current_stream()
@@ -706,9 +829,9 @@ def run_gpu_grad(args, wl):
     line = {"metric": METRIC, "value": b_all / t_max / 1e9, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-            "config": {"workload": args.workload, "description": wl["desc"], "N_r": N, "nnz_off": nnz,
-                       "invariant_terms": opr.is_invariant, "setup_s": t_space, "parent_map": map_info,
-                       "ms": res, "parallelism": f"replicas x{world}"},
+            "config": cfg,
+            "gpu_setup": {"invariant_terms": opr.is_invariant, "setup_s": t_space, "parent_map": map_info,
+                          "ms": res, "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": b / t_fwd / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": b / t_fwd / 1e9 / peak, "traffic": None, "peak_source": peak_src},
             "cpu_baseline": None, "e2e": None, "gpu_launches": args.steps, "clocks": None}
@@ -722,10 +845,10 @@ def run_gpu_grad(args, wl):
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5000)
-    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (default: the workload's, ~3-60 s)")
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="chain24_k0")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="square6x6_k0")
     ap.add_argument("--no-lanczos", action="store_true")
     ap.add_argument("--no-map", action="store_true", help="canonicalise targets instead of using parent-state maps")
     ap.add_argument("--map-bytes", type=int, default=0,
@@ -735,6 +858,7 @@ def main():
                     help="fixed schedule instead of the autotuner: -1/-2/-4 lanes per row (single-sector workloads)")
     ap.add_argument("--pair-targets", type=int, default=2, choices=[0, 2, 4, 8],
                     help="with --tiling: targets per lane and step of the pair-flip schedule (0: term scan)")
+    ap.add_argument("--uniform", action="store_true", help="with --tiling: warp-uniform pair steps (4 or 8 targets)")
     ap.add_argument("--no-table", action="store_true", help="no target tables (look every target up per product)")
     ap.add_argument("--no-pair", action="store_true", help="test every term per row instead of the pair-flip schedule")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -743,6 +867,8 @@ def main():
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     wl = WORKLOADS[args.workload]
+    if args.steps is None:
+        args.steps = wl["steps"]
     if args.impl == "reference":
         run_reference(args, wl)
     elif wl["kind"] == "torus_allk":

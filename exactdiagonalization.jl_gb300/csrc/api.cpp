@@ -10,6 +10,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <thread>
 #include <numeric>
 #include <string>
 #include <unordered_map>
@@ -41,7 +42,7 @@ void require(bool cond, int code, const std::string& msg) {
 }
 
 std::mutex g_init_mu;
-cudaStream_t g_stream = nullptr;
+cudaStream_t g_stream = nullptr;   // stream of the calls that belong to no handle
 int g_sm_count = 0;
 
 void init_device() {
@@ -59,6 +60,32 @@ void init_device() {
 
 // NULL selects the CUDA default stream, like the stream argument of CUDA's own libraries.
 cudaStream_t pick_stream(void* s) { return (cudaStream_t)s; }
+
+// What every handle (space, operator, batch) owns for concurrency: the mutex that serialises calls on
+// the handle, and its own non-blocking stream (created on first use) for the work of calls that take
+// no stream argument (builds, host-buffer products, the autotuner, Lanczos).  Distinct handles run
+// concurrently from different host threads, each on its own stream.
+template <typename M>
+struct HandleSyncT {
+    M mu;
+    cudaStream_t st = nullptr;
+    cudaStream_t stream() {
+        if (!st) EDGPU_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        return st;
+    }
+    HandleSyncT() = default;
+    HandleSyncT(const HandleSyncT&) = delete;
+    HandleSyncT& operator=(const HandleSyncT&) = delete;
+    ~HandleSyncT() {
+        if (st) cudaStreamDestroy(st);
+    }
+};
+using HandleSync = HandleSyncT<std::mutex>;
+// Spaces use a recursive mutex: a batch holds the locks of its sectors' spaces while it launches, and
+// an operator's launch takes its space's lock again.
+using SpaceSync = HandleSyncT<std::recursive_mutex>;
+using OpLock = std::lock_guard<std::mutex>;
+using SpaceLock = std::lock_guard<std::recursive_mutex>;
 
 template <typename T>
 struct DevBuf {
@@ -104,10 +131,12 @@ struct Blob {
     int max_blocks = 0;      // resident blocks for the whole GPU
     int rows_per_tile = 32;
     void* d_diag = nullptr;  // per-row diagonal element in the blob's precision (product mode)
+    size_t cap_d = 0, cap_pair = 0, cap_diag = 0;   // bytes allocated at d, d_pair, d_diag
     size_t smem_rows = 0;    // shared memory of the row-per-lane kernel (no per-warp queues)
     int max_blocks_rows = 0;
     int max_blocks_map = 0;  // resident blocks of the parent-state-map kernel (computed on first use)
     int max_blocks_grad = 0; // resident blocks of the row-per-lane gradient kernel (computed on first use)
+    int max_blocks_pgrad[2] = {0, 0};   // of the pair-flip gradient kernel [target table]
     size_t smem_bond = 0;    // shared memory of the mapped pair-flip kernel (the blob's prefix up to the bond tables)
     size_t smem_bond_canon = 0;   // of the canonicalising one (through the torus row table)
     size_t term_start = 0;   // offset of the term records in the term image (before: group and torus tables)
@@ -116,7 +145,7 @@ struct Blob {
     std::vector<unsigned char> pair_host;   // its host copy (batched images start from it)
     HxParams tmpl_pair{};    // launch template of the pair-flip kernel (offsets into d_pair)
     int max_blocks_bond[2][2] = {{0, 0}, {0, 0}};   // resident blocks of the pair-flip kernel [mapped][4 targets]
-    int max_blocks_table[3] = {0, 0, 0};            // of its target-table flavour [2, 4, 8 targets]
+    int max_blocks_table[2][3] = {{0, 0, 0}, {0, 0, 0}};   // of its target-table flavour [warp-uniform][2, 4, 8 targets]
     ~Blob() {
         if (d) cudaFree(d);
         if (d_diag) cudaFree(d_diag);
@@ -126,12 +155,17 @@ struct Blob {
 
 }  // namespace
 
-struct edgpu_space_s : public Space {};
+// A space handle: the space plus its call lock and stream.  Operators on the space take the lock while
+// they enqueue work that reads the space's parent-state map, so the map cannot be freed under them.
+struct edgpu_space_s : public Space {
+    SpaceSync hs;
+};
 
 // Largest Krylov basis (bytes) the Lanczos driver stores; 0: half of the free device memory.
 int64_t g_krylov_limit = 0;
 
 struct edgpu_op_s {
+    HandleSync hs;                    // call lock and stream of this handle
     edgpu_space_s* space = nullptr;
     int T = 0;
     std::vector<uint64_t> masks, rows, cols;
@@ -150,6 +184,7 @@ struct edgpu_op_s {
     DevBuf<double> x64, y64, z64;
     DevBuf<float> x32, y32;
     DevBuf<double> grad_partial, grad_dev;
+    DevBuf<unsigned long long> diag_scratch;   // device copy of the diagonal terms while the diagonal is computed
     std::map<std::vector<const void*>, cudaGraphExec_t> host_graphs;   // replayed host-buffer products
     // target table of the pair-flip schedule (optional, edgpu_op_build_targets)
     void* d_tab = nullptr;
@@ -158,6 +193,13 @@ struct edgpu_op_s {
     int64_t tab_n = 0;
     int tab_use[2] = {1, 1};          // [precision]: products read the table (chosen by the autotuner)
     int tab_pf[2] = {0, 0};           // [precision]: x prefetched this many steps ahead (chosen by the autotuner)
+    int tab_uni[2] = {0, 0};          // [precision]: warp-uniform pair steps (chosen by the autotuner)
+    long long tab_near[2] = {0, 0};   // [precision]: streamed-load threshold in rows (0: off; autotuned)
+    // adjoint target table (optional, edgpu_op_build_adjoint_targets): per column its sorted run of
+    // (row, slot, orbit-size index of the row, group element) entries
+    long long* d_adj_off = nullptr;
+    unsigned long long* d_adj_tab = nullptr;
+    int64_t adj_n = 0;
     void free_table() {
         if (d_tab) cudaFree(d_tab);
         if (d_tile_off) cudaFree(d_tile_off);
@@ -165,9 +207,17 @@ struct edgpu_op_s {
         d_tile_off = nullptr;
         tab_n = 0;
     }
+    void free_adjoint() {
+        if (d_adj_off) cudaFree(d_adj_off);
+        if (d_adj_tab) cudaFree(d_adj_tab);
+        d_adj_off = nullptr;
+        d_adj_tab = nullptr;
+        adj_n = 0;
+    }
     ~edgpu_op_s() {
         for (auto& kv : host_graphs) cudaGraphExecDestroy(kv.second);
         free_table();
+        free_adjoint();
     }
 };
 
@@ -176,6 +226,7 @@ struct edgpu_op_s {
 // character table), and per set of vector pointers and lanes per row a device copy of that image
 // followed by the sector descriptors, plus the CUDA graph replaying the launch.
 struct edgpu_batch_s {
+    HandleSync hs;                                 // call lock and stream of this handle
     std::vector<edgpu_op_s*> ops;
     int lpr[2] = {0, 0};                           // lanes per row (0: default 1)
     int pair_use[2] = {1, 1};                      // pair-flip schedule where the terms allow it (autotuned)
@@ -214,6 +265,16 @@ struct edgpu_batch_s {
 
 namespace edgpu {
 cudaStream_t lib_stream() { return g_stream; }
+
+void raise_smem_limit(const void* kern, size_t smem) {
+    static std::mutex mu;
+    static std::unordered_map<const void*, size_t> set;
+    std::lock_guard<std::mutex> lk(mu);
+    size_t& cur = set[kern];
+    if (smem <= cur) return;
+    EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    cur = smem;
+}
 int sm_count() { return g_sm_count; }
 int hx_max_blocks_per_sm(bool w32, int gk, int prec, int mode, size_t smem);
 }  // namespace edgpu
@@ -234,11 +295,14 @@ struct BondClasses {
     std::vector<uint64_t> comp;       // [ncls][BOND_MAXC][4]: shift, antiparallel starts, parallel starts, 0
     std::vector<uint64_t> flip;       // [ncls][n]
     std::vector<double> amp;          // [ncls][n][4][2]
+    std::vector<int32_t> cid;         // [ncls][n][4] coupling id of each slot's terms (-1: no term)
+    bool cid_ok = true;               // the terms of every slot share one coupling id
     bool real = true;
 };
 
 bool build_bond_classes(const Layout& lay, const std::vector<uint64_t>& masks, const std::vector<uint64_t>& rows,
-                        const std::vector<uint64_t>& flips, const std::vector<double>& amps, BondClasses& out) {
+                        const std::vector<uint64_t>& flips, const std::vector<double>& amps, BondClasses& out,
+                        const std::vector<int32_t>* cids = nullptr) {
     const int n = lay.nbits;
     if (masks.empty() || n < 2 || n > 64) return false;
     for (int i = 0; i < lay.n_sites; ++i)
@@ -247,6 +311,7 @@ bool build_bond_classes(const Layout& lay, const std::vector<uint64_t>& masks, c
         int a, b;                      // bits a < b
         double amp[4][2];              // by (b_a, b_b) pattern: index b_a | b_b << 1
         bool have[4];
+        int cid[4];                    // coupling id of the pattern's terms (-1: none yet)
     };
     std::map<std::pair<int, int>, Pair> pairs;
     for (size_t t = 0; t < masks.size(); ++t) {
@@ -260,12 +325,18 @@ bool build_bond_classes(const Layout& lay, const std::vector<uint64_t>& masks, c
             for (int v = 0; v < 4; ++v) {
                 P.amp[v][0] = P.amp[v][1] = 0.0;
                 P.have[v] = false;
+                P.cid[v] = -1;
             }
         }
         const int pat = (int)((rows[t] >> a) & 1u) | (int)(((rows[t] >> b) & 1u) << 1);
         P.amp[pat][0] += amps[2 * t];
         P.amp[pat][1] += amps[2 * t + 1];
         P.have[pat] = true;
+        if (cids) {
+            const int c = (*cids)[t];
+            if (P.cid[pat] >= 0 && P.cid[pat] != c) out.cid_ok = false;
+            P.cid[pat] = c;
+        }
     }
     std::vector<Pair> list;
     for (auto& kv : pairs) {
@@ -282,6 +353,7 @@ bool build_bond_classes(const Layout& lay, const std::vector<uint64_t>& masks, c
         std::vector<uint64_t> A, P;
         std::vector<int> partner = std::vector<int>(64, -1);
         std::vector<std::array<double, 8>> amp = std::vector<std::array<double, 8>>(64);
+        std::vector<std::array<int, 4>> cid = std::vector<std::array<int, 4>>(64, std::array<int, 4>{-1, -1, -1, -1});
         bool par = false;
     };
     std::vector<Cls> cls;
@@ -325,6 +397,7 @@ bool build_bond_classes(const Layout& lay, const std::vector<uint64_t>& masks, c
             const int pat = (st == P.a) ? (bs | (bp << 1)) : (bp | (bs << 1));
             C.amp[st][2 * v] = P.amp[pat][0];
             C.amp[st][2 * v + 1] = P.amp[pat][1];
+            C.cid[st][v] = P.cid[pat];
             if (P.amp[pat][1] != 0.0) out.real = false;
         }
         if (P.have[1]) C.A[k] |= 1ull << st;
@@ -338,6 +411,7 @@ bool build_bond_classes(const Layout& lay, const std::vector<uint64_t>& masks, c
     out.comp.assign((size_t)out.ncls * BOND_MAXC * 4, 0);
     out.flip.assign((size_t)out.ncls * n, 0);
     out.amp.assign((size_t)out.ncls * n * 8, 0.0);
+    out.cid.assign((size_t)out.ncls * n * 4, -1);
     for (int c = 0; c < out.ncls; ++c) {
         const Cls& C = cls[c];
         out.info[c] = (int32_t)C.shifts.size() | (C.par ? 1 << 8 : 0);
@@ -350,6 +424,7 @@ bool build_bond_classes(const Layout& lay, const std::vector<uint64_t>& masks, c
             if (C.partner[i] < 0) continue;
             out.flip[(size_t)c * n + i] = (1ull << i) | (1ull << C.partner[i]);
             for (int e = 0; e < 8; ++e) out.amp[((size_t)c * n + i) * 8 + e] = C.amp[i][e];
+            for (int v = 0; v < 4; ++v) out.cid[((size_t)c * n + i) * 4 + v] = C.cid[i][v];
         }
     }
     return true;
@@ -421,10 +496,12 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     const bool use_pair = use_rlut && rowbits <= 6;
     const int lut_bits = use_pair ? 2 * rowbits : rowbits;
     p.rlut_pair = use_pair ? 1 : 0;
-    BondClasses bc;
-    if (mode == 0) {
+    BondClasses bc, bcu;   // bond classes with the coupled amplitudes; (gradient mode) with the unit ones
+    bool grad_pair = false;  // gradient mode: the pair-flip gradient kernel applies
+    if (mode == 0 || dir == 0) {
         std::vector<uint64_t> bm, br, bf;
-        std::vector<double> ba;
+        std::vector<double> ba, bu;
+        std::vector<int32_t> bc_id;
         for (int t : offd) {
             const uint64_t r = dir ? op->cols[t] : op->rows[t];
             const uint64_t c = dir ? op->rows[t] : op->cols[t];
@@ -435,13 +512,26 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
             amp_of(t, false, re, im);
             ba.push_back(re);
             ba.push_back(im);
+            amp_of(t, true, re, im);
+            bu.push_back(re);
+            bu.push_back(im);
+            bc_id.push_back(op->cid[t]);
         }
-        if (!build_bond_classes(s.lay, bm, br, bf, ba, bc)) bc = BondClasses();
-        // keep the pair-flip tables small enough for full occupancy
+        if (!build_bond_classes(s.lay, bm, br, bf, ba, bc, &bc_id)) bc = BondClasses();
+        if (mode == 1 && bc.ncls > 0 && bc.cid_ok) {
+            // the unit-coupling amplitudes of the same classes (the structure depends only on the terms'
+            // masks and patterns)
+            grad_pair = build_bond_classes(s.lay, bm, br, bf, bu, bcu) && bcu.ncls == bc.ncls;
+        }
         // keep the pair-flip kernel's shared memory within 48 KB (five or more blocks per SM)
-        const size_t bond_bytes = (size_t)bc.ncls * (BOND_MAXC * 4 * wsz + 16 + s.lay.nbits * (wsz + 4 * vsz));
+        size_t bond_bytes = (size_t)bc.ncls * (BOND_MAXC * 4 * wsz + 16 + s.lay.nbits * (wsz + 4 * vsz));
+        if (grad_pair) bond_bytes += (size_t)bc.ncls * s.lay.nbits * 4 * (vsz + 4) + (size_t)T_d * (2 * wsz + 20);
         const size_t rlut_bytes = use_rlut ? ((size_t)1 << lut_bits) * 4 : 0;
-        if (off + bond_bytes + rlut_bytes > 48 * 1024) bc = BondClasses();
+        if (off + bond_bytes + rlut_bytes > 48 * 1024) {
+            bc = BondClasses();
+            grad_pair = false;
+        }
+        if (mode == 1 && !grad_pair) bc = BondClasses();
     }
     const int n_b = s.lay.nbits;
     p.bond_ncls = bc.ncls;
@@ -450,6 +540,17 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     p.o_binfo = alloc((size_t)bc.ncls * 4);
     p.o_bflip = alloc((size_t)bc.ncls * n_b * wsz);
     p.o_bamp = alloc((size_t)bc.ncls * n_b * 4 * vsz);
+    // gradient mode of the pair-flip kernel: unit amplitudes and coupling ids of the slots, and a copy
+    // of the diagonal term records (mask, row, unit amplitude, coupling id)
+    p.o_bunit = p.o_bcid = p.o_pdm = p.o_pdr = p.o_pdu = p.o_pdc = -1;
+    if (grad_pair) {
+        p.o_bunit = alloc((size_t)bc.ncls * n_b * 4 * vsz);
+        p.o_bcid = alloc((size_t)bc.ncls * n_b * 4 * 4);
+        p.o_pdm = alloc((size_t)T_d * wsz);
+        p.o_pdr = alloc((size_t)T_d * wsz);
+        p.o_pdu = alloc((size_t)T_d * 16);
+        p.o_pdc = alloc((size_t)T_d * 4);
+    }
     // the prefix a mapped pair-flip launch copies ends here; the torus row table follows (needed by
     // canonicalisation only)
     const size_t bond_prefix = align16(off);
@@ -561,6 +662,20 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
         for (size_t i = 0; i < bc.flip.size(); ++i) putw(p.o_bflip, i, bc.flip[i]);
         for (size_t i = 0; i < bc.flip.size() * 4; ++i) putv(p.o_bamp, i, bc.amp[2 * i], bc.amp[2 * i + 1]);
     }
+    if (grad_pair) {
+        for (size_t i = 0; i < bcu.flip.size() * 4; ++i) putv(p.o_bunit, i, bcu.amp[2 * i], bcu.amp[2 * i + 1]);
+        memcpy(&h[p.o_bcid], bc.cid.data(), bc.cid.size() * 4);
+        for (int k = 0; k < T_d; ++k) {
+            const int t = diag[k];
+            const uint64_t r = dir ? op->cols[t] : op->rows[t];
+            putw(p.o_pdm, k, op->masks[t]);
+            putw(p.o_pdr, k, r);
+            double v[2];
+            amp_of(t, true, v[0], v[1]);
+            memcpy(&h[p.o_pdu + k * 16], v, 16);
+            memcpy(&h[p.o_pdc + k * 4], &op->cid[t], 4);
+        }
+    }
 
     // cut the pair-flip image and the term image
     const size_t bstart = (size_t)p.o_bcomp, bshift = bond_prefix - bstart;
@@ -583,23 +698,33 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     require(tot <= 227 * 1024, EDGPU_ERR_ARG,
             "operator tables do not fit in shared memory (" + std::to_string(tot) + " bytes)");
 
-    if (B.d) cudaFree(B.d);
-    B.d = nullptr;
-    if (B.d_diag) cudaFree(B.d_diag);
-    B.d_diag = nullptr;
+    // device buffers are reused when they are large enough (a rebuild after a change of coupling
+    // values has the same layout and allocates nothing)
+    auto ensure = [](void*& d, size_t& cap, size_t bytes) {
+        bytes = std::max<size_t>(bytes, 16);
+        if (d && cap >= bytes) return;
+        if (d) cudaFree(d);
+        d = nullptr;
+        cap = 0;
+        EDGPU_CUDA(cudaMalloc(&d, bytes));
+        cap = bytes;
+    };
     if (!mode) {
-        EDGPU_CUDA(cudaMalloc(&B.d_diag, std::max<int64_t>(s.dim, 1) * vsz));
+        ensure(B.d_diag, B.cap_diag, (size_t)std::max<int64_t>(s.dim, 1) * vsz);
+        op->diag_scratch.ensure((size_t)std::max(T_d, 1) * 4);
         compute_diagonal(s, T_d, dg_mask.data(), dg_row.data(), dg_amp.data(),
                          prec == EDGPU_FP64 ? (double*)B.d_diag : nullptr,
-                         prec == EDGPU_FP64 ? nullptr : (float*)B.d_diag, g_stream);
+                         prec == EDGPU_FP64 ? nullptr : (float*)B.d_diag, op->diag_scratch.p, op->hs.stream());
     }
-    EDGPU_CUDA(cudaMalloc(&B.d, std::max<size_t>(blob_bytes_t, 16)));
+    ensure(B.d, B.cap_d, blob_bytes_t);
     EDGPU_CUDA(cudaMemcpy(B.d, h.data(), blob_bytes_t, cudaMemcpyHostToDevice));
-    if (B.d_pair) cudaFree(B.d_pair);
-    B.d_pair = nullptr;
     if (bc.ncls > 0) {
-        EDGPU_CUDA(cudaMalloc(&B.d_pair, std::max<size_t>(hp.size(), 16)));
+        ensure(B.d_pair, B.cap_pair, hp.size());
         EDGPU_CUDA(cudaMemcpy(B.d_pair, hp.data(), hp.size(), cudaMemcpyHostToDevice));
+    } else if (B.d_pair) {
+        cudaFree(B.d_pair);
+        B.d_pair = nullptr;
+        B.cap_pair = 0;
     }
     B.pair_host = hp;
     p.blob = B.d;
@@ -648,7 +773,8 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     B.term_start = term_start;
     B.bond_end = bond_prefix;
     B.max_blocks_bond[0][0] = B.max_blocks_bond[0][1] = B.max_blocks_bond[1][0] = B.max_blocks_bond[1][1] = 0;
-    B.max_blocks_table[0] = B.max_blocks_table[1] = B.max_blocks_table[2] = 0;
+    for (auto& a : B.max_blocks_table) a[0] = a[1] = a[2] = 0;
+    B.max_blocks_pgrad[0] = B.max_blocks_pgrad[1] = 0;
     const int per_sm = std::max(1, hx_max_blocks_per_sm(w32, gk, prec, mode, tot));
     B.max_blocks = per_sm * std::max(1, g_sm_count);
     if (!mode) {
@@ -671,7 +797,29 @@ void invalidate_blobs(edgpu_op_s* op) {
                 c.d = nullptr;
                 c.d_diag = nullptr;
                 c.d_pair = nullptr;
+                c.cap_d = c.cap_pair = c.cap_diag = 0;
                 c.ready = false;
+            }
+}
+
+// New coupling values: every table built so far is rewritten in place (same layout, same device
+// buffers: nothing is allocated or freed), after the device has finished the work that may still
+// read the old values.  Tables not built yet are built on first use, as before.
+void refresh_blobs(edgpu_op_s* op) {
+    ++op->gen;
+    bool any = false;
+    for (auto& a : op->blob)
+        for (auto& b : a)
+            for (auto& c : b) any = any || c.ready;
+    if (!any) return;
+    EDGPU_CUDA(cudaDeviceSynchronize());
+    for (int prec = 0; prec < 2; ++prec)
+        for (int dir = 0; dir < 2; ++dir)
+            for (int mode = 0; mode < 2; ++mode) {
+                Blob& B = op->blob[prec][dir][mode];
+                if (!B.ready) continue;
+                B.ready = false;
+                build_blob(op, prec, dir, mode);
             }
 }
 
@@ -693,10 +841,15 @@ void set_map_params(HxParams& p, const Space& sp) {
 // y_c128 (mixed precision, product mode): when the launch goes through the pair-flip kernel, it writes
 // y as complex128 to y_c128 (adding the old value there when acc_c128) instead of complex64 to y, and
 // *wrote_c128 is set; otherwise y is written as usual.
+// max_blocks_cap > 0 limits the grid (the gradient's per-block partial sums must fit a caller's buffer).
 void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, void* y, int accumulate,
                     const void* gy, double* grad_partial, cudaStream_t st, int* blocks_used = nullptr,
-                    int rows_override = 0, void* y_c128 = nullptr, int acc_c128 = 0, bool* wrote_c128 = nullptr) {
+                    int rows_override = 0, void* y_c128 = nullptr, int acc_c128 = 0, bool* wrote_c128 = nullptr,
+                    int max_blocks_cap = 0) {
     if (wrote_c128) *wrote_c128 = false;
+    // the space's parent-state map is read below and by the launched kernel: hold the space's lock
+    // while enqueueing so that the map is not freed in between
+    SpaceLock space_lk(op->space->hs.mu);
     build_blob(op, prec, dir, mode);
     Blob& B = op->blob[prec][dir][mode];
     HxParams p = B.tmpl;
@@ -756,8 +909,12 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
                 p.tab_wide = op->tab_wide;
                 p.tab_cb = op->tab_cb;
                 p.bond_pf = op->tab_pf[prec];
-                int& mt = B.max_blocks_table[p.bond_nt == 8 ? 2 : p.bond_nt == 4 ? 1 : 0];
-                if (mt == 0) mt = std::max(1, hx_table_occupancy(w32, prec, p.bond_nt, smem)) * std::max(1, g_sm_count);
+                p.bond_uni = (op->tab_uni[prec] && p.bond_nt >= 4) ? 1 : 0;
+                p.bond_near = op->tab_near[prec];
+                int& mt = B.max_blocks_table[p.bond_uni][p.bond_nt == 8 ? 2 : p.bond_nt == 4 ? 1 : 0];
+                if (mt == 0)
+                    mt = std::max(1, hx_table_occupancy(w32, prec, p.bond_nt, smem, p.bond_uni != 0)) *
+                         std::max(1, g_sm_count);
                 const long long warps = (p.n_rows + 31) / 32;
                 const int blocks = (int)std::max<long long>(1, std::min<long long>((warps + HX_THREADS / 32 - 1) / (HX_THREADS / 32), mt));
                 if (blocks_used) *blocks_used = blocks;
@@ -790,6 +947,50 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
         else hx_rows_launch_w64(gk, prec, p, blocks, B.smem_rows, st);
         return;
     }
+    auto cap_blocks = [&](int b) { return max_blocks_cap > 0 ? std::max(1, std::min(b, max_blocks_cap)) : b; };
+    if (mode == 1 && B.tmpl.o_bunit >= 0 && op->pair_allowed && (op->d_tab || sp.d_map)) {
+        // gradient on the pair-flip schedule: targets from the target table (or the parent-state map),
+        // per-thread FP64 coupling accumulators in shared memory after the pair-flip image
+        const bool table = op->d_tab != nullptr;
+        HxParams q = B.tmpl_pair;
+        q.o_grad = (int)align16(B.smem_bond);
+        const size_t gsmem = (size_t)q.o_grad + (size_t)op->n_coupl * HX_THREADS * 8;
+        if (gsmem <= 200 * 1024) {
+            build_blob(op, prec, dir, 0);   // the forward diagonal table
+            q.diag = op->blob[prec][dir][0].d_diag;
+            q.blob = B.d_pair;
+            q.blob_words16 = (int)(B.smem_bond / 16);
+            q.lpr = 1;
+            q.rows_per_tile = 32;
+            q.bond_nt = 4;
+            q.bond_pf = 0;
+            q.bond_uni = 0;
+            q.x = x;
+            q.y = y;
+            q.gy = gy;
+            q.grad_partial = grad_partial;
+            q.accumulate = accumulate;
+            if (table) {
+                q.tab = op->d_tab;
+                q.tile_off = op->d_tile_off;
+                q.tab_wide = op->tab_wide;
+                q.tab_cb = op->tab_cb;
+            } else {
+                set_map_params(q, sp);
+                q.map = sp.d_map;
+                q.map_wide = sp.map_wide;
+                q.map_cb = sp.map_cb;
+                q.map_direct = sp.map_direct;
+            }
+            int& mb = B.max_blocks_pgrad[table ? 1 : 0];
+            if (mb == 0) mb = std::max(1, hx_bond_grad_occupancy(sp.w32, table, prec, gsmem)) * std::max(1, g_sm_count);
+            const long long warps = (q.n_rows + 31) / 32;
+            const int blocks = cap_blocks((int)std::max<long long>(1, std::min<long long>((warps + HX_THREADS / 32 - 1) / (HX_THREADS / 32), mb)));
+            if (blocks_used) *blocks_used = blocks;
+            hx_bond_grad_launch(sp.w32, table, prec, q, blocks, gsmem, st);
+            return;
+        }
+    }
     if (mode == 1) {
         // gradient: the row-per-lane kernel with per-thread coupling accumulators when they fit in
         // shared memory (deterministic block sums, no atomics), else the queued kernel below
@@ -811,8 +1012,8 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
                 B.max_blocks_grad = per_sm * std::max(1, g_sm_count);
             }
             const long long warps = (p.n_rows + p.rows_per_tile - 1) / p.rows_per_tile;
-            const int blocks = (int)std::max<long long>(
-                1, std::min<long long>((warps + HX_THREADS / 32 - 1) / (HX_THREADS / 32), B.max_blocks_grad));
+            const int blocks = cap_blocks((int)std::max<long long>(
+                1, std::min<long long>((warps + HX_THREADS / 32 - 1) / (HX_THREADS / 32), B.max_blocks_grad)));
             if (blocks_used) *blocks_used = blocks;
             if (op->space->w32) hx_rows_grad_launch_w32(B.gk, prec, p, blocks, gsmem, st);
             else hx_rows_grad_launch_w64(B.gk, prec, p, blocks, gsmem, st);
@@ -826,7 +1027,7 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
     p.gy = gy;
     p.grad_partial = grad_partial;
     p.accumulate = accumulate;
-    const int blocks = blocks_for(B, p.n_rows, rows);
+    const int blocks = mode == 1 ? cap_blocks(blocks_for(B, p.n_rows, rows)) : blocks_for(B, p.n_rows, rows);
     if (blocks_used) *blocks_used = blocks;
     if (op->space->w32) hx_launch_w32(B.gk, prec, mode, p, blocks, B.smem, st);
     else hx_launch_w64(B.gk, prec, mode, p, blocks, B.smem, st);
@@ -835,6 +1036,28 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
 edgpu_space_s* as_space(edgpu_space s) {
     require(s != nullptr, EDGPU_ERR_ARG, "null space handle");
     return static_cast<edgpu_space_s*>(s);
+}
+
+// The operators of a batch, then their spaces, each locked once in address order (so two batches
+// sharing operators cannot deadlock).
+struct BatchLocks {
+    std::vector<std::unique_lock<std::mutex>> ops;
+    std::vector<std::unique_lock<std::recursive_mutex>> spaces;
+    explicit BatchLocks(const std::vector<edgpu_op_s*>& v);
+};
+
+BatchLocks::BatchLocks(const std::vector<edgpu_op_s*>& v) {
+    std::vector<edgpu_op_s*> o(v);
+    std::sort(o.begin(), o.end());
+    o.erase(std::unique(o.begin(), o.end()), o.end());
+    std::vector<edgpu_space_s*> sp;
+    for (auto* x : o) {
+        ops.emplace_back(x->hs.mu);
+        sp.push_back(x->space);
+    }
+    std::sort(sp.begin(), sp.end());
+    sp.erase(std::unique(sp.begin(), sp.end()), sp.end());
+    for (auto* x : sp) spaces.emplace_back(x->hs.mu);
 }
 
 edgpu_op_s* as_op(edgpu_op o) {
@@ -958,20 +1181,18 @@ std::vector<double> tridiag_eigvec(const std::vector<double>& a, const std::vect
 
 // Support for the entry point in noalloc.cu: expose already-built gradient tables and the error slot.
 namespace edgpu {
-bool coupling_grad_tables(edgpu_op oh, int prec, GradTables* out) {
+std::unique_lock<std::mutex> lock_op(edgpu_op oh) { return std::unique_lock<std::mutex>(as_op(oh)->hs.mu); }
+
+bool coupling_grad_launch_built(edgpu_op oh, int prec, const void* x, const void* gy, void* y, double* partial,
+                                int cap_blocks, cudaStream_t st, int* blocks_used) {
     edgpu_op_s* op = as_op(oh);
-    const Blob& B = op->blob[prec][0][1];
-    if (!B.ready) return false;
-    out->tmpl = B.tmpl;
-    out->smem = B.smem;
-    out->max_blocks = B.max_blocks;
-    out->gk = B.gk;
-    out->rows_per_tile = op->tuned_rows[prec] > 0 ? op->tuned_rows[prec] : B.rows_per_tile;
-    out->n_coupl = op->n_coupl;
-    out->w32 = op->space->w32;
-    out->dim = op->space->dim;
+    if (!op->blob[prec][0][1].ready || !op->blob[prec][0][0].ready) return false;
+    launch_product(op, prec, 0, 1, x, y, 0, gy, partial, st, blocks_used, 0, nullptr, 0, nullptr, cap_blocks);
     return true;
 }
+
+int coupling_count(edgpu_op oh) { return as_op(oh)->n_coupl; }
+int64_t op_dimension(edgpu_op oh) { return as_op(oh)->space->dim; }
 
 int record_api_error(int code, const std::string& msg) { return fail(code, msg); }
 }  // namespace edgpu
@@ -1055,8 +1276,8 @@ int edgpu_space_create(int32_t n_sites, const int32_t* site_dims, int32_t qn_len
         return EDGPU_OK;
     }
     init_device();
-    enumerate_parent(*s, g_stream);
-    if (!s->lazy) build_search_directory(*s, g_stream);
+    enumerate_parent(*s, s->hs.stream());
+    if (!s->lazy) build_search_directory(*s, s->hs.stream());
     *out = s.release();
     API_END
 }
@@ -1101,7 +1322,7 @@ int edgpu_space_from_basis(int32_t n_sites, const int32_t* site_dims, const uint
         EDGPU_CUDA(cudaMalloc(&s->d_keys, std::max<int64_t>(n, 1) * 8));
         EDGPU_CUDA(cudaMemcpy(s->d_keys, b.data(), n * 8, cudaMemcpyHostToDevice));
     }
-    build_search_directory(*s, g_stream);
+    build_search_directory(*s, s->hs.stream());
     *out = s.release();
     API_END
 }
@@ -1123,25 +1344,27 @@ int edgpu_space_nbits(edgpu_space s, int32_t* out) {
 int edgpu_space_get_basis(edgpu_space sh, uint64_t* out, int64_t n) {
     API_BEGIN
     edgpu_space_s* s = as_space(sh);
+    SpaceLock lk_(s->hs.mu);
     require(s->d_keys != nullptr || s->dim == 0, EDGPU_ERR_STATE, "basis of a lazy space is not materialised");
     if (n != s->dim) throw Error(EDGPU_ERR_DIM, "output has length " + std::to_string(n) + " != dimension " +
                                                      std::to_string(s->dim));
     if (n == 0) return EDGPU_OK;
     require(out, EDGPU_ERR_ARG, "null output");
-    get_states(*s, out, g_stream);
+    get_states(*s, out, s->hs.stream());
     API_END
 }
 
 int edgpu_space_lookup(edgpu_space sh, const uint64_t* keys, int64_t n, int64_t* idx_out) {
     API_BEGIN
     edgpu_space_s* s = as_space(sh);
+    SpaceLock lk_(s->hs.mu);
     require(s->d_keys != nullptr, EDGPU_ERR_STATE, "basis of a lazy space is not materialised");
     require(n >= 0 && (n == 0 || (keys && idx_out)), EDGPU_ERR_ARG, "bad arguments");
     if (s->dim == 0) {
         for (int64_t i = 0; i < n; ++i) idx_out[i] = -1;
         return EDGPU_OK;
     }
-    lookup_keys(*s, keys, n, idx_out, g_stream);
+    lookup_keys(*s, keys, n, idx_out, s->hs.stream());
     API_END
 }
 
@@ -1151,6 +1374,7 @@ int edgpu_space_search_stats(edgpu_space sh, int64_t* buckets, int32_t* shift, i
                              int32_t* window_steps, double* inline_fraction) {
     API_BEGIN
     edgpu_space_s* s = as_space(sh);
+    SpaceLock lk_(s->hs.mu);
     require(s->d_dir != nullptr || s->dim == 0, EDGPU_ERR_STATE, "no search directory (lazy or empty space)");
     if (buckets) *buckets = s->dir_nb;
     if (shift) *shift = s->dir_shift;
@@ -1163,10 +1387,11 @@ int edgpu_space_search_stats(edgpu_space sh, int64_t* buckets, int32_t* shift, i
 int edgpu_space_build_map(edgpu_space sh, int64_t max_bytes, int32_t* built) {
     API_BEGIN
     edgpu_space_s* s = as_space(sh);
+    SpaceLock lk_(s->hs.mu);
     require(max_bytes >= 0, EDGPU_ERR_ARG, "negative byte limit");
     require(s->reduced, EDGPU_ERR_ARG, "parent-state maps belong to reduced representations");
-    if (!s->d_dir && s->dim > 0) build_search_directory(*s, g_stream);
-    const bool ok = build_parent_map(*s, max_bytes, g_stream);
+    if (!s->d_dir && s->dim > 0) build_search_directory(*s, s->hs.stream());
+    const bool ok = build_parent_map(*s, max_bytes, s->hs.stream());
     if (built) *built = ok ? 1 : 0;
     API_END
 }
@@ -1174,6 +1399,7 @@ int edgpu_space_build_map(edgpu_space sh, int64_t max_bytes, int32_t* built) {
 int edgpu_space_free_map(edgpu_space sh) {
     API_BEGIN
     edgpu_space_s* s = as_space(sh);
+    SpaceLock lk_(s->hs.mu);
     EDGPU_CUDA(cudaDeviceSynchronize());
     free_parent_map(*s);
     API_END
@@ -1182,6 +1408,7 @@ int edgpu_space_free_map(edgpu_space sh) {
 int edgpu_space_map_info(edgpu_space sh, int64_t* entries, int32_t* entry_bytes) {
     API_BEGIN
     edgpu_space_s* s = as_space(sh);
+    SpaceLock lk_(s->hs.mu);
     if (entries) *entries = s->d_map ? s->map_n : 0;
     if (entry_bytes) *entry_bytes = s->d_map ? (s->map_wide ? 8 : 4) : 0;
     API_END
@@ -1193,6 +1420,7 @@ int edgpu_reduce(edgpu_space parent_h, int32_t n_elems, const int32_t* site_maps
     require(out != nullptr, EDGPU_ERR_ARG, "null output handle");
     *out = nullptr;
     edgpu_space_s* parent = as_space(parent_h);
+    SpaceLock lk_(parent->hs.mu);
     require(!parent->reduced, EDGPU_ERR_ARG, "the parent must be an unreduced representation");
     const Layout& L = parent->lay;
     const int n = L.n_sites;
@@ -1303,10 +1531,10 @@ int edgpu_reduce(edgpu_space parent_h, int32_t n_elems, const int32_t* site_maps
         s->dim = 0;
         EDGPU_CUDA(cudaMalloc(&s->d_keys, 16));
     } else {
-        enumerate_reps(*s, *parent, g_stream);
-        embed_orbit_index(*s, g_stream);
+        enumerate_reps(*s, *parent, s->hs.stream());
+        embed_orbit_index(*s, s->hs.stream());
     }
-    build_search_directory(*s, g_stream);
+    build_search_directory(*s, s->hs.stream());
     *out = s.release();
     API_END
 }
@@ -1314,22 +1542,24 @@ int edgpu_reduce(edgpu_space parent_h, int32_t n_elems, const int32_t* site_maps
 int edgpu_reduce_mapping(edgpu_space reduced, int64_t* index_out, double* ampl_out, int64_t n_parent) {
     API_BEGIN
     edgpu_space_s* s = as_space(reduced);
+    SpaceLock lk_(s->hs.mu);
     require(s->reduced && s->parent, EDGPU_ERR_ARG, "not a reduced representation");
     require(s->parent->d_keys != nullptr || s->parent->dim == 0, EDGPU_ERR_STATE, "the parent basis is not materialised");
     if (n_parent != s->parent->dim) throw Error(EDGPU_ERR_DIM, "output length != parent dimension");
     if (n_parent == 0) return EDGPU_OK;
     require(index_out && ampl_out, EDGPU_ERR_ARG, "null output");
-    build_mapping(*s, *s->parent, index_out, ampl_out, g_stream);
+    build_mapping(*s, *s->parent, index_out, ampl_out, s->hs.stream());
     API_END
 }
 
 int edgpu_space_orbit_sizes(edgpu_space reduced, int32_t* out, int64_t n) {
     API_BEGIN
     edgpu_space_s* s = as_space(reduced);
+    SpaceLock lk_(s->hs.mu);
     if (n != s->dim) throw Error(EDGPU_ERR_DIM, "output length != dimension");
     if (n == 0) return EDGPU_OK;
     require(out, EDGPU_ERR_ARG, "null output");
-    orbit_sizes(*s, out, g_stream);
+    orbit_sizes(*s, out, s->hs.stream());
     API_END
 }
 
@@ -1340,6 +1570,7 @@ int edgpu_op_create(edgpu_space sh, int32_t n_terms, const uint64_t* masks, cons
     require(out != nullptr, EDGPU_ERR_ARG, "null output handle");
     *out = nullptr;
     edgpu_space_s* s = as_space(sh);
+    SpaceLock lk_(s->hs.mu);
     require(s->d_keys != nullptr, EDGPU_ERR_STATE, "the representation's basis is not materialised");
     require(n_terms >= 0, EDGPU_ERR_ARG, "negative term count");
     require(n_terms == 0 || (masks && rows && cols && amps), EDGPU_ERR_ARG, "null term arrays");
@@ -1377,9 +1608,10 @@ int edgpu_op_create(edgpu_space sh, int32_t n_terms, const uint64_t* masks, cons
 int edgpu_op_set_couplings(edgpu_op oh, const double* couplings, int32_t n_couplings) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     require(n_couplings == op->n_coupl && couplings, EDGPU_ERR_DIM, "coupling count mismatch");
     op->coupl.assign(couplings, couplings + n_couplings);
-    invalidate_blobs(op);
+    refresh_blobs(op);
     API_END
 }
 
@@ -1400,6 +1632,7 @@ void edgpu_op_destroy(edgpu_op o) {
 int edgpu_op_set_tiling(edgpu_op oh, int32_t precision, int32_t rows_per_tile) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     check_prec(precision);
     require(rows_per_tile == 0 || rows_per_tile == -1 || rows_per_tile == -2 || rows_per_tile == -4 ||
                 (rows_per_tile >= 1 && rows_per_tile <= 32 && (32 % rows_per_tile) == 0),
@@ -1411,11 +1644,26 @@ int edgpu_op_set_tiling(edgpu_op oh, int32_t precision, int32_t rows_per_tile) {
 int edgpu_op_set_pair_schedule(edgpu_op oh, int32_t enable) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
-    require(enable == 0 || enable == 1 || enable == 2 || enable == 4 || enable == 8, EDGPU_ERR_ARG,
-            "enable must be 0, 1, 2, 4 or 8");
-    op->pair_allowed = enable ? 1 : 0;
-    op->pair_use[0] = op->pair_use[1] = enable ? 1 : 0;
-    op->pair_nt[0] = op->pair_nt[1] = enable >= 4 ? enable : 2;
+    OpLock lk_(op->hs.mu);
+    const int uni = (enable & EDGPU_PAIR_UNIFORM) ? 1 : 0;
+    const int nt = enable & ~EDGPU_PAIR_UNIFORM;
+    require(nt == 0 || nt == 1 || nt == 2 || nt == 4 || nt == 8, EDGPU_ERR_ARG,
+            "enable must be 0, 1, 2, 4 or 8, optionally with EDGPU_PAIR_UNIFORM");
+    require(!uni || nt >= 4, EDGPU_ERR_ARG, "warp-uniform pair steps need 4 or 8 targets per step");
+    op->pair_allowed = nt ? 1 : 0;
+    op->pair_use[0] = op->pair_use[1] = nt ? 1 : 0;
+    op->pair_nt[0] = op->pair_nt[1] = nt >= 4 ? nt : 2;
+    op->tab_uni[0] = op->tab_uni[1] = uni;
+    API_END
+}
+
+int edgpu_op_near_window(edgpu_op oh, int32_t precision, int64_t rows, int64_t* current) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
+    check_prec(precision);
+    if (rows >= 0) op->tab_near[precision] = rows;
+    if (current) *current = op->tab_near[precision];
     API_END
 }
 
@@ -1423,6 +1671,7 @@ int edgpu_op_get_schedule(edgpu_op oh, int32_t precision, int32_t* rows_per_tile
                           int32_t* target_table) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     check_prec(precision);
     if (rows_per_tile) *rows_per_tile = op->tuned_rows[precision];
     build_blob(op, precision, 0, 0);
@@ -1432,7 +1681,7 @@ int edgpu_op_get_schedule(edgpu_op oh, int32_t precision, int32_t* rows_per_tile
     const bool table = on && op->d_tab && op->tab_use[precision];
     int nt = 2;
     if (on && (op->space->d_map || table) && op->pair_nt[precision] >= 4) nt = (table && op->pair_nt[precision] == 8) ? 8 : 4;
-    if (pair_flips) *pair_flips = on ? nt : 0;
+    if (pair_flips) *pair_flips = on ? (nt | ((table && nt >= 4 && op->tab_uni[precision]) ? EDGPU_PAIR_UNIFORM : 0)) : 0;
     if (target_table) *target_table = table ? 1 : 0;
     API_END
 }
@@ -1440,6 +1689,7 @@ int edgpu_op_get_schedule(edgpu_op oh, int32_t precision, int32_t* rows_per_tile
 int edgpu_op_build_targets(edgpu_op oh, int64_t max_bytes, int32_t* built) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     require(max_bytes >= 0, EDGPU_ERR_ARG, "negative byte limit");
     if (built) *built = 0;
     op->free_table();
@@ -1487,8 +1737,8 @@ int edgpu_op_build_targets(edgpu_op oh, int64_t max_bytes, int32_t* built) {
     long long* d_off = nullptr;
     EDGPU_CUDA(cudaMalloc(&d_off, (size_t)n_tiles * sizeof(long long)));
     try {
-        hx_table_count(sp.w32, p, n_tiles, cnt.p, smem, g_stream);
-        const long long total = hx_table_scan(cnt.p, n_tiles, d_off, g_stream);
+        hx_table_count(sp.w32, p, n_tiles, cnt.p, smem, op->hs.stream());
+        const long long total = hx_table_scan(cnt.p, n_tiles, d_off, op->hs.stream());
         const double bytes = (double)total * (wide ? 8.0 : 4.0) + (double)n_tiles * 8.0;
         if (bytes > (double)max_bytes) {
             cudaFree(d_off);
@@ -1501,8 +1751,8 @@ int edgpu_op_build_targets(edgpu_op oh, int64_t max_bytes, int32_t* built) {
         p.tab_wide = wide;
         p.tab_cb = cb;
         try {
-            hx_table_fill(sp.w32, mapped ? GK_MAP : B.gk, p, n_tiles, smem, g_stream);
-            EDGPU_CUDA(cudaStreamSynchronize(g_stream));
+            hx_table_fill(sp.w32, mapped ? GK_MAP : B.gk, p, n_tiles, smem, op->hs.stream());
+            EDGPU_CUDA(cudaStreamSynchronize(op->hs.stream()));
         } catch (...) {
             cudaFree(d_tab);
             throw;
@@ -1524,14 +1774,97 @@ int edgpu_op_build_targets(edgpu_op oh, int64_t max_bytes, int32_t* built) {
 int edgpu_op_free_targets(edgpu_op oh) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
-    EDGPU_CUDA(cudaStreamSynchronize(g_stream));
+    OpLock lk_(op->hs.mu);
+    // products on caller streams may still read the table
+    EDGPU_CUDA(cudaDeviceSynchronize());
     op->free_table();
+    API_END
+}
+
+int edgpu_op_build_adjoint_targets(edgpu_op oh, int64_t max_bytes, int32_t* built) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
+    require(max_bytes >= 0, EDGPU_ERR_ARG, "negative byte limit");
+    if (built) *built = 0;
+    op->free_adjoint();
+    const Space& sp = *op->space;
+    if (!op->d_tab || sp.dim == 0) return EDGPU_OK;
+    int prec = EDGPU_MIXED;
+    build_blob(op, prec, 0, 0);
+    if (op->blob[prec][0][0].tmpl.bond_ncls == 0) {
+        prec = EDGPU_FP64;
+        build_blob(op, prec, 0, 0);
+    }
+    const Blob& B = op->blob[prec][0][0];
+    if (B.tmpl.bond_ncls == 0) return EDGPU_OK;
+    require(sp.dim < ((int64_t)1 << 32) && sp.sb <= 5 && sp.group.G <= (1 << 14), EDGPU_ERR_ARG,
+            "the adjoint table's entries hold rows below 2^32, 5 orbit-size bits and 2^14 group elements");
+    const int64_t n = sp.dim;
+    if ((double)op->tab_n * 8.0 + (double)(n + 1) * 8.0 > (double)max_bytes) return EDGPU_OK;
+    HxParams p = B.tmpl_pair;
+    p.blob = B.d_pair;
+    p.blob_words16 = (int)(B.smem_bond / 16);
+    p.lpr = 1;
+    p.rows_per_tile = 32;
+    p.bond_nt = 4;
+    p.bond_pf = 0;
+    p.bond_uni = 0;
+    p.tab = op->d_tab;
+    p.tile_off = op->d_tile_off;
+    p.tab_wide = op->tab_wide;
+    p.tab_cb = op->tab_cb;
+    const long long n_tiles = (n + 31) / 32;
+    cudaStream_t st = op->hs.stream();
+    DevBuf<unsigned> cnt;
+    cnt.ensure((size_t)n);
+    EDGPU_CUDA(cudaMemsetAsync(cnt.p, 0, (size_t)n * sizeof(unsigned), st));
+    p.adj_cnt = cnt.p;
+    hx_adj_pass(sp.w32, 1, p, n_tiles, B.smem_bond, st);
+    std::vector<unsigned> hc((size_t)n);
+    EDGPU_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, (size_t)n * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    EDGPU_CUDA(cudaStreamSynchronize(st));
+    std::vector<long long> ho((size_t)n + 1);
+    ho[0] = 0;
+    for (int64_t c = 0; c < n; ++c) ho[c + 1] = ho[c] + hc[c];
+    const long long total = ho[n];
+    long long* d_off = nullptr;
+    unsigned long long* d_tab = nullptr;
+    EDGPU_CUDA(cudaMalloc(&d_off, (size_t)(n + 1) * sizeof(long long)));
+    cudaError_t e = cudaMalloc(&d_tab, std::max<size_t>((size_t)total * 8, 16));
+    if (e != cudaSuccess) {
+        cudaFree(d_off);
+        throw Error(e == cudaErrorMemoryAllocation ? EDGPU_ERR_OOM : EDGPU_ERR_CUDA,
+                    std::string("adjoint table: ") + cudaGetErrorString(e));
+    }
+    op->d_adj_off = d_off;
+    op->d_adj_tab = d_tab;
+    EDGPU_CUDA(cudaMemcpyAsync(d_off, ho.data(), (size_t)(n + 1) * sizeof(long long), cudaMemcpyHostToDevice, st));
+    EDGPU_CUDA(cudaMemsetAsync(cnt.p, 0, (size_t)n * sizeof(unsigned), st));
+    p.adj_off = d_off;
+    p.adj_cur = cnt.p;
+    p.adj_tab = d_tab;
+    hx_adj_pass(sp.w32, 2, p, n_tiles, B.smem_bond, st);
+    hx_adj_sort(d_off, d_tab, n, st);
+    EDGPU_CUDA(cudaStreamSynchronize(st));
+    op->adj_n = total;
+    if (built) *built = 1;
+    API_END
+}
+
+int edgpu_op_free_adjoint_targets(edgpu_op oh) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
+    EDGPU_CUDA(cudaDeviceSynchronize());
+    op->free_adjoint();
     API_END
 }
 
 int edgpu_op_targets_info(edgpu_op oh, int64_t* entries, int32_t* entry_bytes) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     if (entries) *entries = op->d_tab ? op->tab_n : 0;
     if (entry_bytes) *entry_bytes = op->d_tab ? (op->tab_wide ? 8 : 4) : 0;
     API_END
@@ -1541,7 +1874,8 @@ int edgpu_pair_classes_of_terms(int32_t n_bits, int32_t n_terms, const uint64_t*
                                 const uint64_t* cols, const double* amps, int32_t cap_classes, int32_t* n_classes,
                                 int32_t* info, uint64_t* comps, uint64_t* flips, double* class_amps) {
     API_BEGIN
-    require(n_bits >= 1 && n_bits <= 64 && n_terms >= 0 && n_classes, EDGPU_ERR_ARG, "bad arguments");
+    require(n_bits >= 1 && n_bits <= 64, EDGPU_ERR_ARG, "n_bits = " + std::to_string(n_bits) + " is not in [1, 64]");
+    require(n_terms >= 0 && n_classes, EDGPU_ERR_ARG, "bad arguments");
     require(n_terms == 0 || (masks && rows && cols && amps), EDGPU_ERR_ARG, "null term arrays");
     Layout lay;
     lay.n_sites = lay.nbits = n_bits;
@@ -1574,6 +1908,7 @@ int edgpu_pair_classes_of_terms(int32_t n_bits, int32_t n_terms, const uint64_t*
 int edgpu_op_pair_classes(edgpu_op oh, int32_t* n_classes, int32_t* n_components) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     std::vector<uint64_t> bm, br, bf;
     std::vector<double> ba;
     for (int t = 0; t < op->T; ++t) {
@@ -1599,30 +1934,42 @@ int edgpu_op_pair_classes(edgpu_op oh, int32_t* n_classes, int32_t* n_components
 int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out, double* best_ms_out) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     check_prec(precision);
     const int64_t n = op->space->dim;
     // Candidates: the term scan with 1, 2 or 4 lanes per row (and the queued schedule with 32 or 16
     // rows per warp tile when there is no parent-state map); where the pair-flip schedule applies
     // (and the caller allows it), that schedule with 2 or 4 targets per step (4 with a map or a
     // target table) and 1, 2 or 4 lanes per row, and its target-table flavour (one lane per row).
-    struct Cand { int pair, nt, table, rows, pf; };
+    struct Cand { int pair, nt, table, rows, pf, uni; long long near; };
     std::vector<Cand> cands;
     build_blob(op, precision, 0, 0);
     const bool pair_ok = op->blob[precision][0][0].tmpl.bond_ncls > 0 && op->pair_allowed;
     const bool mapped = op->space->d_map != nullptr;
     if (pair_ok) {
-        if (op->d_tab)
+        if (op->d_tab) {
             for (int nt : {8, 4, 2})
-                for (int pf : {0, 4, 64}) cands.push_back({1, nt, 1, -1, pf});
+                for (int pf : {0, 4, 64}) cands.push_back({1, nt, 1, -1, pf, 0, 0});
+            for (int nt : {8, 4})
+                for (int pf : {0, 4}) cands.push_back({1, nt, 1, -1, pf, 1, 0});
+            // streamed table and far gathers, with near windows of 2^15 to 2^23 rows, for sectors whose x
+            // is larger than a quarter of L2
+            const size_t vsz = precision == EDGPU_FP64 ? 16 : 8;
+            if ((double)n * vsz > 32e6)
+                for (long long near : {1ll << 15, 1ll << 18, 1ll << 20, 1ll << 22, 1ll << 62})
+                    for (int nt : {8, 4}) cands.push_back({1, nt, 1, -1, 0, 0, near});
+        }
         for (int nt : (mapped ? std::vector<int>{4, 2} : std::vector<int>{2}))
-            for (int r : {-1, -2, -4}) cands.push_back({1, nt, 0, r, 0});
+            for (int r : {-1, -2, -4}) cands.push_back({1, nt, 0, r, 0, 0, 0});
     }
-    for (int r : {-1, -2, -4}) cands.push_back({0, 2, 0, r, 0});
+    for (int r : {-1, -2, -4}) cands.push_back({0, 2, 0, r, 0, 0, 0});
     if (!mapped)
-        for (int r : {32, 16}) cands.push_back({0, 2, 0, r, 0});
+        for (int r : {32, 16}) cands.push_back({0, 2, 0, r, 0, 0, 0});
     Cand best = cands.front();
     double best_ms = 1e30;
     const int keep_pair = op->pair_use[precision], keep_nt = op->pair_nt[precision], keep_tab = op->tab_use[precision];
+    const int keep_uni = op->tab_uni[precision];
+    const long long keep_near = op->tab_near[precision];
     if (n > 0) {
         const size_t vs = precision == EDGPU_FP64 ? 16 : 8;
         void *x = nullptr, *y = nullptr;
@@ -1632,28 +1979,30 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         try {
-            EDGPU_CUDA(cudaMemsetAsync(x, 0, n * vs, g_stream));
+            EDGPU_CUDA(cudaMemsetAsync(x, 0, n * vs, op->hs.stream()));
             for (const Cand& c : cands) {
                 op->pair_use[precision] = c.pair;
                 op->pair_nt[precision] = c.nt;
                 op->tab_use[precision] = c.table;
                 op->tab_pf[precision] = c.pf;
-                launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, g_stream, nullptr, c.rows);
+                op->tab_uni[precision] = c.uni;
+                op->tab_near[precision] = c.near;
+                launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, op->hs.stream(), nullptr, c.rows);
                 // one timed launch, then two back-to-back bursts of enough launches to cover about 2 ms
                 // (1 to 50 per burst), as a solver issues them; the faster burst's time per launch
                 float t_min = 1e30f;
-                EDGPU_CUDA(cudaEventRecord(e0, g_stream));
-                launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, g_stream, nullptr, c.rows);
-                EDGPU_CUDA(cudaEventRecord(e1, g_stream));
+                EDGPU_CUDA(cudaEventRecord(e0, op->hs.stream()));
+                launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, op->hs.stream(), nullptr, c.rows);
+                EDGPU_CUDA(cudaEventRecord(e1, op->hs.stream()));
                 EDGPU_CUDA(cudaEventSynchronize(e1));
                 float ms1 = 0.f;
                 cudaEventElapsedTime(&ms1, e0, e1);
                 const int reps = std::max(1, std::min(50, (int)(2.0f / std::max(ms1, 1e-3f))));
                 for (int burst = 0; burst < 2; ++burst) {
-                    EDGPU_CUDA(cudaEventRecord(e0, g_stream));
+                    EDGPU_CUDA(cudaEventRecord(e0, op->hs.stream()));
                     for (int k = 0; k < reps; ++k)
-                        launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, g_stream, nullptr, c.rows);
-                    EDGPU_CUDA(cudaEventRecord(e1, g_stream));
+                        launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, op->hs.stream(), nullptr, c.rows);
+                    EDGPU_CUDA(cudaEventRecord(e1, op->hs.stream()));
                     EDGPU_CUDA(cudaEventSynchronize(e1));
                     float ms = 0.f;
                     cudaEventElapsedTime(&ms, e0, e1);
@@ -1668,6 +2017,8 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
             op->pair_use[precision] = keep_pair;
             op->pair_nt[precision] = keep_nt;
             op->tab_use[precision] = keep_tab;
+            op->tab_uni[precision] = keep_uni;
+            op->tab_near[precision] = keep_near;
             cudaFree(x);
             cudaFree(y);
             cudaEventDestroy(e0);
@@ -1683,6 +2034,8 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     op->pair_nt[precision] = best.nt;
     op->tab_use[precision] = best.table ? 1 : (op->d_tab ? 0 : 1);
     op->tab_pf[precision] = best.pf;
+    op->tab_uni[precision] = best.uni;
+    op->tab_near[precision] = best.near;
     op->tuned_rows[precision] = best.rows;
     if (rows_per_tile_out) *rows_per_tile_out = best.rows;
     if (best_ms_out) *best_ms_out = best_ms;
@@ -1706,9 +2059,9 @@ void sparse_pass(edgpu_op_s* op, int transpose, double tol, long long row0, long
     require(smem <= 227 * 1024, EDGPU_ERR_ARG, "too many off-diagonal terms per row for sparse assembly");
     if (n_run <= 0) return;
     if (op->space->w32)
-        hx_sparse_launch_w32(B.gk, p, row0, n_run, transpose, tol, d_counts, d_row_ptr, d_cols, d_vals, smem, g_stream);
+        hx_sparse_launch_w32(B.gk, p, row0, n_run, transpose, tol, d_counts, d_row_ptr, d_cols, d_vals, smem, op->hs.stream());
     else
-        hx_sparse_launch_w64(B.gk, p, row0, n_run, transpose, tol, d_counts, d_row_ptr, d_cols, d_vals, smem, g_stream);
+        hx_sparse_launch_w64(B.gk, p, row0, n_run, transpose, tol, d_counts, d_row_ptr, d_cols, d_vals, smem, op->hs.stream());
 }
 
 }  // namespace
@@ -1717,6 +2070,7 @@ int edgpu_op_sparse(edgpu_op oh, int32_t transpose, double tol, int64_t* nnz, in
                     double* values) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     require(nnz && tol >= 0.0 && (transpose == 0 || transpose == 1), EDGPU_ERR_ARG, "bad sparse arguments");
     require(!row_ptr || (col_idx && values), EDGPU_ERR_ARG, "row_ptr, col_idx and values go together");
     const long long n = op->space->dim;
@@ -1725,8 +2079,8 @@ int edgpu_op_sparse(edgpu_op oh, int32_t transpose, double tol, int64_t* nnz, in
     counts.ensure(std::max<long long>(n, 1));
     sparse_pass(op, transpose, tol, 0, n, counts.p, nullptr, nullptr, nullptr);
     std::vector<long long> hc(n);
-    if (n) EDGPU_CUDA(cudaMemcpyAsync(hc.data(), counts.p, n * sizeof(long long), cudaMemcpyDeviceToHost, g_stream));
-    EDGPU_CUDA(cudaStreamSynchronize(g_stream));
+    if (n) EDGPU_CUDA(cudaMemcpyAsync(hc.data(), counts.p, n * sizeof(long long), cudaMemcpyDeviceToHost, op->hs.stream()));
+    EDGPU_CUDA(cudaStreamSynchronize(op->hs.stream()));
     std::vector<long long> hp(n + 1, 0);
     for (long long i = 0; i < n; ++i) hp[i + 1] = hp[i] + hc[i];
     *nnz = hp[n];
@@ -1736,11 +2090,11 @@ int edgpu_op_sparse(edgpu_op oh, int32_t transpose, double tol, int64_t* nnz, in
     rp.ensure(n + 1);
     cols.ensure(hp[n]);
     vals.ensure(2 * hp[n]);
-    EDGPU_CUDA(cudaMemcpyAsync(rp.p, hp.data(), (n + 1) * sizeof(long long), cudaMemcpyHostToDevice, g_stream));
+    EDGPU_CUDA(cudaMemcpyAsync(rp.p, hp.data(), (n + 1) * sizeof(long long), cudaMemcpyHostToDevice, op->hs.stream()));
     sparse_pass(op, transpose, tol, 0, n, nullptr, rp.p, cols.p, (double2*)vals.p);
-    EDGPU_CUDA(cudaMemcpyAsync(col_idx, cols.p, hp[n] * sizeof(long long), cudaMemcpyDeviceToHost, g_stream));
-    EDGPU_CUDA(cudaMemcpyAsync(values, vals.p, 2 * hp[n] * sizeof(double), cudaMemcpyDeviceToHost, g_stream));
-    EDGPU_CUDA(cudaStreamSynchronize(g_stream));
+    EDGPU_CUDA(cudaMemcpyAsync(col_idx, cols.p, hp[n] * sizeof(long long), cudaMemcpyDeviceToHost, op->hs.stream()));
+    EDGPU_CUDA(cudaMemcpyAsync(values, vals.p, 2 * hp[n] * sizeof(double), cudaMemcpyDeviceToHost, op->hs.stream()));
+    EDGPU_CUDA(cudaStreamSynchronize(op->hs.stream()));
     API_END
 }
 
@@ -1748,6 +2102,7 @@ int edgpu_op_get_row(edgpu_op oh, int32_t transpose, int64_t row, double tol, in
                      int64_t* col_idx, double* values) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     require(count && tol >= 0.0 && (transpose == 0 || transpose == 1) && cap >= 0, EDGPU_ERR_ARG,
             "bad get_row arguments");
     require(row >= 0 && row < op->space->dim, EDGPU_ERR_BOUNDS, "row index out of range");
@@ -1756,8 +2111,8 @@ int edgpu_op_get_row(edgpu_op oh, int32_t transpose, int64_t row, double tol, in
     c.ensure(1);
     sparse_pass(op, transpose, tol, row, 1, c.p, nullptr, nullptr, nullptr);
     long long k = 0;
-    EDGPU_CUDA(cudaMemcpyAsync(&k, c.p, sizeof(long long), cudaMemcpyDeviceToHost, g_stream));
-    EDGPU_CUDA(cudaStreamSynchronize(g_stream));
+    EDGPU_CUDA(cudaMemcpyAsync(&k, c.p, sizeof(long long), cudaMemcpyDeviceToHost, op->hs.stream()));
+    EDGPU_CUDA(cudaStreamSynchronize(op->hs.stream()));
     *count = k;
     if (!col_idx || k == 0) return EDGPU_OK;
     require(values && cap >= k, EDGPU_ERR_DIM, "output buffers hold fewer entries than the row");
@@ -1765,17 +2120,18 @@ int edgpu_op_get_row(edgpu_op oh, int32_t transpose, int64_t row, double tol, in
     rp.ensure(1);
     cols.ensure(k);
     vals.ensure(2 * k);
-    EDGPU_CUDA(cudaMemcpyAsync(rp.p, &zero, sizeof(long long), cudaMemcpyHostToDevice, g_stream));
+    EDGPU_CUDA(cudaMemcpyAsync(rp.p, &zero, sizeof(long long), cudaMemcpyHostToDevice, op->hs.stream()));
     sparse_pass(op, transpose, tol, row, 1, nullptr, rp.p, cols.p, (double2*)vals.p);
-    EDGPU_CUDA(cudaMemcpyAsync(col_idx, cols.p, k * sizeof(long long), cudaMemcpyDeviceToHost, g_stream));
-    EDGPU_CUDA(cudaMemcpyAsync(values, vals.p, 2 * k * sizeof(double), cudaMemcpyDeviceToHost, g_stream));
-    EDGPU_CUDA(cudaStreamSynchronize(g_stream));
+    EDGPU_CUDA(cudaMemcpyAsync(col_idx, cols.p, k * sizeof(long long), cudaMemcpyDeviceToHost, op->hs.stream()));
+    EDGPU_CUDA(cudaMemcpyAsync(values, vals.p, 2 * k * sizeof(double), cudaMemcpyDeviceToHost, op->hs.stream()));
+    EDGPU_CUDA(cudaStreamSynchronize(op->hs.stream()));
     API_END
 }
 
 int edgpu_op_count_nnz(edgpu_op oh, int64_t* n_targets, int64_t* nnz_off) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     require(n_targets && nnz_off, EDGPU_ERR_ARG, "null output");
     std::vector<uint64_t> m, r, f;
     for (int t = 0; t < op->T; ++t)
@@ -1784,7 +2140,7 @@ int edgpu_op_count_nnz(edgpu_op oh, int64_t* n_targets, int64_t* nnz_off) {
             r.push_back(op->rows[t]);
             f.push_back(op->rows[t] ^ op->cols[t]);
         }
-    count_nnz(*op->space, (int)m.size(), m.data(), r.data(), f.data(), n_targets, nnz_off, g_stream);
+    count_nnz(*op->space, (int)m.size(), m.data(), r.data(), f.data(), n_targets, nnz_off, op->hs.stream());
     API_END
 }
 
@@ -1834,7 +2190,7 @@ static void host_product_issue(edgpu_op_s* op, int prec, int dir, const double* 
 // buffers and replayed; pageable buffers take the plain stream path.
 static void host_product(edgpu_op_s* op, int prec, int dir, const double* x, double* y, int64_t n, int accumulate,
                          bool conj_io) {
-    cudaStream_t st = g_stream;
+    cudaStream_t st = op->hs.stream();
     op->x64.ensure(2 * n);
     op->y64.ensure(2 * n);
     if (prec == EDGPU_MIXED) {
@@ -1921,6 +2277,7 @@ static void host_product_issue(edgpu_op_s* op, int prec, int dir, const double* 
 int edgpu_mul(edgpu_op oh, int32_t precision, const double* x, double* y, int64_t n, int32_t accumulate) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     check_prec(precision);
     check_dim(op, n, "state");
     if (n == 0) return EDGPU_OK;
@@ -1933,6 +2290,7 @@ int edgpu_mul_device(edgpu_op oh, int32_t precision, const void* x, void* y, int
                      void* stream) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     check_prec(precision);
     check_dim(op, n, "state");
     if (n == 0) return EDGPU_OK;
@@ -1945,6 +2303,7 @@ int edgpu_mul_device(edgpu_op oh, int32_t precision, const void* x, void* y, int
 int edgpu_mul_transpose(edgpu_op oh, int32_t precision, const double* x, double* y, int64_t n, int32_t accumulate) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     check_prec(precision);
     check_dim(op, n, "state");
     if (n == 0) return EDGPU_OK;
@@ -2040,6 +2399,7 @@ bool op_invariant(edgpu_op_s* op) {
 int edgpu_op_is_invariant(edgpu_op oh, int32_t* invariant) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     require(invariant, EDGPU_ERR_ARG, "null output");
     *invariant = op_invariant(op) ? 1 : 0;
     API_END
@@ -2049,6 +2409,7 @@ int edgpu_mul_adjoint_device(edgpu_op oh, int32_t precision, const void* x, void
                              void* stream) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     check_prec(precision);
     check_dim(op, n, "state");
     if (n == 0) return EDGPU_OK;
@@ -2059,8 +2420,25 @@ int edgpu_mul_adjoint_device(edgpu_op oh, int32_t precision, const void* x, void
         launch_product(op, precision, 1, 0, x, y, accumulate ? 1 : 0, nullptr, nullptr, st);
         return EDGPU_OK;
     }
-    // terms that do not commute with the group: the rows of the product's matrix are scattered,
-    // y[c] += conj(H[r, c]) x[r] by atomic adds (summation order not fixed)
+    if (op->d_adj_tab) {
+        // the adjoint target table: every column gathers its run in a fixed order
+        build_blob(op, precision, 0, 0);
+        const Blob& B = op->blob[precision][0][0];
+        HxParams p = B.tmpl_pair;
+        p.blob = B.d_pair;
+        p.blob_words16 = (int)(B.smem_bond / 16);
+        p.gy = x;
+        p.y = y;
+        p.diag = B.d_diag;
+        p.accumulate = accumulate ? 1 : 0;
+        p.adj_off = op->d_adj_off;
+        p.adj_tab = op->d_adj_tab;
+        SpaceLock space_lk(op->space->hs.mu);
+        hx_adj_launch(op->space->w32, precision, p, B.smem_bond, st);
+        return EDGPU_OK;
+    }
+    // terms that do not commute with the group, no adjoint table: the rows of the product's matrix are
+    // scattered, y[c] += conj(H[r, c]) x[r] by atomic adds (summation order not fixed)
     const size_t vs = precision == EDGPU_FP64 ? 16 : 8;
     if (!accumulate) EDGPU_CUDA(cudaMemsetAsync(y, 0, n * vs, st));
     build_blob(op, precision, 0, 0);
@@ -2078,6 +2456,7 @@ int edgpu_coupling_grad_device(edgpu_op oh, int32_t precision, const void* x, co
                                double* grad_out, void* stream) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     check_prec(precision);
     check_dim(op, n, "state");
     require(grad_out, EDGPU_ERR_ARG, "null gradient output");
@@ -2359,6 +2738,8 @@ int edgpu_batch_create(int32_t n_ops, const edgpu_op* ops, edgpu_batch* out) {
 int edgpu_batch_set_tiling(edgpu_batch bh, int32_t precision, int32_t lanes_per_row) {
     API_BEGIN
     require(bh, EDGPU_ERR_ARG, "null batch");
+    std::lock_guard<std::mutex> blk_(bh->hs.mu);
+    BatchLocks locks_(bh->ops);
     check_prec(precision);
     require(lanes_per_row == 0 || lanes_per_row == 1 || lanes_per_row == 2 || lanes_per_row == 4, EDGPU_ERR_ARG,
             "lanes_per_row must be 0 (default), 1, 2 or 4");
@@ -2369,6 +2750,8 @@ int edgpu_batch_set_tiling(edgpu_batch bh, int32_t precision, int32_t lanes_per_
 int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_row_out, double* best_ms_out) {
     API_BEGIN
     require(bh, EDGPU_ERR_ARG, "null batch");
+    std::lock_guard<std::mutex> blk_(bh->hs.mu);
+    BatchLocks locks_(bh->ops);
     check_prec(precision);
     edgpu_batch_s* b = bh;
     batch_prepare(b, precision);
@@ -2399,7 +2782,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
         cudaEventCreate(&e1);
         const int keep = b->lpr[precision];
         try {
-            EDGPU_CUDA(cudaMemsetAsync(x, 0, tot * vs, g_stream));
+            EDGPU_CUDA(cudaMemsetAsync(x, 0, tot * vs, bh->hs.stream()));
             // lanes per row, with and without the pair-flip schedule where it applies
             const bool pair_ok = b->fused[precision].tmpl.bond_ncls > 0 && b->ops[0]->pair_allowed;
             bool mapped = true;
@@ -2422,19 +2805,19 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
                     b->tab_use[precision] = cand >= 3 ? 1 : 0;
                     int blocks = 0;
                     const HxParams p = batch_params(b, precision, xs.data(), ys.data(), &blocks);
-                    batch_launch(b, precision, p, blocks, g_stream);
+                    batch_launch(b, precision, p, blocks, bh->hs.stream());
                     float t_min = 1e30f;
-                    EDGPU_CUDA(cudaEventRecord(e0, g_stream));
-                    batch_launch(b, precision, p, blocks, g_stream);
-                    EDGPU_CUDA(cudaEventRecord(e1, g_stream));
+                    EDGPU_CUDA(cudaEventRecord(e0, bh->hs.stream()));
+                    batch_launch(b, precision, p, blocks, bh->hs.stream());
+                    EDGPU_CUDA(cudaEventRecord(e1, bh->hs.stream()));
                     EDGPU_CUDA(cudaEventSynchronize(e1));
                     float ms1 = 0.f;
                     cudaEventElapsedTime(&ms1, e0, e1);
                     const int reps = std::max(1, std::min(50, (int)(2.0f / std::max(ms1, 1e-3f))));
                     for (int burst = 0; burst < 2; ++burst) {
-                        EDGPU_CUDA(cudaEventRecord(e0, g_stream));
-                        for (int k = 0; k < reps; ++k) batch_launch(b, precision, p, blocks, g_stream);
-                        EDGPU_CUDA(cudaEventRecord(e1, g_stream));
+                        EDGPU_CUDA(cudaEventRecord(e0, bh->hs.stream()));
+                        for (int k = 0; k < reps; ++k) batch_launch(b, precision, p, blocks, bh->hs.stream());
+                        EDGPU_CUDA(cudaEventRecord(e1, bh->hs.stream()));
                         EDGPU_CUDA(cudaEventSynchronize(e1));
                         float ms = 0.f;
                         cudaEventElapsedTime(&ms, e0, e1);
@@ -2455,14 +2838,14 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
             b->pair_use[precision] = 1;
             b->pair_nt[precision] = 2;
             b->tab_use[precision] = 1;
-            cudaStreamSynchronize(g_stream);
+            cudaStreamSynchronize(bh->hs.stream());
             cudaFree(x);
             cudaFree(y);
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
             throw;
         }
-        cudaStreamSynchronize(g_stream);
+        cudaStreamSynchronize(bh->hs.stream());
         // the scratch images refer to freed vectors: forget them
         for (auto& kv : b->images[precision]) cudaFree(kv.second);
         b->images[precision].clear();
@@ -2487,6 +2870,8 @@ int edgpu_batch_get_schedule(edgpu_batch bh, int32_t precision, int32_t* lanes_p
                              int32_t* target_table) {
     API_BEGIN
     require(bh, EDGPU_ERR_ARG, "null batch");
+    std::lock_guard<std::mutex> blk_(bh->hs.mu);
+    BatchLocks locks_(bh->ops);
     check_prec(precision);
     if (lanes_per_row) *lanes_per_row = bh->lpr[precision];
     if (pair_flips) {
@@ -2513,6 +2898,8 @@ int edgpu_batch_mul_device(edgpu_batch bh, int32_t precision, const void* const*
                            void* stream) {
     API_BEGIN
     require(bh && xs && ys, EDGPU_ERR_ARG, "bad batch arguments");
+    std::lock_guard<std::mutex> blk_(bh->hs.mu);
+    BatchLocks locks_(bh->ops);
     check_prec(precision);
     edgpu_batch_s* b = bh;
     cudaStream_t st = pick_stream(stream);
@@ -2583,11 +2970,12 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
                   double* ground_state) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
     check_prec(precision);
     require(n_steps >= 1 && e0 && tol >= 0.0, EDGPU_ERR_ARG, "bad Lanczos arguments");
     const int64_t N = op->space->dim;
     require(N >= 1, EDGPU_ERR_ARG, "empty representation");
-    cudaStream_t st = g_stream;
+    cudaStream_t st = op->hs.stream();
     const int m = (int)std::min<int64_t>(n_steps, N);
     const bool two_phase = refine && precision == EDGPU_MIXED;
     const bool want_vec = ground_state != nullptr;
@@ -2854,7 +3242,8 @@ int edgpu_random_vector_device(int64_t n, uint64_t seed, int32_t precision, void
 
 int edgpu_sync(void) {
     API_BEGIN
-    if (g_stream) EDGPU_CUDA(cudaStreamSynchronize(g_stream));
+    // every handle's stream and the caller streams the library was given
+    if (g_stream) EDGPU_CUDA(cudaDeviceSynchronize());
     API_END
 }
 

@@ -3,6 +3,7 @@
 
 #include <cstdint>
 #include <cstddef>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -137,6 +138,9 @@ std::vector<unsigned long long> generic_luts(const Group& g, const Layout& lay, 
 
 // ---- enumeration (enumerate.cu) ---------------------------------------------------------------
 cudaStream_t lib_stream();
+// Raise a kernel's dynamic shared-memory limit to at least smem bytes, never lowering it, under a
+// process-wide lock (launches from several host threads must not leave a smaller limit in place).
+void raise_smem_limit(const void* kern, size_t smem);
 int sm_count();
 void enumerate_parent(Space& s, cudaStream_t st);
 void enumerate_reps(Space& red, const Space& parent, cudaStream_t st);
@@ -151,9 +155,10 @@ void embed_orbit_index(Space& red, cudaStream_t st);
 void build_search_directory(Space& s, cudaStream_t st);
 void get_states(const Space& s, uint64_t* out_host, cudaStream_t st);
 // Diagonal element of every row: sum of the amplitudes of the row == col terms matching the row's state
-// (FP64), written as complex128 (out64) and/or complex64 (out32).
+// (FP64), written as complex128 (out64) and/or complex64 (out32).  scratch: device room for the T terms
+// (4 words each), or null to allocate it for the call.
 void compute_diagonal(const Space& s, int T, const uint64_t* masks, const uint64_t* rows, const double* amps,
-                      double* out64, float* out32, cudaStream_t st);
+                      double* out64, float* out32, unsigned long long* scratch, cudaStream_t st);
 // Off-diagonal targets of every row (T terms: masks/rows/flips = row ^ col) and how many land in the table.
 void count_nnz(const Space& s, int T, const uint64_t* masks, const uint64_t* rows, const uint64_t* flips,
                int64_t* n_targets, int64_t* n_found, cudaStream_t st);
@@ -212,6 +217,19 @@ struct HxParams {
     int bond_real;                            // every pair amplitude is real
     int bond_nt;                              // targets per lane and step: 2, or 4 (parent-state map only)
     int bond_pf;                              // target tables: x prefetched this many steps ahead (0: none)
+    int bond_uni;                             // target tables: warp-uniform pair steps (bond_tile UNI)
+    long long bond_near;                      // target tables: > 0 streams the table and the gathers of targets
+                                              // at least this many rows from the row (evict-first), 0: default loads
+    // gradient mode of the pair-flip kernel (offsets into its shared-memory image, -1 when absent): the
+    // slots' unit amplitudes and coupling ids, and the diagonal term records
+    int o_bunit, o_bcid, o_pdm, o_pdr, o_pdu, o_pdc;
+    // adjoint target table (column-sorted; built by the ADJ passes of bond_tile): per column the
+    // count, the offset of its run, a fill cursor, and the entries (row << 32 | slot << 19 |
+    // row's orbit-size index << 14 | group element)
+    unsigned* adj_cnt;
+    const long long* adj_off;
+    unsigned* adj_cur;
+    unsigned long long* adj_tab;
     // target table of the pair-flip schedule (GK_TABLE launches and the table's build pass)
     const void* tab;
     const long long* tile_off;
@@ -296,21 +314,33 @@ long long hx_table_scan(const long long* tile_cnt, long long n_tiles, long long*
 void hx_table_fill(bool w32, int gk, const HxParams& p, long long n_tiles, size_t smem, cudaStream_t st);
 // The product through the table (GK_TABLE), one sector and all sectors of a batch.
 void hx_table_launch(bool w32, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
-int hx_table_occupancy(bool w32, int prec, int nt, size_t smem);
+int hx_table_occupancy(bool w32, int prec, int nt, size_t smem, bool uni = false);
 void hx_table_multi_launch(bool w32, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
 int hx_table_multi_occupancy(bool w32, int prec, int nt, size_t smem);
+// The product fused with the coupling gradient on the pair-flip schedule (hx_bond.cuh, GRAD mode):
+// targets from the target table (table) or the parent-state map, four per lane and step.  Shared
+// memory: the pair-flip image up to p.o_grad, then n_couplings x HX_THREADS doubles.
+void hx_bond_grad_launch(bool w32, bool table, int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st);
+int hx_bond_grad_occupancy(bool w32, bool table, int prec, size_t smem);
+// Adjoint target table (hxtable.cu): pass 1 counts every column's targets (p.adj_cnt), pass 2 writes
+// each target's entry into its column's run (p.adj_off, p.adj_cur, p.adj_tab); the runs are then
+// sorted so that the summation order is fixed.  p: the table-flavour pair-flip template (lpr = 1).
+void hx_adj_pass(bool w32, int pass, const HxParams& p, long long n_tiles, size_t smem, cudaStream_t st);
+void hx_adj_sort(const long long* off, unsigned long long* tab, long long n, cudaStream_t st);
+// y = H^dagger x through the adjoint target table: one lane per column, its run in order; p.gy = x.
+void hx_adj_launch(bool w32, int prec, const HxParams& p, size_t smem, cudaStream_t st);
 
 // ---- the coupling-gradient launch for callers that cannot allocate (noalloc.cu) -----------------
-// Launch state of an operator's gradient-mode tables, read without building anything.
-struct GradTables {
-    HxParams tmpl;
-    size_t smem;
-    int max_blocks, gk, rows_per_tile, n_coupl;
-    bool w32;
-    long long dim;
-};
-// False when the tables for this precision have not been built yet (nothing is allocated here).
-bool coupling_grad_tables(edgpu_op op, int prec, GradTables* out);
+// The fused product and coupling gradient exactly as edgpu_coupling_grad_device launches it (same
+// kernel choice), with the per-block partial sums written to partial[blocks][n_couplings] and at most
+// cap_blocks blocks.  False, with nothing launched or allocated, when the operator's tables for this
+// precision (gradient and product mode) have not been built yet.
+bool coupling_grad_launch_built(edgpu_op op, int prec, const void* x, const void* gy, void* y, double* partial,
+                                int cap_blocks, cudaStream_t st, int* blocks_used);
+int coupling_count(edgpu_op op);
+int64_t op_dimension(edgpu_op op);
+// The call lock of an operator handle (calls on one handle are serialised).
+std::unique_lock<std::mutex> lock_op(edgpu_op op);
 // Record an error message for edgpu_last_error() and return code.
 int record_api_error(int code, const std::string& msg);
 

@@ -1198,10 +1198,10 @@ __global__ void k_diag(const W* keys, long long n, int sb, int T, const unsigned
 
 template <typename W>
 void diag_t(const Space& s, int T, const uint64_t* masks, const uint64_t* rows, const double* amps, double* out64,
-            float* out32, cudaStream_t st) {
-    unsigned long long* d = nullptr;
+            float* out32, unsigned long long* scratch, cudaStream_t st) {
+    unsigned long long* d = scratch;
     const size_t Tm = std::max(T, 1);
-    EDGPU_CUDA(cudaMalloc(&d, Tm * (8 + 8 + 16)));
+    if (!scratch) EDGPU_CUDA(cudaMalloc(&d, Tm * (8 + 8 + 16)));
     unsigned long long* dm = d;
     unsigned long long* dr = d + Tm;
     double2* da = (double2*)(d + 2 * Tm);
@@ -1217,14 +1217,14 @@ void diag_t(const Space& s, int T, const uint64_t* masks, const uint64_t* rows, 
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    cudaFree(d);
+    if (!scratch) cudaFree(d);
     if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("diagonal: ") + cudaGetErrorString(e));
 }
 }  // namespace
 
 void compute_diagonal(const Space& s, int T, const uint64_t* masks, const uint64_t* rows, const double* amps,
-                      double* out64, float* out32, cudaStream_t st) {
-    if (s.w32) diag_t<uint32_t>(s, T, masks, rows, amps, out64, out32, st);
-    else diag_t<unsigned long long>(s, T, masks, rows, amps, out64, out32, st);
+                      double* out64, float* out32, unsigned long long* scratch, cudaStream_t st) {
+    if (s.w32) diag_t<uint32_t>(s, T, masks, rows, amps, out64, out32, scratch, st);
+    else diag_t<unsigned long long>(s, T, masks, rows, amps, out64, out32, scratch, st);
 }
 }  // namespace edgpu

@@ -81,18 +81,22 @@ __device__ __forceinline__ int lowest_bit(W m) {
 
 // Entry of the target table at pos (map format: c | sx << cb | g << (cb + sb); all ones when the
 // target's orbit has no representative in the table).
+// stream: load with the evict-first (cache-streaming) policy, so that the table, read once, does not
+// displace lines of x that other rows still gather.
 template <int PREC>
 __device__ __forceinline__ void table_entry(const RowsSector<PREC>& sc, long long pos, bool on, int sb, long long& c,
-                                            int& sx, int& g) {
+                                            int& sx, int& g, bool stream = false) {
     if (!sc.tab_wide) {
-        const unsigned e = on ? __ldg((const unsigned*)sc.tab + pos) : 0xffffffffu;
+        const unsigned* tp = (const unsigned*)sc.tab + pos;
+        const unsigned e = on ? (stream ? __ldcs(tp) : __ldg(tp)) : 0xffffffffu;
         const unsigned cmask = (sc.tab_cb >= 32) ? 0xffffffffu : ((1u << sc.tab_cb) - 1u);
         const unsigned ci = e & cmask;
         c = (ci == cmask) ? -1 : (long long)ci;
         sx = (int)((e >> sc.tab_cb) & ((1u << sb) - 1u));
         g = (int)((e >> (sc.tab_cb + sb)) & 0xfffu);
     } else {
-        const unsigned long long e = on ? __ldg((const unsigned long long*)sc.tab + pos) : ~0ull;
+        const unsigned long long* tp = (const unsigned long long*)sc.tab + pos;
+        const unsigned long long e = on ? (stream ? __ldcs(tp) : __ldg(tp)) : ~0ull;
         const unsigned long long cmask = (1ull << sc.tab_cb) - 1ull;
         const unsigned long long ci = e & cmask;
         c = (ci == cmask) ? -1 : (long long)ci;
@@ -111,6 +115,18 @@ __device__ __forceinline__ void table_prefetch_x(const RowsSector<PREC>& sc, lon
     if (c >= 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(sc.x + c));
 }
 
+// OR of a word over the warp.
+template <typename W>
+__device__ __forceinline__ W warp_or(W v) {
+    if constexpr (sizeof(W) == 8) {
+        const unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)v);
+        const unsigned hi = __reduce_or_sync(0xffffffffu, (unsigned)(v >> 32));
+        return (W)lo | ((W)hi << 32);
+    } else {
+        return (W)__reduce_or_sync(0xffffffffu, (unsigned)v);
+    }
+}
+
 // Matching pairs of every class of the row state b (lpr == 1): the row's number of targets.
 template <typename W, int PREC>
 __device__ __forceinline__ int bond_row_count(W b, const BondTables<W, PREC>& bt, int ncls, int n, W full) {
@@ -124,11 +140,26 @@ __device__ __forceinline__ int bond_row_count(W b, const BondTables<W, PREC>& bt
 // lane and step (2 or 4): their lookups, then their gathers, are issued together.
 //   GK_TABLE  the targets' entries are read from the sector's target table (lpr == 1) in this order;
 //   FILL      the build pass of that table: the entries are looked up with the flavour GK and written
-//             to the table (sc.tab) instead of being gathered and accumulated.
-template <typename W, int GK, int PREC, int NT, bool FILL = false>
+//             to the table (sc.tab) instead of being gathered and accumulated;
+//   UNI       warp-uniform steps (lpr == 1): the warp walks the union of its lanes' matching pairs,
+//             class by class and start bit by start bit, and in every step each lane takes the pairs
+//             of that step its row matches.  Lanes of one step gather the targets of one bond pair of
+//             32 consecutive representatives, which often share a DRAM sector of x (a target whose
+//             representative is itself lies next to the targets of the neighbouring rows), so a warp
+//             issues fewer sector requests than when each lane walks its own matches.  Every lane still
+//             visits its pairs by class, then start bit, so the table positions and the summation
+//             order, hence the results, are the same as without UNI;
+//   GRAD      the coupling gradient fused with the product: every target also adds
+//             Re(conj(gy_r) u x_c), with u its unit-coupling element, to the accumulator of its slot's
+//             coupling (sgrad[coupling][thread], FP64, one slot per thread: no atomics, so the sums
+//             are reproducible), and every diagonal term matching the row adds Re(conj(gy_r) u_t x_r).
+//   ADJ       (1 or 2, with GK_TABLE) the passes that build the adjoint target table: 1 counts every
+//             target on its column, 2 writes row, slot, the row's orbit-size index and the group
+//             element into the column's run.
+template <typename W, int GK, int PREC, int NT, bool FILL = false, bool UNI = false, bool GRAD = false, int ADJ = 0>
 __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W, PREC>& tb,
                                           const BondTables<W, PREC>& bt, const RowsSector<PREC>& sc, long long tile,
-                                          int lane) {
+                                          int lane, double* sgrad = nullptr) {
     typedef typename Cx<PREC>::V V;
     typedef typename Cx<PREC>::R R;
     const W* __restrict__ keys = (const W*)sc.keys;
@@ -142,9 +173,25 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
     const W b = kr >> sb;
     const int ri = (int)(kr & smask);
     V acc = czero<V>();
-    if (!FILL) {
+    V gv = czero<V>();   // GRAD: gy of the row
+    if (!FILL && ADJ == 0) {
         const V xr = act ? x[row] : czero<V>();
         if (act && sub == 0) acc = cmul(sc.diag[row], xr);
+        if (GRAD) {
+            gv = act ? ((const V*)p.gy)[row] : czero<V>();
+            if (act && sub == 0) {
+                const unsigned char* smb = (const unsigned char*)bt.comp - p.o_bcomp;
+                const W* dm = (const W*)(smb + p.o_pdm);
+                const W* dr = (const W*)(smb + p.o_pdr);
+                const double2* du = (const double2*)(smb + p.o_pdu);
+                const int* dc = (const int*)(smb + p.o_pdc);
+                for (int t = 0; t < p.T_d; ++t)
+                    if ((b & dm[t]) == dr[t]) {
+                        const V cu = cmul(from_d2<V>(du[t]), xr);
+                        sgrad[dc[t] * HX_THREADS + threadIdx.x] += (double)(gv.x * cu.x + gv.y * cu.y);
+                    }
+            }
+        }
     }
     const int n = p.nbits;
     const W full = (W)p.full;
@@ -179,11 +226,20 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
     bool cpar = false;   // the current class has terms on parallel bits
     W m = 0;
     while (true) {
-        // lanes whose class ran out move on to their next class with matching pairs
-        while (m == 0 && cls + 1 < ncls) {
-            ++cls;
-            m = bond_class_mask<W, PREC>(b, bt, cls, n, full) & split;
-            cpar = (bt.ninfo[cls] >> 8) != 0;
+        if constexpr (UNI) {
+            // the warp moves on to the next class once no lane has pairs left in this one
+            while (!__any_sync(0xffffffffu, m != 0) && cls + 1 < p.bond_ncls) {
+                ++cls;
+                m = act ? (bond_class_mask<W, PREC>(b, bt, cls, n, full) & split) : (W)0;
+                cpar = (bt.ninfo[cls] >> 8) != 0;
+            }
+        } else {
+            // lanes whose class ran out move on to their next class with matching pairs
+            while (m == 0 && cls + 1 < ncls) {
+                ++cls;
+                m = bond_class_mask<W, PREC>(b, bt, cls, n, full) & split;
+                cpar = (bt.ninfo[cls] >> 8) != 0;
+            }
         }
         if (!__any_sync(0xffffffffu, m != 0)) break;
         int ti[NT];
@@ -191,11 +247,22 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
         W q[NT];
         int g[NT], sx[NT];
         long long c[NT];
+        W u = 0;   // UNI: the pairs of this class some lane of the warp still has to visit
+        if constexpr (UNI) u = warp_or<W>(m);
 #pragma unroll
         for (int h = 0; h < NT; ++h) {
-            on[h] = m != 0;
-            const int i = on[h] ? lowest_bit<W>(m) : 0;
-            m &= m - 1;
+            int i;
+            if constexpr (UNI) {
+                const bool any = u != 0;
+                i = any ? lowest_bit<W>(u) : 0;
+                u &= u - 1;
+                on[h] = any && ((m >> i) & 1);
+                if (on[h]) m &= ~((W)1 << i);
+            } else {
+                on[h] = m != 0;
+                i = on[h] ? lowest_bit<W>(m) : 0;
+                m &= m - 1;
+            }
             ti[h] = on[h] ? cls * n + i : 0;
             // (a table read needs the flip mask only for the parallel test)
             const W f = (GK != GK_TABLE || cpar) ? bt.flip[ti[h]] : (W)0;
@@ -208,7 +275,7 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
         if constexpr (GK == GK_TABLE) {
 #pragma unroll
             for (int h = 0; h < NT; ++h) {
-                table_entry<PREC>(sc, tpos, on[h], sb, c[h], sx[h], g[h]);
+                table_entry<PREC>(sc, tpos, on[h], sb, c[h], sx[h], g[h], p.bond_near > 0);
                 tpos += on[h] ? 1 : 0;
             }
             if (!FILL && p.bond_pf > 0) {
@@ -219,6 +286,20 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
 #pragma unroll
             for (int h = 0; h < NT; h += 2)
                 resolve_targets2<W, GK, PREC>(p, tb, sc, q + h, on + h, c + h, sx + h, g + h);
+        }
+        if constexpr (ADJ != 0) {
+#pragma unroll
+            for (int h = 0; h < NT; ++h) {
+                if (!on[h] || c[h] < 0) continue;
+                if (ADJ == 1) {
+                    atomicAdd(p.adj_cnt + c[h], 1u);
+                } else {
+                    const long long pos = p.adj_off[c[h]] + (long long)atomicAdd(p.adj_cur + c[h], 1u);
+                    p.adj_tab[pos] = ((unsigned long long)row << 32) | ((unsigned long long)ti[h] << 19) |
+                                     ((unsigned long long)ri << 14) | (unsigned long long)(g[h] & 0x3fff);
+                }
+            }
+            continue;
         }
         if constexpr (FILL) {
             const bool with_g = sc.want_arg;
@@ -237,10 +318,32 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
             continue;
         }
         V xv[NT];
+        if (GK == GK_TABLE && p.bond_near > 0) {
+            // near targets (column within bond_near rows of the row: the window the warps in flight
+            // share) keep the default policy; far ones are streamed (evict-first) so that they do not
+            // push the near window out of L2
 #pragma unroll
-        for (int h = 0; h < NT; ++h) xv[h] = (c[h] >= 0) ? x[c[h]] : czero<V>();
+            for (int h = 0; h < NT; ++h) {
+                const long long d = c[h] - row;
+                xv[h] = (c[h] < 0) ? czero<V>() : ((d < p.bond_near && d > -p.bond_near) ? x[c[h]] : __ldcs(x + c[h]));
+            }
+        } else {
+#pragma unroll
+            for (int h = 0; h < NT; ++h) xv[h] = (c[h] >= 0) ? x[c[h]] : czero<V>();
+        }
 #pragma unroll
         for (int h = 0; h < NT; ++h) {
+            if (GRAD && c[h] >= 0) {
+                const unsigned char* smb = (const unsigned char*)bt.comp - p.o_bcomp;
+                V u = ((const V*)(smb + p.o_bunit))[ti[h]];
+                if (GK != GK_TRIVIAL) {
+                    if (sc.want_arg) u = cmul(u, sc.ph[sc.num[g[h]]]);
+                    u = cscale(u, rrow[sx[h]]);
+                }
+                const V t = cmul(u, xv[h]);
+                const int cid = ((const int*)(smb + p.o_bcid))[ti[h]];
+                sgrad[cid * HX_THREADS + threadIdx.x] += (double)(gv.x * t.x + gv.y * t.y);
+            }
             if (c[h] >= 0) {
                 const V a = bt.amp[ti[h]];
                 if (GK == GK_TRIVIAL) {
@@ -264,7 +367,7 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
             }
         }
     }
-    if (FILL) return;
+    if (FILL || ADJ != 0) return;
     // partial sums of the row's lanes (fixed butterfly order)
     for (int d = 1; d < lpr; d <<= 1) acc = cadd(acc, shfl_xor_v(acc, d));
     if (act && sub == 0) {
@@ -286,7 +389,7 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
     }
 }
 
-template <typename W, int GK, int PREC, int NT>
+template <typename W, int GK, int PREC, int NT, bool UNI = false>
 __global__ void __launch_bounds__(HX_THREADS) hx_bond_kernel(const HxParams p) {
     typedef typename Cx<PREC>::V V;
     extern __shared__ __align__(16) unsigned char sm[];
@@ -325,7 +428,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_bond_kernel(const HxParams p) {
     const int rpw = 32 / p.lpr;
     const long long n_tiles = (p.n_rows + rpw - 1) / rpw;
     for (long long tile = (long long)blockIdx.x * wpb + warp; tile < n_tiles; tile += (long long)gridDim.x * wpb)
-        bond_tile<W, GK, PREC, NT>(p, tb, bt, sc, tile, lane);
+        bond_tile<W, GK, PREC, NT, false, UNI>(p, tb, bt, sc, tile, lane);
 }
 
 // All sectors of a batch in one persistent launch (the tile numbering of hx_multi_kernel).
@@ -378,6 +481,54 @@ __global__ void __launch_bounds__(HX_THREADS, 4) hx_bond_multi_kernel(const HxPa
     }
 }
 
+// The product fused with the coupling gradient (GRAD), one sector; GK is GK_MAP or GK_TABLE.  Shared
+// memory: the pair-flip image, then n_couplings x HX_THREADS FP64 accumulators (p.o_grad); each
+// block writes its sums, reduced over its threads in a fixed order, to grad_partial[block][coupling].
+template <typename W, int GK, int PREC, int NT>
+__global__ void __launch_bounds__(HX_THREADS) hx_bond_grad_kernel(const HxParams p) {
+    typedef typename Cx<PREC>::V V;
+    extern __shared__ __align__(16) unsigned char sm[];
+    {
+        const int4* src = (const int4*)p.blob;
+        int4* dst = (int4*)sm;
+        for (int i = threadIdx.x; i < p.blob_words16; i += blockDim.x) dst[i] = src[i];
+    }
+    double* sgrad = (double*)(sm + p.o_grad);
+    for (int i = threadIdx.x; i < p.n_coupl * HX_THREADS; i += blockDim.x) sgrad[i] = 0.0;
+    __syncthreads();
+    const RowsTables<W, PREC> tb(p, sm);
+    const BondTables<W, PREC> bt(p, sm);
+    RowsSector<PREC> sc;
+    sc.keys = p.keys;
+    sc.x = (const V*)p.x;
+    sc.y = (V*)p.y;
+    sc.diag = (const V*)p.diag;
+    sc.n_rows = p.n_rows;
+    sc.ds = p.ds;
+    sc.ph = (const V*)(sm + p.o_ph);
+    sc.num = (const int*)(sm + p.o_num);
+    sc.want_arg = p.want_arg != 0;
+    sc.map = p.map;
+    sc.map_wide = p.map_wide;
+    sc.map_cb = p.map_cb;
+    sc.map_direct = p.map_direct;
+    sc.tab = p.tab;
+    sc.tile_off = p.tile_off;
+    sc.tab_wide = p.tab_wide;
+    sc.tab_cb = p.tab_cb;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    const int rpw = 32 / p.lpr;
+    const long long n_tiles = (p.n_rows + rpw - 1) / rpw;
+    for (long long tile = (long long)blockIdx.x * wpb + warp; tile < n_tiles; tile += (long long)gridDim.x * wpb)
+        bond_tile<W, GK, PREC, NT, false, false, true>(p, tb, bt, sc, tile, lane, sgrad);
+    __syncthreads();
+    for (int i = threadIdx.x; i < p.n_coupl; i += blockDim.x) {
+        double sum = 0.0;
+        for (int t = 0; t < HX_THREADS; ++t) sum += sgrad[i * HX_THREADS + t];
+        p.grad_partial[(size_t)blockIdx.x * p.n_coupl + i] = sum;
+    }
+}
+
 // Launch with programmatic stream serialisation: the kernel may begin while the previous kernel in
 // the stream finishes (it waits for it with griddepcontrol.wait before reading any vector).
 template <typename K>
@@ -395,21 +546,17 @@ void pdl_launch(K kern, const HxParams& p, int blocks, size_t smem, cudaStream_t
     EDGPU_CUDA(cudaLaunchKernelEx(&cfg, kern, p));
 }
 
-template <typename W, int GK, int PREC, int NT>
+template <typename W, int GK, int PREC, int NT, bool UNI = false>
 void hx_bond_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
-    auto kern = hx_bond_kernel<W, GK, PREC, NT>;
-    static size_t smem_set = 0;   // raised once per kernel, never inside a graph capture
-    if (smem > smem_set) {
-        EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        smem_set = smem;
-    }
+    auto kern = hx_bond_kernel<W, GK, PREC, NT, UNI>;
+    raise_smem_limit((const void*)kern, smem);
     pdl_launch(kern, p, blocks, smem, st);
 }
 
-template <typename W, int GK, int PREC, int NT>
+template <typename W, int GK, int PREC, int NT, bool UNI = false>
 int hx_bond_occupancy_one(size_t smem) {
-    auto kern = hx_bond_kernel<W, GK, PREC, NT>;
-    EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    auto kern = hx_bond_kernel<W, GK, PREC, NT, UNI>;
+    raise_smem_limit((const void*)kern, smem);
     int n = 0;
     EDGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, HX_THREADS, smem));
     return n;
@@ -418,18 +565,35 @@ int hx_bond_occupancy_one(size_t smem) {
 template <typename W, int GK, int PREC, int NT>
 void hx_bond_multi_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
     auto kern = hx_bond_multi_kernel<W, GK, PREC, NT>;
-    static size_t smem_set = 0;
-    if (smem > smem_set) {
-        EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        smem_set = smem;
-    }
+    raise_smem_limit((const void*)kern, smem);
     pdl_launch(kern, p, blocks, smem, st);
 }
 
 template <typename W, int GK, int PREC, int NT>
 int hx_bond_multi_occupancy_one(size_t smem) {
     auto kern = hx_bond_multi_kernel<W, GK, PREC, NT>;
-    EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    raise_smem_limit((const void*)kern, smem);
+    int n = 0;
+    EDGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, HX_THREADS, smem));
+    return n;
+}
+
+}  // namespace edgpu
+
+namespace edgpu {
+
+template <typename W, int GK, int PREC, int NT>
+void hx_bond_grad_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
+    auto kern = hx_bond_grad_kernel<W, GK, PREC, NT>;
+    raise_smem_limit((const void*)kern, smem);
+    kern<<<blocks, HX_THREADS, smem, st>>>(p);
+    EDGPU_CUDA(cudaGetLastError());
+}
+
+template <typename W, int GK, int PREC, int NT>
+int hx_bond_grad_occupancy_one(size_t smem) {
+    auto kern = hx_bond_grad_kernel<W, GK, PREC, NT>;
+    raise_smem_limit((const void*)kern, smem);
     int n = 0;
     EDGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, HX_THREADS, smem));
     return n;

@@ -49,6 +49,8 @@ __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_doub
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 template <typename V>
 __device__ __forceinline__ V czero();
 template <>
@@ -344,11 +346,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_kernel(const HxParams p) {
 template <typename W, int GK, int PREC, int MODE>
 void hx_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
     auto kern = hx_kernel<W, GK, PREC, MODE>;
-    static size_t smem_set = 0;   // the attribute is raised once per kernel, never inside a graph capture
-    if (smem > smem_set) {
-        EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        smem_set = smem;
-    }
+    raise_smem_limit((const void*)kern, smem);
     kern<<<blocks, HX_THREADS, smem, st>>>(p);
     EDGPU_CUDA(cudaGetLastError());
 }
@@ -356,7 +354,7 @@ void hx_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t st) 
 template <typename W, int GK, int PREC, int MODE>
 int hx_occupancy_one(size_t smem) {
     auto kern = hx_kernel<W, GK, PREC, MODE>;
-    EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    raise_smem_limit((const void*)kern, smem);
     int n = 0;
     EDGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, HX_THREADS, smem));
     return n;

@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_scatter_adjoint_kernel(const Hx
 template <typename W, int GK, int PREC>
 void hx_scatter_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
     auto kern = hx_scatter_adjoint_kernel<W, GK, PREC>;
-    EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    raise_smem_limit((const void*)kern, smem);
     kern<<<blocks, HX_THREADS, smem, st>>>(p);
     EDGPU_CUDA(cudaGetLastError());
 }
@@ -532,7 +532,7 @@ void hx_sparse_launch_one(const HxParams& p, long long row0, long long n_run, in
                           long long* counts, const long long* row_ptr, long long* cols, double2* vals, size_t smem,
                           cudaStream_t st) {
     auto kern = hx_sparse_kernel<W, GK>;
-    EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    raise_smem_limit((const void*)kern, smem);
     const long long warps = n_run;
     const int blocks = (int)std::max<long long>(1, std::min<long long>((warps + 3) / 4, 152ll * 16));
     kern<<<blocks, SPARSE_THREADS, smem, st>>>(p, row0, n_run, conj_vals, tol, counts, row_ptr, cols, vals);
@@ -542,11 +542,7 @@ void hx_sparse_launch_one(const HxParams& p, long long row0, long long n_run, in
 template <typename W, int GK, int PREC>
 void hx_multi_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
     auto kern = hx_multi_kernel<W, GK, PREC>;
-    static size_t smem_set = 0;   // raised once per kernel, never inside a graph capture
-    if (smem > smem_set) {
-        EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        smem_set = smem;
-    }
+    raise_smem_limit((const void*)kern, smem);
     kern<<<blocks, HX_THREADS, smem, st>>>(p);
     EDGPU_CUDA(cudaGetLastError());
 }
@@ -554,7 +550,7 @@ void hx_multi_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_
 template <typename W, int GK, int PREC>
 int hx_multi_occupancy_one(size_t smem) {
     auto kern = hx_multi_kernel<W, GK, PREC>;
-    EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    raise_smem_limit((const void*)kern, smem);
     int n = 0;
     EDGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, HX_THREADS, smem));
     return n;
@@ -563,11 +559,7 @@ int hx_multi_occupancy_one(size_t smem) {
 template <typename W, int GK, int PREC, int MODE>
 void hx_rows_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t st) {
     auto kern = hx_rows_kernel<W, GK, PREC, MODE>;
-    static size_t smem_set = 0;   // raised once per kernel, never inside a graph capture
-    if (smem > smem_set) {
-        EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        smem_set = smem;
-    }
+    raise_smem_limit((const void*)kern, smem);
     kern<<<blocks, HX_THREADS, smem, st>>>(p);
     EDGPU_CUDA(cudaGetLastError());
 }
@@ -575,7 +567,7 @@ void hx_rows_launch_one(const HxParams& p, int blocks, size_t smem, cudaStream_t
 template <typename W, int GK, int PREC, int MODE>
 int hx_rows_occupancy_one(size_t smem) {
     auto kern = hx_rows_kernel<W, GK, PREC, MODE>;
-    EDGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    raise_smem_limit((const void*)kern, smem);
     int n = 0;
     EDGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, HX_THREADS, smem));
     return n;

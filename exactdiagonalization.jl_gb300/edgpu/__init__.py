@@ -14,5 +14,6 @@ from .representation import (Batch, DirectProductOperation, GlobalBitFlip, Hilbe
                              apply_, coupling_grad, dimension, mul_, mul_adjoint_, random_state, represent, search_stats,
                              symmetry_apply, symmetry_reduce, symmetry_unreduce, translation_symops)
 from .lanczos import LanczosResult, lanczos, set_krylov_limit
+from .autograd import apply_hamiltonian
 
 lib()   # fail loudly at import when libedgpu.so is missing

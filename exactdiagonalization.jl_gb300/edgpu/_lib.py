@@ -14,6 +14,7 @@ LIB_PATH = os.environ.get("EDGPU_LIBRARY") or os.path.join(HERE, "libedgpu.so")
 OK, ERR_ARG, ERR_DIM, ERR_BOUNDS, ERR_KEY, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_STATE = range(9)
 FP64, MIXED = 0, 1
 SPACE_LAZY = 1
+PAIR_UNIFORM = 16   # EDGPU_PAIR_UNIFORM: warp-uniform pair steps of the target-table product
 
 
 class ArgumentError(ValueError):
@@ -77,6 +78,9 @@ SIGNATURES = {
     "edgpu_op_build_targets": (ctypes.c_int, [vp, i64, P(i32)]),
     "edgpu_op_free_targets": (ctypes.c_int, [vp]),
     "edgpu_op_targets_info": (ctypes.c_int, [vp, P(i64), P(i32)]),
+    "edgpu_op_build_adjoint_targets": (ctypes.c_int, [vp, i64, P(i32)]),
+    "edgpu_op_near_window": (ctypes.c_int, [vp, i32, i64, P(i64)]),
+    "edgpu_op_free_adjoint_targets": (ctypes.c_int, [vp]),
     "edgpu_batch_get_schedule": (ctypes.c_int, [vp, i32, P(i32), P(i32), P(i32)]),
     "edgpu_op_sparse": (ctypes.c_int, [vp, i32, dbl, P(i64), P(i64), P(i64), P(dbl)]),
     "edgpu_op_get_row": (ctypes.c_int, [vp, i32, i64, dbl, i64, P(i64), P(i64), P(dbl)]),

@@ -4,10 +4,16 @@ dense eigvals or an external Arpack.eigs that calls mul! repeatedly, docs/src/ex
 FP64 throughout for the scalars, dot products, norms, reorthogonalisation and the tridiagonal
 eigensolve; `precision` selects the product (fp64, or mixed: complex64 vectors and FP32
 accumulation).  tol > 0 stops a run once the lowest Ritz value moved by less than tol |E| over five
-steps.  With refine=True a mixed-precision run to about 1e-7 is followed by FP64 Lanczos from its Ritz
-vector until the eigenvalue settles to tol.  The Krylov basis is kept only when reorthogonalisation
-or a Ritz vector needs it and it fits (see set_krylov_limit); otherwise a Ritz vector is rebuilt by a
-second pass of the recurrence.
+steps.  With refine=True (mixed precision) the mixed-precision run settles its lowest Ritz value to
+max(tol, 1e-9), then one FP64 product gives the Rayleigh quotient E_RQ = <psi|H psi> of its Ritz vector
+psi and the residual r = H psi - E_RQ psi; E_RQ is returned when the Kato-Temple estimate
+|r|^2 / (theta_2 - E_RQ) (theta_2: the second Ritz value of the mixed run) is below
+tol max(1, |E_RQ|), else
+FP64 Lanczos restarts from psi until the eigenvalue settles to tol.  The Krylov basis is kept only
+when reorthogonalisation or a Ritz vector needs it and it fits (see set_krylov_limit): in FP64 for an
+FP64 run, as the complex64 product inputs for a mixed run (reorthogonalisation then uses those
+complex64-rounded vectors with FP64 arithmetic); otherwise a Ritz vector is rebuilt by a second pass of
+the recurrence.
 """
 from __future__ import annotations
 

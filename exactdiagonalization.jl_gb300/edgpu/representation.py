@@ -26,7 +26,7 @@ from typing import List, Optional, Sequence, Tuple
 import numpy as np
 
 from . import _lib
-from ._lib import (ArgumentError, BoundsError, DimensionMismatch, FP64, MIXED, check, lib, ptr)
+from ._lib import (ArgumentError, BoundsError, DimensionMismatch, FP64, MIXED, PAIR_UNIFORM, check, lib, ptr)
 from .hilbert import HilbertSpace, HilbertSpaceSector, basespace
 from .operators import NullOperator, RTOL, simplify, term_arrays
 
@@ -493,6 +493,7 @@ class OperatorRepresentation:
                                     ptr(a, ctypes.c_double), ptr(cid, ctypes.c_int32),
                                     self.n_couplings, ptr(cvals, ctypes.c_double), ctypes.byref(h)))
         self._h = h
+        self._couplings = np.ones(1) if cvals is None else cvals.copy()
 
     @classmethod
     def from_terms(cls, space, masks, rows, cols, amps, coupling_ids=None, couplings=None):
@@ -517,6 +518,7 @@ class OperatorRepresentation:
                                     ptr(amps.view(np.float64), ctypes.c_double), ptr(cid, ctypes.c_int32),
                                     self.n_couplings, ptr(cvals, ctypes.c_double), ctypes.byref(h)))
         self._h = h
+        self._couplings = np.ones(1) if cvals is None else cvals.copy()
         return self
 
     def __del__(self):
@@ -546,8 +548,15 @@ class OperatorRepresentation:
         return (self.space.dimension, self.space.dimension)
 
     def set_couplings(self, values):
+        """New coupling values J_c (same count); the operator's tables are rewritten in place."""
         v = np.ascontiguousarray(values, dtype=np.float64)
         check(lib().edgpu_op_set_couplings(self._h, ptr(v, ctypes.c_double), int(v.size)))
+        self._couplings = v.copy()
+
+    @property
+    def couplings(self) -> np.ndarray:
+        """The current coupling values (a copy)."""
+        return self._couplings.copy()
 
     def autotune(self, precision="mixed"):
         r = ctypes.c_int32()
@@ -564,16 +573,19 @@ class OperatorRepresentation:
     def set_tiling(self, precision, rows_per_tile):
         check(lib().edgpu_op_set_tiling(self._h, _prec(precision), int(rows_per_tile)))
 
-    def set_pair_schedule(self, enable, targets_per_step: int = 2):
+    def set_pair_schedule(self, enable, targets_per_step: int = 2, uniform: bool = False):
         """Use (default) or bypass the pair-flip schedule of the product for operators whose
         off-diagonal terms all flip two spin-1/2 sites; bypassed, every row tests every term.
         targets_per_step: 2, 4 (with a parent-state map or a target table) or 8 (with a target
-        table)."""
-        check(lib().edgpu_op_set_pair_schedule(self._h, int(targets_per_step) if enable else 0))
+        table).  uniform: warp-uniform pair steps of the target-table product (4 or 8 targets per
+        step; same results)."""
+        code = (int(targets_per_step) | (PAIR_UNIFORM if uniform else 0)) if enable else 0
+        check(lib().edgpu_op_set_pair_schedule(self._h, code))
 
     def schedule(self, precision="mixed"):
         """(rows_per_tile as in set_tiling, pair flips) used by the product: pair flips = 0 when
-        every row tests every term, else the targets per lane and step of the pair-flip schedule."""
+        every row tests every term, else the targets per lane and step of the pair-flip schedule
+        (with PAIR_UNIFORM added for warp-uniform steps)."""
         a, b = ctypes.c_int32(), ctypes.c_int32()
         check(lib().edgpu_op_get_schedule(self._h, _prec(precision), ctypes.byref(a), ctypes.byref(b), None))
         return int(a.value), int(b.value)
@@ -594,6 +606,29 @@ class OperatorRepresentation:
         built = ctypes.c_int32()
         check(lib().edgpu_op_build_targets(self._h, int(max_bytes), ctypes.byref(built)))
         return bool(built.value)
+
+    def near_window(self, precision="mixed", rows: Optional[int] = None) -> int:
+        """Cache policy of the target-table product: with rows > 0 the table and the gathers of targets
+        at least `rows` rows from their row are streamed (evict-first) so that L2 keeps the shared
+        window of x; 0 turns it off.  Returns the setting (after setting it when rows is given)."""
+        cur = ctypes.c_int64()
+        check(lib().edgpu_op_near_window(self._h, _prec(precision), -1 if rows is None else int(rows), ctypes.byref(cur)))
+        return int(cur.value)
+
+    def build_adjoint_targets(self, max_bytes: Optional[int] = None) -> bool:
+        """Build the adjoint target table (needs the target table): for terms that do not commute with
+        the symmetry group, mul_adjoint_ then gathers every column's contributions in a fixed order
+        instead of scattering them with atomics.  Returns whether it was built."""
+        if max_bytes is None:
+            import torch
+            free, _ = torch.cuda.mem_get_info()
+            max_bytes = free // 2
+        built = ctypes.c_int32()
+        check(lib().edgpu_op_build_adjoint_targets(self._h, int(max_bytes), ctypes.byref(built)))
+        return bool(built.value)
+
+    def free_adjoint_targets(self) -> None:
+        check(lib().edgpu_op_free_adjoint_targets(self._h))
 
     def free_targets(self) -> None:
         check(lib().edgpu_op_free_targets(self._h))

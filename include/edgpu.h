@@ -23,8 +23,12 @@
  *     EDGPU_FP64 and complex64 for EDGPU_MIXED.
  *   - Device-buffer entry points take a cudaStream_t as void* (NULL = the CUDA default stream) and
  *     are asynchronous on it; host-buffer entry points return after the result is in host memory.
- *   - Handles are not thread-safe for concurrent calls on the same handle;
- *     distinct handles may be used from different threads.
+ *   - Threading: every handle (space, operator, batch) owns a lock and its own CUDA stream.  Calls
+ *     on one handle are serialised by its lock; calls on distinct handles run concurrently from
+ *     different host threads.  Calls without a stream argument (builds, host-buffer products, the
+ *     autotuners, Lanczos) run on the handle's own stream; a call blocks only its calling thread.
+ *     An operator's calls also take its space's lock while they enqueue work, so a space's
+ *     parent-state map cannot be freed while a product is being issued on it.
  */
 #ifndef EDGPU_H
 #define EDGPU_H
@@ -142,7 +146,9 @@ int edgpu_space_orbit_sizes(edgpu_space reduced, int32_t* out, int64_t n);
 int edgpu_op_create(edgpu_space s, int32_t n_terms, const uint64_t* masks, const uint64_t* rows,
                     const uint64_t* cols, const double* amps, const int32_t* coupling_ids,
                     int32_t n_couplings, const double* couplings, edgpu_op* out);
-/* Change the coupling values of an operator created with coupling_ids. */
+/* Change the coupling values of an operator created with coupling_ids.  Tables already built are
+ * rewritten in place (same device buffers, nothing allocated) after the device has finished the work
+ * that may read the old values; the target table does not depend on coupling values and is kept. */
 int edgpu_op_set_couplings(edgpu_op op, const double* couplings, int32_t n_couplings);
 int edgpu_op_dim(edgpu_op op, int64_t* out);
 void edgpu_op_destroy(edgpu_op op);
@@ -163,6 +169,12 @@ int edgpu_op_autotune(edgpu_op op, int32_t precision, int32_t* rows_per_tile_out
  * parent-state map or a target table, 8 with a target table; 1 = 2).  edgpu_op_autotune may change
  * the choice. */
 int edgpu_op_set_pair_schedule(edgpu_op op, int32_t enable);
+/* Flag of edgpu_op_set_pair_schedule (with 4 or 8 targets per step) and of the pair_flips output of
+ * edgpu_op_get_schedule: the target-table product walks warp-uniform steps -- the 32 lanes of a warp
+ * step through the union of their rows' matching pairs together, so that the gathers of one step
+ * are the targets of one bond pair across 32 consecutive representatives and share DRAM sectors more
+ * often.  The visiting order of every row, hence the result, is unchanged. */
+#define EDGPU_PAIR_UNIFORM 16
 /* Bond classes of the pair-flip schedule for this operator (0 when the terms do not allow it) and
  * their rotation components in total. */
 int edgpu_op_pair_classes(edgpu_op op, int32_t* n_classes, int32_t* n_components);
@@ -177,7 +189,8 @@ int edgpu_pair_classes_of_terms(int32_t n_bits, int32_t n_terms, const uint64_t*
                                 int32_t* info, uint64_t* comps, uint64_t* flips, double* class_amps);
 /* The schedule the product uses for this precision: rows_per_tile as in edgpu_op_set_tiling (0 =
  * default), pair_flips = 0 when every row tests every term, else the targets each lane looks up per
- * step in the pair-flip schedule (2; 4 with a parent-state map or a target table; 8 with a table), and
+ * step in the pair-flip schedule (2; 4 with a parent-state map or a target table; 8 with a table),
+ * with EDGPU_PAIR_UNIFORM set for warp-uniform steps, and
  * target_table = 1 when the product reads the target table; every pointer nullable. */
 int edgpu_op_get_schedule(edgpu_op op, int32_t precision, int32_t* rows_per_tile, int32_t* pair_flips,
                           int32_t* target_table);
@@ -191,6 +204,20 @@ int edgpu_op_get_schedule(edgpu_op op, int32_t precision, int32_t* rows_per_tile
  * allow the pair-flip schedule and the table needs at most max_bytes; *built = 0 otherwise. */
 int edgpu_op_build_targets(edgpu_op op, int64_t max_bytes, int32_t* built);
 int edgpu_op_free_targets(edgpu_op op);
+/* Cache policy of the target-table product for this precision: rows > 0 loads the table, and the x of
+ * every target whose column is at least `rows` rows away from its row, with the evict-first
+ * (streaming) policy, so that L2 keeps the window of x that the rows in flight share; 0 uses the
+ * default policy everywhere; rows < 0 only queries.  *current (nullable) receives the setting.  The
+ * autotuner chooses it for sectors whose x exceeds a quarter of L2.  Results do not depend on it. */
+int edgpu_op_near_window(edgpu_op op, int32_t precision, int64_t rows, int64_t* current);
+/* Adjoint target table (no reference counterpart): for every column c of the product's matrix, the
+ * rows r whose targets land on c with their slots, sorted.  It serves edgpu_mul_adjoint_device for
+ * terms that do not commute with the group (whose adjoint is not the row formula of the adjoint
+ * terms): y[c] = sum conj(H[r, c]) x[r] is then a gather in a fixed order (reproducible bit for bit)
+ * instead of a scatter with atomics.  Built from the operator's target table (which must exist) when
+ * it needs at most max_bytes (8 bytes per nonzero plus 8 per row); *built = 0 otherwise. */
+int edgpu_op_build_adjoint_targets(edgpu_op op, int64_t max_bytes, int32_t* built);
+int edgpu_op_free_adjoint_targets(edgpu_op op);
 /* Entries of the target table and bytes per entry; 0 and 0 without a table. */
 int edgpu_op_targets_info(edgpu_op op, int64_t* entries, int32_t* entry_bytes);
 /* Sparse matrix of the representation, assembled on the device in FP64: rows sorted by column,
@@ -238,7 +265,12 @@ int edgpu_op_is_invariant(edgpu_op op, int32_t* invariant);
 int edgpu_mul_adjoint_device(edgpu_op op, int32_t precision, const void* x, void* y, int64_t n,
                              int32_t accumulate, void* stream);
 /* dL/dJ_c = Re <gy | H_c x> for every coupling c (H = sum_c J_c H_c), fused with y = H x
- * (y may be NULL).  grad_out: n_couplings doubles in HOST memory.  Device vectors. */
+ * (y may be NULL).  grad_out: n_couplings doubles in HOST memory.  Device vectors.  With a target table
+ * (or a parent-state map) and pair-flip terms whose every (pair, pattern) slot belongs to one coupling,
+ * the pair-flip kernel runs it; otherwise the term scan.  Both accumulate per thread in FP64 and reduce
+ * per block in a fixed order (reproducible bit for bit) while n_couplings x 2 KiB fits in shared
+ * memory (about 90 couplings); beyond that the queued term scan adds per block with shared-memory
+ * atomics (reproducible only to rounding). */
 int edgpu_coupling_grad_device(edgpu_op op, int32_t precision, const void* x, const void* gy, void* y,
                                int64_t n, double* grad_out, void* stream);
 
@@ -247,11 +279,15 @@ int edgpu_coupling_grad_device(edgpu_op op, int32_t precision, const void* x, co
  * allocation out of a time-step loop).  This entry point has no counterpart in the reference.  It
  * allocates nothing: its scratch is a 2 MiB array inside the library (held on every GPU that loads
  * the library), shared by all calls, so calls that overlap on the GPU race and must be serialised by
- * the caller.  y is required.  Limit: n_couplings <= 131072 (2 doubles each in the scratch).  The operator's gradient tables must have
- * been built by one earlier edgpu_coupling_grad_device call with the same precision (EDGPU_ERR_STATE
- * otherwise).  The first call on a device looks up the scratch address (cudaGetSymbolAddress); make
- * that first call before any stream capture.  grad_out: host memory; the call returns after it is
- * written. */
+ * the caller.  It launches the kernel edgpu_coupling_grad_device would (same schedule); the block
+ * count is limited to what the scratch holds (2^18 / n_couplings - 1 blocks), which changes only the
+ * order in which per-block partial sums are added.  y is required.  The operator's tables for this
+ * precision must have been built by one earlier edgpu_coupling_grad_device call (EDGPU_ERR_STATE
+ * otherwise); edgpu_op_set_couplings rewrites them in place, so coupling changes keep them built and
+ * allocate nothing.  n_couplings is at most 8192 (set at operator creation).  The first call on a
+ * device looks up the scratch address (cudaGetSymbolAddress).  grad_out is host memory: the call
+ * synchronises its stream before returning, so it must not be issued while that stream is being
+ * captured into a CUDA graph. */
 int edgpu_coupling_grad_device_noalloc(edgpu_op op, int32_t precision, const void* x, const void* gy, void* y,
                                        int64_t n, double* grad_out, void* stream);
 
@@ -287,8 +323,10 @@ void edgpu_batch_destroy(edgpu_batch b);
  * start vector (or v0, host complex128 of length dim, if not NULL), full reorthogonalisation when
  * reorth != 0.  Scalars, dots, norms and the tridiagonal eigensolve are FP64; precision selects the
  * product.  tol > 0 stops once the lowest Ritz value moved by less than tol |E| over the last 5 steps.  With
- * refine != 0 and EDGPU_MIXED: a mixed-precision run to about 1e-7, then FP64 Lanczos from its Ritz
- * vector until the eigenvalue settles to tol.  Outputs: e0, alphas/betas of the last run (n_steps
+ * refine != 0 and EDGPU_MIXED: a mixed-precision run settled to max(tol, 1e-9), then one FP64 product
+ * gives the Rayleigh quotient E_RQ of its Ritz vector psi and the residual r = H psi - E_RQ psi; E_RQ is
+ * returned when the Kato-Temple estimate |r|^2 / (theta_2 - E_RQ) (theta_2 the second Ritz value) is at
+ * most tol max(1, |E_RQ|), else FP64 Lanczos continues from psi until the eigenvalue settles to tol.  Outputs: e0, alphas/betas of the last run (n_steps
  * each, nullable), steps_done (all runs).  ground_state (nullable, host complex128 dim): Ritz vector.
  * The Krylov basis is stored (FP64, or the complex64 product inputs of a mixed run) only when
  * reorthogonalisation or a Ritz vector needs it and it fits under the Krylov limit (EDGPU_ERR_OOM when
@@ -306,7 +344,8 @@ int edgpu_set_krylov_limit(int64_t bytes);
 /* Seeded complex Gaussian vector (SplitMix64 + Box-Muller, (g1 + i g2)/sqrt(2), normalised in FP64)
  * written to a DEVICE buffer as complex128 (precision EDGPU_FP64) or complex64 (EDGPU_MIXED). */
 int edgpu_random_vector_device(int64_t n, uint64_t seed, int32_t precision, void* dst, void* stream);
-/* Synchronise the library stream. */
+/* Wait for all work the library has enqueued on the current device (every handle stream and every
+ * caller stream): a device-wide synchronisation. */
 int edgpu_sync(void);
 /* Pinned host memory for the host-buffer entry points (cudaMallocHost / cudaFreeHost). */
 int edgpu_host_alloc(int64_t bytes, void** out);

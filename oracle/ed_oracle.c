@@ -302,3 +302,221 @@ int64_t or_popcount_basis(int n, int k, uint64_t* out, int64_t cap) {
     }
     return cnt;
 }
+
+/* ---- the reference's tables evaluated for one orbit at a time --------------------------------
+ * symmetry_reduce_generic.jl:22-106 fills basis_mapping_index / basis_mapping_amplitude for every
+ * parent state in one ascending sweep.  For sectors whose parent-sized tables do not fit in host
+ * memory (the 6x6 torus: 9.1e9 parent states, ~290 GB of tables), the entries a row needs are
+ * evaluated here for the orbit of one state, with the same semantics:
+ *   - the sweep meets an orbit first at its minimum, which becomes the representative (:50-51, :72);
+ *   - the orbit is kept only if every g with g.rep == rep has amplitude ~1 (:55-64, atol = tol);
+ *   - the "Dict" of members keeps the LAST element i with g_i.rep == q (:74-78), so q's amplitude is
+ *     conj(y_i) of that i over sqrt(#distinct members) (:39, :79-85).
+ * Restricted to parents that are one popcount sector of 1-bit sites (every spin-1/2 2Sz sector):
+ * get(basis_lookup, bcol, -1) on such a parent is -1 exactly when popcount(bcol) differs. */
+typedef struct { uint64_t rep; int compatible; int n_distinct; cplx ampl; } orbit_info;
+
+static orbit_info orbit_of(uint64_t q, int n_sites, const int32_t* bw, const int32_t* off, int G,
+                           const int32_t* maps, const uint64_t* flips, const cplx* y, double tol) {
+    orbit_info o;
+    uint64_t rep = q;
+    for (int g = 1; g < G; ++g) {
+        uint64_t t = or_symmetry_apply(n_sites, bw, off, maps + (size_t)g * n_sites, flips ? flips[g] : 0ull, q);
+        if (t < rep) rep = t;
+    }
+    o.rep = rep;
+    o.compatible = 1;
+    o.n_distinct = 0;
+    o.ampl.re = 0.0; o.ampl.im = 0.0;
+    /* states[i] = g_i.rep, phase conj(y_i); Dict with last write winning */
+    uint64_t dk[4096];
+    int nd = 0, last_q = -1;
+    if (G > 4096) { o.compatible = -1; return o; }
+    for (int i = 0; i < G; ++i) {
+        uint64_t s = (i == 0) ? rep : or_symmetry_apply(n_sites, bw, off, maps + (size_t)i * n_sites,
+                                                           flips ? flips[i] : 0ull, rep);
+        if (i > 0 && s == rep) {
+            double dr = y[i].re - 1.0, di = y[i].im;
+            if (!(sqrt(dr * dr + di * di) <= tol)) o.compatible = 0;
+        }
+        int f = 0;
+        for (int k = 0; k < nd; ++k) if (dk[k] == s) { f = 1; break; }
+        if (!f) dk[nd++] = s;
+        if (s == q) last_q = i;
+    }
+    o.n_distinct = nd;
+    if (last_q >= 0) {
+        /* phases start as ones(ScalarType, G) (:46); only elements i >= 1 get conj(y_i) (:67) */
+        cplx ph = (last_q == 0) ? (cplx){1.0, 0.0} : c_conj(y[last_q]);
+        double inv_norm = 1.0 / sqrt((double)nd);
+        o.ampl.re = ph.re * inv_norm;
+        o.ampl.im = ph.im * inv_norm;
+    }
+    return o;
+}
+
+/* Orbit data of m states: representative, compatibility (1/0), #distinct members and the mapping
+ * amplitude the reference's tables hold for the state. */
+void or_orbit_info(int n_sites, const int32_t* bw, const int32_t* off, int G, const int32_t* maps,
+                   const uint64_t* flips, const double* ampl, double tol, const uint64_t* states, int64_t m,
+                   uint64_t* rep_out, int32_t* compatible_out, int32_t* n_distinct_out, double* ampl_out) {
+    const cplx* y = (const cplx*)ampl;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+    for (int64_t j = 0; j < m; ++j) {
+        orbit_info o = orbit_of(states[j], n_sites, bw, off, G, maps, flips, y, tol);
+        rep_out[j] = o.rep;
+        compatible_out[j] = o.compatible;
+        n_distinct_out[j] = o.n_distinct;
+        ampl_out[2 * j] = o.ampl.re;
+        ampl_out[2 * j + 1] = o.ampl.im;
+    }
+}
+
+/* Selected rows of mul!(out, represent(rhsr, op), state): for each sampled row index r,
+ * out[j] = sum over the row iterator's elements (reduced_operator_representation.jl:57-85):
+ *   brow = basis_list[r]; ampl_row = mapping amplitude of brow (:65-66); for every matching term t
+ *   (operator_iterator.jl:48-54) with bcol = (brow & ~mask) | col in the parent sector (:75-76), the
+ *   column is the index of bcol's representative (:77; dropped when its orbit is not kept, :78), with
+ *   amplitude amp_t * ampl_col / ampl_row (:79-80); summed in term order into a zero (mul! fills out
+ *   with zero first, abstract_operator_representation.jl:115-116).
+ * status[j]: 0 ok; 1 basis_list[r] is not its orbit's representative; 2 its orbit is not kept;
+ * 3 a column's representative is missing from basis_list.  nnz_out[j]: off-diagonal elements with a
+ * valid column (row == col terms are diagonal). */
+void or_sampled_rows(const uint64_t* basis, int64_t n_r, int parent_popcount, int n_sites, const int32_t* bw,
+                     const int32_t* off, int G, const int32_t* maps, const uint64_t* flips, const double* ampl,
+                     double tol, int T, const uint64_t* masks, const uint64_t* rows, const uint64_t* cols,
+                     const double* amps, const double* state, const int64_t* sample, int64_t m, double* out,
+                     int32_t* status, int64_t* nnz_out) {
+    const cplx* y = (const cplx*)ampl;
+    const cplx* a = (const cplx*)amps;
+    const cplx* x = (const cplx*)state;
+    cplx* o = (cplx*)out;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+    for (int64_t j = 0; j < m; ++j) {
+        const int64_t r = sample[j];
+        const uint64_t brow = basis[r];
+        int st = 0;
+        int64_t nnz = 0;
+        cplx acc = {0.0, 0.0};
+        orbit_info orow = orbit_of(brow, n_sites, bw, off, G, maps, flips, y, tol);
+        if (orow.rep != brow) st = 1;
+        else if (orow.compatible != 1) st = 2;
+        const cplx inv_ampl_row = c_inv(orow.ampl);
+        for (int t = 0; t < T && st == 0; ++t) {
+            if ((brow & masks[t]) != rows[t]) continue;
+            const uint64_t bcol = (brow & ~masks[t]) | cols[t];
+            if (parent_popcount >= 0 && __builtin_popcountll(bcol) != parent_popcount) continue;
+            orbit_info oc = orbit_of(bcol, n_sites, bw, off, G, maps, flips, y, tol);
+            if (oc.compatible != 1) continue;
+            const int64_t icol = or_lookup(basis, n_r, oc.rep);
+            if (icol < 0) { st = 3; break; }
+            if (rows[t] != cols[t]) ++nnz;
+            const cplx el = c_mul(c_mul(a[t], oc.ampl), inv_ampl_row);
+            acc = c_add(acc, c_mul(el, x[icol]));
+        }
+        o[j] = acc;
+        status[j] = st;
+        nnz_out[j] = nnz;
+    }
+}
+
+/* ---- representatives of a translation sector, enumerated without a parent basis ----------------
+ * The set symmetry_reduce_generic.jl:22-106 keeps: the sweep over the ascending parent basis meets
+ * every orbit first at its minimum (:50-51), and keeps it when every element fixing it has amplitude
+ * 1 (:55-64).  So the representatives are exactly the states of the sector that are the minimum of
+ * their orbit and whose stabiliser has trivial character.  This enumerates them for the translations
+ * T(a,b) of an L1 x L2 torus of 1-bit sites (site x + L1*y at bit x + L1*y; T(a,b) moves site (x,y)
+ * to (x+a, y+b)) in the popcount-n_up sector, with chi(T(a,b)) = exp(2 pi i num[a + L1 b] / den), in
+ * ascending order, without materialising the parent sector (9.1e9 states for the 6x6 torus).
+ * The sector is split into nchunks colex-ranked chunks handled by OpenMP threads; each chunk's
+ * representatives are counted first, then written at their offsets.  Returns the number of
+ * representatives (out may be NULL to count only). */
+static uint64_t torus_apply(uint64_t v, int L1, int L2, int a, int b, const uint64_t* keep) {
+    const int n = L1 * L2;
+    const uint64_t full = (n >= 64) ? ~0ull : ((1ull << n) - 1ull);
+    /* rows up by b: bit x + L1*y -> x + L1*((y+b) mod L2), a rotation of the n-bit word by L1*b */
+    const int s = (L1 * b) % n;
+    if (s) v = ((v << s) | (v >> (n - s))) & full;
+    /* every row rotated by a within its L1 bits: bits that do not wrap move up by a, the others
+     * move down by L1 - a (keep[a] marks the bits of each row that do not wrap) */
+    if (a) v = ((v & keep[a]) << a) | ((v & ~keep[a] & full) >> (L1 - a));
+    return v;
+}
+
+static double binom_d(int n, int k) {
+    if (k < 0 || k > n) return 0.0;
+    double r = 1.0;
+    for (int i = 1; i <= k; ++i) r = r * (double)(n - k + i) / (double)i;
+    return r;
+}
+
+/* colex unranking of the r-th n-bit word with popcount k (ascending order of the words) */
+static uint64_t colex_unrank(uint64_t r, int n, int k) {
+    uint64_t v = 0;
+    for (int i = n - 1; i >= 0 && k > 0; --i) {
+        const uint64_t c = (uint64_t)binom_d(i, k);   /* words with the top set bit below i */
+        if (r >= c) { v |= 1ull << i; r -= c; --k; }
+    }
+    return v;
+}
+
+static int torus_is_rep(uint64_t v, int L1, int L2, const uint64_t* keep, const int32_t* num, int den) {
+    for (int b = 0; b < L2; ++b)
+        for (int a = 0; a < L1; ++a) {
+            if (a == 0 && b == 0) continue;
+            const uint64_t t = torus_apply(v, L1, L2, a, b, keep);
+            if (t < v) return 0;
+            if (t == v && (num[a + L1 * b] % den) != 0) return 0;
+        }
+    return 1;
+}
+
+int64_t or_torus_reps(int L1, int L2, int n_up, const int32_t* num, int den, int nchunks, uint64_t* out) {
+    const int n = L1 * L2;
+    if (n < 1 || n > 63 || n_up < 0 || n_up > n || L1 > 32) return -1;
+    uint64_t keep[33];
+    for (int a = 0; a < L1; ++a) {
+        uint64_t row = 0;
+        for (int x = 0; x + a < L1; ++x) row |= 1ull << x;
+        keep[a] = 0;
+        for (int y = 0; y < L2; ++y) keep[a] |= row << (L1 * y);
+    }
+    const uint64_t total = (uint64_t)binom_d(n, n_up);
+    if (nchunks < 1) nchunks = 1;
+    int64_t* cnt = (int64_t*)calloc((size_t)nchunks + 1, sizeof(int64_t));
+    for (int pass = 0; pass < 2; ++pass) {
+        if (pass == 1) {   /* exclusive scan of the chunk counts */
+            int64_t s = 0;
+            for (int c = 0; c < nchunks; ++c) { int64_t t = cnt[c]; cnt[c] = s; s += t; }
+            cnt[nchunks] = s;
+            if (!out) break;
+        }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+        for (int c = 0; c < nchunks; ++c) {
+            const uint64_t r0 = total / (uint64_t)nchunks * (uint64_t)c + ((uint64_t)c < total % (uint64_t)nchunks ? (uint64_t)c : total % (uint64_t)nchunks);
+            const uint64_t r1 = r0 + total / (uint64_t)nchunks + ((uint64_t)c < total % (uint64_t)nchunks ? 1u : 0u);
+            if (r1 <= r0) continue;
+            uint64_t v = colex_unrank(r0, n, n_up);
+            int64_t k = 0, pos = (pass == 1) ? cnt[c] : 0;
+            for (uint64_t r = r0; r < r1; ++r) {
+                if (torus_is_rep(v, L1, L2, keep, num, den)) {
+                    if (pass == 1) out[pos++] = v;
+                    else ++k;
+                }
+                if (n_up == 0) break;
+                const uint64_t t = v | (v - 1ull);   /* next word with the same popcount (Gosper) */
+                v = (t + 1ull) | (((~t & (t + 1ull)) - 1ull) >> (__builtin_ctzll(v) + 1));
+            }
+            if (pass == 0) cnt[c] = k;
+        }
+    }
+    const int64_t res = cnt[nchunks];
+    free(cnt);
+    return res;
+}

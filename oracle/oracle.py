@@ -64,6 +64,15 @@ def lib():
         L.or_popcount_basis.argtypes = [ctypes.c_int, ctypes.c_int, u64p, ctypes.c_int64]
         L.or_num_threads.restype = ctypes.c_int
         L.or_num_threads.argtypes = []
+        L.or_orbit_info.restype = None
+        L.or_orbit_info.argtypes = [ctypes.c_int, i32p, i32p, ctypes.c_int, i32p, u64p, dp, ctypes.c_double, u64p,
+                                    ctypes.c_int64, u64p, i32p, i32p, dp]
+        L.or_torus_reps.restype = ctypes.c_int64
+        L.or_torus_reps.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, i32p, ctypes.c_int, ctypes.c_int, u64p]
+        L.or_sampled_rows.restype = None
+        L.or_sampled_rows.argtypes = [u64p, ctypes.c_int64, ctypes.c_int, ctypes.c_int, i32p, i32p, ctypes.c_int, i32p,
+                                      u64p, dp, ctypes.c_double, ctypes.c_int, u64p, u64p, u64p, dp, dp, i64p,
+                                      ctypes.c_int64, dp, i32p, i64p]
         _lib = L
     return _lib
 
@@ -406,6 +415,135 @@ class RowSampler:
                                   _p(self.y.view(np.float64), ctypes.c_double), 0, self.nthreads, int(r0), int(r1),
                                   _p(nnz, ctypes.c_int64) if count else None)
         return int(nnz[0])
+
+
+class OrbitTables:
+    """The reference's mapping tables evaluated orbit by orbit, without parent-sized arrays.
+
+    symmetry_reduce_generic.jl:22-106 fills basis_mapping_index / basis_mapping_amplitude for every
+    parent state; where those tables do not fit in host memory (the 6x6 torus: ~290 GB), the entries a
+    row needs are computed here for one orbit at a time with the same semantics (orbit minimum as
+    representative, stabiliser amplitudes ~1 within tol, the last group element reaching a member
+    gives its phase, 1/sqrt(#distinct members)).  The parent must be one popcount sector of 1-bit sites
+    (a spin-1/2 2Sz sector).  `basis_list` is the sorted representative table under test; every
+    representative a sampled row reaches is looked up in it (a missing one is reported)."""
+
+    def __init__(self, n_sites, parent_popcount, maps, amps, basis_list, flips=None, tol: float = RTOL):
+        self.n = int(n_sites)
+        self.k = int(parent_popcount)
+        self.bw = np.ones(self.n, dtype=np.int32)
+        self.off = np.arange(self.n, dtype=np.int32)
+        self.maps = np.ascontiguousarray(maps, dtype=np.int32)
+        self.G = self.maps.shape[0]
+        self.amps = np.ascontiguousarray(np.asarray(amps, dtype=np.complex128))
+        self.flips = None if flips is None else np.ascontiguousarray(flips, dtype=np.uint64)
+        self.tol = float(tol)
+        self.basis_list = np.ascontiguousarray(basis_list, dtype=np.uint64)
+
+    def orbit_info(self, states):
+        """(representative, kept (bool), #distinct members, mapping amplitude) of every state."""
+        states = np.ascontiguousarray(states, dtype=np.uint64)
+        m = states.size
+        rep = np.empty(m, dtype=np.uint64)
+        comp = np.empty(m, dtype=np.int32)
+        nd = np.empty(m, dtype=np.int32)
+        am = np.empty(m, dtype=np.complex128)
+        lib().or_orbit_info(self.n, _p(self.bw, ctypes.c_int32), _p(self.off, ctypes.c_int32), self.G,
+                            _p(self.maps, ctypes.c_int32), _p(self.flips, ctypes.c_uint64),
+                            _p(self.amps.view(np.float64), ctypes.c_double), self.tol, _p(states, ctypes.c_uint64), m,
+                            _p(rep, ctypes.c_uint64), _p(comp, ctypes.c_int32), _p(nd, ctypes.c_int32),
+                            _p(am.view(np.float64), ctypes.c_double))
+        return rep, comp == 1, nd, am
+
+    def rows(self, terms, x, sample):
+        """Rows `sample` of mul!(out, represent(rhsr, op), x) (reduced_operator_representation.jl:57-85)
+        as (values, status, nnz_off): status 0 ok, 1 not a representative, 2 orbit not kept, 3 a
+        column's representative missing from basis_list."""
+        masks, rows, cols, amps = term_arrays(terms) if not isinstance(terms, tuple) else terms
+        masks = np.ascontiguousarray(masks, dtype=np.uint64)
+        rows = np.ascontiguousarray(rows, dtype=np.uint64)
+        cols = np.ascontiguousarray(cols, dtype=np.uint64)
+        amps = np.ascontiguousarray(amps, dtype=np.complex128)
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        if x.size != self.basis_list.size:
+            raise ValueError("x must have one entry per representative")
+        sample = np.ascontiguousarray(sample, dtype=np.int64)
+        m = sample.size
+        out = np.empty(m, dtype=np.complex128)
+        st = np.empty(m, dtype=np.int32)
+        nnz = np.empty(m, dtype=np.int64)
+        lib().or_sampled_rows(_p(self.basis_list, ctypes.c_uint64), self.basis_list.size, self.k, self.n,
+                              _p(self.bw, ctypes.c_int32), _p(self.off, ctypes.c_int32), self.G,
+                              _p(self.maps, ctypes.c_int32), _p(self.flips, ctypes.c_uint64),
+                              _p(self.amps.view(np.float64), ctypes.c_double), self.tol, len(masks),
+                              _p(masks, ctypes.c_uint64), _p(rows, ctypes.c_uint64), _p(cols, ctypes.c_uint64),
+                              _p(amps.view(np.float64), ctypes.c_double), _p(x.view(np.float64), ctypes.c_double),
+                              _p(sample, ctypes.c_int64), m, _p(out.view(np.float64), ctypes.c_double),
+                              _p(st, ctypes.c_int32), _p(nnz, ctypes.c_int64))
+        return out, st, nnz
+
+
+def torus_representatives(shape, n_up, momentum=(0, 0)) -> np.ndarray:
+    """Sorted representatives of the momentum sector of the n_up sector of an L1 x L2 torus of
+    spin-1/2 sites, enumerated on the host without a parent basis: the states that are the minimum
+    of their translation orbit and whose stabiliser has trivial character -- the set the reference's
+    ascending visited-flag sweep keeps (symmetry_reduce_generic.jl:50-72).  Character convention of
+    translation_symops."""
+    L1, L2 = shape
+    G = L1 * L2
+    m1, m2 = momentum
+    num = np.array([(m1 * (g % L1) * L2 + m2 * (g // L1) * L1) % G for g in range(G)], dtype=np.int32)
+    nch = max(64, 16 * num_threads())
+    n = lib().or_torus_reps(L1, L2, n_up, _p(num, ctypes.c_int32), G, nch, None)
+    if n < 0:
+        raise ArgumentError("unsupported torus")
+    out = np.empty(max(n, 1), dtype=np.uint64)
+    lib().or_torus_reps(L1, L2, n_up, _p(num, ctypes.c_int32), G, nch, _p(out, ctypes.c_uint64))
+    return out[:n]
+
+
+def _cycle_lengths(site_map):
+    n = len(site_map)
+    seen = [False] * n
+    out = []
+    for i in range(n):
+        if seen[i]:
+            continue
+        ln, j = 0, i
+        while not seen[j]:
+            seen[j] = True
+            j = int(site_map[j])
+            ln += 1
+        out.append(ln)
+    return out
+
+
+def sector_dimension(maps, char_num, char_den, n_up):
+    """Dimension of the symmetry sector of the n_up-particle (popcount) sector of 1-bit sites, by
+    Burnside's lemma: (1/|G|) sum_g conj(chi(g)) #{states with n_up ones fixed by g}, with
+    chi(g) = exp(2 pi i char_num[g] / char_den).  A state is fixed by a site permutation when it is
+    constant on every cycle, so the count is the number of cycle subsets holding n_up sites.  It equals
+    the number of representatives whose stabiliser has character 1 (the reduced dimension), since each
+    orbit contributes one to the isotypic component exactly when the character is trivial on its
+    stabiliser.  Exact integer counts per character residue; the final sum is rounded."""
+    maps = np.asarray(maps)
+    G = maps.shape[0]
+    per_res = {}
+    for g in range(G):
+        ways = [0] * (n_up + 1)
+        ways[0] = 1
+        for ln in _cycle_lengths(maps[g]):
+            for t in range(n_up, ln - 1, -1):
+                ways[t] += ways[t - ln]
+        r = int(char_num[g]) % int(char_den)
+        per_res[r] = per_res.get(r, 0) + ways[n_up]
+    total = sum(cnt * complex(math.cos(2 * math.pi * r / char_den), -math.sin(2 * math.pi * r / char_den))
+                for r, cnt in per_res.items())
+    val = total / G
+    out = int(round(val.real))
+    if abs(val.real - out) > 1e-3 or abs(val.imag) > 1e-3:
+        raise ValueError(f"non-integer sector dimension {val}")
+    return out
 
 
 def apply_cols(space, terms, x, out=None, accumulate=False, nthreads=0):

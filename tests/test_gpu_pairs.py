@@ -27,13 +27,13 @@ def relerr(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
 
 
-def run(E, opr, x, prec, sched, pair, tps=2):
+def run(E, opr, x, prec, sched, pair, tps=2, uniform=False):
     import torch
     dt = torch.complex128 if prec == "fp64" else torch.complex64
     xd = torch.from_numpy(x).to(dt).cuda()
     yd = torch.empty_like(xd)
     opr.set_tiling(prec, sched)
-    opr.set_pair_schedule(pair, tps)
+    opr.set_pair_schedule(pair, tps, uniform)
     E.mul_(yd, opr, xd, precision=prec)
     torch.cuda.synchronize()
     opr.set_tiling(prec, 0)
@@ -336,6 +336,12 @@ def test_target_table_chain_all_momenta(edgpu):
                 for tps in (2, 4, 8):
                     y = run(edgpu, opr, x, prec, -1, True, tps)
                     assert torch.equal(y, plain[prec]), (m, with_map, prec, tps)
+                for tps in (4, 8):
+                    # warp-uniform pair steps: same visiting order per row, same bits
+                    opr.set_pair_schedule(True, tps, True)
+                    assert opr.schedule(prec)[1] == tps | edgpu.representation.PAIR_UNIFORM
+                    y = run(edgpu, opr, x, prec, -1, True, tps, True)
+                    assert torch.equal(y, plain[prec]), (m, with_map, prec, tps, "uniform")
             y = run(edgpu, opr, x, "fp64", -1, True).cpu().numpy()
             assert relerr(y, O.apply_rows(red, terms, x)) < FP64_TOL
             opr.free_targets()
@@ -363,6 +369,8 @@ def test_target_table_torus(edgpu, shape, vectors):
         assert opr.build_targets(1 << 28)
         for prec in ("fp64", "mixed"):
             assert torch.equal(run(edgpu, opr, x, prec, -1, True), plain[prec]), (k, prec)
+            for tps in (4, 8):
+                assert torch.equal(run(edgpu, opr, x, prec, -1, True, tps, True), plain[prec]), (k, prec, tps)
         opr.free_targets()
 
 
@@ -492,6 +500,11 @@ def test_full_size_target_table(edgpu, workload):
     assert opr.uses_target_table("fp64")
     _, Hu_tab = hermitian_checks(edgpu, opr, N)
     assert torch.equal(Hu_tab, Hu_map)
+    opr.set_pair_schedule(True, 8, True)
+    Hu_uni = torch.empty_like(Hu_tab)
+    edgpu.mul_(Hu_uni, opr, u)
+    assert torch.equal(Hu_uni, Hu_tab)
+    opr.set_pair_schedule(True)
     u32, H32 = u.to(torch.complex64), torch.empty(N, dtype=torch.complex64, device="cuda")
     edgpu.mul_(H32, opr, u32, precision="mixed")
     assert (torch.linalg.vector_norm(H32.to(torch.complex128) - Hu_tab) /
