@@ -56,20 +56,20 @@ WORKLOADS = {
                          N_r=12870, nnz_off=109824, steps=2000,
                          desc="spin-1/2 Heisenberg chain L=16 PBC J=1, 2Sz=0, no symmetry reduction"),
     "chain28_grad": dict(kind="chain_grad", L=28, k=0, seed=4, x_seed=5, gy_seed=6, cpu_feasible=True,
-                         N_r=1432860, nnz_off=None, steps=200,
+                         N_r=1432860, nnz_off=20803084, steps=200,
                          desc="spin-1/2 Heisenberg chain L=28 PBC, per-bond J_b = 0.5 + U[0,1) (seed 4), 2Sz=0, "
                               "momentum 0: forward H x, coupling gradient dL/dJ_b = Re<gy|H_b x>, adjoint H^dagger gy"),
     "chain28_k0": dict(kind="chain", L=28, k=0, jxy=1.0, jz=1.0, seed=5, lanczos_steps=200, reorth=True,
-                       N_r=1432860, nnz_off=None, steps=500,
+                       N_r=1432860, nnz_off=20803084, steps=500,
                        desc="spin-1/2 Heisenberg chain L=28 PBC, 2Sz=0, momentum 0"),
     "triangular6x5_allk": dict(kind="torus_allk", shape=(6, 5), nn=[(1, 0), (1, 1), (0, 1)],
                                nnn=[(2, 1), (1, 2), (-1, 1)], j1=1.0, j2=0.125, aniso=0.8, seed=3,
-                               cpu_feasible=False, N_r=155117520, nnz_off=None, steps=20,
+                               cpu_feasible=False, N_r=155117520, nnz_off=14441957888, steps=20,
                                desc="spin-1/2 XXZ J1-J2 triangular 6x5 torus (Jz/Jxy=0.8, J2/J1=0.125), 2Sz=0, "
                                     "all 30 momentum sectors in one batched persistent launch"),
     "triangular6x5_k1": dict(kind="torus", shape=(6, 5), k=(1, 0), nn=[(1, 0), (1, 1), (0, 1)],
                              nnn=[(2, 1), (1, 2), (-1, 1)], j1=1.0, j2=0.125, aniso=0.8, seed=3, lanczos_steps=200,
-                             reorth=True, cpu_feasible=False, N_r=5170578, nnz_off=None, steps=200,
+                             reorth=True, cpu_feasible=False, N_r=5170578, nnz_off=481397728, steps=200,
                              desc="spin-1/2 XXZ J1-J2 triangular 6x5 torus (Jz/Jxy=0.8, J2/J1=0.125), 2Sz=0, "
                                   "momentum (1,0) (one sector of the batched workload)"),
     "square6x6_k0": dict(kind="torus", shape=(6, 6), k=(0, 0), nn=[(1, 0), (0, 1)], nnn=[(1, 1), (1, -1)],
@@ -361,7 +361,7 @@ def cpu_orbit_rows(wl, steps, warmup, budget_s=None, rows_per_step=4096):
     t0 = time.perf_counter()
     basis = O.torus_representatives(shape, n // 2, k)
     maps, amps = O.translation_symops(shape, k)
-    ot = O.OrbitTables(n, n // 2, maps, amps, basis)
+    ot = O.OrbitTables(n, n // 2, maps, amps, basis, torus=shape)   # translations applied by word rotations
     terms = O.heisenberg_terms(n, bonds, jxy, jz)
     N = basis.size
     x = O.complex_gaussian(N, wl["seed"])
@@ -384,8 +384,9 @@ def cpu_orbit_rows(wl, steps, warmup, budget_s=None, rows_per_step=4096):
     return {"ms_per_step": 1e3 * per_row * N, "steps": done, "cores": O.num_threads(), "kind": "port",
             "setup_s": setup, "N_r_host": int(N),
             "sample": f"{done} blocks of {rows_per_step} random rows of the {N}-row sector (FP64; representatives "
-                      f"enumerated on the host, mapping entries evaluated orbit by orbit because the reference's "
-                      f"parent-sized tables (~{24 * math.comb(n, n // 2) / 1e9:.0f} GB) exceed host memory), "
+                      f"enumerated on the host, mapping entries evaluated orbit by orbit instead of the reference's "
+                      f"parent-sized tables, ~{24 * math.comb(n, n // 2) / 1e9:.0f} GB over {math.comb(n, n // 2)} parent "
+                      f"states), "
                       f"{tot:.2f} s of CPU time, extrapolated to one whole H*x"}
 
 
@@ -470,6 +471,7 @@ def run_gpu(args, wl):
         opr.set_pair_schedule(args.pair_targets > 0, max(args.pair_targets, 2), args.uniform)
         for prec in ("mixed", "fp64"):
             opr.set_tiling(prec, args.tiling)
+            opr.table_prefetch(prec, args.prefetch)
         tune_mixed = tune_fp64 = (args.tiling, None)
     else:
         tune_mixed = opr.autotune("mixed")
@@ -632,7 +634,9 @@ def run_gpu(args, wl):
                        "parallelism": f"replicas x{world}",
                        "rows_per_tile": {"mixed": tune_mixed[0], "fp64": tune_fp64[0]},
                        "pair_flip_schedule": {"mixed": opr.schedule("mixed")[1], "fp64": opr.schedule("fp64")[1],
-                                              "bond_classes": opr.pair_classes()[0]},
+                                              "bond_classes": opr.pair_classes()[0],
+                                              "prefetch": {"mixed": opr.table_prefetch("mixed"),
+                                                           "fp64": opr.table_prefetch("fp64")}},
                        "target_table": dict(table_info or {"built": False},
                                             used={"mixed": opr.uses_target_table("mixed"),
                                                   "fp64": opr.uses_target_table("fp64")}),
@@ -859,6 +863,7 @@ def main():
     ap.add_argument("--pair-targets", type=int, default=2, choices=[0, 2, 4, 8],
                     help="with --tiling: targets per lane and step of the pair-flip schedule (0: term scan)")
     ap.add_argument("--uniform", action="store_true", help="with --tiling: warp-uniform pair steps (4 or 8 targets)")
+    ap.add_argument("--prefetch", type=int, default=0, help="with --tiling: x prefetch distance of the target-table product")
     ap.add_argument("--no-table", action="store_true", help="no target tables (look every target up per product)")
     ap.add_argument("--no-pair", action="store_true", help="test every term per row instead of the pair-flip schedule")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -194,7 +194,6 @@ struct edgpu_op_s {
     int tab_use[2] = {1, 1};          // [precision]: products read the table (chosen by the autotuner)
     int tab_pf[2] = {0, 0};           // [precision]: x prefetched this many steps ahead (chosen by the autotuner)
     int tab_uni[2] = {0, 0};          // [precision]: warp-uniform pair steps (chosen by the autotuner)
-    long long tab_near[2] = {0, 0};   // [precision]: streamed-load threshold in rows (0: off; autotuned)
     // adjoint target table (optional, edgpu_op_build_adjoint_targets): per column its sorted run of
     // (row, slot, orbit-size index of the row, group element) entries
     long long* d_adj_off = nullptr;
@@ -244,7 +243,7 @@ struct edgpu_batch_s {
         HxParams tmpl{};
         int gk = 0, per_sm = 1, per_sm_map = 0;
         int per_sm_bond[2][2] = {{0, 0}, {0, 0}};   // pair-flip kernel [mapped][4 targets per step]
-        int per_sm_table[2] = {0, 0};               // its target-table flavour [4 targets per step]
+        int per_sm_table[3] = {0, 0, 0};            // its target-table flavour [2, 4, 8 targets per step]
         size_t smem = 0;
         int64_t rows = 0;
     } fused[2];
@@ -910,7 +909,6 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
                 p.tab_cb = op->tab_cb;
                 p.bond_pf = op->tab_pf[prec];
                 p.bond_uni = (op->tab_uni[prec] && p.bond_nt >= 4) ? 1 : 0;
-                p.bond_near = op->tab_near[prec];
                 int& mt = B.max_blocks_table[p.bond_uni][p.bond_nt == 8 ? 2 : p.bond_nt == 4 ? 1 : 0];
                 if (mt == 0)
                     mt = std::max(1, hx_table_occupancy(w32, prec, p.bond_nt, smem, p.bond_uni != 0)) *
@@ -1552,6 +1550,48 @@ int edgpu_reduce_mapping(edgpu_space reduced, int64_t* index_out, double* ampl_o
     API_END
 }
 
+int edgpu_space_parent_dim(edgpu_space reduced, int64_t* out) {
+    API_BEGIN
+    edgpu_space_s* s = as_space(reduced);
+    SpaceLock lk_(s->hs.mu);
+    require(out, EDGPU_ERR_ARG, "null output");
+    require(s->reduced && s->parent, EDGPU_ERR_ARG, "not a reduced representation");
+    *out = parent_dimension(*s->parent);
+    API_END
+}
+
+int edgpu_symmetry_unreduce_device(edgpu_space reduced, int32_t precision, const void* small, int64_t n, void* large,
+                                   int64_t n_parent, void* stream) {
+    API_BEGIN
+    edgpu_space_s* s = as_space(reduced);
+    SpaceLock lk_(s->hs.mu);
+    check_prec(precision);
+    require(s->reduced && s->parent, EDGPU_ERR_ARG, "not a reduced representation");
+    require(n == s->dim, EDGPU_ERR_DIM, "small vector has length " + std::to_string(n) + " != dimension " + std::to_string(s->dim));
+    require(n_parent == parent_dimension(*s->parent), EDGPU_ERR_DIM, "large vector length differs from the parent dimension");
+    if (n_parent == 0) return EDGPU_OK;
+    require(large && (small || n == 0), EDGPU_ERR_ARG, "null vector");
+    cudaStream_t st = stream ? pick_stream(stream) : s->hs.stream();
+    reduce_vector(*s, *s->parent, precision, true, small, large, st);
+    API_END
+}
+
+int edgpu_symmetry_reduce_device(edgpu_space reduced, int32_t precision, const void* large, int64_t n_parent, void* small,
+                                 int64_t n, void* stream) {
+    API_BEGIN
+    edgpu_space_s* s = as_space(reduced);
+    SpaceLock lk_(s->hs.mu);
+    check_prec(precision);
+    require(s->reduced && s->parent, EDGPU_ERR_ARG, "not a reduced representation");
+    require(n == s->dim, EDGPU_ERR_DIM, "small vector has length " + std::to_string(n) + " != dimension " + std::to_string(s->dim));
+    require(n_parent == parent_dimension(*s->parent), EDGPU_ERR_DIM, "large vector length differs from the parent dimension");
+    if (n == 0) return EDGPU_OK;
+    require(small && (large || n_parent == 0), EDGPU_ERR_ARG, "null vector");
+    cudaStream_t st = stream ? pick_stream(stream) : s->hs.stream();
+    reduce_vector(*s, *s->parent, precision, false, large, small, st);
+    API_END
+}
+
 int edgpu_space_orbit_sizes(edgpu_space reduced, int32_t* out, int64_t n) {
     API_BEGIN
     edgpu_space_s* s = as_space(reduced);
@@ -1657,13 +1697,14 @@ int edgpu_op_set_pair_schedule(edgpu_op oh, int32_t enable) {
     API_END
 }
 
-int edgpu_op_near_window(edgpu_op oh, int32_t precision, int64_t rows, int64_t* current) {
+int edgpu_op_table_prefetch(edgpu_op oh, int32_t precision, int32_t steps, int32_t* current) {
     API_BEGIN
     edgpu_op_s* op = as_op(oh);
     OpLock lk_(op->hs.mu);
     check_prec(precision);
-    if (rows >= 0) op->tab_near[precision] = rows;
-    if (current) *current = op->tab_near[precision];
+    require(steps <= 1024, EDGPU_ERR_ARG, "prefetch distance above 1024 steps");
+    if (steps >= 0) op->tab_pf[precision] = steps;
+    if (current) *current = op->tab_pf[precision];
     API_END
 }
 
@@ -1941,7 +1982,7 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     // rows per warp tile when there is no parent-state map); where the pair-flip schedule applies
     // (and the caller allows it), that schedule with 2 or 4 targets per step (4 with a map or a
     // target table) and 1, 2 or 4 lanes per row, and its target-table flavour (one lane per row).
-    struct Cand { int pair, nt, table, rows, pf, uni; long long near; };
+    struct Cand { int pair, nt, table, rows, pf, uni; };
     std::vector<Cand> cands;
     build_blob(op, precision, 0, 0);
     const bool pair_ok = op->blob[precision][0][0].tmpl.bond_ncls > 0 && op->pair_allowed;
@@ -1949,27 +1990,20 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     if (pair_ok) {
         if (op->d_tab) {
             for (int nt : {8, 4, 2})
-                for (int pf : {0, 4, 64}) cands.push_back({1, nt, 1, -1, pf, 0, 0});
+                for (int pf : {0, 4, 64}) cands.push_back({1, nt, 1, -1, pf, 0});
             for (int nt : {8, 4})
-                for (int pf : {0, 4}) cands.push_back({1, nt, 1, -1, pf, 1, 0});
-            // streamed table and far gathers, with near windows of 2^15 to 2^23 rows, for sectors whose x
-            // is larger than a quarter of L2
-            const size_t vsz = precision == EDGPU_FP64 ? 16 : 8;
-            if ((double)n * vsz > 32e6)
-                for (long long near : {1ll << 15, 1ll << 18, 1ll << 20, 1ll << 22, 1ll << 62})
-                    for (int nt : {8, 4}) cands.push_back({1, nt, 1, -1, 0, 0, near});
+                for (int pf : {0, 4}) cands.push_back({1, nt, 1, -1, pf, 1});
         }
         for (int nt : (mapped ? std::vector<int>{4, 2} : std::vector<int>{2}))
-            for (int r : {-1, -2, -4}) cands.push_back({1, nt, 0, r, 0, 0, 0});
+            for (int r : {-1, -2, -4}) cands.push_back({1, nt, 0, r, 0, 0});
     }
-    for (int r : {-1, -2, -4}) cands.push_back({0, 2, 0, r, 0, 0, 0});
+    for (int r : {-1, -2, -4}) cands.push_back({0, 2, 0, r, 0, 0});
     if (!mapped)
-        for (int r : {32, 16}) cands.push_back({0, 2, 0, r, 0, 0, 0});
+        for (int r : {32, 16}) cands.push_back({0, 2, 0, r, 0, 0});
     Cand best = cands.front();
     double best_ms = 1e30;
     const int keep_pair = op->pair_use[precision], keep_nt = op->pair_nt[precision], keep_tab = op->tab_use[precision];
     const int keep_uni = op->tab_uni[precision];
-    const long long keep_near = op->tab_near[precision];
     if (n > 0) {
         const size_t vs = precision == EDGPU_FP64 ? 16 : 8;
         void *x = nullptr, *y = nullptr;
@@ -1986,7 +2020,6 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
                 op->tab_use[precision] = c.table;
                 op->tab_pf[precision] = c.pf;
                 op->tab_uni[precision] = c.uni;
-                op->tab_near[precision] = c.near;
                 launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, op->hs.stream(), nullptr, c.rows);
                 // one timed launch, then two back-to-back bursts of enough launches to cover about 2 ms
                 // (1 to 50 per burst), as a solver issues them; the faster burst's time per launch
@@ -2018,7 +2051,6 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
             op->pair_nt[precision] = keep_nt;
             op->tab_use[precision] = keep_tab;
             op->tab_uni[precision] = keep_uni;
-            op->tab_near[precision] = keep_near;
             cudaFree(x);
             cudaFree(y);
             cudaEventDestroy(e0);
@@ -2035,7 +2067,6 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     op->tab_use[precision] = best.table ? 1 : (op->d_tab ? 0 : 1);
     op->tab_pf[precision] = best.pf;
     op->tab_uni[precision] = best.uni;
-    op->tab_near[precision] = best.near;
     op->tuned_rows[precision] = best.rows;
     if (rows_per_tile_out) *rows_per_tile_out = best.rows;
     if (best_ms_out) *best_ms_out = best_ms;
@@ -2254,6 +2285,16 @@ static void host_product_issue(edgpu_op_s* op, int prec, int dir, const double* 
             launch_product(op, prec, dir, 0, op->x32.p, op->y32.p, 0, nullptr, nullptr, st, nullptr, 0, yd,
                            accumulate, &fused);
             if (!fused) launch_c64_to_c128(n, op->y32.p, yd, accumulate, st);
+            return;
+        }
+    }
+    if (prec == EDGPU_FP64 && !conj_io) {
+        // pinned buffers the device can address: x is copied in (the product gathers it at random),
+        // and the product writes (or, for apply!, updates) y in the host buffer itself
+        double* yd = (double*)device_alias(y);
+        if (yd) {
+            EDGPU_CUDA(cudaMemcpyAsync(op->x64.p, x, n * 16, cudaMemcpyHostToDevice, st));
+            launch_product(op, prec, dir, 0, op->x64.p, yd, accumulate, nullptr, nullptr, st);
             return;
         }
     }
@@ -2673,7 +2714,7 @@ HxParams batch_params(edgpu_batch_s* b, int prec, const void* const* xs, void* c
     p.n_tiles = tiles;
     const bool w32 = b->ops[0]->space->w32;
     int per_sm = mapped ? F.per_sm_map : F.per_sm;
-    p.bond_nt = ((mapped || tabled) && b->pair_nt[prec] == 4) ? 4 : 2;
+    p.bond_nt = (tabled && b->pair_nt[prec] == 8) ? 8 : ((mapped || tabled) && b->pair_nt[prec] >= 4) ? 4 : 2;
     p.tab = nullptr;
     if (tabled) {
         for (int i = 0; i < n; ++i)
@@ -2683,7 +2724,7 @@ HxParams batch_params(edgpu_batch_s* b, int prec, const void* const* xs, void* c
             }
         p.blob_words16 = (int)(F.smem_lookup / 16);
         p.bond_pf = b->tab_pf[prec];
-        int& ps = F.per_sm_table[p.bond_nt == 4 ? 1 : 0];
+        int& ps = F.per_sm_table[p.bond_nt == 8 ? 2 : p.bond_nt == 4 ? 1 : 0];
         if (ps == 0) ps = std::max(1, hx_table_multi_occupancy(w32, prec, p.bond_nt, F.smem_lookup));
         per_sm = ps;
     } else if (pair) {
@@ -2789,8 +2830,8 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
             for (auto* o : b->ops) mapped = mapped && (o->space->d_map != nullptr || o->space->dim == 0);
             bool tabled = pair_ok;
             for (auto* o : b->ops) tabled = tabled && (o->d_tab != nullptr || o->space->dim == 0);
-            // cand 4/3: target tables with 4/2 targets per step; 2/1: pair flips with 4/2; 0: term scan
-            for (int cand = tabled ? 4 : (pair_ok ? (mapped ? 2 : 1) : 0); cand >= 0; --cand)
+            // cand 5/4/3: target tables with 8/4/2 targets per step; 2/1: pair flips with 4/2; 0: term scan
+            for (int cand = tabled ? 5 : (pair_ok ? (mapped ? 2 : 1) : 0); cand >= 0; --cand)
                 for (int l : {1, 2, 4, 5, 6}) {
                     // target tables: one lane per row, x prefetched 0 (l = 1), 4 (l = 5) or 64 (l = 6)
                     // steps ahead; the other schedules: l lanes per row
@@ -2801,7 +2842,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
                     if (l >= 5) l = 1;
                     b->lpr[precision] = l;
                     b->pair_use[precision] = cand > 0 ? 1 : 0;
-                    b->pair_nt[precision] = (cand == 2 || cand == 4) ? 4 : 2;
+                    b->pair_nt[precision] = cand == 5 ? 8 : (cand == 2 || cand == 4) ? 4 : 2;
                     b->tab_use[precision] = cand >= 3 ? 1 : 0;
                     int blocks = 0;
                     const HxParams p = batch_params(b, precision, xs.data(), ys.data(), &blocks);
@@ -2829,7 +2870,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
                         best = l;
                         best_pf = pf;
                         best_pair = cand > 0 ? 1 : 0;
-                        best_nt = (cand == 2 || cand == 4) ? 4 : 2;
+                        best_nt = cand == 5 ? 8 : (cand == 2 || cand == 4) ? 4 : 2;
                         best_tab = cand >= 3 ? 1 : 0;
                     }
                 }
@@ -2882,7 +2923,7 @@ int edgpu_batch_get_schedule(edgpu_batch bh, int32_t precision, int32_t* lanes_p
         for (auto* o : bh->ops) tabled = tabled && (o->d_tab != nullptr || o->space->dim == 0);
         const bool on = bh->fused[precision].tmpl.bond_ncls > 0 && bh->ops[0]->pair_allowed && bh->pair_use[precision];
         tabled = tabled && on && bh->tab_use[precision];
-        *pair_flips = on ? (((mapped || tabled) && bh->pair_nt[precision] == 4) ? 4 : 2) : 0;
+        *pair_flips = on ? ((tabled && bh->pair_nt[precision] == 8) ? 8 : ((mapped || tabled) && bh->pair_nt[precision] >= 4) ? 4 : 2) : 0;
         if (target_table) *target_table = tabled ? 1 : 0;
     } else if (target_table) {
         bool tabled = true;

@@ -154,6 +154,12 @@ int orbit_index_bits(int G);
 void embed_orbit_index(Space& red, cudaStream_t st);
 void build_search_directory(Space& s, cudaStream_t st);
 void get_states(const Space& s, uint64_t* out_host, cudaStream_t st);
+// Vectors between a reduced space and its parent on the device (symmetry_unreduce / symmetry_reduce):
+// unreduce: out[n_parent] from in[dim]; reduce: out[dim] from in[n_parent].  complex128 (EDGPU_FP64) or
+// complex64 (EDGPU_MIXED) vectors; the parent is materialised or a lazy popcount sector.
+void reduce_vector(const Space& red, const Space& parent, int prec, bool unreduce, const void* in, void* out,
+                   cudaStream_t st);
+int64_t parent_dimension(const Space& parent);
 // Diagonal element of every row: sum of the amplitudes of the row == col terms matching the row's state
 // (FP64), written as complex128 (out64) and/or complex64 (out32).  scratch: device room for the T terms
 // (4 words each), or null to allocate it for the call.
@@ -218,8 +224,6 @@ struct HxParams {
     int bond_nt;                              // targets per lane and step: 2, or 4 (parent-state map only)
     int bond_pf;                              // target tables: x prefetched this many steps ahead (0: none)
     int bond_uni;                             // target tables: warp-uniform pair steps (bond_tile UNI)
-    long long bond_near;                      // target tables: > 0 streams the table and the gathers of targets
-                                              // at least this many rows from the row (evict-first), 0: default loads
     // gradient mode of the pair-flip kernel (offsets into its shared-memory image, -1 when absent): the
     // slots' unit amplitudes and coupling ids, and the diagonal term records
     int o_bunit, o_bcid, o_pdm, o_pdr, o_pdu, o_pdc;

@@ -1228,3 +1228,201 @@ void compute_diagonal(const Space& s, int T, const uint64_t* masks, const uint64
     else diag_t<unsigned long long>(s, T, masks, rows, amps, out64, out32, scratch, st);
 }
 }  // namespace edgpu
+
+// ---- vectors between the parent space and the reduced space, on the device -----------------------
+// symmetry_unreduce(rhsr, small) and symmetry_reduce(rhsr, large) (symmetry_reduce.jl:208-225 and
+// :38-56): the reference reads its parent-sized tables basis_mapping_index / basis_mapping_amplitude;
+// here every parent entry's representative, stabiliser and group element are recomputed, so they run
+// for parents whose tables do not fit (a parent vector of 9.1e9 entries for the 6x6 torus does).
+// Parent index i <-> state: the materialised parent's sorted basis, or for a lazy popcount sector the
+// colex rank (rank = sum over the set bits, lowest first, of C(position, count so far)).
+namespace edgpu {
+namespace {
+
+// g.q for element e of the group (T(a, b) with e = a + L1 b for a torus: rows rotated left by a sites,
+// then the rows moved up by b; the chunk tables and flip mask for a general group).
+template <typename W>
+__device__ __forceinline__ W group_elem_apply(W q, int e, const GroupDev& g) {
+    if (g.kind == GK_TORUS) {
+        const int a = e % g.L1, b = e / g.L1;
+        const W full = (W)g.full;
+        W v = q;
+        if (a) {
+            const int s = a * g.w;
+            const W keep = (W)g.keep[a];
+            v = (W)(((v & keep) << s) | ((v & ~keep & full) >> (g.rowbits - s)));
+        }
+        const int sr = b * g.rowbits;
+        if (sr) v = (W)(((v << sr) | (v >> (g.nbits - sr))) & full);
+        return v;
+    }
+    if (g.kind == GK_GENERIC) {
+        W t = 0;
+        const unsigned long long* L = g.lut + (size_t)e * g.nchunks * 16;
+        for (int c = 0; c < g.nchunks; ++c) t |= (W)L[c * 16 + (int)((q >> (4 * c)) & 15u)];
+        return t ^ (W)g.flips[e];
+    }
+    return q;
+}
+
+template <typename W>
+__device__ __forceinline__ long long colex_rank(W q, const unsigned long long* C) {
+    long long r = 0;
+    int j = 0;
+    while (q) {
+        const int pos = (sizeof(W) == 8) ? __ffsll((long long)q) - 1 : __ffs((int)q) - 1;
+        ++j;
+        r += (long long)C[pos * 65 + j];
+        q &= q - 1;
+    }
+    return r;
+}
+
+// large[i] = ampl(p_i) small[c(p_i)] (0 where the orbit has no representative), the parent index i
+// running over [0, n_parent).
+template <typename W, typename PW, typename V>
+__global__ void k_unreduce(const PW* parent, long long n_parent, int n, int k, const unsigned long long* C,
+                           const W* reps, long long n_reps, int sb, GroupDev g, const double2* phase, const V* small,
+                           V* large) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n_parent;
+         i += (long long)gridDim.x * blockDim.x) {
+        const W q = parent ? (W)parent[i] : unrank_combo<W>((unsigned long long)i, n, k, C);
+        W rep = q;
+        int gb = 0, stab = 1;
+        if (g.kind == GK_TORUS) {
+            W keep[64];
+            for (int a = 0; a < g.L1; ++a) keep[a] = (W)g.keep[a];
+            canon_torus<W>(q, g.L1, g.L2, g.w, g.rowbits, g.nbits, (W)g.full, keep, true, true, rep, gb, stab);
+        } else if (g.kind == GK_GENERIC) {
+            stab = 0;
+            for (int e = 0; e < g.G; ++e) {
+                const W t = group_elem_apply<W>(q, e, g);
+                if (t < rep) {
+                    rep = t;
+                    gb = e;
+                }
+                stab += (t == q);
+            }
+        }
+        const long long c = key_find<W>(reps, n_reps, rep, sb, nullptr);
+        V out;
+        out.x = 0;
+        out.y = 0;
+        if (c >= 0) {
+            const double s = sqrt((double)stab / (double)g.G);
+            const double2 ph = phase[g.num[gb]];
+            const V v = small[c];
+            const double ar = ph.x * s, ai = ph.y * s;
+            out.x = (decltype(out.x))(ar * (double)v.x - ai * (double)v.y);
+            out.y = (decltype(out.y))(ar * (double)v.y + ai * (double)v.x);
+        }
+        large[i] = out;
+    }
+}
+
+// small[c] = sum over the orbit members p of rep_c of conj(ampl(p)) large[i(p)].  Every element e of
+// the group gives the member e.rep_c with ampl = conj(chi(e)) sqrt(|stab| / |G|); each distinct
+// member occurs |stab| times among the |G| elements, so the sum over all elements is divided by
+// |stab|.  One thread per representative, elements in a fixed order (reproducible, no atomics).
+template <typename W, typename PW, typename V>
+__global__ void k_reduce(const PW* parent, long long n_parent, const unsigned long long* C, const W* reps,
+                         long long n_reps, int sb, GroupDev g, const double2* phase, const V* large, V* small) {
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n_reps;
+         c += (long long)gridDim.x * blockDim.x) {
+        const W rep = reps[c] >> sb;
+        int stab = 0;
+        for (int e = 0; e < g.G; ++e) stab += (group_elem_apply<W>(rep, e, g) == rep);
+        const double s = sqrt((double)stab / (double)g.G) / (double)stab;
+        double ar = 0.0, ai = 0.0;
+        for (int e = 0; e < g.G; ++e) {
+            const W t = group_elem_apply<W>(rep, e, g);
+            long long i;
+            if (parent) {
+                long long lo = 0, len = n_parent;
+                while (len > 0) {   // searchsortedfirst over the parent basis
+                    const long long half = len >> 1;
+                    if ((W)parent[lo + half] < t) {
+                        lo += half + 1;
+                        len -= half + 1;
+                    } else {
+                        len = half;
+                    }
+                }
+                i = (lo < n_parent && (W)parent[lo] == t) ? lo : -1;
+            } else {
+                i = colex_rank<W>(t, C);
+            }
+            if (i < 0) continue;
+            // conj(ampl(t)) = chi(e) sqrt(|stab| / |G|); chi(e) = phase[num[e]]
+            const double2 ph = phase[g.num[e]];
+            const V v = large[i];
+            ar += ph.x * (double)v.x - ph.y * (double)v.y;
+            ai += ph.x * (double)v.y + ph.y * (double)v.x;
+        }
+        V out;
+        out.x = (decltype(out.x))(ar * s);
+        out.y = (decltype(out.y))(ai * s);
+        small[c] = out;
+    }
+}
+
+template <typename W, typename PW, typename V>
+void reduce_vector_t(const Space& red, const Space& parent, bool unreduce, const void* in, void* out,
+                     cudaStream_t st) {
+    GroupBuffers gb;
+    gb.upload(red.group, parent.lay);
+    std::vector<double> ph(2 * (size_t)red.group.den);
+    for (int j = 0; j < red.group.den; ++j) {
+        const double ang = 2.0 * M_PI * (double)j / (double)red.group.den;
+        ph[2 * j] = std::cos(ang);
+        ph[2 * j + 1] = std::sin(ang);
+    }
+    double2* d_ph = nullptr;
+    EDGPU_CUDA(cudaMalloc(&d_ph, ph.size() * sizeof(double)));
+    cudaError_t e = cudaMemcpyAsync(d_ph, ph.data(), ph.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    const PW* pk = parent.d_keys ? (const PW*)parent.d_keys : nullptr;
+    const long long n_parent = parent.d_keys ? parent.dim : (long long)host_binom(parent.lay.nbits, parent.lay.popcount);
+    const int blocks = std::max(1, sm_count() * 16);
+    if (e == cudaSuccess) {
+        if (unreduce)
+            k_unreduce<W, PW, V><<<blocks, 256, 0, st>>>(pk, n_parent, parent.lay.nbits, parent.lay.popcount,
+                                                          binomial_table(), (const W*)red.d_keys, red.dim, red.sb, gb.dev,
+                                                          d_ph, (const V*)in, (V*)out);
+        else
+            k_reduce<W, PW, V><<<blocks, 256, 0, st>>>(pk, n_parent, binomial_table(), (const W*)red.d_keys, red.dim,
+                                                        red.sb, gb.dev, d_ph, (const V*)in, (V*)out);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_ph);
+    if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("vector reduction: ") + cudaGetErrorString(e));
+}
+
+}  // namespace
+
+int64_t parent_dimension(const Space& parent) {
+    return parent.d_keys ? parent.dim : (int64_t)host_binom(parent.lay.nbits, parent.lay.popcount);
+}
+
+void reduce_vector(const Space& red, const Space& parent, int prec, bool unreduce, const void* in, void* out,
+                   cudaStream_t st) {
+    if (!parent.d_keys && parent.lay.popcount < 0)
+        throw Error(EDGPU_ERR_STATE, "a lazy parent must be one popcount sector of 1-bit sites");
+    const bool pw32 = parent.d_keys && parent.w32;
+#define EDGPU_RV(W)                                                                                         \
+    if (prec == EDGPU_FP64) {                                                                              \
+        if (pw32) reduce_vector_t<W, uint32_t, double2>(red, parent, unreduce, in, out, st);                \
+        else reduce_vector_t<W, unsigned long long, double2>(red, parent, unreduce, in, out, st);           \
+    } else {                                                                                                \
+        if (pw32) reduce_vector_t<W, uint32_t, float2>(red, parent, unreduce, in, out, st);                 \
+        else reduce_vector_t<W, unsigned long long, float2>(red, parent, unreduce, in, out, st);            \
+    }
+    if (red.w32) {
+        EDGPU_RV(uint32_t)
+    } else {
+        EDGPU_RV(unsigned long long)
+    }
+#undef EDGPU_RV
+}
+
+}  // namespace edgpu

@@ -81,22 +81,18 @@ __device__ __forceinline__ int lowest_bit(W m) {
 
 // Entry of the target table at pos (map format: c | sx << cb | g << (cb + sb); all ones when the
 // target's orbit has no representative in the table).
-// stream: load with the evict-first (cache-streaming) policy, so that the table, read once, does not
-// displace lines of x that other rows still gather.
 template <int PREC>
 __device__ __forceinline__ void table_entry(const RowsSector<PREC>& sc, long long pos, bool on, int sb, long long& c,
-                                            int& sx, int& g, bool stream = false) {
+                                            int& sx, int& g) {
     if (!sc.tab_wide) {
-        const unsigned* tp = (const unsigned*)sc.tab + pos;
-        const unsigned e = on ? (stream ? __ldcs(tp) : __ldg(tp)) : 0xffffffffu;
+        const unsigned e = on ? __ldg((const unsigned*)sc.tab + pos) : 0xffffffffu;
         const unsigned cmask = (sc.tab_cb >= 32) ? 0xffffffffu : ((1u << sc.tab_cb) - 1u);
         const unsigned ci = e & cmask;
         c = (ci == cmask) ? -1 : (long long)ci;
         sx = (int)((e >> sc.tab_cb) & ((1u << sb) - 1u));
         g = (int)((e >> (sc.tab_cb + sb)) & 0xfffu);
     } else {
-        const unsigned long long* tp = (const unsigned long long*)sc.tab + pos;
-        const unsigned long long e = on ? (stream ? __ldcs(tp) : __ldg(tp)) : ~0ull;
+        const unsigned long long e = on ? __ldg((const unsigned long long*)sc.tab + pos) : ~0ull;
         const unsigned long long cmask = (1ull << sc.tab_cb) - 1ull;
         const unsigned long long ci = e & cmask;
         c = (ci == cmask) ? -1 : (long long)ci;
@@ -275,7 +271,7 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
         if constexpr (GK == GK_TABLE) {
 #pragma unroll
             for (int h = 0; h < NT; ++h) {
-                table_entry<PREC>(sc, tpos, on[h], sb, c[h], sx[h], g[h], p.bond_near > 0);
+                table_entry<PREC>(sc, tpos, on[h], sb, c[h], sx[h], g[h]);
                 tpos += on[h] ? 1 : 0;
             }
             if (!FILL && p.bond_pf > 0) {
@@ -318,19 +314,8 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
             continue;
         }
         V xv[NT];
-        if (GK == GK_TABLE && p.bond_near > 0) {
-            // near targets (column within bond_near rows of the row: the window the warps in flight
-            // share) keep the default policy; far ones are streamed (evict-first) so that they do not
-            // push the near window out of L2
 #pragma unroll
-            for (int h = 0; h < NT; ++h) {
-                const long long d = c[h] - row;
-                xv[h] = (c[h] < 0) ? czero<V>() : ((d < p.bond_near && d > -p.bond_near) ? x[c[h]] : __ldcs(x + c[h]));
-            }
-        } else {
-#pragma unroll
-            for (int h = 0; h < NT; ++h) xv[h] = (c[h] >= 0) ? x[c[h]] : czero<V>();
-        }
+        for (int h = 0; h < NT; ++h) xv[h] = (c[h] >= 0) ? x[c[h]] : czero<V>();
 #pragma unroll
         for (int h = 0; h < NT; ++h) {
             if (GRAD && c[h] >= 0) {
@@ -431,9 +416,11 @@ __global__ void __launch_bounds__(HX_THREADS) hx_bond_kernel(const HxParams p) {
         bond_tile<W, GK, PREC, NT, false, UNI>(p, tb, bt, sc, tile, lane);
 }
 
-// All sectors of a batch in one persistent launch (the tile numbering of hx_multi_kernel).
+// All sectors of a batch in one persistent launch (the tile numbering of hx_multi_kernel).  With eight
+// targets per step the kernel is held to three resident blocks per SM instead of four, so that like the
+// one-sector launch it keeps its eight entries and gathers in registers.
 template <typename W, int GK, int PREC, int NT>
-__global__ void __launch_bounds__(HX_THREADS, 4) hx_bond_multi_kernel(const HxParams p) {
+__global__ void __launch_bounds__(HX_THREADS, NT == 8 ? 3 : 4) hx_bond_multi_kernel(const HxParams p) {
     typedef typename Cx<PREC>::V V;
     extern __shared__ __align__(16) unsigned char sm[];
     // programmatic dependent launch: the next kernel in the stream may start its own prologue now;

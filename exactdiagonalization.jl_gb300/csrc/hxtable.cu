@@ -126,7 +126,7 @@ void fill_one(int gk, const HxParams& p, long long n_tiles, size_t smem, cudaStr
 
 template <typename W>
 void launch_t(int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t st, bool multi) {
-    const int nt = p.bond_nt == 8 ? (multi ? 4 : 8) : p.bond_nt == 4 ? 4 : 2;
+    const int nt = p.bond_nt == 8 ? 8 : p.bond_nt == 4 ? 4 : 2;
 #define EDGPU_TABLE_CASE(PR, NTV)                                                                          \
     if (prec == PR && nt == NTV) {                                                                         \
         if (multi) return hx_bond_multi_launch_one<W, GK_TABLE, PR, NTV>(p, blocks, smem, st);             \
@@ -143,8 +143,12 @@ void launch_t(int prec, const HxParams& p, int blocks, size_t smem, cudaStream_t
     EDGPU_TABLE_CASE(0, 4)
     EDGPU_TABLE_CASE(1, 2)
     EDGPU_TABLE_CASE(1, 4)
-    // eight targets per step: one-sector launches only (the batched kernel stays at four)
-    if (nt == 8 && !multi) {
+    // eight targets per step (one-sector and batched launches)
+    if (nt == 8) {
+        if (multi) {
+            if (prec == 0) return hx_bond_multi_launch_one<W, GK_TABLE, 0, 8>(p, blocks, smem, st);
+            return hx_bond_multi_launch_one<W, GK_TABLE, 1, 8>(p, blocks, smem, st);
+        }
         if (prec == 0) return hx_bond_launch_one<W, GK_TABLE, 0, 8>(p, blocks, smem, st);
         return hx_bond_launch_one<W, GK_TABLE, 1, 8>(p, blocks, smem, st);
     }
@@ -162,7 +166,9 @@ int occupancy_t(int prec, int nt, size_t smem, bool multi, bool uni) {
     }
     if (nt == 8 && !multi)
         return prec == 0 ? hx_bond_occupancy_one<W, GK_TABLE, 0, 8>(smem) : hx_bond_occupancy_one<W, GK_TABLE, 1, 8>(smem);
-    if (nt == 8) nt = 4;
+    if (nt == 8)
+        return prec == 0 ? hx_bond_multi_occupancy_one<W, GK_TABLE, 0, 8>(smem)
+                         : hx_bond_multi_occupancy_one<W, GK_TABLE, 1, 8>(smem);
     if (prec == 0 && nt != 4) return multi ? hx_bond_multi_occupancy_one<W, GK_TABLE, 0, 2>(smem) : hx_bond_occupancy_one<W, GK_TABLE, 0, 2>(smem);
     if (prec == 0) return multi ? hx_bond_multi_occupancy_one<W, GK_TABLE, 0, 4>(smem) : hx_bond_occupancy_one<W, GK_TABLE, 0, 4>(smem);
     if (nt != 4) return multi ? hx_bond_multi_occupancy_one<W, GK_TABLE, 1, 2>(smem) : hx_bond_occupancy_one<W, GK_TABLE, 1, 2>(smem);

@@ -64,6 +64,9 @@ SIGNATURES = {
     "edgpu_reduce": (ctypes.c_int, [vp, i32, P(i32), P(u64), P(i32), i32, P(vp)]),
     "edgpu_reduce_mapping": (ctypes.c_int, [vp, P(i64), P(dbl), i64]),
     "edgpu_space_orbit_sizes": (ctypes.c_int, [vp, P(i32), i64]),
+    "edgpu_space_parent_dim": (ctypes.c_int, [vp, P(i64)]),
+    "edgpu_symmetry_unreduce_device": (ctypes.c_int, [vp, i32, vp, i64, vp, i64, vp]),
+    "edgpu_symmetry_reduce_device": (ctypes.c_int, [vp, i32, vp, i64, vp, i64, vp]),
     "edgpu_op_create": (ctypes.c_int, [vp, i32, P(u64), P(u64), P(u64), P(dbl), P(i32), i32, P(dbl), P(vp)]),
     "edgpu_op_set_couplings": (ctypes.c_int, [vp, P(dbl), i32]),
     "edgpu_op_dim": (ctypes.c_int, [vp, P(i64)]),
@@ -79,7 +82,7 @@ SIGNATURES = {
     "edgpu_op_free_targets": (ctypes.c_int, [vp]),
     "edgpu_op_targets_info": (ctypes.c_int, [vp, P(i64), P(i32)]),
     "edgpu_op_build_adjoint_targets": (ctypes.c_int, [vp, i64, P(i32)]),
-    "edgpu_op_near_window": (ctypes.c_int, [vp, i32, i64, P(i64)]),
+    "edgpu_op_table_prefetch": (ctypes.c_int, [vp, i32, i32, P(i32)]),
     "edgpu_op_free_adjoint_targets": (ctypes.c_int, [vp]),
     "edgpu_batch_get_schedule": (ctypes.c_int, [vp, i32, P(i32), P(i32), P(i32)]),
     "edgpu_op_sparse": (ctypes.c_int, [vp, i32, dbl, P(i64), P(i64), P(i64), P(dbl)]),

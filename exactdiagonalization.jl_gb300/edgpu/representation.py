@@ -407,15 +407,36 @@ symmetry_reduce_serial = symmetry_reduce
 symmetry_reduce_parallel = symmetry_reduce
 
 
+def _parent_dim(rhsr) -> int:
+    n = ctypes.c_int64()
+    check(lib().edgpu_space_parent_dim(rhsr.handle, ctypes.byref(n)))
+    return int(n.value)
+
+
+def _device_vector_map(rhsr, v, unreduce: bool):
+    """symmetry_unreduce / symmetry_reduce on the device (edgpu_symmetry_unreduce_device /
+    edgpu_symmetry_reduce_device): CUDA tensors in and out (complex128: FP64, complex64: mixed); host
+    arrays go through a complex128 device round trip."""
+    import torch
+    n, npar = rhsr.dimension, _parent_dim(rhsr)
+    n_in, n_out = (n, npar) if unreduce else (npar, n)
+    if len(v) != n_in:
+        what = "reduced" if unreduce else "larger"
+        raise DimensionMismatch(f"Dimension of the input vector should match the {what} representation")
+    host = not _is_torch(v)
+    t = torch.from_numpy(np.ascontiguousarray(v, dtype=np.complex128)).cuda() if host else v
+    if not (t.is_cuda and t.is_contiguous() and t.dtype in (torch.complex128, torch.complex64)):
+        raise ArgumentError("the vector must be a contiguous complex CUDA tensor")
+    prec = FP64 if t.dtype == torch.complex128 else MIXED
+    out = torch.empty(n_out, dtype=t.dtype, device=t.device)
+    fn = lib().edgpu_symmetry_unreduce_device if unreduce else lib().edgpu_symmetry_reduce_device
+    check(fn(rhsr.handle, prec, ctypes.c_void_p(t.data_ptr()), n_in, ctypes.c_void_p(out.data_ptr()), n_out,
+             _torch_stream()))
+    return out.cpu().numpy() if host else out
+
+
 def _reduce_vector(rhsr: ReducedHilbertSpaceRepresentation, large):
-    large = np.asarray(large)
-    if large.shape != (rhsr.parent.dimension,):
-        raise DimensionMismatch("Dimension of the input vector should match the larger representation")
-    idx, amp = rhsr._get_mapping()
-    small = np.zeros(rhsr.dimension, dtype=np.result_type(large.dtype, np.complex128))
-    sel = idx >= 0
-    np.add.at(small, idx[sel], np.conj(amp[sel]) * large[sel])
-    return small
+    return _device_vector_map(rhsr, large, False)
 
 
 def search_stats(space) -> dict:
@@ -429,15 +450,10 @@ def search_stats(space) -> dict:
 
 
 def symmetry_unreduce(rhsr: ReducedHilbertSpaceRepresentation, small):
-    """symmetry_unreduce(rhsr, small_vector) -- symmetry_reduce.jl:208-225."""
-    small = np.asarray(small)
-    if small.shape != (rhsr.dimension,):
-        raise DimensionMismatch("Dimension of the input vector should match the reduced representation")
-    idx, amp = rhsr._get_mapping()
-    large = np.zeros(rhsr.parent.dimension, dtype=np.result_type(small.dtype, np.complex128))
-    sel = idx >= 0
-    large[sel] = amp[sel] * small[idx[sel]]
-    return large
+    """symmetry_unreduce(rhsr, small_vector) -- symmetry_reduce.jl:208-225: the parent-space vector
+    large[i] = ampl(p_i) small[rep(p_i)], computed on the device without parent-sized tables.  CUDA
+    tensors stay on the device; host arrays come back as complex128 numpy arrays."""
+    return _device_vector_map(rhsr, small, True)
 
 
 def translation_symops(shape, momentum=(0, 0)) -> List[Tuple[SitePermutation, complex]]:
@@ -607,12 +623,12 @@ class OperatorRepresentation:
         check(lib().edgpu_op_build_targets(self._h, int(max_bytes), ctypes.byref(built)))
         return bool(built.value)
 
-    def near_window(self, precision="mixed", rows: Optional[int] = None) -> int:
-        """Cache policy of the target-table product: with rows > 0 the table and the gathers of targets
-        at least `rows` rows from their row are streamed (evict-first) so that L2 keeps the shared
-        window of x; 0 turns it off.  Returns the setting (after setting it when rows is given)."""
-        cur = ctypes.c_int64()
-        check(lib().edgpu_op_near_window(self._h, _prec(precision), -1 if rows is None else int(rows), ctypes.byref(cur)))
+    def table_prefetch(self, precision="mixed", steps: Optional[int] = None) -> int:
+        """x prefetch distance (in steps) of the target-table product; sets it when steps is given.
+        Returns the setting."""
+        cur = ctypes.c_int32()
+        check(lib().edgpu_op_table_prefetch(self._h, _prec(precision), -1 if steps is None else int(steps),
+                                            ctypes.byref(cur)))
         return int(cur.value)
 
     def build_adjoint_targets(self, max_bytes: Optional[int] = None) -> bool:

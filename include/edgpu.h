@@ -132,6 +132,22 @@ int edgpu_reduce(edgpu_space parent, int32_t n_elems, const int32_t* site_maps, 
  * (reduced_hilbert_space_representation.jl:13-22) materialised for a parent of n_parent states:
  * index_out[n_parent] (reduced index or -1), ampl_out[2*n_parent].  Requires a materialised parent. */
 int edgpu_reduce_mapping(edgpu_space reduced, int64_t* index_out, double* ampl_out, int64_t n_parent);
+/* Dimension of the parent of a reduced representation (its sector's size; for a lazy parent the number
+ * of words of its popcount). */
+int edgpu_space_parent_dim(edgpu_space reduced, int64_t* out);
+/* symmetry_unreduce(rhsr, small) (symmetry_reduce.jl:208-225): large[i] = ampl(p_i) small[rep(p_i)] for
+ * every parent state p_i (0 where its orbit has no representative), and symmetry_reduce(rhsr, large)
+ * (symmetry_reduce.jl:38-56): small[c] = sum over the orbit of rep_c of conj(ampl(p)) large[i(p)], on
+ * DEVICE vectors (complex128 for EDGPU_FP64, complex64 for EDGPU_MIXED).  The reference reads its
+ * parent-sized tables; here each entry's representative, stabiliser and group element are recomputed,
+ * so no table is built (the 6x6 torus's parent vector of 9.1e9 entries fits where the tables do not).
+ * Parent index i: position in the materialised parent basis, or the colex rank for a lazy parent.
+ * The reduction sums each orbit in a fixed element order (reproducible, no atomics).  The calls return
+ * after the work is done; stream NULL uses the space's own stream. */
+int edgpu_symmetry_unreduce_device(edgpu_space reduced, int32_t precision, const void* small, int64_t n, void* large,
+                                   int64_t n_parent, void* stream);
+int edgpu_symmetry_reduce_device(edgpu_space reduced, int32_t precision, const void* large, int64_t n_parent, void* small,
+                                 int64_t n, void* stream);
 /* Orbit size |O| of every representative (1/sqrt(|O|) is the reference's amplitude of a representative). */
 int edgpu_space_orbit_sizes(edgpu_space reduced, int32_t* out, int64_t n);
 
@@ -204,12 +220,9 @@ int edgpu_op_get_schedule(edgpu_op op, int32_t precision, int32_t* rows_per_tile
  * allow the pair-flip schedule and the table needs at most max_bytes; *built = 0 otherwise. */
 int edgpu_op_build_targets(edgpu_op op, int64_t max_bytes, int32_t* built);
 int edgpu_op_free_targets(edgpu_op op);
-/* Cache policy of the target-table product for this precision: rows > 0 loads the table, and the x of
- * every target whose column is at least `rows` rows away from its row, with the evict-first
- * (streaming) policy, so that L2 keeps the window of x that the rows in flight share; 0 uses the
- * default policy everywhere; rows < 0 only queries.  *current (nullable) receives the setting.  The
- * autotuner chooses it for sectors whose x exceeds a quarter of L2.  Results do not depend on it. */
-int edgpu_op_near_window(edgpu_op op, int32_t precision, int64_t rows, int64_t* current);
+/* x prefetch distance of the target-table product for this precision, in steps of targets (0: none;
+ * steps < 0 only queries; *current nullable).  Chosen by edgpu_op_autotune; results do not depend on it. */
+int edgpu_op_table_prefetch(edgpu_op op, int32_t precision, int32_t steps, int32_t* current);
 /* Adjoint target table (no reference counterpart): for every column c of the product's matrix, the
  * rows r whose targets land on c with their slots, sorted.  It serves edgpu_mul_adjoint_device for
  * terms that do not commute with the group (whose adjoint is not the row formula of the adjoint

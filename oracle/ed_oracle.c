@@ -314,14 +314,49 @@ int64_t or_popcount_basis(int n, int k, uint64_t* out, int64_t cap) {
  *     conj(y_i) of that i over sqrt(#distinct members) (:39, :79-85).
  * Restricted to parents that are one popcount sector of 1-bit sites (every spin-1/2 2Sz sector):
  * get(basis_lookup, bcol, -1) on such a parent is -1 exactly when popcount(bcol) differs. */
+static uint64_t torus_apply(uint64_t v, int L1, int L2, int a, int b, const uint64_t* keep) {
+    const int n = L1 * L2;
+    const uint64_t full = (n >= 64) ? ~0ull : ((1ull << n) - 1ull);
+    /* rows up by b: bit x + L1*y -> x + L1*((y+b) mod L2), a rotation of the n-bit word by L1*b */
+    const int s = (L1 * b) % n;
+    if (s) v = ((v << s) | (v >> (n - s))) & full;
+    /* every row rotated by a within its L1 bits: bits that do not wrap move up by a, the others
+     * move down by L1 - a (keep[a] marks the bits of each row that do not wrap) */
+    if (a) v = ((v & keep[a]) << a) | ((v & ~keep[a] & full) >> (L1 - a));
+    return v;
+}
+
+/* Row masks of the torus rotations: keep[a] marks, in every row of L1 bits, the bits that a rotation
+ * by a within the row moves up without wrapping. */
+static void torus_keep(int L1, int L2, uint64_t* keep) {
+    for (int a = 0; a < L1; ++a) {
+        uint64_t row = 0;
+        for (int x = 0; x + a < L1; ++x) row |= 1ull << x;
+        keep[a] = 0;
+        for (int y = 0; y < L2; ++y) keep[a] |= row << (L1 * y);
+    }
+}
+
 typedef struct { uint64_t rep; int compatible; int n_distinct; cplx ampl; } orbit_info;
 
-static orbit_info orbit_of(uint64_t q, int n_sites, const int32_t* bw, const int32_t* off, int G,
-                           const int32_t* maps, const uint64_t* flips, const cplx* y, double tol) {
+/* g.v for element g: the site permutation (symmetry_apply.jl:82-92), or, when the group is the
+ * translation group of an L1 x L2 torus of 1-bit sites listed as g = a + L1 b (tor != NULL: L1, L2 and
+ * the row masks), the same permutation by word rotations. */
+typedef struct { int L1, L2; uint64_t keep[33]; } torus_spec;
+
+static inline uint64_t group_apply(int g, uint64_t v, int n_sites, const int32_t* bw, const int32_t* off,
+                                   const int32_t* maps, const uint64_t* flips, const torus_spec* tor) {
+    if (tor) return torus_apply(v, tor->L1, tor->L2, g % tor->L1, g / tor->L1, tor->keep);
+    return or_symmetry_apply(n_sites, bw, off, maps + (size_t)g * n_sites, flips ? flips[g] : 0ull, v);
+}
+
+static orbit_info orbit_of_t(uint64_t q, int n_sites, const int32_t* bw, const int32_t* off, int G,
+                             const int32_t* maps, const uint64_t* flips, const cplx* y, double tol,
+                             const torus_spec* tor) {
     orbit_info o;
     uint64_t rep = q;
     for (int g = 1; g < G; ++g) {
-        uint64_t t = or_symmetry_apply(n_sites, bw, off, maps + (size_t)g * n_sites, flips ? flips[g] : 0ull, q);
+        uint64_t t = group_apply(g, q, n_sites, bw, off, maps, flips, tor);
         if (t < rep) rep = t;
     }
     o.rep = rep;
@@ -333,8 +368,7 @@ static orbit_info orbit_of(uint64_t q, int n_sites, const int32_t* bw, const int
     int nd = 0, last_q = -1;
     if (G > 4096) { o.compatible = -1; return o; }
     for (int i = 0; i < G; ++i) {
-        uint64_t s = (i == 0) ? rep : or_symmetry_apply(n_sites, bw, off, maps + (size_t)i * n_sites,
-                                                           flips ? flips[i] : 0ull, rep);
+        uint64_t s = (i == 0) ? rep : group_apply(i, rep, n_sites, bw, off, maps, flips, tor);
         if (i > 0 && s == rep) {
             double dr = y[i].re - 1.0, di = y[i].im;
             if (!(sqrt(dr * dr + di * di) <= tol)) o.compatible = 0;
@@ -353,6 +387,11 @@ static orbit_info orbit_of(uint64_t q, int n_sites, const int32_t* bw, const int
         o.ampl.im = ph.im * inv_norm;
     }
     return o;
+}
+
+static orbit_info orbit_of(uint64_t q, int n_sites, const int32_t* bw, const int32_t* off, int G,
+                           const int32_t* maps, const uint64_t* flips, const cplx* y, double tol) {
+    return orbit_of_t(q, n_sites, bw, off, G, maps, flips, y, tol, NULL);
 }
 
 /* Orbit data of m states: representative, compatibility (1/0), #distinct members and the mapping
@@ -384,11 +423,42 @@ void or_orbit_info(int n_sites, const int32_t* bw, const int32_t* off, int G, co
  * status[j]: 0 ok; 1 basis_list[r] is not its orbit's representative; 2 its orbit is not kept;
  * 3 a column's representative is missing from basis_list.  nnz_out[j]: off-diagonal elements with a
  * valid column (row == col terms are diagonal). */
+static void sampled_rows(const uint64_t* basis, int64_t n_r, int parent_popcount, int n_sites, const int32_t* bw,
+                         const int32_t* off, int G, const int32_t* maps, const uint64_t* flips, const double* ampl,
+                         double tol, int T, const uint64_t* masks, const uint64_t* rows, const uint64_t* cols,
+                         const double* amps, const double* state, const int64_t* sample, int64_t m, double* out,
+                         int32_t* status, int64_t* nnz_out, const torus_spec* tor);
+
 void or_sampled_rows(const uint64_t* basis, int64_t n_r, int parent_popcount, int n_sites, const int32_t* bw,
                      const int32_t* off, int G, const int32_t* maps, const uint64_t* flips, const double* ampl,
                      double tol, int T, const uint64_t* masks, const uint64_t* rows, const uint64_t* cols,
                      const double* amps, const double* state, const int64_t* sample, int64_t m, double* out,
                      int32_t* status, int64_t* nnz_out) {
+    sampled_rows(basis, n_r, parent_popcount, n_sites, bw, off, G, maps, flips, ampl, tol, T, masks, rows, cols,
+                 amps, state, sample, m, out, status, nnz_out, NULL);
+}
+
+/* The same rows with the translations of an L1 x L2 torus (elements g = a + L1 b, as listed by the
+ * caller's maps) applied by word rotations instead of the site loop: identical results, used where
+ * the host time of the restatement is measured. */
+void or_sampled_rows_torus(int L1, int L2, const uint64_t* basis, int64_t n_r, int parent_popcount, int n_sites,
+                           const int32_t* bw, const int32_t* off, int G, const int32_t* maps, const double* ampl,
+                           double tol, int T, const uint64_t* masks, const uint64_t* rows, const uint64_t* cols,
+                           const double* amps, const double* state, const int64_t* sample, int64_t m, double* out,
+                           int32_t* status, int64_t* nnz_out) {
+    torus_spec tor;
+    tor.L1 = L1;
+    tor.L2 = L2;
+    torus_keep(L1, L2, tor.keep);
+    sampled_rows(basis, n_r, parent_popcount, n_sites, bw, off, G, maps, NULL, ampl, tol, T, masks, rows, cols,
+                 amps, state, sample, m, out, status, nnz_out, &tor);
+}
+
+static void sampled_rows(const uint64_t* basis, int64_t n_r, int parent_popcount, int n_sites, const int32_t* bw,
+                         const int32_t* off, int G, const int32_t* maps, const uint64_t* flips, const double* ampl,
+                         double tol, int T, const uint64_t* masks, const uint64_t* rows, const uint64_t* cols,
+                         const double* amps, const double* state, const int64_t* sample, int64_t m, double* out,
+                         int32_t* status, int64_t* nnz_out, const torus_spec* tor) {
     const cplx* y = (const cplx*)ampl;
     const cplx* a = (const cplx*)amps;
     const cplx* x = (const cplx*)state;
@@ -402,7 +472,7 @@ void or_sampled_rows(const uint64_t* basis, int64_t n_r, int parent_popcount, in
         int st = 0;
         int64_t nnz = 0;
         cplx acc = {0.0, 0.0};
-        orbit_info orow = orbit_of(brow, n_sites, bw, off, G, maps, flips, y, tol);
+        orbit_info orow = orbit_of_t(brow, n_sites, bw, off, G, maps, flips, y, tol, tor);
         if (orow.rep != brow) st = 1;
         else if (orow.compatible != 1) st = 2;
         const cplx inv_ampl_row = c_inv(orow.ampl);
@@ -410,7 +480,7 @@ void or_sampled_rows(const uint64_t* basis, int64_t n_r, int parent_popcount, in
             if ((brow & masks[t]) != rows[t]) continue;
             const uint64_t bcol = (brow & ~masks[t]) | cols[t];
             if (parent_popcount >= 0 && __builtin_popcountll(bcol) != parent_popcount) continue;
-            orbit_info oc = orbit_of(bcol, n_sites, bw, off, G, maps, flips, y, tol);
+            orbit_info oc = orbit_of_t(bcol, n_sites, bw, off, G, maps, flips, y, tol, tor);
             if (oc.compatible != 1) continue;
             const int64_t icol = or_lookup(basis, n_r, oc.rep);
             if (icol < 0) { st = 3; break; }
@@ -435,18 +505,6 @@ void or_sampled_rows(const uint64_t* basis, int64_t n_r, int parent_popcount, in
  * The sector is split into nchunks colex-ranked chunks handled by OpenMP threads; each chunk's
  * representatives are counted first, then written at their offsets.  Returns the number of
  * representatives (out may be NULL to count only). */
-static uint64_t torus_apply(uint64_t v, int L1, int L2, int a, int b, const uint64_t* keep) {
-    const int n = L1 * L2;
-    const uint64_t full = (n >= 64) ? ~0ull : ((1ull << n) - 1ull);
-    /* rows up by b: bit x + L1*y -> x + L1*((y+b) mod L2), a rotation of the n-bit word by L1*b */
-    const int s = (L1 * b) % n;
-    if (s) v = ((v << s) | (v >> (n - s))) & full;
-    /* every row rotated by a within its L1 bits: bits that do not wrap move up by a, the others
-     * move down by L1 - a (keep[a] marks the bits of each row that do not wrap) */
-    if (a) v = ((v & keep[a]) << a) | ((v & ~keep[a] & full) >> (L1 - a));
-    return v;
-}
-
 static double binom_d(int n, int k) {
     if (k < 0 || k > n) return 0.0;
     double r = 1.0;
@@ -479,12 +537,7 @@ int64_t or_torus_reps(int L1, int L2, int n_up, const int32_t* num, int den, int
     const int n = L1 * L2;
     if (n < 1 || n > 63 || n_up < 0 || n_up > n || L1 > 32) return -1;
     uint64_t keep[33];
-    for (int a = 0; a < L1; ++a) {
-        uint64_t row = 0;
-        for (int x = 0; x + a < L1; ++x) row |= 1ull << x;
-        keep[a] = 0;
-        for (int y = 0; y < L2; ++y) keep[a] |= row << (L1 * y);
-    }
+    torus_keep(L1, L2, keep);
     const uint64_t total = (uint64_t)binom_d(n, n_up);
     if (nchunks < 1) nchunks = 1;
     int64_t* cnt = (int64_t*)calloc((size_t)nchunks + 1, sizeof(int64_t));

@@ -67,6 +67,10 @@ def lib():
         L.or_orbit_info.restype = None
         L.or_orbit_info.argtypes = [ctypes.c_int, i32p, i32p, ctypes.c_int, i32p, u64p, dp, ctypes.c_double, u64p,
                                     ctypes.c_int64, u64p, i32p, i32p, dp]
+        L.or_sampled_rows_torus.restype = None
+        L.or_sampled_rows_torus.argtypes = [ctypes.c_int, ctypes.c_int, u64p, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
+                                            i32p, i32p, ctypes.c_int, i32p, dp, ctypes.c_double, ctypes.c_int, u64p,
+                                            u64p, u64p, dp, dp, i64p, ctypes.c_int64, dp, i32p, i64p]
         L.or_torus_reps.restype = ctypes.c_int64
         L.or_torus_reps.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, i32p, ctypes.c_int, ctypes.c_int, u64p]
         L.or_sampled_rows.restype = None
@@ -428,7 +432,7 @@ class OrbitTables:
     (a spin-1/2 2Sz sector).  `basis_list` is the sorted representative table under test; every
     representative a sampled row reaches is looked up in it (a missing one is reported)."""
 
-    def __init__(self, n_sites, parent_popcount, maps, amps, basis_list, flips=None, tol: float = RTOL):
+    def __init__(self, n_sites, parent_popcount, maps, amps, basis_list, flips=None, tol: float = RTOL, torus=None):
         self.n = int(n_sites)
         self.k = int(parent_popcount)
         self.bw = np.ones(self.n, dtype=np.int32)
@@ -439,6 +443,9 @@ class OrbitTables:
         self.flips = None if flips is None else np.ascontiguousarray(flips, dtype=np.uint64)
         self.tol = float(tol)
         self.basis_list = np.ascontiguousarray(basis_list, dtype=np.uint64)
+        # torus=(L1, L2): the group is the torus translation group in translation_symops's order;
+        # rows() then applies its elements by word rotations (same results, faster), for timing
+        self.torus = torus
 
     def orbit_info(self, states):
         """(representative, kept (bool), #distinct members, mapping amplitude) of every state."""
@@ -472,14 +479,17 @@ class OrbitTables:
         out = np.empty(m, dtype=np.complex128)
         st = np.empty(m, dtype=np.int32)
         nnz = np.empty(m, dtype=np.int64)
-        lib().or_sampled_rows(_p(self.basis_list, ctypes.c_uint64), self.basis_list.size, self.k, self.n,
-                              _p(self.bw, ctypes.c_int32), _p(self.off, ctypes.c_int32), self.G,
-                              _p(self.maps, ctypes.c_int32), _p(self.flips, ctypes.c_uint64),
-                              _p(self.amps.view(np.float64), ctypes.c_double), self.tol, len(masks),
-                              _p(masks, ctypes.c_uint64), _p(rows, ctypes.c_uint64), _p(cols, ctypes.c_uint64),
-                              _p(amps.view(np.float64), ctypes.c_double), _p(x.view(np.float64), ctypes.c_double),
-                              _p(sample, ctypes.c_int64), m, _p(out.view(np.float64), ctypes.c_double),
-                              _p(st, ctypes.c_int32), _p(nnz, ctypes.c_int64))
+        common = (_p(self.basis_list, ctypes.c_uint64), self.basis_list.size, self.k, self.n,
+                  _p(self.bw, ctypes.c_int32), _p(self.off, ctypes.c_int32), self.G, _p(self.maps, ctypes.c_int32))
+        tail = (_p(self.amps.view(np.float64), ctypes.c_double), self.tol, len(masks),
+                _p(masks, ctypes.c_uint64), _p(rows, ctypes.c_uint64), _p(cols, ctypes.c_uint64),
+                _p(amps.view(np.float64), ctypes.c_double), _p(x.view(np.float64), ctypes.c_double),
+                _p(sample, ctypes.c_int64), m, _p(out.view(np.float64), ctypes.c_double),
+                _p(st, ctypes.c_int32), _p(nnz, ctypes.c_int64))
+        if self.torus is not None and self.flips is None:
+            lib().or_sampled_rows_torus(int(self.torus[0]), int(self.torus[1]), *common, *tail)
+        else:
+            lib().or_sampled_rows(*common, _p(self.flips, ctypes.c_uint64), *tail)
         return out, st, nnz
 
 

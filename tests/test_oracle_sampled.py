@@ -137,3 +137,20 @@ def test_torus_representatives_match_the_sweep(shape, k, n_up):
     maps, amps = O.translation_symops(shape, k)
     red = O.symmetry_reduce(parent, bw, off, maps, amps)
     assert np.array_equal(O.torus_representatives(shape, n_up, k), red.basis_list)
+
+
+@pytest.mark.parametrize("shape,k", [((6, 4), (1, 2)), ((5, 4), (0, 0)), ((6, 3), (3, 1))])
+def test_orbit_tables_torus_rotations_equal_site_loop(shape, k):
+    """The torus variant of the orbit-by-orbit rows (elements applied by word rotations, used where the
+    host restatement is timed) gives exactly the rows of the site-permutation loop."""
+    L1, L2 = shape
+    n = L1 * L2
+    basis = O.torus_representatives(shape, n // 2, k)
+    maps, amps = O.translation_symops(shape, k)
+    terms = _torus_terms(shape, [(1, 0), (0, 1)], [(1, 1)], 1.0, 0.4, 0.8, np.random.default_rng(2))
+    x = O.complex_gaussian(basis.size, 5)
+    rows = np.arange(basis.size)
+    a = O.OrbitTables(n, n // 2, maps, amps, basis).rows(terms, x, rows)
+    b = O.OrbitTables(n, n // 2, maps, amps, basis, torus=shape).rows(terms, x, rows)
+    for u, v in zip(a, b):
+        assert np.array_equal(u, v)

@@ -57,15 +57,20 @@ def test_noalloc_gradient_matches_allocating_entry_point(table, reduced):
         y_ref = torch.empty_like(x)
         g_ref = edgpu.coupling_grad(opr, x, gy, precision=prec, y=y_ref)
         y = torch.full_like(x, 7.0)
+        ny = torch.linalg.vector_norm(y_ref.to(torch.complex128)).item()
         torch.cuda.synchronize()
-        free0 = torch.cuda.mem_get_info()[0]
-        for call in range(2):
+        free0 = None
+        for call in range(3):
             g = np.full(L, np.nan)
             _lib.check(_noalloc(lib, _lib, opr, prec, x, gy, y, N, g, _torch_stream()))
             torch.cuda.synchronize()
             assert np.allclose(g, g_ref, rtol=tol, atol=tol), (call, g, g_ref)
             dy = torch.linalg.vector_norm((y - y_ref).to(torch.complex128)).item()
-            assert dy <= tol * max(1.0, torch.linalg.vector_norm(y_ref.to(torch.complex128)).item()), (call, dy)
+            assert dy <= tol * max(1.0, ny), (call, dy)
+            if free0 is None:
+                # the first call on a device may make the driver place the library's device globals
+                # (the scratch array) in memory; the later calls must change nothing
+                free0 = torch.cuda.mem_get_info()[0]
         assert torch.cuda.mem_get_info()[0] == free0, "the no-allocation entry point changed the free device memory"
         # new coupling values are written into the existing tables: still no allocation, new results
         J2 = J[::-1].copy()
