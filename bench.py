@@ -799,7 +799,11 @@ def run_gpu_grad(args, wl):
         raise RuntimeError(f"sector size {N} / nonzeros {nnz} differ from the workload's {wl['N_r']} / {wl['nnz_off']}")
     cfg = workload_config(dict(wl, nnz_off=nnz), args.workload)
     map_info = build_maps([space], args)
+    table_info = build_tables([opr], [space], args)
+    # the column-sorted adjoint table: the adjoint of these (non-invariant) terms as a gather in a fixed order
+    adjoint_table = bool(table_info and table_info.get("built")) and opr.build_adjoint_targets()
     opr.autotune("mixed")
+    opr.autotune("fp64")
     stream = torch.cuda.current_stream()
     res = {}
     for prec in ("mixed", "fp64"):
@@ -835,6 +839,8 @@ def run_gpu_grad(args, wl):
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
             "config": cfg,
             "gpu_setup": {"invariant_terms": opr.is_invariant, "setup_s": t_space, "parent_map": map_info,
+                          "target_table": table_info, "adjoint_table": adjoint_table,
+                          "grad_kernel": {"mixed": opr.grad_kernel("mixed"), "fp64": opr.grad_kernel("fp64")},
                           "ms": res, "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": b / t_fwd / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": b / t_fwd / 1e9 / peak, "traffic": None, "peak_source": peak_src},

@@ -2493,6 +2493,22 @@ int edgpu_mul_adjoint_device(edgpu_op oh, int32_t precision, const void* x, void
     API_END
 }
 
+int edgpu_op_grad_kernel(edgpu_op oh, int32_t precision, int32_t* kind) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
+    check_prec(precision);
+    require(kind, EDGPU_ERR_ARG, "null output");
+    build_blob(op, precision, 0, 1);
+    const Blob& B = op->blob[precision][0][1];
+    const size_t gsmem = align16(B.smem_bond) + (size_t)op->n_coupl * HX_THREADS * 8;
+    if (B.tmpl.o_bunit >= 0 && op->pair_allowed && (op->d_tab || op->space->d_map) && gsmem <= 200 * 1024)
+        *kind = op->d_tab ? 2 : 1;
+    else
+        *kind = ((size_t)B.tmpl.o_grad + (size_t)op->n_coupl * HX_THREADS * 8 <= 200 * 1024) ? 0 : -1;
+    API_END
+}
+
 int edgpu_coupling_grad_device(edgpu_op oh, int32_t precision, const void* x, const void* gy, void* y, int64_t n,
                                double* grad_out, void* stream) {
     API_BEGIN
@@ -2518,6 +2534,7 @@ int edgpu_coupling_grad_device(edgpu_op oh, int32_t precision, const void* x, co
         }
     }
     build_blob(op, precision, 0, 1);
+    build_blob(op, precision, 0, 0);   // the forward tables (diagonal), so that every gradient kernel finds them
     // partial sums of either gradient kernel: at most 8 resident blocks of 256 threads per SM
     const int max_blocks = std::max(op->blob[precision][0][1].max_blocks, 8 * std::max(1, g_sm_count));
     op->grad_partial.ensure((size_t)max_blocks * op->n_coupl);

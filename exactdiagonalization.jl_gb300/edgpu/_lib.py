@@ -83,6 +83,7 @@ SIGNATURES = {
     "edgpu_op_targets_info": (ctypes.c_int, [vp, P(i64), P(i32)]),
     "edgpu_op_build_adjoint_targets": (ctypes.c_int, [vp, i64, P(i32)]),
     "edgpu_op_table_prefetch": (ctypes.c_int, [vp, i32, i32, P(i32)]),
+    "edgpu_op_grad_kernel": (ctypes.c_int, [vp, i32, P(i32)]),
     "edgpu_op_free_adjoint_targets": (ctypes.c_int, [vp]),
     "edgpu_batch_get_schedule": (ctypes.c_int, [vp, i32, P(i32), P(i32), P(i32)]),
     "edgpu_op_sparse": (ctypes.c_int, [vp, i32, dbl, P(i64), P(i64), P(i64), P(dbl)]),

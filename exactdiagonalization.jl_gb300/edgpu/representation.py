@@ -623,6 +623,12 @@ class OperatorRepresentation:
         check(lib().edgpu_op_build_targets(self._h, int(max_bytes), ctypes.byref(built)))
         return bool(built.value)
 
+    def grad_kernel(self, precision="mixed") -> str:
+        """The kernel coupling_grad runs: "pair-flip table", "pair-flip map", "term scan" or "queued"."""
+        k = ctypes.c_int32()
+        check(lib().edgpu_op_grad_kernel(self._h, _prec(precision), ctypes.byref(k)))
+        return {2: "pair-flip table", 1: "pair-flip map", 0: "term scan", -1: "queued"}[k.value]
+
     def table_prefetch(self, precision="mixed", steps: Optional[int] = None) -> int:
         """x prefetch distance (in steps) of the target-table product; sets it when steps is given.
         Returns the setting."""

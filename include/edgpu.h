@@ -287,6 +287,10 @@ int edgpu_mul_adjoint_device(edgpu_op op, int32_t precision, const void* x, void
 int edgpu_coupling_grad_device(edgpu_op op, int32_t precision, const void* x, const void* gy, void* y,
                                int64_t n, double* grad_out, void* stream);
 
+/* Which kernel edgpu_coupling_grad_device runs for this precision (no reference counterpart): 2 the
+ * pair-flip gradient kernel through the target table, 1 through the parent-state map, 0 the
+ * row-per-lane term scan, -1 the queued term scan (couplings beyond the shared-memory accumulators). */
+int edgpu_op_grad_kernel(edgpu_op op, int32_t precision, int32_t* kind);
 /* The same fused product and coupling gradient for callers that cannot allocate device memory (their
  * device memory is owned by another allocator, e.g. a Julia or PyTorch memory pool, or they keep
  * allocation out of a time-step loop).  This entry point has no counterpart in the reference.  It

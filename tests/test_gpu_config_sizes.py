@@ -172,6 +172,7 @@ def test_chain28_random_bond_gradients_full_size(E):
     assert _rel(y32, y_ref) < 1e-5
     xd, gyd = torch.from_numpy(x).cuda(), torch.from_numpy(gy).cuda()
     yd = torch.empty_like(xd)
+    assert opr.grad_kernel("fp64") == "pair-flip table" and opr.grad_kernel("mixed") == "pair-flip table"
     g = E.coupling_grad(opr, xd, gyd, precision="fp64", y=yd)
     torch.cuda.synchronize()
     assert _rel(yd.cpu().numpy(), y_ref) < 1e-12
