@@ -720,6 +720,26 @@ def run_gpu_batch(args, wl):
     value = b_all / t_max / 1e9
     achieved = b_step / (ms / args.steps / 1e3) / 1e9
 
+    # the same sectors as separate products, each operator with its own autotuned schedule, launched
+    # one after the other on one stream (what a caller without the batch would do)
+    per_sector_ms = None
+    if not args.no_per_sector:
+        for o in oprs:
+            o.autotune("mixed")
+        xs, ys = sets[0]
+        for o, x, y in zip(oprs, xs, ys):
+            edgpu.mul_(y, o, x, precision="mixed")
+        torch.cuda.synchronize()
+        ps_steps = max(3, min(args.steps, 10))
+        e0.record(stream)
+        for i in range(ps_steps):
+            xs, ys = sets[i % P]
+            for o, x, y in zip(oprs, xs, ys):
+                edgpu.mul_(y, o, x, precision="mixed")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        per_sector_ms = e0.elapsed_time(e1) / ps_steps
+
     # library graph path (the call a user makes: captured once per pointer set, replayed)
     xs, ys = sets[0]
     batch.mul_(ys, xs, precision="mixed", use_graph=True)
@@ -761,7 +781,10 @@ def run_gpu_batch(args, wl):
                        "target_table": dict(table_info or {"built": False}, used=batch.uses_target_tables("mixed")),
                        "bond_classes": oprs[0].pair_classes()[0], "l2": f"inputs cycled from {P} sets of x/y ({2 * P * N * s_c / 1e6:.0f} MB "
                        f"> 2x L2)", "parallelism": f"replicas x{world}", "setup_s": t_space,
-                       "library_graph_ms_per_step": ms_graph, "parent_map": map_info},
+                       "library_graph_ms_per_step": ms_graph, "parent_map": map_info,
+                       "batch_launch": {0: "one persistent launch"}.get(batch.launch("mixed"),
+                                                                         f"per-sector launches on {batch.launch('mixed')} stream(s)"),
+                       "per_sector_launches_ms_per_step": per_sector_ms},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": profiled_traffic(args.workload), "peak_source": peak_src},
             "cpu_baseline": None if args.no_cpu_baseline else
@@ -873,6 +896,8 @@ def main():
     ap.add_argument("--no-table", action="store_true", help="no target tables (look every target up per product)")
     ap.add_argument("--no-pair", action="store_true", help="test every term per row instead of the pair-flip schedule")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-per-sector", action="store_true",
+                    help="batched workload: skip timing the sectors as separate products")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     if args.warmup < 3:

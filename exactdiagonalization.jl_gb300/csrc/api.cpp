@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <memory>
 #include <mutex>
 #include <thread>
@@ -199,6 +200,30 @@ struct edgpu_op_s {
     long long* d_adj_off = nullptr;
     unsigned long long* d_adj_tab = nullptr;
     int64_t adj_n = 0;
+    // column-slab table (optional, edgpu_op_build_slabs; mixed-precision products, hxslab.cu)
+    struct Slab {
+        unsigned* tab = nullptr;            // entries, pass after pass
+        unsigned char* counts = nullptr;    // [n_pass][dim] entries of each row in each pass
+        unsigned* off = nullptr;            // [n_pass][tiles] tile offsets relative to the pass
+        std::vector<long long> base;        // [n_pass + 1] first entry of each pass
+        int n_pass = 0, colbits = 0, n_ids = 0, den = 1, nd = 1;
+        long long wc = 0;                   // columns per slab
+        int64_t n = 0;                      // entries
+        std::vector<int> amp_cid;           // per amplitude id: its coupling id (-1: none)
+        std::vector<double> amp_unit;       // per amplitude id: unit amplitude (re, im)
+        std::vector<int> divs;              // orbit sizes by orbit-size index
+        DevBuf<float> lut;                  // coefficients by id: float, or (re, im) when !lut_real
+        int lut_real = 1;
+    } slab;
+    int slab_use[2] = {0, 0};         // [precision]: products read the slab table (chosen by the autotuner)
+    void free_slabs() {
+        if (slab.tab) cudaFree(slab.tab);
+        if (slab.counts) cudaFree(slab.counts);
+        if (slab.off) cudaFree(slab.off);
+        slab.lut.release();
+        slab = Slab();
+        slab_use[0] = slab_use[1] = 0;
+    }
     void free_table() {
         if (d_tab) cudaFree(d_tab);
         if (d_tile_off) cudaFree(d_tile_off);
@@ -217,6 +242,7 @@ struct edgpu_op_s {
         for (auto& kv : host_graphs) cudaGraphExecDestroy(kv.second);
         free_table();
         free_adjoint();
+        free_slabs();
     }
 };
 
@@ -232,6 +258,19 @@ struct edgpu_batch_s {
     int pair_nt[2] = {2, 2};                       // its targets per lane and step with sector maps
     int tab_use[2] = {1, 1};                       // read the sectors' target tables (autotuned)
     int tab_pf[2] = {0, 0};                        // their x prefetch distance in steps (autotuned)
+    // launch: 0 = all sectors in one persistent launch; k >= 1 = one product launch per sector (the
+    // operator's product kernel with the batch's schedule), spread over k streams that run
+    // concurrently (the calling stream alone for k = 1)
+    int seq[2] = {0, 0};
+    cudaStream_t lane_st[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t fork_ev = nullptr, join_ev[3] = {nullptr, nullptr, nullptr};
+    void ensure_lanes(int k) {
+        if (!fork_ev) EDGPU_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+        for (int i = 0; i < k; ++i) {
+            if (!lane_st[i]) EDGPU_CUDA(cudaStreamCreateWithFlags(&lane_st[i], cudaStreamNonBlocking));
+            if (!join_ev[i]) EDGPU_CUDA(cudaEventCreateWithFlags(&join_ev[i], cudaEventDisableTiming));
+        }
+    }
     struct Fused {
         bool ready = false;
         std::vector<uint64_t> gens;                // operator table generations the image was built from
@@ -259,6 +298,14 @@ struct edgpu_batch_s {
     ~edgpu_batch_s() {
         drop(0);
         drop(1);
+        for (int i = 0; i < 3; ++i) {
+            if (lane_st[i]) {
+                cudaStreamSynchronize(lane_st[i]);
+                cudaStreamDestroy(lane_st[i]);
+            }
+            if (join_ev[i]) cudaEventDestroy(join_ev[i]);
+        }
+        if (fork_ev) cudaEventDestroy(fork_ev);
     }
 };
 
@@ -542,13 +589,66 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     // gradient mode of the pair-flip kernel: unit amplitudes and coupling ids of the slots, and a copy
     // of the diagonal term records (mask, row, unit amplitude, coupling id)
     p.o_bunit = p.o_bcid = p.o_pdm = p.o_pdr = p.o_pdu = p.o_pdc = -1;
+    p.o_pdb = p.o_pdv = -1;
+    p.n_pdb = -1;
+    p.bunit_real = 0;
+    // the diagonal records by site pair: when every record's mask has at most two bits, the records of
+    // one (pair, coupling) become one entry with a unit amplitude per pattern of the pair's two bits
+    // (a one-bit mask is the pair (i, i), patterns 0 and 3; an empty mask adds to both), so that the
+    // gradient kernel looks up one value per entry and row instead of testing every record
+    struct DiagPair { int i, j, cid; double u[4][2]; };
+    std::vector<DiagPair> dpairs;
+    if (grad_pair) {
+        std::map<std::tuple<int, int, int>, int> at;
+        bool ok = true;
+        for (int k = 0; k < T_d && ok; ++k) {
+            const int t = diag[k];
+            const uint64_t m = op->masks[t];
+            const uint64_t r = dir ? op->cols[t] : op->rows[t];
+            const int pc = __builtin_popcountll(m);
+            if (pc > 2) {
+                ok = false;
+                break;
+            }
+            const int i = pc ? __builtin_ctzll(m) : 0;
+            const int j = pc == 2 ? 63 - __builtin_clzll(m) : i;
+            const auto key = std::make_tuple(i, j, op->cid[t]);
+            auto it = at.find(key);
+            if (it == at.end()) {
+                it = at.emplace(key, (int)dpairs.size()).first;
+                DiagPair d{};
+                d.i = i;
+                d.j = j;
+                d.cid = op->cid[t];
+                dpairs.push_back(d);
+            }
+            double v[2];
+            amp_of(t, true, v[0], v[1]);
+            DiagPair& d = dpairs[it->second];
+            for (int pat = 0; pat < 4; ++pat) {
+                const int bi = pat & 1, bj = pat >> 1;
+                if (pc == 1 && bi != bj) continue;   // pattern of the pair (i, i)
+                const bool match = pc == 0 || (((r >> i) & 1) == (uint64_t)bi && ((r >> j) & 1) == (uint64_t)bj);
+                if (match) {
+                    d.u[pat][0] += v[0];
+                    d.u[pat][1] += v[1];
+                }
+            }
+        }
+        if (!ok) dpairs.clear();
+        else p.n_pdb = (int)dpairs.size();
+    }
     if (grad_pair) {
         p.o_bunit = alloc((size_t)bc.ncls * n_b * 4 * vsz);
         p.o_bcid = alloc((size_t)bc.ncls * n_b * 4 * 4);
         p.o_pdm = alloc((size_t)T_d * wsz);
         p.o_pdr = alloc((size_t)T_d * wsz);
-        p.o_pdu = alloc((size_t)T_d * 16);
+        p.o_pdu = alloc((size_t)T_d * vsz);
         p.o_pdc = alloc((size_t)T_d * 4);
+        if (p.n_pdb >= 0) {
+            p.o_pdb = alloc(dpairs.size() * 4);
+            p.o_pdv = alloc(dpairs.size() * 4 * vsz);
+        }
     }
     // the prefix a mapped pair-flip launch copies ends here; the torus row table follows (needed by
     // canonicalisation only)
@@ -662,6 +762,7 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
         for (size_t i = 0; i < bc.flip.size() * 4; ++i) putv(p.o_bamp, i, bc.amp[2 * i], bc.amp[2 * i + 1]);
     }
     if (grad_pair) {
+        p.bunit_real = bcu.real ? 1 : 0;
         for (size_t i = 0; i < bcu.flip.size() * 4; ++i) putv(p.o_bunit, i, bcu.amp[2 * i], bcu.amp[2 * i + 1]);
         memcpy(&h[p.o_bcid], bc.cid.data(), bc.cid.size() * 4);
         for (int k = 0; k < T_d; ++k) {
@@ -671,8 +772,13 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
             putw(p.o_pdr, k, r);
             double v[2];
             amp_of(t, true, v[0], v[1]);
-            memcpy(&h[p.o_pdu + k * 16], v, 16);
+            putv(p.o_pdu, k, v[0], v[1]);
             memcpy(&h[p.o_pdc + k * 4], &op->cid[t], 4);
+        }
+        for (size_t k = 0; k < dpairs.size(); ++k) {
+            const int32_t e = dpairs[k].i | (dpairs[k].j << 8) | (dpairs[k].cid << 16);
+            memcpy(&h[p.o_pdb + k * 4], &e, 4);
+            for (int pat = 0; pat < 4; ++pat) putv(p.o_pdv, k * 4 + pat, dpairs[k].u[pat][0], dpairs[k].u[pat][1]);
         }
     }
 
@@ -801,6 +907,43 @@ void invalidate_blobs(edgpu_op_s* op) {
             }
 }
 
+// Coefficient table of the slab product for the current coupling values (mixed precision), written
+// into the table's existing buffer: id = ((amplitude id x den + character index) x nd + orbit-size
+// index of the row) x nd + orbit-size index of the column, coefficient = J_c u_a chi sqrt(|O_c| / |O_r|)
+// as the one-pass product forms it (hx_bond.cuh), here in FP64 and rounded once.
+void slab_refresh_lut(edgpu_op_s* op) {
+    auto& S = op->slab;
+    if (!S.tab) return;
+    const int na = (int)S.amp_cid.size();
+    bool real = S.den == 1;
+    for (int a = 0; a < na && real; ++a)
+        if (S.amp_unit[2 * a + 1] != 0.0) real = false;
+    std::vector<float> h((size_t)S.n_ids * 2, 0.f);
+    for (int id = 0; id < S.n_ids; ++id) {
+        int rest = id;
+        const int sxc = rest % S.nd;
+        rest /= S.nd;
+        const int sxr = rest % S.nd;
+        rest /= S.nd;
+        const int ph = rest % S.den;
+        const int a = rest / S.den;
+        if (a >= na) continue;
+        const double J = S.amp_cid[a] >= 0 ? op->coupl[S.amp_cid[a]] : 0.0;
+        const double ur = S.amp_unit[2 * a] * J, ui = S.amp_unit[2 * a + 1] * J;
+        const double ang = 2.0 * M_PI * (double)ph / (double)S.den;
+        const double cr = std::cos(ang), ci = std::sin(ang);
+        const double f = std::sqrt((double)S.divs[sxc] / (double)S.divs[sxr]);
+        const double re = (ur * cr - ui * ci) * f, im = (ur * ci + ui * cr) * f;
+        if (real) h[id] = (float)re;
+        else {
+            h[2 * (size_t)id] = (float)re;
+            h[2 * (size_t)id + 1] = (float)im;
+        }
+    }
+    S.lut_real = real ? 1 : 0;
+    EDGPU_CUDA(cudaMemcpy(S.lut.p, h.data(), (size_t)S.n_ids * (real ? 1 : 2) * sizeof(float), cudaMemcpyHostToDevice));
+}
+
 // New coupling values: every table built so far is rewritten in place (same layout, same device
 // buffers: nothing is allocated or freed), after the device has finished the work that may still
 // read the old values.  Tables not built yet are built on first use, as before.
@@ -810,7 +953,7 @@ void refresh_blobs(edgpu_op_s* op) {
     for (auto& a : op->blob)
         for (auto& b : a)
             for (auto& c : b) any = any || c.ready;
-    if (!any) return;
+    if (!any && !op->slab.tab) return;
     EDGPU_CUDA(cudaDeviceSynchronize());
     for (int prec = 0; prec < 2; ++prec)
         for (int dir = 0; dir < 2; ++dir)
@@ -820,6 +963,7 @@ void refresh_blobs(edgpu_op_s* op) {
                 B.ready = false;
                 build_blob(op, prec, dir, mode);
             }
+    slab_refresh_lut(op);
 }
 
 int blocks_for(const Blob& B, long long n_rows, int rows_per_tile) {
@@ -835,6 +979,12 @@ void set_map_params(HxParams& p, const Space& sp) {
     p.rank_k = sp.lay.popcount;
     p.rank_nc = (sp.lay.nbits + RANK_CHUNK - 1) / RANK_CHUNK;
     p.rank_split = sp.rank_split;
+}
+
+// Shared memory of the pair-flip gradient kernel's per-thread coupling accumulators (the product's
+// real type: FP32 in mixed precision, FP64 in FP64).
+static size_t pair_grad_acc_bytes(const edgpu_op_s* op, int prec) {
+    return (size_t)op->n_coupl * HX_THREADS * (prec == EDGPU_MIXED ? 4 : 8);
 }
 
 // y_c128 (mixed precision, product mode): when the launch goes through the pair-flip kernel, it writes
@@ -866,6 +1016,38 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
         p.map_cb = sp.map_cb;
         p.map_direct = sp.map_direct;
         if (rows > 0) rows = -1;
+    }
+    if (mode == 0 && dir == 0 && prec == EDGPU_MIXED && op->slab.tab && op->slab_use[prec] && op->pair_allowed &&
+        op->pair_use[prec] && rows < 0) {
+        // the column-slab table: one launch per slab (hxslab.cu); the last writes complex128 to
+        // y_c128 when given
+        const auto& S = op->slab;
+        SlabRun r{};
+        r.x = x;
+        r.y = y;
+        r.diag = B.d_diag;
+        r.lut = S.lut.p;
+        r.n_lut = S.n_ids;
+        r.lut_real = S.lut_real;
+        r.n_rows = p.n_rows;
+        r.n_tiles = (p.n_rows + 31) / 32;
+        r.colbits = S.colbits;
+        r.colmask = (unsigned)((1ull << S.colbits) - 1ull);
+        r.y_c128 = y_c128;
+        r.acc_c128 = acc_c128;
+        r.accumulate = y_c128 ? 0 : accumulate;
+        for (int q = 0; q < S.n_pass; ++q) {
+            r.cnt = S.counts + (size_t)q * p.n_rows;
+            r.off = S.off + (size_t)q * r.n_tiles;
+            r.tab = S.tab + S.base[q];
+            r.xs = (const float2*)x + (size_t)q * S.wc;
+            r.first = q == 0;
+            r.last = q == S.n_pass - 1;
+            hx_slab_launch(prec, r, st);
+        }
+        if (wrote_c128) *wrote_c128 = y_c128 != nullptr;
+        if (blocks_used) *blocks_used = 0;
+        return;
     }
     if (rows < 0 && mode == 0) {
         // row-per-lane strategy: -lpr lanes per row, one warp per 32/lpr consecutive rows
@@ -952,7 +1134,7 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
         const bool table = op->d_tab != nullptr;
         HxParams q = B.tmpl_pair;
         q.o_grad = (int)align16(B.smem_bond);
-        const size_t gsmem = (size_t)q.o_grad + (size_t)op->n_coupl * HX_THREADS * 8;
+        const size_t gsmem = (size_t)q.o_grad + pair_grad_acc_bytes(op, prec);
         if (gsmem <= 200 * 1024) {
             build_blob(op, prec, dir, 0);   // the forward diagonal table
             q.diag = op->blob[prec][dir][0].d_diag;
@@ -1911,6 +2093,189 @@ int edgpu_op_targets_info(edgpu_op oh, int64_t* entries, int32_t* entry_bytes) {
     API_END
 }
 
+int edgpu_op_build_slabs(edgpu_op oh, int64_t slab_bytes, int64_t max_bytes, int32_t* built) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
+    require(slab_bytes > 0 && max_bytes >= 0, EDGPU_ERR_ARG, "slab_bytes must be positive and max_bytes >= 0");
+    if (built) *built = 0;
+    EDGPU_CUDA(cudaDeviceSynchronize());   // products on caller streams may still read an old slab table
+    op->free_slabs();
+    const Space& sp = *op->space;
+    if (!op->d_tab || sp.dim == 0 || sp.dim >= ((int64_t)1 << 32)) return EDGPU_OK;
+    int prec = EDGPU_MIXED;
+    build_blob(op, prec, 0, 0);
+    if (op->blob[prec][0][0].tmpl.bond_ncls == 0) {
+        prec = EDGPU_FP64;
+        build_blob(op, prec, 0, 0);
+    }
+    const Blob& B = op->blob[prec][0][0];
+    if (B.tmpl.bond_ncls == 0) return EDGPU_OK;
+    // the slots' unit amplitudes and coupling ids: the FP64 gradient-mode image (absent when the terms
+    // of one slot have different couplings)
+    build_blob(op, EDGPU_FP64, 0, 1);
+    const Blob& G = op->blob[EDGPU_FP64][0][1];
+    const HxParams& gp = G.tmpl_pair;
+    const int nb = sp.lay.nbits, ncls = B.tmpl.bond_ncls;
+    if (G.tmpl.o_bunit < 0 || gp.bond_ncls != ncls) return EDGPU_OK;
+    const size_t wsz = sp.w32 ? 4 : 8;
+    const size_t fl_bytes = (size_t)ncls * nb * wsz;
+    if ((size_t)B.tmpl_pair.o_bflip + fl_bytes > B.pair_host.size() || (size_t)gp.o_bflip + fl_bytes > G.pair_host.size() ||
+        memcmp(&B.pair_host[B.tmpl_pair.o_bflip], &G.pair_host[gp.o_bflip], fl_bytes) != 0)
+        return EDGPU_OK;
+    // a row's targets in one slab are counted in a byte: at most 255 pairs
+    int n_pairs = 0;
+    for (int k = 0; k < ncls * nb; ++k) {
+        uint64_t f = 0;
+        memcpy(&f, &G.pair_host[gp.o_bflip + k * wsz], wsz);
+        n_pairs += f != 0;
+    }
+    if (n_pairs > 255) return EDGPU_OK;
+    auto& S = op->slab;
+    const int n_slots = ncls * nb * 4;
+    std::vector<unsigned short> amp_id((size_t)n_slots, 0);
+    std::map<std::tuple<int, double, double>, int> ids;
+    for (int k = 0; k < n_slots; ++k) {
+        double u[2];
+        int32_t c = -1;
+        memcpy(u, &G.pair_host[gp.o_bunit + (size_t)k * 16], 16);
+        memcpy(&c, &G.pair_host[gp.o_bcid + (size_t)k * 4], 4);
+        if (c < 0) continue;
+        const auto key = std::make_tuple((int)c, u[0], u[1]);
+        auto it = ids.find(key);
+        if (it == ids.end()) {
+            it = ids.emplace(key, (int)S.amp_cid.size()).first;
+            S.amp_cid.push_back(c);
+            S.amp_unit.push_back(u[0]);
+            S.amp_unit.push_back(u[1]);
+        }
+        amp_id[k] = (unsigned short)it->second;
+    }
+    const int n_amp = std::max<int>(1, (int)S.amp_cid.size());
+    S.den = std::max(1, sp.group.den);
+    S.divs.clear();
+    for (int d = 1; d <= sp.group.G; ++d)
+        if (sp.group.G % d == 0) S.divs.push_back(d);
+    S.nd = (int)S.divs.size();
+    const long long n_ids = (long long)n_amp * S.den * S.nd * S.nd;
+    int idbits = 1;
+    while (((long long)1 << idbits) < n_ids) ++idbits;
+    const int colbits = 32 - idbits;
+    if (colbits < 12 || n_ids * 8 > 48 * 1024 || n_amp > 65535) {
+        op->free_slabs();
+        return EDGPU_OK;
+    }
+    const long long wc = std::max<long long>(1024, std::min<long long>(slab_bytes / 8, (long long)1 << colbits));
+    const int n_pass = (int)((sp.dim + wc - 1) / wc);
+    const long long n_tiles = (sp.dim + 31) / 32;
+    if (n_pass > 64) {
+        op->free_slabs();
+        return EDGPU_OK;
+    }
+    HxParams p = B.tmpl_pair;
+    p.blob = B.d_pair;
+    p.blob_words16 = (int)(B.smem_bond / 16);
+    p.lpr = 1;
+    p.rows_per_tile = 32;
+    p.tab = op->d_tab;
+    p.tile_off = op->d_tile_off;
+    p.tab_wide = op->tab_wide;
+    p.tab_cb = op->tab_cb;
+    cudaStream_t st = op->hs.stream();
+    SlabBuild sb{};
+    sb.wc = wc;
+    sb.n_pass = n_pass;
+    sb.n_tiles = n_tiles;
+    sb.colbits = colbits;
+    sb.n_slots = n_slots;
+    sb.o_ctr = (int)align16(B.smem_bond);
+    const size_t meta = (size_t)n_pass * sp.dim + (size_t)n_pass * n_tiles * 4;
+    if ((double)meta > (double)max_bytes) {
+        op->free_slabs();
+        return EDGPU_OK;
+    }
+    DevBuf<unsigned> tile_sum;
+    DevBuf<unsigned short> d_amp;
+    DevBuf<long long> d_base;
+    try {
+        EDGPU_CUDA(cudaMalloc(&S.counts, std::max<size_t>((size_t)n_pass * sp.dim, 16)));
+        EDGPU_CUDA(cudaMalloc(&S.off, std::max<size_t>((size_t)n_pass * n_tiles * 4, 16)));
+        tile_sum.ensure((size_t)n_pass * n_tiles);
+        sb.counts = S.counts;
+        sb.tile_sum = tile_sum.p;
+        hx_slab_build(sp.w32, prec, 1, p, sb, (size_t)sb.o_ctr + (size_t)n_pass * HX_THREADS, st);
+        std::vector<unsigned long long> totals;
+        hx_slab_scan(tile_sum.p, S.off, n_pass, n_tiles, totals, st);
+        S.base.assign((size_t)n_pass + 1, 0);
+        for (int q = 0; q < n_pass; ++q) {
+            require(totals[q] < ((unsigned long long)1 << 32), EDGPU_ERR_ARG, "slab pass with 2^32 entries or more");
+            S.base[q + 1] = S.base[q] + (long long)totals[q];
+        }
+        S.n = S.base[n_pass];
+        if ((double)meta + (double)S.n * 4.0 > (double)max_bytes) {
+            op->free_slabs();
+            return EDGPU_OK;
+        }
+        EDGPU_CUDA(cudaMalloc(&S.tab, std::max<size_t>((size_t)S.n * 4, 16)));
+        d_amp.ensure((size_t)n_slots);
+        d_base.ensure((size_t)n_pass);
+        EDGPU_CUDA(cudaMemcpyAsync(d_amp.p, amp_id.data(), (size_t)n_slots * 2, cudaMemcpyHostToDevice, st));
+        EDGPU_CUDA(cudaMemcpyAsync(d_base.p, S.base.data(), (size_t)n_pass * 8, cudaMemcpyHostToDevice, st));
+        sb.off = S.off;
+        sb.base = d_base.p;
+        sb.tab = S.tab;
+        sb.amp_id = d_amp.p;
+        hx_slab_build(sp.w32, prec, 2, p, sb, (size_t)sb.o_ctr + (size_t)n_pass * HX_THREADS * 4, st);
+        EDGPU_CUDA(cudaStreamSynchronize(st));
+        S.n_pass = n_pass;
+        S.wc = wc;
+        S.colbits = colbits;
+        S.n_ids = (int)n_ids;
+        S.lut.ensure((size_t)n_ids * 2);
+        slab_refresh_lut(op);
+    } catch (...) {
+        cudaStreamSynchronize(st);
+        op->free_slabs();
+        throw;
+    }
+    op->slab_use[EDGPU_MIXED] = 1;
+    if (built) *built = 1;
+    API_END
+}
+
+int edgpu_op_free_slabs(edgpu_op oh) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
+    EDGPU_CUDA(cudaDeviceSynchronize());
+    op->free_slabs();
+    API_END
+}
+
+int edgpu_op_slabs_info(edgpu_op oh, int32_t* passes, int64_t* columns_per_slab, int64_t* entries) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
+    const bool on = op->slab.tab != nullptr;
+    if (passes) *passes = on ? op->slab.n_pass : 0;
+    if (columns_per_slab) *columns_per_slab = on ? op->slab.wc : 0;
+    if (entries) *entries = on ? op->slab.n : 0;
+    API_END
+}
+
+int edgpu_op_slab_use(edgpu_op oh, int32_t precision, int32_t use, int32_t* current) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
+    check_prec(precision);
+    require(use >= -1 && use <= 1, EDGPU_ERR_ARG, "use must be -1 (query), 0 or 1");
+    require(use != 1 || (op->slab.tab && precision == EDGPU_MIXED), EDGPU_ERR_STATE,
+            "no slab table (edgpu_op_build_slabs), or not mixed precision");
+    if (use >= 0) op->slab_use[precision] = use;
+    if (current) *current = op->slab_use[precision];
+    API_END
+}
+
 int edgpu_pair_classes_of_terms(int32_t n_bits, int32_t n_terms, const uint64_t* masks, const uint64_t* rows,
                                 const uint64_t* cols, const double* amps, int32_t cap_classes, int32_t* n_classes,
                                 int32_t* info, uint64_t* comps, uint64_t* flips, double* class_amps) {
@@ -1982,12 +2347,14 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     // rows per warp tile when there is no parent-state map); where the pair-flip schedule applies
     // (and the caller allows it), that schedule with 2 or 4 targets per step (4 with a map or a
     // target table) and 1, 2 or 4 lanes per row, and its target-table flavour (one lane per row).
-    struct Cand { int pair, nt, table, rows, pf, uni; };
+    // With a slab table (mixed precision), also its multi-pass product.
+    struct Cand { int pair, nt, table, rows, pf, uni, slab = 0; };
     std::vector<Cand> cands;
     build_blob(op, precision, 0, 0);
     const bool pair_ok = op->blob[precision][0][0].tmpl.bond_ncls > 0 && op->pair_allowed;
     const bool mapped = op->space->d_map != nullptr;
     if (pair_ok) {
+        if (op->slab.tab && precision == EDGPU_MIXED) cands.push_back({1, 4, 1, -1, 0, 0, 1});
         if (op->d_tab) {
             for (int nt : {8, 4, 2})
                 for (int pf : {0, 4, 64}) cands.push_back({1, nt, 1, -1, pf, 0});
@@ -2003,7 +2370,7 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     Cand best = cands.front();
     double best_ms = 1e30;
     const int keep_pair = op->pair_use[precision], keep_nt = op->pair_nt[precision], keep_tab = op->tab_use[precision];
-    const int keep_uni = op->tab_uni[precision];
+    const int keep_uni = op->tab_uni[precision], keep_slab = op->slab_use[precision];
     if (n > 0) {
         const size_t vs = precision == EDGPU_FP64 ? 16 : 8;
         void *x = nullptr, *y = nullptr;
@@ -2020,6 +2387,7 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
                 op->tab_use[precision] = c.table;
                 op->tab_pf[precision] = c.pf;
                 op->tab_uni[precision] = c.uni;
+                op->slab_use[precision] = c.slab;
                 launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, op->hs.stream(), nullptr, c.rows);
                 // one timed launch, then two back-to-back bursts of enough launches to cover about 2 ms
                 // (1 to 50 per burst), as a solver issues them; the faster burst's time per launch
@@ -2051,6 +2419,7 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
             op->pair_nt[precision] = keep_nt;
             op->tab_use[precision] = keep_tab;
             op->tab_uni[precision] = keep_uni;
+            op->slab_use[precision] = keep_slab;
             cudaFree(x);
             cudaFree(y);
             cudaEventDestroy(e0);
@@ -2067,6 +2436,7 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     op->tab_use[precision] = best.table ? 1 : (op->d_tab ? 0 : 1);
     op->tab_pf[precision] = best.pf;
     op->tab_uni[precision] = best.uni;
+    op->slab_use[precision] = best.slab;
     op->tuned_rows[precision] = best.rows;
     if (rows_per_tile_out) *rows_per_tile_out = best.rows;
     if (best_ms_out) *best_ms_out = best_ms;
@@ -2501,7 +2871,7 @@ int edgpu_op_grad_kernel(edgpu_op oh, int32_t precision, int32_t* kind) {
     require(kind, EDGPU_ERR_ARG, "null output");
     build_blob(op, precision, 0, 1);
     const Blob& B = op->blob[precision][0][1];
-    const size_t gsmem = align16(B.smem_bond) + (size_t)op->n_coupl * HX_THREADS * 8;
+    const size_t gsmem = align16(B.smem_bond) + pair_grad_acc_bytes(op, precision);
     if (B.tmpl.o_bunit >= 0 && op->pair_allowed && (op->d_tab || op->space->d_map) && gsmem <= 200 * 1024)
         *kind = op->d_tab ? 2 : 1;
     else
@@ -2781,6 +3151,62 @@ void batch_launch(edgpu_batch_s* b, int prec, const HxParams& p, int blocks, cud
     else hx_multi_launch_w64(gk, prec, p, blocks, b->fused[prec].smem, st);
 }
 
+// One sector of a batch launched on its own: the operator's product kernel with the batch's schedule
+// (pair flips, targets per step, target table, prefetch, lanes per row) in place of the operator's
+// own for this launch.  The caller holds the operators' locks.
+void batch_sector_launch(edgpu_batch_s* b, int prec, int i, const void* x, void* y, cudaStream_t st) {
+    edgpu_op_s* op = b->ops[i];
+    if (op->space->dim == 0) return;
+    const int keep[5] = {op->pair_use[prec], op->pair_nt[prec], op->tab_use[prec], op->tab_pf[prec], op->tab_uni[prec]};
+    op->pair_use[prec] = b->pair_use[prec];
+    op->pair_nt[prec] = b->pair_nt[prec];
+    op->tab_use[prec] = b->tab_use[prec];
+    op->tab_pf[prec] = b->tab_pf[prec];
+    op->tab_uni[prec] = 0;
+    auto restore = [&] {
+        op->pair_use[prec] = keep[0];
+        op->pair_nt[prec] = keep[1];
+        op->tab_use[prec] = keep[2];
+        op->tab_pf[prec] = keep[3];
+        op->tab_uni[prec] = keep[4];
+    };
+    try {
+        launch_product(op, prec, 0, 0, x, y, 0, nullptr, nullptr, st, nullptr, -(b->lpr[prec] ? b->lpr[prec] : 1));
+    } catch (...) {
+        restore();
+        throw;
+    }
+    restore();
+}
+
+// The batched product y_k = H_k x_k in the batch's launch mode (edgpu_batch_s::seq), enqueued on st.
+// Per-sector launches on k > 1 streams fork from st and join back into it, so that st orders them
+// after the work before the call and the work after it after all of them (also under stream capture).
+void batch_run(edgpu_batch_s* b, int prec, const void* const* xs, void* const* ys, cudaStream_t st) {
+    const int k = b->seq[prec];
+    const int n = (int)b->ops.size();
+    if (k <= 0) {
+        int blocks = 0;
+        const HxParams p = batch_params(b, prec, xs, ys, &blocks);
+        batch_launch(b, prec, p, blocks, st);
+        return;
+    }
+    for (int i = 0; i < n; ++i)
+        require(b->ops[i]->space->dim == 0 || (xs[i] && ys[i]), EDGPU_ERR_ARG, "null vector in batch");
+    if (k == 1) {
+        for (int i = 0; i < n; ++i) batch_sector_launch(b, prec, i, xs[i], ys[i], st);
+        return;
+    }
+    b->ensure_lanes(k);
+    EDGPU_CUDA(cudaEventRecord(b->fork_ev, st));
+    for (int j = 0; j < k; ++j) EDGPU_CUDA(cudaStreamWaitEvent(b->lane_st[j], b->fork_ev, 0));
+    for (int i = 0; i < n; ++i) batch_sector_launch(b, prec, i, xs[i], ys[i], b->lane_st[i % k]);
+    for (int j = 0; j < k; ++j) {
+        EDGPU_CUDA(cudaEventRecord(b->join_ev[j], b->lane_st[j]));
+        EDGPU_CUDA(cudaStreamWaitEvent(st, b->join_ev[j], 0));
+    }
+}
+
 }  // namespace
 
 int edgpu_batch_create(int32_t n_ops, const edgpu_op* ops, edgpu_batch* out) {
@@ -2817,7 +3243,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
     const size_t vs = precision == EDGPU_FP64 ? 16 : 8;
     int64_t tot = 0;
     for (auto* o : b->ops) tot += o->space->dim;
-    int best = 1, best_pair = 1, best_nt = 2, best_tab = 1, best_pf = 0;
+    int best = 1, best_pair = 1, best_nt = 2, best_tab = 1, best_pf = 0, best_seq = 0;
     double best_ms = 1e30;
     if (tot > 0) {
         void *x = nullptr, *y = nullptr;
@@ -2847,55 +3273,65 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
             for (auto* o : b->ops) mapped = mapped && (o->space->d_map != nullptr || o->space->dim == 0);
             bool tabled = pair_ok;
             for (auto* o : b->ops) tabled = tabled && (o->d_tab != nullptr || o->space->dim == 0);
-            // cand 5/4/3: target tables with 8/4/2 targets per step; 2/1: pair flips with 4/2; 0: term scan
+            // cand 5/4/3: target tables with 8/4/2 targets per step; 2/1: pair flips with 4/2; 0: term scan.
+            // l: target tables: one lane per row, x prefetched 0 (l = 1), 4 (l = 5) or 64 (l = 6) steps
+            // ahead; the other schedules: l lanes per row.  sq: the launch mode (edgpu_batch_s::seq),
+            // per-sector launches only with one lane per row and no prefetch.
+            struct Cand { int cand, l, sq; };
+            std::vector<Cand> cands;
             for (int cand = tabled ? 5 : (pair_ok ? (mapped ? 2 : 1) : 0); cand >= 0; --cand)
                 for (int l : {1, 2, 4, 5, 6}) {
-                    // target tables: one lane per row, x prefetched 0 (l = 1), 4 (l = 5) or 64 (l = 6)
-                    // steps ahead; the other schedules: l lanes per row
                     if (cand >= 3 && !(l == 1 || l >= 5)) continue;
                     if (cand < 3 && l >= 5) continue;
-                    const int pf = l == 5 ? 4 : (l == 6 ? 64 : 0);
-                    b->tab_pf[precision] = pf;
-                    if (l >= 5) l = 1;
-                    b->lpr[precision] = l;
-                    b->pair_use[precision] = cand > 0 ? 1 : 0;
-                    b->pair_nt[precision] = cand == 5 ? 8 : (cand == 2 || cand == 4) ? 4 : 2;
-                    b->tab_use[precision] = cand >= 3 ? 1 : 0;
-                    int blocks = 0;
-                    const HxParams p = batch_params(b, precision, xs.data(), ys.data(), &blocks);
-                    batch_launch(b, precision, p, blocks, bh->hs.stream());
-                    float t_min = 1e30f;
+                    for (int sq = 0; sq <= 3; ++sq)
+                        if (sq == 0 || (l == 1 && cand > 0)) cands.push_back({cand, l, sq});
+                }
+            for (const Cand& cd : cands) {
+                const int cand = cd.cand;
+                int l = cd.l;
+                const int pf = l == 5 ? 4 : (l == 6 ? 64 : 0);
+                b->tab_pf[precision] = pf;
+                if (l >= 5) l = 1;
+                b->lpr[precision] = l;
+                b->pair_use[precision] = cand > 0 ? 1 : 0;
+                b->pair_nt[precision] = cand == 5 ? 8 : (cand == 2 || cand == 4) ? 4 : 2;
+                b->tab_use[precision] = cand >= 3 ? 1 : 0;
+                b->seq[precision] = cd.sq;
+                auto run = [&] { batch_run(b, precision, xs.data(), ys.data(), bh->hs.stream()); };
+                run();
+                float t_min = 1e30f;
+                EDGPU_CUDA(cudaEventRecord(e0, bh->hs.stream()));
+                run();
+                EDGPU_CUDA(cudaEventRecord(e1, bh->hs.stream()));
+                EDGPU_CUDA(cudaEventSynchronize(e1));
+                float ms1 = 0.f;
+                cudaEventElapsedTime(&ms1, e0, e1);
+                const int reps = std::max(1, std::min(50, (int)(2.0f / std::max(ms1, 1e-3f))));
+                for (int burst = 0; burst < 2; ++burst) {
                     EDGPU_CUDA(cudaEventRecord(e0, bh->hs.stream()));
-                    batch_launch(b, precision, p, blocks, bh->hs.stream());
+                    for (int k = 0; k < reps; ++k) run();
                     EDGPU_CUDA(cudaEventRecord(e1, bh->hs.stream()));
                     EDGPU_CUDA(cudaEventSynchronize(e1));
-                    float ms1 = 0.f;
-                    cudaEventElapsedTime(&ms1, e0, e1);
-                    const int reps = std::max(1, std::min(50, (int)(2.0f / std::max(ms1, 1e-3f))));
-                    for (int burst = 0; burst < 2; ++burst) {
-                        EDGPU_CUDA(cudaEventRecord(e0, bh->hs.stream()));
-                        for (int k = 0; k < reps; ++k) batch_launch(b, precision, p, blocks, bh->hs.stream());
-                        EDGPU_CUDA(cudaEventRecord(e1, bh->hs.stream()));
-                        EDGPU_CUDA(cudaEventSynchronize(e1));
-                        float ms = 0.f;
-                        cudaEventElapsedTime(&ms, e0, e1);
-                        t_min = std::min(t_min, ms / reps);
-                    }
-                    const float sum = t_min;
-                    if (sum < best_ms) {
-                        best_ms = sum;
-                        best = l;
-                        best_pf = pf;
-                        best_pair = cand > 0 ? 1 : 0;
-                        best_nt = cand == 5 ? 8 : (cand == 2 || cand == 4) ? 4 : 2;
-                        best_tab = cand >= 3 ? 1 : 0;
-                    }
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    t_min = std::min(t_min, ms / reps);
                 }
+                if (t_min < best_ms) {
+                    best_ms = t_min;
+                    best = l;
+                    best_pf = pf;
+                    best_pair = cand > 0 ? 1 : 0;
+                    best_nt = cand == 5 ? 8 : (cand == 2 || cand == 4) ? 4 : 2;
+                    best_tab = cand >= 3 ? 1 : 0;
+                    best_seq = cd.sq;
+                }
+            }
         } catch (...) {
             b->lpr[precision] = keep;
             b->pair_use[precision] = 1;
             b->pair_nt[precision] = 2;
             b->tab_use[precision] = 1;
+            b->seq[precision] = 0;
             cudaStreamSynchronize(bh->hs.stream());
             cudaFree(x);
             cudaFree(y);
@@ -2919,6 +3355,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
     b->pair_nt[precision] = best_nt;
     b->tab_use[precision] = best_tab;
     b->tab_pf[precision] = best_pf;
+    b->seq[precision] = best_seq;
     if (lanes_per_row_out) *lanes_per_row_out = best;
     if (best_ms_out) *best_ms_out = best_ms;
     API_END
@@ -2952,6 +3389,26 @@ int edgpu_batch_get_schedule(edgpu_batch bh, int32_t precision, int32_t* lanes_p
     API_END
 }
 
+int edgpu_batch_set_launch(edgpu_batch bh, int32_t precision, int32_t streams) {
+    API_BEGIN
+    require(bh, EDGPU_ERR_ARG, "null batch");
+    std::lock_guard<std::mutex> blk_(bh->hs.mu);
+    BatchLocks locks_(bh->ops);
+    check_prec(precision);
+    require(streams >= 0 && streams <= 3, EDGPU_ERR_ARG, "streams must be 0 (one persistent launch) or 1 to 3");
+    bh->seq[precision] = streams;
+    API_END
+}
+
+int edgpu_batch_get_launch(edgpu_batch bh, int32_t precision, int32_t* streams) {
+    API_BEGIN
+    require(bh && streams, EDGPU_ERR_ARG, "null argument");
+    std::lock_guard<std::mutex> blk_(bh->hs.mu);
+    check_prec(precision);
+    *streams = bh->seq[precision];
+    API_END
+}
+
 int edgpu_batch_mul_device(edgpu_batch bh, int32_t precision, const void* const* xs, void* const* ys, int32_t use_graph,
                            void* stream) {
     API_BEGIN
@@ -2963,17 +3420,26 @@ int edgpu_batch_mul_device(edgpu_batch bh, int32_t precision, const void* const*
     cudaStream_t st = pick_stream(stream);
     const int n = (int)b->ops.size();
     batch_prepare(b, precision);
-    int blocks = 0;
-    const HxParams p = batch_params(b, precision, xs, ys, &blocks);
     if (!use_graph) {
-        batch_launch(b, precision, p, blocks, st);
+        batch_run(b, precision, xs, ys, st);
         return EDGPU_OK;
     }
+    const int sq = b->seq[precision];
     std::vector<const void*> key;
-    key.push_back((const void*)(intptr_t)p.lpr);
+    key.push_back((const void*)(intptr_t)b->lpr[precision]);
     key.push_back((const void*)(intptr_t)(b->pair_use[precision] * 8 + b->pair_nt[precision] +
-                                          (p.tab ? 16 : 0) + 32 * p.bond_pf));   // the kernel
-    key.push_back(p.blob);   // the image (vectors, sector maps) the launch reads
+                                          b->tab_use[precision] * 16 + 32 * b->tab_pf[precision]));   // the kernel
+    key.push_back((const void*)(intptr_t)sq);   // the launch mode
+    if (sq == 0) {
+        int blocks = 0;
+        key.push_back(batch_params(b, precision, xs, ys, &blocks).blob);   // the image (vectors, sector maps)
+    } else {
+        for (int i = 0; i < n; ++i) {
+            // per-sector launches read the operators' own tables
+            key.push_back(b->ops[i]->d_tab);
+            key.push_back(b->ops[i]->space->d_map);
+        }
+    }
     for (int i = 0; i < n; ++i) {
         key.push_back(xs[i]);
         key.push_back(ys[i]);
@@ -2992,7 +3458,7 @@ int edgpu_batch_mul_device(edgpu_batch bh, int32_t precision, const void* const*
             throw Error(EDGPU_ERR_CUDA, std::string("begin capture: ") + cudaGetErrorString(e));
         }
         try {
-            batch_launch(b, precision, p, blocks, cap);
+            batch_run(b, precision, xs, ys, cap);
         } catch (...) {
             cudaStreamEndCapture(cap, &graph);
             if (graph) cudaGraphDestroy(graph);

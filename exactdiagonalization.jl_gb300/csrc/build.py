@@ -15,7 +15,7 @@ PKG = os.path.dirname(HERE)
 ROOT = os.path.dirname(PKG)
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "edgpu", "libedgpu.so")
-SOURCES = ["api.cpp", "enumerate.cu", "hx32.cu", "hx64.cu", "hxbond.cu", "hxtable.cu", "linalg.cu", "noalloc.cu"]
+SOURCES = ["api.cpp", "enumerate.cu", "hx32.cu", "hx64.cu", "hxbond.cu", "hxtable.cu", "linalg.cu", "noalloc.cu", "hxslab.cu"]
 HEADERS = ["edgpu_internal.h", "edgpu_device.cuh", "hx_kernel.cuh", "hx_rows.cuh", "hx_bond.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]

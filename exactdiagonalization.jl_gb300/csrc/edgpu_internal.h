@@ -227,6 +227,10 @@ struct HxParams {
     // gradient mode of the pair-flip kernel (offsets into its shared-memory image, -1 when absent): the
     // slots' unit amplitudes and coupling ids, and the diagonal term records
     int o_bunit, o_bcid, o_pdm, o_pdr, o_pdu, o_pdc;
+    int bunit_real;                           // every unit pair amplitude is real
+    // the diagonal records by site pair (n_pdb entries; -1: a record has a mask of more than two bits):
+    // i | j << 8 | coupling id << 16, and per entry the unit amplitudes of the pair's four bit patterns
+    int o_pdb, o_pdv, n_pdb;
     // adjoint target table (column-sorted; built by the ADJ passes of bond_tile): per column the
     // count, the offset of its run, a fill cursor, and the entries (row << 32 | slot << 19 |
     // row's orbit-size index << 14 | group element)
@@ -333,6 +337,54 @@ void hx_adj_pass(bool w32, int pass, const HxParams& p, long long n_tiles, size_
 void hx_adj_sort(const long long* off, unsigned long long* tab, long long n, cudaStream_t st);
 // y = H^dagger x through the adjoint target table: one lane per column, its run in order; p.gy = x.
 void hx_adj_launch(bool w32, int prec, const HxParams& p, size_t smem, cudaStream_t st);
+
+// ---- column-slab table of the pair-flip schedule (hxslab.cu) -------------------------------------
+// The target table's entries regrouped by column slab: slab q holds the columns [q wc, (q + 1) wc).
+// Pass q of the product gathers only from slab q (sized to stay in L2 while the pass runs) and adds
+// its share to y.  Per pass: a count byte per row, a 32-bit offset per warp tile of 32 rows
+// (relative to the pass's first entry), and the entries tile by tile, row by row, each row's
+// entries in the target table's order; an entry is (column - q wc) | id << colbits, where id
+// indexes the coefficient table: id = ((amplitude id x den + character index) x nd + orbit-size
+// index of the row) x nd + orbit-size index of the column.
+struct SlabBuild {
+    long long wc;                   // columns per slab
+    int n_pass;
+    long long n_tiles;
+    unsigned char* counts;          // [n_pass][n_rows] (written by the count pass)
+    unsigned* tile_sum;             // [n_pass][n_tiles] (written by the count pass)
+    const unsigned* off;            // [n_pass][n_tiles] tile offsets relative to the pass (fill pass)
+    const long long* base;          // [n_pass] first entry of each pass (fill pass)
+    unsigned* tab;                  // the entries (fill pass)
+    const unsigned short* amp_id;   // [n_slots] amplitude id of every pair-flip slot (fill pass)
+    int n_slots;
+    int colbits;
+    int o_ctr;                      // shared-memory offset of the per-thread pass counters / cursors
+};
+struct SlabRun {
+    const unsigned char* cnt;       // this pass's count bytes [n_rows]
+    const unsigned* off;            // this pass's tile offsets [n_tiles]
+    const unsigned* tab;            // this pass's entries
+    const void* xs;                 // x from the slab's first column
+    const void* x;                  // x (first pass: the diagonal's product)
+    void* y;
+    const void* diag;
+    const void* lut;                // coefficients by id: V, or R when lut_real
+    void* y_c128;                   // mixed precision, last pass: complex128 output instead of y
+    long long n_rows, n_tiles;
+    unsigned colmask;
+    int colbits, n_lut, lut_real;
+    int first, last, accumulate, acc_c128;
+};
+// Count pass (1) or fill pass (2) of the slab table from the target table.  p: the table-flavour
+// pair-flip template (tab, tile_off set; lpr = 1); smem: its image plus s.o_ctr's counters.
+void hx_slab_build(bool w32, int prec, int pass, const HxParams& p, const SlabBuild& s, size_t smem,
+                   cudaStream_t st);
+// Per pass: exclusive scan of the tile sums [n_pass][n_tiles] into 32-bit offsets relative to the
+// pass; totals[q] = entries of pass q (host, after a synchronisation).
+void hx_slab_scan(const unsigned* tile_sum, unsigned* off, int n_pass, long long n_tiles,
+                  std::vector<unsigned long long>& totals, cudaStream_t st);
+// One pass of the slab product.
+void hx_slab_launch(int prec, const SlabRun& r, cudaStream_t st);
 
 // ---- the coupling-gradient launch for callers that cannot allocate (noalloc.cu) -----------------
 // The fused product and coupling gradient exactly as edgpu_coupling_grad_device launches it (same

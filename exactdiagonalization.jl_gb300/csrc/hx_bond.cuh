@@ -147,15 +147,17 @@ __device__ __forceinline__ int bond_row_count(W b, const BondTables<W, PREC>& bt
 //             order, hence the results, are the same as without UNI;
 //   GRAD      the coupling gradient fused with the product: every target also adds
 //             Re(conj(gy_r) u x_c), with u its unit-coupling element, to the accumulator of its slot's
-//             coupling (sgrad[coupling][thread], FP64, one slot per thread: no atomics, so the sums
-//             are reproducible), and every diagonal term matching the row adds Re(conj(gy_r) u_t x_r).
+//             coupling (sgrad[coupling][thread], one slot per thread: no atomics, so the sums are
+//             reproducible), and every diagonal term matching the row adds Re(u_t z_r) with
+//             z_r = conj(gy_r) x_r.  The accumulators have the product's arithmetic type R (FP32 in
+//             mixed precision: a thread adds a few dozen terms before the block sums them in FP64).
 //   ADJ       (1 or 2, with GK_TABLE) the passes that build the adjoint target table: 1 counts every
 //             target on its column, 2 writes row, slot, the row's orbit-size index and the group
 //             element into the column's run.
 template <typename W, int GK, int PREC, int NT, bool FILL = false, bool UNI = false, bool GRAD = false, int ADJ = 0>
 __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W, PREC>& tb,
                                           const BondTables<W, PREC>& bt, const RowsSector<PREC>& sc, long long tile,
-                                          int lane, double* sgrad = nullptr) {
+                                          int lane, typename Cx<PREC>::R* sgrad = nullptr) {
     typedef typename Cx<PREC>::V V;
     typedef typename Cx<PREC>::R R;
     const W* __restrict__ keys = (const W*)sc.keys;
@@ -179,13 +181,28 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
                 const unsigned char* smb = (const unsigned char*)bt.comp - p.o_bcomp;
                 const W* dm = (const W*)(smb + p.o_pdm);
                 const W* dr = (const W*)(smb + p.o_pdr);
-                const double2* du = (const double2*)(smb + p.o_pdu);
+                const V* du = (const V*)(smb + p.o_pdu);
                 const int* dc = (const int*)(smb + p.o_pdc);
-                for (int t = 0; t < p.T_d; ++t)
-                    if ((b & dm[t]) == dr[t]) {
-                        const V cu = cmul(from_d2<V>(du[t]), xr);
-                        sgrad[dc[t] * HX_THREADS + threadIdx.x] += (double)(gv.x * cu.x + gv.y * cu.y);
+                // z = conj(gy_r) x_r; a term's share is Re(u z) = u.x z.x - u.y z.y
+                const R zr = gv.x * xr.x + gv.y * xr.y, zi = gv.x * xr.y - gv.y * xr.x;
+                if (p.n_pdb >= 0) {
+                    // one entry per (site pair, coupling): the unit amplitude of the row's two bits
+                    const int* db = (const int*)(smb + p.o_pdb);
+                    const V* dv = (const V*)(smb + p.o_pdv);
+                    for (int k = 0; k < p.n_pdb; ++k) {
+                        const int e = db[k];
+                        const int pat = (int)((b >> (e & 0xff)) & 1) | ((int)((b >> ((e >> 8) & 0xff)) & 1) << 1);
+                        const V u = dv[k * 4 + pat];
+                        R& a = sgrad[(e >> 16) * HX_THREADS + threadIdx.x];
+                        a = fma_r(u.x, zr, fma_r(-u.y, zi, a));
                     }
+                } else {
+                    for (int t = 0; t < p.T_d; ++t)
+                        if ((b & dm[t]) == dr[t]) {
+                            R& a = sgrad[dc[t] * HX_THREADS + threadIdx.x];
+                            a = fma_r(du[t].x, zr, fma_r(-du[t].y, zi, a));
+                        }
+                }
             }
         }
     }
@@ -320,14 +337,22 @@ __device__ __forceinline__ void bond_tile(const HxParams& p, const RowsTables<W,
         for (int h = 0; h < NT; ++h) {
             if (GRAD && c[h] >= 0) {
                 const unsigned char* smb = (const unsigned char*)bt.comp - p.o_bcomp;
-                V u = ((const V*)(smb + p.o_bunit))[ti[h]];
-                if (GK != GK_TRIVIAL) {
-                    if (sc.want_arg) u = cmul(u, sc.ph[sc.num[g[h]]]);
-                    u = cscale(u, rrow[sx[h]]);
-                }
-                const V t = cmul(u, xv[h]);
+                const V u0 = ((const V*)(smb + p.o_bunit))[ti[h]];
                 const int cid = ((const int*)(smb + p.o_bcid))[ti[h]];
-                sgrad[cid * HX_THREADS + threadIdx.x] += (double)(gv.x * t.x + gv.y * t.y);
+                R& a = sgrad[cid * HX_THREADS + threadIdx.x];
+                if (p.bunit_real && !sc.want_arg) {
+                    // real unit amplitude, trivial characters: u x_c is a real multiple of x_c
+                    const R f = GK == GK_TRIVIAL ? u0.x : u0.x * rrow[sx[h]];
+                    a = fma_r(f, gv.x * xv[h].x + gv.y * xv[h].y, a);
+                } else {
+                    V u = u0;
+                    if (GK != GK_TRIVIAL) {
+                        if (sc.want_arg) u = cmul(u, sc.ph[sc.num[g[h]]]);
+                        u = cscale(u, rrow[sx[h]]);
+                    }
+                    const V t = cmul(u, xv[h]);
+                    a += gv.x * t.x + gv.y * t.y;
+                }
             }
             if (c[h] >= 0) {
                 const V a = bt.amp[ti[h]];
@@ -480,8 +505,9 @@ __global__ void __launch_bounds__(HX_THREADS) hx_bond_grad_kernel(const HxParams
         int4* dst = (int4*)sm;
         for (int i = threadIdx.x; i < p.blob_words16; i += blockDim.x) dst[i] = src[i];
     }
-    double* sgrad = (double*)(sm + p.o_grad);
-    for (int i = threadIdx.x; i < p.n_coupl * HX_THREADS; i += blockDim.x) sgrad[i] = 0.0;
+    typedef typename Cx<PREC>::R R;
+    R* sgrad = (R*)(sm + p.o_grad);
+    for (int i = threadIdx.x; i < p.n_coupl * HX_THREADS; i += blockDim.x) sgrad[i] = (R)0;
     __syncthreads();
     const RowsTables<W, PREC> tb(p, sm);
     const BondTables<W, PREC> bt(p, sm);
@@ -509,10 +535,14 @@ __global__ void __launch_bounds__(HX_THREADS) hx_bond_grad_kernel(const HxParams
     for (long long tile = (long long)blockIdx.x * wpb + warp; tile < n_tiles; tile += (long long)gridDim.x * wpb)
         bond_tile<W, GK, PREC, NT, false, false, true>(p, tb, bt, sc, tile, lane, sgrad);
     __syncthreads();
-    for (int i = threadIdx.x; i < p.n_coupl; i += blockDim.x) {
+    // block sums in FP64, one warp per coupling: lane l adds the accumulators of threads l, l + 32, ...
+    // in turn, then a butterfly over the lanes (a fixed order)
+    for (int i = warp; i < p.n_coupl; i += wpb) {
         double sum = 0.0;
-        for (int t = 0; t < HX_THREADS; ++t) sum += sgrad[i * HX_THREADS + t];
-        p.grad_partial[(size_t)blockIdx.x * p.n_coupl + i] = sum;
+        for (int t = lane; t < HX_THREADS; t += 32) sum += (double)sgrad[i * HX_THREADS + t];
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, d);
+        if (lane == 0) p.grad_partial[(size_t)blockIdx.x * p.n_coupl + i] = sum;
     }
 }
 

@@ -1,0 +1,346 @@
+// Column-slab table of the pair-flip schedule and its multi-pass product.
+//
+// On a large sector the target-table product (hx_bond.cuh, GK_TABLE) gathers x at random: with x
+// many times the size of L2, nearly every gather is a DRAM sector of 32 bytes for 8 bytes of x.  The
+// slab table regroups the same entries by the column slab their target lies in.  Pass q of the
+// product reads only the entries whose columns lie in slab q, so while it runs the gathers hit a
+// window of x small enough to stay in L2; its share is added to y.  y is then read and written once
+// per pass, which is streamed traffic, instead of one random DRAM sector per target.
+//
+// The entries are those of the target table (itself the (row, target) form of the reference's
+// basis_mapping_index, symmetry_reduce_generic.jl:33-35), with the coefficient of each element
+// (amplitude x character x orbit-size ratio, reduced_operator_representation.jl:57-85) replaced by an
+// index into a small table of the distinct coefficients.  Within a pass every row adds its entries
+// in the target table's order and the passes are added in order, so results are reproducible run to
+// run; they differ from the one-pass product by the order of the additions.
+#include "hx_bond.cuh"
+
+namespace edgpu {
+
+namespace {
+
+// Calls f(slot, c, sx, g) for every target of the row state b in the target table's order (class,
+// then start bit), reading the entries from position tpos on; slot = (class n + i) << 2 | v.
+template <typename W, int PREC, typename F>
+__device__ __forceinline__ void slab_walk(const HxParams& p, const BondTables<W, PREC>& bt,
+                                          const RowsSector<PREC>& sc, W b, long long tpos, F&& f) {
+    const int n = p.nbits;
+    const W full = (W)p.full;
+    for (int cls = 0; cls < p.bond_ncls; ++cls) {
+        W m = bond_class_mask<W, PREC>(b, bt, cls, n, full);
+        const bool cpar = (bt.ninfo[cls] >> 8) != 0;
+        while (m) {
+            const int i = lowest_bit<W>(m);
+            m &= m - 1;
+            const int ti = cls * n + i;
+            int v = (int)(b >> i) & 1;
+            if (cpar) v |= (__popcll((unsigned long long)(b & bt.flip[ti])) != 1) << 1;
+            long long c;
+            int sx, g;
+            table_entry<PREC>(sc, tpos, true, p.sb, c, sx, g);
+            ++tpos;
+            f((ti << 2) | v, c, sx, g);
+        }
+    }
+}
+
+// Pass 1 counts every row's targets per slab (counts[q][row], tile sums); pass 2 writes every entry
+// at its place (a per-thread cursor per slab, started at the tile's offset plus the counts of the
+// tile's earlier rows).
+template <typename W, int PREC, int PASS>
+__global__ void __launch_bounds__(HX_THREADS) hx_slab_build_kernel(const HxParams p, const SlabBuild s) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    {
+        const int4* src = (const int4*)p.blob;
+        int4* dst = (int4*)sm;
+        for (int i = threadIdx.x; i < p.blob_words16; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const BondTables<W, PREC> bt(p, sm);
+    RowsSector<PREC> sc{};
+    sc.tab = p.tab;
+    sc.tile_off = p.tile_off;
+    sc.tab_wide = p.tab_wide;
+    sc.tab_cb = p.tab_cb;
+    const int* num = (const int*)(sm + p.o_num);
+    const W* __restrict__ keys = (const W*)p.keys;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    const W smask = (W)((((W)1) << p.sb) - 1);
+    const unsigned wc = (unsigned)s.wc;
+    const int P = s.n_pass;
+    for (long long tile = (long long)blockIdx.x * wpb + warp; tile < s.n_tiles; tile += (long long)gridDim.x * wpb) {
+        const long long row = tile * 32 + lane;
+        const bool act = row < p.n_rows;
+        const W kr = act ? keys[row] : (W)0;
+        const W b = kr >> p.sb;
+        const int ri = (int)(kr & smask);
+        const int cnt = bond_row_count<W, PREC>(b, bt, act ? p.bond_ncls : 0, p.nbits, (W)p.full);
+        int incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += u;
+        }
+        const long long tpos = p.tile_off[tile] + (incl - cnt);
+        if constexpr (PASS == 1) {
+            unsigned char* ctr = sm + s.o_ctr;
+            for (int q = 0; q < P; ++q) ctr[q * HX_THREADS + threadIdx.x] = 0;
+            if (act)
+                slab_walk<W, PREC>(p, bt, sc, b, tpos, [&](int, long long c, int, int) {
+                    if (c >= 0) ++ctr[((unsigned)c / wc) * HX_THREADS + threadIdx.x];
+                });
+            for (int q = 0; q < P; ++q) {
+                const unsigned v = ctr[q * HX_THREADS + threadIdx.x];
+                if (act) s.counts[(size_t)q * p.n_rows + row] = (unsigned char)v;
+                unsigned t = v;
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) t += __shfl_xor_sync(0xffffffffu, t, d);
+                if (lane == 0) s.tile_sum[(size_t)q * s.n_tiles + tile] = t;
+            }
+        } else {
+            unsigned* cur = (unsigned*)(sm + s.o_ctr);
+            for (int q = 0; q < P; ++q) {
+                const unsigned v = act ? s.counts[(size_t)q * p.n_rows + row] : 0u;
+                unsigned inc = v;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const unsigned u = __shfl_up_sync(0xffffffffu, inc, d);
+                    if (lane >= d) inc += u;
+                }
+                cur[q * HX_THREADS + threadIdx.x] = s.off[(size_t)q * s.n_tiles + tile] + (inc - v);
+            }
+            if (act)
+                slab_walk<W, PREC>(p, bt, sc, b, tpos, [&](int slot, long long c, int sx, int g) {
+                    if (c < 0) return;
+                    const unsigned q = (unsigned)c / wc;
+                    const unsigned rel = cur[q * HX_THREADS + threadIdx.x]++;
+                    const unsigned ph = p.want_arg ? (unsigned)num[g] : 0u;
+                    const unsigned id = (((unsigned)__ldg(s.amp_id + slot) * (unsigned)p.den + ph) * (unsigned)p.nd +
+                                         (unsigned)ri) * (unsigned)p.nd + (unsigned)sx;
+                    s.tab[s.base[q] + rel] = ((unsigned)c - q * wc) | (id << s.colbits);
+                });
+        }
+    }
+}
+
+// Exclusive scan of the tile sums of every pass, in chunks of SLAB_CHUNK per block (blockIdx.y =
+// pass): chunk totals, then a scan of the chunk totals per pass, then the offsets.
+constexpr int SLAB_CHUNK = HX_THREADS * 16;
+
+__global__ void k_slab_scan_part(const unsigned* ts, long long n_tiles, unsigned long long* part, int nb) {
+    __shared__ long long tmp[32];
+    const int q = blockIdx.y;
+    const unsigned* a = ts + (size_t)q * n_tiles;
+    const long long beg = (long long)blockIdx.x * SLAB_CHUNK + (long long)threadIdx.x * 16;
+    long long s = 0;
+    for (long long i = beg; i < min(n_tiles, beg + 16); ++i) s += a[i];
+    long long tot = 0;
+    block_exclusive_scan(s, tmp, &tot);
+    if (threadIdx.x == 0) part[(size_t)q * nb + blockIdx.x] = (unsigned long long)tot;
+}
+
+__global__ void k_slab_scan_mid(unsigned long long* part, int nb, unsigned long long* totals) {
+    __shared__ long long tmp[32];
+    unsigned long long* a = part + (size_t)blockIdx.x * nb;
+    long long carry = 0;
+    for (int b0 = 0; b0 < nb; b0 += blockDim.x) {
+        const int i = b0 + threadIdx.x;
+        const long long v = i < nb ? (long long)a[i] : 0;
+        long long tot = 0;
+        const long long ex = block_exclusive_scan(v, tmp, &tot);
+        if (i < nb) a[i] = (unsigned long long)(carry + ex);
+        carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) totals[blockIdx.x] = (unsigned long long)carry;
+}
+
+__global__ void k_slab_scan_out(const unsigned* ts, long long n_tiles, const unsigned long long* part, int nb,
+                                unsigned* off) {
+    __shared__ long long tmp[32];
+    const int q = blockIdx.y;
+    const unsigned* a = ts + (size_t)q * n_tiles;
+    unsigned* o = off + (size_t)q * n_tiles;
+    const long long beg = (long long)blockIdx.x * SLAB_CHUNK + (long long)threadIdx.x * 16;
+    const long long end = min(n_tiles, beg + 16);
+    long long s = 0;
+    for (long long i = beg; i < end; ++i) s += a[i];
+    long long ex = block_exclusive_scan(s, tmp, nullptr) + (long long)part[(size_t)q * nb + blockIdx.x];
+    for (long long i = beg; i < end; ++i) {
+        o[i] = (unsigned)ex;
+        ex += a[i];
+    }
+}
+
+// One pass of the product: a warp per tile of 32 rows, one lane per row; the lane adds its row's
+// entries of this pass (NT per step, loads then gathers), then adds the sum to y (the first pass
+// writes y = diag x + sum; the last pass may write complex128 instead).
+template <bool REAL, int NT>
+__global__ void __launch_bounds__(HX_THREADS) hx_slab_kernel(const SlabRun r) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    pdl_launch_dependents();
+    if (REAL) {
+        const float* src = (const float*)r.lut;
+        for (int i = threadIdx.x; i < r.n_lut; i += blockDim.x) ((float*)sm)[i] = src[i];
+    } else {
+        const float2* src = (const float2*)r.lut;
+        for (int i = threadIdx.x; i < r.n_lut; i += blockDim.x) ((float2*)sm)[i] = src[i];
+    }
+    __syncthreads();
+    pdl_wait();
+    const float* lr = (const float*)sm;
+    const float2* lv = (const float2*)sm;
+    const float2* __restrict__ xs = (const float2*)r.xs;
+    const unsigned* __restrict__ tab = r.tab;
+    float2* y = (float2*)r.y;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    const bool to_c128 = r.last && r.y_c128 != nullptr;
+    for (long long tile = (long long)blockIdx.x * wpb + warp; tile < r.n_tiles; tile += (long long)gridDim.x * wpb) {
+        const long long row = tile * 32 + lane;
+        const bool act = row < r.n_rows;
+        const int cnt = act ? (int)r.cnt[row] : 0;
+        int incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += u;
+        }
+        const long long start = (long long)r.off[tile] + (incl - cnt);
+        float2 acc = make_float2(0.f, 0.f);
+        for (int j = 0; __any_sync(0xffffffffu, j < cnt); j += NT) {
+            unsigned e[NT];
+#pragma unroll
+            for (int h = 0; h < NT; ++h) e[h] = (j + h < cnt) ? __ldg(tab + start + j + h) : 0u;
+            float2 xv[NT];
+#pragma unroll
+            for (int h = 0; h < NT; ++h) xv[h] = (j + h < cnt) ? xs[e[h] & r.colmask] : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int h = 0; h < NT; ++h) {
+                if (j + h >= cnt) continue;
+                const unsigned id = e[h] >> r.colbits;
+                if (REAL) {
+                    const float f = lr[id];
+                    acc.x = __fmaf_rn(f, xv[h].x, acc.x);
+                    acc.y = __fmaf_rn(f, xv[h].y, acc.y);
+                } else {
+                    acc = cadd(acc, cmul(lv[id], xv[h]));
+                }
+            }
+        }
+        if (!act) continue;
+        float2 t;
+        if (r.first) {
+            t = cadd(cmul(((const float2*)r.diag)[row], ((const float2*)r.x)[row]), acc);
+            if (r.accumulate) t = cadd(y[row], t);
+        } else {
+            if (cnt == 0 && !to_c128) continue;   // nothing to add to this row
+            t = cadd(y[row], acc);
+        }
+        if (to_c128) {
+            double2 o = make_double2((double)t.x, (double)t.y);
+            double2* yc = (double2*)r.y_c128;
+            if (r.acc_c128) {
+                const double2 old = yc[row];
+                o.x += old.x;
+                o.y += old.y;
+            }
+            yc[row] = o;
+        } else {
+            y[row] = t;
+        }
+    }
+}
+
+template <typename K>
+void slab_pdl_launch(K kern, const SlabRun& r, int blocks, size_t smem, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3(HX_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    EDGPU_CUDA(cudaLaunchKernelEx(&cfg, kern, r));
+}
+
+template <typename K>
+int slab_blocks(K kern, size_t smem, long long n_tiles) {
+    raise_smem_limit((const void*)kern, smem);
+    int n = 0;
+    EDGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, HX_THREADS, smem));
+    const long long need = (n_tiles + HX_THREADS / 32 - 1) / (HX_THREADS / 32);
+    return (int)std::max<long long>(1, std::min<long long>(need, (long long)std::max(1, n) * sm_count()));
+}
+
+template <typename W, int PREC>
+void slab_build_t(int pass, const HxParams& p, const SlabBuild& s, size_t smem, cudaStream_t st) {
+    const int blocks = (int)std::max<long long>(
+        1, std::min<long long>((s.n_tiles + HX_THREADS / 32 - 1) / (HX_THREADS / 32), (long long)sm_count() * 8));
+    if (pass == 1) {
+        auto k = hx_slab_build_kernel<W, PREC, 1>;
+        raise_smem_limit((const void*)k, smem);
+        k<<<blocks, HX_THREADS, smem, st>>>(p, s);
+    } else {
+        auto k = hx_slab_build_kernel<W, PREC, 2>;
+        raise_smem_limit((const void*)k, smem);
+        k<<<blocks, HX_THREADS, smem, st>>>(p, s);
+    }
+    EDGPU_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+void hx_slab_build(bool w32, int prec, int pass, const HxParams& p, const SlabBuild& s, size_t smem,
+                   cudaStream_t st) {
+    if (w32) {
+        if (prec == 0) slab_build_t<unsigned, 0>(pass, p, s, smem, st);
+        else slab_build_t<unsigned, 1>(pass, p, s, smem, st);
+    } else {
+        if (prec == 0) slab_build_t<unsigned long long, 0>(pass, p, s, smem, st);
+        else slab_build_t<unsigned long long, 1>(pass, p, s, smem, st);
+    }
+}
+
+void hx_slab_scan(const unsigned* tile_sum, unsigned* off, int n_pass, long long n_tiles,
+                  std::vector<unsigned long long>& totals, cudaStream_t st) {
+    totals.assign((size_t)n_pass, 0);
+    if (n_pass == 0 || n_tiles == 0) return;
+    const int nb = (int)((n_tiles + SLAB_CHUNK - 1) / SLAB_CHUNK);
+    unsigned long long* part = nullptr;
+    unsigned long long* tot = nullptr;
+    EDGPU_CUDA(cudaMalloc(&part, (size_t)nb * n_pass * sizeof(unsigned long long)));
+    cudaError_t e = cudaMalloc(&tot, (size_t)n_pass * sizeof(unsigned long long));
+    if (e != cudaSuccess) {
+        cudaFree(part);
+        throw Error(EDGPU_ERR_OOM, std::string("slab scan: ") + cudaGetErrorString(e));
+    }
+    const dim3 grid((unsigned)nb, (unsigned)n_pass);
+    k_slab_scan_part<<<grid, HX_THREADS, 0, st>>>(tile_sum, n_tiles, part, nb);
+    k_slab_scan_mid<<<n_pass, 1024, 0, st>>>(part, nb, tot);
+    k_slab_scan_out<<<grid, HX_THREADS, 0, st>>>(tile_sum, n_tiles, part, nb, off);
+    e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(totals.data(), tot, (size_t)n_pass * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(part);
+    cudaFree(tot);
+    if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("slab scan: ") + cudaGetErrorString(e));
+}
+
+void hx_slab_launch(int prec, const SlabRun& r, cudaStream_t st) {
+    if (prec != 1) throw Error(EDGPU_ERR_ARG, "the slab product is mixed precision only");
+    if (r.n_tiles == 0) return;
+    const size_t smem = (size_t)r.n_lut * (r.lut_real ? 4 : 8);
+    if (r.lut_real) {
+        auto k = hx_slab_kernel<true, 4>;
+        slab_pdl_launch(k, r, slab_blocks(k, smem, r.n_tiles), smem, st);
+    } else {
+        auto k = hx_slab_kernel<false, 4>;
+        slab_pdl_launch(k, r, slab_blocks(k, smem, r.n_tiles), smem, st);
+    }
+}
+
+}  // namespace edgpu

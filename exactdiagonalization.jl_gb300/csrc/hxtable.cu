@@ -337,6 +337,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_adj_kernel(const HxParams p) {
     const V* __restrict__ diag = (const V*)p.diag;
     const W smask = (W)((((W)1) << p.sb) - 1);
     const bool want_arg = p.want_arg != 0;
+    const bool real_fast = p.bond_real && !want_arg;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < p.n_rows; c += (long long)gridDim.x * blockDim.x) {
         const int sxc = (int)(keys[c] & smask);
         V acc = cmul(cconj(diag[c]), x[c]);
@@ -347,10 +348,18 @@ __global__ void __launch_bounds__(HX_THREADS) hx_adj_kernel(const HxParams p) {
             const int ti = (int)((e >> 19) & 0x1fffu);
             const int sxr = (int)((e >> 14) & 0x1fu);
             const int g = (int)(e & 0x3fffu);
+            const V xr = x[r];
+            if (real_fast) {
+                // real amplitude, trivial characters: the element is its own conjugate
+                const R f = bt.amp[ti].x * tb.ratio[sxr * p.nd + sxc];
+                acc.x = fma_r(f, xr.x, acc.x);
+                acc.y = fma_r(f, xr.y, acc.y);
+                continue;
+            }
             V coef = bt.amp[ti];
             if (want_arg) coef = cmul(coef, ph[num[g]]);
             coef = cscale(coef, tb.ratio[sxr * p.nd + sxc]);
-            acc = cadd(acc, cmul(cconj(coef), x[r]));
+            acc = cadd(acc, cmul(cconj(coef), xr));
         }
         if (p.accumulate) acc = cadd(acc, y[c]);
         y[c] = acc;

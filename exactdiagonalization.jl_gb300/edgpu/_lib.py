@@ -81,6 +81,10 @@ SIGNATURES = {
     "edgpu_op_build_targets": (ctypes.c_int, [vp, i64, P(i32)]),
     "edgpu_op_free_targets": (ctypes.c_int, [vp]),
     "edgpu_op_targets_info": (ctypes.c_int, [vp, P(i64), P(i32)]),
+    "edgpu_op_build_slabs": (ctypes.c_int, [vp, i64, i64, P(i32)]),
+    "edgpu_op_free_slabs": (ctypes.c_int, [vp]),
+    "edgpu_op_slabs_info": (ctypes.c_int, [vp, P(i32), P(i64), P(i64)]),
+    "edgpu_op_slab_use": (ctypes.c_int, [vp, i32, i32, P(i32)]),
     "edgpu_op_build_adjoint_targets": (ctypes.c_int, [vp, i64, P(i32)]),
     "edgpu_op_table_prefetch": (ctypes.c_int, [vp, i32, i32, P(i32)]),
     "edgpu_op_grad_kernel": (ctypes.c_int, [vp, i32, P(i32)]),
@@ -99,6 +103,8 @@ SIGNATURES = {
     "edgpu_batch_create": (ctypes.c_int, [i32, P(vp), P(vp)]),
     "edgpu_batch_set_tiling": (ctypes.c_int, [vp, i32, i32]),
     "edgpu_batch_autotune": (ctypes.c_int, [vp, i32, P(i32), P(ctypes.c_double)]),
+    "edgpu_batch_set_launch": (ctypes.c_int, [vp, i32, i32]),
+    "edgpu_batch_get_launch": (ctypes.c_int, [vp, i32, P(i32)]),
     "edgpu_batch_mul_device": (ctypes.c_int, [vp, i32, P(vp), P(vp), i32, vp]),
     "edgpu_batch_destroy": (None, [vp]),
     "edgpu_lanczos": (ctypes.c_int, [vp, i32, i32, i32, u64, P(dbl), i32, dbl, P(dbl), P(dbl), P(dbl), P(i32),

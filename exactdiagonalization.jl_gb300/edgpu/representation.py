@@ -662,6 +662,36 @@ class OperatorRepresentation:
         check(lib().edgpu_op_targets_info(self._h, ctypes.byref(n), ctypes.byref(b)))
         return int(n.value), int(b.value)
 
+    def build_slabs(self, slab_bytes: int = 54 << 20, max_bytes: Optional[int] = None) -> bool:
+        """Build the column-slab table from the target table (which must exist): the product then runs
+        one pass per slab of slab_bytes of complex64 x, each gathering only from its slab (mixed
+        precision).  max_bytes defaults to a quarter of the free device memory.  Returns whether it
+        was built."""
+        if max_bytes is None:
+            import torch
+            free, _ = torch.cuda.mem_get_info()
+            max_bytes = free // 4
+        built = ctypes.c_int32()
+        check(lib().edgpu_op_build_slabs(self._h, int(slab_bytes), int(max_bytes), ctypes.byref(built)))
+        return bool(built.value)
+
+    def free_slabs(self) -> None:
+        check(lib().edgpu_op_free_slabs(self._h))
+
+    @property
+    def slabs_info(self) -> Tuple[int, int, int]:
+        """(passes, columns per slab, entries) of the slab table; zeros without one."""
+        a, b, c = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int64()
+        check(lib().edgpu_op_slabs_info(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return int(a.value), int(b.value), int(c.value)
+
+    def slab_use(self, precision="mixed", use: Optional[bool] = None) -> bool:
+        """Whether products read the slab table; sets it when use is given."""
+        cur = ctypes.c_int32()
+        check(lib().edgpu_op_slab_use(self._h, _prec(precision), -1 if use is None else int(bool(use)),
+                                      ctypes.byref(cur)))
+        return bool(cur.value)
+
     def pair_classes(self):
         """(bond classes, rotation components) of the pair-flip schedule; (0, 0) when it does not apply."""
         a, b = ctypes.c_int32(), ctypes.c_int32()
@@ -940,9 +970,20 @@ class Batch:
         check(lib().edgpu_batch_get_schedule(self._h, _prec(precision), None, None, ctypes.byref(t)))
         return bool(t.value)
 
+    def set_launch(self, precision, streams: int):
+        """0: all sectors in one persistent launch; 1: one product launch per sector on the call's
+        stream; 2 or 3: per-sector launches spread over that many concurrent streams."""
+        check(lib().edgpu_batch_set_launch(self._h, _prec(precision), int(streams)))
+
+    def launch(self, precision="mixed") -> int:
+        """The launch mode (see set_launch)."""
+        k = ctypes.c_int32()
+        check(lib().edgpu_batch_get_launch(self._h, _prec(precision), ctypes.byref(k)))
+        return int(k.value)
+
     def autotune(self, precision="mixed"):
-        """Time 1, 2 and 4 lanes per row, with and without the pair-flip schedule, and keep the
-        fastest; returns (lanes_per_row, ms)."""
+        """Time 1, 2 and 4 lanes per row, with and without the pair-flip schedule, and per-sector
+        launches on 1 to 3 streams, and keep the fastest; returns (lanes_per_row, ms)."""
         l = ctypes.c_int32()
         ms = ctypes.c_double()
         check(lib().edgpu_batch_autotune(self._h, _prec(precision), ctypes.byref(l), ctypes.byref(ms)))

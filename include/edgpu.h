@@ -233,6 +233,23 @@ int edgpu_op_build_adjoint_targets(edgpu_op op, int64_t max_bytes, int32_t* buil
 int edgpu_op_free_adjoint_targets(edgpu_op op);
 /* Entries of the target table and bytes per entry; 0 and 0 without a table. */
 int edgpu_op_targets_info(edgpu_op op, int64_t* entries, int32_t* entry_bytes);
+/* Column-slab table, built from the target table (which must exist) for mixed-precision products on
+ * large sectors.  The columns are cut into slabs of slab_bytes of complex64 x (at most 64 slabs);
+ * the product then runs one pass per slab, gathering only from that slab (sized to stay in L2) and
+ * adding its share to y, instead of gathering at random from all of x.  Results equal the one-pass
+ * product up to the order of the additions (the passes are added in order: reproducible run to
+ * run).  *built = 0 (nothing kept) when the table would exceed max_bytes, the sector has 2^32 rows or
+ * more, a row has more than 255 targets, the terms of one pair slot have different couplings, or the
+ * coefficient table does not fit; the autotuner then never picks it.  A new build replaces the old
+ * one; new coupling values rewrite its coefficient table in place. */
+int edgpu_op_build_slabs(edgpu_op op, int64_t slab_bytes, int64_t max_bytes, int32_t* built);
+int edgpu_op_free_slabs(edgpu_op op);
+/* Slabs (passes), columns per slab and entries of the slab table; zeros without one. */
+int edgpu_op_slabs_info(edgpu_op op, int32_t* passes, int64_t* columns_per_slab, int64_t* entries);
+/* Whether mixed-precision products read the slab table: use = 1 or 0 sets it (1 needs the table:
+ * EDGPU_ERR_STATE otherwise), -1 only queries; *current = the setting.  Building the table sets it;
+ * the autotuner times it against the one-pass schedules. */
+int edgpu_op_slab_use(edgpu_op op, int32_t precision, int32_t use, int32_t* current);
 /* Sparse matrix of the representation, assembled on the device in FP64: rows sorted by column,
  * entries of equal column summed, entries with |value| < tol dropped (tol: the reference's
  * Base.rtoldefault(Float64) = sqrt(eps) gives its default).  This is sparse(opr)
@@ -321,13 +338,24 @@ int edgpu_batch_create(int32_t n_ops, const edgpu_op* ops, edgpu_batch* out);
 /* Lanes per row of the batched launch for this precision: 0 (default: 1), 1, 2 or 4. */
 int edgpu_batch_set_tiling(edgpu_batch b, int32_t precision, int32_t lanes_per_row);
 /* In-library autotuner: times the batched launch for 1, 2 and 4 lanes per row, with and without the
- * pair-flip schedule where it applies (and the first operator allows it), on scratch vectors
- * (allocated and freed here) and keeps the fastest. */
+ * pair-flip schedule where it applies (and the first operator allows it), and for the pair-flip
+ * schedules also per-sector launches on 1, 2 and 3 streams (edgpu_batch_set_launch), on scratch
+ * vectors (allocated and freed here) and keeps the fastest. */
 int edgpu_batch_autotune(edgpu_batch b, int32_t precision, int32_t* lanes_per_row_out, double* best_ms_out);
 /* The batched launch's lanes per row (0 = default), and pair_flips and target_table as in
  * edgpu_op_get_schedule (the batch reads target tables when every operator has one). */
 int edgpu_batch_get_schedule(edgpu_batch b, int32_t precision, int32_t* lanes_per_row, int32_t* pair_flips,
                              int32_t* target_table);
+/* How the batch launches (autotuned with the schedule; default 0):
+ *   0       all sectors in ONE persistent launch (above);
+ *   1       one product launch per sector, in order on the call's stream: each sector's own product
+ *           kernel with the batch's schedule (results equal edgpu_mul_device on the sector, bit for bit);
+ *   2 or 3  the same per-sector launches spread over that many streams of the batch (sector k on
+ *           stream k mod streams), forked from and joined back into the call's stream, so that a
+ *           sector's launch fills the SMs that the previous sector's last blocks leave idle.
+ * The per-sector modes read the operators' own tables, not a batched image. */
+int edgpu_batch_set_launch(edgpu_batch b, int32_t precision, int32_t streams);
+int edgpu_batch_get_launch(edgpu_batch b, int32_t precision, int32_t* streams);
 /* y_k = H_k x_k for every k, device vectors (arrays of n_ops pointers).  The first call with a set of
  * pointers uploads the sector descriptors (synchronous); if use_graph != 0 that launch is also
  * captured once into a CUDA graph and replayed on the later calls with the same pointers. */

@@ -1,5 +1,5 @@
-"""Batched sectors in one persistent launch (edgpu_batch_*) against the oracle and against the
-single-sector product.
+"""Batched sectors (edgpu_batch_*: one persistent launch, or per-sector launches on one to three
+streams) against the oracle and against the single-sector product.
 
 Every momentum sector of one Hamiltonian goes through one launch; each sector's result must equal
 the single-sector product with the same lanes per row bit for bit, and the oracle's reduced product
@@ -72,13 +72,18 @@ def run_batch_checks(E, oprs, reds, terms):
                 E.mul_(y, o, x, precision=prec)
                 ref.append(y)
                 o.set_tiling(prec, 0)
-            for use_graph in (False, True, True):
-                ys = [torch.full_like(x, float("nan")) for x in xs]
-                b.mul_(ys, xs, precision=prec, use_graph=use_graph)
-                torch.cuda.synchronize()
-                for k, (y, r, w) in enumerate(zip(ys, ref, want)):
-                    assert torch.equal(y, r), (prec, lpr, use_graph, k)
-                    assert relerr(y.cpu().numpy().astype(np.complex128), w) < tol, (prec, lpr, k)
+            # one persistent launch; with one lane per row also per-sector launches on 1 to 3 streams
+            for launch in ((0, 1, 2, 3) if lpr == 1 else (0,)):
+                b.set_launch(prec, launch)
+                assert b.launch(prec) == launch
+                for use_graph in (False, True, True):
+                    ys = [torch.full_like(x, float("nan")) for x in xs]
+                    b.mul_(ys, xs, precision=prec, use_graph=use_graph)
+                    torch.cuda.synchronize()
+                    for k, (y, r, w) in enumerate(zip(ys, ref, want)):
+                        assert torch.equal(y, r), (prec, lpr, launch, use_graph, k)
+                        assert relerr(y.cpu().numpy().astype(np.complex128), w) < tol, (prec, lpr, k)
+            b.set_launch(prec, 0)
         b.set_tiling(prec, 0)
     return b
 
@@ -165,6 +170,8 @@ def test_batch_rejects_different_operators(edgpu):
         edgpu.Batch([o1, o1]).mul_(ys, xs)
     with pytest.raises(edgpu.ArgumentError):
         b.set_tiling("mixed", 3)
+    with pytest.raises(edgpu.ArgumentError):
+        b.set_launch("mixed", 4)
 
 
 def test_batch_follows_coupling_changes_and_autotune(edgpu):
@@ -181,6 +188,7 @@ def test_batch_follows_coupling_changes_and_autotune(edgpu):
     b = edgpu.Batch(oprs)
     lpr, ms = b.autotune("mixed")
     assert lpr in (1, 2, 4) and ms > 0
+    assert b.launch("mixed") in (0, 1, 2, 3)
     xs = [edgpu.random_state(o.dimension, 10 + i, "mixed") for i, o in enumerate(oprs)]
     for step in range(2):
         ys = [torch.empty_like(x) for x in xs]
