@@ -62,6 +62,10 @@ WORKLOADS = {
     "chain28_k0": dict(kind="chain", L=28, k=0, jxy=1.0, jz=1.0, seed=5, lanczos_steps=200, reorth=True,
                        N_r=1432860, nnz_off=20803084, steps=500,
                        desc="spin-1/2 Heisenberg chain L=28 PBC, 2Sz=0, momentum 0"),
+    "chain32_k0": dict(kind="chain", L=32, k=0, jxy=1.0, jz=1.0, seed=6, lanczos_steps=200, reorth=False,
+                       cpu_feasible=False, N_r=18784170, nnz_off=None, steps=50,
+                       desc="spin-1/2 Heisenberg chain L=32 PBC, 2Sz=0, momentum 0 (the smallest chain sector "
+                            "whose x exceeds L2: the small case for profiling the slab product)"),
     "triangular6x5_allk": dict(kind="torus_allk", shape=(6, 5), nn=[(1, 0), (1, 1), (0, 1)],
                                nnn=[(2, 1), (1, 2), (-1, 1)], j1=1.0, j2=0.125, aniso=0.8, seed=3,
                                cpu_feasible=False, N_r=155117520, nnz_off=14441957888, steps=20,
@@ -161,6 +165,24 @@ def build_tables(oprs, spaces, args):
             sp.free_map()
             freed = True
     return {"built": True, "entries": entries, "bytes": nbytes, "build_s": dt, "maps_freed": freed}
+
+
+def build_slabs(opr, N, args):
+    """Column-slab table of a sector whose complex64 x exceeds L2, unless --slab-mb 0:
+    {"built", "passes", "columns_per_slab", "entries", "bytes", "build_s"} or None."""
+    import torch
+    if args.slab_mb <= 0 or 8 * N <= L2_BYTES or not hasattr(opr, "build_slabs"):
+        return None
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    free, _ = torch.cuda.mem_get_info()
+    built = opr.build_slabs(slab_bytes=int(args.slab_mb * (1 << 20)), max_bytes=int(0.8 * free))
+    dt = time.perf_counter() - t0
+    if not built:
+        return {"built": False}
+    passes, wc, entries = opr.slabs_info
+    return {"built": True, "passes": passes, "columns_per_slab": wc, "entries": entries,
+            "bytes": entries * 4 + passes * N + passes * ((N + 31) // 32) * 4, "build_s": dt}
 
 
 def build_gpu_operator(wl):
@@ -464,10 +486,11 @@ def run_gpu(args, wl):
     dir_stats = edgpu.search_stats(space)
     map_info = build_maps([space], args)
     table_info = build_tables([opr], [space], args)
+    slab_info = build_slabs(opr, N, args) if table_info and table_info.get("built") else None
     if args.no_pair:
         opr.set_pair_schedule(False)
     if args.tiling:
-        # a fixed schedule instead of the autotuner (reproducible profiles)
+        # a fixed schedule instead of the autotuner (reproducible profiles); the slab table when built
         opr.set_pair_schedule(args.pair_targets > 0, max(args.pair_targets, 2), args.uniform)
         for prec in ("mixed", "fp64"):
             opr.set_tiling(prec, args.tiling)
@@ -625,7 +648,10 @@ def run_gpu(args, wl):
                "kind": r["kind"], "sample": r["sample"], "ms_per_step": r["ms_per_step"]}
 
     peak, peak_src = measured_peak()
-    traffic = profiled_traffic(args.workload)
+    slab_used = bool(slab_info and slab_info.get("built") and opr.slab_use("mixed"))
+    # DRAM bytes per step of the product as profiled: the slab product's passes, or the one-pass kernel
+    traffic = profiled_traffic(args.workload + ("_slabs" if slab_used else ""))
+    launches_per_step = slab_info["passes"] if slab_used else 1
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
@@ -640,11 +666,12 @@ def run_gpu(args, wl):
                        "target_table": dict(table_info or {"built": False},
                                             used={"mixed": opr.uses_target_table("mixed"),
                                                   "fp64": opr.uses_target_table("fp64")}),
+                       "slab_table": dict(slab_info or {"built": False}, used={"mixed": slab_used}),
                        "setup_s": t_space, "search_directory": dir_stats, "parent_map": map_info},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_src},
             "cpu_baseline": cpu, "e2e": e2e, "e2e_more": e2e_more, "host_link": host_link,
-            "gpu_launches": args.steps, "clocks": clk,
+            "gpu_launches": args.steps * launches_per_step, "clocks": clk,
             "fp64": {"value": value64, "unit": "GB/s", "ms_per_step": ms64 / fp64_steps, "frac": value64 / peak},
             "e0": e0_info}
     if rank == 0:
@@ -894,6 +921,8 @@ def main():
     ap.add_argument("--uniform", action="store_true", help="with --tiling: warp-uniform pair steps (4 or 8 targets)")
     ap.add_argument("--prefetch", type=int, default=0, help="with --tiling: x prefetch distance of the target-table product")
     ap.add_argument("--no-table", action="store_true", help="no target tables (look every target up per product)")
+    ap.add_argument("--slab-mb", type=float, default=54.0,
+                    help="column slabs of this many MB of complex64 x for sectors whose x exceeds L2 (0: none)")
     ap.add_argument("--no-pair", action="store_true", help="test every term per row instead of the pair-flip schedule")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-per-sector", action="store_true",
@@ -905,7 +934,11 @@ def main():
     wl = WORKLOADS[args.workload]
     if args.steps is None:
         args.steps = wl["steps"]
-    if args.impl == "reference":
+    if args.impl == "reference" and wl["nnz_off"] is None:
+        if int(os.environ.get("RANK", "0")) == 0:
+            print(json.dumps({"impl": "reference", "unavailable": f"{args.workload} is a profiling case without "
+                                                                  "a fixed nonzero count for the byte model"}))
+    elif args.impl == "reference":
         run_reference(args, wl)
     elif wl["kind"] == "torus_allk":
         run_gpu_batch(args, wl)

@@ -216,7 +216,15 @@ struct edgpu_op_s {
         int lut_real = 1;
     } slab;
     int slab_use[2] = {0, 0};         // [precision]: products read the slab table (chosen by the autotuner)
+    // the optional tables change: cached graphs (this handle's host-buffer graphs, and batches, which
+    // compare gen) must not replay launches that read the old ones
+    void drop_host_graphs() {
+        for (auto& kv : host_graphs) cudaGraphExecDestroy(kv.second);
+        host_graphs.clear();
+        ++gen;
+    }
     void free_slabs() {
+        drop_host_graphs();
         if (slab.tab) cudaFree(slab.tab);
         if (slab.counts) cudaFree(slab.counts);
         if (slab.off) cudaFree(slab.off);
@@ -225,6 +233,7 @@ struct edgpu_op_s {
         slab_use[0] = slab_use[1] = 0;
     }
     void free_table() {
+        drop_host_graphs();
         if (d_tab) cudaFree(d_tab);
         if (d_tile_off) cudaFree(d_tile_off);
         d_tab = nullptr;
@@ -232,6 +241,7 @@ struct edgpu_op_s {
         tab_n = 0;
     }
     void free_adjoint() {
+        drop_host_graphs();
         if (d_adj_off) cudaFree(d_adj_off);
         if (d_adj_tab) cudaFree(d_adj_tab);
         d_adj_off = nullptr;
@@ -239,7 +249,7 @@ struct edgpu_op_s {
         adj_n = 0;
     }
     ~edgpu_op_s() {
-        for (auto& kv : host_graphs) cudaGraphExecDestroy(kv.second);
+        drop_host_graphs();
         free_table();
         free_adjoint();
         free_slabs();
@@ -544,6 +554,9 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     p.rlut_pair = use_pair ? 1 : 0;
     BondClasses bc, bcu;   // bond classes with the coupled amplitudes; (gradient mode) with the unit ones
     bool grad_pair = false;  // gradient mode: the pair-flip gradient kernel applies
+    struct DiagPair { int i, j, cid; double u[4][2]; };
+    std::vector<DiagPair> dpairs;   // gradient mode: the diagonal records by site pair (below)
+    int n_pdb = -1;
     if (mode == 0 || dir == 0) {
         std::vector<uint64_t> bm, br, bf;
         std::vector<double> ba, bu;
@@ -569,9 +582,55 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
             // masks and patterns)
             grad_pair = build_bond_classes(s.lay, bm, br, bf, bu, bcu) && bcu.ncls == bc.ncls;
         }
+        // the diagonal records by site pair: when every record's mask has at most two bits, the records of
+        // one (pair, coupling) become one entry with a unit amplitude per pattern of the pair's two bits
+        // (a one-bit mask is the pair (i, i), patterns 0 and 3; an empty mask adds to both), so that the
+        // gradient kernel looks up one value per entry and row instead of testing every record
+        if (grad_pair) {
+            std::map<std::tuple<int, int, int>, int> at;
+            bool ok = true;
+            for (int k = 0; k < T_d && ok; ++k) {
+                const int t = diag[k];
+                const uint64_t m = op->masks[t];
+                const uint64_t r = dir ? op->cols[t] : op->rows[t];
+                const int pc = __builtin_popcountll(m);
+                if (pc > 2) {
+                    ok = false;
+                    break;
+                }
+                const int i = pc ? __builtin_ctzll(m) : 0;
+                const int j = pc == 2 ? 63 - __builtin_clzll(m) : i;
+                const auto key = std::make_tuple(i, j, op->cid[t]);
+                auto it = at.find(key);
+                if (it == at.end()) {
+                    it = at.emplace(key, (int)dpairs.size()).first;
+                    DiagPair d{};
+                    d.i = i;
+                    d.j = j;
+                    d.cid = op->cid[t];
+                    dpairs.push_back(d);
+                }
+                double v[2];
+                amp_of(t, true, v[0], v[1]);
+                DiagPair& d = dpairs[it->second];
+                for (int pat = 0; pat < 4; ++pat) {
+                    const int bi = pat & 1, bj = pat >> 1;
+                    if (pc == 1 && bi != bj) continue;   // pattern of the pair (i, i)
+                    const bool match = pc == 0 || (((r >> i) & 1) == (uint64_t)bi && ((r >> j) & 1) == (uint64_t)bj);
+                    if (match) {
+                        d.u[pat][0] += v[0];
+                        d.u[pat][1] += v[1];
+                    }
+                }
+            }
+            if (!ok) dpairs.clear();
+            else n_pdb = (int)dpairs.size();
+        }
         // keep the pair-flip kernel's shared memory within 48 KB (five or more blocks per SM)
         size_t bond_bytes = (size_t)bc.ncls * (BOND_MAXC * 4 * wsz + 16 + s.lay.nbits * (wsz + 4 * vsz));
-        if (grad_pair) bond_bytes += (size_t)bc.ncls * s.lay.nbits * 4 * (vsz + 4) + (size_t)T_d * (2 * wsz + 20);
+        if (grad_pair)
+            bond_bytes += (size_t)bc.ncls * s.lay.nbits * 4 * (vsz + 4) +
+                          (n_pdb >= 0 ? (size_t)n_pdb * (4 + 4 * vsz) : (size_t)T_d * (2 * wsz + vsz + 4));
         const size_t rlut_bytes = use_rlut ? ((size_t)1 << lut_bits) * 4 : 0;
         if (off + bond_bytes + rlut_bytes > 48 * 1024) {
             bc = BondClasses();
@@ -590,64 +649,19 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     // of the diagonal term records (mask, row, unit amplitude, coupling id)
     p.o_bunit = p.o_bcid = p.o_pdm = p.o_pdr = p.o_pdu = p.o_pdc = -1;
     p.o_pdb = p.o_pdv = -1;
-    p.n_pdb = -1;
+    p.n_pdb = grad_pair ? n_pdb : -1;
     p.bunit_real = 0;
-    // the diagonal records by site pair: when every record's mask has at most two bits, the records of
-    // one (pair, coupling) become one entry with a unit amplitude per pattern of the pair's two bits
-    // (a one-bit mask is the pair (i, i), patterns 0 and 3; an empty mask adds to both), so that the
-    // gradient kernel looks up one value per entry and row instead of testing every record
-    struct DiagPair { int i, j, cid; double u[4][2]; };
-    std::vector<DiagPair> dpairs;
-    if (grad_pair) {
-        std::map<std::tuple<int, int, int>, int> at;
-        bool ok = true;
-        for (int k = 0; k < T_d && ok; ++k) {
-            const int t = diag[k];
-            const uint64_t m = op->masks[t];
-            const uint64_t r = dir ? op->cols[t] : op->rows[t];
-            const int pc = __builtin_popcountll(m);
-            if (pc > 2) {
-                ok = false;
-                break;
-            }
-            const int i = pc ? __builtin_ctzll(m) : 0;
-            const int j = pc == 2 ? 63 - __builtin_clzll(m) : i;
-            const auto key = std::make_tuple(i, j, op->cid[t]);
-            auto it = at.find(key);
-            if (it == at.end()) {
-                it = at.emplace(key, (int)dpairs.size()).first;
-                DiagPair d{};
-                d.i = i;
-                d.j = j;
-                d.cid = op->cid[t];
-                dpairs.push_back(d);
-            }
-            double v[2];
-            amp_of(t, true, v[0], v[1]);
-            DiagPair& d = dpairs[it->second];
-            for (int pat = 0; pat < 4; ++pat) {
-                const int bi = pat & 1, bj = pat >> 1;
-                if (pc == 1 && bi != bj) continue;   // pattern of the pair (i, i)
-                const bool match = pc == 0 || (((r >> i) & 1) == (uint64_t)bi && ((r >> j) & 1) == (uint64_t)bj);
-                if (match) {
-                    d.u[pat][0] += v[0];
-                    d.u[pat][1] += v[1];
-                }
-            }
-        }
-        if (!ok) dpairs.clear();
-        else p.n_pdb = (int)dpairs.size();
-    }
     if (grad_pair) {
         p.o_bunit = alloc((size_t)bc.ncls * n_b * 4 * vsz);
         p.o_bcid = alloc((size_t)bc.ncls * n_b * 4 * 4);
-        p.o_pdm = alloc((size_t)T_d * wsz);
-        p.o_pdr = alloc((size_t)T_d * wsz);
-        p.o_pdu = alloc((size_t)T_d * vsz);
-        p.o_pdc = alloc((size_t)T_d * 4);
         if (p.n_pdb >= 0) {
             p.o_pdb = alloc(dpairs.size() * 4);
             p.o_pdv = alloc(dpairs.size() * 4 * vsz);
+        } else {
+            p.o_pdm = alloc((size_t)T_d * wsz);
+            p.o_pdr = alloc((size_t)T_d * wsz);
+            p.o_pdu = alloc((size_t)T_d * vsz);
+            p.o_pdc = alloc((size_t)T_d * 4);
         }
     }
     // the prefix a mapped pair-flip launch copies ends here; the torus row table follows (needed by
@@ -765,7 +779,7 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
         p.bunit_real = bcu.real ? 1 : 0;
         for (size_t i = 0; i < bcu.flip.size() * 4; ++i) putv(p.o_bunit, i, bcu.amp[2 * i], bcu.amp[2 * i + 1]);
         memcpy(&h[p.o_bcid], bc.cid.data(), bc.cid.size() * 4);
-        for (int k = 0; k < T_d; ++k) {
+        for (int k = 0; k < T_d && p.n_pdb < 0; ++k) {
             const int t = diag[k];
             const uint64_t r = dir ? op->cols[t] : op->rows[t];
             putw(p.o_pdm, k, op->masks[t]);
@@ -2111,43 +2125,56 @@ int edgpu_op_build_slabs(edgpu_op oh, int64_t slab_bytes, int64_t max_bytes, int
     }
     const Blob& B = op->blob[prec][0][0];
     if (B.tmpl.bond_ncls == 0) return EDGPU_OK;
-    // the slots' unit amplitudes and coupling ids: the FP64 gradient-mode image (absent when the terms
-    // of one slot have different couplings)
-    build_blob(op, EDGPU_FP64, 0, 1);
-    const Blob& G = op->blob[EDGPU_FP64][0][1];
-    const HxParams& gp = G.tmpl_pair;
+    // the slots' coupling ids and unit amplitudes: the bond classes of the terms, once with the coupled
+    // amplitudes (and coupling ids), once with the unit ones; their pairs must be the product's
     const int nb = sp.lay.nbits, ncls = B.tmpl.bond_ncls;
-    if (G.tmpl.o_bunit < 0 || gp.bond_ncls != ncls) return EDGPU_OK;
+    BondClasses bc, bcu;
+    {
+        std::vector<uint64_t> bm, br, bf;
+        std::vector<double> ba, bu;
+        std::vector<int32_t> bid;
+        for (int t = 0; t < op->T; ++t) {
+            if (op->rows[t] == op->cols[t]) continue;
+            bm.push_back(op->masks[t]);
+            br.push_back(op->rows[t]);
+            bf.push_back(op->rows[t] ^ op->cols[t]);
+            const double c = op->coupl[op->cid[t]];
+            ba.push_back(op->unit[2 * t] * c);
+            ba.push_back(op->unit[2 * t + 1] * c);
+            bu.push_back(op->unit[2 * t]);
+            bu.push_back(op->unit[2 * t + 1]);
+            bid.push_back(op->cid[t]);
+        }
+        if (!build_bond_classes(sp.lay, bm, br, bf, ba, bc, &bid) || !bc.cid_ok ||
+            !build_bond_classes(sp.lay, bm, br, bf, bu, bcu) || bc.ncls != ncls || bcu.ncls != ncls)
+            return EDGPU_OK;
+    }
     const size_t wsz = sp.w32 ? 4 : 8;
-    const size_t fl_bytes = (size_t)ncls * nb * wsz;
-    if ((size_t)B.tmpl_pair.o_bflip + fl_bytes > B.pair_host.size() || (size_t)gp.o_bflip + fl_bytes > G.pair_host.size() ||
-        memcmp(&B.pair_host[B.tmpl_pair.o_bflip], &G.pair_host[gp.o_bflip], fl_bytes) != 0)
-        return EDGPU_OK;
-    // a row's targets in one slab are counted in a byte: at most 255 pairs
+    if ((size_t)B.tmpl_pair.o_bflip + (size_t)ncls * nb * wsz > B.pair_host.size()) return EDGPU_OK;
     int n_pairs = 0;
     for (int k = 0; k < ncls * nb; ++k) {
         uint64_t f = 0;
-        memcpy(&f, &G.pair_host[gp.o_bflip + k * wsz], wsz);
+        memcpy(&f, &B.pair_host[B.tmpl_pair.o_bflip + k * wsz], wsz);
+        if (f != bc.flip[k] || f != bcu.flip[k]) return EDGPU_OK;
         n_pairs += f != 0;
     }
+    // a row's targets in one slab are counted in a byte: at most 255 pairs
     if (n_pairs > 255) return EDGPU_OK;
     auto& S = op->slab;
     const int n_slots = ncls * nb * 4;
     std::vector<unsigned short> amp_id((size_t)n_slots, 0);
     std::map<std::tuple<int, double, double>, int> ids;
     for (int k = 0; k < n_slots; ++k) {
-        double u[2];
-        int32_t c = -1;
-        memcpy(u, &G.pair_host[gp.o_bunit + (size_t)k * 16], 16);
-        memcpy(&c, &G.pair_host[gp.o_bcid + (size_t)k * 4], 4);
+        const int32_t c = bc.cid[k];
         if (c < 0) continue;
-        const auto key = std::make_tuple((int)c, u[0], u[1]);
+        const double u0 = bcu.amp[2 * (size_t)k], u1 = bcu.amp[2 * (size_t)k + 1];
+        const auto key = std::make_tuple((int)c, u0, u1);
         auto it = ids.find(key);
         if (it == ids.end()) {
             it = ids.emplace(key, (int)S.amp_cid.size()).first;
             S.amp_cid.push_back(c);
-            S.amp_unit.push_back(u[0]);
-            S.amp_unit.push_back(u[1]);
+            S.amp_unit.push_back(u0);
+            S.amp_unit.push_back(u1);
         }
         amp_id[k] = (unsigned short)it->second;
     }
@@ -2604,11 +2631,19 @@ static void host_product(edgpu_op_s* op, int prec, int dir, const double* x, dou
         return;
     }
     build_blob(op, prec, dir, 0);
+    // the graph replays the launches of this call: the key holds everything they depend on (buffers,
+    // tables, the schedule)
     const std::vector<const void*> key = {(const void*)x, (const void*)y, (const void*)(intptr_t)n,
                                           (const void*)(intptr_t)(prec * 8 + dir * 4 + accumulate * 2 + (conj_io ? 1 : 0)),
                                           (const void*)op->x64.p, (const void*)op->y64.p,
+                                          (const void*)op->x32.p, (const void*)op->y32.p,
                                           (const void*)op->space->d_map, (const void*)(uintptr_t)op->gen,
-                                          (const void*)(intptr_t)op->tuned_rows[prec]};
+                                          (const void*)(intptr_t)op->tuned_rows[prec],
+                                          op->d_tab, (const void*)op->slab.tab,
+                                          (const void*)(intptr_t)(op->pair_allowed + 2 * op->pair_use[prec] +
+                                                                  4 * op->pair_nt[prec] + 64 * op->tab_use[prec] +
+                                                                  128 * op->tab_uni[prec] + 256 * op->slab_use[prec] +
+                                                                  512 * op->tab_pf[prec])};
     auto it = op->host_graphs.find(key);
     if (it == op->host_graphs.end()) {
         cudaStream_t cap = nullptr;
@@ -3152,23 +3187,26 @@ void batch_launch(edgpu_batch_s* b, int prec, const HxParams& p, int blocks, cud
 }
 
 // One sector of a batch launched on its own: the operator's product kernel with the batch's schedule
-// (pair flips, targets per step, target table, prefetch, lanes per row) in place of the operator's
-// own for this launch.  The caller holds the operators' locks.
+// (pair flips, targets per step, target table, prefetch, lanes per row; no slab table) in place of
+// the operator's own for this launch.  The caller holds the operators' locks.
 void batch_sector_launch(edgpu_batch_s* b, int prec, int i, const void* x, void* y, cudaStream_t st) {
     edgpu_op_s* op = b->ops[i];
     if (op->space->dim == 0) return;
-    const int keep[5] = {op->pair_use[prec], op->pair_nt[prec], op->tab_use[prec], op->tab_pf[prec], op->tab_uni[prec]};
+    const int keep[6] = {op->pair_use[prec], op->pair_nt[prec], op->tab_use[prec], op->tab_pf[prec], op->tab_uni[prec],
+                         op->slab_use[prec]};
     op->pair_use[prec] = b->pair_use[prec];
     op->pair_nt[prec] = b->pair_nt[prec];
     op->tab_use[prec] = b->tab_use[prec];
     op->tab_pf[prec] = b->tab_pf[prec];
     op->tab_uni[prec] = 0;
+    op->slab_use[prec] = 0;
     auto restore = [&] {
         op->pair_use[prec] = keep[0];
         op->pair_nt[prec] = keep[1];
         op->tab_use[prec] = keep[2];
         op->tab_pf[prec] = keep[3];
         op->tab_uni[prec] = keep[4];
+        op->slab_use[prec] = keep[5];
     };
     try {
         launch_product(op, prec, 0, 0, x, y, 0, nullptr, nullptr, st, nullptr, -(b->lpr[prec] ? b->lpr[prec] : 1));

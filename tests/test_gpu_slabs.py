@@ -1,0 +1,161 @@
+"""The column-slab table and its multi-pass mixed-precision product (edgpu_op_build_slabs).
+
+Small slabs force several passes on sectors the oracle handles in seconds: the product must match the
+oracle's reduced product within 1e-5 (mixed precision) and the one-pass target-table product within
+1e-6, be reproducible bit for bit, accumulate (y += H x), write complex128 host buffers, follow new
+coupling values, and cover real and complex coefficients (momentum 0 and k != 0), a torus and a
+chain."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def relerr(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def _chain(E, L, k, coupled):
+    from edgpu import lattice
+    hs, _ = E.spin_half_system(L)
+    hsr = E.represent(E.HilbertSpaceSector(hs, 0))
+    rh = E.symmetry_reduce(hsr, E.translation_symops(L, k))
+    sites = O.spin_half_sites(L)
+    parent = O.hs_get_basis_list(sites, [(0,)])
+    bw, off = O.bit_layout(sites)
+    maps, amps = O.translation_symops((L, 1), (k, 0))
+    red = O.symmetry_reduce(parent, bw, off, maps, amps)
+    if coupled:
+        m, r, c, a, ids = lattice.heisenberg_coupled(hs, lattice.chain_bonds(L))
+        J = 0.5 + np.random.default_rng(3).random(L)
+        opr = E.OperatorRepresentation.from_terms(rh, m, r, c, a, coupling_ids=ids, couplings=J)
+        terms = [(int(m[t]), int(r[t]), int(c[t]), complex(a[t]) * J[ids[t]]) for t in range(len(m))]
+        return opr, red, terms, (m, r, c, a, ids, J)
+    bonds = lattice.chain_bonds(L) + [(i, (i + 2) % L) for i in range(L)]
+    jxy, jz = [1.0] * L + [0.4] * L, [0.8] * L + [0.3] * L
+    H = lattice.xxz_hamiltonian(hs, bonds, jxy, jz)
+    return E.represent(rh, H), red, O.heisenberg_terms(L, bonds, jxy, jz), None
+
+
+def _products(E, opr, x):
+    import torch
+    xd = torch.from_numpy(x).to(torch.complex64).cuda()
+    y = torch.empty_like(xd)
+    E.mul_(y, opr, xd, precision="mixed")
+    torch.cuda.synchronize()
+    return xd, y
+
+
+@pytest.mark.parametrize("L,k,coupled", [(20, 0, False), (18, 5, False), (20, 0, True)])
+def test_slab_product_chain(L, k, coupled):
+    import torch
+    import edgpu as E
+    opr, red, terms, extra = _chain(E, L, k, coupled)
+    N = opr.dimension
+    assert opr.build_targets(1 << 30)
+    x = O.complex_gaussian(N, 7)
+    want = O.apply_rows(red, terms, x)
+    xd, y_tab = _products(E, opr, x)
+    # slabs of 1024 columns: several passes
+    assert opr.build_slabs(slab_bytes=1024 * 8, max_bytes=1 << 30)
+    passes, wc, entries = opr.slabs_info
+    assert wc == 1024 and passes == (N + 1023) // 1024 and passes >= 3
+    assert 0 < entries <= opr.targets_info[0]   # the targets with a representative
+    assert opr.slab_use("mixed")
+    y = torch.empty_like(xd)
+    E.mul_(y, opr, xd, precision="mixed")
+    y2 = torch.full_like(xd, float("nan"))
+    E.mul_(y2, opr, xd, precision="mixed")
+    torch.cuda.synchronize()
+    assert torch.equal(y, y2)
+    yn = y.cpu().numpy().astype(np.complex128)
+    assert relerr(yn, want) < 1e-5
+    assert relerr(yn, y_tab.cpu().numpy().astype(np.complex128)) < 1e-6
+    # y += H x
+    y3 = y.clone()
+    E.apply_(y3, opr, xd, precision="mixed")
+    torch.cuda.synchronize()
+    assert relerr(y3.cpu().numpy().astype(np.complex128), 2 * want) < 1e-5
+    # complex128 host buffers (the last pass writes complex128)
+    yh = np.zeros(N, dtype=np.complex128)
+    E.mul_(yh, opr, x, precision="mixed")
+    assert relerr(yh, want) < 1e-5
+    yh2 = yh.copy()
+    E.apply_(yh2, opr, x, precision="mixed")
+    assert relerr(yh2, 2 * want) < 1e-5
+    # FP64 products do not read the slab table
+    yf = np.zeros(N, dtype=np.complex128)
+    E.mul_(yf, opr, x, precision="fp64")
+    assert relerr(yf, want) < 1e-12
+    if coupled:
+        m, r, c, a, ids, J = extra
+        J2 = J[::-1] * 1.3
+        opr.set_couplings(J2)
+        terms2 = [(int(m[t]), int(r[t]), int(c[t]), complex(a[t]) * J2[ids[t]]) for t in range(len(m))]
+        _, y4 = _products(E, opr, x)
+        assert relerr(y4.cpu().numpy().astype(np.complex128), O.apply_rows(red, terms2, x)) < 1e-5
+    # switched off: the one-pass product again, bit for bit
+    assert not opr.slab_use("mixed", False)
+    if not coupled:
+        _, y5 = _products(E, opr, x)
+        assert torch.equal(y5, y_tab)
+    # the autotuner times the slab product among the others
+    opr.autotune("mixed")
+    _, y6 = _products(E, opr, x)
+    assert relerr(y6.cpu().numpy().astype(np.complex128), want if not coupled else
+                  O.apply_rows(red, terms2, x)) < 1e-5
+    opr.free_slabs()
+    assert opr.slabs_info == (0, 0, 0)
+    with pytest.raises(RuntimeError):
+        opr.slab_use("mixed", True)
+
+
+def test_slab_product_torus_j1j2():
+    import torch
+    import edgpu as E
+    from edgpu import lattice
+    shape = (6, 3)
+    n = shape[0] * shape[1]
+    hs, _ = E.spin_half_system(n)
+    nn = lattice.torus_bonds(*shape, [(1, 0), (0, 1)])
+    nnn = lattice.torus_bonds(*shape, [(1, 1), (1, -1)])
+    jj = [1.0] * len(nn) + [0.5] * len(nnn)
+    H = lattice.xxz_hamiltonian(hs, nn + nnn, jj, jj)
+    terms = O.heisenberg_terms(n, nn + nnn, jj, jj)
+    sites = O.spin_half_sites(n)
+    parent = O.hs_get_basis_list(sites, [(0,)])
+    bw, off = O.bit_layout(sites)
+    for k in ((0, 0), (1, 1)):
+        hsr = E.represent(E.HilbertSpaceSector(hs, 0))
+        opr = E.represent(E.symmetry_reduce(hsr, E.translation_symops(shape, k)), H)
+        maps, amps = O.translation_symops(shape, k)
+        red = O.symmetry_reduce(parent, bw, off, maps, amps)
+        N = opr.dimension
+        assert opr.build_targets(1 << 30)
+        assert opr.build_slabs(slab_bytes=1024 * 8, max_bytes=1 << 30)
+        assert opr.slabs_info[0] >= 3
+        x = O.complex_gaussian(N, 9)
+        _, y = _products(E, opr, x)
+        assert relerr(y.cpu().numpy().astype(np.complex128), O.apply_rows(red, terms, x)) < 1e-5
+
+
+def test_slab_build_refusals():
+    import edgpu as E
+    opr, _, _, _ = _chain(E, 12, 0, False)
+    # no target table: nothing built
+    assert not opr.build_slabs(slab_bytes=1 << 20)
+    assert opr.build_targets(1 << 30)
+    # a byte limit below the table's size: nothing kept
+    assert not opr.build_slabs(slab_bytes=1 << 20, max_bytes=16)
+    assert opr.slabs_info == (0, 0, 0)
+    # slabs of at least 1024 columns: one pass for this small sector (the first pass is also the last)
+    assert opr.build_slabs(slab_bytes=8, max_bytes=1 << 30)
+    assert opr.slabs_info[0] == 1 and opr.slabs_info[1] == 1024
+    import torch
+    x = O.complex_gaussian(opr.dimension, 2)
+    _, y = _products(E, opr, x)
+    opr.slab_use("mixed", False)
+    _, y0 = _products(E, opr, x)
+    assert relerr(y.cpu().numpy().astype(np.complex128), y0.cpu().numpy().astype(np.complex128)) < 1e-6
