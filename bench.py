@@ -495,10 +495,18 @@ def run_gpu(args, wl):
         for prec in ("mixed", "fp64"):
             opr.set_tiling(prec, args.tiling)
             opr.table_prefetch(prec, args.prefetch)
+            if slab_info and slab_info.get("built"):
+                opr.slab_use(prec, 2 if args.slab_hints else 1)
         tune_mixed = tune_fp64 = (args.tiling, None)
     else:
         tune_mixed = opr.autotune("mixed")
         tune_fp64 = opr.autotune("fp64")
+    if slab_info and slab_info.get("built") and opr.slab_use("mixed") and opr.slab_use("fp64") and \
+            not args.keep_targets:
+        # both precisions read the slab table: the target table (75 GB on 6x6) is only kept for the
+        # autotuner, and its memory goes to the Krylov basis of the E0 runs
+        opr.free_targets()
+        table_info["freed_after_slabs"] = True
     stream = torch.cuda.current_stream()
 
     def pool(prec):
@@ -666,7 +674,10 @@ def run_gpu(args, wl):
                        "target_table": dict(table_info or {"built": False},
                                             used={"mixed": opr.uses_target_table("mixed"),
                                                   "fp64": opr.uses_target_table("fp64")}),
-                       "slab_table": dict(slab_info or {"built": False}, used={"mixed": slab_used}),
+                       "slab_table": dict(slab_info or {"built": False},
+                                          used={"mixed": opr.slab_use("mixed") if slab_info and slab_info.get("built") else 0,
+                                                "fp64": opr.slab_use("fp64") if slab_info and slab_info.get("built") else 0},
+                                          use_codes="0 none, 1 slab product, 2 slab product with cache hints"),
                        "setup_s": t_space, "search_directory": dir_stats, "parent_map": map_info},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_src},
@@ -921,7 +932,11 @@ def main():
     ap.add_argument("--uniform", action="store_true", help="with --tiling: warp-uniform pair steps (4 or 8 targets)")
     ap.add_argument("--prefetch", type=int, default=0, help="with --tiling: x prefetch distance of the target-table product")
     ap.add_argument("--no-table", action="store_true", help="no target tables (look every target up per product)")
-    ap.add_argument("--slab-mb", type=float, default=54.0,
+    ap.add_argument("--keep-targets", action="store_true",
+                    help="keep the target table when both precisions read the slab table")
+    ap.add_argument("--slab-hints", action="store_true",
+                    help="with --tiling: the slab product's cache-hint variant")
+    ap.add_argument("--slab-mb", type=float, default=112.0,
                     help="column slabs of this many MB of complex64 x for sectors whose x exceeds L2 (0: none)")
     ap.add_argument("--no-pair", action="store_true", help="test every term per row instead of the pair-flip schedule")
     ap.add_argument("--no-cpu-baseline", action="store_true")

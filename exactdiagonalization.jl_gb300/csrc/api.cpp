@@ -213,9 +213,11 @@ struct edgpu_op_s {
         std::vector<double> amp_unit;       // per amplitude id: unit amplitude (re, im)
         std::vector<int> divs;              // orbit sizes by orbit-size index
         DevBuf<float> lut;                  // coefficients by id: float, or (re, im) when !lut_real
+        DevBuf<double> lut64;               // the same in FP64
         int lut_real = 1;
     } slab;
     int slab_use[2] = {0, 0};         // [precision]: products read the slab table (chosen by the autotuner)
+    int slab_hint[2] = {0, 0};        // [precision]: the slab product's cache hints (chosen by the autotuner)
     // the optional tables change: cached graphs (this handle's host-buffer graphs, and batches, which
     // compare gen) must not replay launches that read the old ones
     void drop_host_graphs() {
@@ -229,6 +231,7 @@ struct edgpu_op_s {
         if (slab.counts) cudaFree(slab.counts);
         if (slab.off) cudaFree(slab.off);
         slab.lut.release();
+        slab.lut64.release();
         slab = Slab();
         slab_use[0] = slab_use[1] = 0;
     }
@@ -921,8 +924,8 @@ void invalidate_blobs(edgpu_op_s* op) {
             }
 }
 
-// Coefficient table of the slab product for the current coupling values (mixed precision), written
-// into the table's existing buffer: id = ((amplitude id x den + character index) x nd + orbit-size
+// Coefficient tables of the slab product (FP32 and FP64) for the current coupling values, written
+// into the tables' existing buffers: id = ((amplitude id x den + character index) x nd + orbit-size
 // index of the row) x nd + orbit-size index of the column, coefficient = J_c u_a chi sqrt(|O_c| / |O_r|)
 // as the one-pass product forms it (hx_bond.cuh), here in FP64 and rounded once.
 void slab_refresh_lut(edgpu_op_s* op) {
@@ -933,6 +936,7 @@ void slab_refresh_lut(edgpu_op_s* op) {
     for (int a = 0; a < na && real; ++a)
         if (S.amp_unit[2 * a + 1] != 0.0) real = false;
     std::vector<float> h((size_t)S.n_ids * 2, 0.f);
+    std::vector<double> h64((size_t)S.n_ids * 2, 0.0);
     for (int id = 0; id < S.n_ids; ++id) {
         int rest = id;
         const int sxc = rest % S.nd;
@@ -948,14 +952,20 @@ void slab_refresh_lut(edgpu_op_s* op) {
         const double cr = std::cos(ang), ci = std::sin(ang);
         const double f = std::sqrt((double)S.divs[sxc] / (double)S.divs[sxr]);
         const double re = (ur * cr - ui * ci) * f, im = (ur * ci + ui * cr) * f;
-        if (real) h[id] = (float)re;
-        else {
+        if (real) {
+            h[id] = (float)re;
+            h64[id] = re;
+        } else {
             h[2 * (size_t)id] = (float)re;
             h[2 * (size_t)id + 1] = (float)im;
+            h64[2 * (size_t)id] = re;
+            h64[2 * (size_t)id + 1] = im;
         }
     }
     S.lut_real = real ? 1 : 0;
     EDGPU_CUDA(cudaMemcpy(S.lut.p, h.data(), (size_t)S.n_ids * (real ? 1 : 2) * sizeof(float), cudaMemcpyHostToDevice));
+    EDGPU_CUDA(cudaMemcpy(S.lut64.p, h64.data(), (size_t)S.n_ids * (real ? 1 : 2) * sizeof(double),
+                          cudaMemcpyHostToDevice));
 }
 
 // New coupling values: every table built so far is rewritten in place (same layout, same device
@@ -995,6 +1005,12 @@ void set_map_params(HxParams& p, const Space& sp) {
     p.rank_split = sp.rank_split;
 }
 
+// Whether a product launch (mode 0 = product) goes through the column-slab table.
+bool slab_active(const edgpu_op_s* op, int prec, int dir, int mode, int rows) {
+    return mode == 0 && dir == 0 && op->slab.tab && op->slab_use[prec] && op->pair_allowed && op->pair_use[prec] &&
+           rows < 0;
+}
+
 // Shared memory of the pair-flip gradient kernel's per-thread coupling accumulators (the product's
 // real type: FP32 in mixed precision, FP64 in FP64).
 static size_t pair_grad_acc_bytes(const edgpu_op_s* op, int prec) {
@@ -1031,8 +1047,7 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
         p.map_direct = sp.map_direct;
         if (rows > 0) rows = -1;
     }
-    if (mode == 0 && dir == 0 && prec == EDGPU_MIXED && op->slab.tab && op->slab_use[prec] && op->pair_allowed &&
-        op->pair_use[prec] && rows < 0) {
+    if (slab_active(op, prec, dir, mode, rows)) {
         // the column-slab table: one launch per slab (hxslab.cu); the last writes complex128 to
         // y_c128 when given
         const auto& S = op->slab;
@@ -1040,7 +1055,7 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
         r.x = x;
         r.y = y;
         r.diag = B.d_diag;
-        r.lut = S.lut.p;
+        r.lut = prec == EDGPU_FP64 ? (const void*)S.lut64.p : (const void*)S.lut.p;
         r.n_lut = S.n_ids;
         r.lut_real = S.lut_real;
         r.n_rows = p.n_rows;
@@ -1050,11 +1065,12 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
         r.y_c128 = y_c128;
         r.acc_c128 = acc_c128;
         r.accumulate = y_c128 ? 0 : accumulate;
+        r.hints = op->slab_hint[prec];
         for (int q = 0; q < S.n_pass; ++q) {
             r.cnt = S.counts + (size_t)q * p.n_rows;
             r.off = S.off + (size_t)q * r.n_tiles;
             r.tab = S.tab + S.base[q];
-            r.xs = (const float2*)x + (size_t)q * S.wc;
+            r.xs = (const char*)x + (size_t)q * S.wc * (prec == EDGPU_FP64 ? 16 : 8);
             r.first = q == 0;
             r.last = q == S.n_pass - 1;
             hx_slab_launch(prec, r, st);
@@ -2259,13 +2275,14 @@ int edgpu_op_build_slabs(edgpu_op oh, int64_t slab_bytes, int64_t max_bytes, int
         S.colbits = colbits;
         S.n_ids = (int)n_ids;
         S.lut.ensure((size_t)n_ids * 2);
+        S.lut64.ensure((size_t)n_ids * 2);
         slab_refresh_lut(op);
     } catch (...) {
         cudaStreamSynchronize(st);
         op->free_slabs();
         throw;
     }
-    op->slab_use[EDGPU_MIXED] = 1;
+    op->slab_use[EDGPU_MIXED] = op->slab_use[EDGPU_FP64] = 1;
     if (built) *built = 1;
     API_END
 }
@@ -2295,11 +2312,13 @@ int edgpu_op_slab_use(edgpu_op oh, int32_t precision, int32_t use, int32_t* curr
     edgpu_op_s* op = as_op(oh);
     OpLock lk_(op->hs.mu);
     check_prec(precision);
-    require(use >= -1 && use <= 1, EDGPU_ERR_ARG, "use must be -1 (query), 0 or 1");
-    require(use != 1 || (op->slab.tab && precision == EDGPU_MIXED), EDGPU_ERR_STATE,
-            "no slab table (edgpu_op_build_slabs), or not mixed precision");
-    if (use >= 0) op->slab_use[precision] = use;
-    if (current) *current = op->slab_use[precision];
+    require(use >= -1 && use <= 2, EDGPU_ERR_ARG, "use must be -1 (query), 0, 1 or 2");
+    require(use <= 0 || op->slab.tab, EDGPU_ERR_STATE, "no slab table (edgpu_op_build_slabs)");
+    if (use >= 0) {
+        op->slab_use[precision] = use > 0 ? 1 : 0;
+        op->slab_hint[precision] = use == 2 ? 1 : 0;
+    }
+    if (current) *current = op->slab_use[precision] ? 1 + op->slab_hint[precision] : 0;
     API_END
 }
 
@@ -2375,13 +2394,14 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     // (and the caller allows it), that schedule with 2 or 4 targets per step (4 with a map or a
     // target table) and 1, 2 or 4 lanes per row, and its target-table flavour (one lane per row).
     // With a slab table (mixed precision), also its multi-pass product.
-    struct Cand { int pair, nt, table, rows, pf, uni, slab = 0; };
+    struct Cand { int pair, nt, table, rows, pf, uni, slab = 0, hint = 0; };
     std::vector<Cand> cands;
     build_blob(op, precision, 0, 0);
     const bool pair_ok = op->blob[precision][0][0].tmpl.bond_ncls > 0 && op->pair_allowed;
     const bool mapped = op->space->d_map != nullptr;
     if (pair_ok) {
-        if (op->slab.tab && precision == EDGPU_MIXED) cands.push_back({1, 4, 1, -1, 0, 0, 1});
+        if (op->slab.tab)
+            for (int hint : {0, 1}) cands.push_back({1, 4, 1, -1, 0, 0, 1, hint});
         if (op->d_tab) {
             for (int nt : {8, 4, 2})
                 for (int pf : {0, 4, 64}) cands.push_back({1, nt, 1, -1, pf, 0});
@@ -2397,7 +2417,7 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     Cand best = cands.front();
     double best_ms = 1e30;
     const int keep_pair = op->pair_use[precision], keep_nt = op->pair_nt[precision], keep_tab = op->tab_use[precision];
-    const int keep_uni = op->tab_uni[precision], keep_slab = op->slab_use[precision];
+    const int keep_uni = op->tab_uni[precision], keep_slab = op->slab_use[precision], keep_hint = op->slab_hint[precision];
     if (n > 0) {
         const size_t vs = precision == EDGPU_FP64 ? 16 : 8;
         void *x = nullptr, *y = nullptr;
@@ -2415,6 +2435,7 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
                 op->tab_pf[precision] = c.pf;
                 op->tab_uni[precision] = c.uni;
                 op->slab_use[precision] = c.slab;
+                op->slab_hint[precision] = c.hint;
                 launch_product(op, precision, 0, 0, x, y, 0, nullptr, nullptr, op->hs.stream(), nullptr, c.rows);
                 // one timed launch, then two back-to-back bursts of enough launches to cover about 2 ms
                 // (1 to 50 per burst), as a solver issues them; the faster burst's time per launch
@@ -2447,6 +2468,7 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
             op->tab_use[precision] = keep_tab;
             op->tab_uni[precision] = keep_uni;
             op->slab_use[precision] = keep_slab;
+            op->slab_hint[precision] = keep_hint;
             cudaFree(x);
             cudaFree(y);
             cudaEventDestroy(e0);
@@ -2464,6 +2486,7 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     op->tab_pf[precision] = best.pf;
     op->tab_uni[precision] = best.uni;
     op->slab_use[precision] = best.slab;
+    op->slab_hint[precision] = best.hint;
     op->tuned_rows[precision] = best.rows;
     if (rows_per_tile_out) *rows_per_tile_out = best.rows;
     if (best_ms_out) *best_ms_out = best_ms;
@@ -2643,7 +2666,7 @@ static void host_product(edgpu_op_s* op, int prec, int dir, const double* x, dou
                                           (const void*)(intptr_t)(op->pair_allowed + 2 * op->pair_use[prec] +
                                                                   4 * op->pair_nt[prec] + 64 * op->tab_use[prec] +
                                                                   128 * op->tab_uni[prec] + 256 * op->slab_use[prec] +
-                                                                  512 * op->tab_pf[prec])};
+                                                                  512 * op->tab_pf[prec] + (1 << 20) * op->slab_hint[prec])};
     auto it = op->host_graphs.find(key);
     if (it == op->host_graphs.end()) {
         cudaStream_t cap = nullptr;
@@ -2699,6 +2722,15 @@ static void host_product_issue(edgpu_op_s* op, int prec, int dir, const double* 
         double* yd = (double*)device_alias(y);
         if (yd) {
             EDGPU_CUDA(cudaMemcpyAsync(op->x64.p, x, n * 16, cudaMemcpyHostToDevice, st));
+            const int rows = op->tuned_rows[prec] ? op->tuned_rows[prec] : -1;
+            if (slab_active(op, prec, dir, 0, (rows > 0 && op->space->d_map) ? -1 : rows)) {
+                // the slab passes add into the device buffer; the last writes the host buffer
+                bool wrote = false;
+                launch_product(op, prec, dir, 0, op->x64.p, op->y64.p, 0, nullptr, nullptr, st, nullptr, 0, yd,
+                               accumulate, &wrote);
+                require(wrote, EDGPU_ERR_STATE, "internal: slab product did not write the host buffer");
+                return;
+            }
             launch_product(op, prec, dir, 0, op->x64.p, yd, accumulate, nullptr, nullptr, st);
             return;
         }

@@ -369,11 +369,12 @@ struct SlabRun {
     void* y;
     const void* diag;
     const void* lut;                // coefficients by id: V, or R when lut_real
-    void* y_c128;                   // mixed precision, last pass: complex128 output instead of y
+    void* y_c128;                   // last pass: complex128 output instead of y (host buffers)
     long long n_rows, n_tiles;
     unsigned colmask;
     int colbits, n_lut, lut_real;
     int first, last, accumulate, acc_c128;
+    int hints;                      // 1: gathers cached in L2 only, streamed data evict-first
 };
 // Count pass (1) or fill pass (2) of the slab table from the target table.  p: the table-flavour
 // pair-flip template (tab, tile_off set; lpr = 1); smem: its image plus s.o_ctr's counters.

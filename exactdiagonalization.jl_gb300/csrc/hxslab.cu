@@ -1,4 +1,4 @@
-// Column-slab table of the pair-flip schedule and its multi-pass product.
+// Column-slab table of the pair-flip schedule and its multi-pass product (both precisions).
 //
 // On a large sector the target-table product (hx_bond.cuh, GK_TABLE) gathers x at random: with x
 // many times the size of L2, nearly every gather is a DRAM sector of 32 bytes for 8 bytes of x.  The
@@ -172,69 +172,90 @@ __global__ void k_slab_scan_out(const unsigned* ts, long long n_tiles, const uns
     }
 }
 
+// Loads and stores with or without cache hints (CH): the gathers of x cached in L2 only (they have
+// no reuse in L1), the streamed count bytes, offsets and y marked evict-first, so that the slab of x
+// keeps its place in L2.
+template <bool CH, typename T>
+__device__ __forceinline__ T ld_gather(const T* p) {
+    if constexpr (CH) return __ldcg(p);
+    else return *p;
+}
+template <bool CH, typename T>
+__device__ __forceinline__ T ld_stream(const T* p) {
+    if constexpr (CH) return __ldcs(p);
+    else return *p;
+}
+template <bool CH, typename T>
+__device__ __forceinline__ void st_stream(T* p, T v) {
+    if constexpr (CH) __stcs(p, v);
+    else *p = v;
+}
+
 // One pass of the product: a warp per tile of 32 rows, one lane per row; the lane adds its row's
 // entries of this pass (NT per step, loads then gathers), then adds the sum to y (the first pass
-// writes y = diag x + sum; the last pass may write complex128 instead).
-template <bool REAL, int NT>
+// writes y = diag x + sum; the last pass may write complex128 to y_c128 instead).
+template <int PREC, bool REAL, int NT, bool CH>
 __global__ void __launch_bounds__(HX_THREADS) hx_slab_kernel(const SlabRun r) {
+    typedef typename Cx<PREC>::V V;
+    typedef typename Cx<PREC>::R R;
     extern __shared__ __align__(16) unsigned char sm[];
     pdl_launch_dependents();
     if (REAL) {
-        const float* src = (const float*)r.lut;
-        for (int i = threadIdx.x; i < r.n_lut; i += blockDim.x) ((float*)sm)[i] = src[i];
+        const R* src = (const R*)r.lut;
+        for (int i = threadIdx.x; i < r.n_lut; i += blockDim.x) ((R*)sm)[i] = src[i];
     } else {
-        const float2* src = (const float2*)r.lut;
-        for (int i = threadIdx.x; i < r.n_lut; i += blockDim.x) ((float2*)sm)[i] = src[i];
+        const V* src = (const V*)r.lut;
+        for (int i = threadIdx.x; i < r.n_lut; i += blockDim.x) ((V*)sm)[i] = src[i];
     }
     __syncthreads();
     pdl_wait();
-    const float* lr = (const float*)sm;
-    const float2* lv = (const float2*)sm;
-    const float2* __restrict__ xs = (const float2*)r.xs;
+    const R* lr = (const R*)sm;
+    const V* lv = (const V*)sm;
+    const V* __restrict__ xs = (const V*)r.xs;
     const unsigned* __restrict__ tab = r.tab;
-    float2* y = (float2*)r.y;
+    V* y = (V*)r.y;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
     const bool to_c128 = r.last && r.y_c128 != nullptr;
     for (long long tile = (long long)blockIdx.x * wpb + warp; tile < r.n_tiles; tile += (long long)gridDim.x * wpb) {
         const long long row = tile * 32 + lane;
         const bool act = row < r.n_rows;
-        const int cnt = act ? (int)r.cnt[row] : 0;
+        const int cnt = act ? (int)ld_stream<CH>(r.cnt + row) : 0;
         int incl = cnt;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
             const int u = __shfl_up_sync(0xffffffffu, incl, d);
             if (lane >= d) incl += u;
         }
-        const long long start = (long long)r.off[tile] + (incl - cnt);
-        float2 acc = make_float2(0.f, 0.f);
+        const long long start = (long long)ld_stream<CH>(r.off + tile) + (incl - cnt);
+        V acc = czero<V>();
         for (int j = 0; __any_sync(0xffffffffu, j < cnt); j += NT) {
             unsigned e[NT];
 #pragma unroll
             for (int h = 0; h < NT; ++h) e[h] = (j + h < cnt) ? __ldg(tab + start + j + h) : 0u;
-            float2 xv[NT];
+            V xv[NT];
 #pragma unroll
-            for (int h = 0; h < NT; ++h) xv[h] = (j + h < cnt) ? xs[e[h] & r.colmask] : make_float2(0.f, 0.f);
+            for (int h = 0; h < NT; ++h) xv[h] = (j + h < cnt) ? ld_gather<CH>(xs + (e[h] & r.colmask)) : czero<V>();
 #pragma unroll
             for (int h = 0; h < NT; ++h) {
                 if (j + h >= cnt) continue;
                 const unsigned id = e[h] >> r.colbits;
                 if (REAL) {
-                    const float f = lr[id];
-                    acc.x = __fmaf_rn(f, xv[h].x, acc.x);
-                    acc.y = __fmaf_rn(f, xv[h].y, acc.y);
+                    const R f = lr[id];
+                    acc.x = fma_r(f, xv[h].x, acc.x);
+                    acc.y = fma_r(f, xv[h].y, acc.y);
                 } else {
                     acc = cadd(acc, cmul(lv[id], xv[h]));
                 }
             }
         }
         if (!act) continue;
-        float2 t;
+        V t;
         if (r.first) {
-            t = cadd(cmul(((const float2*)r.diag)[row], ((const float2*)r.x)[row]), acc);
-            if (r.accumulate) t = cadd(y[row], t);
+            t = cadd(cmul(ld_stream<CH>((const V*)r.diag + row), ld_stream<CH>((const V*)r.x + row)), acc);
+            if (r.accumulate) t = cadd(ld_stream<CH>(y + row), t);
         } else {
             if (cnt == 0 && !to_c128) continue;   // nothing to add to this row
-            t = cadd(y[row], acc);
+            t = cadd(ld_stream<CH>(y + row), acc);
         }
         if (to_c128) {
             double2 o = make_double2((double)t.x, (double)t.y);
@@ -246,7 +267,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_slab_kernel(const SlabRun r) {
             }
             yc[row] = o;
         } else {
-            y[row] = t;
+            st_stream<CH>(y + row, t);
         }
     }
 }
@@ -330,16 +351,26 @@ void hx_slab_scan(const unsigned* tile_sum, unsigned* off, int n_pass, long long
     if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("slab scan: ") + cudaGetErrorString(e));
 }
 
-void hx_slab_launch(int prec, const SlabRun& r, cudaStream_t st) {
-    if (prec != 1) throw Error(EDGPU_ERR_ARG, "the slab product is mixed precision only");
-    if (r.n_tiles == 0) return;
-    const size_t smem = (size_t)r.n_lut * (r.lut_real ? 4 : 8);
+template <int PREC, bool CH>
+void slab_launch_t(const SlabRun& r, size_t smem, cudaStream_t st) {
     if (r.lut_real) {
-        auto k = hx_slab_kernel<true, 4>;
+        auto k = hx_slab_kernel<PREC, true, 4, CH>;
         slab_pdl_launch(k, r, slab_blocks(k, smem, r.n_tiles), smem, st);
     } else {
-        auto k = hx_slab_kernel<false, 4>;
+        auto k = hx_slab_kernel<PREC, false, 4, CH>;
         slab_pdl_launch(k, r, slab_blocks(k, smem, r.n_tiles), smem, st);
+    }
+}
+
+void hx_slab_launch(int prec, const SlabRun& r, cudaStream_t st) {
+    if (r.n_tiles == 0) return;
+    const size_t smem = (size_t)r.n_lut * (r.lut_real ? 1 : 2) * (prec == 0 ? 8 : 4);
+    if (prec == 0) {
+        if (r.hints) slab_launch_t<0, true>(r, smem, st);
+        else slab_launch_t<0, false>(r, smem, st);
+    } else {
+        if (r.hints) slab_launch_t<1, true>(r, smem, st);
+        else slab_launch_t<1, false>(r, smem, st);
     }
 }
 

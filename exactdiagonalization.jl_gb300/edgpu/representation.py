@@ -685,12 +685,13 @@ class OperatorRepresentation:
         check(lib().edgpu_op_slabs_info(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
         return int(a.value), int(b.value), int(c.value)
 
-    def slab_use(self, precision="mixed", use: Optional[bool] = None) -> bool:
-        """Whether products read the slab table; sets it when use is given."""
+    def slab_use(self, precision="mixed", use=None) -> int:
+        """Whether products read the slab table: 0 (no), 1 (yes), 2 (yes, with cache hints); sets it
+        when use is given (False/True or 0, 1, 2)."""
         cur = ctypes.c_int32()
-        check(lib().edgpu_op_slab_use(self._h, _prec(precision), -1 if use is None else int(bool(use)),
+        check(lib().edgpu_op_slab_use(self._h, _prec(precision), -1 if use is None else int(use),
                                       ctypes.byref(cur)))
-        return bool(cur.value)
+        return int(cur.value)
 
     def pair_classes(self):
         """(bond classes, rotation components) of the pair-flip schedule; (0, 0) when it does not apply."""

@@ -233,8 +233,8 @@ int edgpu_op_build_adjoint_targets(edgpu_op op, int64_t max_bytes, int32_t* buil
 int edgpu_op_free_adjoint_targets(edgpu_op op);
 /* Entries of the target table and bytes per entry; 0 and 0 without a table. */
 int edgpu_op_targets_info(edgpu_op op, int64_t* entries, int32_t* entry_bytes);
-/* Column-slab table, built from the target table (which must exist) for mixed-precision products on
- * large sectors.  The columns are cut into slabs of slab_bytes of complex64 x (at most 64 slabs);
+/* Column-slab table, built from the target table (which must exist) for products on large sectors
+ * (both precisions).  The columns are cut into slabs of slab_bytes of complex64 x (at most 64 slabs);
  * the product then runs one pass per slab, gathering only from that slab (sized to stay in L2) and
  * adding its share to y, instead of gathering at random from all of x.  Results equal the one-pass
  * product up to the order of the additions (the passes are added in order: reproducible run to
@@ -246,9 +246,11 @@ int edgpu_op_build_slabs(edgpu_op op, int64_t slab_bytes, int64_t max_bytes, int
 int edgpu_op_free_slabs(edgpu_op op);
 /* Slabs (passes), columns per slab and entries of the slab table; zeros without one. */
 int edgpu_op_slabs_info(edgpu_op op, int32_t* passes, int64_t* columns_per_slab, int64_t* entries);
-/* Whether mixed-precision products read the slab table: use = 1 or 0 sets it (1 needs the table:
- * EDGPU_ERR_STATE otherwise), -1 only queries; *current = the setting.  Building the table sets it;
- * the autotuner times it against the one-pass schedules. */
+/* Whether products of this precision read the slab table: use = 0 (no), 1 (yes) or 2 (yes, with
+ * cache hints: the gathers of x cached in L2 only, the streamed counts, offsets and y evict-first)
+ * sets it (1 and 2 need the table: EDGPU_ERR_STATE otherwise), -1 only queries; *current = the
+ * setting.  Building the table sets 1 for both precisions; the autotuner times 1 and 2 against the
+ * one-pass schedules. */
 int edgpu_op_slab_use(edgpu_op op, int32_t precision, int32_t use, int32_t* current);
 /* Sparse matrix of the representation, assembled on the device in FP64: rows sorted by column,
  * entries of equal column summed, entries with |value| < tol dropped (tol: the reference's

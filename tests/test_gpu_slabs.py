@@ -4,7 +4,7 @@ Small slabs force several passes on sectors the oracle handles in seconds: the p
 oracle's reduced product within 1e-5 (mixed precision) and the one-pass target-table product within
 1e-6, be reproducible bit for bit, accumulate (y += H x), write complex128 host buffers, follow new
 coupling values, and cover real and complex coefficients (momentum 0 and k != 0), a torus and a
-chain."""
+chain; the FP64 product through the same table must match the oracle within 1e-12."""
 import numpy as np
 import pytest
 
@@ -70,6 +70,13 @@ def test_slab_product_chain(L, k, coupled):
     E.mul_(y2, opr, xd, precision="mixed")
     torch.cuda.synchronize()
     assert torch.equal(y, y2)
+    # with cache hints: the same arithmetic, the same bits
+    assert opr.slab_use("mixed", 2) == 2
+    y2.fill_(float("nan"))
+    E.mul_(y2, opr, xd, precision="mixed")
+    torch.cuda.synchronize()
+    assert torch.equal(y, y2)
+    assert opr.slab_use("mixed", 1) == 1
     yn = y.cpu().numpy().astype(np.complex128)
     assert relerr(yn, want) < 1e-5
     assert relerr(yn, y_tab.cpu().numpy().astype(np.complex128)) < 1e-6
@@ -85,10 +92,25 @@ def test_slab_product_chain(L, k, coupled):
     yh2 = yh.copy()
     E.apply_(yh2, opr, x, precision="mixed")
     assert relerr(yh2, 2 * want) < 1e-5
-    # FP64 products do not read the slab table
+    # FP64 products read it too: device vectors, pageable and pinned host buffers (the last pass
+    # writes the pinned buffer), y += H x
+    assert opr.slab_use("fp64")
+    x64 = torch.from_numpy(x).cuda()
+    yd64 = torch.empty_like(x64)
+    E.mul_(yd64, opr, x64, precision="fp64")
+    torch.cuda.synchronize()
+    assert relerr(yd64.cpu().numpy(), want) < 1e-12
     yf = np.zeros(N, dtype=np.complex128)
     E.mul_(yf, opr, x, precision="fp64")
     assert relerr(yf, want) < 1e-12
+    xp = torch.from_numpy(x).pin_memory()
+    yp = torch.zeros(N, dtype=torch.complex128).pin_memory()
+    for prec, tol in (("fp64", 1e-12), ("mixed", 1e-5)):
+        yp.zero_()
+        E.mul_(yp.numpy(), opr, xp.numpy(), precision=prec)
+        assert relerr(yp.numpy(), want) < tol
+        E.apply_(yp.numpy(), opr, xp.numpy(), precision=prec)
+        assert relerr(yp.numpy(), 2 * want) < tol
     if coupled:
         m, r, c, a, ids, J = extra
         J2 = J[::-1] * 1.3
@@ -98,6 +120,7 @@ def test_slab_product_chain(L, k, coupled):
         assert relerr(y4.cpu().numpy().astype(np.complex128), O.apply_rows(red, terms2, x)) < 1e-5
     # switched off: the one-pass product again, bit for bit
     assert not opr.slab_use("mixed", False)
+    assert not opr.slab_use("fp64", False)
     if not coupled:
         _, y5 = _products(E, opr, x)
         assert torch.equal(y5, y_tab)
@@ -137,8 +160,12 @@ def test_slab_product_torus_j1j2():
         assert opr.build_slabs(slab_bytes=1024 * 8, max_bytes=1 << 30)
         assert opr.slabs_info[0] >= 3
         x = O.complex_gaussian(N, 9)
+        want = O.apply_rows(red, terms, x)
         _, y = _products(E, opr, x)
-        assert relerr(y.cpu().numpy().astype(np.complex128), O.apply_rows(red, terms, x)) < 1e-5
+        assert relerr(y.cpu().numpy().astype(np.complex128), want) < 1e-5
+        y64 = np.zeros(N, dtype=np.complex128)
+        E.mul_(y64, opr, x, precision="fp64")
+        assert relerr(y64, want) < 1e-12
 
 
 def test_slab_build_refusals():
