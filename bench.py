@@ -680,7 +680,10 @@ def run_gpu(args, wl):
                                           use_codes="0 none, 1 slab product, 2 slab product with cache hints"),
                        "setup_s": t_space, "search_directory": dir_stats, "parent_map": map_info},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "peak_source": peak_src},
+                         "traffic": traffic, "peak_source": peak_src,
+                         "scope": f"one H*x ({launches_per_step} launch{'es' if launches_per_step > 1 else ''}): "
+                                  "model bytes over its device time; traffic = DRAM bytes of one H*x from the "
+                                  "committed ncu summary"},
             "cpu_baseline": cpu, "e2e": e2e, "e2e_more": e2e_more, "host_link": host_link,
             "gpu_launches": args.steps * launches_per_step, "clocks": clk,
             "fp64": {"value": value64, "unit": "GB/s", "ms_per_step": ms64 / fp64_steps, "frac": value64 / peak},
@@ -824,7 +827,9 @@ def run_gpu_batch(args, wl):
                                                                          f"per-sector launches on {batch.launch('mixed')} stream(s)"),
                        "per_sector_launches_ms_per_step": per_sector_ms},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": profiled_traffic(args.workload), "peak_source": peak_src},
+                         "traffic": profiled_traffic(args.workload), "peak_source": peak_src,
+                         "scope": "one batched H*x over all sectors; traffic = 30 x the DRAM bytes of one sector's "
+                                  "product launch (ncu capture of the k=(1,0) sector, cold cache)"},
             "cpu_baseline": None if args.no_cpu_baseline else
             {"value": None, "unit": "GB/s", "cores": None, "kind": "port",
              "sample": "not run: the reference builds a 155M-state parent basis and 3.7 GB of mapping tables per sector"},
