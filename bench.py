@@ -496,7 +496,7 @@ def run_gpu(args, wl):
             opr.set_tiling(prec, args.tiling)
             opr.table_prefetch(prec, args.prefetch)
             if slab_info and slab_info.get("built"):
-                opr.slab_use(prec, 2 if args.slab_hints else 1)
+                opr.slab_use(prec, args.slab_mode)
         tune_mixed = tune_fp64 = (args.tiling, None)
     else:
         tune_mixed = opr.autotune("mixed")
@@ -939,8 +939,8 @@ def main():
     ap.add_argument("--no-table", action="store_true", help="no target tables (look every target up per product)")
     ap.add_argument("--keep-targets", action="store_true",
                     help="keep the target table when both precisions read the slab table")
-    ap.add_argument("--slab-hints", action="store_true",
-                    help="with --tiling: the slab product's cache-hint variant")
+    ap.add_argument("--slab-mode", type=int, default=1, choices=[1, 2],
+                    help="with --tiling: the slab product's variant (1 plain, 2 with cache hints)")
     ap.add_argument("--slab-mb", type=float, default=112.0,
                     help="column slabs of this many MB of complex64 x for sectors whose x exceeds L2 (0: none)")
     ap.add_argument("--no-pair", action="store_true", help="test every term per row instead of the pair-flip schedule")

@@ -2316,7 +2316,7 @@ int edgpu_op_slab_use(edgpu_op oh, int32_t precision, int32_t use, int32_t* curr
     require(use <= 0 || op->slab.tab, EDGPU_ERR_STATE, "no slab table (edgpu_op_build_slabs)");
     if (use >= 0) {
         op->slab_use[precision] = use > 0 ? 1 : 0;
-        op->slab_hint[precision] = use == 2 ? 1 : 0;
+        op->slab_hint[precision] = use > 0 ? use - 1 : 0;
     }
     if (current) *current = op->slab_use[precision] ? 1 + op->slab_hint[precision] : 0;
     API_END

@@ -172,6 +172,16 @@ __global__ void k_slab_scan_out(const unsigned* ts, long long n_tiles, const uns
     }
 }
 
+// acc += c x with explicit fused multiply-adds (the same roundings in every kernel of this file)
+template <typename V>
+__device__ __forceinline__ V cfma_acc(V acc, V c, V x) {
+    acc.x = fma_r(c.x, x.x, acc.x);
+    acc.x = fma_r(-c.y, x.y, acc.x);
+    acc.y = fma_r(c.x, x.y, acc.y);
+    acc.y = fma_r(c.y, x.x, acc.y);
+    return acc;
+}
+
 // Loads and stores with or without cache hints (CH): the gathers of x cached in L2 only (they have
 // no reuse in L1), the streamed count bytes, offsets and y marked evict-first, so that the slab of x
 // keeps its place in L2.
@@ -244,14 +254,14 @@ __global__ void __launch_bounds__(HX_THREADS) hx_slab_kernel(const SlabRun r) {
                     acc.x = fma_r(f, xv[h].x, acc.x);
                     acc.y = fma_r(f, xv[h].y, acc.y);
                 } else {
-                    acc = cadd(acc, cmul(lv[id], xv[h]));
+                    acc = cfma_acc(acc, lv[id], xv[h]);
                 }
             }
         }
         if (!act) continue;
         V t;
         if (r.first) {
-            t = cadd(cmul(ld_stream<CH>((const V*)r.diag + row), ld_stream<CH>((const V*)r.x + row)), acc);
+            t = cfma_acc(acc, ld_stream<CH>((const V*)r.diag + row), ld_stream<CH>((const V*)r.x + row));
             if (r.accumulate) t = cadd(ld_stream<CH>(y + row), t);
         } else {
             if (cnt == 0 && !to_c128) continue;   // nothing to add to this row

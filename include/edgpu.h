@@ -249,8 +249,8 @@ int edgpu_op_slabs_info(edgpu_op op, int32_t* passes, int64_t* columns_per_slab,
 /* Whether products of this precision read the slab table: use = 0 (no), 1 (yes) or 2 (yes, with
  * cache hints: the gathers of x cached in L2 only, the streamed counts, offsets and y evict-first)
  * sets it (1 and 2 need the table: EDGPU_ERR_STATE otherwise), -1 only queries; *current = the
- * setting.  Building the table sets 1 for both precisions; the autotuner times 1 and 2 against the
- * one-pass schedules. */
+ * setting.  1 and 2 give the same results bit for bit.  Building the table sets 1 for both
+ * precisions; the autotuner times 1 and 2 against the one-pass schedules. */
 int edgpu_op_slab_use(edgpu_op op, int32_t precision, int32_t use, int32_t* current);
 /* Sparse matrix of the representation, assembled on the device in FP64: rows sorted by column,
  * entries of equal column summed, entries with |value| < tol dropped (tol: the reference's

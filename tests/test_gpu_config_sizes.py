@@ -16,7 +16,8 @@ target table, autotuned schedule), and checked against the oracle:
   sector (252,091,362 rows), whose parent-sized tables do not fit in host memory: the representative
   table against Burnside's count, sortedness and orbit minimality of sampled rows, completeness for
   sampled parent states, and sampled rows of the product against the oracle's orbit-by-orbit
-  evaluation of the same row formula (oracle.OrbitTables); the 6x6 ground-state energy against the
+  evaluation of the same row formula (oracle.OrbitTables), through the target table and through the
+  column-slab table; the 6x6 ground-state energy against the
   published 36-site value.
 
 Tolerances: FP64 products 1e-12 relative (to the largest |y| entry of the compared set), mixed
@@ -257,7 +258,7 @@ def test_chain28_random_bond_gradients_full_size(E):
 
 # ---- 6x5 triangular k=(1,0) and 6x6 J1-J2 k=(0,0): sampled rows ------------------------------------
 
-def _torus_sampled(E, workload, momentum, n_rows_sample, seed):
+def _torus_sampled(E, workload, momentum, n_rows_sample, seed, slab_mb=None):
     import torch
     from edgpu import lattice
     bench = _bench()
@@ -299,19 +300,34 @@ def _torus_sampled(E, workload, momentum, n_rows_sample, seed):
     assert (st == 0).all()
     assert _rel(y64[sample], vals) < 1e-12
     assert _rel(y32[sample], vals) < 1e-5
+    if slab_mb is not None:
+        # the column-slab product (several passes) in both precisions: the sampled rows against the
+        # oracle, the whole vectors against the one-pass target-table product; then the target table
+        # is freed (the products read the slab table from here on)
+        free, _ = torch.cuda.mem_get_info()
+        assert opr.build_slabs(slab_bytes=int(slab_mb * (1 << 20)), max_bytes=int(0.8 * free))
+        assert opr.slabs_info[0] >= 3
+        y64s, y32s = _products(E, opr, x)
+        assert _rel(y64s[sample], vals) < 1e-12
+        assert _rel(y32s[sample], vals) < 1e-5
+        assert _rel(y64s, y64) < 1e-12
+        assert _rel(y32s, y32) < 1e-6
+        del y64s, y32s
+        opr.free_targets()
     del y64, y32
     return opr, N, x
 
 
 def test_triangular6x5_k10_sector_sampled_rows(E):
-    _torus_sampled(E, "triangular6x5_k1", (1, 0), 20000, 31)
+    # complex characters; slabs of 16 MB of x: 3 passes
+    _torus_sampled(E, "triangular6x5_k1", (1, 0), 20000, 31, slab_mb=16)
 
 
 def test_square6x6_k0_sector_sampled_rows_and_e0(E):
     """Config 5.  The ground-state energy per site of the 36-site J1-J2 model at J2/J1 = 0.5 (in units of
     J1, H = sum J S_i.S_j) is -0.50381 in H. J. Schulz, T. A. L. Ziman and D. Poilblanc, J. Phys. I
     France 6, 675 (1996) (Table of 6x6 energies); the k=(0,0), 2Sz=0 sector holds that ground state."""
-    opr, N, _ = _torus_sampled(E, "square6x6_k0", (0, 0), 10000, 37)
+    opr, N, _ = _torus_sampled(E, "square6x6_k0", (0, 0), 10000, 37, slab_mb=112)
     assert N == 252091362
     bench = _bench()
     wl = bench.WORKLOADS["square6x6_k0"]

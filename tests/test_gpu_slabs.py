@@ -70,12 +70,13 @@ def test_slab_product_chain(L, k, coupled):
     E.mul_(y2, opr, xd, precision="mixed")
     torch.cuda.synchronize()
     assert torch.equal(y, y2)
-    # with cache hints: the same arithmetic, the same bits
-    assert opr.slab_use("mixed", 2) == 2
-    y2.fill_(float("nan"))
-    E.mul_(y2, opr, xd, precision="mixed")
-    torch.cuda.synchronize()
-    assert torch.equal(y, y2)
+    # with cache hints: the same arithmetic in the same order, the same bits
+    for mode in (2,):
+        assert opr.slab_use("mixed", mode) == mode
+        y2.fill_(float("nan"))
+        E.mul_(y2, opr, xd, precision="mixed")
+        torch.cuda.synchronize()
+        assert torch.equal(y, y2), mode
     assert opr.slab_use("mixed", 1) == 1
     yn = y.cpu().numpy().astype(np.complex128)
     assert relerr(yn, want) < 1e-5
@@ -100,6 +101,13 @@ def test_slab_product_chain(L, k, coupled):
     E.mul_(yd64, opr, x64, precision="fp64")
     torch.cuda.synchronize()
     assert relerr(yd64.cpu().numpy(), want) < 1e-12
+    for mode in (2,):
+        opr.slab_use("fp64", mode)
+        yd64b = torch.full_like(x64, float("nan"))
+        E.mul_(yd64b, opr, x64, precision="fp64")
+        torch.cuda.synchronize()
+        assert torch.equal(yd64, yd64b), mode
+    opr.slab_use("fp64", 1)
     yf = np.zeros(N, dtype=np.complex128)
     E.mul_(yf, opr, x, precision="fp64")
     assert relerr(yf, want) < 1e-12
