@@ -133,6 +133,8 @@ struct Blob {
     int rows_per_tile = 32;
     void* d_diag = nullptr;  // per-row diagonal element in the blob's precision (product mode)
     size_t cap_d = 0, cap_pair = 0, cap_diag = 0;   // bytes allocated at d, d_pair, d_diag
+    void* d_lut = nullptr;   // GENERIC permutation tables in global memory (when too large for shared memory)
+    size_t cap_lut = 0;
     size_t smem_rows = 0;    // shared memory of the row-per-lane kernel (no per-warp queues)
     int max_blocks_rows = 0;
     int max_blocks_map = 0;  // resident blocks of the parent-state-map kernel (computed on first use)
@@ -151,6 +153,7 @@ struct Blob {
         if (d) cudaFree(d);
         if (d_diag) cudaFree(d_diag);
         if (d_pair) cudaFree(d_pair);
+        if (d_lut) cudaFree(d_lut);
     }
 };
 
@@ -547,7 +550,11 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     p.o_ratio = alloc(nd * nd * rsz);
     p.o_keep = alloc(keep.size() * wsz);
     p.o_keep32 = alloc(keep.size() * 4);
-    p.o_lut = alloc(lut.size() * wsz);
+    // permutation tables of a large general group stay in global memory (read through L1/L2) so
+    // that the rest of the image fits in shared memory
+    const bool lut_global = lut.size() * wsz > GENERIC_SMEM_LUT;
+    p.o_lut = lut_global ? -1 : alloc(lut.size() * wsz);
+    p.lut_g = nullptr;
     p.o_flip = alloc((g.kind == GK_GENERIC ? g.G : 0) * wsz);
     // torus row table: smallest rotation of every row value and the rotation steps reaching it
     const int rowbits = g.L1 * g.w;
@@ -769,7 +776,8 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
             memcpy(&h[p.o_rlut + v * 4], &e, 4);
         }
     }
-    for (size_t i = 0; i < lut.size(); ++i) putw(p.o_lut, i, lut[i]);
+    if (!lut_global)
+        for (size_t i = 0; i < lut.size(); ++i) putw(p.o_lut, i, lut[i]);
     if (g.kind == GK_GENERIC)
         for (int e = 0; e < g.G; ++e) putw(p.o_flip, e, e < (int)g.flips.size() ? g.flips[e] : 0ull);
     if (bc.ncls > 0) {
@@ -840,6 +848,20 @@ void build_blob(edgpu_op_s* op, int prec, int dir, int mode) {
     }
     ensure(B.d, B.cap_d, blob_bytes_t);
     EDGPU_CUDA(cudaMemcpy(B.d, h.data(), blob_bytes_t, cudaMemcpyHostToDevice));
+    if (lut_global) {
+        std::vector<unsigned char> lh(lut.size() * wsz);
+        for (size_t i = 0; i < lut.size(); ++i) {
+            if (w32) {
+                const uint32_t u = (uint32_t)lut[i];
+                memcpy(&lh[i * 4], &u, 4);
+            } else {
+                memcpy(&lh[i * 8], &lut[i], 8);
+            }
+        }
+        ensure(B.d_lut, B.cap_lut, lh.size());
+        EDGPU_CUDA(cudaMemcpy(B.d_lut, lh.data(), lh.size(), cudaMemcpyHostToDevice));
+        p.lut_g = B.d_lut;
+    }
     if (bc.ncls > 0) {
         ensure(B.d_pair, B.cap_pair, hp.size());
         EDGPU_CUDA(cudaMemcpy(B.d_pair, hp.data(), hp.size(), cudaMemcpyHostToDevice));
@@ -916,10 +938,12 @@ void invalidate_blobs(edgpu_op_s* op) {
                 if (c.d) cudaFree(c.d);
                 if (c.d_diag) cudaFree(c.d_diag);
                 if (c.d_pair) cudaFree(c.d_pair);
+                if (c.d_lut) cudaFree(c.d_lut);
                 c.d = nullptr;
                 c.d_diag = nullptr;
                 c.d_pair = nullptr;
-                c.cap_d = c.cap_pair = c.cap_diag = 0;
+                c.d_lut = nullptr;
+                c.cap_d = c.cap_pair = c.cap_diag = c.cap_lut = 0;
                 c.ready = false;
             }
 }

@@ -199,6 +199,7 @@ struct HxParams {
     DirSearch ds;                             // the search directory of the table
     const void* diag;                         // per-row diagonal element (V), product mode
     int o_ph, o_num, o_ratio, o_keep, o_lut, o_flip, o_grad;
+    const void* lut_g;                        // GENERIC permutation tables in global memory (o_lut < 0)
     int o_rlut;                               // torus row table for top-row pruning, -1 when absent
     unsigned l1inv;                           // ceil(2^16 / L1) (candidate bit -> row of the pruned torus search)
     int rlut_pair;                            // the row table holds pairs of rows (rowbits <= 6)
@@ -267,6 +268,7 @@ struct __align__(16) SectorDesc {
 constexpr int BOND_MAXC = 4;       // rotation components per bond class of the pair-flip schedule
 constexpr int BOND_MAXCLS = 24;    // bond classes at most (more: the term-matching schedule)
 
+constexpr size_t GENERIC_SMEM_LUT = 64 * 1024;   // larger GENERIC permutation tables stay in global memory
 constexpr int HX_QCAP = 128;         // per-warp target queue capacity (entries; 2 batches of 32 + 31)
 constexpr int HX_THREADS = 256;      // threads per block of the product kernel
 int hx_warp_bytes(bool w32);

@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_kernel(const HxParams p) {
     const int* num = (const int*)(sm + p.o_num);
     const R* ratio = (const R*)(sm + p.o_ratio);
     const W* keep = (const W*)(sm + p.o_keep);
-    const W* lut = (const W*)(sm + p.o_lut);
+    const W* lut = p.o_lut >= 0 ? (const W*)(sm + p.o_lut) : (const W*)p.lut_g;
     const W* flips = (const W*)(sm + p.o_flip);
     const unsigned* rlut = (const unsigned*)(sm + (p.o_rlut >= 0 ? p.o_rlut : 0));
     const unsigned* keep32 = (const unsigned*)(sm + p.o_keep32);

@@ -39,7 +39,7 @@ struct RowsTables {
         dc = (const int*)(sm + p.o_dc);
         ratio = (const R*)(sm + p.o_ratio);
         keep = (const W*)(sm + p.o_keep);
-        lut = (const W*)(sm + p.o_lut);
+        lut = p.o_lut >= 0 ? (const W*)(sm + p.o_lut) : (const W*)p.lut_g;
         flips = (const W*)(sm + p.o_flip);
         rlut = (const unsigned*)(sm + (p.o_rlut >= 0 ? p.o_rlut : 0));
         keep32 = (const unsigned*)(sm + p.o_keep32);

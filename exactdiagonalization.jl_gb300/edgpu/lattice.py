@@ -69,3 +69,58 @@ def heisenberg_coupled(hs, bonds):
             ids.append(c)
     return (np.array(masks, dtype=np.uint64), np.array(rows, dtype=np.uint64), np.array(cols, dtype=np.uint64),
             np.array(amps, dtype=np.complex128), np.array(ids, dtype=np.int32))
+
+
+# C4v about site (0, 0) of an L x L torus: (class, (x, y) -> (x', y')); the characters of its four
+# one-dimensional irreps by class
+C4V_ELEMENTS = [
+    ("E", lambda x, y: (x, y)),
+    ("C4", lambda x, y: (-y, x)),
+    ("C2", lambda x, y: (-x, -y)),
+    ("C4", lambda x, y: (y, -x)),
+    ("sv", lambda x, y: (-x, y)),
+    ("sv", lambda x, y: (x, -y)),
+    ("sd", lambda x, y: (y, x)),
+    ("sd", lambda x, y: (-y, -x)),
+]
+C4V_CHARACTERS = {
+    "A1": {"E": 1, "C2": 1, "C4": 1, "sv": 1, "sd": 1},
+    "A2": {"E": 1, "C2": 1, "C4": 1, "sv": -1, "sd": -1},
+    "B1": {"E": 1, "C2": 1, "C4": -1, "sv": 1, "sd": -1},
+    "B2": {"E": 1, "C2": 1, "C4": -1, "sv": -1, "sd": 1},
+}
+
+
+def square_c4v_maps(L: int, momentum=(0, 0), irrep: str = "A1"):
+    """Site maps and amplitudes of the symmorphic space group T x C4v of an L x L square torus (the
+    translations times the point group about site 0, examples/spinhalfsquare_large.jl's
+    tsymbed x psymbed), element t o p with amplitude exp(-2 pi i k.t / L) chi(p), identity first.
+    k must be invariant under C4v (k = (0, 0) or (L/2, L/2)); irrep is one of A1, A2, B1, B2.
+    Returns (maps [L^4 * 2][L^2] int32, amplitudes complex)."""
+    k1, k2 = momentum
+    for _, f in C4V_ELEMENTS:
+        a, b = f(k1, k2)
+        if (a - k1) % L or (b - k2) % L:
+            raise ValueError(f"momentum {momentum} is not invariant under C4v")
+    chi = C4V_CHARACTERS[irrep]
+    n = L * L
+    maps, amps = [], []
+    for ty in range(L):
+        for tx in range(L):
+            ph = np.exp(-2j * np.pi * (k1 * tx + k2 * ty) / L)
+            for cls, f in C4V_ELEMENTS:
+                m = []
+                for s in range(n):
+                    x, y = s % L, s // L
+                    px, py = f(x, y)
+                    m.append((px + tx) % L + L * ((py + ty) % L))
+                maps.append(m)
+                amps.append(ph * chi[cls])
+    return np.array(maps, dtype=np.int32), np.array(amps)
+
+
+def square_c4v_symops(L: int, momentum=(0, 0), irrep: str = "A1"):
+    """square_c4v_maps as [(SitePermutation, amplitude)] for symmetry_reduce."""
+    from .representation import SitePermutation
+    maps, amps = square_c4v_maps(L, momentum, irrep)
+    return [(SitePermutation(m), complex(a)) for m, a in zip(maps, amps)]

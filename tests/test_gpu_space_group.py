@@ -53,6 +53,15 @@ def space_group(k, irrep):
     return np.array(maps, dtype=np.int32), np.array(amps)
 
 
+def test_library_maps_equal_test_maps():
+    from edgpu import lattice
+    for k in ((0, 0), (2, 2)):
+        for irrep in ("A1", "B2"):
+            m1, a1 = space_group(k, irrep)
+            m2, a2 = lattice.square_c4v_maps(4, k, irrep)
+            assert np.array_equal(m1, m2) and np.allclose(a1, a2)
+
+
 @pytest.mark.parametrize("k", [(0, 0), (2, 2)])
 @pytest.mark.parametrize("irrep", ["A1", "A2", "B1", "B2"])
 def test_square4x4_translations_times_c4v(k, irrep):
@@ -95,3 +104,58 @@ def test_square4x4_translations_times_c4v(k, irrep):
     r = E.lanczos(opr, min(N, 120), precision="fp64", reorth=True)
     assert abs(r.e0 - e_dense) < 1e-9 * max(1.0, abs(e_dense)), (r.e0, e_dense)
     torch.cuda.synchronize()
+
+
+def test_square6x6_translations_times_c4v_sampled_rows_and_e0():
+    """6x6 J1-J2 (J2/J1 = 0.5), 2Sz=0, A1 at Gamma of T x C4v (288 elements): 31,566,122
+    representatives (Burnside), sampled orbit minimality and completeness, sampled product rows through
+    the target table and the slab table against the oracle's orbit-by-orbit row formula, and the
+    ground-state energy against the translation-only k=(0,0) sector's (the ground state is in A1)."""
+    import torch
+    import edgpu as E
+    from edgpu import lattice
+    L = 6
+    n = L * L
+    hs, _ = E.spin_half_system(n)
+    nn = lattice.torus_bonds(L, L, lattice.SQUARE_NN)
+    nnn = lattice.torus_bonds(L, L, [(1, 1), (1, -1)])
+    jj = [1.0] * len(nn) + [0.5] * len(nnn)
+    H = lattice.xxz_hamiltonian(hs, nn + nnn, jj, jj)
+    terms = O.heisenberg_terms(n, nn + nnn, jj, jj)
+    maps, amps = lattice.square_c4v_maps(L, (0, 0), "A1")
+    hsr = E.represent(E.HilbertSpaceSector(hs, 0), lazy=True)
+    rh = E.symmetry_reduce(hsr, lattice.square_c4v_symops(L, (0, 0), "A1"))
+    N = rh.dimension
+    assert N == O.sector_dimension(maps, np.zeros(len(maps), dtype=int), 1, n // 2) == 31566122
+    basis = rh.basis_list
+    assert np.all(basis[1:] > basis[:-1])
+    ot = O.OrbitTables(n, n // 2, maps, amps, basis)
+    rng = np.random.default_rng(41)
+    sample = np.unique(np.concatenate([rng.integers(0, N, 2000), np.arange(16), np.arange(N - 16, N)]))
+    rep, kept, nd, _ = ot.orbit_info(basis[sample])
+    assert np.array_equal(rep, basis[sample]) and kept.all()
+    assert np.array_equal(nd, rh.orbit_sizes()[sample])
+    parent_states = np.array([int(sum(1 << int(b) for b in rng.choice(n, n // 2, replace=False)))
+                              for _ in range(5000)], dtype=np.uint64)
+    prep, pkept, _, _ = ot.orbit_info(parent_states)
+    assert np.all((O.lookup(basis, prep) >= 0) == pkept)
+    opr = E.represent(rh, H)
+    free, _ = torch.cuda.mem_get_info()
+    assert opr.build_targets(int(0.5 * free))
+    x = O.complex_gaussian(N, 5)
+    vals, st, _ = ot.rows(terms, x, sample)
+    assert (st == 0).all()
+    xd = torch.from_numpy(x).cuda()
+    for slabs in (False, True):
+        if slabs:
+            free, _ = torch.cuda.mem_get_info()
+            assert opr.build_slabs(slab_bytes=112 << 20, max_bytes=int(0.5 * free))
+        for prec, tol in (("fp64", 1e-12), ("mixed", 1e-5)):
+            xx = xd if prec == "fp64" else xd.to(torch.complex64)
+            y = torch.empty_like(xx)
+            E.mul_(y, opr, xx, precision=prec)
+            torch.cuda.synchronize()
+            ys = y.cpu().numpy().astype(np.complex128)[sample]
+            assert np.max(np.abs(ys - vals)) <= tol * np.max(np.abs(vals)), (slabs, prec)
+    r = E.lanczos(opr, 300, precision="fp64", reorth=False, seed=7, tol=1e-11)
+    assert abs(r.e0 - (-18.13714754007)) < 1e-8, r.e0
