@@ -1,4 +1,5 @@
-"""Concurrent products from several host threads on two operator handles.
+"""Concurrent products from several host threads on two operator handles (one of them through the
+multi-pass slab product).
 
 Calls on one handle are serialised by the handle's lock; distinct handles run concurrently, each on
 its own stream (host-buffer calls) or on the caller's stream (device-buffer calls).  Four threads,
@@ -29,6 +30,9 @@ def test_two_handles_from_four_threads_equal_serial():
     import edgpu
     from oracle import oracle as O
     ops = [_operator(20, 0), _operator(18, 5)]
+    # the first operator runs the multi-pass slab product (small slabs: several launches per product)
+    assert ops[0].build_targets(1 << 28) and ops[0].build_slabs(slab_bytes=1024 * 8, max_bytes=1 << 28)
+    assert ops[0].slabs_info[0] >= 3
     xs = [O.complex_gaussian(o.dimension, 3 + i) for i, o in enumerate(ops)]
     ref = {}
     for i, o in enumerate(ops):
