@@ -177,10 +177,11 @@ def build_tables(oprs, spaces, args):
 
 
 def build_slabs(opr, N, args):
-    """Column-slab table of a sector whose complex64 x exceeds L2, unless --slab-mb 0:
+    """Column-slab table of the operator (the autotuner times it against the one-pass schedules), unless
+    --slab-mb 0:
     {"built", "passes", "columns_per_slab", "entries", "bytes", "build_s"} or None."""
     import torch
-    if args.slab_mb <= 0 or 8 * N <= L2_BYTES or not hasattr(opr, "build_slabs"):
+    if args.slab_mb <= 0 or not hasattr(opr, "build_slabs"):
         return None
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -723,6 +724,22 @@ def run_gpu_batch(args, wl):
     cfg = workload_config(dict(wl, nnz_off=nnz), args.workload)
     map_info = build_maps(spaces, args)
     table_info = build_tables(oprs, spaces, args)
+    slab_info = None
+    if table_info and table_info.get("built") and args.slab_mb > 0:
+        # every sector's slab table (the batch autotuner times per-sector launches through them)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        slab_info = {"built": True, "passes": [], "entries": 0}
+        for o in oprs:
+            free, _ = torch.cuda.mem_get_info()
+            if not o.build_slabs(slab_bytes=int(args.slab_mb * (1 << 20)), max_bytes=int(0.5 * free)):
+                slab_info = {"built": False}
+                break
+            slab_info["passes"].append(o.slabs_info[0])
+            slab_info["entries"] += o.slabs_info[2]
+        if slab_info["built"]:
+            slab_info["passes"] = sorted(set(slab_info["passes"]))
+        slab_info["build_s"] = time.perf_counter() - t0
     if args.no_pair:
         for o in oprs:
             o.set_pair_schedule(False)
@@ -834,9 +851,10 @@ def run_gpu_batch(args, wl):
                        "target_table": dict(table_info or {"built": False}, used=batch.uses_target_tables("mixed")),
                        "bond_classes": oprs[0].pair_classes()[0], "l2": f"inputs cycled from {P} sets of x/y ({2 * P * N * s_c / 1e6:.0f} MB "
                        f"> 2x L2)", "parallelism": f"replicas x{world}", "setup_s": t_space,
-                       "library_graph_ms_per_step": ms_graph, "parent_map": map_info,
-                       "batch_launch": {0: "one persistent launch"}.get(batch.launch("mixed"),
-                                                                         f"per-sector launches on {batch.launch('mixed')} stream(s)"),
+                       "library_graph_ms_per_step": ms_graph, "parent_map": map_info, "slab_tables": slab_info,
+                       "batch_launch": {0: "one persistent launch"}.get(
+                           batch.launch("mixed"), f"per-sector launches on {batch.launch('mixed') & 3} stream(s)" +
+                           (", through the sectors' slab tables" if batch.launch("mixed") >= 5 else "")),
                        "per_sector_launches_ms_per_step": per_sector_ms},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": profiled_traffic(args.workload), "peak_source": peak_src,
@@ -954,7 +972,7 @@ def main():
     ap.add_argument("--slab-mode", type=int, default=1, choices=[1, 2],
                     help="with --tiling: the slab product's variant (1 plain, 2 with cache hints)")
     ap.add_argument("--slab-mb", type=float, default=112.0,
-                    help="column slabs of this many MB of complex64 x for sectors whose x exceeds L2 (0: none)")
+                    help="column slabs of this many MB of complex64 x (0: no slab table)")
     ap.add_argument("--no-pair", action="store_true", help="test every term per row instead of the pair-flip schedule")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-per-sector", action="store_true",

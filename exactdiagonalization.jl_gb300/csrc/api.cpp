@@ -278,6 +278,7 @@ struct edgpu_batch_s {
     // operator's product kernel with the batch's schedule), spread over k streams that run
     // concurrently (the calling stream alone for k = 1)
     int seq[2] = {0, 0};
+    int seq_slab[2] = {0, 0};                      // per-sector launches read the sectors' slab tables
     cudaStream_t lane_st[3] = {nullptr, nullptr, nullptr};
     cudaEvent_t fork_ev = nullptr, join_ev[3] = {nullptr, nullptr, nullptr};
     void ensure_lanes(int k) {
@@ -3243,8 +3244,9 @@ void batch_launch(edgpu_batch_s* b, int prec, const HxParams& p, int blocks, cud
 }
 
 // One sector of a batch launched on its own: the operator's product kernel with the batch's schedule
-// (pair flips, targets per step, target table, prefetch, lanes per row; no slab table) in place of
-// the operator's own for this launch.  The caller holds the operators' locks.
+// (pair flips, targets per step, target table, prefetch, lanes per row, and whether to read the
+// sector's slab table, with the operator's own slab variant) in place of the operator's own for this
+// launch.  The caller holds the operators' locks.
 void batch_sector_launch(edgpu_batch_s* b, int prec, int i, const void* x, void* y, cudaStream_t st) {
     edgpu_op_s* op = b->ops[i];
     if (op->space->dim == 0) return;
@@ -3255,7 +3257,7 @@ void batch_sector_launch(edgpu_batch_s* b, int prec, int i, const void* x, void*
     op->tab_use[prec] = b->tab_use[prec];
     op->tab_pf[prec] = b->tab_pf[prec];
     op->tab_uni[prec] = 0;
-    op->slab_use[prec] = 0;
+    op->slab_use[prec] = (b->seq_slab[prec] && op->slab.tab) ? 1 : 0;
     auto restore = [&] {
         op->pair_use[prec] = keep[0];
         op->pair_nt[prec] = keep[1];
@@ -3337,7 +3339,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
     const size_t vs = precision == EDGPU_FP64 ? 16 : 8;
     int64_t tot = 0;
     for (auto* o : b->ops) tot += o->space->dim;
-    int best = 1, best_pair = 1, best_nt = 2, best_tab = 1, best_pf = 0, best_seq = 0;
+    int best = 1, best_pair = 1, best_nt = 2, best_tab = 1, best_pf = 0, best_seq = 0, best_slab = 0;
     double best_ms = 1e30;
     if (tot > 0) {
         void *x = nullptr, *y = nullptr;
@@ -3371,15 +3373,20 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
             // l: target tables: one lane per row, x prefetched 0 (l = 1), 4 (l = 5) or 64 (l = 6) steps
             // ahead; the other schedules: l lanes per row.  sq: the launch mode (edgpu_batch_s::seq),
             // per-sector launches only with one lane per row and no prefetch.
-            struct Cand { int cand, l, sq; };
+            // per-sector launches also through the sectors' slab tables when every sector has one
+            bool slabbed = tabled;
+            for (auto* o : b->ops) slabbed = slabbed && (o->slab.tab != nullptr || o->space->dim == 0);
+            struct Cand { int cand, l, sq, slab; };
             std::vector<Cand> cands;
             for (int cand = tabled ? 5 : (pair_ok ? (mapped ? 2 : 1) : 0); cand >= 0; --cand)
                 for (int l : {1, 2, 4, 5, 6}) {
                     if (cand >= 3 && !(l == 1 || l >= 5)) continue;
                     if (cand < 3 && l >= 5) continue;
                     for (int sq = 0; sq <= 3; ++sq)
-                        if (sq == 0 || (l == 1 && cand > 0)) cands.push_back({cand, l, sq});
+                        if (sq == 0 || (l == 1 && cand > 0)) cands.push_back({cand, l, sq, 0});
                 }
+            if (slabbed)
+                for (int sq = 1; sq <= 3; ++sq) cands.push_back({4, 1, sq, 1});
             for (const Cand& cd : cands) {
                 const int cand = cd.cand;
                 int l = cd.l;
@@ -3391,6 +3398,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
                 b->pair_nt[precision] = cand == 5 ? 8 : (cand == 2 || cand == 4) ? 4 : 2;
                 b->tab_use[precision] = cand >= 3 ? 1 : 0;
                 b->seq[precision] = cd.sq;
+                b->seq_slab[precision] = cd.slab;
                 auto run = [&] { batch_run(b, precision, xs.data(), ys.data(), bh->hs.stream()); };
                 run();
                 float t_min = 1e30f;
@@ -3418,6 +3426,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
                     best_nt = cand == 5 ? 8 : (cand == 2 || cand == 4) ? 4 : 2;
                     best_tab = cand >= 3 ? 1 : 0;
                     best_seq = cd.sq;
+                    best_slab = cd.slab;
                 }
             }
         } catch (...) {
@@ -3426,6 +3435,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
             b->pair_nt[precision] = 2;
             b->tab_use[precision] = 1;
             b->seq[precision] = 0;
+            b->seq_slab[precision] = 0;
             cudaStreamSynchronize(bh->hs.stream());
             cudaFree(x);
             cudaFree(y);
@@ -3450,6 +3460,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
     b->tab_use[precision] = best_tab;
     b->tab_pf[precision] = best_pf;
     b->seq[precision] = best_seq;
+    b->seq_slab[precision] = best_slab;
     if (lanes_per_row_out) *lanes_per_row_out = best;
     if (best_ms_out) *best_ms_out = best_ms;
     API_END
@@ -3489,8 +3500,15 @@ int edgpu_batch_set_launch(edgpu_batch bh, int32_t precision, int32_t streams) {
     std::lock_guard<std::mutex> blk_(bh->hs.mu);
     BatchLocks locks_(bh->ops);
     check_prec(precision);
-    require(streams >= 0 && streams <= 3, EDGPU_ERR_ARG, "streams must be 0 (one persistent launch) or 1 to 3");
-    bh->seq[precision] = streams;
+    require(streams >= 0 && streams <= 7 && streams != 4, EDGPU_ERR_ARG,
+            "streams must be 0 (one persistent launch), 1 to 3, or 5 to 7 (per-sector launches through the "
+            "sectors' slab tables)");
+    if (streams >= 5)
+        for (auto* o : bh->ops)
+            require(o->slab.tab != nullptr || o->space->dim == 0, EDGPU_ERR_STATE,
+                    "a sector has no slab table (edgpu_op_build_slabs)");
+    bh->seq[precision] = streams & 3;
+    bh->seq_slab[precision] = streams >= 5 ? 1 : 0;
     API_END
 }
 
@@ -3499,7 +3517,7 @@ int edgpu_batch_get_launch(edgpu_batch bh, int32_t precision, int32_t* streams) 
     require(bh && streams, EDGPU_ERR_ARG, "null argument");
     std::lock_guard<std::mutex> blk_(bh->hs.mu);
     check_prec(precision);
-    *streams = bh->seq[precision];
+    *streams = bh->seq[precision] + (bh->seq_slab[precision] ? 4 : 0);
     API_END
 }
 
@@ -3523,15 +3541,17 @@ int edgpu_batch_mul_device(edgpu_batch bh, int32_t precision, const void* const*
     key.push_back((const void*)(intptr_t)b->lpr[precision]);
     key.push_back((const void*)(intptr_t)(b->pair_use[precision] * 8 + b->pair_nt[precision] +
                                           b->tab_use[precision] * 16 + 32 * b->tab_pf[precision]));   // the kernel
-    key.push_back((const void*)(intptr_t)sq);   // the launch mode
+    key.push_back((const void*)(intptr_t)(sq + 8 * b->seq_slab[precision]));   // the launch mode
     if (sq == 0) {
         int blocks = 0;
         key.push_back(batch_params(b, precision, xs, ys, &blocks).blob);   // the image (vectors, sector maps)
     } else {
         for (int i = 0; i < n; ++i) {
-            // per-sector launches read the operators' own tables
+            // per-sector launches read the operators' own tables (and their slab variants)
             key.push_back(b->ops[i]->d_tab);
             key.push_back(b->ops[i]->space->d_map);
+            key.push_back(b->ops[i]->slab.tab);
+            key.push_back((const void*)(intptr_t)b->ops[i]->slab_hint[precision]);
         }
     }
     for (int i = 0; i < n; ++i) {

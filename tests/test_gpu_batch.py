@@ -151,6 +151,40 @@ def test_batch_generic_group(edgpu):
     run_batch_checks(edgpu, oprs, reds, terms)
 
 
+def test_batch_per_sector_slab_tables(edgpu):
+    """Per-sector launches through each sector's slab table (launch modes 5 to 7): every sector's
+    result equals that operator's own slab product bit for bit, and the oracle within tolerance."""
+    import torch
+    oprs, reds, terms = triangular_sectors(edgpu, 4, 3, 0)
+    b = edgpu.Batch(oprs)
+    with pytest.raises(RuntimeError):
+        b.set_launch("mixed", 5)          # no slab tables yet
+    for o in oprs:
+        if o.dimension:
+            assert o.build_targets(1 << 26) and o.build_slabs(slab_bytes=8, max_bytes=1 << 26)
+    xs_np = [O.complex_gaussian(o.dimension, 30 + i) for i, o in enumerate(oprs)]
+    want = [O.apply_rows(r, terms, x) for r, x in zip(reds, xs_np)]
+    for prec, tol, dt in (("fp64", FP64_TOL, torch.complex128), ("mixed", MIXED_TOL, torch.complex64)):
+        xs = [torch.from_numpy(x).to(dt).cuda() for x in xs_np]
+        ref = []
+        for o, x in zip(oprs, xs):
+            y = torch.empty_like(x)
+            edgpu.mul_(y, o, x, precision=prec)
+            ref.append(y)
+        for launch in (5, 6, 7):
+            b.set_launch(prec, launch)
+            assert b.launch(prec) == launch
+            for use_graph in (False, True, True):
+                ys = [torch.full_like(x, float("nan")) for x in xs]
+                b.mul_(ys, xs, precision=prec, use_graph=use_graph)
+                torch.cuda.synchronize()
+                for k, (y, r, w) in enumerate(zip(ys, ref, want)):
+                    assert torch.equal(y, r), (prec, launch, use_graph, k)
+                    assert relerr(y.cpu().numpy().astype(np.complex128), w) < tol, (prec, launch, k)
+    lpr, ms = b.autotune("mixed")
+    assert b.launch("mixed") in (0, 1, 2, 3, 5, 6, 7)
+
+
 def test_batch_rejects_different_operators(edgpu):
     import torch
     from edgpu import lattice
@@ -172,6 +206,8 @@ def test_batch_rejects_different_operators(edgpu):
         b.set_tiling("mixed", 3)
     with pytest.raises(edgpu.ArgumentError):
         b.set_launch("mixed", 4)
+    with pytest.raises(edgpu.ArgumentError):
+        b.set_launch("mixed", 8)
 
 
 def test_batch_follows_coupling_changes_and_autotune(edgpu):
