@@ -278,7 +278,7 @@ struct edgpu_batch_s {
     // operator's product kernel with the batch's schedule), spread over k streams that run
     // concurrently (the calling stream alone for k = 1)
     int seq[2] = {0, 0};
-    int seq_slab[2] = {0, 0};                      // per-sector launches read the sectors' slab tables
+    int seq_own[2] = {0, 0};                       // per-sector launches keep each operator's own schedule
     cudaStream_t lane_st[3] = {nullptr, nullptr, nullptr};
     cudaEvent_t fork_ev = nullptr, join_ev[3] = {nullptr, nullptr, nullptr};
     void ensure_lanes(int k) {
@@ -3244,12 +3244,17 @@ void batch_launch(edgpu_batch_s* b, int prec, const HxParams& p, int blocks, cud
 }
 
 // One sector of a batch launched on its own: the operator's product kernel with the batch's schedule
-// (pair flips, targets per step, target table, prefetch, lanes per row, and whether to read the
-// sector's slab table, with the operator's own slab variant) in place of the operator's own for this
-// launch.  The caller holds the operators' locks.
+// (pair flips, targets per step, target table, prefetch, lanes per row; no slab table) in place of
+// the operator's own for this launch, or (seq_own) with the operator's own schedule.  The caller holds
+// the operators' locks.
 void batch_sector_launch(edgpu_batch_s* b, int prec, int i, const void* x, void* y, cudaStream_t st) {
     edgpu_op_s* op = b->ops[i];
     if (op->space->dim == 0) return;
+    if (b->seq_own[prec]) {
+        // the operator's own (autotuned) schedule, as edgpu_mul_device on the sector
+        launch_product(op, prec, 0, 0, x, y, 0, nullptr, nullptr, st);
+        return;
+    }
     const int keep[6] = {op->pair_use[prec], op->pair_nt[prec], op->tab_use[prec], op->tab_pf[prec], op->tab_uni[prec],
                          op->slab_use[prec]};
     op->pair_use[prec] = b->pair_use[prec];
@@ -3257,7 +3262,7 @@ void batch_sector_launch(edgpu_batch_s* b, int prec, int i, const void* x, void*
     op->tab_use[prec] = b->tab_use[prec];
     op->tab_pf[prec] = b->tab_pf[prec];
     op->tab_uni[prec] = 0;
-    op->slab_use[prec] = (b->seq_slab[prec] && op->slab.tab) ? 1 : 0;
+    op->slab_use[prec] = 0;
     auto restore = [&] {
         op->pair_use[prec] = keep[0];
         op->pair_nt[prec] = keep[1];
@@ -3373,9 +3378,8 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
             // l: target tables: one lane per row, x prefetched 0 (l = 1), 4 (l = 5) or 64 (l = 6) steps
             // ahead; the other schedules: l lanes per row.  sq: the launch mode (edgpu_batch_s::seq),
             // per-sector launches only with one lane per row and no prefetch.
-            // per-sector launches also through the sectors' slab tables when every sector has one
-            bool slabbed = tabled;
-            for (auto* o : b->ops) slabbed = slabbed && (o->slab.tab != nullptr || o->space->dim == 0);
+            // per-sector launches also with each operator's own schedule (its autotuned one: the slab
+            // table, the target table or the term scan, which may differ from sector to sector)
             struct Cand { int cand, l, sq, slab; };
             std::vector<Cand> cands;
             for (int cand = tabled ? 5 : (pair_ok ? (mapped ? 2 : 1) : 0); cand >= 0; --cand)
@@ -3385,8 +3389,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
                     for (int sq = 0; sq <= 3; ++sq)
                         if (sq == 0 || (l == 1 && cand > 0)) cands.push_back({cand, l, sq, 0});
                 }
-            if (slabbed)
-                for (int sq = 1; sq <= 3; ++sq) cands.push_back({4, 1, sq, 1});
+            for (int sq = 1; sq <= 3; ++sq) cands.push_back({4, 1, sq, 1});
             for (const Cand& cd : cands) {
                 const int cand = cd.cand;
                 int l = cd.l;
@@ -3398,7 +3401,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
                 b->pair_nt[precision] = cand == 5 ? 8 : (cand == 2 || cand == 4) ? 4 : 2;
                 b->tab_use[precision] = cand >= 3 ? 1 : 0;
                 b->seq[precision] = cd.sq;
-                b->seq_slab[precision] = cd.slab;
+                b->seq_own[precision] = cd.slab;
                 auto run = [&] { batch_run(b, precision, xs.data(), ys.data(), bh->hs.stream()); };
                 run();
                 float t_min = 1e30f;
@@ -3435,7 +3438,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
             b->pair_nt[precision] = 2;
             b->tab_use[precision] = 1;
             b->seq[precision] = 0;
-            b->seq_slab[precision] = 0;
+            b->seq_own[precision] = 0;
             cudaStreamSynchronize(bh->hs.stream());
             cudaFree(x);
             cudaFree(y);
@@ -3460,7 +3463,7 @@ int edgpu_batch_autotune(edgpu_batch bh, int32_t precision, int32_t* lanes_per_r
     b->tab_use[precision] = best_tab;
     b->tab_pf[precision] = best_pf;
     b->seq[precision] = best_seq;
-    b->seq_slab[precision] = best_slab;
+    b->seq_own[precision] = best_slab;
     if (lanes_per_row_out) *lanes_per_row_out = best;
     if (best_ms_out) *best_ms_out = best_ms;
     API_END
@@ -3501,14 +3504,10 @@ int edgpu_batch_set_launch(edgpu_batch bh, int32_t precision, int32_t streams) {
     BatchLocks locks_(bh->ops);
     check_prec(precision);
     require(streams >= 0 && streams <= 7 && streams != 4, EDGPU_ERR_ARG,
-            "streams must be 0 (one persistent launch), 1 to 3, or 5 to 7 (per-sector launches through the "
-            "sectors' slab tables)");
-    if (streams >= 5)
-        for (auto* o : bh->ops)
-            require(o->slab.tab != nullptr || o->space->dim == 0, EDGPU_ERR_STATE,
-                    "a sector has no slab table (edgpu_op_build_slabs)");
+            "streams must be 0 (one persistent launch), 1 to 3, or 5 to 7 (per-sector launches with each "
+            "operator's own schedule)");
     bh->seq[precision] = streams & 3;
-    bh->seq_slab[precision] = streams >= 5 ? 1 : 0;
+    bh->seq_own[precision] = streams >= 5 ? 1 : 0;
     API_END
 }
 
@@ -3517,7 +3516,7 @@ int edgpu_batch_get_launch(edgpu_batch bh, int32_t precision, int32_t* streams) 
     require(bh && streams, EDGPU_ERR_ARG, "null argument");
     std::lock_guard<std::mutex> blk_(bh->hs.mu);
     check_prec(precision);
-    *streams = bh->seq[precision] + (bh->seq_slab[precision] ? 4 : 0);
+    *streams = bh->seq[precision] + (bh->seq_own[precision] ? 4 : 0);
     API_END
 }
 
@@ -3541,7 +3540,7 @@ int edgpu_batch_mul_device(edgpu_batch bh, int32_t precision, const void* const*
     key.push_back((const void*)(intptr_t)b->lpr[precision]);
     key.push_back((const void*)(intptr_t)(b->pair_use[precision] * 8 + b->pair_nt[precision] +
                                           b->tab_use[precision] * 16 + 32 * b->tab_pf[precision]));   // the kernel
-    key.push_back((const void*)(intptr_t)(sq + 8 * b->seq_slab[precision]));   // the launch mode
+    key.push_back((const void*)(intptr_t)(sq + 8 * b->seq_own[precision]));   // the launch mode
     if (sq == 0) {
         int blocks = 0;
         key.push_back(batch_params(b, precision, xs, ys, &blocks).blob);   // the image (vectors, sector maps)
@@ -3550,8 +3549,15 @@ int edgpu_batch_mul_device(edgpu_batch bh, int32_t precision, const void* const*
             // per-sector launches read the operators' own tables (and their slab variants)
             key.push_back(b->ops[i]->d_tab);
             key.push_back(b->ops[i]->space->d_map);
-            key.push_back(b->ops[i]->slab.tab);
-            key.push_back((const void*)(intptr_t)b->ops[i]->slab_hint[precision]);
+            const edgpu_op_s* o = b->ops[i];
+            key.push_back(o->slab.tab);
+            // the operator's own schedule (modes 5 to 7 launch with it)
+            key.push_back((const void*)(intptr_t)(o->pair_allowed + 2 * o->pair_use[precision] + 4 * o->pair_nt[precision] +
+                                                  64 * o->tab_use[precision] + 128 * o->tab_uni[precision] +
+                                                  256 * o->slab_use[precision] + 512 * o->tab_pf[precision] +
+                                                  (1 << 20) * o->slab_hint[precision]));
+            key.push_back((const void*)(intptr_t)o->tuned_rows[precision]);
+            key.push_back((const void*)(uintptr_t)o->gen);
         }
     }
     for (int i = 0; i < n; ++i) {

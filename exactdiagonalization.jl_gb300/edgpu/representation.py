@@ -974,7 +974,7 @@ class Batch:
     def set_launch(self, precision, streams: int):
         """0: all sectors in one persistent launch; 1: one product launch per sector on the call's
         stream; 2 or 3: per-sector launches spread over that many concurrent streams; 5 to 7: the
-        same on 1 to 3 streams through each sector's slab table."""
+        same on 1 to 3 streams with each operator's own (autotuned) schedule."""
         check(lib().edgpu_batch_set_launch(self._h, _prec(precision), int(streams)))
 
     def launch(self, precision="mixed") -> int:

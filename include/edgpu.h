@@ -341,9 +341,9 @@ int edgpu_batch_create(int32_t n_ops, const edgpu_op* ops, edgpu_batch* out);
 int edgpu_batch_set_tiling(edgpu_batch b, int32_t precision, int32_t lanes_per_row);
 /* In-library autotuner: times the batched launch for 1, 2 and 4 lanes per row, with and without the
  * pair-flip schedule where it applies (and the first operator allows it), and for the pair-flip
- * schedules also per-sector launches on 1, 2 and 3 streams (edgpu_batch_set_launch), through the
- * sectors' slab tables when every sector has one, on scratch vectors (allocated and freed here), and
- * keeps the fastest. */
+ * schedules also per-sector launches on 1, 2 and 3 streams (edgpu_batch_set_launch), with the batch's
+ * schedule and with each operator's own, on scratch vectors (allocated and freed here), and keeps the
+ * fastest. */
 int edgpu_batch_autotune(edgpu_batch b, int32_t precision, int32_t* lanes_per_row_out, double* best_ms_out);
 /* The batched launch's lanes per row (0 = default), and pair_flips and target_table as in
  * edgpu_op_get_schedule (the batch reads target tables when every operator has one). */
@@ -356,8 +356,9 @@ int edgpu_batch_get_schedule(edgpu_batch b, int32_t precision, int32_t* lanes_pe
  *   2 or 3  the same per-sector launches spread over that many streams of the batch (sector k on
  *           stream k mod streams), forked from and joined back into the call's stream, so that a
  *           sector's launch fills the SMs that the previous sector's last blocks leave idle;
- *   5 to 7  per-sector launches on 1 to 3 streams through each sector's slab table (every sector
- *           needs one: EDGPU_ERR_STATE otherwise), with the operator's slab variant.
+ *   5 to 7  per-sector launches on 1 to 3 streams, each with its operator's own schedule (the one
+ *           edgpu_op_autotune chose for it: slab table, target table or term scan; the best may differ
+ *           between sectors).  Results equal edgpu_mul_device on each sector bit for bit.
  * The per-sector modes read the operators' own tables, not a batched image. */
 int edgpu_batch_set_launch(edgpu_batch b, int32_t precision, int32_t streams);
 int edgpu_batch_get_launch(edgpu_batch b, int32_t precision, int32_t* streams);
