@@ -744,10 +744,22 @@ def run_gpu_batch(args, wl):
         for o in oprs:
             o.set_pair_schedule(False)
     batch = edgpu.Batch(oprs)
-    # each sector's own schedule first (the batch autotuner also times per-sector launches with them)
-    for o in oprs:
-        o.autotune("mixed")
-    lpr, tune_ms = batch.autotune("mixed")
+    if args.tiling:
+        # a fixed schedule for every sector and a fixed batch launch mode instead of the autotuners
+        # (reproducible profiles)
+        for o in oprs:
+            o.set_pair_schedule(args.pair_targets > 0, max(args.pair_targets, 2), args.uniform)
+            o.set_tiling("mixed", args.tiling)
+            o.table_prefetch("mixed", args.prefetch)
+            if slab_info and slab_info.get("built"):
+                o.slab_use("mixed", args.slab_mode)
+        batch.set_launch("mixed", args.batch_launch)
+        lpr, tune_ms = -args.tiling, None
+    else:
+        # each sector's own schedule first (the batch autotuner also times per-sector launches with them)
+        for o in oprs:
+            o.autotune("mixed")
+        lpr, tune_ms = batch.autotune("mixed")
     stream = torch.cuda.current_stream()
     s_c = 8
     P = max(2, math.ceil(2 * L2_BYTES / (2 * N * s_c)))
@@ -980,6 +992,8 @@ def main():
     ap.add_argument("--no-table", action="store_true", help="no target tables (look every target up per product)")
     ap.add_argument("--keep-targets", action="store_true",
                     help="keep the target table when both precisions read the slab table")
+    ap.add_argument("--batch-launch", type=int, default=7, choices=[0, 1, 2, 3, 5, 6, 7],
+                    help="batched workload with --tiling: the batch launch mode (edgpu_batch_set_launch)")
     ap.add_argument("--slab-mode", type=int, default=1, choices=[1, 2],
                     help="with --tiling: the slab product's variant (1 plain, 2 with cache hints)")
     ap.add_argument("--slab-mb", type=float, default=112.0,
