@@ -783,10 +783,14 @@ def run_gpu_batch(args, wl):
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     tw0 = time.time()
+    if args.profile_range:
+        torch.cuda.profiler.start()       # a profiler started with --profile-from-start off sees this only
     e0.record(stream)
     graph.replay()
     e1.record(stream)
     torch.cuda.synchronize()
+    if args.profile_range:
+        torch.cuda.profiler.stop()
     tw1 = time.time()
     barrier()
     ms = e0.elapsed_time(e1)
@@ -992,6 +996,9 @@ def main():
     ap.add_argument("--no-table", action="store_true", help="no target tables (look every target up per product)")
     ap.add_argument("--keep-targets", action="store_true",
                     help="keep the target table when both precisions read the slab table")
+    ap.add_argument("--profile-range", action="store_true",
+                    help="batched workload: bracket the timed steps with cudaProfilerStart/Stop (for a "
+                         "profiler run with --profile-from-start off: the autotuners run unprofiled)")
     ap.add_argument("--batch-launch", type=int, default=7, choices=[0, 1, 2, 3, 5, 6, 7],
                     help="batched workload with --tiling: the batch launch mode (edgpu_batch_set_launch)")
     ap.add_argument("--slab-mode", type=int, default=1, choices=[1, 2],
