@@ -925,6 +925,8 @@ def run_gpu_grad(args, wl):
     table_info = build_tables([opr], [space], args)
     # the column-sorted adjoint table: the adjoint of these (non-invariant) terms as a gather in a fixed order
     adjoint_table = bool(table_info and table_info.get("built")) and opr.build_adjoint_targets()
+    # the slab table for the forward product (the gradient and the adjoint have their own kernels)
+    slab_info = build_slabs(opr, N, args) if table_info and table_info.get("built") else None
     opr.autotune("mixed")
     opr.autotune("fp64")
     stream = torch.cuda.current_stream()
@@ -963,6 +965,9 @@ def run_gpu_grad(args, wl):
             "config": cfg,
             "gpu_setup": {"invariant_terms": opr.is_invariant, "setup_s": t_space, "parent_map": map_info,
                           "target_table": table_info, "adjoint_table": adjoint_table,
+                          "slab_table": dict(slab_info or {"built": False},
+                                             forward_uses={p: opr.slab_use(p) for p in ("mixed", "fp64")}
+                                             if slab_info and slab_info.get("built") else None),
                           "grad_kernel": {"mixed": opr.grad_kernel("mixed"), "fp64": opr.grad_kernel("fp64")},
                           "ms": res, "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": b / t_fwd / 1e9, "peak": peak, "unit": "GB/s",
