@@ -220,6 +220,19 @@ struct edgpu_op_s {
         int lut_real = 1;
     } slab;
     int slab_use[2] = {0, 0};         // [precision]: products read the slab table (chosen by the autotuner)
+    // host-buffer slab products: a second stream converting x slab by slab while the passes run
+    cudaStream_t aux_st = nullptr;
+    cudaEvent_t aux_fork = nullptr;
+    std::vector<cudaEvent_t> slab_ready;
+    void ensure_slab_events(int n) {
+        if (!aux_st) EDGPU_CUDA(cudaStreamCreateWithFlags(&aux_st, cudaStreamNonBlocking));
+        if (!aux_fork) EDGPU_CUDA(cudaEventCreateWithFlags(&aux_fork, cudaEventDisableTiming));
+        while ((int)slab_ready.size() < n) {
+            cudaEvent_t e = nullptr;
+            EDGPU_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            slab_ready.push_back(e);
+        }
+    }
     int slab_hint[2] = {0, 0};        // [precision]: the slab product's cache hints (chosen by the autotuner)
     // the optional tables change: cached graphs (this handle's host-buffer graphs, and batches, which
     // compare gen) must not replay launches that read the old ones
@@ -259,6 +272,12 @@ struct edgpu_op_s {
         free_table();
         free_adjoint();
         free_slabs();
+        if (aux_st) {
+            cudaStreamSynchronize(aux_st);
+            cudaStreamDestroy(aux_st);
+        }
+        if (aux_fork) cudaEventDestroy(aux_fork);
+        for (auto e : slab_ready) cudaEventDestroy(e);
     }
 };
 
@@ -1036,6 +1055,39 @@ bool slab_active(const edgpu_op_s* op, int prec, int dir, int mode, int rows) {
            rows < 0;
 }
 
+// The column-slab product: one launch per slab (hxslab.cu); the last pass adds the diagonal term and
+// writes complex128 to y_c128 when given.  With ready != null, pass q first waits for ready[q] (the
+// event after which slab q of x, and for the last pass all of x, is in place).
+void launch_slab_passes(edgpu_op_s* op, int prec, const Blob& B, const void* x, void* y, int accumulate,
+                        void* y_c128, int acc_c128, cudaStream_t st, const cudaEvent_t* ready) {
+    const auto& S = op->slab;
+    SlabRun r{};
+    r.x = x;
+    r.y = y;
+    r.diag = B.d_diag;
+    r.lut = prec == EDGPU_FP64 ? (const void*)S.lut64.p : (const void*)S.lut.p;
+    r.n_lut = S.n_ids;
+    r.lut_real = S.lut_real;
+    r.n_rows = B.tmpl.n_rows;
+    r.n_tiles = (r.n_rows + 31) / 32;
+    r.colbits = S.colbits;
+    r.colmask = (unsigned)((1ull << S.colbits) - 1ull);
+    r.y_c128 = y_c128;
+    r.acc_c128 = acc_c128;
+    r.accumulate = y_c128 ? 0 : accumulate;
+    r.hints = op->slab_hint[prec];
+    for (int q = 0; q < S.n_pass; ++q) {
+        if (ready) EDGPU_CUDA(cudaStreamWaitEvent(st, ready[q], 0));
+        r.cnt = S.counts + (size_t)q * r.n_rows;
+        r.off = S.off + (size_t)q * r.n_tiles;
+        r.tab = S.tab + S.base[q];
+        r.xs = (const char*)x + (size_t)q * S.wc * (prec == EDGPU_FP64 ? 16 : 8);
+        r.first = q == 0;
+        r.last = q == S.n_pass - 1;
+        hx_slab_launch(prec, r, st);
+    }
+}
+
 // Shared memory of the pair-flip gradient kernel's per-thread coupling accumulators (the product's
 // real type: FP32 in mixed precision, FP64 in FP64).
 static size_t pair_grad_acc_bytes(const edgpu_op_s* op, int prec) {
@@ -1073,33 +1125,7 @@ void launch_product(edgpu_op_s* op, int prec, int dir, int mode, const void* x, 
         if (rows > 0) rows = -1;
     }
     if (slab_active(op, prec, dir, mode, rows)) {
-        // the column-slab table: one launch per slab (hxslab.cu); the last writes complex128 to
-        // y_c128 when given
-        const auto& S = op->slab;
-        SlabRun r{};
-        r.x = x;
-        r.y = y;
-        r.diag = B.d_diag;
-        r.lut = prec == EDGPU_FP64 ? (const void*)S.lut64.p : (const void*)S.lut.p;
-        r.n_lut = S.n_ids;
-        r.lut_real = S.lut_real;
-        r.n_rows = p.n_rows;
-        r.n_tiles = (p.n_rows + 31) / 32;
-        r.colbits = S.colbits;
-        r.colmask = (unsigned)((1ull << S.colbits) - 1ull);
-        r.y_c128 = y_c128;
-        r.acc_c128 = acc_c128;
-        r.accumulate = y_c128 ? 0 : accumulate;
-        r.hints = op->slab_hint[prec];
-        for (int q = 0; q < S.n_pass; ++q) {
-            r.cnt = S.counts + (size_t)q * p.n_rows;
-            r.off = S.off + (size_t)q * r.n_tiles;
-            r.tab = S.tab + S.base[q];
-            r.xs = (const char*)x + (size_t)q * S.wc * (prec == EDGPU_FP64 ? 16 : 8);
-            r.first = q == 0;
-            r.last = q == S.n_pass - 1;
-            hx_slab_launch(prec, r, st);
-        }
+        launch_slab_passes(op, prec, B, x, y, accumulate, y_c128, acc_c128, st, nullptr);
         if (wrote_c128) *wrote_c128 = y_c128 != nullptr;
         if (blocks_used) *blocks_used = 0;
         return;
@@ -2731,6 +2757,25 @@ static void host_product_issue(edgpu_op_s* op, int prec, int dir, const double* 
         // write y to host memory directly (no staging copies)
         const double* xd = (const double*)device_alias(x);
         double* yd = (double*)device_alias(y);
+        const int rows = op->tuned_rows[prec] ? op->tuned_rows[prec] : -1;
+        if (xd && yd && slab_active(op, prec, dir, 0, (rows > 0 && op->space->d_map) ? -1 : rows)) {
+            // the slab passes: slab q of x is converted on a second stream while the earlier passes
+            // run (pass q waits for it; the last pass, which adds the diagonal term, for all of x), and
+            // the last pass writes the complex128 result to the host buffer
+            build_blob(op, prec, dir, 0);
+            const auto& S = op->slab;
+            op->ensure_slab_events(S.n_pass);
+            EDGPU_CUDA(cudaEventRecord(op->aux_fork, st));
+            EDGPU_CUDA(cudaStreamWaitEvent(op->aux_st, op->aux_fork, 0));
+            for (int q = 0; q < S.n_pass; ++q) {
+                const int64_t c0 = (int64_t)q * S.wc, c1 = std::min<int64_t>(n, c0 + S.wc);
+                launch_c128_to_c64(c1 - c0, xd + 2 * c0, op->x32.p + 2 * c0, op->aux_st);
+                EDGPU_CUDA(cudaEventRecord(op->slab_ready[q], op->aux_st));
+            }
+            launch_slab_passes(op, prec, op->blob[prec][dir][0], op->x32.p, op->y32.p, 0, yd, accumulate, st,
+                               op->slab_ready.data());
+            return;
+        }
         if (xd && yd) {
             launch_c128_to_c64(n, xd, op->x32.p, st);
             // the pair-flip kernel writes the complex128 result to the host buffer itself
@@ -2746,16 +2791,27 @@ static void host_product_issue(edgpu_op_s* op, int prec, int dir, const double* 
         // and the product writes (or, for apply!, updates) y in the host buffer itself
         double* yd = (double*)device_alias(y);
         if (yd) {
-            EDGPU_CUDA(cudaMemcpyAsync(op->x64.p, x, n * 16, cudaMemcpyHostToDevice, st));
             const int rows = op->tuned_rows[prec] ? op->tuned_rows[prec] : -1;
             if (slab_active(op, prec, dir, 0, (rows > 0 && op->space->d_map) ? -1 : rows)) {
-                // the slab passes add into the device buffer; the last writes the host buffer
-                bool wrote = false;
-                launch_product(op, prec, dir, 0, op->x64.p, op->y64.p, 0, nullptr, nullptr, st, nullptr, 0, yd,
-                               accumulate, &wrote);
-                require(wrote, EDGPU_ERR_STATE, "internal: slab product did not write the host buffer");
+                // the slab passes add into the device buffer and the last writes the host buffer; x is
+                // copied in slab by slab on a second stream (one copy per slab) while the earlier
+                // passes run
+                build_blob(op, prec, dir, 0);
+                const auto& S = op->slab;
+                op->ensure_slab_events(S.n_pass);
+                EDGPU_CUDA(cudaEventRecord(op->aux_fork, st));
+                EDGPU_CUDA(cudaStreamWaitEvent(op->aux_st, op->aux_fork, 0));
+                for (int q = 0; q < S.n_pass; ++q) {
+                    const int64_t c0 = (int64_t)q * S.wc, c1 = std::min<int64_t>(n, c0 + S.wc);
+                    EDGPU_CUDA(cudaMemcpyAsync(op->x64.p + 2 * c0, x + 2 * c0, (size_t)(c1 - c0) * 16,
+                                               cudaMemcpyHostToDevice, op->aux_st));
+                    EDGPU_CUDA(cudaEventRecord(op->slab_ready[q], op->aux_st));
+                }
+                launch_slab_passes(op, prec, op->blob[prec][dir][0], op->x64.p, op->y64.p, 0, yd, accumulate, st,
+                                   op->slab_ready.data());
                 return;
             }
+            EDGPU_CUDA(cudaMemcpyAsync(op->x64.p, x, n * 16, cudaMemcpyHostToDevice, st));
             launch_product(op, prec, dir, 0, op->x64.p, yd, accumulate, nullptr, nullptr, st);
             return;
         }

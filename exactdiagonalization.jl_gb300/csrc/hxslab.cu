@@ -203,7 +203,7 @@ __device__ __forceinline__ void st_stream(T* p, T v) {
 
 // One pass of the product: a warp per tile of 32 rows, one lane per row; the lane adds its row's
 // entries of this pass (NT per step, loads then gathers), then adds the sum to y (the first pass
-// writes y = diag x + sum; the last pass may write complex128 to y_c128 instead).
+// writes it, the last adds the diagonal term too and may write complex128 to y_c128 instead).
 template <int PREC, bool REAL, int NT, bool CH>
 __global__ void __launch_bounds__(HX_THREADS) hx_slab_kernel(const SlabRun r) {
     typedef typename Cx<PREC>::V V;
@@ -259,14 +259,16 @@ __global__ void __launch_bounds__(HX_THREADS) hx_slab_kernel(const SlabRun r) {
             }
         }
         if (!act) continue;
+        // passes add their sums in order; the last adds the diagonal term diag x (so that a pass needs
+        // only its own slab of x, the last one all of it)
         V t;
         if (r.first) {
-            t = cfma_acc(acc, ld_stream<CH>((const V*)r.diag + row), ld_stream<CH>((const V*)r.x + row));
-            if (r.accumulate) t = cadd(ld_stream<CH>(y + row), t);
+            t = (r.accumulate) ? cadd(ld_stream<CH>(y + row), acc) : acc;
         } else {
-            if (cnt == 0 && !to_c128) continue;   // nothing to add to this row
+            if (cnt == 0 && !r.last) continue;   // nothing to add to this row
             t = cadd(ld_stream<CH>(y + row), acc);
         }
+        if (r.last) t = cfma_acc(t, ld_stream<CH>((const V*)r.diag + row), ld_stream<CH>((const V*)r.x + row));
         if (to_c128) {
             double2 o = make_double2((double)t.x, (double)t.y);
             double2* yc = (double2*)r.y_c128;
