@@ -690,7 +690,7 @@ def run_gpu(args, wl):
                        "slab_table": dict(slab_info or {"built": False},
                                           used={"mixed": opr.slab_use("mixed") if slab_info and slab_info.get("built") else 0,
                                                 "fp64": opr.slab_use("fp64") if slab_info and slab_info.get("built") else 0},
-                                          use_codes="0 none, 1 slab product, 2 slab product with cache hints"),
+                                          use_codes="0 none, 1 slab product, 2 with cache hints, 3 eight entries per step, 4 both"),
                        "setup_s": t_space, "search_directory": dir_stats, "parent_map": map_info},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_src,
@@ -1006,8 +1006,9 @@ def main():
                          "profiler run with --profile-from-start off: the autotuners run unprofiled)")
     ap.add_argument("--batch-launch", type=int, default=7, choices=[0, 1, 2, 3, 5, 6, 7],
                     help="batched workload with --tiling: the batch launch mode (edgpu_batch_set_launch)")
-    ap.add_argument("--slab-mode", type=int, default=1, choices=[1, 2],
-                    help="with --tiling: the slab product's variant (1 plain, 2 with cache hints)")
+    ap.add_argument("--slab-mode", type=int, default=1, choices=[1, 2, 3, 4],
+                    help="with --tiling: the slab product's variant (1 plain, 2 cache hints, 3 eight entries "
+                         "per step, 4 both)")
     ap.add_argument("--slab-mb", type=float, default=112.0,
                     help="column slabs of this many MB of complex64 x (0: no slab table)")
     ap.add_argument("--no-pair", action="store_true", help="test every term per row instead of the pair-flip schedule")

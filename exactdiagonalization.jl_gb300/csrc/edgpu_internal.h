@@ -376,7 +376,8 @@ struct SlabRun {
     unsigned colmask;
     int colbits, n_lut, lut_real;
     int first, last, accumulate, acc_c128;
-    int hints;                      // 1: gathers cached in L2 only, streamed data evict-first
+    int hints;                      // bit 0: gathers cached in L2 only, streamed data evict-first;
+                                    // bit 1: eight entries per lane and step instead of four
 };
 // Count pass (1) or fill pass (2) of the slab table from the target table.  p: the table-flavour
 // pair-flip template (tab, tile_off set; lpr = 1); smem: its image plus s.o_ctr's counters.

@@ -363,27 +363,33 @@ void hx_slab_scan(const unsigned* tile_sum, unsigned* off, int n_pass, long long
     if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("slab scan: ") + cudaGetErrorString(e));
 }
 
-template <int PREC, bool CH>
+template <int PREC, bool CH, int NT>
 void slab_launch_t(const SlabRun& r, size_t smem, cudaStream_t st) {
     if (r.lut_real) {
-        auto k = hx_slab_kernel<PREC, true, 4, CH>;
+        auto k = hx_slab_kernel<PREC, true, NT, CH>;
         slab_pdl_launch(k, r, slab_blocks(k, smem, r.n_tiles), smem, st);
     } else {
-        auto k = hx_slab_kernel<PREC, false, 4, CH>;
+        auto k = hx_slab_kernel<PREC, false, NT, CH>;
         slab_pdl_launch(k, r, slab_blocks(k, smem, r.n_tiles), smem, st);
+    }
+}
+
+// hints: bit 0 the cache hints, bit 1 eight entries per lane and step instead of four
+template <int PREC>
+void slab_launch_p(const SlabRun& r, size_t smem, cudaStream_t st) {
+    switch (r.hints & 3) {
+        case 0: slab_launch_t<PREC, false, 4>(r, smem, st); break;
+        case 1: slab_launch_t<PREC, true, 4>(r, smem, st); break;
+        case 2: slab_launch_t<PREC, false, 8>(r, smem, st); break;
+        default: slab_launch_t<PREC, true, 8>(r, smem, st); break;
     }
 }
 
 void hx_slab_launch(int prec, const SlabRun& r, cudaStream_t st) {
     if (r.n_tiles == 0) return;
     const size_t smem = (size_t)r.n_lut * (r.lut_real ? 1 : 2) * (prec == 0 ? 8 : 4);
-    if (prec == 0) {
-        if (r.hints) slab_launch_t<0, true>(r, smem, st);
-        else slab_launch_t<0, false>(r, smem, st);
-    } else {
-        if (r.hints) slab_launch_t<1, true>(r, smem, st);
-        else slab_launch_t<1, false>(r, smem, st);
-    }
+    if (prec == 0) slab_launch_p<0>(r, smem, st);
+    else slab_launch_p<1>(r, smem, st);
 }
 
 }  // namespace edgpu

@@ -686,8 +686,8 @@ class OperatorRepresentation:
         return int(a.value), int(b.value), int(c.value)
 
     def slab_use(self, precision="mixed", use=None) -> int:
-        """Whether products read the slab table: 0 (no), 1 (yes), 2 (yes, with cache hints); sets it
-        when use is given (False/True or 0, 1, 2)."""
+        """Whether products read the slab table: 0 (no), or 1 + v for the variant v (bit 0: cache
+        hints, bit 1: eight entries per lane and step); sets it when use is given (False/True or 0 to 4)."""
         cur = ctypes.c_int32()
         check(lib().edgpu_op_slab_use(self._h, _prec(precision), -1 if use is None else int(use),
                                       ctypes.byref(cur)))

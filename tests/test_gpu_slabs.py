@@ -70,8 +70,8 @@ def test_slab_product_chain(L, k, coupled):
     E.mul_(y2, opr, xd, precision="mixed")
     torch.cuda.synchronize()
     assert torch.equal(y, y2)
-    # with cache hints: the same arithmetic in the same order, the same bits
-    for mode in (2,):
+    # the other variants (cache hints, eight entries per step): the same arithmetic in the same order
+    for mode in (2, 3, 4):
         assert opr.slab_use("mixed", mode) == mode
         y2.fill_(float("nan"))
         E.mul_(y2, opr, xd, precision="mixed")
@@ -101,7 +101,7 @@ def test_slab_product_chain(L, k, coupled):
     E.mul_(yd64, opr, x64, precision="fp64")
     torch.cuda.synchronize()
     assert relerr(yd64.cpu().numpy(), want) < 1e-12
-    for mode in (2,):
+    for mode in (2, 3, 4):
         opr.slab_use("fp64", mode)
         yd64b = torch.full_like(x64, float("nan"))
         E.mul_(yd64b, opr, x64, precision="fp64")
