@@ -1006,9 +1006,9 @@ def main():
                          "profiler run with --profile-from-start off: the autotuners run unprofiled)")
     ap.add_argument("--batch-launch", type=int, default=7, choices=[0, 1, 2, 3, 5, 6, 7],
                     help="batched workload with --tiling: the batch launch mode (edgpu_batch_set_launch)")
-    ap.add_argument("--slab-mode", type=int, default=1, choices=[1, 2, 3, 4],
+    ap.add_argument("--slab-mode", type=int, default=1, choices=[1, 2, 3, 4, 5, 6],
                     help="with --tiling: the slab product's variant (1 plain, 2 cache hints, 3 eight entries "
-                         "per step, 4 both)")
+                         "per step, 4 both, 5 two lanes per row, 6 four lanes per row)")
     ap.add_argument("--slab-mb", type=float, default=112.0,
                     help="column slabs of this many MB of complex64 x (0: no slab table)")
     ap.add_argument("--no-pair", action="store_true", help="test every term per row instead of the pair-flip schedule")

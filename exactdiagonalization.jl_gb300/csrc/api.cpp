@@ -2363,7 +2363,7 @@ int edgpu_op_slab_use(edgpu_op oh, int32_t precision, int32_t use, int32_t* curr
     edgpu_op_s* op = as_op(oh);
     OpLock lk_(op->hs.mu);
     check_prec(precision);
-    require(use >= -1 && use <= 4, EDGPU_ERR_ARG, "use must be -1 (query) or 0 to 4");
+    require(use >= -1 && use <= 6, EDGPU_ERR_ARG, "use must be -1 (query) or 0 to 6");
     require(use <= 0 || op->slab.tab, EDGPU_ERR_STATE, "no slab table (edgpu_op_build_slabs)");
     if (use >= 0) {
         op->slab_use[precision] = use > 0 ? 1 : 0;
@@ -2452,7 +2452,7 @@ int edgpu_op_autotune(edgpu_op oh, int32_t precision, int32_t* rows_per_tile_out
     const bool mapped = op->space->d_map != nullptr;
     if (pair_ok) {
         if (op->slab.tab)
-            for (int hint : {0, 1, 2, 3}) cands.push_back({1, 4, 1, -1, 0, 0, 1, hint});
+            for (int hint : {0, 1, 2, 3, 4, 5}) cands.push_back({1, 4, 1, -1, 0, 0, 1, hint});
         if (op->d_tab) {
             for (int nt : {8, 4, 2})
                 for (int pf : {0, 4, 64}) cands.push_back({1, nt, 1, -1, pf, 0});

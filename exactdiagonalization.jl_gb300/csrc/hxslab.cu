@@ -201,10 +201,12 @@ __device__ __forceinline__ void st_stream(T* p, T v) {
     else *p = v;
 }
 
-// One pass of the product: a warp per tile of 32 rows, one lane per row; the lane adds its row's
-// entries of this pass (NT per step, loads then gathers), then adds the sum to y (the first pass
-// writes it, the last adds the diagonal term too and may write complex128 to y_c128 instead).
-template <int PREC, bool REAL, int NT, bool CH>
+// One pass of the product: a warp per tile of 32 rows with one lane per row (LPR = 1), or per part of
+// 32 / LPR rows of a tile with LPR lanes per row (lane sub of a row takes the row's entries sub,
+// sub + LPR, ...; the partial sums are added by a fixed butterfly).  A lane adds its entries of this
+// pass (NT per step, loads then gathers); the row's sum is then added to y (the first pass writes it,
+// the last adds the diagonal term too and may write complex128 to y_c128 instead).
+template <int PREC, bool REAL, int NT, bool CH, int LPR>
 __global__ void __launch_bounds__(HX_THREADS) hx_slab_kernel(const SlabRun r) {
     typedef typename Cx<PREC>::V V;
     typedef typename Cx<PREC>::R R;
@@ -225,29 +227,39 @@ __global__ void __launch_bounds__(HX_THREADS) hx_slab_kernel(const SlabRun r) {
     const unsigned* __restrict__ tab = r.tab;
     V* y = (V*)r.y;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    const int sub = lane & (LPR - 1);
     const bool to_c128 = r.last && r.y_c128 != nullptr;
-    for (long long tile = (long long)blockIdx.x * wpb + warp; tile < r.n_tiles; tile += (long long)gridDim.x * wpb) {
-        const long long row = tile * 32 + lane;
-        const bool act = row < r.n_rows;
-        const int cnt = act ? (int)ld_stream<CH>(r.cnt + row) : 0;
-        int incl = cnt;
+    const long long n_parts = r.n_tiles * LPR;
+    for (long long part = (long long)blockIdx.x * wpb + warp; part < n_parts; part += (long long)gridDim.x * wpb) {
+        const long long tile = part / LPR;
+        // the counts of the tile's 32 rows and their exclusive prefix
+        const long long row32 = tile * 32 + lane;
+        const int c32 = row32 < r.n_rows ? (int)ld_stream<CH>(r.cnt + row32) : 0;
+        int incl = c32;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
             const int u = __shfl_up_sync(0xffffffffu, incl, d);
             if (lane >= d) incl += u;
         }
-        const long long start = (long long)ld_stream<CH>(r.off + tile) + (incl - cnt);
+        // this lane's row in the tile
+        const int rl = LPR == 1 ? lane : (int)(part % LPR) * (32 / LPR) + lane / LPR;
+        const int cnt = LPR == 1 ? c32 : __shfl_sync(0xffffffffu, c32, rl);
+        const int excl = LPR == 1 ? incl - c32 : __shfl_sync(0xffffffffu, incl - c32, rl);
+        const long long row = tile * 32 + rl;
+        const bool act = row < r.n_rows;
+        const long long start = (long long)ld_stream<CH>(r.off + tile) + excl;
         V acc = czero<V>();
-        for (int j = 0; __any_sync(0xffffffffu, j < cnt); j += NT) {
+        for (int j = sub; __any_sync(0xffffffffu, j < cnt); j += NT * LPR) {
             unsigned e[NT];
 #pragma unroll
-            for (int h = 0; h < NT; ++h) e[h] = (j + h < cnt) ? __ldg(tab + start + j + h) : 0u;
+            for (int h = 0; h < NT; ++h) e[h] = (j + h * LPR < cnt) ? __ldg(tab + start + j + h * LPR) : 0u;
             V xv[NT];
 #pragma unroll
-            for (int h = 0; h < NT; ++h) xv[h] = (j + h < cnt) ? ld_gather<CH>(xs + (e[h] & r.colmask)) : czero<V>();
+            for (int h = 0; h < NT; ++h)
+                xv[h] = (j + h * LPR < cnt) ? ld_gather<CH>(xs + (e[h] & r.colmask)) : czero<V>();
 #pragma unroll
             for (int h = 0; h < NT; ++h) {
-                if (j + h >= cnt) continue;
+                if (j + h * LPR >= cnt) continue;
                 const unsigned id = e[h] >> r.colbits;
                 if (REAL) {
                     const R f = lr[id];
@@ -258,7 +270,12 @@ __global__ void __launch_bounds__(HX_THREADS) hx_slab_kernel(const SlabRun r) {
                 }
             }
         }
-        if (!act) continue;
+#pragma unroll
+        for (int d = 1; d < LPR; d <<= 1) {
+            acc.x += __shfl_xor_sync(0xffffffffu, acc.x, d);
+            acc.y += __shfl_xor_sync(0xffffffffu, acc.y, d);
+        }
+        if (!act || sub != 0) continue;
         // passes add their sums in order; the last adds the diagonal term diag x (so that a pass needs
         // only its own slab of x, the last one all of it)
         V t;
@@ -363,25 +380,28 @@ void hx_slab_scan(const unsigned* tile_sum, unsigned* off, int n_pass, long long
     if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("slab scan: ") + cudaGetErrorString(e));
 }
 
-template <int PREC, bool CH, int NT>
+template <int PREC, bool CH, int NT, int LPR>
 void slab_launch_t(const SlabRun& r, size_t smem, cudaStream_t st) {
     if (r.lut_real) {
-        auto k = hx_slab_kernel<PREC, true, NT, CH>;
-        slab_pdl_launch(k, r, slab_blocks(k, smem, r.n_tiles), smem, st);
+        auto k = hx_slab_kernel<PREC, true, NT, CH, LPR>;
+        slab_pdl_launch(k, r, slab_blocks(k, smem, r.n_tiles * LPR), smem, st);
     } else {
-        auto k = hx_slab_kernel<PREC, false, NT, CH>;
-        slab_pdl_launch(k, r, slab_blocks(k, smem, r.n_tiles), smem, st);
+        auto k = hx_slab_kernel<PREC, false, NT, CH, LPR>;
+        slab_pdl_launch(k, r, slab_blocks(k, smem, r.n_tiles * LPR), smem, st);
     }
 }
 
-// hints: bit 0 the cache hints, bit 1 eight entries per lane and step instead of four
+// hints: 0 to 3 one lane per row (bit 0 the cache hints, bit 1 eight entries per lane and step
+// instead of four); 4 and 5: two and four lanes per row, four entries per lane and step
 template <int PREC>
 void slab_launch_p(const SlabRun& r, size_t smem, cudaStream_t st) {
-    switch (r.hints & 3) {
-        case 0: slab_launch_t<PREC, false, 4>(r, smem, st); break;
-        case 1: slab_launch_t<PREC, true, 4>(r, smem, st); break;
-        case 2: slab_launch_t<PREC, false, 8>(r, smem, st); break;
-        default: slab_launch_t<PREC, true, 8>(r, smem, st); break;
+    switch (r.hints) {
+        case 0: slab_launch_t<PREC, false, 4, 1>(r, smem, st); break;
+        case 1: slab_launch_t<PREC, true, 4, 1>(r, smem, st); break;
+        case 2: slab_launch_t<PREC, false, 8, 1>(r, smem, st); break;
+        case 3: slab_launch_t<PREC, true, 8, 1>(r, smem, st); break;
+        case 4: slab_launch_t<PREC, false, 4, 2>(r, smem, st); break;
+        default: slab_launch_t<PREC, false, 4, 4>(r, smem, st); break;
     }
 }
 

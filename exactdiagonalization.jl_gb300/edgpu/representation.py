@@ -686,8 +686,10 @@ class OperatorRepresentation:
         return int(a.value), int(b.value), int(c.value)
 
     def slab_use(self, precision="mixed", use=None) -> int:
-        """Whether products read the slab table: 0 (no), or 1 + v for the variant v (bit 0: cache
-        hints, bit 1: eight entries per lane and step); sets it when use is given (False/True or 0 to 4)."""
+        """Whether products read the slab table: 0 (no), or 1 + v for the variant v; sets it when use is
+        given (False/True or 0 to 6).  v = 0 to 3: one lane per row (bit 0: cache hints, bit 1: eight
+        entries per lane and step), bit-identical; v = 4, 5: two, four lanes per row (their sums are
+        added in another fixed order, so they differ from v = 0 to 3 by rounding)."""
         cur = ctypes.c_int32()
         check(lib().edgpu_op_slab_use(self._h, _prec(precision), -1 if use is None else int(use),
                                       ctypes.byref(cur)))

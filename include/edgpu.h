@@ -247,11 +247,13 @@ int edgpu_op_free_slabs(edgpu_op op);
 /* Slabs (passes), columns per slab and entries of the slab table; zeros without one. */
 int edgpu_op_slabs_info(edgpu_op op, int32_t* passes, int64_t* columns_per_slab, int64_t* entries);
 /* Whether products of this precision read the slab table, and how: use = 0 (no), or 1 + v for the
- * variant v = 0 to 3 (bit 0: cache hints, the gathers of x cached in L2 only and the streamed counts,
- * offsets and y evict-first; bit 1: eight entries per lane and step instead of four) sets it (1 to 4
- * need the table: EDGPU_ERR_STATE otherwise), -1 only queries; *current = the setting.  All variants
- * give the same results bit for bit.  Building the table sets 1 for both precisions; the autotuner
- * times the variants against the one-pass schedules. */
+ * variant v = 0 to 5 sets it (1 to 6 need the table: EDGPU_ERR_STATE otherwise), -1 only queries;
+ * *current = the setting.  v = 0 to 3: one lane per row (bit 0: cache hints, the gathers of x cached
+ * in L2 only and the streamed counts, offsets and y evict-first; bit 1: eight entries per lane and
+ * step instead of four), all four bit-identical; v = 4 and 5: two and four lanes per row (for sectors
+ * too small to fill the GPU), whose partial sums are added in another fixed order, so their results
+ * differ from v = 0 to 3 by rounding (each is deterministic).  Building the table sets 1 for both
+ * precisions; the autotuner times the variants against the one-pass schedules. */
 int edgpu_op_slab_use(edgpu_op op, int32_t precision, int32_t use, int32_t* current);
 /* Sparse matrix of the representation, assembled on the device in FP64: rows sorted by column,
  * entries of equal column summed, entries with |value| < tol dropped (tol: the reference's

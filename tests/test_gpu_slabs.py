@@ -77,6 +77,19 @@ def test_slab_product_chain(L, k, coupled):
         E.mul_(y2, opr, xd, precision="mixed")
         torch.cuda.synchronize()
         assert torch.equal(y, y2), mode
+    # two and four lanes per row: another fixed order of the sums, deterministic, equal within rounding
+    for mode in (5, 6):
+        assert opr.slab_use("mixed", mode) == mode
+        y2.fill_(float("nan"))
+        E.mul_(y2, opr, xd, precision="mixed")
+        y2b = torch.full_like(xd, float("nan"))
+        E.mul_(y2b, opr, xd, precision="mixed")
+        torch.cuda.synchronize()
+        assert torch.equal(y2, y2b), mode
+        assert relerr(y2.cpu().numpy().astype(np.complex128), want) < 1e-5, mode
+        yh5 = np.zeros(N, dtype=np.complex128)
+        E.mul_(yh5, opr, x, precision="mixed")
+        assert relerr(yh5, want) < 1e-5, mode
     assert opr.slab_use("mixed", 1) == 1
     yn = y.cpu().numpy().astype(np.complex128)
     assert relerr(yn, want) < 1e-5
@@ -107,6 +120,12 @@ def test_slab_product_chain(L, k, coupled):
         E.mul_(yd64b, opr, x64, precision="fp64")
         torch.cuda.synchronize()
         assert torch.equal(yd64, yd64b), mode
+    for mode in (5, 6):
+        opr.slab_use("fp64", mode)
+        yd64b = torch.full_like(x64, float("nan"))
+        E.mul_(yd64b, opr, x64, precision="fp64")
+        torch.cuda.synchronize()
+        assert relerr(yd64b.cpu().numpy(), want) < 1e-12, mode
     opr.slab_use("fp64", 1)
     yf = np.zeros(N, dtype=np.complex128)
     E.mul_(yf, opr, x, precision="fp64")
