@@ -690,7 +690,8 @@ def run_gpu(args, wl):
                        "slab_table": dict(slab_info or {"built": False},
                                           used={"mixed": opr.slab_use("mixed") if slab_info and slab_info.get("built") else 0,
                                                 "fp64": opr.slab_use("fp64") if slab_info and slab_info.get("built") else 0},
-                                          use_codes="0 none, 1 slab product, 2 with cache hints, 3 eight entries per step, 4 both"),
+                                          use_codes="0 none, 1 slab product, 2 with cache hints, 3 eight entries "
+                                                    "per step, 4 both, 5 two lanes per row, 6 four lanes per row"),
                        "setup_s": t_space, "search_directory": dir_stats, "parent_map": map_info},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_src,
