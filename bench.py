@@ -178,21 +178,24 @@ def build_tables(oprs, spaces, args):
 
 def build_slabs(opr, N, args):
     """Column-slab table of the operator (the autotuner times it against the one-pass schedules), unless
-    --slab-mb 0:
-    {"built", "passes", "columns_per_slab", "entries", "bytes", "build_s"} or None."""
+    --slab-mb 0; --slab-scaling picks its layout:
+    {"built", "passes", "columns_per_slab", "entries", "bytes", "build_s", "scaled"} or None."""
     import torch
     if args.slab_mb <= 0 or not hasattr(opr, "build_slabs"):
         return None
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     free, _ = torch.cuda.mem_get_info()
+    opr.slab_scaling(args.slab_scaling)
     built = opr.build_slabs(slab_bytes=int(args.slab_mb * (1 << 20)), max_bytes=int(0.8 * free))
     dt = time.perf_counter() - t0
     if not built:
         return {"built": False}
     passes, wc, entries = opr.slabs_info
+    scaled = opr.slab_scaling()
     return {"built": True, "passes": passes, "columns_per_slab": wc, "entries": entries,
-            "bytes": entries * 4 + passes * N + passes * ((N + 31) // 32) * 4, "build_s": dt}
+            "bytes": entries * 4 + passes * N + passes * ((N + 31) // 32) * 4 + (17 * N if scaled else 0),
+            "build_s": dt, "scaled": scaled}
 
 
 def build_gpu_operator(wl):
@@ -733,11 +736,13 @@ def run_gpu_batch(args, wl):
         slab_info = {"built": True, "passes": [], "entries": 0}
         for o in oprs:
             free, _ = torch.cuda.mem_get_info()
+            o.slab_scaling(args.slab_scaling)
             if not o.build_slabs(slab_bytes=int(args.slab_mb * (1 << 20)), max_bytes=int(0.5 * free)):
                 slab_info = {"built": False}
                 break
             slab_info["passes"].append(o.slabs_info[0])
             slab_info["entries"] += o.slabs_info[2]
+            slab_info["scaled_sectors"] = slab_info.get("scaled_sectors", 0) + int(o.slab_scaling())
         if slab_info["built"]:
             slab_info["passes"] = sorted(set(slab_info["passes"]))
         slab_info["build_s"] = time.perf_counter() - t0
@@ -1010,6 +1015,9 @@ def main():
     ap.add_argument("--slab-mode", type=int, default=1, choices=[1, 2, 3, 4, 5, 6],
                     help="with --tiling: the slab product's variant (1 plain, 2 cache hints, 3 eight entries "
                          "per step, 4 both, 5 two lanes per row, 6 four lanes per row)")
+    ap.add_argument("--slab-scaling", type=int, default=0, choices=[0, 1, 2],
+                    help="slab table layout (edgpu_op_slab_scaling): 0 scaled on sectors of 2^22 rows or more "
+                         "where that saves passes or the coefficients are complex, 1 never, 2 always")
     ap.add_argument("--slab-mb", type=float, default=112.0,
                     help="column slabs of this many MB of complex64 x (0: no slab table)")
     ap.add_argument("--no-pair", action="store_true", help="test every term per row instead of the pair-flip schedule")

@@ -218,7 +218,16 @@ struct edgpu_op_s {
         DevBuf<float> lut;                  // coefficients by id: float, or (re, im) when !lut_real
         DevBuf<double> lut64;               // the same in FP64
         int lut_real = 1;
+        int lut_mode = 0;                   // SlabRun::lut_mode
+        // scaled table: ids carry no orbit-size indices; x is scaled by sqrt(|O_c|) into xsc before the
+        // passes and row r of the result by 1 / sqrt(|O_r|) in the last pass
+        int scaled = 0;
+        unsigned char* cls = nullptr;       // [dim] orbit-size index of every representative
+        DevBuf<float> sc32;                 // [2 nd] sqrt(|O|), then 1 / sqrt(|O|), by orbit-size index
+        DevBuf<double> sc64;
+        DevBuf<double> xsc;                 // [2 dim] the scaled x (complex64 or complex128)
     } slab;
+    int slab_scaling = 0;             // scaled slab tables: 0 for sectors of 2^22 rows or more, 1 never, 2 always
     int slab_use[2] = {0, 0};         // [precision]: products read the slab table (chosen by the autotuner)
     // host-buffer slab products: a second stream converting x slab by slab while the passes run
     cudaStream_t aux_st = nullptr;
@@ -246,8 +255,12 @@ struct edgpu_op_s {
         if (slab.tab) cudaFree(slab.tab);
         if (slab.counts) cudaFree(slab.counts);
         if (slab.off) cudaFree(slab.off);
+        if (slab.cls) cudaFree(slab.cls);
         slab.lut.release();
         slab.lut64.release();
+        slab.sc32.release();
+        slab.sc64.release();
+        slab.xsc.release();
         slab = Slab();
         slab_use[0] = slab_use[1] = 0;
     }
@@ -971,7 +984,9 @@ void invalidate_blobs(edgpu_op_s* op) {
 // Coefficient tables of the slab product (FP32 and FP64) for the current coupling values, written
 // into the tables' existing buffers: id = ((amplitude id x den + character index) x nd + orbit-size
 // index of the row) x nd + orbit-size index of the column, coefficient = J_c u_a chi sqrt(|O_c| / |O_r|)
-// as the one-pass product forms it (hx_bond.cuh), here in FP64 and rounded once.
+// as the one-pass product forms it (hx_bond.cuh), here in FP64 and rounded once.  A scaled table's
+// id is amplitude id x den + character index and its coefficient J_c u_a chi: the ratio's factors
+// sqrt(|O_c|) and 1 / sqrt(|O_r|) go to x and to the row's result.
 void slab_refresh_lut(edgpu_op_s* op) {
     auto& S = op->slab;
     if (!S.tab) return;
@@ -982,11 +997,13 @@ void slab_refresh_lut(edgpu_op_s* op) {
     std::vector<float> h((size_t)S.n_ids * 2, 0.f);
     std::vector<double> h64((size_t)S.n_ids * 2, 0.0);
     for (int id = 0; id < S.n_ids; ++id) {
-        int rest = id;
-        const int sxc = rest % S.nd;
-        rest /= S.nd;
-        const int sxr = rest % S.nd;
-        rest /= S.nd;
+        int rest = id, sxc = 0, sxr = 0;
+        if (!S.scaled) {
+            sxc = rest % S.nd;
+            rest /= S.nd;
+            sxr = rest % S.nd;
+            rest /= S.nd;
+        }
         const int ph = rest % S.den;
         const int a = rest / S.den;
         if (a >= na) continue;
@@ -994,7 +1011,8 @@ void slab_refresh_lut(edgpu_op_s* op) {
         const double ur = S.amp_unit[2 * a] * J, ui = S.amp_unit[2 * a + 1] * J;
         const double ang = 2.0 * M_PI * (double)ph / (double)S.den;
         const double cr = std::cos(ang), ci = std::sin(ang);
-        const double f = std::sqrt((double)S.divs[sxc] / (double)S.divs[sxr]);
+        // the orbit-size ratio; on a scaled table it is applied to x and y instead
+        const double f = S.scaled ? 1.0 : std::sqrt((double)S.divs[sxc] / (double)S.divs[sxr]);
         const double re = (ur * cr - ui * ci) * f, im = (ur * ci + ui * cr) * f;
         if (real) {
             h[id] = (float)re;
@@ -1007,6 +1025,9 @@ void slab_refresh_lut(edgpu_op_s* op) {
         }
     }
     S.lut_real = real ? 1 : 0;
+    // registers for a few real coefficients, one copy per bank group for a small complex table (its
+    // lookups then never conflict), else one shared-memory copy
+    S.lut_mode = (real && S.n_ids <= SLAB_REG_LUT) ? 2 : (!real && (size_t)S.n_ids * 128 <= (size_t)SLAB_REP_BYTES) ? 1 : 0;
     EDGPU_CUDA(cudaMemcpy(S.lut.p, h.data(), (size_t)S.n_ids * (real ? 1 : 2) * sizeof(float), cudaMemcpyHostToDevice));
     EDGPU_CUDA(cudaMemcpy(S.lut64.p, h64.data(), (size_t)S.n_ids * (real ? 1 : 2) * sizeof(double),
                           cudaMemcpyHostToDevice));
@@ -1057,10 +1078,36 @@ bool slab_active(const edgpu_op_s* op, int prec, int dir, int mode, int rows) {
 
 // The column-slab product: one launch per slab (hxslab.cu); the last pass adds the diagonal term and
 // writes complex128 to y_c128 when given.  With ready != null, pass q first waits for ready[q] (the
-// event after which slab q of x, and for the last pass all of x, is in place).
+// event after which slab q of x, and for the last pass all of x, is in place).  On a scaled table x
+// is the caller's unscaled vector, unless pre_scaled: the caller has written the scaled x to the
+// table's buffer (slab q by the event ready[q]).  Otherwise slab q of x is scaled into that buffer on
+// the handle's second stream while the earlier passes run.
 void launch_slab_passes(edgpu_op_s* op, int prec, const Blob& B, const void* x, void* y, int accumulate,
-                        void* y_c128, int acc_c128, cudaStream_t st, const cudaEvent_t* ready) {
-    const auto& S = op->slab;
+                        void* y_c128, int acc_c128, cudaStream_t st, const cudaEvent_t* ready,
+                        bool pre_scaled = false) {
+    auto& S = op->slab;
+    const size_t esz = prec == EDGPU_FP64 ? 16 : 8;
+    const void* scale = prec == EDGPU_FP64 ? (const void*)S.sc64.p : (const void*)S.sc32.p;
+    if (S.scaled) {
+        if (!pre_scaled) {
+            const int64_t n = B.tmpl.n_rows;
+            if (S.n_pass == 1) {
+                launch_slab_xscale(prec, x, S.cls, scale, S.xsc.p, 0, n, st);
+                ready = nullptr;
+            } else {
+                op->ensure_slab_events(S.n_pass);
+                EDGPU_CUDA(cudaEventRecord(op->aux_fork, st));
+                EDGPU_CUDA(cudaStreamWaitEvent(op->aux_st, op->aux_fork, 0));
+                for (int q = 0; q < S.n_pass; ++q) {
+                    const int64_t c0 = (int64_t)q * S.wc, c1 = std::min<int64_t>(n, c0 + S.wc);
+                    launch_slab_xscale(prec, x, S.cls, scale, S.xsc.p, c0, c1, op->aux_st);
+                    EDGPU_CUDA(cudaEventRecord(op->slab_ready[q], op->aux_st));
+                }
+                ready = op->slab_ready.data();
+            }
+        }
+        x = S.xsc.p;
+    }
     SlabRun r{};
     r.x = x;
     r.y = y;
@@ -1068,6 +1115,11 @@ void launch_slab_passes(edgpu_op_s* op, int prec, const Blob& B, const void* x, 
     r.lut = prec == EDGPU_FP64 ? (const void*)S.lut64.p : (const void*)S.lut.p;
     r.n_lut = S.n_ids;
     r.lut_real = S.lut_real;
+    r.lut_mode = S.lut_mode;
+    r.scaled = S.scaled;
+    r.cls = S.cls;
+    r.scale = scale;
+    r.nd = S.nd;
     r.n_rows = B.tmpl.n_rows;
     r.n_tiles = (r.n_rows + 31) / 32;
     r.colbits = S.colbits;
@@ -1081,7 +1133,7 @@ void launch_slab_passes(edgpu_op_s* op, int prec, const Blob& B, const void* x, 
         r.cnt = S.counts + (size_t)q * r.n_rows;
         r.off = S.off + (size_t)q * r.n_tiles;
         r.tab = S.tab + S.base[q];
-        r.xs = (const char*)x + (size_t)q * S.wc * (prec == EDGPU_FP64 ? 16 : 8);
+        r.xs = (const char*)x + (size_t)q * S.wc * esz;
         r.first = q == 0;
         r.last = q == S.n_pass - 1;
         hx_slab_launch(prec, r, st);
@@ -2251,16 +2303,38 @@ int edgpu_op_build_slabs(edgpu_op oh, int64_t slab_bytes, int64_t max_bytes, int
     for (int d = 1; d <= sp.group.G; ++d)
         if (sp.group.G % d == 0) S.divs.push_back(d);
     S.nd = (int)S.divs.size();
-    const long long n_ids = (long long)n_amp * S.den * S.nd * S.nd;
-    int idbits = 1;
-    while (((long long)1 << idbits) < n_ids) ++idbits;
-    const int colbits = 32 - idbits;
-    if (colbits < 12 || n_ids * 8 > 48 * 1024 || n_amp > 65535) {
+    // columns per slab and passes of a layout with n_ids coefficient ids (0 passes: ids too many)
+    auto layout = [&](long long n_ids, long long& wc) {
+        int idbits = 1;
+        while (((long long)1 << idbits) < n_ids) ++idbits;
+        if (32 - idbits < 12 || n_ids * 8 > 48 * 1024) return 0;
+        wc = std::max<long long>(1024, std::min<long long>(slab_bytes / 8, (long long)1 << (32 - idbits)));
+        return (int)((sp.dim + wc - 1) / wc);
+    };
+    bool complex_coef = S.den > 1;
+    for (size_t a = 0; a < S.amp_cid.size(); ++a) complex_coef = complex_coef || S.amp_unit[2 * a + 1] != 0.0;
+    const long long ids_full = (long long)n_amp * S.den * S.nd * S.nd, ids_scaled = (long long)n_amp * S.den;
+    long long wc_full = 0, wc_scaled = 0;
+    const int pass_full = layout(ids_full, wc_full), pass_scaled = layout(ids_scaled, wc_scaled);
+    // the scaled layout pays a scaling pass over x per product; by default it is taken on sectors of
+    // 2^22 rows or more where it saves passes or replaces a complex coefficient table (whose lookups
+    // conflict in shared memory)
+    bool scaled = false;
+    if (S.nd > 1 && pass_scaled > 0) {
+        if (op->slab_scaling == 2) scaled = true;
+        else if (op->slab_scaling == 0)
+            scaled = pass_full == 0 || (sp.dim >= ((int64_t)1 << 22) && (pass_scaled < pass_full || complex_coef));
+    }
+    const long long n_ids = scaled ? ids_scaled : ids_full;
+    const long long wc = scaled ? wc_scaled : wc_full;
+    const int n_pass = scaled ? pass_scaled : pass_full;
+    if (n_pass == 0 || n_amp > 65535) {
         op->free_slabs();
         return EDGPU_OK;
     }
-    const long long wc = std::max<long long>(1024, std::min<long long>(slab_bytes / 8, (long long)1 << colbits));
-    const int n_pass = (int)((sp.dim + wc - 1) / wc);
+    int idbits = 1;
+    while (((long long)1 << idbits) < n_ids) ++idbits;
+    const int colbits = 32 - idbits;
     const long long n_tiles = (sp.dim + 31) / 32;
     if (n_pass > 64) {
         op->free_slabs();
@@ -2282,8 +2356,10 @@ int edgpu_op_build_slabs(edgpu_op oh, int64_t slab_bytes, int64_t max_bytes, int
     sb.n_tiles = n_tiles;
     sb.colbits = colbits;
     sb.n_slots = n_slots;
+    sb.scaled = scaled ? 1 : 0;
     sb.o_ctr = (int)align16(B.smem_bond);
-    const size_t meta = (size_t)n_pass * sp.dim + (size_t)n_pass * n_tiles * 4;
+    // counts and tile offsets; a scaled table's orbit-size bytes and scaled-x buffer (complex128)
+    const size_t meta = (size_t)n_pass * sp.dim + (size_t)n_pass * n_tiles * 4 + (scaled ? (size_t)sp.dim * 17 : 0);
     if ((double)meta > (double)max_bytes) {
         op->free_slabs();
         return EDGPU_OK;
@@ -2295,6 +2371,11 @@ int edgpu_op_build_slabs(edgpu_op oh, int64_t slab_bytes, int64_t max_bytes, int
         EDGPU_CUDA(cudaMalloc(&S.counts, std::max<size_t>((size_t)n_pass * sp.dim, 16)));
         EDGPU_CUDA(cudaMalloc(&S.off, std::max<size_t>((size_t)n_pass * n_tiles * 4, 16)));
         tile_sum.ensure((size_t)n_pass * n_tiles);
+        if (scaled) {
+            EDGPU_CUDA(cudaMalloc(&S.cls, (size_t)sp.dim));
+            S.xsc.ensure(2 * (size_t)sp.dim);
+        }
+        sb.cls = S.cls;
         sb.counts = S.counts;
         sb.tile_sum = tile_sum.p;
         hx_slab_build(sp.w32, prec, 1, p, sb, (size_t)sb.o_ctr + (size_t)n_pass * HX_THREADS, st);
@@ -2325,6 +2406,22 @@ int edgpu_op_build_slabs(edgpu_op oh, int64_t slab_bytes, int64_t max_bytes, int
         S.wc = wc;
         S.colbits = colbits;
         S.n_ids = (int)n_ids;
+        S.scaled = scaled ? 1 : 0;
+        if (scaled && n_pass > 1) op->ensure_slab_events(n_pass);
+        if (scaled) {
+            std::vector<float> f(2 * (size_t)S.nd);
+            std::vector<double> d(2 * (size_t)S.nd);
+            for (int k = 0; k < S.nd; ++k) {
+                d[k] = std::sqrt((double)S.divs[k]);
+                d[S.nd + k] = 1.0 / std::sqrt((double)S.divs[k]);
+                f[k] = (float)d[k];
+                f[S.nd + k] = (float)d[S.nd + k];
+            }
+            S.sc32.ensure(f.size());
+            S.sc64.ensure(d.size());
+            EDGPU_CUDA(cudaMemcpy(S.sc32.p, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
+            EDGPU_CUDA(cudaMemcpy(S.sc64.p, d.data(), d.size() * sizeof(double), cudaMemcpyHostToDevice));
+        }
         S.lut.ensure((size_t)n_ids * 2);
         S.lut64.ensure((size_t)n_ids * 2);
         slab_refresh_lut(op);
@@ -2355,6 +2452,16 @@ int edgpu_op_slabs_info(edgpu_op oh, int32_t* passes, int64_t* columns_per_slab,
     if (passes) *passes = on ? op->slab.n_pass : 0;
     if (columns_per_slab) *columns_per_slab = on ? op->slab.wc : 0;
     if (entries) *entries = on ? op->slab.n : 0;
+    API_END
+}
+
+int edgpu_op_slab_scaling(edgpu_op oh, int32_t mode, int32_t* scaled) {
+    API_BEGIN
+    edgpu_op_s* op = as_op(oh);
+    OpLock lk_(op->hs.mu);
+    require(mode >= -1 && mode <= 2, EDGPU_ERR_ARG, "mode must be -1 (query), 0, 1 or 2");
+    if (mode >= 0) op->slab_scaling = mode;
+    if (scaled) *scaled = op->slab.tab ? op->slab.scaled : 0;
     API_END
 }
 
@@ -2767,13 +2874,16 @@ static void host_product_issue(edgpu_op_s* op, int prec, int dir, const double* 
             op->ensure_slab_events(S.n_pass);
             EDGPU_CUDA(cudaEventRecord(op->aux_fork, st));
             EDGPU_CUDA(cudaStreamWaitEvent(op->aux_st, op->aux_fork, 0));
+            // (on a scaled table the conversion writes the scaled x to the table's buffer)
+            float* xdst = S.scaled ? (float*)S.xsc.p : op->x32.p;
             for (int q = 0; q < S.n_pass; ++q) {
                 const int64_t c0 = (int64_t)q * S.wc, c1 = std::min<int64_t>(n, c0 + S.wc);
-                launch_c128_to_c64(c1 - c0, xd + 2 * c0, op->x32.p + 2 * c0, op->aux_st);
+                if (S.scaled) launch_slab_xscale_c128_c64(xd, S.cls, S.sc32.p, xdst, c0, c1, op->aux_st);
+                else launch_c128_to_c64(c1 - c0, xd + 2 * c0, xdst + 2 * c0, op->aux_st);
                 EDGPU_CUDA(cudaEventRecord(op->slab_ready[q], op->aux_st));
             }
-            launch_slab_passes(op, prec, op->blob[prec][dir][0], op->x32.p, op->y32.p, 0, yd, accumulate, st,
-                               op->slab_ready.data());
+            launch_slab_passes(op, prec, op->blob[prec][dir][0], xdst, op->y32.p, 0, yd, accumulate, st,
+                               op->slab_ready.data(), true);
             return;
         }
         if (xd && yd) {
@@ -2801,14 +2911,16 @@ static void host_product_issue(edgpu_op_s* op, int prec, int dir, const double* 
                 op->ensure_slab_events(S.n_pass);
                 EDGPU_CUDA(cudaEventRecord(op->aux_fork, st));
                 EDGPU_CUDA(cudaStreamWaitEvent(op->aux_st, op->aux_fork, 0));
+                // (on a scaled table each copied slab is then scaled into the table's buffer)
                 for (int q = 0; q < S.n_pass; ++q) {
                     const int64_t c0 = (int64_t)q * S.wc, c1 = std::min<int64_t>(n, c0 + S.wc);
                     EDGPU_CUDA(cudaMemcpyAsync(op->x64.p + 2 * c0, x + 2 * c0, (size_t)(c1 - c0) * 16,
                                                cudaMemcpyHostToDevice, op->aux_st));
+                    if (S.scaled) launch_slab_xscale(prec, op->x64.p, S.cls, S.sc64.p, S.xsc.p, c0, c1, op->aux_st);
                     EDGPU_CUDA(cudaEventRecord(op->slab_ready[q], op->aux_st));
                 }
-                launch_slab_passes(op, prec, op->blob[prec][dir][0], op->x64.p, op->y64.p, 0, yd, accumulate, st,
-                                   op->slab_ready.data());
+                launch_slab_passes(op, prec, op->blob[prec][dir][0], S.scaled ? (const void*)S.xsc.p : op->x64.p,
+                                   op->y64.p, 0, yd, accumulate, st, op->slab_ready.data(), true);
                 return;
             }
             EDGPU_CUDA(cudaMemcpyAsync(op->x64.p, x, n * 16, cudaMemcpyHostToDevice, st));

@@ -358,8 +358,10 @@ struct SlabBuild {
     const long long* base;          // [n_pass] first entry of each pass (fill pass)
     unsigned* tab;                  // the entries (fill pass)
     const unsigned short* amp_id;   // [n_slots] amplitude id of every pair-flip slot (fill pass)
+    unsigned char* cls;             // [n_rows] every row's orbit-size index (count pass; null: not kept)
     int n_slots;
     int colbits;
+    int scaled;                     // ids without the orbit-size indices (amplitude id x den + character)
     int o_ctr;                      // shared-memory offset of the per-thread pass counters / cursors
 };
 struct SlabRun {
@@ -376,9 +378,29 @@ struct SlabRun {
     unsigned colmask;
     int colbits, n_lut, lut_real;
     int first, last, accumulate, acc_c128;
-    int hints;                      // bit 0: gathers cached in L2 only, streamed data evict-first;
-                                    // bit 1: eight entries per lane and step instead of four
+    int hints;                      // 0 to 3: one lane per row (bit 0: gathers cached in L2 only,
+                                    // streamed data evict-first; bit 1: eight entries per lane and step
+                                    // instead of four); 4, 5: two, four lanes per row
+    int lut_mode;                   // 0: one shared-memory copy of the coefficients; 1: a copy per
+                                    // bank group (conflict-free lookups); 2: real, at most 4, in registers
+    // scaled tables: xs and x hold sqrt(|O_c|) x_c; the last pass multiplies row r by 1/sqrt(|O_r|)
+    // (and the first pass of y += H x the old y_r by sqrt(|O_r|))
+    int scaled;
+    const unsigned char* cls;       // [n_rows] orbit-size index of every row
+    const void* scale;              // R[2 nd]: sqrt(|O|) by orbit-size index, then 1 / sqrt(|O|)
+    int nd;
 };
+// Coefficient tables of at most this many entries go to registers (real) or to one copy per shared-
+// memory bank group (SLAB_REP_BYTES in all, which keeps eight blocks of the slab kernel per SM).
+constexpr int SLAB_REG_LUT = 4;
+constexpr int SLAB_REP_BYTES = 24 * 1024;
+// x_c -> sqrt(|O_c|) x_c for the columns [c0, c1) of x (R = float for complex64, double for complex128;
+// scale = the column scales by orbit-size index), written to out at the same columns.  From a complex128
+// source to a complex64 result (mixed precision from host buffers) x_c is rounded to complex64 first.
+void launch_slab_xscale(int prec, const void* x, const unsigned char* cls, const void* scale, void* out,
+                        int64_t c0, int64_t c1, cudaStream_t st);
+void launch_slab_xscale_c128_c64(const double* x, const unsigned char* cls, const float* scale, float* out,
+                                 int64_t c0, int64_t c1, cudaStream_t st);
 // Count pass (1) or fill pass (2) of the slab table from the target table.  p: the table-flavour
 // pair-flip template (tab, tile_off set; lpr = 1); smem: its image plus s.o_ctr's counters.
 void hx_slab_build(bool w32, int prec, int pass, const HxParams& p, const SlabBuild& s, size_t smem,

@@ -15,6 +15,8 @@
 // run; they differ from the one-pass product by the order of the additions.
 #include "hx_bond.cuh"
 
+#include <type_traits>
+
 namespace edgpu {
 
 namespace {
@@ -83,6 +85,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_slab_build_kernel(const HxParam
         }
         const long long tpos = p.tile_off[tile] + (incl - cnt);
         if constexpr (PASS == 1) {
+            if (s.cls && act) s.cls[row] = (unsigned char)ri;
             unsigned char* ctr = sm + s.o_ctr;
             for (int q = 0; q < P; ++q) ctr[q * HX_THREADS + threadIdx.x] = 0;
             if (act)
@@ -115,8 +118,8 @@ __global__ void __launch_bounds__(HX_THREADS) hx_slab_build_kernel(const HxParam
                     const unsigned q = (unsigned)c / wc;
                     const unsigned rel = cur[q * HX_THREADS + threadIdx.x]++;
                     const unsigned ph = p.want_arg ? (unsigned)num[g] : 0u;
-                    const unsigned id = (((unsigned)__ldg(s.amp_id + slot) * (unsigned)p.den + ph) * (unsigned)p.nd +
-                                         (unsigned)ri) * (unsigned)p.nd + (unsigned)sx;
+                    const unsigned ap = (unsigned)__ldg(s.amp_id + slot) * (unsigned)p.den + ph;
+                    const unsigned id = s.scaled ? ap : (ap * (unsigned)p.nd + (unsigned)ri) * (unsigned)p.nd + (unsigned)sx;
                     s.tab[s.base[q] + rel] = ((unsigned)c - q * wc) | (id << s.colbits);
                 });
         }
@@ -205,29 +208,39 @@ __device__ __forceinline__ void st_stream(T* p, T v) {
 // 32 / LPR rows of a tile with LPR lanes per row (lane sub of a row takes the row's entries sub,
 // sub + LPR, ...; the partial sums are added by a fixed butterfly).  A lane adds its entries of this
 // pass (NT per step, loads then gathers); the row's sum is then added to y (the first pass writes it,
-// the last adds the diagonal term too and may write complex128 to y_c128 instead).
-template <int PREC, bool REAL, int NT, bool CH, int LPR>
+// the last adds the diagonal term too and may write complex128 to y_c128 instead).  LUTM: where the
+// coefficients are read (SlabRun::lut_mode).
+template <int PREC, bool REAL, int NT, bool CH, int LPR, int LUTM>
 __global__ void __launch_bounds__(HX_THREADS) hx_slab_kernel(const SlabRun r) {
     typedef typename Cx<PREC>::V V;
     typedef typename Cx<PREC>::R R;
+    typedef typename std::conditional<REAL, R, V>::type C;
+    constexpr int REPS = 128 / (int)sizeof(C);   // copies per coefficient: one per bank group
     extern __shared__ __align__(16) unsigned char sm[];
     pdl_launch_dependents();
-    if (REAL) {
-        const R* src = (const R*)r.lut;
-        for (int i = threadIdx.x; i < r.n_lut; i += blockDim.x) ((R*)sm)[i] = src[i];
+    const C* src = (const C*)r.lut;
+    R c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+    if constexpr (LUTM == 2) {
+        const R* lr0 = (const R*)r.lut;
+        c0 = __ldg(lr0);
+        c1 = __ldg(lr0 + min(1, r.n_lut - 1));
+        c2 = __ldg(lr0 + min(2, r.n_lut - 1));
+        c3 = __ldg(lr0 + min(3, r.n_lut - 1));
+    } else if constexpr (LUTM == 1) {
+        for (int i = threadIdx.x; i < r.n_lut * REPS; i += blockDim.x) ((C*)sm)[i] = src[i / REPS];
+        __syncthreads();
     } else {
-        const V* src = (const V*)r.lut;
-        for (int i = threadIdx.x; i < r.n_lut; i += blockDim.x) ((V*)sm)[i] = src[i];
+        for (int i = threadIdx.x; i < r.n_lut; i += blockDim.x) ((C*)sm)[i] = src[i];
+        __syncthreads();
     }
-    __syncthreads();
     pdl_wait();
-    const R* lr = (const R*)sm;
-    const V* lv = (const V*)sm;
+    const C* lut = (const C*)sm;
     const V* __restrict__ xs = (const V*)r.xs;
     const unsigned* __restrict__ tab = r.tab;
     V* y = (V*)r.y;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
     const int sub = lane & (LPR - 1);
+    const int rep = lane & (REPS - 1);
     const bool to_c128 = r.last && r.y_c128 != nullptr;
     const long long n_parts = r.n_tiles * LPR;
     for (long long part = (long long)blockIdx.x * wpb + warp; part < n_parts; part += (long long)gridDim.x * wpb) {
@@ -261,12 +274,19 @@ __global__ void __launch_bounds__(HX_THREADS) hx_slab_kernel(const SlabRun r) {
             for (int h = 0; h < NT; ++h) {
                 if (j + h * LPR >= cnt) continue;
                 const unsigned id = e[h] >> r.colbits;
-                if (REAL) {
-                    const R f = lr[id];
+                C f;
+                if constexpr (LUTM == 2) {
+                    f = (id & 2u) ? ((id & 1u) ? c3 : c2) : ((id & 1u) ? c1 : c0);
+                } else if constexpr (LUTM == 1) {
+                    f = lut[id * REPS + rep];
+                } else {
+                    f = lut[id];
+                }
+                if constexpr (REAL) {
                     acc.x = fma_r(f, xv[h].x, acc.x);
                     acc.y = fma_r(f, xv[h].y, acc.y);
                 } else {
-                    acc = cfma_acc(acc, lv[id], xv[h]);
+                    acc = cfma_acc(acc, f, xv[h]);
                 }
             }
         }
@@ -280,12 +300,30 @@ __global__ void __launch_bounds__(HX_THREADS) hx_slab_kernel(const SlabRun r) {
         // only its own slab of x, the last one all of it)
         V t;
         if (r.first) {
-            t = (r.accumulate) ? cadd(ld_stream<CH>(y + row), acc) : acc;
+            if (r.accumulate) {
+                V yo = ld_stream<CH>(y + row);
+                if (r.scaled) {
+                    // y += H x on a scaled table: the old y_r enters the row's scaled sum as sqrt(|O_r|) y_r
+                    const R sr = __ldg((const R*)r.scale + r.cls[row]);
+                    yo.x *= sr;
+                    yo.y *= sr;
+                }
+                t = cadd(yo, acc);
+            } else {
+                t = acc;
+            }
         } else {
             if (cnt == 0 && !r.last) continue;   // nothing to add to this row
             t = cadd(ld_stream<CH>(y + row), acc);
         }
-        if (r.last) t = cfma_acc(t, ld_stream<CH>((const V*)r.diag + row), ld_stream<CH>((const V*)r.x + row));
+        if (r.last) {
+            t = cfma_acc(t, ld_stream<CH>((const V*)r.diag + row), ld_stream<CH>((const V*)r.x + row));
+            if (r.scaled) {
+                const R rs = __ldg((const R*)r.scale + r.nd + r.cls[row]);
+                t.x *= rs;
+                t.y *= rs;
+            }
+        }
         if (to_c128) {
             double2 o = make_double2((double)t.x, (double)t.y);
             double2* yc = (double2*)r.y_c128;
@@ -299,6 +337,38 @@ __global__ void __launch_bounds__(HX_THREADS) hx_slab_kernel(const SlabRun r) {
             st_stream<CH>(y + row, t);
         }
     }
+}
+
+// x_c -> sqrt(|O_c|) x_c over the columns [c0, c1)
+template <typename V, typename R>
+__global__ void k_slab_xscale(const V* __restrict__ x, const unsigned char* __restrict__ cls,
+                              const R* __restrict__ scale, V* __restrict__ out, long long c0, long long c1) {
+    for (long long c = c0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; c < c1;
+         c += (long long)gridDim.x * blockDim.x) {
+        const R f = scale[cls[c]];
+        V v = x[c];
+        v.x *= f;
+        v.y *= f;
+        out[c] = v;
+    }
+}
+
+// the same from complex128 to complex64: x_c rounded to complex64, then scaled in FP32 (as the
+// device-buffer path scales a complex64 x)
+__global__ void k_slab_xscale_c128_c64(const double2* __restrict__ x, const unsigned char* __restrict__ cls,
+                                       const float* __restrict__ scale, float2* __restrict__ out, long long c0,
+                                       long long c1) {
+    for (long long c = c0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; c < c1;
+         c += (long long)gridDim.x * blockDim.x) {
+        const float f = scale[cls[c]];
+        const double2 v = x[c];
+        out[c] = make_float2((float)v.x * f, (float)v.y * f);
+    }
+}
+
+int xscale_blocks(long long n) {
+    const long long need = (n + 255) / 256;
+    return (int)std::max<long long>(1, std::min<long long>(need, (long long)sm_count() * 8));
 }
 
 template <typename K>
@@ -380,15 +450,28 @@ void hx_slab_scan(const unsigned* tile_sum, unsigned* off, int n_pass, long long
     if (e != cudaSuccess) throw Error(EDGPU_ERR_CUDA, std::string("slab scan: ") + cudaGetErrorString(e));
 }
 
-template <int PREC, bool CH, int NT, int LPR>
-void slab_launch_t(const SlabRun& r, size_t smem, cudaStream_t st) {
-    if (r.lut_real) {
-        auto k = hx_slab_kernel<PREC, true, NT, CH, LPR>;
+template <int PREC, bool REAL, bool CH, int NT, int LPR>
+void slab_launch_m(const SlabRun& r, size_t smem, cudaStream_t st) {
+    if constexpr (REAL) {
+        if (r.lut_mode == 2) {
+            auto k = hx_slab_kernel<PREC, true, NT, CH, LPR, 2>;
+            slab_pdl_launch(k, r, slab_blocks(k, 0, r.n_tiles * LPR), 0, st);
+            return;
+        }
+    }
+    if (r.lut_mode == 1) {
+        auto k = hx_slab_kernel<PREC, REAL, NT, CH, LPR, 1>;
         slab_pdl_launch(k, r, slab_blocks(k, smem, r.n_tiles * LPR), smem, st);
     } else {
-        auto k = hx_slab_kernel<PREC, false, NT, CH, LPR>;
+        auto k = hx_slab_kernel<PREC, REAL, NT, CH, LPR, 0>;
         slab_pdl_launch(k, r, slab_blocks(k, smem, r.n_tiles * LPR), smem, st);
     }
+}
+
+template <int PREC, bool CH, int NT, int LPR>
+void slab_launch_t(const SlabRun& r, size_t smem, cudaStream_t st) {
+    if (r.lut_real) slab_launch_m<PREC, true, CH, NT, LPR>(r, smem, st);
+    else slab_launch_m<PREC, false, CH, NT, LPR>(r, smem, st);
 }
 
 // hints: 0 to 3 one lane per row (bit 0 the cache hints, bit 1 eight entries per lane and step
@@ -407,9 +490,31 @@ void slab_launch_p(const SlabRun& r, size_t smem, cudaStream_t st) {
 
 void hx_slab_launch(int prec, const SlabRun& r, cudaStream_t st) {
     if (r.n_tiles == 0) return;
-    const size_t smem = (size_t)r.n_lut * (r.lut_real ? 1 : 2) * (prec == 0 ? 8 : 4);
+    const size_t csize = (size_t)(r.lut_real ? 1 : 2) * (prec == 0 ? 8 : 4);
+    const size_t smem = (size_t)r.n_lut * (r.lut_mode == 1 ? 128 : csize);
     if (prec == 0) slab_launch_p<0>(r, smem, st);
     else slab_launch_p<1>(r, smem, st);
+}
+
+void launch_slab_xscale(int prec, const void* x, const unsigned char* cls, const void* scale, void* out,
+                        int64_t c0, int64_t c1, cudaStream_t st) {
+    if (c1 <= c0) return;
+    const int blocks = xscale_blocks(c1 - c0);
+    if (prec == 0)
+        k_slab_xscale<double2, double><<<blocks, 256, 0, st>>>((const double2*)x, cls, (const double*)scale,
+                                                              (double2*)out, c0, c1);
+    else
+        k_slab_xscale<float2, float><<<blocks, 256, 0, st>>>((const float2*)x, cls, (const float*)scale,
+                                                            (float2*)out, c0, c1);
+    EDGPU_CUDA(cudaGetLastError());
+}
+
+void launch_slab_xscale_c128_c64(const double* x, const unsigned char* cls, const float* scale, float* out,
+                                 int64_t c0, int64_t c1, cudaStream_t st) {
+    if (c1 <= c0) return;
+    k_slab_xscale_c128_c64<<<xscale_blocks(c1 - c0), 256, 0, st>>>((const double2*)x, cls, scale, (float2*)out,
+                                                                  c0, c1);
+    EDGPU_CUDA(cudaGetLastError());
 }
 
 }  // namespace edgpu

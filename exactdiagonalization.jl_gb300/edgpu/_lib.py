@@ -85,6 +85,7 @@ SIGNATURES = {
     "edgpu_op_free_slabs": (ctypes.c_int, [vp]),
     "edgpu_op_slabs_info": (ctypes.c_int, [vp, P(i32), P(i64), P(i64)]),
     "edgpu_op_slab_use": (ctypes.c_int, [vp, i32, i32, P(i32)]),
+    "edgpu_op_slab_scaling": (ctypes.c_int, [vp, i32, P(i32)]),
     "edgpu_op_build_adjoint_targets": (ctypes.c_int, [vp, i64, P(i32)]),
     "edgpu_op_table_prefetch": (ctypes.c_int, [vp, i32, i32, P(i32)]),
     "edgpu_op_grad_kernel": (ctypes.c_int, [vp, i32, P(i32)]),

@@ -695,6 +695,15 @@ class OperatorRepresentation:
                                       ctypes.byref(cur)))
         return int(cur.value)
 
+    def slab_scaling(self, mode=None) -> bool:
+        """Layout of the next slab table (mode 0: scaled on sectors of 2^22 rows or more where that saves
+        passes or the coefficients are complex, 1: never, 2: always); returns whether the current table
+        is scaled (the orbit-size ratio applied to x and to the result rows instead of each entry's
+        coefficient)."""
+        cur = ctypes.c_int32()
+        check(lib().edgpu_op_slab_scaling(self._h, -1 if mode is None else int(mode), ctypes.byref(cur)))
+        return bool(cur.value)
+
     def pair_classes(self):
         """(bond classes, rotation components) of the pair-flip schedule; (0, 0) when it does not apply."""
         a, b = ctypes.c_int32(), ctypes.c_int32()

@@ -255,6 +255,17 @@ int edgpu_op_slabs_info(edgpu_op op, int32_t* passes, int64_t* columns_per_slab,
  * differ from v = 0 to 3 by rounding (each is deterministic).  Building the table sets 1 for both
  * precisions; the autotuner times the variants against the one-pass schedules. */
 int edgpu_op_slab_use(edgpu_op op, int32_t precision, int32_t use, int32_t* current);
+/* Layout of the next slab table: mode 0 (default) scaled on sectors of 2^22 representatives or more
+ * where that saves passes or the coefficients are complex (and wherever the unscaled ids do not fit in
+ * an entry), 1 never, 2 always; -1 only queries.  *scaled = whether the current table is scaled.  A scaled
+ * table's entries carry the coefficient without the orbit-size ratio sqrt(|O_c| / |O_r|): each product
+ * first scales x by sqrt(|O_c|) into a buffer of the table (slab by slab on the handle's second
+ * stream while the earlier passes run), and the last pass scales row r by 1 / sqrt(|O_r|).  Fewer
+ * distinct coefficients (a few in registers, or a conflict-free shared-memory copy per bank group)
+ * and more column bits per entry (fewer passes) against one more streamed pass over x.  Results agree
+ * with the unscaled layout to rounding.  Products of one operator through a scaled table are ordered
+ * by the calling stream (the scaled x is one buffer per table). */
+int edgpu_op_slab_scaling(edgpu_op op, int32_t mode, int32_t* scaled);
 /* Sparse matrix of the representation, assembled on the device in FP64: rows sorted by column,
  * entries of equal column summed, entries with |value| < tol dropped (tol: the reference's
  * Base.rtoldefault(Float64) = sqrt(eps) gives its default).  This is sparse(opr)

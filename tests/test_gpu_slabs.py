@@ -4,7 +4,9 @@ Small slabs force several passes on sectors the oracle handles in seconds: the p
 oracle's reduced product within 1e-5 (mixed precision) and the one-pass target-table product within
 1e-6, be reproducible bit for bit, accumulate (y += H x), write complex128 host buffers, follow new
 coupling values, and cover real and complex coefficients (momentum 0 and k != 0), a torus and a
-chain; the FP64 product through the same table must match the oracle within 1e-12."""
+chain; the FP64 product through the same table must match the oracle within 1e-12.  Both table
+layouts: coefficients with the orbit-size ratio, and the scaled layout (ratio applied to x and to the
+result rows)."""
 import numpy as np
 import pytest
 
@@ -48,8 +50,13 @@ def _products(E, opr, x):
     return xd, y
 
 
+@pytest.mark.parametrize("scaling", [1, 2])
 @pytest.mark.parametrize("L,k,coupled", [(20, 0, False), (18, 5, False), (20, 0, True)])
-def test_slab_product_chain(L, k, coupled):
+def test_slab_product_chain(L, k, coupled, scaling):
+    """scaling 1: coefficients with the orbit-size ratio; 2: the scaled layout (x scaled slab by slab on
+    the handle's second stream, rows in the last pass), whose coefficients sit in registers (k = 0,
+    two couplings), in a copy per shared-memory bank group (k = 5, complex) or in one shared-memory
+    copy (per-bond couplings)."""
     import torch
     import edgpu as E
     opr, red, terms, extra = _chain(E, L, k, coupled)
@@ -59,7 +66,9 @@ def test_slab_product_chain(L, k, coupled):
     want = O.apply_rows(red, terms, x)
     xd, y_tab = _products(E, opr, x)
     # slabs of 1024 columns: several passes
+    assert not opr.slab_scaling(scaling)
     assert opr.build_slabs(slab_bytes=1024 * 8, max_bytes=1 << 30)
+    assert opr.slab_scaling() == (scaling == 2)
     passes, wc, entries = opr.slabs_info
     assert wc == 1024 and passes == (N + 1023) // 1024 and passes >= 3
     assert 0 < entries <= opr.targets_info[0]   # the targets with a representative
@@ -184,8 +193,9 @@ def test_slab_product_torus_j1j2():
         red = O.symmetry_reduce(parent, bw, off, maps, amps)
         N = opr.dimension
         assert opr.build_targets(1 << 30)
+        opr.slab_scaling(2 if k == (1, 1) else 0)
         assert opr.build_slabs(slab_bytes=1024 * 8, max_bytes=1 << 30)
-        assert opr.slabs_info[0] >= 3
+        assert opr.slabs_info[0] >= 3 and opr.slab_scaling() == (k == (1, 1))
         x = O.complex_gaussian(N, 9)
         want = O.apply_rows(red, terms, x)
         _, y = _products(E, opr, x)
@@ -193,6 +203,49 @@ def test_slab_product_torus_j1j2():
         y64 = np.zeros(N, dtype=np.complex128)
         E.mul_(y64, opr, x, precision="fp64")
         assert relerr(y64, want) < 1e-12
+
+
+@pytest.mark.parametrize("k", [0, 3])
+def test_slab_product_scaled_one_pass(k):
+    """A scaled table of one pass (x scaled on the calling stream before the pass): device vectors,
+    y += H x, pinned and pageable host buffers in both precisions, against the oracle."""
+    import torch
+    import edgpu as E
+    opr, red, terms, _ = _chain(E, 16, k, False)
+    N = opr.dimension
+    assert opr.build_targets(1 << 30)
+    opr.slab_scaling(2)
+    assert opr.build_slabs(slab_bytes=1 << 20, max_bytes=1 << 30)
+    assert opr.slab_scaling() and opr.slabs_info[0] == 1
+    x = O.complex_gaussian(N, 4)
+    want = O.apply_rows(red, terms, x)
+    xd, y = _products(E, opr, x)
+    assert relerr(y.cpu().numpy().astype(np.complex128), want) < 1e-5
+    y2 = y.clone()
+    E.apply_(y2, opr, xd, precision="mixed")
+    torch.cuda.synchronize()
+    assert relerr(y2.cpu().numpy().astype(np.complex128), 2 * want) < 1e-5
+    x64 = torch.from_numpy(x).cuda()
+    y64 = torch.empty_like(x64)
+    E.mul_(y64, opr, x64, precision="fp64")
+    torch.cuda.synchronize()
+    assert relerr(y64.cpu().numpy(), want) < 1e-12
+    E.apply_(y64, opr, x64, precision="fp64")
+    torch.cuda.synchronize()
+    assert relerr(y64.cpu().numpy(), 2 * want) < 1e-12
+    xp = torch.from_numpy(x).pin_memory()
+    yp = torch.zeros(N, dtype=torch.complex128).pin_memory()
+    for prec, tol in (("fp64", 1e-12), ("mixed", 1e-5)):
+        yp.zero_()
+        E.mul_(yp.numpy(), opr, xp.numpy(), precision=prec)
+        assert relerr(yp.numpy(), want) < tol
+        yh = np.zeros(N, dtype=np.complex128)
+        E.mul_(yh, opr, x, precision=prec)
+        assert relerr(yh, want) < tol
+    # the default policy keeps a sector this small unscaled
+    opr.slab_scaling(0)
+    assert opr.build_slabs(slab_bytes=1 << 20, max_bytes=1 << 30)
+    assert not opr.slab_scaling()
 
 
 def test_slab_build_refusals():
