@@ -640,11 +640,12 @@ def run_gpu(args, wl):
         # to 1e-9) followed by the FP64 Rayleigh quotient of its Ritz vector, accepted when the
         # Kato-Temple estimate of its error is below 1e-10 relative (else FP64 Lanczos from that vector).
         # the stored Krylov basis (which gives the Ritz vector without a second pass of the recurrence)
-        # may take 80% of the device memory left after the operator's tables
+        # may take the device memory left after the operator's tables (the Lanczos driver sizes it after
+        # its other buffers and keeps 2 GiB free)
         torch.cuda.synchronize()
         torch.cuda.empty_cache()
         free_b, _ = torch.cuda.mem_get_info()
-        krylov_limit = int(0.8 * free_b)
+        krylov_limit = int(free_b)
         edgpu.set_krylov_limit(krylov_limit)
         t0 = time.perf_counter()
         r64 = edgpu.lanczos(opr, wl["lanczos_steps"], precision="fp64", reorth=wl["reorth"], seed=wl["seed"], tol=1e-12)

@@ -3800,7 +3800,7 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
     enum Store { ROLL = 0, F64 = 1, F32 = 2 };
     size_t free_b = 0, total_b = 0;
     EDGPU_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    const double limit = g_krylov_limit > 0 ? (double)g_krylov_limit : 0.5 * (double)free_b;
+    double limit = g_krylov_limit > 0 ? (double)g_krylov_limit : 0.5 * (double)free_b;
     auto fits64 = [&](int k) { return (double)(k + 1) * (double)N * 16.0 <= limit; };
     auto fits32 = [&](int k) { return (double)(k + 1) * (double)N * 8.0 <= limit; };
 
@@ -3938,8 +3938,18 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
         E = lowest(A, B);
         done = (int)A.size();
     } else {
-        // 1. mixed-precision Lanczos to about 1e-7 with a stored basis (FP64, else complex64, capped by
-        //    the Krylov limit), or rolling with a second pass for the Ritz vector
+        // 1. mixed-precision Lanczos to about 1e-9 with a stored basis (FP64, else complex64, capped by
+        //    the Krylov limit and by the device memory left once the run's other buffers are in place,
+        //    less 2 GiB), or rolling with a second pass for the Ritz vector
+        psi.ensure(2 * N);
+        V64.ensure(2 * 2 * N);
+        y32.ensure(2 * N);
+        {
+            size_t fb = 0, tb = 0;
+            EDGPU_CUDA(cudaMemGetInfo(&fb, &tb));
+            const double room = (double)fb + (double)V32.n * sizeof(float) - (double)(2ull << 30);
+            limit = std::max(0.0, std::min(limit, room));
+        }
         int store = ROLL, m1 = m;
         if (fits64(m)) store = F64;
         else if (fits32(m)) store = F32;
@@ -3996,6 +4006,7 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
         // 3. otherwise FP64 Lanczos from the mixed-precision Ritz vector until the eigenvalue settles to tol
         const bool store2 = (reorth || want_vec) && fits64(m);
         if (!certified) {
+            V32.release();   // the mixed run's basis makes room for the FP64 run's
             setup(EDGPU_FP64, store2 ? F64 : ROLL, m, reorth != 0 && store2);
             start_from(psi.p, nullptr);
             std::vector<double> A2, B2;

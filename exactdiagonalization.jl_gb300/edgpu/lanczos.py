@@ -55,5 +55,7 @@ def lanczos(opr: OperatorRepresentation, n_steps: int = 200, precision="fp64", r
 
 def set_krylov_limit(nbytes: int) -> None:
     """Largest Krylov basis (bytes) the Lanczos driver stores; 0 restores the default (half of the free
-    device memory).  Below it, Ritz vectors are rebuilt by a second pass of the recurrence."""
+    device memory).  Below it, Ritz vectors are rebuilt by a second pass of the recurrence.  The
+    complex64 basis of a refined mixed-precision run is also held to the device memory left after the
+    run's other buffers, less 2 GiB."""
     check(lib().edgpu_set_krylov_limit(int(nbytes)))

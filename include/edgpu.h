@@ -402,7 +402,8 @@ int edgpu_lanczos(edgpu_op op, int32_t precision, int32_t n_steps, int32_t reort
                   const double* v0, int32_t refine, double tol, double* e0, double* alphas, double* betas,
                   int32_t* steps_done, double* ground_state);
 /* Largest Krylov basis in bytes that edgpu_lanczos may store (0, the default: half of the free device
- * memory at the call). */
+ * memory at the call).  The complex64 basis of a mixed-precision run with refine is also held to the
+ * device memory left once the run's other buffers are allocated, less 2 GiB. */
 int edgpu_set_krylov_limit(int64_t bytes);
 
 /* ---- utilities --------------------------------------------------------------------------- */
