@@ -3843,11 +3843,30 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
         if (cur_store == ROLL) EDGPU_CUDA(cudaMemcpyAsync(vstart.p, vec64(0), N * 16, cudaMemcpyDeviceToDevice, st));
     };
 
+    // Kato-Temple estimate of the lowest Ritz value's error after a step with the next beta:
+    // (beta s_last)^2 / (theta_2 - theta_1) <= kt max(1, |theta_1|), s the lowest eigenvector of the
+    // tridiagonal matrix (beta |s_last| is the Ritz pair's residual norm) and theta_2 its second
+    // eigenvalue (or the given one when not NaN).
+    auto kt_ok = [&](const std::vector<double>& A, const std::vector<double>& B, double beta, double th1,
+                     double th2_given, double kt) {
+        if (A.size() < 2) return false;
+        const double th2 = std::isnan(th2_given) ? kth_eigenvalue(A, B, 2) : th2_given;
+        if (!(th2 > th1)) return false;
+        const std::vector<double> sv = tridiag_eigvec(A, B, th1);
+        double nrm = 0.0;
+        for (double v : sv) nrm += v * v;
+        const double res = beta * std::fabs(sv.back()) / std::sqrt(nrm);
+        return res * res / (th2 - th1) <= kt * std::max(1.0, std::fabs(th1));
+    };
     // Lanczos steps j = 0 .. steps-1 from vec64(0); fills A, B.  conv_tol > 0: stop once the lowest Ritz
-    // value moved by less than conv_tol |E| over the last 5 steps.  With acc: psi += acc[j] v_j only.
+    // value moved by less than conv_tol |E| over the last 5 steps (with kt > 0: once that has held for
+    // `patience` steps, or earlier when the Kato-Temple estimate is below kt, from step kt_min on).
+    // With acc: psi += acc[j] v_j only.
     auto run = [&](int steps, double conv_tol, std::vector<double>& A, std::vector<double>& B,
-                   const std::vector<double>* acc) {
+                   const std::vector<double>* acc, double kt = 0.0, double kt_th2 = NAN, int kt_min = 10,
+                   int patience = 1) {
         std::vector<double> hist;   // lowest Ritz value after every step (with conv_tol > 0)
+        int settled_for = 0;
         for (int j = 0; j < steps; ++j) {
             double* vj = vec64(j);
             if (acc) {
@@ -3885,7 +3904,10 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
                 const double e = lowest_eigenvalue(A, B);
                 hist.push_back(e);
                 const size_t h = hist.size();
-                if (h > 5 && std::fabs(e - hist[h - 6]) < conv_tol * std::max(1.0, std::fabs(e))) break;
+                const bool settled = h > 5 && std::fabs(e - hist[h - 6]) < conv_tol * std::max(1.0, std::fabs(e));
+                settled_for = settled ? settled_for + 1 : 0;
+                if (kt > 0.0 && (int)A.size() >= kt_min && kt_ok(A, B, beta, e, kt_th2, kt)) break;
+                if (settled_for >= (kt > 0.0 ? patience : 1)) break;
             }
             B.push_back(beta);
             launch_normalize(N, w.p, d_beta, vec64(j + 1), cur_prec == EDGPU_MIXED ? vin32(j + 1) : nullptr, st);
@@ -3934,7 +3956,9 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
                     " MiB); use reorth = 0");
         setup(precision, store, m, reorth != 0);
         start_from(nullptr, v0);
-        run(m, tol, A, B, nullptr);
+        // the Kato-Temple rule certifies the eigenvalue, not the vector: a wanted ground state runs on
+        // until the eigenvalue has settled
+        run(m, tol, A, B, nullptr, want_vec ? 0.0 : tol);
         E = lowest(A, B);
         done = (int)A.size();
     } else {
@@ -3972,7 +3996,10 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
             A.clear();
             B.clear();
             const int budget = std::min(m1, m - done);
-            run(budget, tol1, A, B, nullptr);
+            // on until the Ritz pair's residual predicts that the FP64 Rayleigh quotient below will be
+            // certified (a quarter of tol, for the complex64 roundings), or for 6 steps after the Ritz
+            // value has settled to tol1 (the roundings may hold the residual above that)
+            run(budget, tol1, A, B, nullptr, 0.25 * tol, NAN, 10, 6);
             E = lowest(A, B);
             done += (int)A.size();
             ritz_vector(A, B, E);
@@ -3984,6 +4011,7 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
         //    psi and is estimated by the Kato-Temple bound |r|^2 / (theta_2 - E_RQ), theta_2 the
         //    second-lowest Ritz value of the mixed run; accepted when that is below tol |E_RQ|.
         bool certified = false;
+        double theta2_mixed = NAN;
         if (A.size() >= 2) {
             launch_norm2_c128(N, psi.p, scratch.p, d_tmp, st);
             launch_normalize(N, psi.p, d_tmp, psi.p, nullptr, st);
@@ -3997,6 +4025,7 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
             EDGPU_CUDA(cudaStreamSynchronize(st));
             const double e_rq = hb[0], rn = hb[1];
             const double theta2 = kth_eigenvalue(A, std::vector<double>(B.begin(), B.begin() + (A.size() - 1)), 2);
+            theta2_mixed = theta2;
             ++done;
             if (theta2 > e_rq && rn * rn / (theta2 - e_rq) <= tol * std::max(1.0, std::fabs(e_rq))) {
                 E = e_rq;
@@ -4010,7 +4039,8 @@ int edgpu_lanczos(edgpu_op oh, int32_t precision, int32_t n_steps, int32_t reort
             setup(EDGPU_FP64, store2 ? F64 : ROLL, m, reorth != 0 && store2);
             start_from(psi.p, nullptr);
             std::vector<double> A2, B2;
-            run(m, tol, A2, B2, nullptr);
+            // stopped by the Kato-Temple estimate with the mixed run's second Ritz value as the gap
+            run(m, tol, A2, B2, nullptr, tol, theta2_mixed, std::isnan(theta2_mixed) ? 10 : 2);
             A = A2;
             B = B2;
             E = lowest(A, B);

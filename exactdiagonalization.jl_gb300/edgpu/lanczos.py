@@ -4,12 +4,14 @@ dense eigvals or an external Arpack.eigs that calls mul! repeatedly, docs/src/ex
 FP64 throughout for the scalars, dot products, norms, reorthogonalisation and the tridiagonal
 eigensolve; `precision` selects the product (fp64, or mixed: complex64 vectors and FP32
 accumulation).  tol > 0 stops a run once the lowest Ritz value moved by less than tol |E| over five
-steps.  With refine=True (mixed precision) the mixed-precision run settles its lowest Ritz value to
-max(tol, 1e-9), then one FP64 product gives the Rayleigh quotient E_RQ = <psi|H psi> of its Ritz vector
-psi and the residual r = H psi - E_RQ psi; E_RQ is returned when the Kato-Temple estimate
-|r|^2 / (theta_2 - E_RQ) (theta_2: the second Ritz value of the mixed run) is below
-tol max(1, |E_RQ|), else
-FP64 Lanczos restarts from psi until the eigenvalue settles to tol.  The Krylov basis is kept only
+steps or (when no vector is wanted, from step 10 on) once the Kato-Temple estimate of its error from
+the tridiagonal matrix, (beta s_last)^2 / (theta_2 - theta_1), is below tol max(1, |E|).  With
+refine=True (mixed precision) the mixed-precision run goes on until that estimate is below tol / 4,
+or for 6 steps after its lowest Ritz value settled to max(tol, 1e-9); then one FP64 product gives
+the Rayleigh quotient E_RQ = <psi|H psi> of its Ritz vector psi and the residual r = H psi - E_RQ psi;
+E_RQ is returned when the Kato-Temple estimate |r|^2 / (theta_2 - E_RQ) (theta_2: the second Ritz
+value of the mixed run) is below tol max(1, |E_RQ|), else FP64 Lanczos restarts from psi until the
+eigenvalue settles to tol or the estimate certifies it.  The Krylov basis is kept only
 when reorthogonalisation or a Ritz vector needs it and it fits (see set_krylov_limit): in FP64 for an
 FP64 run, as the complex64 product inputs for a mixed run (reorthogonalisation then uses those
 complex64-rounded vectors with FP64 arithmetic); otherwise a Ritz vector is rebuilt by a second pass of

@@ -387,11 +387,15 @@ void edgpu_batch_destroy(edgpu_batch b);
 /* Lowest eigenvalue by Lanczos on the device: at most n_steps steps from a seeded complex Gaussian
  * start vector (or v0, host complex128 of length dim, if not NULL), full reorthogonalisation when
  * reorth != 0.  Scalars, dots, norms and the tridiagonal eigensolve are FP64; precision selects the
- * product.  tol > 0 stops once the lowest Ritz value moved by less than tol |E| over the last 5 steps.  With
- * refine != 0 and EDGPU_MIXED: a mixed-precision run settled to max(tol, 1e-9), then one FP64 product
- * gives the Rayleigh quotient E_RQ of its Ritz vector psi and the residual r = H psi - E_RQ psi; E_RQ is
- * returned when the Kato-Temple estimate |r|^2 / (theta_2 - E_RQ) (theta_2 the second Ritz value) is at
- * most tol max(1, |E_RQ|), else FP64 Lanczos continues from psi until the eigenvalue settles to tol.  Outputs: e0, alphas/betas of the last run (n_steps
+ * product.  tol > 0 stops once the lowest Ritz value moved by less than tol |E| over the last 5 steps,
+ * or (without ground_state) from step 10 on once the Kato-Temple estimate of its error,
+ * (beta s_last)^2 / (theta_2 - theta_1) from the tridiagonal matrix, is at most tol max(1, |E|).  With
+ * refine != 0 and EDGPU_MIXED: a mixed-precision run until that estimate is at most tol / 4, or 6 steps
+ * after its Ritz value settled to max(tol, 1e-9); then one FP64 product gives the Rayleigh quotient
+ * E_RQ of its Ritz vector psi and the residual r = H psi - E_RQ psi; E_RQ is returned when the
+ * Kato-Temple estimate |r|^2 / (theta_2 - E_RQ) (theta_2 the second Ritz value) is at most
+ * tol max(1, |E_RQ|), else FP64 Lanczos continues from psi until the eigenvalue settles to tol or the
+ * estimate (with the mixed run's theta_2) certifies it.  Outputs: e0, alphas/betas of the last run (n_steps
  * each, nullable), steps_done (all runs).  ground_state (nullable, host complex128 dim): Ritz vector.
  * The Krylov basis is stored (FP64, or the complex64 product inputs of a mixed run) only when
  * reorthogonalisation or a Ritz vector needs it and it fits under the Krylov limit (EDGPU_ERR_OOM when
