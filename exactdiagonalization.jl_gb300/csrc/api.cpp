@@ -6,6 +6,7 @@
 #include <array>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <tuple>
@@ -242,6 +243,18 @@ struct edgpu_op_s {
             slab_ready.push_back(e);
         }
     }
+    // host-buffer slab products in row blocks: each block's last pass (which writes the host buffer)
+    // runs on this stream while the next block's passes run
+    cudaStream_t blk_st = nullptr;
+    std::vector<cudaEvent_t> blk_ev;   // [block] its passes before the last are done; then: all done
+    void ensure_block_events(int n) {
+        if (!blk_st) EDGPU_CUDA(cudaStreamCreateWithFlags(&blk_st, cudaStreamNonBlocking));
+        while ((int)blk_ev.size() < n + 1) {
+            cudaEvent_t e = nullptr;
+            EDGPU_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            blk_ev.push_back(e);
+        }
+    }
     int slab_hint[2] = {0, 0};        // [precision]: the slab product's cache hints (chosen by the autotuner)
     // the optional tables change: cached graphs (this handle's host-buffer graphs, and batches, which
     // compare gen) must not replay launches that read the old ones
@@ -291,6 +304,11 @@ struct edgpu_op_s {
         }
         if (aux_fork) cudaEventDestroy(aux_fork);
         for (auto e : slab_ready) cudaEventDestroy(e);
+        if (blk_st) {
+            cudaStreamSynchronize(blk_st);
+            cudaStreamDestroy(blk_st);
+        }
+        for (auto e : blk_ev) cudaEventDestroy(e);
     }
 };
 
@@ -1084,7 +1102,7 @@ bool slab_active(const edgpu_op_s* op, int prec, int dir, int mode, int rows) {
 // the handle's second stream while the earlier passes run.
 void launch_slab_passes(edgpu_op_s* op, int prec, const Blob& B, const void* x, void* y, int accumulate,
                         void* y_c128, int acc_c128, cudaStream_t st, const cudaEvent_t* ready,
-                        bool pre_scaled = false) {
+                        bool pre_scaled = false, int row_blocks = 1) {
     auto& S = op->slab;
     const size_t esz = prec == EDGPU_FP64 ? 16 : 8;
     const void* scale = prec == EDGPU_FP64 ? (const void*)S.sc64.p : (const void*)S.sc32.p;
@@ -1128,16 +1146,61 @@ void launch_slab_passes(edgpu_op_s* op, int prec, const Blob& B, const void* x, 
     r.acc_c128 = acc_c128;
     r.accumulate = y_c128 ? 0 : accumulate;
     r.hints = op->slab_hint[prec];
-    for (int q = 0; q < S.n_pass; ++q) {
-        if (ready) EDGPU_CUDA(cudaStreamWaitEvent(st, ready[q], 0));
+    const long long n_tiles = r.n_tiles;
+    auto set_pass = [&](int q) {
         r.cnt = S.counts + (size_t)q * r.n_rows;
-        r.off = S.off + (size_t)q * r.n_tiles;
+        r.off = S.off + (size_t)q * n_tiles;
         r.tab = S.tab + S.base[q];
         r.xs = (const char*)x + (size_t)q * S.wc * esz;
         r.first = q == 0;
         r.last = q == S.n_pass - 1;
+    };
+    if (row_blocks > 1 && S.n_pass > 1 && n_tiles >= row_blocks) {
+        // rows in blocks: a block's passes before the last run on st with one block slot per SM left
+        // free; its last pass (which writes y, e.g. to a host buffer) runs on the handle's block stream
+        // with one block per SM, beside the next block's passes
+        op->ensure_block_events(row_blocks);
+        const long long per = (n_tiles + row_blocks - 1) / row_blocks;
+        for (int b = 0; b < row_blocks; ++b) {
+            const long long t0 = (long long)b * per, t1 = std::min(n_tiles, t0 + per);
+            if (t0 >= t1) break;
+            r.tile0 = t0;
+            r.n_tiles = t1 - t0;
+            r.blocks_per_sm = -1;
+            for (int q = 0; q + 1 < S.n_pass; ++q) {
+                if (ready && b == 0) EDGPU_CUDA(cudaStreamWaitEvent(st, ready[q], 0));
+                set_pass(q);
+                hx_slab_launch(prec, r, st);
+            }
+            EDGPU_CUDA(cudaEventRecord(op->blk_ev[b], st));
+            EDGPU_CUDA(cudaStreamWaitEvent(op->blk_st, op->blk_ev[b], 0));
+            if (ready && b == 0) EDGPU_CUDA(cudaStreamWaitEvent(op->blk_st, ready[S.n_pass - 1], 0));
+            r.blocks_per_sm = 1;
+            set_pass(S.n_pass - 1);
+            hx_slab_launch(prec, r, op->blk_st);
+        }
+        EDGPU_CUDA(cudaEventRecord(op->blk_ev[row_blocks], op->blk_st));
+        EDGPU_CUDA(cudaStreamWaitEvent(st, op->blk_ev[row_blocks], 0));
+        return;
+    }
+    for (int q = 0; q < S.n_pass; ++q) {
+        if (ready) EDGPU_CUDA(cudaStreamWaitEvent(st, ready[q], 0));
+        set_pass(q);
         hx_slab_launch(prec, r, st);
     }
+}
+
+// Row blocks of a host-buffer slab product (launch_slab_passes): EDGPU_SLAB_ROW_BLOCKS when set (1 to
+// 64); else 2 for mixed precision on sectors of 2^22 rows or more with at least 4 passes (on 6x6 k=0,
+// 252M rows: 101.8 -> 96.9 ms per H x with pinned complex128 buffers; 4 and 8 blocks gain no more,
+// and the FP64 product is slower in blocks), 1 otherwise.
+int slab_row_blocks(const edgpu_op_s* op, int prec, int64_t n) {
+    const char* v = std::getenv("EDGPU_SLAB_ROW_BLOCKS");
+    if (v && *v) {
+        const int k = std::atoi(v);
+        if (k >= 1 && k <= 64) return k;
+    }
+    return (prec == EDGPU_MIXED && n >= ((int64_t)1 << 22) && op->slab.n_pass >= 4) ? 2 : 1;
 }
 
 // Shared memory of the pair-flip gradient kernel's per-thread coupling accumulators (the product's
@@ -2824,7 +2887,8 @@ static void host_product(edgpu_op_s* op, int prec, int dir, const double* x, dou
                                           (const void*)(intptr_t)(op->pair_allowed + 2 * op->pair_use[prec] +
                                                                   4 * op->pair_nt[prec] + 64 * op->tab_use[prec] +
                                                                   128 * op->tab_uni[prec] + 256 * op->slab_use[prec] +
-                                                                  512 * op->tab_pf[prec] + (1 << 20) * op->slab_hint[prec])};
+                                                                  512 * op->tab_pf[prec] + (1 << 20) * op->slab_hint[prec]),
+                                          (const void*)(intptr_t)slab_row_blocks(op, prec, n)};
     auto it = op->host_graphs.find(key);
     if (it == op->host_graphs.end()) {
         cudaStream_t cap = nullptr;
@@ -2883,7 +2947,7 @@ static void host_product_issue(edgpu_op_s* op, int prec, int dir, const double* 
                 EDGPU_CUDA(cudaEventRecord(op->slab_ready[q], op->aux_st));
             }
             launch_slab_passes(op, prec, op->blob[prec][dir][0], xdst, op->y32.p, 0, yd, accumulate, st,
-                               op->slab_ready.data(), true);
+                               op->slab_ready.data(), true, slab_row_blocks(op, prec, n));
             return;
         }
         if (xd && yd) {
@@ -2920,7 +2984,8 @@ static void host_product_issue(edgpu_op_s* op, int prec, int dir, const double* 
                     EDGPU_CUDA(cudaEventRecord(op->slab_ready[q], op->aux_st));
                 }
                 launch_slab_passes(op, prec, op->blob[prec][dir][0], S.scaled ? (const void*)S.xsc.p : op->x64.p,
-                                   op->y64.p, 0, yd, accumulate, st, op->slab_ready.data(), true);
+                                   op->y64.p, 0, yd, accumulate, st, op->slab_ready.data(), true,
+                                   slab_row_blocks(op, prec, n));
                 return;
             }
             EDGPU_CUDA(cudaMemcpyAsync(op->x64.p, x, n * 16, cudaMemcpyHostToDevice, st));

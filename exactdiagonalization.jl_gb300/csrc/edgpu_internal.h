@@ -389,6 +389,8 @@ struct SlabRun {
     const unsigned char* cls;       // [n_rows] orbit-size index of every row
     const void* scale;              // R[2 nd]: sqrt(|O|) by orbit-size index, then 1 / sqrt(|O|)
     int nd;
+    long long tile0;                // the launch covers the tiles [tile0, tile0 + n_tiles)
+    int blocks_per_sm;              // 0: as many as fit; > 0: at most that many; < 0: leave -blocks_per_sm free
 };
 // Coefficient tables of at most this many entries go to registers (real) or to one copy per shared-
 // memory bank group (SLAB_REP_BYTES in all, which keeps eight blocks of the slab kernel per SM).

@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(HX_THREADS) hx_slab_kernel(const SlabRun r) {
     const bool to_c128 = r.last && r.y_c128 != nullptr;
     const long long n_parts = r.n_tiles * LPR;
     for (long long part = (long long)blockIdx.x * wpb + warp; part < n_parts; part += (long long)gridDim.x * wpb) {
-        const long long tile = part / LPR;
+        const long long tile = r.tile0 + part / LPR;
         // the counts of the tile's 32 rows and their exclusive prefix
         const long long row32 = tile * 32 + lane;
         const int c32 = row32 < r.n_rows ? (int)ld_stream<CH>(r.cnt + row32) : 0;
@@ -387,10 +387,12 @@ void slab_pdl_launch(K kern, const SlabRun& r, int blocks, size_t smem, cudaStre
 }
 
 template <typename K>
-int slab_blocks(K kern, size_t smem, long long n_tiles) {
+int slab_blocks(K kern, size_t smem, long long n_tiles, int per_sm = 0) {
     raise_smem_limit((const void*)kern, smem);
     int n = 0;
     EDGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, HX_THREADS, smem));
+    if (per_sm > 0) n = std::min(n, per_sm);
+    else if (per_sm < 0) n = std::max(1, n + per_sm);
     const long long need = (n_tiles + HX_THREADS / 32 - 1) / (HX_THREADS / 32);
     return (int)std::max<long long>(1, std::min<long long>(need, (long long)std::max(1, n) * sm_count()));
 }
@@ -455,16 +457,16 @@ void slab_launch_m(const SlabRun& r, size_t smem, cudaStream_t st) {
     if constexpr (REAL) {
         if (r.lut_mode == 2) {
             auto k = hx_slab_kernel<PREC, true, NT, CH, LPR, 2>;
-            slab_pdl_launch(k, r, slab_blocks(k, 0, r.n_tiles * LPR), 0, st);
+            slab_pdl_launch(k, r, slab_blocks(k, 0, r.n_tiles * LPR, r.blocks_per_sm), 0, st);
             return;
         }
     }
     if (r.lut_mode == 1) {
         auto k = hx_slab_kernel<PREC, REAL, NT, CH, LPR, 1>;
-        slab_pdl_launch(k, r, slab_blocks(k, smem, r.n_tiles * LPR), smem, st);
+        slab_pdl_launch(k, r, slab_blocks(k, smem, r.n_tiles * LPR, r.blocks_per_sm), smem, st);
     } else {
         auto k = hx_slab_kernel<PREC, REAL, NT, CH, LPR, 0>;
-        slab_pdl_launch(k, r, slab_blocks(k, smem, r.n_tiles * LPR), smem, st);
+        slab_pdl_launch(k, r, slab_blocks(k, smem, r.n_tiles * LPR, r.blocks_per_sm), smem, st);
     }
 }
 

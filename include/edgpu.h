@@ -266,6 +266,12 @@ int edgpu_op_slab_use(edgpu_op op, int32_t precision, int32_t use, int32_t* curr
  * with the unscaled layout to rounding.  Products of one operator through a scaled table are ordered
  * by the calling stream (the scaled x is one buffer per table). */
 int edgpu_op_slab_scaling(edgpu_op op, int32_t mode, int32_t* scaled);
+/* Host-buffer products through the slab table (pinned complex128 buffers the device can address) run
+ * their passes in row blocks: each block's last pass, which writes the block's rows of the result
+ * into the host buffer, runs on a second stream of the handle beside the next block's passes.  Two
+ * blocks for mixed precision on sectors of 2^22 rows or more with at least 4 passes, else one; the
+ * environment variable EDGPU_SLAB_ROW_BLOCKS (1 to 64) sets the count.  The sums are the same, in the
+ * same order, for every count. */
 /* Sparse matrix of the representation, assembled on the device in FP64: rows sorted by column,
  * entries of equal column summed, entries with |value| < tol dropped (tol: the reference's
  * Base.rtoldefault(Float64) = sqrt(eps) gives its default).  This is sparse(opr)

@@ -248,6 +248,36 @@ def test_slab_product_scaled_one_pass(k):
     assert not opr.slab_scaling()
 
 
+@pytest.mark.parametrize("scaling", [1, 2])
+def test_slab_row_blocks_host_buffers(monkeypatch, scaling):
+    """Host-buffer products in row blocks (each block's last pass on a second stream beside the next
+    block's passes): the same sums in the same order as one block, bit for bit, in both precisions and
+    for y += H x."""
+    import torch
+    import edgpu as E
+    opr, red, terms, _ = _chain(E, 20, 0, False)
+    N = opr.dimension
+    assert opr.build_targets(1 << 30)
+    opr.slab_scaling(scaling)
+    assert opr.build_slabs(slab_bytes=1024 * 8, max_bytes=1 << 30)
+    assert opr.slabs_info[0] >= 3
+    x = O.complex_gaussian(N, 8)
+    want = O.apply_rows(red, terms, x)
+    xp = torch.from_numpy(x).pin_memory()
+    out = {}
+    for blocks in ("1", "3", "7"):
+        monkeypatch.setenv("EDGPU_SLAB_ROW_BLOCKS", blocks)
+        for prec in ("mixed", "fp64"):
+            yp = torch.zeros(N, dtype=torch.complex128).pin_memory()
+            E.mul_(yp.numpy(), opr, xp.numpy(), precision=prec)
+            E.apply_(yp.numpy(), opr, xp.numpy(), precision=prec)
+            out[blocks, prec] = yp.numpy().copy()
+    for prec, tol in (("mixed", 1e-5), ("fp64", 1e-12)):
+        assert relerr(out["1", prec], 2 * want) < tol
+        assert np.array_equal(out["3", prec], out["1", prec]), prec
+        assert np.array_equal(out["7", prec], out["1", prec]), prec
+
+
 def test_slab_build_refusals():
     import edgpu as E
     opr, _, _, _ = _chain(E, 12, 0, False)
