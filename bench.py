@@ -676,7 +676,8 @@ def run_gpu(args, wl):
     slab_used = bool(slab_info and slab_info.get("built") and opr.slab_use("mixed"))
     # DRAM bytes per step of the product as profiled: the slab product's passes, or the one-pass kernel
     traffic = profiled_traffic(args.workload + ("_slabs" if slab_used else ""))
-    launches_per_step = slab_info["passes"] if slab_used else 1
+    # one launch per slab pass, and on a scaled slab table one scaling of x per pass
+    launches_per_step = slab_info["passes"] * (2 if slab_info.get("scaled") else 1) if slab_used else 1
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
@@ -819,7 +820,8 @@ def run_gpu_batch(args, wl):
     if mode == 0:
         launches_per_step = 1
     elif mode >= 5:
-        launches_per_step = sum((o.slabs_info[0] if o.slab_use("mixed") else 1) for o in oprs if o.dimension)
+        launches_per_step = sum((o.slabs_info[0] * (2 if o.slab_scaling() else 1) if o.slab_use("mixed") else 1)
+                                for o in oprs if o.dimension)
     else:
         launches_per_step = sum(1 for o in oprs if o.dimension)
     value = b_all / t_max / 1e9
