@@ -12,7 +12,9 @@
 // (amplitude x character x orbit-size ratio, reduced_operator_representation.jl:57-85) replaced by an
 // index into a small table of the distinct coefficients.  Within a pass every row adds its entries
 // in the target table's order and the passes are added in order, so results are reproducible run to
-// run; they differ from the one-pass product by the order of the additions.
+// run; they differ from the one-pass product by the order of the additions.  A scaled table's index
+// leaves the orbit-size ratio sqrt(|O_c| / |O_r|) out: x is scaled by sqrt(|O_c|) before the passes
+// (k_slab_xscale) and each row's result by 1 / sqrt(|O_r|) in the last pass.
 #include "hx_bond.cuh"
 
 #include <type_traits>
