@@ -48,6 +48,12 @@ def test_argument_errors_before_device():
     assert L.edgpu_op_create(None, 0, None, None, None, None, None, 0, None, ctypes.byref(h)) == _lib.ERR_ARG
     assert L.edgpu_mul(None, 0, None, None, 0, 0) == _lib.ERR_ARG
     assert L.edgpu_reduce(None, 1, None, None, None, 1, ctypes.byref(h)) == _lib.ERR_ARG
+    # the slab table's entry points: null handles are refused before any device work
+    cur = ctypes.c_int32()
+    assert L.edgpu_op_slab_scaling(None, 2, ctypes.byref(cur)) == _lib.ERR_ARG
+    assert L.edgpu_op_slab_use(None, 0, 1, ctypes.byref(cur)) == _lib.ERR_ARG
+    assert L.edgpu_op_build_slabs(None, 1 << 20, 0, ctypes.byref(cur)) == _lib.ERR_ARG
+    assert L.edgpu_op_free_slabs(None) == _lib.ERR_ARG
     with pytest.raises(edgpu.ArgumentError):
         _lib.check(_lib.ERR_ARG)
     with pytest.raises(edgpu.DimensionMismatch):
