@@ -60,3 +60,13 @@ def test_reference_arm_prints_contract_line():
         assert key in line
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+
+
+def test_bench_options_parse_without_gpu():
+    """The bench's command line (slab variants and layouts, batch launch modes) parses on the CPU."""
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--help"], capture_output=True, text=True,
+                       cwd=ROOT, timeout=120)
+    assert r.returncode == 0, r.stderr
+    for opt in ("--slab-mode", "--slab-scaling", "--slab-mb", "--batch-launch", "--workload"):
+        assert opt in r.stdout
+    assert "four lanes per row" in r.stdout
